@@ -1,0 +1,335 @@
+"""Benchmark of the DISCUS Fourier path on GB300.
+
+Workload: the 3D volume of the tensor-core form -- fcc binary alloy,
+a = 3.6 A, 50^3 cells x 4 = 500,000 atoms, 50/50 with short-range order
+from 20 seeded NN-Ising exchange sweeps, sigma = 0.02 A, FP32-representable
+coordinates; 101^3 grid h,k,l in [-4,4] step 0.08.  One step = one
+four_run (tables, Friedel reduction, type sums, combine, mirror, statistics).
+
+Metric: G atom.hkl pairs/s = sum_t N_t x (full grid points) / step time.
+`value`: device-resident inputs (dgpu_four_run_device), CUDA-event time on
+the library's stream, L2 flushed (256 MB write) before every step.
+`e2e`: the host C-ABI (dgpu_four_run) with pinned host buffers, copies in
+and out inside the timed region.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from diffusecode_gb300 import _abi  # noqa: E402
+from diffusecode_gb300 import structures as S  # noqa: E402
+
+METRIC = "G atom.hkl pairs/s for |F|^2"
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def workload(name):
+    if name == "fcc-alloy-101^3":
+        return S.fcc_alloy_volume()
+    if name == "perovskite-201^2":
+        return S.perovskite_plane()
+    if name == "hex-layers-1001^2":
+        return S.hex_layers_plane()
+    raise SystemExit(f"unknown workload {name}")
+
+
+def peaks():
+    try:
+        with open(PEAKS) as f:
+            p = json.load(f)
+        return p, "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        except Exception:
+            return out
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].strip().replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) < 9:
+                continue
+            for k, nm in enumerate(names):
+                if "Active" in r[5 + k] and "Not" not in r[5 + k]:
+                    reasons.add(nm)
+        if sm:
+            out["sm_mhz"] = statistics.median(sm)
+            out["sm_max_mhz"] = max(mx) if mx else None
+        out["reasons"] = sorted(reasons)
+        out["samples"] = len(rows)
+        return out
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl"
+        import torch
+        torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, v):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline(cr, grid, seconds=12.0, nthreads=0):
+    """REF22 restatement of four_strucf_omp on a bounded sample of abscissa
+    rows (the reference's OMP loop is uniform per row), all types."""
+    from oracle import oracle as O
+    nthreads = nthreads or (os.cpu_count() or 1)
+    fn1 = (grid.inc[0] + 1) // 2
+    r0 = fn1 // 2
+    sec, pairs = O.time_ref_rows(cr, grid, r0, r0 + 1, nthreads)
+    rows = max(1, min(fn1, int(seconds / max(sec, 1e-6))))
+    rows = min(rows, fn1 - 0)
+    lo = max(0, fn1 // 2 - rows // 2)
+    sec, pairs = O.time_ref_rows(cr, grid, lo, lo + rows, nthreads)
+    return pairs / sec / 1e9, nthreads, rows, sec
+
+
+def run_reference(args, world, rank):
+    cr, grid = workload(args.workload)
+    if rank != 0:
+        return
+    nthreads = os.cpu_count() or 1
+    vals = []
+    rows_used = 0
+    for s in range(args.warmup + args.steps):
+        per_step_seconds = 8.0 if s >= args.warmup else 2.0
+        v, nth, rows, sec = cpu_baseline(cr, grid, seconds=per_step_seconds, nthreads=nthreads)
+        if s >= args.warmup:
+            vals.append(v)
+            rows_used = rows
+    value = statistics.median(vals)
+    pairs_full = cr.n_scattering() * grid.npoints
+    line = {
+        "metric": METRIC, "value": value, "unit": "G pairs/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": pairs_full / (value * 1e9) * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": args.workload, "atoms": cr.n_scattering(), "grid": list(grid.inc),
+                   "pairs_per_step": pairs_full, "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": value, "unit": "G pairs/s", "cores": nthreads, "kind": "port",
+                         "sample": f"REF22 four_strucf_omp restatement, {rows_used} abscissa rows of the "
+                                   f"Friedel half per step, all atom types, scaled per pair"},
+        "e2e": {"value": value, "unit": "G pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args, world, rank, local):
+    import torch
+
+    from diffusecode_gb300 import _lib
+    from diffusecode_gb300 import fourier as FR
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    cr, grid = workload(args.workload)
+    ctx = _lib.Context(local)
+    engine = {"auto": _abi.ENGINE_AUTO, "direct": _abi.ENGINE_DIRECT, "tc": _abi.ENGINE_TC}[args.engine]
+    op = _abi.default_opts(ldbw=1, phase=_abi.PHASE_EXACT64, form=_abi.FORM_TABLE, engine=engine)
+    npnt = grid.npoints
+    pos = torch.from_numpy(cr.pos).to(dev)
+    isc = torch.from_numpy(cr.iscat).to(dev)
+    csf = torch.zeros(2 * npnt, dtype=torch.float64, device=dev)
+    acsf = torch.zeros_like(csf)
+    dsi = torch.zeros(npnt, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    c = cr.to_c(pos_ptr=C.cast(pos.data_ptr(), C.POINTER(C.c_double)),
+                iscat_ptr=C.cast(isc.data_ptr(), C.POINTER(C.c_int32)))
+    g = grid.to_c()
+    info = _abi.Info()
+
+    def step():
+        ctx.check(ctx.lib.dgpu_four_run_device(ctx.h, C.byref(c), C.byref(g), C.byref(op),
+                                               C.c_void_p(csf.data_ptr()), C.c_void_p(acsf.data_ptr()),
+                                               C.c_void_p(dsi.data_ptr()), C.byref(info)))
+        return info.total_ms, info.kernel_ms
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier(world)
+    times, ktimes = [], []
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            tt, kt = step()
+            times.append(tt)
+            ktimes.append(kt)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    barrier(world)
+    engine_used = info.engine_used
+    ms = max_over_ranks(world, sum(times) / len(times))
+    kms = sum(ktimes) / len(ktimes)
+    pairs_full = info.pairs
+    value = world * pairs_full / (ms * 1e-3) / 1e9
+
+    # e2e through the host C-ABI with pinned buffers
+    pin_pos = torch.from_numpy(cr.pos).pin_memory()
+    pin_isc = torch.from_numpy(cr.iscat).pin_memory()
+    pin_csf = torch.zeros(2 * npnt, dtype=torch.float64).pin_memory()
+    pin_dsi = torch.zeros(npnt, dtype=torch.float64).pin_memory()
+    ch = cr.to_c(pos_ptr=C.cast(pin_pos.data_ptr(), C.POINTER(C.c_double)),
+                 iscat_ptr=C.cast(pin_isc.data_ptr(), C.POINTER(C.c_int32)))
+    info2 = _abi.Info()
+
+    def step_e2e():
+        ctx.check(ctx.lib.dgpu_four_run(ctx.h, C.byref(ch), C.byref(g), C.byref(op),
+                                        C.cast(pin_csf.data_ptr(), C.POINTER(C.c_double)), None,
+                                        C.cast(pin_dsi.data_ptr(), C.POINTER(C.c_double)), C.byref(info2)))
+
+    for _ in range(max(1, args.warmup)):
+        step_e2e()
+    torch.cuda.synchronize()
+    barrier(world)
+    et = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        step_e2e()
+        et.append(time.perf_counter() - t0)
+    e2e_s = max_over_ranks(world, sum(et) / len(et))
+    e2e_val = world * pairs_full / e2e_s / 1e9
+    h2d = cr.natoms * (24 + 4)
+    d2h = npnt * (16 + 8)
+
+    if rank != 0:
+        return
+    pk, pk_kind = peaks()
+    fnum_pts = int(np.prod(list(info.fnum)))
+    pairs_computed = cr.n_scattering() * fnum_pts
+    if engine_used == _abi.ENGINE_TC:
+        flops = 24.0 * pairs_computed
+        achieved = flops / (kms * 1e-3) / 1e12
+        peak = pk.get("bf16_tflops", 1900.0)
+        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None,
+                "note": f"24 tensor flops per computed pair (3 split products x 8); peak {pk_kind}"}
+    else:
+        # direct engine: FP32 pipe; 4 flops/pair of accumulation + phasor
+        flops = 4.0 * pairs_computed
+        achieved = flops / (kms * 1e-3) / 1e12
+        roof = {"bound": "tensor", "achieved": achieved, "peak": pk.get("bf16_tflops", 1900.0), "unit": "TFLOP/s",
+                "frac": achieved / pk.get("bf16_tflops", 1900.0), "traffic": None,
+                "note": "direct FP32 engine (no tensor cores); 4 algorithmic flops per computed pair"}
+    line = {
+        "metric": METRIC, "value": value, "unit": "G pairs/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32-phasor/f64-reduce" if engine_used != _abi.ENGINE_TC else "f16x3-split",
+        "data": "synthetic",
+        "config": {"workload": args.workload, "atoms": cr.n_scattering(), "grid": list(grid.inc),
+                   "pairs_per_step": pairs_full, "friedel_points": fnum_pts,
+                   "engine": {1: "direct", 2: "tc"}.get(engine_used, str(engine_used)),
+                   "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas{world}"},
+        "kernel_ms_per_step": kms,
+        "wall_s_timed": wall,
+        "roofline": roof,
+        "clocks": clk.summary(),
+        "gpu_launches": None,
+        "e2e": {"value": e2e_val, "unit": "G pairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+    }
+    if not args.no_cpu_baseline:
+        v, nth, rows, sec = cpu_baseline(cr, grid, seconds=args.cpu_seconds)
+        line["cpu_baseline"] = {"value": v, "unit": "G pairs/s", "cores": nth, "kind": "port",
+                                "sample": f"REF22 four_strucf_omp restatement (oracle), {rows} abscissa rows "
+                                          f"of the Friedel half, {sec:.1f} s, scaled per pair"}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--engine", default="auto", choices=["auto", "direct", "tc"])
+    ap.add_argument("--workload", default="fcc-alloy-101^3")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_init()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,151 @@
+"""ctypes mirror of include/discus_gpu.h (structs, constants).
+
+The C-ABI is the product boundary; this module only describes its plain-C
+structs so that Python callers (the Fourier menu mirror, tests, bench) can
+fill them from numpy arrays.
+"""
+import ctypes as C
+
+import numpy as np
+
+DGPU_OK = 0
+DGPU_WARN_NO_CELL = 1
+DGPU_ERR_ARG = -1
+DGPU_ERR_CUDA = -2
+DGPU_ERR_NOMEM = -3
+DGPU_ERR_STL_RANGE = -4
+DGPU_ERR_ZERO_INC = -5
+DGPU_ERR_UNSUPPORTED = -6
+DGPU_ERR_TIMEOUT = -7
+DGPU_ERR_CANCELLED = -14
+DGPU_ERR_NO_ATOMS = -198
+DGPU_ERR_SCRATCH_SIZE = -20
+
+CFPKT = 9999
+CFINC = 0.001
+I2PI = 65536
+
+PHASE_REF22 = 0
+PHASE_EXACT64 = 1
+FORM_TABLE = 0
+FORM_ANALYTIC = 1
+ENGINE_AUTO = 0
+ENGINE_DIRECT = 1
+ENGINE_TC = 2
+SPLIT_F16 = 0
+SPLIT_BF16 = 1
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+_fp = C.POINTER(C.c_float)
+
+
+class Crystal(C.Structure):
+    _fields_ = [
+        ("natoms", C.c_int64),
+        ("pos", _dp),
+        ("iscat", _ip),
+        ("atom_occ", _fp),
+        ("nscat", C.c_int32),
+        ("ncatoms", C.c_int32),
+        ("icc", C.c_int32 * 3),
+        ("dim0", C.c_double * 3),
+        ("rten", C.c_double * 9),
+        ("scat", _dp),
+        ("occ", _dp),
+        ("dw", _dp),
+        ("delfr", _dp),
+        ("delfi", _dp),
+    ]
+
+
+class Grid(C.Structure):
+    _fields_ = [
+        ("eck", C.c_double * 12),
+        ("vi", C.c_double * 9),
+        ("inc", C.c_int32 * 3),
+    ]
+
+
+class Opts(C.Structure):
+    _fields_ = [
+        ("lxray", C.c_int32),
+        ("power", C.c_int32),
+        ("ano", C.c_int32),
+        ("ldbw", C.c_int32),
+        ("friedel", C.c_int32),
+        ("fave", C.c_double),
+        ("aver_cells", C.POINTER(C.c_uint8)),
+        ("diff_scale", C.c_double),
+        ("phase", C.c_int32),
+        ("form", C.c_int32),
+        ("engine", C.c_int32),
+        ("split", C.c_int32),
+        ("tc_tile_n", C.c_int32),
+        ("tc_kslice", C.c_int32),
+        ("cancel", C.POINTER(C.c_int32)),
+    ]
+
+
+class Info(C.Structure):
+    _fields_ = [
+        ("fnum", C.c_int32 * 3),
+        ("friedel_dim", C.c_int32),
+        ("lmn", C.c_int32 * 6),
+        ("off_shift", C.c_double * 9),
+        ("ncell", C.c_int32),
+        ("engine_used", C.c_int32),
+        ("pairs", C.c_int64),
+        ("pairs_aver", C.c_int64),
+        ("res", C.c_double * 7),
+        ("kernel_ms", C.c_double),
+        ("total_ms", C.c_double),
+    ]
+
+
+def dptr(a):
+    """double* of a contiguous float64 numpy array (None -> NULL)."""
+    if a is None:
+        return C.cast(None, _dp)
+    assert a.dtype == np.float64 and a.flags.c_contiguous or a.flags.f_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+def iptr(a):
+    if a is None:
+        return C.cast(None, _ip)
+    assert a.dtype == np.int32
+    return a.ctypes.data_as(_ip)
+
+
+def fptr(a):
+    if a is None:
+        return C.cast(None, _fp)
+    assert a.dtype == np.float32
+    return a.ctypes.data_as(_fp)
+
+
+def default_opts(**kw):
+    """fourier_reset.f90:42-101 defaults (xray, 4 Gaussians, temp ignore,
+    Friedel on, aver off, scale 1) plus phase/form/engine choices."""
+    o = Opts()
+    o.lxray = 1
+    o.power = 4
+    o.ano = 0
+    o.ldbw = 0
+    o.friedel = 1
+    o.fave = 0.0
+    o.aver_cells = C.cast(None, C.POINTER(C.c_uint8))
+    o.diff_scale = 1.0
+    o.phase = PHASE_EXACT64
+    o.form = FORM_TABLE
+    o.engine = ENGINE_AUTO
+    o.split = SPLIT_F16
+    o.tc_tile_n = 0
+    o.tc_kslice = 0
+    o.cancel = C.cast(None, C.POINTER(C.c_int32))
+    for k, v in kw.items():
+        if k == "aver_cells":
+            continue
+        setattr(o, k, v)
+    return o

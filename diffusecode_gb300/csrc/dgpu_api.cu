@@ -1,0 +1,508 @@
+// C-ABI entry points and the four_run orchestration on the device.
+//
+// dgpu_four_run replaces four_run (discus/prog/fourier_sup.f90:11-323) for
+// LOT_OFF crystals with isotropic ADPs.  The order of work follows it:
+// four_layer/fourier_lmn (:71,:82), four_stltab (:84), four_formtab (:120),
+// four_test_friedel (:132), four_aver (:134), the loop over atom types
+// (:224-244), csf -= acsf and dsi += |csf|^2 (:250-254), four_apply_friedel
+// (:256), scaling (:281-282) and four_qinfo (:294).
+#include <math.h>
+#include <stdarg.h>
+#include <stdlib.h>
+
+#include "dgpu_internal.h"
+
+int dgpu_set_error(dgpu_ctx *ctx, int code, const char *fmt, ...)
+{
+    if (ctx) {
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(ctx->err, sizeof(ctx->err), fmt, ap);
+        va_end(ap);
+    }
+    return code;
+}
+
+extern "C" const char *dgpu_last_error(const dgpu_ctx *ctx) { return ctx ? ctx->err : "no context"; }
+
+extern "C" void dgpu_default_opts(dgpu_opts *o)
+{
+    memset(o, 0, sizeof(*o));
+    o->lxray = 1;
+    o->power = 4;
+    o->ano = 0;
+    o->ldbw = 0;
+    o->friedel = 1;
+    o->fave = 0.0;
+    o->aver_cells = nullptr;
+    o->diff_scale = 1.0;
+    o->phase = DGPU_PHASE_EXACT64;
+    o->form = DGPU_FORM_TABLE;
+    o->engine = DGPU_ENGINE_AUTO;
+    o->split = DGPU_SPLIT_F16;
+    o->cancel = nullptr;
+}
+
+extern "C" int dgpu_ctx_create(int device, dgpu_ctx **out)
+{
+    if (!out) return DGPU_ERR_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return DGPU_ERR_CUDA;
+    if (device < 0 || device >= ndev) return DGPU_ERR_ARG;
+    dgpu_ctx *c = new dgpu_ctx();
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess) { delete c; return DGPU_ERR_CUDA; }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) { delete c; return DGPU_ERR_CUDA; }
+    c->nsm = prop.multiProcessorCount;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { delete c; return DGPU_ERR_CUDA; }
+    for (int i = 0; i < 6; i++)
+        if (cudaEventCreate(&c->ev[i]) != cudaSuccess) { delete c; return DGPU_ERR_CUDA; }
+    *out = c;
+    return DGPU_OK;
+}
+
+extern "C" int dgpu_ctx_destroy(dgpu_ctx *c)
+{
+    if (!c) return DGPU_OK;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    DevBuf *bufs[] = {&c->pos, &c->iscat, &c->aocc, &c->sel, &c->counts, &c->type_start, &c->ph0, &c->du,
+                      &c->dv, &c->dw, &c->w, &c->aph0, &c->adu, &c->adv, &c->adw, &c->aw, &c->istl,
+                      &c->cfact, &c->part, &c->apart, &c->lat, &c->csf, &c->acsf, &c->dsi, &c->stats,
+                      &c->flag, &c->tc_part, &c->tc_work, &c->gq, &c->gpart, &c->grad, &c->batch_desc,
+                      &c->batch_aux};
+    for (DevBuf *b : bufs) b->release();
+    for (int i = 0; i < 6; i++)
+        if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return DGPU_OK;
+}
+
+extern "C" int dgpu_fourier_lmn(const double eck[12], const double vi[9], const int32_t inc[3],
+                                int32_t lmn[6], double off_shift[9])
+{
+    if (!eck || !vi || !inc || !lmn || !off_shift) return DGPU_ERR_ARG;
+    return dgpu_lmn_host(eck, vi, inc, lmn, off_shift);
+}
+
+// ---------------------------------------------------------------------------
+static int check_inputs(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op)
+{
+    if (!ctx || !cr || !g || !op) return DGPU_ERR_ARG;
+    if (cr->natoms < 1) return dgpu_set_error(ctx, DGPU_ERR_NO_ATOMS, "no atoms: no fourier will be calculated");
+    if (!cr->pos || !cr->iscat || !cr->scat || !cr->occ || !cr->dw)
+        return dgpu_set_error(ctx, DGPU_ERR_ARG, "crystal arrays missing");
+    if (cr->nscat < 1 || cr->nscat > 63)
+        return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "nscat=%d outside 1..63", cr->nscat);
+    for (int k = 0; k < 3; k++)
+        if (g->inc[k] < 1) return dgpu_set_error(ctx, DGPU_ERR_ARG, "inc(%d)=%d", k + 1, g->inc[k]);
+    if (op->power < 0 || op->power > 5) return dgpu_set_error(ctx, DGPU_ERR_ARG, "power=%d", op->power);
+    if (op->phase != DGPU_PHASE_REF22 && op->phase != DGPU_PHASE_EXACT64)
+        return dgpu_set_error(ctx, DGPU_ERR_ARG, "phase=%d", op->phase);
+    if (op->form != DGPU_FORM_TABLE && op->form != DGPU_FORM_ANALYTIC)
+        return dgpu_set_error(ctx, DGPU_ERR_ARG, "form=%d", op->form);
+    if (op->fave < 0.0) return dgpu_set_error(ctx, DGPU_ERR_ARG, "fave=%g", op->fave);
+    if (op->fave > 0.0 && op->fave < 1.0 && !op->aver_cells)
+        return dgpu_set_error(ctx, DGPU_ERR_ARG, "0<fave<1 needs the caller's cell selection");
+    if (op->diff_scale < 0.0) return dgpu_set_error(ctx, DGPU_ERR_ARG, "diff_scale<0");
+    return DGPU_OK;
+}
+
+int dgpu_fill_formspec(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *op, const dgpu_grid *g,
+                       FormSpec &fs)
+{
+    memset(&fs, 0, sizeof(fs));
+    fs.mode = op->form;
+    fs.nscat = cr->nscat;
+    fs.lxray = op->lxray;
+    fs.power = op->power;
+    fs.ano = op->ano;
+    fs.ldbw = op->ldbw;
+    for (int t = 0; t <= cr->nscat; t++) {
+        for (int i = 0; i < 11; i++) fs.scat[11 * t + i] = cr->scat[11 * t + i];
+        fs.occ[t] = cr->occ[t];
+        fs.dw[t] = cr->dw[t];
+        fs.delfr[t] = cr->delfr ? cr->delfr[t] : 0.0;
+        fs.delfi[t] = cr->delfi ? cr->delfi[t] : 0.0;
+    }
+    memcpy(fs.rten, cr->rten, sizeof(fs.rten));
+    for (int k = 0; k < 3; k++) fs.eck[k] = g->eck[k];
+    memcpy(fs.vi, g->vi, sizeof(fs.vi));
+    (void)ctx;
+    return DGPU_OK;
+}
+
+// four_test_friedel (fourier_sup.f90:3645-3722)
+static int friedel_test(const dgpu_grid *g, const dgpu_opts *op, int32_t fnum[3])
+{
+    const double eps = (double)1.0e-6f;
+    for (int k = 0; k < 3; k++) fnum[k] = g->inc[k];
+    if (!op->friedel || op->ano) return 0;
+    if (!(fnum[0] % 2 && fnum[1] % 2 && fnum[2] % 2)) return 0;
+    for (int k = 0; k < 3; k++) {
+        double rut = g->eck[k] + g->vi[k] * (fnum[0] - 1) + g->vi[3 + k] * (fnum[1] - 1) + g->vi[6 + k] * (fnum[2] - 1);
+        if (!(fabs(g->eck[k] + rut) < eps)) return 0;
+    }
+    for (int a = 0; a < 3; a++)
+        if (fnum[a] > 1) {
+            fnum[a] = (fnum[a] + 1) / 2;
+            return a + 1;
+        }
+    return 0;
+}
+
+static bool cancelled(const dgpu_opts *op) { return op->cancel && *op->cancel; }
+
+static int pick_engine(dgpu_ctx *ctx, const dgpu_opts *op)
+{
+    if (op->engine == DGPU_ENGINE_DIRECT) return DGPU_ENGINE_DIRECT;
+    bool tc_ok = op->phase == DGPU_PHASE_EXACT64 && dgpu_tc_available(ctx);
+    if (op->engine == DGPU_ENGINE_TC) return tc_ok ? DGPU_ENGINE_TC : -1;
+    return tc_ok ? DGPU_ENGINE_TC : DGPU_ENGINE_DIRECT;
+}
+
+static int engine_sums(dgpu_ctx *ctx, int engine, DevBuf &ph0, DevBuf &du, DevBuf &dv, DevBuf &dw, DevBuf &w,
+                       const int64_t *ts, int32_t ntype, const dgpu_opts *op, const BoxSpec &box, DevBuf &part,
+                       int32_t *nslice)
+{
+    if (engine == DGPU_ENGINE_TC)
+        return dgpu_tc_sums(ctx, ph0.as<uint64_t>(), du.as<uint64_t>(), dv.as<uint64_t>(), dw.as<uint64_t>(),
+                            w.as<float>(), ts, ntype, box, op, part, nslice);
+    return dgpu_direct_sums(ctx, ph0.as<uint64_t>(), du.as<uint64_t>(), dv.as<uint64_t>(), dw.as<uint64_t>(),
+                            w.as<float>(), ts, ntype, op->phase == DGPU_PHASE_REF22, box, part, nslice);
+}
+
+// The whole path with device-resident crystal arrays and outputs.
+static int four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,
+                        double2 *d_csf, double2 *d_acsf, double *d_dsi, dgpu_info *info)
+{
+    int rc = check_inputs(ctx, cr, g, op);
+    if (rc) return rc;
+    DGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+    DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
+    const int32_t *num = g->inc;
+    const int64_t np = (int64_t)num[0] * num[1] * num[2];
+
+    PhaseGeom geo;
+    memset(&geo, 0, sizeof(geo));
+    geo.mode = op->phase;
+    rc = dgpu_lmn_host(g->eck, g->vi, g->inc, geo.lmn, geo.off);
+    if (rc) return dgpu_set_error(ctx, rc, rc == DGPU_ERR_ZERO_INC ? "zero increment vector with inc>1"
+                                                                   : "fourier_lmn failed");
+    for (int k = 0; k < 3; k++) geo.eck[k] = g->eck[k];
+    memcpy(geo.vi, g->vi, sizeof(geo.vi));
+
+    int engine = pick_engine(ctx, op);
+    if (engine < 0)
+        return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "tensor-core engine needs EXACT64 phases on sm_100+");
+
+    // tables
+    DGPU_CUDA(ctx, ctx->istl.ensure(np * sizeof(int32_t)));
+    rc = dgpu_stltab_dev(ctx, g->eck, g->vi, num, cr->rten, ctx->istl.as<int32_t>());
+    if (rc) return rc;
+    DGPU_CUDA(ctx, ctx->cfact.ensure((size_t)cr->nscat * DGPU_NTAB * sizeof(double2)));
+    rc = dgpu_formtab_dev(ctx, cr, op, ctx->cfact.as<double2>());
+    if (rc) return rc;
+
+    int32_t fnum[3];
+    int idim = friedel_test(g, op, fnum);
+    BoxSpec box;
+    for (int k = 0; k < 3; k++) { box.f[k] = fnum[k]; box.num[k] = num[k]; }
+    FormSpec fs;
+    dgpu_fill_formspec(ctx, cr, op, g, fs);
+
+    DGPU_CUDA(ctx, cudaMemsetAsync(d_csf, 0, np * sizeof(double2), ctx->stream));
+    DGPU_CUDA(ctx, cudaMemsetAsync(d_dsi, 0, np * sizeof(double), ctx->stream));
+    DGPU_CUDA(ctx, cudaMemsetAsync(d_acsf, 0, np * sizeof(double2), ctx->stream));
+
+    int warn = 0;
+    int32_t ncell = 0;
+    int64_t pairs_aver = 0;
+    float kernel_ms = 0.f;
+    int64_t ts[66];
+
+    // ---- <F> (four_aver) ----
+    if (op->fave != 0.0) {
+        const int64_t ncells = (int64_t)cr->icc[0] * cr->icc[1] * cr->icc[2];
+        FoldSpec fold = {1, cr->ncatoms, {cr->icc[0], cr->icc[1], cr->icc[2]},
+                         {cr->dim0[0], cr->dim0[1], cr->dim0[2]}, nullptr};
+        if (op->fave < 1.0) {
+            DGPU_CUDA(ctx, ctx->sel.ensure(ncells));
+            DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->sel.p, op->aver_cells, ncells, cudaMemcpyHostToDevice, ctx->stream));
+            fold.sel = ctx->sel.as<uint8_t>();
+            for (int64_t c = 0; c < ncells; c++) ncell += op->aver_cells[c] ? 1 : 0;
+        } else {
+            ncell = (int32_t)ncells;
+        }
+        rc = dgpu_prepare_atoms(ctx, cr->pos, cr->iscat, cr->atom_occ, cr->natoms, cr->nscat, geo, fold,
+                                ctx->aph0, ctx->adu, ctx->adv, ctx->adw, ctx->aw, ts);
+        if (rc) return rc;
+        int32_t anslice = 1;
+        DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
+        rc = engine_sums(ctx, engine, ctx->aph0, ctx->adu, ctx->adv, ctx->adw, ctx->aw, ts, cr->nscat, op, box,
+                         ctx->apart, &anslice);
+        if (rc) return rc;
+        pairs_aver += ts[cr->nscat] * np;
+        // lattice of all cells (four_getav LOT_OFF + four_strucf(0,...) on the full num)
+        int32_t lat_nslice = 1, closed = op->phase == DGPU_PHASE_EXACT64;
+        if (!closed) {
+            rc = dgpu_prepare_lattice(ctx, cr->icc, cr->dim0, geo, ctx->ph0, ctx->du, ctx->dv, ctx->dw, ctx->w);
+            if (rc) return rc;
+            int64_t lts[2] = {0, ncells};
+            BoxSpec full;
+            for (int k = 0; k < 3; k++) { full.f[k] = num[k]; full.num[k] = num[k]; }
+            rc = dgpu_direct_sums(ctx, ctx->ph0.as<uint64_t>(), ctx->du.as<uint64_t>(), ctx->dv.as<uint64_t>(),
+                                  ctx->dw.as<uint64_t>(), ctx->w.as<float>(), lts, 1, 1, full, ctx->lat,
+                                  &lat_nslice);
+            if (rc) return rc;
+            pairs_aver += ncells * np;
+        }
+        DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
+        double norm = 0.0;
+        if (ncell > 0) norm = 1.0 / ncell;
+        else {
+            warn = DGPU_WARN_NO_CELL;
+            dgpu_set_error(ctx, DGPU_WARN_NO_CELL, "no unit cell selected for <F>");
+        }
+        rc = dgpu_aver_combine(ctx, fs, box, ctx->apart.as<double2>(), anslice, ctx->istl.as<int32_t>(),
+                               ctx->cfact.as<double2>(), closed ? nullptr : ctx->lat.as<double2>(), lat_nslice,
+                               closed, cr->icc, cr->dim0, norm, d_acsf);
+        if (rc) return rc;
+        float ms = 0.f;
+        DGPU_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]));
+        kernel_ms += ms;
+        if (cancelled(op)) return dgpu_set_error(ctx, DGPU_ERR_CANCELLED, "cancelled");
+    }
+
+    // ---- type sums (fourier_sup.f90:224-244) ----
+    FoldSpec nofold = {0, cr->ncatoms, {cr->icc[0], cr->icc[1], cr->icc[2]}, {0, 0, 0}, nullptr};
+    rc = dgpu_prepare_atoms(ctx, cr->pos, cr->iscat, cr->atom_occ, cr->natoms, cr->nscat, geo, nofold, ctx->ph0,
+                            ctx->du, ctx->dv, ctx->dw, ctx->w, ts);
+    if (rc) return rc;
+    int32_t nslice = 1;
+    DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
+    rc = engine_sums(ctx, engine, ctx->ph0, ctx->du, ctx->dv, ctx->dw, ctx->w, ts, cr->nscat, op, box, ctx->part,
+                     &nslice);
+    if (rc) return rc;
+    DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
+    rc = dgpu_combine(ctx, fs, box, ctx->part.as<double2>(), nslice, ctx->istl.as<int32_t>(),
+                      ctx->cfact.as<double2>(), op->fave != 0.0 ? d_acsf : nullptr, d_csf, d_dsi, op->diff_scale);
+    if (rc) return rc;
+    {
+        float ms = 0.f;
+        DGPU_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]));
+        kernel_ms += ms;
+    }
+    if (cancelled(op)) return dgpu_set_error(ctx, DGPU_ERR_CANCELLED, "cancelled");
+    rc = dgpu_friedel_mirror(ctx, box, idim, d_csf, d_acsf, d_dsi);
+    if (rc) return rc;
+    double res[7];
+    rc = dgpu_qinfo(ctx, g->eck, g->vi, num, d_dsi, res);
+    if (rc) return rc;
+    DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
+    DGPU_CUDA(ctx, cudaEventSynchronize(ctx->ev[1]));
+    DGPU_CUDA(ctx, cudaGetLastError());
+    if (info) {
+        memset(info, 0, sizeof(*info));
+        for (int k = 0; k < 3; k++) info->fnum[k] = fnum[k];
+        info->friedel_dim = idim;
+        for (int k = 0; k < 6; k++) info->lmn[k] = geo.lmn[k];
+        for (int k = 0; k < 9; k++) info->off_shift[k] = geo.off[k];
+        info->ncell = ncell;
+        info->engine_used = engine;
+        info->pairs = ts[cr->nscat] * np;
+        info->pairs_aver = pairs_aver;
+        for (int k = 0; k < 7; k++) info->res[k] = res[k];
+        info->kernel_ms = kernel_ms;
+        float tot = 0.f;
+        DGPU_CUDA(ctx, cudaEventElapsedTime(&tot, ctx->ev[0], ctx->ev[1]));
+        info->total_ms = tot;
+    }
+    return warn;
+}
+
+extern "C" int dgpu_four_run_device(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid,
+                                    const dgpu_opts *opts, double *d_csf, double *d_acsf, double *d_dsi,
+                                    dgpu_info *info)
+{
+    if (!ctx || !cr || !grid || !opts || !d_csf || !d_dsi) return DGPU_ERR_ARG;
+    int64_t np = (int64_t)grid->inc[0] * grid->inc[1] * grid->inc[2];
+    double2 *acsf = (double2 *)d_acsf;
+    if (!acsf) {
+        DGPU_CUDA(ctx, ctx->acsf.ensure(np * sizeof(double2)));
+        acsf = ctx->acsf.as<double2>();
+    }
+    return four_run_dev(ctx, cr, grid, opts, (double2 *)d_csf, acsf, d_dsi, info);
+}
+
+extern "C" int dgpu_four_run(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid, const dgpu_opts *opts,
+                             double *csf, double *acsf, double *dsi, dgpu_info *info)
+{
+    if (!ctx || !cr || !grid || !opts || !csf || !dsi) return DGPU_ERR_ARG;
+    int rc = check_inputs(ctx, cr, grid, opts);
+    if (rc) return rc;
+    DGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int64_t n = cr->natoms;
+    const int64_t np = (int64_t)grid->inc[0] * grid->inc[1] * grid->inc[2];
+    DGPU_CUDA(ctx, ctx->pos.ensure(n * 3 * sizeof(double)));
+    DGPU_CUDA(ctx, ctx->iscat.ensure(n * sizeof(int32_t)));
+    DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->pos.p, cr->pos, n * 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->iscat.p, cr->iscat, n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+    dgpu_crystal dc = *cr;
+    dc.pos = ctx->pos.as<double>();
+    dc.iscat = ctx->iscat.as<int32_t>();
+    if (cr->atom_occ) {
+        DGPU_CUDA(ctx, ctx->aocc.ensure(n * sizeof(float)));
+        DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->aocc.p, cr->atom_occ, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+        dc.atom_occ = ctx->aocc.as<float>();
+    }
+    DGPU_CUDA(ctx, ctx->csf.ensure(np * sizeof(double2)));
+    DGPU_CUDA(ctx, ctx->acsf.ensure(np * sizeof(double2)));
+    DGPU_CUDA(ctx, ctx->dsi.ensure(np * sizeof(double)));
+    rc = four_run_dev(ctx, &dc, grid, opts, ctx->csf.as<double2>(), ctx->acsf.as<double2>(), ctx->dsi.as<double>(),
+                      info);
+    if (rc < 0) return rc;
+    DGPU_CUDA(ctx, cudaMemcpyAsync(csf, ctx->csf.p, np * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
+    DGPU_CUDA(ctx, cudaMemcpyAsync(dsi, ctx->dsi.p, np * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    if (acsf)
+        DGPU_CUDA(ctx, cudaMemcpyAsync(acsf, ctx->acsf.p, np * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
+    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return rc;
+}
+
+// ---------------------------------------------------------------------------
+// per-type drop-in: four_strucf + tcsf_form_iso
+__global__ void k_xat_phase_prepare(const double *xat, int64_t n, double *pos3, int32_t *types)
+{
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    pos3[3 * k] = xat[k];
+    pos3[3 * k + 1] = xat[n + k];
+    pos3[3 * k + 2] = xat[2 * n + k];
+    types[k] = 1;
+}
+
+extern "C" int dgpu_four_strucf(dgpu_ctx *ctx, const double *xat, int64_t nxat, const double uin[3],
+                                const double vin[3], const double win[3], const double off_shift[9],
+                                const int32_t lmn[6], const int32_t num[3], const int32_t fnum[3],
+                                const double *cfact, const int32_t *istl, double *tcsf)
+{
+    if (!ctx || !uin || !vin || !win || !off_shift || !lmn || !num || !fnum || !tcsf) return DGPU_ERR_ARG;
+    if (nxat < 0 || (nxat > 0 && !xat)) return DGPU_ERR_ARG;
+    if (cfact && !istl) return dgpu_set_error(ctx, DGPU_ERR_ARG, "cfact without istl");
+    for (int k = 0; k < 3; k++)
+        if (num[k] < 1 || fnum[k] < 1 || fnum[k] > num[k]) return dgpu_set_error(ctx, DGPU_ERR_ARG, "num/fnum");
+    DGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int64_t np = (int64_t)num[0] * num[1] * num[2];
+    DGPU_CUDA(ctx, ctx->csf.ensure(np * sizeof(double2)));
+    DGPU_CUDA(ctx, ctx->dsi.ensure(np * sizeof(double)));
+    DGPU_CUDA(ctx, cudaMemsetAsync(ctx->csf.p, 0, np * sizeof(double2), ctx->stream));
+    if (nxat > 0) {
+        DGPU_CUDA(ctx, ctx->tc_work.ensure(nxat * 3 * sizeof(double)));
+        DGPU_CUDA(ctx, ctx->pos.ensure(nxat * 3 * sizeof(double)));
+        DGPU_CUDA(ctx, ctx->iscat.ensure(nxat * sizeof(int32_t)));
+        DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->tc_work.p, xat, nxat * 3 * sizeof(double), cudaMemcpyHostToDevice,
+                                       ctx->stream));
+        k_xat_phase_prepare<<<(unsigned)dgpu_cdiv(nxat, 256), 256, 0, ctx->stream>>>(
+            ctx->tc_work.as<double>(), nxat, ctx->pos.as<double>(), ctx->iscat.as<int32_t>());
+        DGPU_CUDA(ctx, cudaGetLastError());
+        PhaseGeom geo;
+        memset(&geo, 0, sizeof(geo));
+        geo.mode = DGPU_PHASE_REF22;
+        memcpy(geo.lmn, lmn, sizeof(geo.lmn));
+        for (int k = 0; k < 3; k++) { geo.vi[k] = uin[k]; geo.vi[3 + k] = vin[k]; geo.vi[6 + k] = win[k]; }
+        memcpy(geo.off, off_shift, sizeof(geo.off));
+        FoldSpec nofold = {0, 1, {1, 1, 1}, {0, 0, 0}, nullptr};
+        int64_t ts[3];
+        int rc = dgpu_prepare_atoms(ctx, ctx->pos.as<double>(), ctx->iscat.as<int32_t>(), nullptr, nxat, 1, geo,
+                                    nofold, ctx->ph0, ctx->du, ctx->dv, ctx->dw, ctx->w, ts);
+        if (rc) return rc;
+        BoxSpec box;
+        for (int k = 0; k < 3; k++) { box.f[k] = fnum[k]; box.num[k] = num[k]; }
+        int32_t nslice = 1;
+        rc = dgpu_direct_sums(ctx, ctx->ph0.as<uint64_t>(), ctx->du.as<uint64_t>(), ctx->dv.as<uint64_t>(),
+                              ctx->dw.as<uint64_t>(), ctx->w.as<float>(), ts, 1, 1, box, ctx->part, &nslice);
+        if (rc) return rc;
+        // form factor: table lookup through istl, or unity
+        DGPU_CUDA(ctx, ctx->cfact.ensure(DGPU_NTAB * sizeof(double2)));
+        DGPU_CUDA(ctx, ctx->istl.ensure(np * sizeof(int32_t)));
+        if (cfact) {
+            DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->cfact.p, cfact, DGPU_NTAB * sizeof(double2), cudaMemcpyHostToDevice,
+                                           ctx->stream));
+            DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->istl.p, istl, np * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                           ctx->stream));
+        } else {
+            double2 one[1] = {make_double2(1.0, 0.0)};
+            DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->cfact.p, one, sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
+            DGPU_CUDA(ctx, cudaMemsetAsync(ctx->istl.p, 0, np * sizeof(int32_t), ctx->stream));
+        }
+        FormSpec fs;
+        memset(&fs, 0, sizeof(fs));
+        fs.mode = DGPU_FORM_TABLE;
+        fs.nscat = 1;
+        rc = dgpu_combine(ctx, fs, box, ctx->part.as<double2>(), nslice, ctx->istl.as<int32_t>(),
+                          ctx->cfact.as<double2>(), nullptr, ctx->csf.as<double2>(), ctx->dsi.as<double>(), 1.0);
+        if (rc) return rc;
+    }
+    DGPU_CUDA(ctx, cudaMemcpyAsync(tcsf, ctx->csf.p, np * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
+    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return DGPU_OK;
+}
+
+extern "C" int dgpu_four_stltab(dgpu_ctx *ctx, const dgpu_grid *grid, const double rten[9], int32_t *istl)
+{
+    if (!ctx || !grid || !rten || !istl) return DGPU_ERR_ARG;
+    DGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int64_t np = (int64_t)grid->inc[0] * grid->inc[1] * grid->inc[2];
+    DGPU_CUDA(ctx, ctx->istl.ensure(np * sizeof(int32_t)));
+    int rc = dgpu_stltab_dev(ctx, grid->eck, grid->vi, grid->inc, rten, ctx->istl.as<int32_t>());
+    DGPU_CUDA(ctx, cudaMemcpyAsync(istl, ctx->istl.p, np * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return rc;
+}
+
+extern "C" int dgpu_four_formtab(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *opts, double *cfact)
+{
+    if (!ctx || !cr || !opts || !cfact || !cr->scat || !cr->occ || !cr->dw) return DGPU_ERR_ARG;
+    DGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+    DGPU_CUDA(ctx, ctx->cfact.ensure((size_t)cr->nscat * DGPU_NTAB * sizeof(double2)));
+    int rc = dgpu_formtab_dev(ctx, cr, opts, ctx->cfact.as<double2>());
+    if (rc) return rc;
+    DGPU_CUDA(ctx, cudaMemcpyAsync(cfact, ctx->cfact.p, (size_t)cr->nscat * DGPU_NTAB * sizeof(double2),
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return DGPU_OK;
+}
+
+extern "C" int dgpu_four_increments(dgpu_ctx *ctx, const double *xat, int64_t nxat, const double uin[3],
+                                    const double vin[3], const double win[3], const double off_shift[9],
+                                    int64_t *inc_out)
+{
+    if (!ctx || !uin || !vin || !win || !off_shift || !inc_out || nxat < 0 || (nxat > 0 && !xat))
+        return DGPU_ERR_ARG;
+    if (nxat == 0) return DGPU_OK;
+    DGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+    DGPU_CUDA(ctx, ctx->tc_work.ensure(nxat * 3 * sizeof(double) + 256 + nxat * 6 * sizeof(int64_t)));
+    double *d_x = ctx->tc_work.as<double>();
+    int64_t *d_o = (int64_t *)((char *)ctx->tc_work.p + ((nxat * 3 * sizeof(double) + 255) & ~(size_t)255));
+    DGPU_CUDA(ctx, cudaMemcpyAsync(d_x, xat, nxat * 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    int rc = dgpu_increments_dev(ctx, d_x, nxat, uin, vin, win, off_shift, d_o);
+    if (rc) return rc;
+    DGPU_CUDA(ctx, cudaMemcpyAsync(inc_out, d_o, nxat * 6 * sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return DGPU_OK;
+}
+
+extern "C" int dgpu_chi2_grad(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid, const dgpu_opts *opts,
+                              const double *i_target, const double *weight, double *chi2, double *grad_pos,
+                              double *grad_occ, dgpu_info *info)
+{
+    int rc = check_inputs(ctx, cr, grid, opts);
+    if (rc) return rc;
+    if (!i_target || !chi2) return dgpu_set_error(ctx, DGPU_ERR_ARG, "i_target/chi2 missing");
+    DGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+    return dgpu_chi2_grad_impl(ctx, cr, grid, opts, i_target, weight, chi2, grad_pos, grad_occ, info);
+}

@@ -1,0 +1,171 @@
+// Internal declarations of the GB300 Fourier structure-factor library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "../../include/discus_gpu.h"
+
+#define DGPU_NTAB (DGPU_CFPKT + 1)
+
+// ---------------------------------------------------------------------------
+// device buffer that only grows
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = bytes < 256 ? 256 : bytes;
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    template <class T> T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+// Per-atom phase data, grouped by type (SoA).  Phases are 64-bit fixed point
+// in units of 2^-64 turn: phase(n) = ph0 + n0*d0 + n1*d1 + n2*d2 (mod 2^64).
+struct AtomSet {
+    uint64_t *ph0, *du, *dv, *dw;
+    float *w;
+    int64_t *type_start;   // [nscat+2] (host copy kept in HostAtomSet)
+    int64_t n;             // total atoms stored
+};
+
+struct Tables {
+    int32_t *istl;         // [np] full grid
+    double2 *cfact;        // [nscat][NTAB]
+};
+
+struct dgpu_ctx {
+    int device = 0;
+    int nsm = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[6] = {};
+    char err[512] = {0};
+    // cached buffers
+    DevBuf pos, iscat, aocc, sel;
+    DevBuf counts, type_start;
+    DevBuf ph0, du, dv, dw, w;          // main atom set
+    DevBuf aph0, adu, adv, adw, aw;     // folded atoms for <F>
+    DevBuf istl, cfact, part, apart, lat, csf, acsf, dsi, stats, flag;
+    DevBuf tc_part, tc_work;
+    DevBuf gq, gpart, grad, batch_desc, batch_aux;
+    double batch_ms = 0.0;
+};
+
+// error helpers ---------------------------------------------------------
+int dgpu_set_error(dgpu_ctx *ctx, int code, const char *fmt, ...);
+#define DGPU_CUDA(ctx, call)                                                          \
+    do {                                                                              \
+        cudaError_t _e = (call);                                                      \
+        if (_e != cudaSuccess)                                                        \
+            return dgpu_set_error((ctx), _e == cudaErrorMemoryAllocation ? DGPU_ERR_NOMEM \
+                                                                         : DGPU_ERR_CUDA, \
+                                  "%s: %s (%s:%d)", #call, cudaGetErrorString(_e),   \
+                                  __FILE__, __LINE__);                                \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// Phase geometry passed to kernels
+struct PhaseGeom {
+    int32_t mode;          // DGPU_PHASE_*
+    int32_t lmn[6];
+    double eck[3];         // eck(:,1)
+    double vi[9];          // vi(:,1..3) column-major
+    double off[9];         // off_shift column-major
+};
+
+// host side: fourier_lmn
+int dgpu_lmn_host(const double eck[12], const double vi[9], const int32_t inc[3],
+                  int32_t lmn[6], double off[9]);
+
+// prepare.cu ------------------------------------------------------------
+// Stable gather of atoms by type into phase data.  If fold != 0, atoms are
+// folded into their unit cell (four_aver) and only selected cells are kept.
+struct FoldSpec {
+    int32_t fold;
+    int32_t ncatoms;
+    int32_t icc[3];
+    double dim0[3];
+    const uint8_t *sel;    // device, may be null (all cells)
+};
+int dgpu_prepare_atoms(dgpu_ctx *ctx, const double *d_pos, const int32_t *d_iscat,
+                       const float *d_aocc, int64_t natoms, int32_t nscat,
+                       const PhaseGeom &g, const FoldSpec &fs, DevBuf &ph0, DevBuf &du,
+                       DevBuf &dv, DevBuf &dw, DevBuf &w, int64_t *h_type_start);
+// Lattice points of all cells (four_getav LOT_OFF) as one atom set.
+int dgpu_prepare_lattice(dgpu_ctx *ctx, const int32_t icc[3], const double dim0[3],
+                         const PhaseGeom &g, DevBuf &ph0, DevBuf &du, DevBuf &dv,
+                         DevBuf &dw, DevBuf &w);
+
+// tables.cu -------------------------------------------------------------
+int dgpu_stltab_dev(dgpu_ctx *ctx, const double eck[3], const double vi[9],
+                    const int32_t num[3], const double rten[9], int32_t *d_istl);
+int dgpu_formtab_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *op,
+                     double2 *d_cfact);
+int dgpu_increments_dev(dgpu_ctx *ctx, const double *d_xat, int64_t nxat,
+                        const double uin[3], const double vin[3], const double win[3],
+                        const double off[9], int64_t *d_out);
+
+// direct.cu -------------------------------------------------------------
+// Sum over the atoms of each type: part[t][s][p] (complex double) on the
+// box fnum; ntype types with atom ranges from type_start.
+struct BoxSpec {
+    int32_t f[3];          // computed box
+    int32_t num[3];        // full grid
+};
+int dgpu_direct_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du,
+                     const uint64_t *dv, const uint64_t *dw, const float *w,
+                     const int64_t *h_type_start, int32_t ntype, int32_t ref_mask,
+                     const BoxSpec &box, DevBuf &part, int32_t *nslice_out);
+
+// tc.cu -----------------------------------------------------------------
+int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const uint64_t *dv,
+                 const uint64_t *dw, const float *w, const int64_t *h_type_start,
+                 int32_t ntype, const BoxSpec &box, const dgpu_opts *op, DevBuf &part,
+                 int32_t *nslice_out);
+bool dgpu_tc_available(dgpu_ctx *ctx);
+
+// epilogue.cu -----------------------------------------------------------
+struct FormSpec {
+    int32_t mode;          // DGPU_FORM_*
+    int32_t nscat;
+    int32_t lxray, power, ano, ldbw;
+    double scat[64 * 11];  // per type coefficients (types 1..nscat, <=63)
+    double occ[64], dw[64], delfr[64], delfi[64];
+    double rten[9];
+    double eck[3], vi[9];
+};
+int dgpu_combine(dgpu_ctx *ctx, const FormSpec &fs, const BoxSpec &box, const double2 *part,
+                 int32_t nslice, const int32_t *istl, const double2 *cfact,
+                 const double2 *acsf_box_in, double2 *csf, double *dsi, double diff_scale);
+int dgpu_aver_combine(dgpu_ctx *ctx, const FormSpec &fs, const BoxSpec &box,
+                      const double2 *apart, int32_t anslice, const int32_t *istl,
+                      const double2 *cfact, const double2 *lat, int32_t lat_nslice,
+                      int32_t lat_closed, const int32_t icc[3], const double dim0[3],
+                      double norm, double2 *acsf);
+int dgpu_friedel_mirror(dgpu_ctx *ctx, const BoxSpec &box, int32_t idim, double2 *csf,
+                        double2 *acsf, double *dsi);
+int dgpu_qinfo(dgpu_ctx *ctx, const double eck[3], const double vi[9], const int32_t num[3],
+               const double *dsi, double res[7]);
+
+// adjoint.cu / batch.cu ---------------------------------------------------
+int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid,
+                        const dgpu_opts *op, const double *i_target, const double *weight,
+                        double *chi2, double *grad_pos, double *grad_occ, dgpu_info *info);
+int dgpu_fill_formspec(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *op,
+                       const dgpu_grid *g, FormSpec &fs);
+
+// small helpers -------------------------------------------------------------
+static inline int64_t dgpu_cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }

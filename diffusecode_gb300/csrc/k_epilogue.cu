@@ -1,0 +1,328 @@
+// Epilogue kernels of four_run (discus/prog/fourier_sup.f90:224-294):
+//   * combine: csf = sum_t cfact_t(point) * S_t - acsf ; dsi = |csf|^2
+//     (tcsf_form_iso, fourier_form.f90:147-177; fourier_sup.f90:232,250-254),
+//     with diff_scale applied (fourier_sup.f90:281-282);
+//   * <F>: acsf = (sum_t cfact_t * Savg_t) * lattice / ncell
+//     (four_aver, fourier_sup.f90:1194-1357); the lattice sum is either the
+//     direct sum over all cells or its closed form (a product of three
+//     geometric series);
+//   * Friedel mirror (four_apply_friedel, fourier_sup.f90:3726-3757), with the
+//     net effect of its sequential in-place loop on the middle slab;
+//   * four_qinfo statistics (fourier_sup.f90:2859-2942).
+#include "dgpu_internal.h"
+
+__device__ __forceinline__ void hvec(const FormSpec *fs, int64_t i, int64_t j, int64_t l, double h[3])
+{
+    for (int k = 0; k < 3; k++)
+        h[k] = __dadd_rn(__dadd_rn(__dadd_rn(fs->eck[k], __dmul_rn(fs->vi[k], (double)i)),
+                                   __dmul_rn(fs->vi[3 + k], (double)j)),
+                         __dmul_rn(fs->vi[6 + k], (double)l));
+}
+
+// cfact of type t (1-based) at a point: table or exact sin(theta)/lambda
+__device__ __forceinline__ double2 cfact_at(const FormSpec *fs, const double2 *cfact, int32_t istl,
+                                            int t, const double h[3])
+{
+    if (fs->mode == DGPU_FORM_TABLE) return cfact[(int64_t)(t - 1) * DGPU_NTAB + istl];
+    const double *r = fs->rten;
+    double t0 = __dadd_rn(__dadd_rn(__dmul_rn(r[0], h[0]), __dmul_rn(r[3], h[1])), __dmul_rn(r[6], h[2]));
+    double t1 = __dadd_rn(__dadd_rn(__dmul_rn(r[1], h[0]), __dmul_rn(r[4], h[1])), __dmul_rn(r[7], h[2]));
+    double t2 = __dadd_rn(__dadd_rn(__dmul_rn(r[2], h[0]), __dmul_rn(r[5], h[1])), __dmul_rn(r[8], h[2]));
+    double q2 = __dadd_rn(__dadd_rn(__dmul_rn(h[0], t0), __dmul_rn(h[1], t1)), __dmul_rn(h[2], t2)) / 4.0;
+    const double *sc = fs->scat + 11 * t;
+    double f = sc[0];
+    if (fs->lxray)
+        for (int i = 1; i <= fs->power; i++) f = __dadd_rn(f, __dmul_rn(sc[2 * i - 1], exp(-__dmul_rn(sc[2 * i], q2))));
+    double fp = fs->ano ? fs->delfr[t] : 0.0, fpp = fs->ano ? fs->delfi[t] : 0.0;
+    double sb = fs->ldbw ? __dmul_rn(exp(-__dmul_rn(fs->dw[t], q2)), fs->occ[t]) : fs->occ[t];
+    return make_double2(__dmul_rn(sb, __dadd_rn(f, fp)), __dmul_rn(sb, fpp));
+}
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b)
+{
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+__global__ void k_combine(const FormSpec *fs, BoxSpec box, const double2 *__restrict__ part,
+                          int32_t nslice, const int32_t *__restrict__ istl,
+                          const double2 *__restrict__ cfact, const double2 *__restrict__ acsf,
+                          double2 *__restrict__ csf, double *__restrict__ dsi, double ds, double sqds)
+{
+    int64_t pb = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    if (pb >= nb) return;
+    int64_t i = pb % box.f[0], j = (pb / box.f[0]) % box.f[1], l = pb / ((int64_t)box.f[0] * box.f[1]);
+    int64_t idx = i + (int64_t)box.num[0] * (j + (int64_t)box.num[1] * l);
+    double h[3];
+    if (fs->mode != DGPU_FORM_TABLE) hvec(fs, i, j, l, h);
+    int32_t q = istl ? istl[idx] : 0;
+    double2 F = make_double2(0.0, 0.0);
+    for (int t = 1; t <= fs->nscat; t++) {
+        double2 s = make_double2(0.0, 0.0);
+        const double2 *pt = part + (int64_t)(t - 1) * nslice * nb + pb;
+        for (int k = 0; k < nslice; k++) {
+            double2 v = pt[(int64_t)k * nb];
+            s.x += v.x;
+            s.y += v.y;
+        }
+        double2 c = cfact_at(fs, cfact, q, t, h);
+        double2 m = cmul(s, c);
+        F.x += m.x;
+        F.y += m.y;
+    }
+    if (acsf) {
+        double2 a = acsf[idx];
+        F.x -= a.x;
+        F.y -= a.y;
+    }
+    csf[idx] = make_double2(F.x * sqds, F.y * sqds);
+    dsi[idx] = (F.x * F.x + F.y * F.y) * ds;
+}
+
+// one-axis geometric series sum_{m<n} exp(2 pi i x m)
+__device__ __forceinline__ double2 geom_series(double x, int32_t n)
+{
+    double xr = x - rint(x);
+    if (xr == 0.0) return make_double2((double)n, 0.0);
+    double num = sinpi((double)n * xr), den = sinpi(xr);
+    double r = num / den, sp, cp;
+    sincospi(xr * (double)(n - 1), &sp, &cp);
+    return make_double2(r * cp, r * sp);
+}
+
+__global__ void k_aver_combine(const FormSpec *fs, BoxSpec box, const double2 *__restrict__ apart,
+                               int32_t anslice, const int32_t *__restrict__ istl,
+                               const double2 *__restrict__ cfact, const double2 *__restrict__ lat,
+                               int32_t lat_nslice, int32_t lat_closed, int32_t c0, int32_t c1,
+                               int32_t c2, double d0, double d1, double d2, double norm,
+                               double2 *__restrict__ acsf)
+{
+    int64_t pb = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    if (pb >= nb) return;
+    int64_t i = pb % box.f[0], j = (pb / box.f[0]) % box.f[1], l = pb / ((int64_t)box.f[0] * box.f[1]);
+    int64_t idx = i + (int64_t)box.num[0] * (j + (int64_t)box.num[1] * l);
+    int64_t nfull = (int64_t)box.num[0] * box.num[1] * box.num[2];
+    double h[3];
+    hvec(fs, i, j, l, h);
+    int32_t q = istl ? istl[idx] : 0;
+    double2 A = make_double2(0.0, 0.0);
+    for (int t = 1; t <= fs->nscat; t++) {
+        double2 s = make_double2(0.0, 0.0);
+        const double2 *pt = apart + (int64_t)(t - 1) * anslice * nb + pb;
+        for (int k = 0; k < anslice; k++) {
+            double2 v = pt[(int64_t)k * nb];
+            s.x += v.x;
+            s.y += v.y;
+        }
+        double2 m = cmul(s, cfact_at(fs, cfact, q, t, h));
+        A.x += m.x;
+        A.y += m.y;
+    }
+    double2 L;
+    if (lat_closed) {
+        double2 g0 = geom_series(h[0], c0), g1 = geom_series(h[1], c1), g2 = geom_series(h[2], c2);
+        L = cmul(cmul(g0, g1), g2);
+        // exp(2 pi i h.dim0) with the phase reduced exactly
+        double p0 = h[0] * d0, e0 = fma(h[0], d0, -p0);
+        double p1 = h[1] * d1, e1 = fma(h[1], d1, -p1);
+        double p2 = h[2] * d2, e2 = fma(h[2], d2, -p2);
+        double ph = (p0 - rint(p0)) + (p1 - rint(p1)) + (p2 - rint(p2)) + (e0 + e1 + e2);
+        double sp, cp;
+        sincospi(2.0 * ph, &sp, &cp);
+        L = cmul(L, make_double2(cp, sp));
+    } else {
+        L = make_double2(0.0, 0.0);
+        for (int k = 0; k < lat_nslice; k++) {
+            double2 v = lat[(int64_t)k * nfull + idx];
+            L.x += v.x;
+            L.y += v.y;
+        }
+    }
+    double2 r = cmul(A, L);
+    acsf[idx] = make_double2(r.x * norm, r.y * norm);
+}
+
+// four_apply_friedel: points past the halved axis' middle take the conjugate
+// of their mirror; on the middle slab the sequential loop leaves the first
+// half, conjugates the centre and mirrors the second half.
+__global__ void k_mirror(BoxSpec box, int32_t a, double2 *csf, double2 *acsf, double *dsi)
+{
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int32_t *n = box.num;
+    int64_t np = (int64_t)n[0] * n[1] * n[2];
+    if (p >= np) return;
+    int32_t c[3] = {(int32_t)(p % n[0]), (int32_t)((p / n[0]) % n[1]), (int32_t)(p / ((int64_t)n[0] * n[1]))};
+    int32_t mid = box.f[a] - 1;
+    if (c[a] < mid) return;
+    int64_t m = (n[0] - 1 - c[0]) + (int64_t)n[0] * ((n[1] - 1 - c[1]) + (int64_t)n[1] * (n[2] - 1 - c[2]));
+    if (c[a] == mid) {
+        // linear index over the later axes, last axis fastest
+        int64_t L = 0, N = 1;
+        for (int k = a + 1; k < 3; k++) {
+            L = L * n[k] + c[k];
+            N *= n[k];
+        }
+        if (2 * L < N - 1) return;
+        if (2 * L == N - 1) {
+            csf[p].y = -csf[p].y;
+            if (acsf) acsf[p].y = -acsf[p].y;
+            return;
+        }
+    }
+    double2 v = csf[m];
+    csf[p] = make_double2(v.x, -v.y);
+    if (acsf) {
+        double2 u = acsf[m];
+        acsf[p] = make_double2(u.x, -u.y);
+    }
+    dsi[p] = dsi[m];
+}
+
+struct QStat {
+    double bmax, bmin, dmax, dmin, dsum, dsum2;
+    long long nd;
+};
+
+__device__ __forceinline__ void qmerge(QStat &a, const QStat &b)
+{
+    a.bmax = fmax(a.bmax, b.bmax);
+    a.bmin = fmin(a.bmin, b.bmin);
+    a.dmax = fmax(a.dmax, b.dmax);
+    a.dmin = fmin(a.dmin, b.dmin);
+    a.dsum += b.dsum;
+    a.dsum2 += b.dsum2;
+    a.nd += b.nd;
+}
+
+#define QNT 256
+__global__ void k_qinfo_part(double e0, double e1, double e2, FormSpec const *fs, int32_t n0,
+                             int32_t n1, int32_t n2, const double *dsi, QStat *out)
+{
+    QStat s = {-9999.0, (double)1e19f, -9999.0, (double)1e19f, 0.0, 0.0, 0};
+    int64_t np = (int64_t)n0 * n1 * n2;
+    double e[3] = {e0, e1, e2};
+    for (int64_t p = (int64_t)blockIdx.x * QNT + threadIdx.x; p < np; p += (int64_t)gridDim.x * QNT) {
+        int64_t i = p % n0, j = (p / n0) % n1, l = p / ((int64_t)n0 * n1);
+        bool bragg = true;
+        for (int k = 0; k < 3; k++) {
+            double h = __dadd_rn(__dadd_rn(__dadd_rn(e[k], __dmul_rn(fs->vi[k], (double)(float)i)),
+                                           __dmul_rn(fs->vi[3 + k], (double)(float)j)),
+                                 __dmul_rn(fs->vi[6 + k], (double)(float)l));
+            bragg = bragg && (h == trunc(h));
+        }
+        double v = dsi[p];
+        if (bragg) {
+            s.bmax = fmax(s.bmax, v);
+            s.bmin = fmin(s.bmin, v);
+        } else {
+            s.dmax = fmax(s.dmax, v);
+            s.dmin = fmin(s.dmin, v);
+            s.dsum += v;
+            s.dsum2 += v * v;
+            s.nd++;
+        }
+    }
+    __shared__ QStat sh[QNT];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = QNT / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) qmerge(sh[threadIdx.x], sh[threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = sh[0];
+}
+
+__global__ void k_qinfo_final(const QStat *part, int n, double *res)
+{
+    if (threadIdx.x != 0) return;
+    QStat s = part[0];
+    for (int k = 1; k < n; k++) qmerge(s, part[k]);
+    double ave = 0.0, sig = 0.0;
+    if (s.nd) {
+        ave = s.dsum / (double)s.nd;
+        sig = sqrt(s.dsum2 / (double)s.nd - ave * ave);
+    }
+    res[0] = 6.0;
+    res[1] = s.dmin;
+    res[2] = s.dmax;
+    res[3] = ave;
+    res[4] = sig;
+    res[5] = s.bmin;
+    res[6] = s.bmax;
+}
+
+// ---------------------------------------------------------------------------
+static int upload_formspec(dgpu_ctx *ctx, const FormSpec &fs, FormSpec **d)
+{
+    DGPU_CUDA(ctx, ctx->stats.ensure(sizeof(FormSpec) + 4096 * sizeof(QStat) + 64));
+    *d = ctx->stats.as<FormSpec>();
+    DGPU_CUDA(ctx, cudaMemcpyAsync(*d, &fs, sizeof(FormSpec), cudaMemcpyHostToDevice, ctx->stream));
+    return DGPU_OK;
+}
+
+int dgpu_combine(dgpu_ctx *ctx, const FormSpec &fs, const BoxSpec &box, const double2 *part,
+                 int32_t nslice, const int32_t *istl, const double2 *cfact,
+                 const double2 *acsf_in, double2 *csf, double *dsi, double diff_scale)
+{
+    FormSpec *d;
+    int rc = upload_formspec(ctx, fs, &d);
+    if (rc) return rc;
+    int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    k_combine<<<(unsigned)dgpu_cdiv(nb, 256), 256, 0, ctx->stream>>>(d, box, part, nslice, istl, cfact, acsf_in,
+                                                                      csf, dsi, diff_scale, sqrt(diff_scale));
+    DGPU_CUDA(ctx, cudaGetLastError());
+    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));   // FormSpec block reused next
+    return DGPU_OK;
+}
+
+int dgpu_aver_combine(dgpu_ctx *ctx, const FormSpec &fs, const BoxSpec &box, const double2 *apart,
+                      int32_t anslice, const int32_t *istl, const double2 *cfact, const double2 *lat,
+                      int32_t lat_nslice, int32_t lat_closed, const int32_t icc[3],
+                      const double dim0[3], double norm, double2 *acsf)
+{
+    FormSpec *d;
+    int rc = upload_formspec(ctx, fs, &d);
+    if (rc) return rc;
+    int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    k_aver_combine<<<(unsigned)dgpu_cdiv(nb, 256), 256, 0, ctx->stream>>>(
+        d, box, apart, anslice, istl, cfact, lat, lat_nslice, lat_closed, icc[0], icc[1], icc[2],
+        dim0[0], dim0[1], dim0[2], norm, acsf);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return DGPU_OK;
+}
+
+int dgpu_friedel_mirror(dgpu_ctx *ctx, const BoxSpec &box, int32_t idim, double2 *csf, double2 *acsf,
+                        double *dsi)
+{
+    if (idim < 1 || idim > 3) return DGPU_OK;
+    int64_t np = (int64_t)box.num[0] * box.num[1] * box.num[2];
+    k_mirror<<<(unsigned)dgpu_cdiv(np, 256), 256, 0, ctx->stream>>>(box, idim - 1, csf, acsf, dsi);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    return DGPU_OK;
+}
+
+int dgpu_qinfo(dgpu_ctx *ctx, const double eck[3], const double vi[9], const int32_t num[3],
+               const double *dsi, double res[7])
+{
+    FormSpec fs;
+    memset(&fs, 0, sizeof(fs));
+    memcpy(fs.vi, vi, sizeof(fs.vi));
+    FormSpec *d;
+    int rc = upload_formspec(ctx, fs, &d);
+    if (rc) return rc;
+    QStat *parts = (QStat *)((char *)ctx->stats.p + ((sizeof(FormSpec) + 63) & ~(size_t)63));
+    int64_t np = (int64_t)num[0] * num[1] * num[2];
+    int nblk = (int)(dgpu_cdiv(np, QNT) < 1024 ? dgpu_cdiv(np, QNT) : 1024);
+    if (nblk < 1) nblk = 1;
+    DGPU_CUDA(ctx, ctx->flag.ensure(64 + 7 * sizeof(double)));
+    double *d_res = (double *)((char *)ctx->flag.p + 64);
+    k_qinfo_part<<<nblk, QNT, 0, ctx->stream>>>(eck[0], eck[1], eck[2], d, num[0], num[1], num[2], dsi, parts);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    k_qinfo_final<<<1, 32, 0, ctx->stream>>>(parts, nblk, d_res);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    DGPU_CUDA(ctx, cudaMemcpyAsync(res, d_res, 7 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return DGPU_OK;
+}

@@ -1,0 +1,403 @@
+// Atom preparation and lookup tables.
+//
+//  * per-atom phase data: the reference's integer increments
+//    (discus/prog/four_strucf_OMP_mod.f90:135-149, REF22) or an exact 64-bit
+//    fixed-point h.r mod 1 (EXACT64), gathered by type in a stable order
+//    (four_getatm LOT_OFF, discus/prog/fourier_sup.f90:1839-1848) or folded
+//    into the unit cell for <F> (four_aver, fourier_sup.f90:1243-1281);
+//  * istl (four_stltab, fourier_sup.f90:2637-2687) and cfact
+//    (four_formtab, fourier_sup.f90:2691-2743) on the device.
+#include "dgpu_internal.h"
+
+#define PREP_BLK 1024
+#define MAXT 64
+
+// ---------------------------------------------------------------------------
+// phase arithmetic
+
+// a*x products and sums kept unfused: the reference's xinc = u1*x1+u2*x2+u3*x3
+__device__ __forceinline__ double dot3_nc(const double *a, double x0, double x1, double x2)
+{
+    return __dadd_rn(__dadd_rn(__dmul_rn(a[0], x0), __dmul_rn(a[1], x1)), __dmul_rn(a[2], x2));
+}
+
+// NINT(64*I2PI*(x - INT(x) + 0)) : the 2^22 increment of one atom
+__device__ __forceinline__ int64_t inc22(double x)
+{
+    double fr = __dadd_rn(__dsub_rn(x, trunc(x)), 0.0);
+    return (int64_t)llround(__dmul_rn(4194304.0, fr));
+}
+
+// frac(a.x) as a 64-bit fixed-point turn, from error-free FP64 products
+__device__ __forceinline__ uint64_t frac64_dot(const double *a, double x0, double x1, double x2)
+{
+    double p0 = __dmul_rn(a[0], x0), e0 = fma(a[0], x0, -p0);
+    double p1 = __dmul_rn(a[1], x1), e1 = fma(a[1], x1, -p1);
+    double p2 = __dmul_rn(a[2], x2), e2 = fma(a[2], x2, -p2);
+    double s = __dadd_rn(p0, p1);
+    double z = __dsub_rn(s, p0);
+    double es = __dadd_rn(__dsub_rn(p0, __dsub_rn(s, z)), __dsub_rn(p1, z));
+    double t = __dadd_rn(s, p2);
+    z = __dsub_rn(t, s);
+    double et = __dadd_rn(__dsub_rn(s, __dsub_rn(t, z)), __dsub_rn(p2, z));
+    double hi = __dsub_rn(t, floor(t));
+    double lo = __dadd_rn(__dadd_rn(__dadd_rn(es, et), __dadd_rn(e0, e1)), e2);
+    double v = __dadd_rn(hi, lo);
+    double a32 = __dmul_rn(v, 4294967296.0);
+    double ah = floor(a32);
+    double rem = __dsub_rn(a32, ah);
+    uint64_t h32 = (uint64_t)(int64_t)ah;
+    uint64_t l32 = (uint64_t)llrint(__dmul_rn(rem, 4294967296.0));
+    return (h32 << 32) + l32;
+}
+
+struct PhaseOut {
+    uint64_t ph0, du, dv, dw;
+};
+
+__device__ __forceinline__ PhaseOut atom_phase(const PhaseGeom &g, double x0, double x1, double x2)
+{
+    PhaseOut o;
+    if (g.mode == DGPU_PHASE_REF22) {
+        int64_t iu = inc22(dot3_nc(g.vi + 0, x0, x1, x2));
+        int64_t iv = inc22(dot3_nc(g.vi + 3, x0, x1, x2));
+        int64_t iw = inc22(dot3_nc(g.vi + 6, x0, x1, x2));
+        int64_t ju = inc22(dot3_nc(g.off + 0, x0, x1, x2));
+        int64_t jv = inc22(dot3_nc(g.off + 3, x0, x1, x2));
+        int64_t jw = inc22(dot3_nc(g.off + 6, x0, x1, x2));
+        int64_t base = (int64_t)g.lmn[0] * iu + (int64_t)g.lmn[1] * iv + (int64_t)g.lmn[2] * iw
+                     + (int64_t)g.lmn[3] * ju + (int64_t)g.lmn[4] * jv + (int64_t)g.lmn[5] * jw;
+        // unit 2^-22 turn -> 2^-64 turn; bits 6..21 of iarg become bits 48..63
+        o.ph0 = (uint64_t)base << 42;
+        o.du = (uint64_t)iu << 42;
+        o.dv = (uint64_t)iv << 42;
+        o.dw = (uint64_t)iw << 42;
+    } else {
+        o.ph0 = frac64_dot(g.eck, x0, x1, x2);
+        o.du = frac64_dot(g.vi + 0, x0, x1, x2);
+        o.dv = frac64_dot(g.vi + 3, x0, x1, x2);
+        o.dw = frac64_dot(g.vi + 6, x0, x1, x2);
+    }
+    return o;
+}
+
+// effective type of atom i: 0 = not summed
+__device__ __forceinline__ int eff_type(const int32_t *iscat, int64_t i, int64_t n, int32_t nscat,
+                                        const FoldSpec &fs)
+{
+    if (i >= n) return 0;
+    int t = iscat[i];
+    if (t < 1 || t > nscat) return 0;
+    if (fs.fold) {
+        int64_t ncell = (int64_t)fs.icc[0] * fs.icc[1] * fs.icc[2];
+        if (i >= ncell * fs.ncatoms) return 0;     // only atoms in DISCUS cell order
+        int64_t c = i / fs.ncatoms;
+        if (fs.sel && !fs.sel[c]) return 0;
+    }
+    return t;
+}
+
+__global__ void k_type_count(const int32_t *iscat, int64_t n, int32_t nscat, FoldSpec fs,
+                             int32_t *counts, int64_t nblk)
+{
+    __shared__ int32_t hist[MAXT];
+    for (int t = threadIdx.x; t < MAXT; t += blockDim.x) hist[t] = 0;
+    __syncthreads();
+    int64_t i = (int64_t)blockIdx.x * PREP_BLK + threadIdx.x;
+    int t = eff_type(iscat, i, n, nscat, fs);
+    if (t) atomicAdd(&hist[t], 1);
+    __syncthreads();
+    for (int tt = threadIdx.x; tt < nscat; tt += blockDim.x)
+        counts[(int64_t)tt * nblk + blockIdx.x] = hist[tt + 1];
+}
+
+// exclusive scan of len int32 counts into int64 offsets (one CTA)
+__global__ void k_scan_counts(const int32_t *counts, int64_t len, int64_t *offs,
+                              int64_t nblk, int32_t nscat, int64_t *type_start)
+{
+    __shared__ int64_t warp_sums[32];
+    __shared__ int64_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int64_t base = 0; base < len; base += blockDim.x) {
+        int64_t i = base + threadIdx.x;
+        int64_t v = i < len ? counts[i] : 0;
+        int64_t x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_sums[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            int64_t s = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                int64_t y = __shfl_up_sync(0xffffffffu, s, o);
+                if (lane >= o) s += y;
+            }
+            warp_sums[lane] = s;
+        }
+        __syncthreads();
+        int64_t incl = x + (wid > 0 ? warp_sums[wid - 1] : 0) + carry;
+        if (i < len) offs[i] = incl - v;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry = incl;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        for (int t = 0; t < nscat; t++) type_start[t] = offs[(int64_t)t * nblk];
+        type_start[nscat] = carry;
+    }
+}
+
+__global__ void k_scatter_atoms(const double *pos, const int32_t *iscat, const float *aocc,
+                                int64_t n, int32_t nscat, FoldSpec fs, PhaseGeom g,
+                                const int64_t *offs, int64_t nblk, uint64_t *ph0, uint64_t *du,
+                                uint64_t *dv, uint64_t *dw, float *w)
+{
+    __shared__ int32_t wcnt[32][MAXT];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int k = threadIdx.x; k < 32 * MAXT; k += blockDim.x) (&wcnt[0][0])[k] = 0;
+    __syncthreads();
+    int64_t i = (int64_t)blockIdx.x * PREP_BLK + threadIdx.x;
+    int t = eff_type(iscat, i, n, nscat, fs);
+    unsigned same = __match_any_sync(0xffffffffu, t);
+    int rank = __popc(same & ((1u << lane) - 1u));
+    if (t && rank == 0) wcnt[wid][t] = __popc(same);
+    __syncthreads();
+    // exclusive prefix over warps, per type (one thread per type)
+    if (threadIdx.x >= 1 && threadIdx.x <= nscat) {
+        int tt = threadIdx.x, run = 0;
+        for (int ww = 0; ww < 32; ww++) {
+            int c = wcnt[ww][tt];
+            wcnt[ww][tt] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    if (!t) return;
+    int64_t dst = offs[(int64_t)(t - 1) * nblk + blockIdx.x] + wcnt[wid][t] + rank;
+    double x0 = pos[3 * i], x1 = pos[3 * i + 1], x2 = pos[3 * i + 2];
+    if (fs.fold) {
+        int64_t c = i / fs.ncatoms;
+        int64_t ci = c % fs.icc[0];
+        int64_t cj = (c / fs.icc[0]) % fs.icc[1];
+        int64_t ck = c / ((int64_t)fs.icc[0] * fs.icc[1]);
+        // xat = cr_pos - (icell-1) - cr_dim0 (fourier_sup.f90:1272-1281)
+        x0 = __dsub_rn(__dsub_rn(x0, (double)ci), fs.dim0[0]);
+        x1 = __dsub_rn(__dsub_rn(x1, (double)cj), fs.dim0[1]);
+        x2 = __dsub_rn(__dsub_rn(x2, (double)ck), fs.dim0[2]);
+    }
+    PhaseOut o = atom_phase(g, x0, x1, x2);
+    ph0[dst] = o.ph0;
+    du[dst] = o.du;
+    dv[dst] = o.dv;
+    dw[dst] = o.dw;
+    w[dst] = aocc ? aocc[i] : 1.0f;
+}
+
+int dgpu_prepare_atoms(dgpu_ctx *ctx, const double *d_pos, const int32_t *d_iscat,
+                       const float *d_aocc, int64_t natoms, int32_t nscat, const PhaseGeom &g,
+                       const FoldSpec &fs, DevBuf &ph0, DevBuf &du, DevBuf &dv, DevBuf &dw,
+                       DevBuf &w, int64_t *h_type_start)
+{
+    if (nscat < 1 || nscat >= MAXT)
+        return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "nscat=%d outside 1..%d", nscat, MAXT - 1);
+    int64_t nblk = dgpu_cdiv(natoms, PREP_BLK);
+    if (nblk < 1) nblk = 1;
+    int64_t len = nblk * nscat;
+    size_t cnt_bytes = ((size_t)len * sizeof(int32_t) + 255) & ~(size_t)255;
+    DGPU_CUDA(ctx, ctx->counts.ensure(cnt_bytes + (size_t)len * sizeof(int64_t)));
+    int32_t *counts = ctx->counts.as<int32_t>();
+    int64_t *offs = (int64_t *)((char *)ctx->counts.p + cnt_bytes);
+    DGPU_CUDA(ctx, ctx->type_start.ensure((MAXT + 2) * sizeof(int64_t)));
+    int64_t *d_ts = ctx->type_start.as<int64_t>();
+    k_type_count<<<(unsigned)nblk, PREP_BLK, 0, ctx->stream>>>(d_iscat, natoms, nscat, fs, counts, nblk);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    k_scan_counts<<<1, 1024, 0, ctx->stream>>>(counts, len, offs, nblk, nscat, d_ts);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    DGPU_CUDA(ctx, cudaMemcpyAsync(h_type_start, d_ts, (nscat + 1) * sizeof(int64_t),
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    int64_t total = h_type_start[nscat];
+    size_t cap = (size_t)(total > 0 ? total : 1);
+    DGPU_CUDA(ctx, ph0.ensure(cap * 8));
+    DGPU_CUDA(ctx, du.ensure(cap * 8));
+    DGPU_CUDA(ctx, dv.ensure(cap * 8));
+    DGPU_CUDA(ctx, dw.ensure(cap * 8));
+    DGPU_CUDA(ctx, w.ensure(cap * 4));
+    k_scatter_atoms<<<(unsigned)nblk, PREP_BLK, 0, ctx->stream>>>(
+        d_pos, d_iscat, d_aocc, natoms, nscat, fs, g, offs, nblk, ph0.as<uint64_t>(),
+        du.as<uint64_t>(), dv.as<uint64_t>(), dw.as<uint64_t>(), w.as<float>());
+    DGPU_CUDA(ctx, cudaGetLastError());
+    return DGPU_OK;
+}
+
+__global__ void k_lattice(int64_t ncell, int32_t i0, int32_t i1, double d0, double d1, double d2,
+                          PhaseGeom g, uint64_t *ph0, uint64_t *du, uint64_t *dv, uint64_t *dw,
+                          float *w)
+{
+    int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    int64_t ii = c % i0, jj = (c / i0) % i1, kk = c / ((int64_t)i0 * i1);
+    // four_getav LOT_OFF: xat = (ii,jj,kk) + cr_dim0 (fourier_sup.f90:2457-2466)
+    double x0 = __dadd_rn((double)ii, d0), x1 = __dadd_rn((double)jj, d1), x2 = __dadd_rn((double)kk, d2);
+    PhaseOut o = atom_phase(g, x0, x1, x2);
+    ph0[c] = o.ph0;
+    du[c] = o.du;
+    dv[c] = o.dv;
+    dw[c] = o.dw;
+    w[c] = 1.0f;
+}
+
+int dgpu_prepare_lattice(dgpu_ctx *ctx, const int32_t icc[3], const double dim0[3],
+                         const PhaseGeom &g, DevBuf &ph0, DevBuf &du, DevBuf &dv, DevBuf &dw,
+                         DevBuf &w)
+{
+    int64_t ncell = (int64_t)icc[0] * icc[1] * icc[2];
+    DGPU_CUDA(ctx, ph0.ensure(ncell * 8));
+    DGPU_CUDA(ctx, du.ensure(ncell * 8));
+    DGPU_CUDA(ctx, dv.ensure(ncell * 8));
+    DGPU_CUDA(ctx, dw.ensure(ncell * 8));
+    DGPU_CUDA(ctx, w.ensure(ncell * 4));
+    k_lattice<<<(unsigned)dgpu_cdiv(ncell, 256), 256, 0, ctx->stream>>>(
+        ncell, icc[0], icc[1], dim0[0], dim0[1], dim0[2], g, ph0.as<uint64_t>(),
+        du.as<uint64_t>(), dv.as<uint64_t>(), dw.as<uint64_t>(), w.as<float>());
+    DGPU_CUDA(ctx, cudaGetLastError());
+    return DGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// tables
+
+// istl(i,j,l) = NINT(sqrt(h.G*.h/4)/CFINC) with h rounded to REAL(4)
+__global__ void k_stltab(double e0, double e1, double e2, PhaseGeom vg, int32_t n0, int32_t n1,
+                         int32_t n2, double r00, double r10, double r20, double r01, double r11,
+                         double r21, double r02, double r12, double r22, int32_t *istl,
+                         int32_t *flag)
+{
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t np = (int64_t)n0 * n1 * n2;
+    if (p >= np) return;
+    int64_t i = p % n0, j = (p / n0) % n1, l = p / ((int64_t)n0 * n1);
+    const double *vi = vg.vi;
+    double e[3] = {e0, e1, e2}, h[3];
+    for (int k = 0; k < 3; k++) {
+        double s = __dadd_rn(__dadd_rn(__dadd_rn(e[k], __dmul_rn(vi[k], (double)i)),
+                                       __dmul_rn(vi[3 + k], (double)j)),
+                             __dmul_rn(vi[6 + k], (double)l));
+        h[k] = (double)__double2float_rn(s);
+    }
+    double t0 = __dadd_rn(__dadd_rn(__dmul_rn(r00, h[0]), __dmul_rn(r01, h[1])), __dmul_rn(r02, h[2]));
+    double t1 = __dadd_rn(__dadd_rn(__dmul_rn(r10, h[0]), __dmul_rn(r11, h[1])), __dmul_rn(r12, h[2]));
+    double t2 = __dadd_rn(__dadd_rn(__dmul_rn(r20, h[0]), __dmul_rn(r21, h[1])), __dmul_rn(r22, h[2]));
+    double q = __dadd_rn(__dadd_rn(__dmul_rn(h[0], t0), __dmul_rn(h[1], t1)), __dmul_rn(h[2], t2));
+    double q2 = q / 4.0;
+    long long v = llround(__dmul_rn(__dsqrt_rn(q2), 1000.0));
+    istl[p] = (int32_t)v;
+    if (v > DGPU_CFPKT) atomicExch(flag, 1);
+}
+
+int dgpu_stltab_dev(dgpu_ctx *ctx, const double eck[3], const double vi[9], const int32_t num[3],
+                    const double rten[9], int32_t *d_istl)
+{
+    int64_t np = (int64_t)num[0] * num[1] * num[2];
+    DGPU_CUDA(ctx, ctx->flag.ensure(64));
+    int32_t *flag = ctx->flag.as<int32_t>();
+    DGPU_CUDA(ctx, cudaMemsetAsync(flag, 0, 4, ctx->stream));
+    PhaseGeom vg;
+    memset(&vg, 0, sizeof(vg));
+    memcpy(vg.vi, vi, sizeof(vg.vi));
+    k_stltab<<<(unsigned)dgpu_cdiv(np, 256), 256, 0, ctx->stream>>>(
+        eck[0], eck[1], eck[2], vg, num[0], num[1], num[2], rten[0], rten[1], rten[2], rten[3],
+        rten[4], rten[5], rten[6], rten[7], rten[8], d_istl, flag);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    int32_t hflag = 0;
+    DGPU_CUDA(ctx, cudaMemcpyAsync(&hflag, flag, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (hflag)
+        return dgpu_set_error(ctx, DGPU_ERR_STL_RANGE,
+                              "sin(theta)/lambda beyond the form-factor table (istl > %d)", DGPU_CFPKT);
+    return DGPU_OK;
+}
+
+struct FormCoef {
+    double scat[MAXT * 11];
+    double occ[MAXT], dw[MAXT], delfr[MAXT], delfi[MAXT];
+};
+
+// cfact(iq,t) = sb*(f+f') + i sb*f'' ; f = c + sum_i a_i exp(-b_i s^2)
+__global__ void k_formtab(const FormCoef *fc, int32_t nscat, int32_t lxray, int32_t power,
+                          int32_t ano, int32_t ldbw, double2 *cfact)
+{
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= (int64_t)nscat * DGPU_NTAB) return;
+    int t = (int)(k / DGPU_NTAB) + 1, iq = (int)(k % DGPU_NTAB);
+    double s = __dmul_rn((double)iq, DGPU_CFINC);
+    double q2 = __dmul_rn(s, s);
+    const double *sc = fc->scat + 11 * t;
+    double f = sc[0];
+    if (lxray)
+        for (int i = 1; i <= power; i++) f = __dadd_rn(f, __dmul_rn(sc[2 * i - 1], exp(-__dmul_rn(sc[2 * i], q2))));
+    double fp = ano ? fc->delfr[t] : 0.0, fpp = ano ? fc->delfi[t] : 0.0;
+    double sb = ldbw ? __dmul_rn(exp(-__dmul_rn(fc->dw[t], q2)), fc->occ[t]) : fc->occ[t];
+    cfact[k] = make_double2(__dmul_rn(sb, __dadd_rn(f, fp)), __dmul_rn(sb, fpp));
+}
+
+int dgpu_formtab_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *op, double2 *d_cfact)
+{
+    if (cr->nscat < 1 || cr->nscat >= MAXT)
+        return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "nscat=%d outside 1..%d", cr->nscat, MAXT - 1);
+    FormCoef h;
+    memset(&h, 0, sizeof(h));
+    for (int t = 0; t <= cr->nscat; t++) {
+        for (int i = 0; i < 11; i++) h.scat[11 * t + i] = cr->scat[11 * t + i];
+        h.occ[t] = cr->occ[t];
+        h.dw[t] = cr->dw[t];
+        h.delfr[t] = cr->delfr ? cr->delfr[t] : 0.0;
+        h.delfi[t] = cr->delfi ? cr->delfi[t] : 0.0;
+    }
+    DGPU_CUDA(ctx, ctx->stats.ensure(sizeof(FormCoef)));
+    FormCoef *d = ctx->stats.as<FormCoef>();
+    DGPU_CUDA(ctx, cudaMemcpyAsync(d, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->stream));
+    int64_t n = (int64_t)cr->nscat * DGPU_NTAB;
+    k_formtab<<<(unsigned)dgpu_cdiv(n, 256), 256, 0, ctx->stream>>>(d, cr->nscat, op->lxray, op->power,
+                                                                      op->ano, op->ldbw, d_cfact);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    // the coefficient block lives in ctx->stats: finish before it is reused
+    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return DGPU_OK;
+}
+
+__global__ void k_increments(const double *xat, int64_t n, PhaseGeom g, int64_t *out)
+{
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    double x0 = xat[k], x1 = xat[n + k], x2 = xat[2 * n + k];
+    out[0 * n + k] = inc22(dot3_nc(g.vi + 0, x0, x1, x2));
+    out[1 * n + k] = inc22(dot3_nc(g.vi + 3, x0, x1, x2));
+    out[2 * n + k] = inc22(dot3_nc(g.vi + 6, x0, x1, x2));
+    out[3 * n + k] = inc22(dot3_nc(g.off + 0, x0, x1, x2));
+    out[4 * n + k] = inc22(dot3_nc(g.off + 3, x0, x1, x2));
+    out[5 * n + k] = inc22(dot3_nc(g.off + 6, x0, x1, x2));
+}
+
+int dgpu_increments_dev(dgpu_ctx *ctx, const double *d_xat, int64_t nxat, const double uin[3],
+                        const double vin[3], const double win[3], const double off[9],
+                        int64_t *d_out)
+{
+    PhaseGeom g;
+    memset(&g, 0, sizeof(g));
+    for (int k = 0; k < 3; k++) {
+        g.vi[k] = uin[k];
+        g.vi[3 + k] = vin[k];
+        g.vi[6 + k] = win[k];
+    }
+    memcpy(g.off, off, sizeof(g.off));
+    if (nxat > 0) {
+        k_increments<<<(unsigned)dgpu_cdiv(nxat, 256), 256, 0, ctx->stream>>>(d_xat, nxat, g, d_out);
+        DGPU_CUDA(ctx, cudaGetLastError());
+    }
+    return DGPU_OK;
+}

@@ -1,0 +1,164 @@
+"""Python mirror of DISCUS's `fourier` menu for the `run` path.
+
+The menu state (discus/prog/fourier.f90:9-1062, defaults from
+fourier_reset.f90:42-101) is kept in a `Fourier` object; `run()` calls the
+C-ABI (dgpu_four_run) and returns csf, acsf, dsi shaped (num1, num2, num3)
+in Fortran order, plus the four_qinfo values of res[].
+
+    f = Fourier(crystal)
+    f.ll, f.lr, f.ul = (-5,-5,0), (5,-5,0), (-5,5,0)
+    f.nabs, f.nord = 201, 201
+    f.temp = "use"
+    out = f.run()
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi
+from ._lib import default_context
+from .structures import CrystalData, GridData
+
+
+@dataclass
+class FourierResult:
+    csf: np.ndarray
+    acsf: np.ndarray
+    dsi: np.ndarray
+    info: _abi.Info
+    status: int
+
+    @property
+    def res(self):
+        """four_qinfo: res[0]=6, diffumin, diffumax, diffuave, diffusig, braggmin, braggmax."""
+        return list(self.info.res)
+
+
+def _cplx(buf, shape):
+    return (buf[0::2] + 1j * buf[1::2]).reshape(shape, order="F")
+
+
+def four_run(cr: CrystalData, grid: GridData, opts: _abi.Opts, ctx=None, aver_cells=None):
+    """four_run (discus/prog/fourier_sup.f90:11-323) on the GPU."""
+    ctx = ctx or default_context()
+    np_ = grid.npoints
+    csf = np.zeros(2 * np_)
+    acsf = np.zeros(2 * np_)
+    dsi = np.zeros(np_)
+    info = _abi.Info()
+    c = cr.to_c()
+    g = grid.to_c()
+    keep = None
+    if aver_cells is not None:
+        keep = np.ascontiguousarray(np.asarray(aver_cells, dtype=np.uint8).reshape(-1, order="F"))
+        opts.aver_cells = keep.ctypes.data_as(C.POINTER(C.c_uint8))
+    rc = ctx.check(ctx.lib.dgpu_four_run(ctx.h, C.byref(c), C.byref(g), C.byref(opts), _abi.dptr(csf),
+                                         _abi.dptr(acsf), _abi.dptr(dsi), C.byref(info)))
+    del keep
+    shp = grid.inc
+    return FourierResult(_cplx(csf, shp), _cplx(acsf, shp), dsi.reshape(shp, order="F"), info, rc)
+
+
+def fourier_lmn(eck, vi, inc, ctx=None):
+    """fourier_lmn (discus/prog/fourier_lmn_mod.f90:4-280): (rc, lmn[6], off_shift(3,3))."""
+    ctx = ctx or default_context()
+    e = np.asarray(eck, dtype=np.float64).reshape(-1, order="F").copy()
+    v = np.asarray(vi, dtype=np.float64).reshape(-1, order="F").copy()
+    i = np.asarray(inc, dtype=np.int32).copy()
+    lmn = np.zeros(6, np.int32)
+    off = np.zeros(9)
+    rc = ctx.lib.dgpu_fourier_lmn(_abi.dptr(e), _abi.dptr(v), _abi.iptr(i), _abi.iptr(lmn), _abi.dptr(off))
+    return rc, lmn, off.reshape(3, 3, order="F")
+
+
+def four_stltab(grid: GridData, rten, ctx=None):
+    """four_stltab (fourier_sup.f90:2637-2687) on the device: (rc, istl)."""
+    ctx = ctx or default_context()
+    g = grid.to_c()
+    rt = np.asarray(rten, dtype=np.float64).reshape(-1, order="F").copy()
+    istl = np.zeros(grid.npoints, np.int32)
+    rc = ctx.lib.dgpu_four_stltab(ctx.h, C.byref(g), _abi.dptr(rt), _abi.iptr(istl))
+    return rc, istl.reshape(grid.inc, order="F")
+
+
+def four_formtab(cr: CrystalData, opts, ctx=None):
+    """four_formtab (fourier_sup.f90:2691-2743): cfact (nscat, CFPKT+1) complex."""
+    ctx = ctx or default_context()
+    c = cr.to_c()
+    out = np.zeros(2 * cr.nscat * (_abi.CFPKT + 1))
+    ctx.check(ctx.lib.dgpu_four_formtab(ctx.h, C.byref(c), C.byref(opts), _abi.dptr(out)))
+    return (out[0::2] + 1j * out[1::2]).reshape(cr.nscat, _abi.CFPKT + 1)
+
+
+def four_increments(xat, uin, vin, win, off, ctx=None):
+    """Per-atom REF22 increments (four_strucf_OMP_mod.f90:135-149): int64 (6, n)."""
+    ctx = ctx or default_context()
+    x = np.asfortranarray(xat, dtype=np.float64)
+    n = x.shape[0]
+    out = np.zeros(6 * max(n, 1), np.int64)
+    u, v, w = (np.asarray(a, dtype=np.float64).copy() for a in (uin, vin, win))
+    o = np.asarray(off, dtype=np.float64).reshape(-1, order="F").copy()
+    ctx.check(ctx.lib.dgpu_four_increments(ctx.h, x.ctypes.data_as(C.POINTER(C.c_double)), n, _abi.dptr(u),
+                                           _abi.dptr(v), _abi.dptr(w), _abi.dptr(o),
+                                           out.ctypes.data_as(C.POINTER(C.c_int64))))
+    return out[: 6 * n].reshape(6, n)
+
+
+def four_strucf(xat, uin, vin, win, off, lmn, num, fnum, cfact=None, istl=None, ctx=None):
+    """four_strucf (four_strucf_OMP_mod.f90:19-68) + tcsf_form_iso: tcsf(num)."""
+    ctx = ctx or default_context()
+    x = np.asfortranarray(xat, dtype=np.float64)
+    n = x.shape[0]
+    u, v, w = (np.asarray(a, dtype=np.float64).copy() for a in (uin, vin, win))
+    o = np.asarray(off, dtype=np.float64).reshape(-1, order="F").copy()
+    lm = np.asarray(lmn, dtype=np.int32).copy()
+    nm = np.asarray(num, dtype=np.int32).copy()
+    fn = np.asarray(fnum, dtype=np.int32).copy()
+    np_ = int(np.prod(num))
+    out = np.zeros(2 * np_)
+    cf = None
+    ist = None
+    if cfact is not None:
+        cf = np.ascontiguousarray(np.stack([np.real(cfact), np.imag(cfact)], -1).ravel())
+        ist = np.asfortranarray(istl, dtype=np.int32).reshape(-1, order="F").copy()
+    ctx.check(ctx.lib.dgpu_four_strucf(ctx.h, x.ctypes.data_as(C.POINTER(C.c_double)), n, _abi.dptr(u),
+                                       _abi.dptr(v), _abi.dptr(w), _abi.dptr(o), _abi.iptr(lm), _abi.iptr(nm),
+                                       _abi.iptr(fn), _abi.dptr(cf), _abi.iptr(ist), _abi.dptr(out)))
+    return _cplx(out, tuple(num))
+
+
+class Fourier:
+    """Menu state of `fourier` with its reset defaults (fourier_reset.f90:42-101)."""
+
+    def __init__(self, crystal: CrystalData):
+        self.crystal = crystal
+        self.ll = (0.0, 0.0, 0.0)
+        self.lr = (5.0, 0.0, 0.0)
+        self.ul = (0.0, 5.0, 0.0)
+        self.tl = None
+        self.nabs, self.nord, self.ntop = 121, 121, 1
+        self.radiation = "xray"     # xray | neut
+        self.power = 4
+        self.temp = "ignore"        # use | ignore
+        self.aver = 0.0             # set aver
+        self.friedel = True         # set friedel
+        self.anomalous = False
+        self.scale = 1.0
+        self.phase = _abi.PHASE_EXACT64
+        self.form = _abi.FORM_TABLE
+        self.engine = _abi.ENGINE_AUTO
+
+    def grid(self) -> GridData:
+        return GridData.from_corners(self.ll, self.lr, self.ul, self.tl, inc=(self.nabs, self.nord, self.ntop))
+
+    def opts(self) -> _abi.Opts:
+        return _abi.default_opts(lxray=int(self.radiation == "xray"), power=self.power,
+                                 ano=int(self.anomalous), ldbw=int(self.temp == "use"),
+                                 friedel=int(self.friedel), fave=float(self.aver), diff_scale=self.scale,
+                                 phase=self.phase, form=self.form, engine=self.engine)
+
+    def run(self, ctx=None, aver_cells=None) -> FourierResult:
+        return four_run(self.crystal, self.grid(), self.opts(), ctx=ctx, aver_cells=aver_cells)

@@ -1,0 +1,217 @@
+/*
+ * discus_gpu.h -- C-ABI of the GB300 Fourier structure-factor library.
+ *
+ * This is the drop-in boundary for DISCUS's `fourier` -> `run` path
+ * (discus/prog/fourier.f90:639-747 -> four_run, discus/prog/fourier_sup.f90:11-323).
+ * Every entry point takes plain pointers, sizes and POD structs; nothing
+ * here depends on PyTorch.  Arrays follow the Fortran layout DISCUS uses:
+ * column-major, first index fastest, so a Fortran caller passes its module
+ * arrays (csf, dsi, acsf, cr_pos, cr_iscat, ...) straight through
+ * ISO_C_BINDING without copies.
+ *
+ * Complex arrays are interleaved (re, im) doubles, i.e. Fortran
+ * COMPLEX(KIND=8) / C99 double _Complex.
+ *
+ * Return values: 0 = success, >0 = warning (result valid), <0 = error.
+ * Errors map onto DISCUS's ier_num/ier_typ (lib_f90/errlist_mod.f90:48);
+ * the mapping is given beside each code.  dgpu_last_error() returns the
+ * message that would go into ier_msg.
+ */
+#ifndef DISCUS_GPU_H
+#define DISCUS_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define DGPU_OK                 0
+#define DGPU_WARN_NO_CELL       1   /* four_aver: ncell == 0 (ier_num=+1, ER_FOUR)            */
+#define DGPU_ERR_ARG          (-1)  /* invalid argument / shape                                */
+#define DGPU_ERR_CUDA         (-2)  /* CUDA runtime failure                                     */
+#define DGPU_ERR_NOMEM        (-3)  /* device allocation failed                                 */
+#define DGPU_ERR_STL_RANGE    (-4)  /* sin(theta)/lambda beyond table (ier_num=-3, ER_FOUR)    */
+#define DGPU_ERR_ZERO_INC     (-5)  /* inc>1 with zero increment vector (ier_num=-132, ER_APPL) */
+#define DGPU_ERR_UNSUPPORTED  (-6)  /* option not available on this path                       */
+#define DGPU_ERR_TIMEOUT      (-7)  /* a bounded device wait gave up                            */
+#define DGPU_ERR_CANCELLED   (-14)  /* cancel flag seen (ier_num=-14, ER_COMM, like ier_ctrlc)  */
+#define DGPU_ERR_NO_ATOMS   (-198)  /* cr_natoms < 1 (ier_num=-198, ER_APPL)                   */
+#define DGPU_ERR_SCRATCH_SIZE (-20) /* request exceeds a fixed scratch capacity                */
+
+/* ---- tables (discus/prog/discus_config_mod.f90:27-28, diffuse_mod.f90:20-21) */
+#define DGPU_CFPKT   9999          /* last index of the sin(theta)/lambda table              */
+#define DGPU_CFINC   0.001         /* its step in 1/Angstrom                                 */
+#define DGPU_I2PI    65536         /* entries of the phase table cex(0:MASK)                 */
+
+/* ---- phase arithmetic --------------------------------------------------- */
+/* REF22: the reference's integer phase.  Per-atom increments are
+ * NINT(2^22 * frac(x.v)) and the phase index is (iarg>>6)&0xFFFF, i.e. the
+ * phase is truncated to 2^-16 turn (four_strucf_OMP_mod.f90:136-148,163-170).
+ * EXACT64: 64-bit fixed-point h.r mod 1 (2^-64 turn resolution).           */
+#define DGPU_PHASE_REF22    0
+#define DGPU_PHASE_EXACT64  1
+
+/* Form factor: TABLE = cfact(istl) lookup on the 0.001 1/A grid
+ * (four_formtab/four_stltab, fourier_sup.f90:2637-2743); ANALYTIC = the
+ * same formula evaluated at the exact sin(theta)/lambda of each point.     */
+#define DGPU_FORM_TABLE     0
+#define DGPU_FORM_ANALYTIC  1
+
+/* Engine for the atom x point sum. */
+#define DGPU_ENGINE_AUTO    0   /* TC when the phase mode allows it, else DIRECT */
+#define DGPU_ENGINE_DIRECT  1   /* FP32 direct sum on CUDA cores                 */
+#define DGPU_ENGINE_TC      2   /* tcgen05 split-precision complex GEMM          */
+
+/* Operand split of the tensor-core engine. */
+#define DGPU_SPLIT_F16      0   /* fp16 hi + fp16 lo, 3 products  (default)      */
+#define DGPU_SPLIT_BF16     1   /* bf16 hi + bf16 lo, 3 products                 */
+
+typedef struct dgpu_ctx dgpu_ctx;   /* opaque: device, stream, cached buffers */
+
+/* The crystal: crystal_mod (discus/prog/crystal_mod.f90:25-138). */
+typedef struct dgpu_crystal {
+    int64_t        natoms;     /* cr_natoms                                              */
+    const double  *pos;        /* cr_pos(3,natoms): pos[3*i+k], lattice units            */
+    const int32_t *iscat;      /* cr_iscat(1,:): type 1..nscat, 0 = VOID (skipped)       */
+    const float   *atom_occ;   /* per-atom occupancy weight, NULL = 1 (not in DISCUS)    */
+    int32_t        nscat;      /* cr_nscat                                               */
+    int32_t        ncatoms;    /* cr_ncatoms, sites per unit cell                        */
+    int32_t        icc[3];     /* cr_icc, unit cells per axis                            */
+    double         dim0[3];    /* cr_dim0(:,1), lower corner of the crystal              */
+    double         rten[9];    /* cr_rten(3,3), reciprocal metric tensor, column-major   */
+    const double  *scat;       /* cr_scat(11,0:nscat): scat[11*t+0]=c, [11*t+2i-1]=a_i,
+                                  [11*t+2i]=b_i (i=1..5)                                  */
+    const double  *occ;        /* cr_occ(0:nscat)                                        */
+    const double  *dw;         /* cr_dw(0:nscat), isotropic B in A^2                     */
+    const double  *delfr;      /* cr_delfr(0:nscat), f', used only when ano != 0         */
+    const double  *delfi;      /* cr_delfi(0:nscat), f'', used only when ano != 0        */
+} dgpu_crystal;
+
+/* The reciprocal-space grid: diffuse_mod eck/vi/inc (diffuse_mod.f90:100,113-119). */
+typedef struct dgpu_grid {
+    double  eck[12];   /* eck(3,4): corners ll, lr, ul, tl, column-major         */
+    double  vi[9];     /* vi(3,3): abscissa, ordinate, top increment vectors    */
+    int32_t inc[3];    /* points per axis (num)                                 */
+} dgpu_grid;
+
+/* Fourier menu state that four_run reads (fourier_reset.f90:42-101 defaults). */
+typedef struct dgpu_opts {
+    int32_t lxray;          /* 1: X-ray Gaussian form factors; 0: neutron, c only    */
+    int32_t power;          /* diff_power: number of Gaussians, 4 or 5              */
+    int32_t ano;            /* anomalous scattering                                 */
+    int32_t ldbw;           /* 'temp use': isotropic Debye-Waller in cfact          */
+    int32_t friedel;        /* four_friedel: halve the grid when allowed            */
+    double  fave;           /* 'set aver': 0 off, 1 all cells; 0<fave<1 needs cells  */
+    const uint8_t *aver_cells; /* cell selection for 0<fave<1, cells(icc1,icc2,icc3),
+                                  drawn by the caller's ran1 stream (fourier_sup.f90:1235-1241) */
+    double  diff_scale;     /* intensity scale (fourier_sup.f90:281-282), default 1  */
+    int32_t phase;          /* DGPU_PHASE_*                                         */
+    int32_t form;           /* DGPU_FORM_*                                          */
+    int32_t engine;         /* DGPU_ENGINE_*                                        */
+    int32_t split;          /* DGPU_SPLIT_* (tensor-core engine)                    */
+    int32_t tc_tile_n;      /* tensor-core N tile in points (0 = autotuned)         */
+    int32_t tc_kslice;      /* atoms per tensor-core work item (0 = autotuned)      */
+    volatile int32_t *cancel; /* optional host flag polled between atom types      */
+} dgpu_opts;
+
+/* What four_run reports besides the arrays. */
+typedef struct dgpu_info {
+    int32_t fnum[3];           /* points computed (Friedel-reduced)                   */
+    int32_t friedel_dim;       /* 0 none, else the halved axis (diff_idim)            */
+    int32_t lmn[6];            /* fourier_lmn output                                  */
+    double  off_shift[9];      /* fourier_lmn output                                  */
+    int32_t ncell;             /* cells used for <F>                                  */
+    int32_t engine_used;       /* DGPU_ENGINE_DIRECT or DGPU_ENGINE_TC                */
+    int64_t pairs;             /* atom x full-grid-point pairs of the type sums       */
+    int64_t pairs_aver;        /* atom/cell x point pairs of <F>                      */
+    double  res[7];            /* four_qinfo: res[0]=6, diffumin, diffumax, diffuave,
+                                  diffusig, braggmin, braggmax (fourier_sup.f90:2930-2936) */
+    double  kernel_ms;         /* device time of the atom x point sums               */
+    double  total_ms;          /* device time of the whole call                      */
+} dgpu_info;
+
+/* ---- context ------------------------------------------------------------ */
+int  dgpu_ctx_create(int device, dgpu_ctx **out);
+int  dgpu_ctx_destroy(dgpu_ctx *ctx);
+const char *dgpu_last_error(const dgpu_ctx *ctx);
+void dgpu_default_opts(dgpu_opts *opts);   /* fourier_reset.f90 defaults + engine AUTO */
+
+/* ---- the whole path ----------------------------------------------------- */
+/* Replaces four_run (discus/prog/fourier_sup.f90:11-323) for LOT_OFF with
+ * isotropic ADPs: tables, Friedel reduction, <F> (four_aver), the per-type
+ * structure-factor sums, csf -= acsf, dsi += |csf|^2, mirror, scale and
+ * four_qinfo statistics.  Host buffers: csf/acsf are complex num(1)*num(2)*num(3),
+ * dsi is real.  acsf may be NULL.                                          */
+int dgpu_four_run(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid,
+                  const dgpu_opts *opts, double *csf, double *acsf, double *dsi,
+                  dgpu_info *info);
+
+/* Same as dgpu_four_run, but cr->pos, cr->iscat, cr->atom_occ and the three
+ * output arrays are DEVICE pointers (resident in HBM); the small per-type
+ * arrays (scat, occ, dw, delfr, delfi) stay on the host.                   */
+int dgpu_four_run_device(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid,
+                         const dgpu_opts *opts, double *d_csf, double *d_acsf,
+                         double *d_dsi, dgpu_info *info);
+
+/* ---- per-type drop-in ----------------------------------------------------- */
+/* Replaces four_strucf (discus/prog/four_strucf_OMP_mod.f90:19-68) as the
+ * RMC/stack/powder callers use it: the reference's REF22 phase of nxat atoms
+ * xat(nxat,3) on the grid num with increments uin/vin/win, corner lmn and
+ * off_shift, then (if cfact != NULL) tcsf *= cfact(istl) on fnum
+ * (fourier_form.f90:147-177).  tcsf is complex num(1)*num(2)*num(3); points
+ * outside fnum are zero.  cfact is complex(0:CFPKT) for this type, istl is
+ * int32 num(1)*num(2)*num(3).  Host buffers.                                */
+int dgpu_four_strucf(dgpu_ctx *ctx, const double *xat, int64_t nxat,
+                     const double uin[3], const double vin[3], const double win[3],
+                     const double off_shift[9], const int32_t lmn[6],
+                     const int32_t num[3], const int32_t fnum[3],
+                     const double *cfact, const int32_t *istl, double *tcsf);
+
+/* ---- tables (each replaces one reference routine; host buffers) ---------- */
+/* fourier_lmn (discus/prog/fourier_lmn_mod.f90:4-280), host quad precision. */
+int dgpu_fourier_lmn(const double eck[12], const double vi[9], const int32_t inc[3],
+                     int32_t lmn[6], double off_shift[9]);
+/* four_stltab (fourier_sup.f90:2637-2687), computed on the device.         */
+int dgpu_four_stltab(dgpu_ctx *ctx, const dgpu_grid *grid, const double rten[9],
+                     int32_t *istl);
+/* four_formtab (fourier_sup.f90:2691-2743): cfact(0:CFPKT, 1:nscat), complex. */
+int dgpu_four_formtab(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *opts,
+                      double *cfact);
+/* Per-atom REF22 increments iincu,iincv,iincw,jincu,jincv,jincw
+ * (four_strucf_OMP_mod.f90:136-148) as int64 [6][nxat], computed on the device. */
+int dgpu_four_increments(dgpu_ctx *ctx, const double *xat, int64_t nxat,
+                         const double uin[3], const double vin[3], const double win[3],
+                         const double off_shift[9], int64_t *inc_out);
+
+/* ---- adjoint: chi^2 and its gradient ------------------------------------- */
+/* chi2 = sum_h w(h) (I(h) - I_target(h))^2 over the full grid, I = diff_scale*|csf|^2
+ * as dgpu_four_run computes it (EXACT64 phase, ANALYTIC or TABLE form).
+ * grad_pos is d chi2 / d cr_pos (3*natoms, lattice units), grad_occ is
+ * d chi2 / d atom_occ (natoms).  VOID atoms get zero.  Host buffers; the
+ * gradient arrays may be NULL.  Used by RMC/REFINE in place of finite
+ * differences (refine/prog/refine_run.f90:491-759).                         */
+int dgpu_chi2_grad(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid,
+                   const dgpu_opts *opts, const double *i_target, const double *weight,
+                   double *chi2, double *grad_pos, double *grad_occ, dgpu_info *info);
+
+/* ---- batched population --------------------------------------------------- */
+/* Many independent crystals (a DIFFEV population, diffev/prog/with_mpi.f90:281-510
+ * farms one four_run per member) in one persistent launch.  dsi[c] receives
+ * crystal c's intensity (host buffer, num(1)*num(2)*num(3) of grids[c]);
+ * when i_target != NULL, chi2[c] and the gradients of member c are returned
+ * as well (grad_pos[c], grad_occ[c] may be NULL).                           */
+int dgpu_batch_run(dgpu_ctx *ctx, int32_t ncrystal, const dgpu_crystal *crystals,
+                   const dgpu_grid *grids, const dgpu_opts *opts,
+                   double *const *dsi,
+                   const double *const *i_target, const double *const *weight,
+                   double *chi2, double *const *grad_pos, double *const *grad_occ);
+
+/* Device time of the last dgpu_batch_run call's persistent launch, ms. */
+double dgpu_batch_last_ms(const dgpu_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DISCUS_GPU_H */

@@ -1,0 +1,829 @@
+/*
+ * CPU oracle of DISCUS's Fourier path -- TEST INFRASTRUCTURE ONLY.
+ * See discus_oracle.h: parity unpinned (no Fortran compiler, no reference
+ * tests); only tests/, smoke() and bench.py's CPU legs may use this file.
+ *
+ * Every function cites the reference routine it restates (paths relative to
+ * the DiffuseCode source tree).  Build: oracle/build_oracle.sh (gcc, OpenMP,
+ * -ffp-contract=off so that a*b+c is never fused: the reference's own
+ * rounding under -ffast-math is compiler dependent, this file fixes one).
+ */
+#include "discus_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define CFPKT DGPU_CFPKT
+#define NTAB  (CFPKT + 1)
+
+/* ---------------------------------------------------------------------- */
+/* quad precision for fourier_lmn (PREC_QP, lib_f90/precision_mod.f90:13)  */
+#if defined(__aarch64__)
+typedef long double qreal;           /* IEEE binary128 on aarch64 */
+#else
+typedef __float128 qreal;            /* IEEE binary128 on x86_64 */
+#endif
+
+static qreal q_abs(qreal x) { return x < 0 ? -x : x; }
+static qreal q_sqrt(qreal x)
+{
+    if (x <= 0) return 0;
+    qreal y = (qreal)sqrt((double)x);
+    y = 0.5 * (y + x / y);           /* two Newton steps from a double seed */
+    y = 0.5 * (y + x / y);
+    return y;
+}
+/* Fortran NINT: round half away from zero */
+static int64_t q_nint(qreal x)
+{
+    return x >= 0 ? (int64_t)(x + (qreal)0.5) : -(int64_t)(-x + (qreal)0.5);
+}
+
+#define M3(a, r, c) (a)[3 * (c) + (r)]          /* column-major 3x3, 0-based */
+
+/* matinv3_q / det3_q, lib_f90/matrix_mod.f90:81-92,271-300 */
+static int q_matinv3(const qreal *a, qreal *b)
+{
+    qreal det = M3(a,0,0)*M3(a,1,1)*M3(a,2,2) - M3(a,0,0)*M3(a,1,2)*M3(a,2,1)
+              - M3(a,0,1)*M3(a,1,0)*M3(a,2,2) + M3(a,0,1)*M3(a,1,2)*M3(a,2,0)
+              + M3(a,0,2)*M3(a,1,0)*M3(a,2,1) - M3(a,0,2)*M3(a,1,1)*M3(a,2,0);
+    for (int i = 0; i < 9; i++) b[i] = 0;
+    if (det == 0) return -1;
+    qreal di = (qreal)1 / det;
+    M3(b,0,0) = +di * (M3(a,1,1)*M3(a,2,2) - M3(a,1,2)*M3(a,2,1));
+    M3(b,1,0) = -di * (M3(a,1,0)*M3(a,2,2) - M3(a,1,2)*M3(a,2,0));
+    M3(b,2,0) = +di * (M3(a,1,0)*M3(a,2,1) - M3(a,1,1)*M3(a,2,0));
+    M3(b,0,1) = -di * (M3(a,0,1)*M3(a,2,2) - M3(a,0,2)*M3(a,2,1));
+    M3(b,1,1) = +di * (M3(a,0,0)*M3(a,2,2) - M3(a,0,2)*M3(a,2,0));
+    M3(b,2,1) = -di * (M3(a,0,0)*M3(a,2,1) - M3(a,0,1)*M3(a,2,0));
+    M3(b,0,2) = +di * (M3(a,0,1)*M3(a,1,2) - M3(a,0,2)*M3(a,1,1));
+    M3(b,1,2) = -di * (M3(a,0,0)*M3(a,1,2) - M3(a,0,2)*M3(a,1,0));
+    M3(b,2,2) = +di * (M3(a,0,0)*M3(a,1,1) - M3(a,0,1)*M3(a,1,0));
+    return 0;
+}
+
+/* fourier_lmn, discus/prog/fourier_lmn_mod.f90:4-279.
+ * The ran1 draws of the "line through the origin" branch (:185-195) only
+ * feed offset directions whose lmn multiplier is zero, so fixed values are
+ * used here. */
+int oc_fourier_lmn(const double eck_in[12], const double vi_in[9], const int32_t inc[3],
+                   int32_t lmn[6], double off_out[9])
+{
+    const qreal big = 10000000;
+    const qreal eps7 = (qreal)1.0e-7f;               /* 1.0E-7 default real */
+    const qreal tiny = (qreal)1.0e-9;                /* 1.0D-9 */
+    qreal eck[12], vi[9], off[9], mat_a[9], mat_i[9], vec_r[3], vec_t[3];
+    int direc[3] = {0, 0, 0}, nooff[3] = {0, 0, 0}, dimen = 0, need_work = 1;
+    static const double ranv[6] = {0.3141592, 0.2718281, 0.5772156,
+                                   0.6931471, 0.4142135, 0.7320508};
+
+    for (int i = 0; i < 12; i++) eck[i] = (qreal)q_nint((qreal)eck_in[i] * big) / big;
+    for (int i = 0; i < 9; i++)  vi[i]  = (qreal)q_nint((qreal)vi_in[i] * big) / big;
+    for (int i = 0; i < 9; i++) { mat_a[i] = 0; mat_i[i] = 0; off[i] = 0; }
+    for (int i = 0; i < 6; i++) lmn[i] = 0;
+
+    for (int i = 0; i < 3; i++) {
+        if (inc[i] > 1) {
+            qreal d = q_sqrt(q_abs(M3(vi,0,i)*M3(vi,0,i) + M3(vi,1,i)*M3(vi,1,i)
+                                   + M3(vi,2,i)*M3(vi,2,i)));
+            if (d > eps7) {
+                direc[dimen++] = i;
+                nooff[i] = 1;
+                for (int j = 0; j < 3; j++) M3(mat_a,j,i) = M3(vi,j,i);
+            } else {
+                return DGPU_ERR_ZERO_INC;              /* ier_num = -132 */
+            }
+        }
+    }
+
+    if (dimen == 0) {
+        M3(off,0,0) = 1; M3(off,1,1) = 1; M3(off,2,2) = 1;
+        for (int i = 0; i < 9; i++) mat_a[i] = off[i];
+    } else if (dimen == 1) {
+        int j = direc[0], j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+        /* axis-parallel rows (:103-169) read vi(:,1) and set everything */
+        if (M3(vi,1,j) == 0 && M3(vi,2,j) == 0) {            /* parallel a* */
+            if (M3(vi,0,0) == 0) return DGPU_ERR_ARG;
+            qreal r = M3(eck,0,0) / M3(vi,0,0);
+            lmn[0] = (int32_t)q_nint(r);
+            if (q_abs(r - (qreal)q_nint(r)) > tiny) { lmn[3] = 1; M3(off,0,0) = r - (qreal)q_nint(r); }
+            lmn[4] = 1; lmn[5] = 1;
+            M3(off,1,1) = M3(eck,1,0);
+            M3(off,2,2) = M3(eck,2,0);
+            need_work = 0;
+        } else if (M3(vi,0,j) == 0 && M3(vi,2,j) == 0) {     /* parallel b* */
+            if (M3(vi,1,0) == 0) return DGPU_ERR_ARG;
+            qreal r = M3(eck,1,0) / M3(vi,1,0);
+            lmn[0] = (int32_t)q_nint(r);
+            if (q_abs(r - (qreal)q_nint(r)) > tiny) { lmn[3] = 1; M3(off,1,0) = r - (qreal)q_nint(r); }
+            lmn[4] = 1; lmn[5] = 1;
+            M3(off,0,1) = M3(eck,0,0);
+            M3(off,2,2) = M3(eck,2,0);
+            need_work = 0;
+        } else if (M3(vi,0,j) == 0 && M3(vi,1,j) == 0) {     /* parallel c* */
+            if (M3(vi,2,0) == 0) return DGPU_ERR_ARG;
+            qreal r = M3(eck,2,0) / M3(vi,2,0);
+            lmn[0] = (int32_t)q_nint(r);
+            if (q_abs(r - (qreal)q_nint(r)) > tiny) { lmn[3] = 1; M3(off,2,0) = r - (qreal)q_nint(r); }
+            lmn[4] = 1; lmn[5] = 1;
+            M3(off,0,1) = M3(eck,0,0);
+            M3(off,1,2) = M3(eck,1,0);
+            need_work = 0;
+        } else {
+            const qreal s001 = (qreal)0.001f;          /* 0.001 default real */
+            M3(off,0,j2) = M3(eck,1,0)*M3(vi,2,j) - M3(eck,2,0)*M3(vi,1,j);
+            M3(off,1,j2) = M3(eck,2,0)*M3(vi,0,j) - M3(eck,0,0)*M3(vi,2,j);
+            M3(off,2,j2) = M3(eck,0,0)*M3(vi,1,j) - M3(eck,1,0)*M3(vi,0,j);
+            qreal d = q_sqrt(q_abs(M3(off,0,j2)*M3(off,0,j2) + M3(off,1,j2)*M3(off,1,j2)
+                                   + M3(off,2,j2)*M3(off,2,j2)));
+            if (d > eps7) {
+                for (int k = 0; k < 3; k++) M3(off,k,j2) = M3(off,k,j2) * s001 / d;
+                M3(off,0,j1) = M3(off,1,j2)*M3(vi,2,j) - M3(off,2,j2)*M3(vi,1,j);
+                M3(off,1,j1) = M3(off,2,j2)*M3(vi,0,j) - M3(off,0,j2)*M3(vi,2,j);
+                M3(off,2,j1) = M3(off,0,j2)*M3(vi,1,j) - M3(off,1,j2)*M3(vi,0,j);
+                d = q_sqrt(q_abs(M3(off,0,j1)*M3(off,0,j1) + M3(off,1,j1)*M3(off,1,j1)
+                                 + M3(off,2,j1)*M3(off,2,j1)));
+                if (d > eps7) {
+                    for (int k = 0; k < 3; k++) M3(off,k,j1) = M3(off,k,j1) * s001 / d;
+                } else {
+                    for (int k = 0; k < 3; k++) M3(off,k,j1) = ranv[k];
+                }
+            } else {
+                for (int k = 0; k < 3; k++) { M3(off,k,j1) = ranv[k]; M3(off,k,j2) = ranv[3 + k]; }
+            }
+            for (int k = 0; k < 3; k++) { M3(mat_a,k,j1) = M3(off,k,j1); M3(mat_a,k,j2) = M3(off,k,j2); }
+        }
+    } else if (dimen == 2) {
+        int j = direc[0], j1 = direc[1], j2 = 3 - j - j1;
+        M3(off,0,j2) = M3(vi,1,j)*M3(vi,2,j1) - M3(vi,2,j)*M3(vi,1,j1);
+        M3(off,1,j2) = M3(vi,2,j)*M3(vi,0,j1) - M3(vi,0,j)*M3(vi,2,j1);
+        M3(off,2,j2) = M3(vi,0,j)*M3(vi,1,j1) - M3(vi,1,j)*M3(vi,0,j1);
+        qreal d = q_sqrt(M3(off,0,j2)*M3(off,0,j2) + M3(off,1,j2)*M3(off,1,j2)
+                         + M3(off,2,j2)*M3(off,2,j2));
+        for (int k = 0; k < 3; k++) M3(off,k,j2) = M3(off,k,j2) * (qreal)0.001 / d;
+        for (int k = 0; k < 3; k++) M3(mat_a,k,j2) = M3(off,k,j2);
+    }
+
+    if (need_work) {
+        if (q_matinv3(mat_a, mat_i) != 0) return DGPU_ERR_ARG;
+        for (int a = 0; a < 3; a++) {
+            vec_r[a] = 0;
+            for (int b = 0; b < 3; b++) vec_r[a] += M3(mat_i,a,b) * M3(eck,b,0);
+        }
+        for (int a = 0; a < 3; a++)
+            if (q_abs(vec_r[a] - (qreal)q_nint(vec_r[a])) < tiny) vec_r[a] = (qreal)q_nint(vec_r[a]);
+        qreal fr[3];
+        for (int a = 0; a < 3; a++) { lmn[a] = (int32_t)q_nint(vec_r[a]); fr[a] = vec_r[a] - (qreal)q_nint(vec_r[a]); }
+        for (int a = 0; a < 3; a++) {
+            vec_t[a] = 0;
+            for (int b = 0; b < 3; b++) vec_t[a] += M3(mat_a,a,b) * fr[b];
+        }
+        for (int j = 0; j < 3; j++) {
+            if (!nooff[j]) {
+                lmn[j + 3] = lmn[j];
+                lmn[j] = 0;
+            } else {
+                M3(off,j,j) = M3(off,j,j) + vec_t[j];
+                lmn[3 + j] = 1;
+                if (q_abs(M3(off,j,j)) < tiny) { M3(off,j,j) = 0; lmn[3 + j] = 0; }
+            }
+        }
+    }
+    for (int i = 0; i < 9; i++) off_out[i] = (double)off[i];
+    return DGPU_OK;
+}
+
+/* four_cexpt, fourier_sup.f90:2602-2632: cex(k) = exp(2 pi i k / 2^16) */
+void oc_cexpt(double *cex)
+{
+    const double zpi = 2.0 * 3.1415926535897932384626433832795028841971693993751;
+    for (int i = 0; i < DGPU_I2PI; i++) {
+        double xarg = zpi * ((double)i * 1.0 / (double)DGPU_I2PI);
+        cex[2 * i] = cos(xarg);
+        cex[2 * i + 1] = sin(xarg);
+    }
+}
+
+/* four_stltab, fourier_sup.f90:2637-2687.  h is rounded to default REAL
+ * (single precision) before the metric, as REAL() does there; the metric
+ * is skalpro = dot_product(h, matmul(rten,h)) (discus/prog/metric.f90:90-105). */
+int oc_stltab(const double eck[12], const double vi[9], const int32_t num[3],
+              const double rten[9], int32_t *istl)
+{
+    int err = 0;
+    for (int l = 0; l < num[2]; l++)
+        for (int j = 0; j < num[1]; j++)
+            for (int i = 0; i < num[0]; i++) {
+                double h[3], t[3];
+                for (int k = 0; k < 3; k++)
+                    h[k] = (double)(float)(eck[k] + vi[k] * (double)i + vi[3 + k] * (double)j
+                                           + vi[6 + k] * (double)l);
+                for (int a = 0; a < 3; a++)
+                    t[a] = M3(rten,a,0) * h[0] + M3(rten,a,1) * h[1] + M3(rten,a,2) * h[2];
+                double q2 = (h[0] * t[0] + h[1] * t[1] + h[2] * t[2]) / 4.0;
+                long v = lround(sqrt(q2) * 1000.0);
+                istl[i + (int64_t)num[0] * (j + (int64_t)num[1] * l)] = (int32_t)v;
+                if (v > CFPKT) err = DGPU_ERR_STL_RANGE;
+            }
+    return err;
+}
+
+/* form, fourier_sup.f90:2947-2971 */
+static double oc_form(const double *scat, int t, int lxray, double h2, int power)
+{
+    double f = scat[11 * t + 0];
+    if (lxray)
+        for (int i = 1; i <= power; i++)
+            f = f + scat[11 * t + 2 * i - 1] * exp(-scat[11 * t + 2 * i] * h2);
+    return f;
+}
+
+/* cfact for one type at sin(theta)/lambda squared q2, four_formtab body
+ * (fourier_sup.f90:2716-2736) */
+static void oc_cfact_at(const dgpu_crystal *cr, const dgpu_opts *op, int t, double q2,
+                        double *re, double *im)
+{
+    double sf = oc_form(cr->scat, t, op->lxray, q2, op->power);
+    double sfp = 0, sfpp = 0, sb;
+    if (op->ano) { sfp = cr->delfr ? cr->delfr[t] : 0; sfpp = cr->delfi ? cr->delfi[t] : 0; }
+    if (op->ldbw) sb = exp(-(cr->dw[t] * q2)) * cr->occ[t];
+    else sb = 1.0 * cr->occ[t];
+    *re = sb * (sf + sfp);
+    *im = sb * sfpp;
+}
+
+/* four_formtab, fourier_sup.f90:2691-2743: cfact(0:CFPKT, 1:nscat) */
+void oc_formtab(const dgpu_crystal *cr, const dgpu_opts *op, double *cfact)
+{
+    for (int t = 1; t <= cr->nscat; t++)
+        for (int iq = 0; iq <= CFPKT; iq++) {
+            double s = (double)iq * DGPU_CFINC;
+            double q2 = s * s;
+            double *c = cfact + 2 * ((int64_t)(t - 1) * NTAB + iq);
+            oc_cfact_at(cr, op, t, q2, &c[0], &c[1]);
+        }
+}
+
+/* Per-atom increments, four_strucf_OMP_mod.f90:135-149.
+ * INT truncates toward zero, NINT rounds half away from zero. */
+static int64_t oc_inc1(double x)
+{
+    double fr = x - (double)(int64_t)x + 0.0;
+    return (int64_t)lround(4194304.0 * fr);          /* 64 * I2PI = 2^22 */
+}
+void oc_increments(const double *xat, int64_t nxat, const double uin[3],
+                   const double vin[3], const double win[3], const double off[9],
+                   int64_t *inc6)
+{
+    for (int64_t k = 0; k < nxat; k++) {
+        double x0 = xat[k], x1 = xat[nxat + k], x2 = xat[2 * nxat + k];
+        double xu = uin[0] * x0 + uin[1] * x1 + uin[2] * x2;
+        double xv = vin[0] * x0 + vin[1] * x1 + vin[2] * x2;
+        double xw = win[0] * x0 + win[1] * x1 + win[2] * x2;
+        double ou = off[0] * x0 + off[1] * x1 + off[2] * x2;   /* off_shift(:,1) */
+        double ov = off[3] * x0 + off[4] * x1 + off[5] * x2;
+        double ow = off[6] * x0 + off[7] * x1 + off[8] * x2;
+        inc6[0 * nxat + k] = oc_inc1(xu);
+        inc6[1 * nxat + k] = oc_inc1(xv);
+        inc6[2 * nxat + k] = oc_inc1(xw);
+        inc6[3 * nxat + k] = oc_inc1(ou);
+        inc6[4 * nxat + k] = oc_inc1(ov);
+        inc6[5 * nxat + k] = oc_inc1(ow);
+    }
+}
+
+/* four_strucf_omp, four_strucf_OMP_mod.f90:72-188 (without the form factor):
+ * tcsf(j,i,h) = sum_k w_k cex(IAND(ISHFT(iarg,-6),MASK)) over rows
+ * j in [row_lo,row_hi) of fnum(1); atoms summed in order for each point.   */
+void oc_strucf_ref(const double *xat, const float *w, int64_t nxat,
+                   const double uin[3], const double vin[3], const double win[3],
+                   const double off[9], const int32_t lmn[6], const int32_t num[3],
+                   const int32_t fnum[3], const double *cex, int32_t row_lo,
+                   int32_t row_hi, int nthreads, double *tcsf)
+{
+    int64_t *inc = (int64_t *)malloc(sizeof(int64_t) * 6 * (nxat > 0 ? nxat : 1));
+    oc_increments(xat, nxat, uin, vin, win, off, inc);
+    const int64_t *iu = inc, *iv = inc + nxat, *iw = inc + 2 * nxat;
+    const int64_t *ju = inc + 3 * nxat, *jv = inc + 4 * nxat, *jw = inc + 5 * nxat;
+    int64_t n1 = num[0], n12 = (int64_t)num[0] * num[1];
+    int32_t f2 = fnum[1], f3 = fnum[2];
+    (void)nthreads;
+#pragma omp parallel num_threads(nthreads > 0 ? nthreads : 1)
+    {
+        double *part = (double *)malloc(sizeof(double) * 2 * (size_t)f2 * f3);
+#pragma omp for schedule(static)
+        for (int32_t j = row_lo; j < row_hi; j++) {
+            memset(part, 0, sizeof(double) * 2 * (size_t)f2 * f3);
+            for (int64_t k = 0; k < nxat; k++) {
+                int64_t iarg0 = (int64_t)lmn[0] * iu[k] + (int64_t)lmn[1] * iv[k]
+                              + (int64_t)lmn[2] * iw[k] + (int64_t)lmn[3] * ju[k]
+                              + (int64_t)lmn[4] * jv[k] + (int64_t)lmn[5] * jw[k]
+                              + (int64_t)j * iu[k];
+                double wk = w ? (double)w[k] : 1.0;
+                for (int32_t i = 0; i < f2; i++) {
+                    int64_t iarg = iarg0 + iv[k] * i;
+                    double *p = part + 2 * (size_t)i;
+                    for (int32_t h = 0; h < f3; h++) {
+                        int64_t idx = (int64_t)(((uint64_t)iarg >> 6) & 0xFFFF);
+                        if (w) {
+                            p[2 * (size_t)h * f2]     += wk * cex[2 * idx];
+                            p[2 * (size_t)h * f2 + 1] += wk * cex[2 * idx + 1];
+                        } else {
+                            p[2 * (size_t)h * f2]     += cex[2 * idx];
+                            p[2 * (size_t)h * f2 + 1] += cex[2 * idx + 1];
+                        }
+                        iarg += iw[k];
+                    }
+                }
+            }
+            for (int32_t i = 0; i < f2; i++)
+                for (int32_t h = 0; h < f3; h++) {
+                    int64_t o = 2 * (j + n1 * i + n12 * h);
+                    tcsf[o]     += part[2 * ((size_t)h * f2 + i)];
+                    tcsf[o + 1] += part[2 * ((size_t)h * f2 + i) + 1];
+                }
+        }
+        free(part);
+    }
+    free(inc);
+}
+
+/* four_strucf + tcsf_form_iso as one call (four_strucf_OMP_mod.f90:72-188,
+ * fourier_form.f90:147-177). tcsf is zeroed over num first. */
+int oc_four_strucf(const double *xat, int64_t nxat, const double uin[3],
+                   const double vin[3], const double win[3], const double off[9],
+                   const int32_t lmn[6], const int32_t num[3], const int32_t fnum[3],
+                   const double *cfact, const int32_t *istl, double *tcsf)
+{
+    int64_t np = (int64_t)num[0] * num[1] * num[2];
+    double *cex = (double *)malloc(sizeof(double) * 2 * DGPU_I2PI);
+    oc_cexpt(cex);
+    memset(tcsf, 0, sizeof(double) * 2 * np);
+    oc_strucf_ref(xat, NULL, nxat, uin, vin, win, off, lmn, num, fnum, cex, 0, fnum[0], 1, tcsf);
+    if (cfact) {
+        for (int32_t h = 0; h < fnum[2]; h++)
+            for (int32_t j = 0; j < fnum[1]; j++)
+                for (int32_t i = 0; i < fnum[0]; i++) {
+                    int64_t p = i + (int64_t)num[0] * (j + (int64_t)num[1] * h);
+                    int32_t q = istl[p];
+                    double ar = tcsf[2 * p], ai = tcsf[2 * p + 1];
+                    double br = cfact[2 * q], bi = cfact[2 * q + 1];
+                    tcsf[2 * p] = ar * br - ai * bi;
+                    tcsf[2 * p + 1] = ar * bi + ai * br;
+                }
+    }
+    free(cex);
+    return DGPU_OK;
+}
+
+/* ---------------------------------------------------------------------- */
+/* EXACT64: h.r mod 1 with error-free products (fma) and FP64 sin/cos.     */
+static double oc_frac_dot(const double h[3], double x0, double x1, double x2)
+{
+    double p0 = h[0] * x0, e0 = fma(h[0], x0, -p0);
+    double p1 = h[1] * x1, e1 = fma(h[1], x1, -p1);
+    double p2 = h[2] * x2, e2 = fma(h[2], x2, -p2);
+    double s = p0 + p1, z = s - p0, es = (p0 - (s - z)) + (p1 - z);   /* TwoSum */
+    double t = s + p2;  z = t - s;  double et = (s - (t - z)) + (p2 - z);
+    double hi = t - nearbyint(t);
+    return hi + (es + et + e0 + e1 + e2);
+}
+
+static void oc_hvec(const double eck[12], const double vi[9], int32_t i, int32_t j,
+                    int32_t l, double h[3])
+{
+    for (int k = 0; k < 3; k++)
+        h[k] = eck[k] + vi[k] * (double)i + vi[3 + k] * (double)j + vi[6 + k] * (double)l;
+}
+
+/* sum_k w_k exp(2 pi i h.x_k) on the points of fnum, exact FP64 phase */
+static void oc_strucf_exact(const double *xat, const float *w, int64_t nxat,
+                            const double eck[12], const double vi[9],
+                            const int32_t num[3], const int32_t fnum[3], int nthreads,
+                            double *tcsf)
+{
+    const double zpi = 6.283185307179586476925286766559;
+    int64_t nf = (int64_t)fnum[0] * fnum[1] * fnum[2];
+    (void)nthreads;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads > 0 ? nthreads : 1)
+    for (int64_t p = 0; p < nf; p++) {
+        int32_t i = (int32_t)(p % fnum[0]);
+        int32_t j = (int32_t)((p / fnum[0]) % fnum[1]);
+        int32_t l = (int32_t)(p / ((int64_t)fnum[0] * fnum[1]));
+        double h[3];
+        oc_hvec(eck, vi, i, j, l, h);
+        double sr = 0, si = 0;
+        for (int64_t k = 0; k < nxat; k++) {
+            double ph = oc_frac_dot(h, xat[k], xat[nxat + k], xat[2 * nxat + k]);
+            double wk = w ? (double)w[k] : 1.0;
+            sr += wk * cos(zpi * ph);
+            si += wk * sin(zpi * ph);
+        }
+        int64_t o = i + (int64_t)num[0] * (j + (int64_t)num[1] * l);
+        tcsf[2 * o] += sr;
+        tcsf[2 * o + 1] += si;
+    }
+}
+
+/* ---------------------------------------------------------------------- */
+/* Friedel reduction, fourier_sup.f90:3645-3722 */
+static int oc_test_friedel(const dgpu_grid *g, const dgpu_opts *op, int32_t fnum[3])
+{
+    const double EPS = (double)1.0e-6f;
+    for (int k = 0; k < 3; k++) fnum[k] = g->inc[k];
+    if (!op->friedel || op->ano) return 0;
+    double rut[3], point[3];
+    for (int k = 0; k < 3; k++) {
+        rut[k] = g->eck[k] + g->vi[k] * (fnum[0] - 1) + g->vi[3 + k] * (fnum[1] - 1)
+               + g->vi[6 + k] * (fnum[2] - 1);
+        point[k] = g->eck[k] + rut[k];
+    }
+    int all_odd = (fnum[0] % 2) && (fnum[1] % 2) && (fnum[2] % 2);
+    if (!all_odd) return 0;
+    if (!(fabs(point[0]) < EPS && fabs(point[2]) < EPS && fabs(point[1]) < EPS)) return 0;
+    if (fnum[0] > 1) { fnum[0] = (fnum[0] + 1) / 2; return 1; }
+    if (fnum[1] > 1) { fnum[1] = (fnum[1] + 1) / 2; return 2; }
+    if (fnum[2] > 1) { fnum[2] = (fnum[2] + 1) / 2; return 3; }
+    return 0;
+}
+
+/* four_apply_friedel, fourier_sup.f90:3726-3757, in its sequential order */
+static void oc_apply_friedel(const int32_t num[3], const int32_t fnum[3], double *acsf,
+                             double *csf, double *dsi)
+{
+    for (int32_t i = 0; i < fnum[0]; i++)
+        for (int32_t j = 0; j < fnum[1]; j++)
+            for (int32_t k = 0; k < fnum[2]; k++) {
+                int64_t s = i + (int64_t)num[0] * (j + (int64_t)num[1] * k);
+                int64_t m = (num[0] - 1 - i) + (int64_t)num[0] * ((num[1] - 1 - j)
+                          + (int64_t)num[1] * (num[2] - 1 - k));
+                if (acsf) { acsf[2 * m] = acsf[2 * s]; acsf[2 * m + 1] = -acsf[2 * s + 1]; }
+                csf[2 * m] = csf[2 * s]; csf[2 * m + 1] = -csf[2 * s + 1];
+                dsi[m] = dsi[s];
+            }
+}
+
+/* four_qinfo, fourier_sup.f90:2859-2942 */
+static void oc_qinfo(const dgpu_grid *g, const double *dsi, double res[7])
+{
+    double bmax = -9999.0, bmin = (double)1e19f, dmax = -9999.0, dmin = (double)1e19f;
+    double dsum = 0, dsum2 = 0;
+    int64_t nd = 0;
+    const int32_t *num = g->inc;
+    for (int32_t l = 0; l < num[2]; l++)
+        for (int32_t j = 0; j < num[1]; j++)
+            for (int32_t i = 0; i < num[0]; i++) {
+                int bragg = 1;
+                for (int k = 0; k < 3; k++) {
+                    double h = g->eck[k] + g->vi[k] * (double)(float)i
+                             + g->vi[3 + k] * (double)(float)j + g->vi[6 + k] * (double)(float)l;
+                    bragg = bragg && (fmod(h, 1.0) == 0.0);
+                }
+                double v = dsi[i + (int64_t)num[0] * (j + (int64_t)num[1] * l)];
+                if (bragg) { if (v > bmax) bmax = v; if (v < bmin) bmin = v; }
+                else {
+                    if (v > dmax) dmax = v;
+                    if (v < dmin) dmin = v;
+                    dsum += v; dsum2 += v * v; nd++;
+                }
+            }
+    double ave = 0, sig = 0;
+    if (nd) { ave = dsum / (double)nd; sig = sqrt(dsum2 / (double)nd - ave * ave); }
+    res[0] = 6; res[1] = dmin; res[2] = dmax; res[3] = ave; res[4] = sig;
+    res[5] = bmin; res[6] = bmax;
+}
+
+/* Gather atoms of one type (four_getatm LOT_OFF, fourier_sup.f90:1839-1848). */
+static int64_t oc_getatm(const dgpu_crystal *cr, int t, double *xat, float *w)
+{
+    int64_t n = 0;
+    for (int64_t i = 0; i < cr->natoms; i++)
+        if (cr->iscat[i] == t) n++;
+    int64_t m = 0;
+    for (int64_t i = 0; i < cr->natoms; i++)
+        if (cr->iscat[i] == t) {
+            for (int k = 0; k < 3; k++) xat[k * n + m] = cr->pos[3 * i + k];
+            if (w) w[m] = cr->atom_occ ? cr->atom_occ[i] : 1.0f;
+            m++;
+        }
+    return n;
+}
+
+/* Multiply by the form factor on fnum (tcsf_form_iso, fourier_form.f90:147-177),
+ * by table (istl) or at the exact sin(theta)/lambda. */
+static void oc_apply_form(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,
+                          int t, const double *cfact, const int32_t *istl,
+                          const int32_t fnum[3], double *tcsf)
+{
+    const int32_t *num = g->inc;
+    for (int32_t l = 0; l < fnum[2]; l++)
+        for (int32_t j = 0; j < fnum[1]; j++)
+            for (int32_t i = 0; i < fnum[0]; i++) {
+                int64_t p = i + (int64_t)num[0] * (j + (int64_t)num[1] * l);
+                double br, bi;
+                if (op->form == DGPU_FORM_TABLE) {
+                    const double *c = cfact + 2 * ((int64_t)(t - 1) * NTAB + istl[p]);
+                    br = c[0]; bi = c[1];
+                } else {
+                    double h[3], tt[3];
+                    oc_hvec(g->eck, g->vi, i, j, l, h);
+                    for (int a = 0; a < 3; a++)
+                        tt[a] = M3(cr->rten,a,0) * h[0] + M3(cr->rten,a,1) * h[1] + M3(cr->rten,a,2) * h[2];
+                    double q2 = (h[0] * tt[0] + h[1] * tt[1] + h[2] * tt[2]) / 4.0;
+                    oc_cfact_at(cr, op, t, q2, &br, &bi);
+                }
+                double ar = tcsf[2 * p], ai = tcsf[2 * p + 1];
+                tcsf[2 * p] = ar * br - ai * bi;
+                tcsf[2 * p + 1] = ar * bi + ai * br;
+            }
+}
+
+/* One type's (or the lattice's) sum into tcsf (zeroed over num first). */
+static void oc_strucf_mode(const dgpu_grid *g, const dgpu_opts *op, const double *xat,
+                           const float *w, int64_t nxat, const int32_t lmn[6],
+                           const double off[9], const int32_t fnum[3], const double *cex,
+                           int nthreads, double *tcsf)
+{
+    const int32_t *num = g->inc;
+    int64_t np = (int64_t)num[0] * num[1] * num[2];
+    memset(tcsf, 0, sizeof(double) * 2 * np);
+    if (op->phase == DGPU_PHASE_REF22)
+        oc_strucf_ref(xat, w, nxat, g->vi, g->vi + 3, g->vi + 6, off, lmn, num, fnum, cex,
+                      0, fnum[0], nthreads, tcsf);
+    else
+        oc_strucf_exact(xat, w, nxat, g->eck, g->vi, num, fnum, nthreads, tcsf);
+}
+
+/* four_run for LOT_OFF and isotropic ADPs, fourier_sup.f90:11-323 */
+int oc_four_run(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,
+                double *csf, double *acsf_out, double *dsi, dgpu_info *info, int nthreads)
+{
+    const int32_t *num = g->inc;
+    int64_t np = (int64_t)num[0] * num[1] * num[2];
+    int32_t lmn[6], fnum[3];
+    double off[9];
+    int rc, warn = 0;
+    if (cr->natoms < 1) return DGPU_ERR_NO_ATOMS;
+
+    memset(csf, 0, sizeof(double) * 2 * np);
+    memset(dsi, 0, sizeof(double) * np);
+    double *acsf = (double *)calloc(2 * np, sizeof(double));
+    double *tcsf = (double *)malloc(sizeof(double) * 2 * np);
+    int32_t *istl = (int32_t *)malloc(sizeof(int32_t) * np);
+    double *cfact = (double *)malloc(sizeof(double) * 2 * NTAB * (cr->nscat > 0 ? cr->nscat : 1));
+    double *cex = (double *)malloc(sizeof(double) * 2 * DGPU_I2PI);
+    double *xat = (double *)malloc(sizeof(double) * 3 * cr->natoms);
+    float *w = (float *)malloc(sizeof(float) * cr->natoms);
+
+    rc = oc_fourier_lmn(g->eck, g->vi, g->inc, lmn, off);
+    if (rc) goto done;
+    oc_cexpt(cex);
+    rc = oc_stltab(g->eck, g->vi, num, cr->rten, istl);
+    if (rc && op->form == DGPU_FORM_TABLE) goto done;
+    rc = 0;
+    oc_formtab(cr, op, cfact);
+    int idim = oc_test_friedel(g, op, fnum);
+
+    /* four_aver, fourier_sup.f90:1194-1357 */
+    int32_t ncell = 0;
+    if (op->fave != 0.0) {
+        int64_t ncells = (int64_t)cr->icc[0] * cr->icc[1] * cr->icc[2];
+        for (int t = 1; t <= cr->nscat; t++) {
+            int64_t nx = 0;
+            for (int32_t ii = 0; ii < cr->icc[0]; ii++)
+                for (int32_t jj = 0; jj < cr->icc[1]; jj++)
+                    for (int32_t kk = 0; kk < cr->icc[2]; kk++) {
+                        int64_t c = ii + (int64_t)cr->icc[0] * (jj + (int64_t)cr->icc[1] * kk);
+                        int sel = op->fave >= 1.0 ? 1 : (op->aver_cells ? op->aver_cells[c] != 0 : 0);
+                        if (!sel) continue;
+                        ncell++;
+                        for (int32_t is = 0; is < cr->ncatoms; is++) {
+                            int64_t ia = c * cr->ncatoms + is;              /* celltoindex */
+                            if (ia >= cr->natoms || cr->iscat[ia] != t) continue;
+                            nx++;
+                        }
+                    }
+            double *xa = (double *)malloc(sizeof(double) * 3 * (nx > 0 ? nx : 1));
+            float *wa = (float *)malloc(sizeof(float) * (nx > 0 ? nx : 1));
+            int64_t m = 0;
+            for (int32_t ii = 0; ii < cr->icc[0]; ii++)
+                for (int32_t jj = 0; jj < cr->icc[1]; jj++)
+                    for (int32_t kk = 0; kk < cr->icc[2]; kk++) {
+                        int64_t c = ii + (int64_t)cr->icc[0] * (jj + (int64_t)cr->icc[1] * kk);
+                        int sel = op->fave >= 1.0 ? 1 : (op->aver_cells ? op->aver_cells[c] != 0 : 0);
+                        if (!sel) continue;
+                        int32_t icell[3] = {ii, jj, kk};
+                        for (int32_t is = 0; is < cr->ncatoms; is++) {
+                            int64_t ia = c * cr->ncatoms + is;
+                            if (ia >= cr->natoms || cr->iscat[ia] != t) continue;
+                            for (int k = 0; k < 3; k++)
+                                xa[k * nx + m] = cr->pos[3 * ia + k] - (double)icell[k] - cr->dim0[k];
+                            wa[m] = cr->atom_occ ? cr->atom_occ[ia] : 1.0f;
+                            m++;
+                        }
+                    }
+            oc_strucf_mode(g, op, xa, cr->atom_occ ? wa : NULL, nx, lmn, off, fnum, cex, nthreads, tcsf);
+            oc_apply_form(cr, g, op, t, cfact, istl, fnum, tcsf);
+            for (int64_t p = 0; p < 2 * np; p++) acsf[p] += tcsf[p];
+            free(xa); free(wa);
+            (void)ncells;
+        }
+        ncell = ncell / cr->nscat;
+        /* four_getav LOT_OFF (fourier_sup.f90:2457-2466), summed on the full num */
+        int64_t nl = (int64_t)cr->icc[0] * cr->icc[1] * cr->icc[2];
+        double *xl = (double *)malloc(sizeof(double) * 3 * nl);
+        int64_t m = 0;
+        for (int32_t ii = 0; ii < cr->icc[0]; ii++)
+            for (int32_t jj = 0; jj < cr->icc[1]; jj++)
+                for (int32_t kk = 0; kk < cr->icc[2]; kk++) {
+                    xl[m] = (double)ii + cr->dim0[0];
+                    xl[nl + m] = (double)jj + cr->dim0[1];
+                    xl[2 * nl + m] = (double)kk + cr->dim0[2];
+                    m++;
+                }
+        oc_strucf_mode(g, op, xl, NULL, nl, lmn, off, num, cex, nthreads, tcsf);
+        free(xl);
+        double norm = 0.0;
+        if (ncell > 0) norm = 1.0 / ncell; else warn = DGPU_WARN_NO_CELL;
+        for (int64_t p = 0; p < np; p++) {
+            double ar = acsf[2 * p], ai = acsf[2 * p + 1];
+            double br = tcsf[2 * p], bi = tcsf[2 * p + 1];
+            double cr_ = ar * br - ai * bi, ci = ar * bi + ai * br;
+            acsf[2 * p] = cr_ * norm;
+            acsf[2 * p + 1] = ci * norm;
+        }
+    }
+
+    /* loop over types (fourier_sup.f90:224-244) */
+    for (int t = 1; t <= cr->nscat; t++) {
+        int64_t nx = oc_getatm(cr, t, xat, w);
+        if (nx <= 0) continue;
+        oc_strucf_mode(g, op, xat, cr->atom_occ ? w : NULL, nx, lmn, off, fnum, cex, nthreads, tcsf);
+        oc_apply_form(cr, g, op, t, cfact, istl, fnum, tcsf);
+        for (int64_t p = 0; p < 2 * np; p++) csf[p] += tcsf[p];
+        if (op->cancel && *op->cancel) { rc = DGPU_ERR_CANCELLED; goto done; }
+    }
+    for (int64_t p = 0; p < np; p++) {
+        csf[2 * p] -= acsf[2 * p];
+        csf[2 * p + 1] -= acsf[2 * p + 1];
+        dsi[p] = dsi[p] + (csf[2 * p] * csf[2 * p] + csf[2 * p + 1] * csf[2 * p + 1]);
+    }
+    if (idim) oc_apply_friedel(num, fnum, acsf, csf, dsi);
+    {
+        double sq = sqrt(op->diff_scale);
+        for (int64_t p = 0; p < 2 * np; p++) csf[p] *= sq;
+        for (int64_t p = 0; p < np; p++) dsi[p] *= op->diff_scale;
+    }
+    if (info) {
+        memset(info, 0, sizeof(*info));
+        for (int k = 0; k < 3; k++) info->fnum[k] = fnum[k];
+        info->friedel_dim = idim;
+        for (int k = 0; k < 6; k++) info->lmn[k] = lmn[k];
+        for (int k = 0; k < 9; k++) info->off_shift[k] = off[k];
+        info->ncell = ncell;
+        int64_t nat = 0;
+        for (int64_t i = 0; i < cr->natoms; i++) if (cr->iscat[i] >= 1 && cr->iscat[i] <= cr->nscat) nat++;
+        info->pairs = nat * np;
+        oc_qinfo(g, dsi, info->res);
+    }
+    if (acsf_out) memcpy(acsf_out, acsf, sizeof(double) * 2 * np);
+    rc = warn;
+done:
+    free(acsf); free(tcsf); free(istl); free(cfact); free(cex); free(xat); free(w);
+    return rc;
+}
+
+/* ---------------------------------------------------------------------- */
+/* chi^2 = sum_h wt(h) (I(h) - It(h))^2 and its gradient, exact FP64, full
+ * grid, fave = 0, no Friedel reduction.  I = diff_scale |F|^2 with
+ * F = sum_t cf_t(h) sum_j w_j exp(2 pi i h.r_j).                            */
+int oc_chi2_grad(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,
+                 const double *it, const double *wt, double *chi2, double *grad_pos,
+                 double *grad_occ, int nthreads)
+{
+    const double zpi = 6.283185307179586476925286766559;
+    const int32_t *num = g->inc;
+    int64_t np = (int64_t)num[0] * num[1] * num[2];
+    int ns = cr->nscat;
+    double *cf = (double *)malloc(sizeof(double) * 2 * np * (ns > 0 ? ns : 1));
+    double *F = (double *)calloc(2 * np, sizeof(double));
+    double *Q = (double *)malloc(sizeof(double) * 2 * np * (ns > 0 ? ns : 1));
+    double *H = (double *)malloc(sizeof(double) * 3 * np);
+    int32_t *istl = (int32_t *)malloc(sizeof(int32_t) * np);
+    double *cfact = (double *)malloc(sizeof(double) * 2 * NTAB * (ns > 0 ? ns : 1));
+    (void)nthreads;
+    oc_stltab(g->eck, g->vi, num, cr->rten, istl);
+    oc_formtab(cr, op, cfact);
+    for (int32_t l = 0; l < num[2]; l++)
+        for (int32_t j = 0; j < num[1]; j++)
+            for (int32_t i = 0; i < num[0]; i++) {
+                int64_t p = i + (int64_t)num[0] * (j + (int64_t)num[1] * l);
+                double h[3], tt[3];
+                oc_hvec(g->eck, g->vi, i, j, l, h);
+                for (int k = 0; k < 3; k++) H[3 * p + k] = h[k];
+                for (int a = 0; a < 3; a++)
+                    tt[a] = M3(cr->rten,a,0) * h[0] + M3(cr->rten,a,1) * h[1] + M3(cr->rten,a,2) * h[2];
+                double q2 = (h[0] * tt[0] + h[1] * tt[1] + h[2] * tt[2]) / 4.0;
+                for (int t = 1; t <= ns; t++) {
+                    double br, bi;
+                    if (op->form == DGPU_FORM_TABLE) {
+                        const double *c = cfact + 2 * ((int64_t)(t - 1) * NTAB + istl[p]);
+                        br = c[0]; bi = c[1];
+                    } else {
+                        oc_cfact_at(cr, op, t, q2, &br, &bi);
+                    }
+                    cf[2 * ((int64_t)(t - 1) * np + p)] = br;
+                    cf[2 * ((int64_t)(t - 1) * np + p) + 1] = bi;
+                }
+            }
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads > 0 ? nthreads : 1)
+    for (int64_t p = 0; p < np; p++) {
+        double fr = 0, fi = 0;
+        for (int64_t a = 0; a < cr->natoms; a++) {
+            int t = cr->iscat[a];
+            if (t < 1 || t > ns) continue;
+            double ph = oc_frac_dot(H + 3 * p, cr->pos[3 * a], cr->pos[3 * a + 1], cr->pos[3 * a + 2]);
+            double wa = cr->atom_occ ? (double)cr->atom_occ[a] : 1.0;
+            double c = cos(zpi * ph) * wa, s = sin(zpi * ph) * wa;
+            double br = cf[2 * ((int64_t)(t - 1) * np + p)], bi = cf[2 * ((int64_t)(t - 1) * np + p) + 1];
+            fr += br * c - bi * s;
+            fi += br * s + bi * c;
+        }
+        F[2 * p] = fr; F[2 * p + 1] = fi;
+    }
+    double x2 = 0;
+    for (int64_t p = 0; p < np; p++) {
+        double I = op->diff_scale * (F[2 * p] * F[2 * p] + F[2 * p + 1] * F[2 * p + 1]);
+        double d = I - it[p];
+        double wp = wt ? wt[p] : 1.0;
+        x2 += wp * d * d;
+        double gsc = 2.0 * wp * d * op->diff_scale;       /* d chi2 / d|F|^2 */
+        for (int t = 1; t <= ns; t++) {
+            /* Q_t = 2 g conj(F) cf_t */
+            double br = cf[2 * ((int64_t)(t - 1) * np + p)], bi = cf[2 * ((int64_t)(t - 1) * np + p) + 1];
+            double fr = F[2 * p], fi = -F[2 * p + 1];
+            Q[2 * ((int64_t)(t - 1) * np + p)] = 2.0 * gsc * (fr * br - fi * bi);
+            Q[2 * ((int64_t)(t - 1) * np + p) + 1] = 2.0 * gsc * (fr * bi + fi * br);
+        }
+    }
+    if (chi2) *chi2 = x2;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads > 0 ? nthreads : 1)
+    for (int64_t a = 0; a < cr->natoms; a++) {
+        int t = cr->iscat[a];
+        double go = 0, gx[3] = {0, 0, 0};
+        if (t >= 1 && t <= ns) {
+            for (int64_t p = 0; p < np; p++) {
+                double ph = oc_frac_dot(H + 3 * p, cr->pos[3 * a], cr->pos[3 * a + 1], cr->pos[3 * a + 2]);
+                double c = cos(zpi * ph), s = sin(zpi * ph);
+                double qr = Q[2 * ((int64_t)(t - 1) * np + p)], qi = Q[2 * ((int64_t)(t - 1) * np + p) + 1];
+                double zr = qr * c - qi * s, zi = qr * s + qi * c;
+                go += zr;
+                for (int k = 0; k < 3; k++) gx[k] += H[3 * p + k] * zi;
+            }
+        }
+        double wa = cr->atom_occ ? (double)cr->atom_occ[a] : 1.0;
+        if (grad_occ) grad_occ[a] = go;
+        if (grad_pos) for (int k = 0; k < 3; k++) grad_pos[3 * a + k] = -zpi * wa * gx[k];
+    }
+    free(cf); free(F); free(Q); free(H); free(istl); free(cfact);
+    return DGPU_OK;
+}
+
+/* Time the REF22 type sums of four_run on rows [row_lo,row_hi) of the
+ * abscissa (the reference's OMP loop is uniform per row), all types.
+ * Returns seconds; *pairs_out = atoms x points covered.                   */
+double oc_time_ref_rows(const dgpu_crystal *cr, const dgpu_grid *g, int32_t row_lo,
+                        int32_t row_hi, int nthreads, int64_t *pairs_out)
+{
+    const int32_t *num = g->inc;
+    int64_t np = (int64_t)num[0] * num[1] * num[2];
+    int32_t lmn[6], fnum[3] = {num[0], num[1], num[2]};
+    double off[9];
+    oc_fourier_lmn(g->eck, g->vi, g->inc, lmn, off);
+    double *cex = (double *)malloc(sizeof(double) * 2 * DGPU_I2PI);
+    oc_cexpt(cex);
+    double *tcsf = (double *)calloc(2 * np, sizeof(double));
+    double *xat = (double *)malloc(sizeof(double) * 3 * cr->natoms);
+    int64_t pairs = 0;
+    double t0 = 0, t1 = 0;
+#ifdef _OPENMP
+    t0 = omp_get_wtime();
+#endif
+    for (int t = 1; t <= cr->nscat; t++) {
+        int64_t nx = oc_getatm(cr, t, xat, NULL);
+        if (nx <= 0) continue;
+        oc_strucf_ref(xat, NULL, nx, g->vi, g->vi + 3, g->vi + 6, off, lmn, num, fnum, cex,
+                      row_lo, row_hi, nthreads, tcsf);
+        pairs += nx * (int64_t)(row_hi - row_lo) * num[1] * num[2];
+    }
+#ifdef _OPENMP
+    t1 = omp_get_wtime();
+#endif
+    free(cex); free(tcsf); free(xat);
+    if (pairs_out) *pairs_out = pairs;
+    return t1 - t0;
+}

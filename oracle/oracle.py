@@ -1,0 +1,163 @@
+"""ctypes wrapper of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Used by tests/, __graft_entry__.smoke() and bench.py's CPU legs as the
+checker / timed CPU baseline; never by the product package.
+Parity unpinned (see discus_oracle.h).
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from diffusecode_gb300 import _abi
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+
+def build():
+    subprocess.check_call(["sh", os.path.join(_HERE, "build_oracle.sh")])
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB):
+            build()
+        L = C.CDLL(_LIB)
+        dp, ip, fp = C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_float)
+        L.oc_fourier_lmn.argtypes = [dp, dp, ip, ip, dp]
+        L.oc_cexpt.argtypes = [dp]
+        L.oc_stltab.argtypes = [dp, dp, ip, dp, ip]
+        L.oc_formtab.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Opts), dp]
+        L.oc_increments.argtypes = [dp, C.c_int64, dp, dp, dp, dp, C.POINTER(C.c_int64)]
+        L.oc_four_strucf.argtypes = [dp, C.c_int64, dp, dp, dp, dp, ip, ip, ip, dp, ip, dp]
+        L.oc_four_run.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Grid), C.POINTER(_abi.Opts),
+                                  dp, dp, dp, C.POINTER(_abi.Info), C.c_int]
+        L.oc_chi2_grad.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Grid), C.POINTER(_abi.Opts),
+                                   dp, dp, dp, dp, dp, C.c_int]
+        L.oc_time_ref_rows.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Grid), C.c_int32,
+                                       C.c_int32, C.c_int, C.POINTER(C.c_int64)]
+        L.oc_time_ref_rows.restype = C.c_double
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _i(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def fourier_lmn(eck, vi, inc):
+    eck = np.asfortranarray(eck, dtype=np.float64).reshape(-1, order="F").copy()
+    vi = np.asfortranarray(vi, dtype=np.float64).reshape(-1, order="F").copy()
+    inc = np.asarray(inc, dtype=np.int32).copy()
+    lmn = np.zeros(6, np.int32)
+    off = np.zeros(9, np.float64)
+    rc = lib().oc_fourier_lmn(_d(eck), _d(vi), _i(inc), _i(lmn), _d(off))
+    return rc, lmn, off.reshape(3, 3, order="F")
+
+
+def cexpt():
+    cex = np.zeros(2 * _abi.I2PI)
+    lib().oc_cexpt(_d(cex))
+    return cex[0::2] + 1j * cex[1::2]
+
+
+def stltab(grid, rten):
+    g = grid.to_c()
+    eck = np.array(g.eck[:], dtype=np.float64)
+    vi = np.array(g.vi[:], dtype=np.float64)
+    num = np.array(grid.inc, dtype=np.int32)
+    rt = np.asarray(rten, dtype=np.float64).reshape(-1, order="F").copy()
+    istl = np.zeros(int(np.prod(grid.inc)), np.int32)
+    rc = lib().oc_stltab(_d(eck), _d(vi), _i(num), _d(rt), _i(istl))
+    return rc, istl.reshape(grid.inc, order="F")
+
+
+def formtab(cr, opts):
+    c = cr.to_c()
+    out = np.zeros(2 * (_abi.CFPKT + 1) * cr.nscat)
+    lib().oc_formtab(C.byref(c), C.byref(opts), _d(out))
+    z = out[0::2] + 1j * out[1::2]
+    return z.reshape(cr.nscat, _abi.CFPKT + 1)
+
+
+def increments(xat, uin, vin, win, off):
+    """xat (n,3) -> int64 (6,n): iincu, iincv, iincw, jincu, jincv, jincw."""
+    x = np.asfortranarray(xat, dtype=np.float64)
+    n = x.shape[0]
+    out = np.zeros(6 * n, np.int64)
+    u, v, w = (np.asarray(a, dtype=np.float64).copy() for a in (uin, vin, win))
+    o = np.asarray(off, dtype=np.float64).reshape(-1, order="F").copy()
+    lib().oc_increments(_d(x), n, _d(u), _d(v), _d(w), _d(o), out.ctypes.data_as(C.POINTER(C.c_int64)))
+    return out.reshape(6, n)
+
+
+def four_strucf(xat, uin, vin, win, off, lmn, num, fnum, cfact=None, istl=None):
+    x = np.asfortranarray(xat, dtype=np.float64)
+    n = x.shape[0]
+    u, v, w = (np.asarray(a, dtype=np.float64).copy() for a in (uin, vin, win))
+    o = np.asarray(off, dtype=np.float64).reshape(-1, order="F").copy()
+    lm = np.asarray(lmn, dtype=np.int32).copy()
+    nm = np.asarray(num, dtype=np.int32).copy()
+    fn = np.asarray(fnum, dtype=np.int32).copy()
+    np_ = int(np.prod(num))
+    out = np.zeros(2 * np_)
+    cf = None if cfact is None else np.ascontiguousarray(np.stack([cfact.real, cfact.imag], -1).ravel())
+    ist = None if istl is None else np.asfortranarray(istl, dtype=np.int32).reshape(-1, order="F").copy()
+    lib().oc_four_strucf(_d(x), n, _d(u), _d(v), _d(w), _d(o), _i(lm), _i(nm), _i(fn),
+                         _d(cf) if cf is not None else None, _i(ist) if ist is not None else None, _d(out))
+    return (out[0::2] + 1j * out[1::2]).reshape(num, order="F")
+
+
+def four_run(cr, grid, opts, nthreads=0):
+    """Returns (rc, csf, acsf, dsi, info); arrays shaped grid.inc (Fortran order)."""
+    if nthreads <= 0:
+        nthreads = os.cpu_count() or 1
+    c = cr.to_c()
+    g = grid.to_c()
+    np_ = grid.npoints
+    csf = np.zeros(2 * np_)
+    acsf = np.zeros(2 * np_)
+    dsi = np.zeros(np_)
+    info = _abi.Info()
+    rc = lib().oc_four_run(C.byref(c), C.byref(g), C.byref(opts), _d(csf), _d(acsf), _d(dsi),
+                           C.byref(info), nthreads)
+    shp = grid.inc
+    return (rc, (csf[0::2] + 1j * csf[1::2]).reshape(shp, order="F"),
+            (acsf[0::2] + 1j * acsf[1::2]).reshape(shp, order="F"),
+            dsi.reshape(shp, order="F"), info)
+
+
+def chi2_grad(cr, grid, opts, i_target, weight=None, nthreads=0):
+    if nthreads <= 0:
+        nthreads = os.cpu_count() or 1
+    c = cr.to_c()
+    g = grid.to_c()
+    it = np.asfortranarray(i_target, dtype=np.float64).reshape(-1, order="F").copy()
+    wt = None if weight is None else np.asfortranarray(weight, dtype=np.float64).reshape(-1, order="F").copy()
+    chi2 = np.zeros(1)
+    gp = np.zeros(3 * cr.natoms)
+    go = np.zeros(cr.natoms)
+    rc = lib().oc_chi2_grad(C.byref(c), C.byref(g), C.byref(opts), _d(it),
+                            _d(wt) if wt is not None else None, _d(chi2), _d(gp), _d(go), nthreads)
+    assert rc == 0
+    return float(chi2[0]), gp.reshape(-1, 3), go
+
+
+def time_ref_rows(cr, grid, row_lo, row_hi, nthreads=0):
+    """Seconds and pairs for the REF22 type sums over abscissa rows [lo,hi)."""
+    if nthreads <= 0:
+        nthreads = os.cpu_count() or 1
+    c = cr.to_c()
+    g = grid.to_c()
+    pairs = C.c_int64(0)
+    sec = lib().oc_time_ref_rows(C.byref(c), C.byref(g), int(row_lo), int(row_hi), int(nthreads),
+                                 C.byref(pairs))
+    return sec, int(pairs.value)
