@@ -235,9 +235,17 @@ __global__ void k_qinfo_part(double e0, double e1, double e2, FormSpec const *fs
 
 __global__ void k_qinfo_final(const QStat *part, int n, double *res)
 {
+    __shared__ QStat sh[QNT];
+    QStat s = {-9999.0, (double)1e19f, -9999.0, (double)1e19f, 0.0, 0.0, 0};
+    for (int k = threadIdx.x; k < n; k += QNT) qmerge(s, part[k]);
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = QNT / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) qmerge(sh[threadIdx.x], sh[threadIdx.x + o]);
+        __syncthreads();
+    }
     if (threadIdx.x != 0) return;
-    QStat s = part[0];
-    for (int k = 1; k < n; k++) qmerge(s, part[k]);
+    s = sh[0];
     double ave = 0.0, sig = 0.0;
     if (s.nd) {
         ave = s.dsum / (double)s.nd;
@@ -320,7 +328,7 @@ int dgpu_qinfo(dgpu_ctx *ctx, const double eck[3], const double vi[9], const int
     double *d_res = (double *)((char *)ctx->flag.p + 64);
     k_qinfo_part<<<nblk, QNT, 0, ctx->stream>>>(eck[0], eck[1], eck[2], d, num[0], num[1], num[2], dsi, parts);
     DGPU_CUDA(ctx, cudaGetLastError());
-    k_qinfo_final<<<1, 32, 0, ctx->stream>>>(parts, nblk, d_res);
+    k_qinfo_final<<<1, QNT, 0, ctx->stream>>>(parts, nblk, d_res);
     DGPU_CUDA(ctx, cudaGetLastError());
     DGPU_CUDA(ctx, cudaMemcpyAsync(res, d_res, 7 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

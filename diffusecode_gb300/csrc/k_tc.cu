@@ -1,11 +1,576 @@
-// Tensor-core engine (placeholder until the tcgen05 kernel lands).
+// Tensor-core engine: the type sums as a split-precision complex GEMM on
+// tcgen05 (sm_100 family), accumulators in TMEM.
+//
+// For the computed box, one grid axis ac is the GEMM's N dimension
+// ("columns") and the other two, flattened, its M dimension ("rows").  The
+// phase of point (row r, column c) and atom j splits exactly:
+//     phase = [ph0_j + n_ra(r) d_ra,j + n_rb(r) d_rb,j] + [n_ac(c) d_ac,j]
+// so  S(r,c) = sum_j U[r,j] V[j,c]  with  U = w_j exp(2 pi i A-phase),
+// V = exp(2 pi i B-phase); K = the atoms of one type (a slice of them per
+// work item).  Each CTA generates its U (128 rows) and V (N columns) tiles
+// for KA = 32 atoms per stage directly in shared memory from the 64-bit
+// fixed-point phases (no operand traffic in HBM), splits every FP32 phasor
+// value into fp16 (or bf16) hi + lo, and issues per 16 atoms the 12 MMAs
+//     Re += Ur Vr^T - Ui Vi^T ,  Im += Ur Vi^T + Ui Vr^T
+// for the split products (hi,hi), (hi,lo), (lo,hi).  Partial sums of one
+// work item (FP32 in TMEM) go to global memory as double2, and the combine
+// kernel adds the K slices in FP64.
+//
+// Warp roles (416 threads): warps 0-7 produce operand stages, warp 8 owns
+// TMEM and issues the MMAs (one elected lane), warps 9-12 drain TMEM.  All
+// waits are bounded (globaltimer); a wait that gives up sets an error flag,
+// the CTA stops issuing, waits for its own MMAs, frees TMEM and returns.
+//
+// Shared-memory operands use the canonical K-major layout without swizzle:
+// 8x8 fp16 core matrices of 128 contiguous bytes, LBO = 128 B between
+// K-adjacent core matrices, SBO = (KA/8)*128 B between 8-row groups.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
 #include "dgpu_internal.h"
 
-bool dgpu_tc_available(dgpu_ctx *ctx) { (void)ctx; return false; }
+#define TC_KA 32
+#define TC_M 128
+#define TC_PROD_WARPS 8
+#define TC_MMA_WARP 8
+#define TC_EPI_WARP0 9
+#define TC_THREADS (13 * 32)
+#define TC_PROD_THREADS (TC_PROD_WARPS * 32)
+#define TC_A_BYTES (TC_M * TC_KA * 2)          // one operand (e.g. Ur_hi): 8 KB
+#define TC_SBO ((TC_KA / 8) * 128)
+#define TC_LBO 128
+#define TC_TIMEOUT_NS 2000000000ull            // 2 s per wait
 
-int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *, const uint64_t *, const uint64_t *, const uint64_t *,
-                 const float *, const int64_t *, int32_t, const BoxSpec &, const dgpu_opts *, DevBuf &,
-                 int32_t *)
+struct TcGeom {
+    int32_t f[3];
+    int32_t ra, rb, ac, fra;
+    int64_t sra, srb, sac;   // box-index strides of the row and column axes
+    int32_t nrows, ncols;
+    int32_t N;               // columns per tile (multiple of 16, <= 256)
+    int32_t m_tiles, n_tiles, nslice, ntype;
+    int64_t slice_len, nitems, pbox;
+    int32_t stages;
+    int32_t bf16;
+    uint32_t tmem_cols;
+    int64_t ts[65];
+};
+
+// ---------------------------------------------------------------------------
+// PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t gtimer()
 {
-    return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "tensor-core engine not built");
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait: false if the error flag is up or the wait timed out
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int32_t *err, int code)
+{
+    if (mbar_try(bar, parity)) return true;
+    uint64_t t0 = gtimer();
+    for (uint32_t it = 1;; ++it) {
+        if (mbar_try(bar, parity)) return true;
+        if ((it & 63) == 0) {
+            if (*err) return false;
+            if (gtimer() - t0 > TC_TIMEOUT_NS) {
+                atomicCAS((int32_t *)err, 0, code);
+                return false;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((TC_LBO >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((TC_SBO >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;          // descriptor version of the sm_100 family; no swizzle
+    return d;
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t dt, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dt),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16])
+{
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+          "=r"(r[15])
+        : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// ---------------------------------------------------------------------------
+// operand generation
+
+// exp(2 pi i phase) from the top 32 bits of a 64-bit fixed-point turn
+__device__ __forceinline__ void phasor(uint64_t ph, float &c, float &s)
+{
+    float ang = (float)(int32_t)(ph >> 32) * 1.4629180792671596e-09f;   // 2 pi / 2^32
+    __sincosf(ang, &s, &c);
+}
+
+__device__ __forceinline__ uint32_t pack2(float a, float b, bool bf)
+{
+    if (bf) {
+        __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+        return *reinterpret_cast<uint32_t *>(&v);
+    }
+    __half2 v = __floats2half2_rn(a, b);
+    return *reinterpret_cast<uint32_t *>(&v);
+}
+
+__device__ __forceinline__ float2 unpack2(uint32_t u, bool bf)
+{
+    if (bf) {
+        __nv_bfloat162 v = *reinterpret_cast<__nv_bfloat162 *>(&u);
+        return __bfloat1622float2(v);
+    }
+    __half2 v = *reinterpret_cast<__half2 *>(&u);
+    return __half22float2(v);
+}
+
+// 8 values -> hi (rounded) and lo (remainder, rounded) packed as 16 bytes each
+__device__ __forceinline__ void split8(const float (&v)[8], uint4 &hi, uint4 &lo, bool bf)
+{
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        h[k] = pack2(v[2 * k], v[2 * k + 1], bf);
+        float2 b = unpack2(h[k], bf);
+        l[k] = pack2(v[2 * k] - b.x, v[2 * k + 1] - b.y, bf);
+    }
+    hi = make_uint4(h[0], h[1], h[2], h[3]);
+    lo = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+// byte offset of (row, k-group) in one operand of the canonical layout
+__device__ __forceinline__ uint32_t core_off(int row, int q) { return (row >> 3) * TC_SBO + q * TC_LBO + (row & 7) * 16; }
+
+struct TcArgs {
+    const uint64_t *ph0;
+    const uint64_t *dra, *drb, *dac;   // increments along the row axes and the column axis
+    const float *w;
+    double2 *part;
+    int32_t *err;
+};
+
+__device__ __forceinline__ void decode_item(const TcGeom &g, int64_t item, int &t, int &ks, int &nt, int &mt)
+{
+    mt = (int)(item % g.m_tiles);
+    int64_t r = item / g.m_tiles;
+    nt = (int)(r % g.n_tiles);
+    r /= g.n_tiles;
+    ks = (int)(r % g.nslice);
+    t = (int)(r / g.nslice);
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcGeom g, const TcArgs args)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const int S = g.stages;
+    const int N = g.N;
+    const uint32_t b_bytes = (uint32_t)N * TC_KA * 2;      // one B operand
+    const uint32_t stage_bytes = 4 * TC_A_BYTES + 4 * b_bytes;
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + (size_t)S * stage_bytes);
+    uint64_t *empty = full + S;
+    uint64_t *tfull = empty + S;
+    uint64_t *tempty = tfull + 1;
+    uint64_t *drain = tempty + 1;
+    uint32_t *tbase = reinterpret_cast<uint32_t *>(drain + 1);
+    volatile int32_t *err = args.err;
+    const bool bf = g.bf16 != 0;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < S; s++) {
+            mbar_init(&full[s], TC_PROD_THREADS);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(tfull, 1);
+        mbar_init(tempty, 4 * 32);
+        mbar_init(drain, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == TC_MMA_WARP) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tbase)),
+                     "r"(g.tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tbase;
+
+    if (warp < TC_PROD_WARPS) {
+        // ------------------------------------------------------------ producers
+        const int tid = threadIdx.x;
+        uint32_t it = 0;
+        bool ok = true;
+        for (int64_t item = blockIdx.x; item < g.nitems && ok; item += gridDim.x) {
+            int t, ks, nt, mt;
+            decode_item(g, item, t, ks, nt, mt);
+            const int64_t a0 = g.ts[t] + (int64_t)ks * g.slice_len;
+            const int64_t a1 = min(g.ts[t + 1], a0 + g.slice_len);
+            const int64_t cnt = a1 > a0 ? a1 - a0 : 0;
+            const int nst = (int)((cnt + TC_KA - 1) / TC_KA);
+            const uint64_t *dra = args.dra, *drb = args.drb, *dac = args.dac;
+            for (int st = 0; st < nst; st++, it++) {
+                const int s = it % S;
+                if (it >= (uint32_t)S && !mbar_wait(&empty[s], ((it / S) - 1) & 1, err, 1)) { ok = false; break; }
+                uint8_t *A = smem + (size_t)s * stage_bytes;
+                uint8_t *B = A + 4 * TC_A_BYTES;
+                const int64_t ab = a0 + (int64_t)st * TC_KA;
+                const int units = 4 * TC_M + 4 * N;
+                for (int u = tid; u < units; u += TC_PROD_THREADS) {
+                    float re[8], im[8];
+                    uint32_t off;
+                    uint8_t *base;
+                    uint32_t ostride;
+                    if (u < 4 * TC_M) {
+                        const int r = u % TC_M, q = u / TC_M;
+                        const int64_t rg = (int64_t)mt * TC_M + r;
+                        const bool rv = rg < g.nrows;
+                        const uint32_t na = rv ? (uint32_t)(rg % g.fra) : 0u;
+                        const uint32_t nb = rv ? (uint32_t)(rg / g.fra) : 0u;
+#pragma unroll
+                        for (int e = 0; e < 8; e++) {
+                            const int64_t a = ab + q * 8 + e;
+                            if (rv && a < a1) {
+                                uint64_t ph = __ldg(&args.ph0[a]) + na * __ldg(&dra[a]) + nb * __ldg(&drb[a]);
+                                float c, sn;
+                                phasor(ph, c, sn);
+                                const float wj = __ldg(&args.w[a]);
+                                re[e] = wj * c;
+                                im[e] = wj * sn;
+                            } else {
+                                re[e] = 0.f;
+                                im[e] = 0.f;
+                            }
+                        }
+                        off = core_off(r, q);
+                        base = A;
+                        ostride = TC_A_BYTES;
+                    } else {
+                        const int v = u - 4 * TC_M;
+                        const int c = v % N, q = v / N;
+                        const int64_t cg = (int64_t)nt * N + c;
+                        const bool cv = cg < g.ncols;
+                        const uint32_t nc = (uint32_t)cg;
+#pragma unroll
+                        for (int e = 0; e < 8; e++) {
+                            const int64_t a = ab + q * 8 + e;
+                            if (cv && a < a1) {
+                                float cs, sn;
+                                phasor(nc * __ldg(&dac[a]), cs, sn);
+                                re[e] = cs;
+                                im[e] = sn;
+                            } else {
+                                re[e] = 0.f;
+                                im[e] = 0.f;
+                            }
+                        }
+                        off = core_off(c, q);
+                        base = B;
+                        ostride = b_bytes;
+                    }
+                    uint4 hr, lr, hi_, li;
+                    split8(re, hr, lr, bf);
+                    split8(im, hi_, li, bf);
+                    *reinterpret_cast<uint4 *>(base + 0 * ostride + off) = hr;   // real hi
+                    *reinterpret_cast<uint4 *>(base + 1 * ostride + off) = lr;   // real lo
+                    *reinterpret_cast<uint4 *>(base + 2 * ostride + off) = hi_;  // imag hi
+                    *reinterpret_cast<uint4 *>(base + 3 * ostride + off) = li;   // imag lo
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_arrive(&full[s]);
+            }
+        }
+    } else if (warp == TC_MMA_WARP) {
+        // ------------------------------------------------------------ MMA issuer
+        const uint32_t fmt = bf ? 1u : 0u;
+        const uint32_t idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(N >> 3) << 17) |
+                               ((uint32_t)(TC_M >> 4) << 24);
+        const uint32_t idesc_neg = idesc | (1u << 13);     // negate A: the -Ui Vi^T product
+        const uint32_t d_re = tmem, d_im = tmem + (uint32_t)N;
+        uint32_t it = 0, nitem = 0;
+        bool ok = true, issued = false;
+        for (int64_t item = blockIdx.x; item < g.nitems && ok; item += gridDim.x) {
+            int t, ks, nt, mt;
+            decode_item(g, item, t, ks, nt, mt);
+            const int64_t a0 = g.ts[t] + (int64_t)ks * g.slice_len;
+            const int64_t a1 = min(g.ts[t + 1], a0 + g.slice_len);
+            const int64_t cnt = a1 > a0 ? a1 - a0 : 0;
+            const int nst = (int)((cnt + TC_KA - 1) / TC_KA);
+            if (nst == 0) continue;
+            if (nitem > 0 && !mbar_wait(tempty, (nitem - 1) & 1, err, 2)) { ok = false; break; }
+            tc_fence_after();
+            for (int st = 0; st < nst; st++, it++) {
+                const int s = it % S;
+                if (!mbar_wait(&full[s], (it / S) & 1, err, 3)) { ok = false; break; }
+                tc_fence_after();
+                if (lane == 0) {
+                    const uint32_t A = smem_u32(smem + (size_t)s * stage_bytes);
+                    const uint32_t B = A + 4 * TC_A_BYTES;
+#pragma unroll
+                    for (int kk = 0; kk < TC_KA / 16; kk++) {
+                        const uint32_t ko = kk * 2 * TC_LBO;
+                        const uint64_t ar[2] = {sdesc(A + 0 * TC_A_BYTES + ko), sdesc(A + 1 * TC_A_BYTES + ko)};
+                        const uint64_t ai[2] = {sdesc(A + 2 * TC_A_BYTES + ko), sdesc(A + 3 * TC_A_BYTES + ko)};
+                        const uint64_t br[2] = {sdesc(B + 0 * b_bytes + ko), sdesc(B + 1 * b_bytes + ko)};
+                        const uint64_t bi[2] = {sdesc(B + 2 * b_bytes + ko), sdesc(B + 3 * b_bytes + ko)};
+#pragma unroll
+                        for (int p = 0; p < 3; p++) {
+                            const int x = p == 2 ? 1 : 0;     // A: hi, hi, lo
+                            const int y = p == 1 ? 1 : 0;     // B: hi, lo, hi
+                            const uint32_t acc = (st > 0 || kk > 0 || p > 0) ? 1u : 0u;
+                            mma_f16(d_re, ar[x], br[y], idesc, acc);
+                            mma_f16(d_re, ai[x], bi[y], idesc_neg, 1u);
+                            mma_f16(d_im, ar[x], bi[y], idesc, acc);
+                            mma_f16(d_im, ai[x], br[y], idesc, 1u);
+                        }
+                    }
+                    mma_commit(&empty[s]);
+                    issued = true;
+                }
+                __syncwarp();
+            }
+            if (!ok) break;
+            if (lane == 0) mma_commit(tfull);
+            __syncwarp();
+            nitem++;
+        }
+        // make sure no MMA of this CTA is still running before TMEM is freed
+        if (lane == 0 && issued) {
+            mma_commit(drain);
+        }
+        __syncwarp();
+        if (__shfl_sync(0xffffffffu, issued ? 1 : 0, 0)) mbar_wait(drain, 0, err, 4);
+        tc_fence_before();
+    } else {
+        // ------------------------------------------------------------ epilogue
+        const int q = warp & 3;                       // TMEM lane quadrant of this warp
+        const int r = q * 32 + lane;
+        uint32_t nitem = 0;
+        bool ok = true;
+        for (int64_t item = blockIdx.x; item < g.nitems && ok; item += gridDim.x) {
+            int t, ks, nt, mt;
+            decode_item(g, item, t, ks, nt, mt);
+            const int64_t a0 = g.ts[t] + (int64_t)ks * g.slice_len;
+            const int64_t a1 = min(g.ts[t + 1], a0 + g.slice_len);
+            const bool has = a1 > a0;
+            if (has) {
+                if (!mbar_wait(tfull, nitem & 1, err, 5)) { ok = false; break; }
+                tc_fence_after();
+            }
+            const int64_t rg = (int64_t)mt * TC_M + r;
+            const bool rv = rg < g.nrows;
+            const int64_t prow = rv ? (rg % g.fra) * g.sra + (rg / g.fra) * g.srb : 0;
+            double2 *out = args.part + ((int64_t)t * g.nslice + ks) * g.pbox + prow;
+            for (int c0 = 0; c0 < N; c0 += 16) {
+                uint32_t vr[16], vi[16];
+                if (has) {
+                    const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
+                    tmem_ld16(ta, vr);
+                    tmem_ld16(ta + (uint32_t)N, vi);
+                    tmem_wait_ld();
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 16; k++) vr[k] = vi[k] = 0u;
+                }
+                const int64_t cbase = (int64_t)nt * N + c0;
+#pragma unroll
+                for (int k = 0; k < 16; k++) {
+                    if (rv && cbase + k < g.ncols)
+                        out[(cbase + k) * g.sac] =
+                            make_double2((double)__uint_as_float(vr[k]), (double)__uint_as_float(vi[k]));
+                }
+            }
+            if (has) {
+                tc_fence_before();
+                mbar_arrive(tempty);
+                nitem++;
+            }
+        }
+    }
+    __syncthreads();
+    if (warp == TC_MMA_WARP) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(g.tmem_cols)
+                     : "memory");
+    }
+}
+
+// ---------------------------------------------------------------------------
+bool dgpu_tc_available(dgpu_ctx *ctx)
+{
+    static int cached = -1;
+    if (cached < 0) {
+        cudaDeviceProp p;
+        cached = (cudaGetDeviceProperties(&p, ctx->device) == cudaSuccess && p.major == 10) ? 1 : 0;
+    }
+    return cached == 1;
+}
+
+static uint32_t pow2_cols(int n)
+{
+    uint32_t c = 32;
+    while (c < (uint32_t)n) c <<= 1;
+    return c;
+}
+
+int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const uint64_t *dv, const uint64_t *dw,
+                 const float *w, const int64_t *h_type_start, int32_t ntype, const BoxSpec &box,
+                 const dgpu_opts *op, DevBuf &part, int32_t *nslice_out)
+{
+    if (ntype < 1 || ntype > 64) return dgpu_set_error(ctx, DGPU_ERR_ARG, "ntype=%d", ntype);
+    TcGeom g;
+    memset(&g, 0, sizeof(g));
+    for (int k = 0; k < 3; k++) g.f[k] = box.f[k];
+    // column axis: the one whose tile padding wastes least, longer axis on ties
+    int ac = -1;
+    double best = 1e30;
+    int want_n = op->tc_tile_n;
+    for (int a = 0; a < 3; a++) {
+        if (box.f[a] < 2 && !(box.f[0] * box.f[1] * box.f[2] == box.f[a])) continue;
+        int n = box.f[a];
+        int tiles = (int)dgpu_cdiv(n, 256);
+        int N = (int)dgpu_cdiv(dgpu_cdiv(n, tiles), 16) * 16;
+        if (want_n > 0) {
+            N = want_n;
+            tiles = (int)dgpu_cdiv(n, N);
+        }
+        int64_t rows = (int64_t)box.f[0] * box.f[1] * box.f[2] / n;
+        double cost = (double)tiles * N * dgpu_cdiv(rows, TC_M) * TC_M;   // padded MMA area
+        cost *= (1.0 + 16.0 / N);                                         // operand-generation overhead
+        if (cost < best - 1e-9) { best = cost; ac = a; }
+    }
+    if (ac < 0) ac = 0;
+    g.ac = ac;
+    g.ra = ac == 0 ? 1 : 0;
+    g.rb = 3 - ac - g.ra;
+    g.ncols = box.f[ac];
+    g.fra = box.f[g.ra];
+    {
+        const int64_t stride[3] = {1, (int64_t)box.f[0], (int64_t)box.f[0] * box.f[1]};
+        g.sra = stride[g.ra];
+        g.srb = stride[g.rb];
+        g.sac = stride[ac];
+    }
+    g.nrows = box.f[g.ra] * box.f[g.rb];
+    g.n_tiles = (int32_t)dgpu_cdiv(g.ncols, 256);
+    g.N = (int32_t)(dgpu_cdiv(dgpu_cdiv(g.ncols, g.n_tiles), 16) * 16);
+    if (want_n > 0) {
+        if (want_n % 16 || want_n < 16 || want_n > 256)
+            return dgpu_set_error(ctx, DGPU_ERR_ARG, "tc_tile_n=%d (multiple of 16 in 16..256)", want_n);
+        g.N = want_n;
+        g.n_tiles = (int32_t)dgpu_cdiv(g.ncols, g.N);
+    }
+    g.m_tiles = (int32_t)dgpu_cdiv(g.nrows, TC_M);
+    g.pbox = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    g.ntype = ntype;
+    g.bf16 = op->split == DGPU_SPLIT_BF16;
+    int64_t maxn = 0;
+    for (int t = 0; t < ntype; t++) {
+        g.ts[t] = h_type_start[t];
+        int64_t n = h_type_start[t + 1] - h_type_start[t];
+        maxn = n > maxn ? n : maxn;
+    }
+    g.ts[ntype] = h_type_start[ntype];
+    // K slices: enough work items for all SMs, at most tc_kslice atoms each
+    int64_t tiles = (int64_t)g.m_tiles * g.n_tiles * ntype;
+    int64_t nsl = dgpu_cdiv(4LL * ctx->nsm, tiles);
+    int64_t max_len = op->tc_kslice > 0 ? op->tc_kslice : 32768;
+    if (nsl < dgpu_cdiv(maxn, max_len)) nsl = dgpu_cdiv(maxn, max_len);
+    int64_t min_len = 1024;
+    if (nsl > 1 && dgpu_cdiv(maxn, nsl) < min_len) nsl = dgpu_cdiv(maxn, min_len);
+    if (nsl < 1) nsl = 1;
+    g.slice_len = dgpu_cdiv(maxn > 0 ? maxn : 1, nsl);
+    g.slice_len = dgpu_cdiv(g.slice_len, TC_KA) * TC_KA;
+    g.nslice = (int32_t)dgpu_cdiv(maxn > 0 ? maxn : 1, g.slice_len);
+    g.nitems = tiles * g.nslice;
+    const uint32_t stage_bytes = 4 * TC_A_BYTES + 4u * g.N * TC_KA * 2;
+    const uint32_t bar_bytes = 256;
+    int stages = (int)((200 * 1024 - bar_bytes) / stage_bytes);
+    g.stages = stages > 4 ? 4 : stages;
+    if (g.stages < 2) return dgpu_set_error(ctx, DGPU_ERR_ARG, "tile too large for shared memory");
+    g.tmem_cols = pow2_cols(2 * g.N);
+    size_t smem = (size_t)g.stages * stage_bytes + bar_bytes;
+
+    DGPU_CUDA(ctx, part.ensure((size_t)ntype * g.nslice * g.pbox * sizeof(double2)));
+    DGPU_CUDA(ctx, ctx->flag.ensure(64));
+    int32_t *d_err = ctx->flag.as<int32_t>() + 8;
+    DGPU_CUDA(ctx, cudaMemsetAsync(d_err, 0, sizeof(int32_t), ctx->stream));
+    TcArgs args;
+    args.ph0 = ph0;
+    const uint64_t *dd[3] = {du, dv, dw};
+    args.dra = dd[g.ra];
+    args.drb = dd[g.rb];
+    args.dac = dd[g.ac];
+    args.w = w;
+    args.part = part.as<double2>();
+    args.err = d_err;
+    static bool attr_set = false;
+    if (!attr_set) {
+        DGPU_CUDA(ctx, cudaFuncSetAttribute(k_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+        attr_set = true;
+    }
+    int grid = (int)(g.nitems < ctx->nsm ? g.nitems : ctx->nsm);
+    if (grid < 1) grid = 1;
+    k_tc<<<grid, TC_THREADS, smem, ctx->stream>>>(g, args);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    int32_t herr = 0;
+    DGPU_CUDA(ctx, cudaMemcpyAsync(&herr, d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (herr) return dgpu_set_error(ctx, DGPU_ERR_TIMEOUT, "tensor-core kernel wait gave up (site %d)", herr);
+    *nslice_out = g.nslice;
+    return DGPU_OK;
 }

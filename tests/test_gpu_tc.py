@@ -1,0 +1,87 @@
+"""Tensor-core engine (tcgen05 split-precision GEMM) against the oracle's
+exact FP64 sums: max |I - I_64| / (I_64 + N<|f|^2>) <= 1e-5 with the fp16
+hi/lo split.  Shapes exercise padding of rows (M = 128) and columns
+(N multiple of 16), several K slices per type and several work items per CTA."""
+import numpy as np
+import pytest
+
+import kat_cases as K
+from diffusecode_gb300 import _abi
+from diffusecode_gb300 import fourier as FR
+from diffusecode_gb300 import structures as S
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+
+def tc_opts(**kw):
+    base = dict(phase=_abi.PHASE_EXACT64, engine=_abi.ENGINE_TC)
+    base.update(kw)
+    return K.opts(**base)
+
+
+@pytest.mark.parametrize("inc,natoms", [((13, 11, 7), 300), ((37, 5, 3), 1000), ((3, 129, 2), 77),
+                                        ((201, 1, 1), 40)])
+def test_tc_random_vs_oracle(oracle, ctx, inc, natoms):
+    cr, g = S.small_random(seed=31, natoms=natoms, nscat=3, inc=inc)
+    for form in (_abi.FORM_TABLE, _abi.FORM_ANALYTIC):
+        op = tc_opts(form=form)
+        rc, csf, acsf, dsi, info = oracle.four_run(cr, g, op)
+        r = FR.four_run(cr, g, op, ctx=ctx)
+        assert r.info.engine_used == _abi.ENGINE_TC
+        assert K.rel_err(r.dsi, dsi, K.incoherent_floor(cr, g, op)) <= TOL
+
+
+@pytest.mark.parametrize("tile_n,kslice", [(16, 1024), (64, 2048), (208, 0), (256, 1024)])
+def test_tc_tiles_and_slices(oracle, ctx, tile_n, kslice):
+    cr, g = S.perovskite_plane(cells=6)
+    op = tc_opts(tc_tile_n=tile_n, tc_kslice=kslice)
+    rc, csf, acsf, dsi, info = oracle.four_run(cr, g, op)
+    r = FR.four_run(cr, g, op, ctx=ctx)
+    assert K.rel_err(r.dsi, dsi, K.incoherent_floor(cr, g, op)) <= TOL
+
+
+def test_tc_perovskite_plane(oracle, ctx):
+    cr, g = S.perovskite_plane()
+    op = tc_opts()
+    rc, csf, acsf, dsi, info = oracle.four_run(cr, g, op)
+    r = FR.four_run(cr, g, op, ctx=ctx)
+    err = K.rel_err(r.dsi, dsi, K.incoherent_floor(cr, g, op))
+    print(f"perovskite TC rel err {err:.2e}")
+    assert err <= TOL
+
+
+def test_tc_average_structure(oracle, ctx):
+    cr, g = S.perovskite_plane(cells=5)
+    op = tc_opts(fave=1.0)
+    rc, csf, acsf, dsi, info = oracle.four_run(cr, g, op)
+    r = FR.four_run(cr, g, op, ctx=ctx)
+    assert np.max(np.abs(r.acsf - acsf)) <= 1e-5 * np.abs(acsf).max()
+    assert K.rel_err(r.dsi, dsi, K.incoherent_floor(cr, g, op)) <= TOL
+
+
+def test_tc_known_answers(ctx):
+    cr, g, F = K.laue()
+    r = FR.four_run(cr, g, tc_opts(form=_abi.FORM_ANALYTIC), ctx=ctx)
+    assert np.max(np.abs(r.csf - F)) <= 1e-5 * np.abs(F).max()
+    cr, g, F = K.two_atoms()
+    r = FR.four_run(cr, g, tc_opts(form=_abi.FORM_ANALYTIC, friedel=0), ctx=ctx)
+    assert np.max(np.abs(r.csf - F)) <= 1e-5 * np.abs(F).max()
+
+
+def test_tc_bf16_split_error_is_reported(oracle, ctx):
+    """bf16 hi/lo keeps ~16 significant bits; it runs, with a larger error."""
+    cr, g = S.perovskite_plane(cells=4)
+    op = tc_opts(split=_abi.SPLIT_BF16)
+    rc, csf, acsf, dsi, info = oracle.four_run(cr, g, op)
+    r = FR.four_run(cr, g, op, ctx=ctx)
+    err = K.rel_err(r.dsi, dsi, K.incoherent_floor(cr, g, op))
+    print(f"bf16 split rel err {err:.2e}")
+    assert err <= 1e-3
+
+
+def test_tc_ref22_rejected(ctx):
+    cr, g = S.perovskite_plane(cells=2)
+    with pytest.raises(Exception) as e:
+        FR.four_run(cr, g, tc_opts(phase=_abi.PHASE_REF22), ctx=ctx)
+    assert getattr(e.value, "code", None) == _abi.DGPU_ERR_UNSUPPORTED
