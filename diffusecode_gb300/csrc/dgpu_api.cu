@@ -166,13 +166,20 @@ static int pick_engine(dgpu_ctx *ctx, const dgpu_opts *op)
 
 static int engine_sums(dgpu_ctx *ctx, int engine, DevBuf &ph0, DevBuf &du, DevBuf &dv, DevBuf &dw, DevBuf &w,
                        const int64_t *ts, int32_t ntype, const dgpu_opts *op, const BoxSpec &box, DevBuf &part,
-                       int32_t *nslice)
+                       PartRef *ref)
 {
+    int rc;
+    int32_t nslice = 1;
     if (engine == DGPU_ENGINE_TC)
-        return dgpu_tc_sums(ctx, ph0.as<uint64_t>(), du.as<uint64_t>(), dv.as<uint64_t>(), dw.as<uint64_t>(),
-                            w.as<float>(), ts, ntype, box, op, part, nslice);
-    return dgpu_direct_sums(ctx, ph0.as<uint64_t>(), du.as<uint64_t>(), dv.as<uint64_t>(), dw.as<uint64_t>(),
-                            w.as<float>(), ts, ntype, op->phase == DGPU_PHASE_REF22, box, part, nslice);
+        rc = dgpu_tc_sums(ctx, ph0.as<uint64_t>(), du.as<uint64_t>(), dv.as<uint64_t>(), dw.as<uint64_t>(),
+                          w.as<float>(), ts, ntype, box, op, part, &nslice);
+    else
+        rc = dgpu_direct_sums(ctx, ph0.as<uint64_t>(), du.as<uint64_t>(), dv.as<uint64_t>(), dw.as<uint64_t>(),
+                              w.as<float>(), ts, ntype, op->phase == DGPU_PHASE_REF22, box, part, &nslice);
+    ref->p = part.p;
+    ref->nslice = nslice;
+    ref->f32 = engine == DGPU_ENGINE_TC;
+    return rc;
 }
 
 // The whole path with device-resident crystal arrays and outputs.
@@ -240,10 +247,10 @@ static int four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
         rc = dgpu_prepare_atoms(ctx, cr->pos, cr->iscat, cr->atom_occ, cr->natoms, cr->nscat, geo, fold,
                                 ctx->aph0, ctx->adu, ctx->adv, ctx->adw, ctx->aw, ts);
         if (rc) return rc;
-        int32_t anslice = 1;
+        PartRef aref;
         DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
         rc = engine_sums(ctx, engine, ctx->aph0, ctx->adu, ctx->adv, ctx->adw, ctx->aw, ts, cr->nscat, op, box,
-                         ctx->apart, &anslice);
+                         ctx->apart, &aref);
         if (rc) return rc;
         pairs_aver += ts[cr->nscat] * np;
         // lattice of all cells (four_getav LOT_OFF + four_strucf(0,...) on the full num)
@@ -267,7 +274,7 @@ static int four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
             warn = DGPU_WARN_NO_CELL;
             dgpu_set_error(ctx, DGPU_WARN_NO_CELL, "no unit cell selected for <F>");
         }
-        rc = dgpu_aver_combine(ctx, fs, box, ctx->apart.as<double2>(), anslice, ctx->istl.as<int32_t>(),
+        rc = dgpu_aver_combine(ctx, fs, box, aref, ctx->istl.as<int32_t>(),
                                ctx->cfact.as<double2>(), closed ? nullptr : ctx->lat.as<double2>(), lat_nslice,
                                closed, cr->icc, cr->dim0, norm, d_acsf);
         if (rc) return rc;
@@ -282,13 +289,13 @@ static int four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
     rc = dgpu_prepare_atoms(ctx, cr->pos, cr->iscat, cr->atom_occ, cr->natoms, cr->nscat, geo, nofold, ctx->ph0,
                             ctx->du, ctx->dv, ctx->dw, ctx->w, ts);
     if (rc) return rc;
-    int32_t nslice = 1;
+    PartRef pref;
     DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
     rc = engine_sums(ctx, engine, ctx->ph0, ctx->du, ctx->dv, ctx->dw, ctx->w, ts, cr->nscat, op, box, ctx->part,
-                     &nslice);
+                     &pref);
     if (rc) return rc;
     DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
-    rc = dgpu_combine(ctx, fs, box, ctx->part.as<double2>(), nslice, ctx->istl.as<int32_t>(),
+    rc = dgpu_combine(ctx, fs, box, pref, ctx->istl.as<int32_t>(),
                       ctx->cfact.as<double2>(), op->fave != 0.0 ? d_acsf : nullptr, d_csf, d_dsi, op->diff_scale);
     if (rc) return rc;
     {
@@ -443,7 +450,8 @@ extern "C" int dgpu_four_strucf(dgpu_ctx *ctx, const double *xat, int64_t nxat, 
         memset(&fs, 0, sizeof(fs));
         fs.mode = DGPU_FORM_TABLE;
         fs.nscat = 1;
-        rc = dgpu_combine(ctx, fs, box, ctx->part.as<double2>(), nslice, ctx->istl.as<int32_t>(),
+        PartRef pref = {ctx->part.p, nslice, 0};
+        rc = dgpu_combine(ctx, fs, box, pref, ctx->istl.as<int32_t>(),
                           ctx->cfact.as<double2>(), nullptr, ctx->csf.as<double2>(), ctx->dsi.as<double>(), 1.0);
         if (rc) return rc;
     }

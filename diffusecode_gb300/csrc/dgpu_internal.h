@@ -131,6 +131,7 @@ int dgpu_direct_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du,
                      const BoxSpec &box, DevBuf &part, int32_t *nslice_out);
 
 // tc.cu -----------------------------------------------------------------
+// Partial sums are float2 (FP32, one per work item, RN-accumulated drains).
 int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const uint64_t *dv,
                  const uint64_t *dw, const float *w, const int64_t *h_type_start,
                  int32_t ntype, const BoxSpec &box, const dgpu_opts *op, DevBuf &part,
@@ -147,11 +148,17 @@ struct FormSpec {
     double rten[9];
     double eck[3], vi[9];
 };
-int dgpu_combine(dgpu_ctx *ctx, const FormSpec &fs, const BoxSpec &box, const double2 *part,
-                 int32_t nslice, const int32_t *istl, const double2 *cfact,
+// Partial sums part[t][s][p] of either engine: double2 (direct) or float2 (TC).
+struct PartRef {
+    const void *p;
+    int32_t nslice;
+    int32_t f32;
+};
+int dgpu_combine(dgpu_ctx *ctx, const FormSpec &fs, const BoxSpec &box, const PartRef &part,
+                 const int32_t *istl, const double2 *cfact,
                  const double2 *acsf_box_in, double2 *csf, double *dsi, double diff_scale);
 int dgpu_aver_combine(dgpu_ctx *ctx, const FormSpec &fs, const BoxSpec &box,
-                      const double2 *apart, int32_t anslice, const int32_t *istl,
+                      const PartRef &apart, const int32_t *istl,
                       const double2 *cfact, const double2 *lat, int32_t lat_nslice,
                       int32_t lat_closed, const int32_t icc[3], const double dim0[3],
                       double norm, double2 *acsf);

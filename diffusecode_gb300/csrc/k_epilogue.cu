@@ -43,7 +43,15 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b)
     return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-__global__ void k_combine(const FormSpec *fs, BoxSpec box, const double2 *__restrict__ part,
+__device__ __forceinline__ double2 ld_part(const double2 *p) { return *p; }
+__device__ __forceinline__ double2 ld_part(const float2 *p)
+{
+    float2 v = *p;
+    return make_double2((double)v.x, (double)v.y);
+}
+
+template <class P>
+__global__ void k_combine(const FormSpec *fs, BoxSpec box, const P *__restrict__ part,
                           int32_t nslice, const int32_t *__restrict__ istl,
                           const double2 *__restrict__ cfact, const double2 *__restrict__ acsf,
                           double2 *__restrict__ csf, double *__restrict__ dsi, double ds, double sqds)
@@ -59,9 +67,9 @@ __global__ void k_combine(const FormSpec *fs, BoxSpec box, const double2 *__rest
     double2 F = make_double2(0.0, 0.0);
     for (int t = 1; t <= fs->nscat; t++) {
         double2 s = make_double2(0.0, 0.0);
-        const double2 *pt = part + (int64_t)(t - 1) * nslice * nb + pb;
+        const P *pt = part + (int64_t)(t - 1) * nslice * nb + pb;
         for (int k = 0; k < nslice; k++) {
-            double2 v = pt[(int64_t)k * nb];
+            double2 v = ld_part(pt + (int64_t)k * nb);
             s.x += v.x;
             s.y += v.y;
         }
@@ -90,7 +98,8 @@ __device__ __forceinline__ double2 geom_series(double x, int32_t n)
     return make_double2(r * cp, r * sp);
 }
 
-__global__ void k_aver_combine(const FormSpec *fs, BoxSpec box, const double2 *__restrict__ apart,
+template <class P>
+__global__ void k_aver_combine(const FormSpec *fs, BoxSpec box, const P *__restrict__ apart,
                                int32_t anslice, const int32_t *__restrict__ istl,
                                const double2 *__restrict__ cfact, const double2 *__restrict__ lat,
                                int32_t lat_nslice, int32_t lat_closed, int32_t c0, int32_t c1,
@@ -109,9 +118,9 @@ __global__ void k_aver_combine(const FormSpec *fs, BoxSpec box, const double2 *_
     double2 A = make_double2(0.0, 0.0);
     for (int t = 1; t <= fs->nscat; t++) {
         double2 s = make_double2(0.0, 0.0);
-        const double2 *pt = apart + (int64_t)(t - 1) * anslice * nb + pb;
+        const P *pt = apart + (int64_t)(t - 1) * anslice * nb + pb;
         for (int k = 0; k < anslice; k++) {
-            double2 v = pt[(int64_t)k * nb];
+            double2 v = ld_part(pt + (int64_t)k * nb);
             s.x += v.x;
             s.y += v.y;
         }
@@ -269,23 +278,28 @@ static int upload_formspec(dgpu_ctx *ctx, const FormSpec &fs, FormSpec **d)
     return DGPU_OK;
 }
 
-int dgpu_combine(dgpu_ctx *ctx, const FormSpec &fs, const BoxSpec &box, const double2 *part,
-                 int32_t nslice, const int32_t *istl, const double2 *cfact,
+int dgpu_combine(dgpu_ctx *ctx, const FormSpec &fs, const BoxSpec &box, const PartRef &part,
+                 const int32_t *istl, const double2 *cfact,
                  const double2 *acsf_in, double2 *csf, double *dsi, double diff_scale)
 {
     FormSpec *d;
     int rc = upload_formspec(ctx, fs, &d);
     if (rc) return rc;
     int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
-    k_combine<<<(unsigned)dgpu_cdiv(nb, 256), 256, 0, ctx->stream>>>(d, box, part, nslice, istl, cfact, acsf_in,
-                                                                      csf, dsi, diff_scale, sqrt(diff_scale));
+    const unsigned nblk = (unsigned)dgpu_cdiv(nb, 256);
+    if (part.f32)
+        k_combine<float2><<<nblk, 256, 0, ctx->stream>>>(d, box, (const float2 *)part.p, part.nslice, istl, cfact,
+                                                          acsf_in, csf, dsi, diff_scale, sqrt(diff_scale));
+    else
+        k_combine<double2><<<nblk, 256, 0, ctx->stream>>>(d, box, (const double2 *)part.p, part.nslice, istl, cfact,
+                                                           acsf_in, csf, dsi, diff_scale, sqrt(diff_scale));
     DGPU_CUDA(ctx, cudaGetLastError());
     DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));   // FormSpec block reused next
     return DGPU_OK;
 }
 
-int dgpu_aver_combine(dgpu_ctx *ctx, const FormSpec &fs, const BoxSpec &box, const double2 *apart,
-                      int32_t anslice, const int32_t *istl, const double2 *cfact, const double2 *lat,
+int dgpu_aver_combine(dgpu_ctx *ctx, const FormSpec &fs, const BoxSpec &box, const PartRef &apart,
+                      const int32_t *istl, const double2 *cfact, const double2 *lat,
                       int32_t lat_nslice, int32_t lat_closed, const int32_t icc[3],
                       const double dim0[3], double norm, double2 *acsf)
 {
@@ -293,9 +307,15 @@ int dgpu_aver_combine(dgpu_ctx *ctx, const FormSpec &fs, const BoxSpec &box, con
     int rc = upload_formspec(ctx, fs, &d);
     if (rc) return rc;
     int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
-    k_aver_combine<<<(unsigned)dgpu_cdiv(nb, 256), 256, 0, ctx->stream>>>(
-        d, box, apart, anslice, istl, cfact, lat, lat_nslice, lat_closed, icc[0], icc[1], icc[2],
-        dim0[0], dim0[1], dim0[2], norm, acsf);
+    const unsigned nblk = (unsigned)dgpu_cdiv(nb, 256);
+    if (apart.f32)
+        k_aver_combine<float2><<<nblk, 256, 0, ctx->stream>>>(
+            d, box, (const float2 *)apart.p, apart.nslice, istl, cfact, lat, lat_nslice, lat_closed, icc[0], icc[1],
+            icc[2], dim0[0], dim0[1], dim0[2], norm, acsf);
+    else
+        k_aver_combine<double2><<<nblk, 256, 0, ctx->stream>>>(
+            d, box, (const double2 *)apart.p, apart.nslice, istl, cfact, lat, lat_nslice, lat_closed, icc[0], icc[1],
+            icc[2], dim0[0], dim0[1], dim0[2], norm, acsf);
     DGPU_CUDA(ctx, cudaGetLastError());
     DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return DGPU_OK;

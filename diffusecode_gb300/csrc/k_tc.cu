@@ -12,9 +12,17 @@
 // fixed-point phases (no operand traffic in HBM), splits every FP32 phasor
 // value into fp16 (or bf16) hi + lo, and issues per 16 atoms the 12 MMAs
 //     Re += Ur Vr^T - Ui Vi^T ,  Im += Ur Vi^T + Ui Vr^T
-// for the split products (hi,hi), (hi,lo), (lo,hi).  Partial sums of one
-// work item (FP32 in TMEM) go to global memory as double2, and the combine
-// kernel adds the K slices in FP64.
+// for the split products (hi,hi), (hi,lo), (lo,hi).
+//
+// Accumulation.  Every MMA truncates its FP32 accumulator by about one ulp,
+// so the error of one TMEM accumulator grows with the number of MMAs chained
+// into it.  The large (hi,hi) products therefore go to a "main" accumulator
+// that is drained every `flush` stages (flush*32 atoms) into the work item's
+// FP32 partial in global memory (round-to-nearest adds on CUDA cores, the
+// partial stays in L2), and the small (hi,lo)+(lo,hi) corrections go to a
+// separate accumulator drained once per work item.  With nbuf = 2 the main
+// accumulator is double-buffered so the drain overlaps the next chunk.  The
+// combine kernel adds the K slices of all work items in FP64.
 //
 // Warp roles (416 threads): warps 0-7 produce operand stages, warp 8 owns
 // TMEM and issues the MMAs (one elected lane), warps 9-12 drain TMEM.  All
@@ -40,16 +48,21 @@
 #define TC_SBO ((TC_KA / 8) * 128)
 #define TC_LBO 128
 #define TC_TIMEOUT_NS 2000000000ull            // 2 s per wait
+#ifndef TC_FLUSH_STAGES
+#define TC_FLUSH_STAGES 16                     // 512 atoms per drain of the main accumulator
+#endif
 
 struct TcGeom {
     int32_t f[3];
     int32_t ra, rb, ac, fra;
     int64_t sra, srb, sac;   // box-index strides of the row and column axes
     int32_t nrows, ncols;
-    int32_t N;               // columns per tile (multiple of 16, <= 256)
+    int32_t N;               // columns per tile (multiple of 16, <= 128)
     int32_t m_tiles, n_tiles, nslice, ntype;
     int64_t slice_len, nitems, pbox;
     int32_t stages;
+    int32_t flush;           // stages per drain of the main accumulator
+    int32_t nbuf;            // main accumulator buffers in TMEM (1 or 2)
     int32_t bf16;
     uint32_t tmem_cols;
     int64_t ts[65];
@@ -153,8 +166,12 @@ __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.
 // exp(2 pi i phase) from the top 32 bits of a 64-bit fixed-point turn
 __device__ __forceinline__ void phasor(uint64_t ph, float &c, float &s)
 {
+#ifdef TC_PHASOR_ACCURATE
+    sincospif((float)(int32_t)(ph >> 32) * 4.656612873077393e-10f, &s, &c);
+#else
     float ang = (float)(int32_t)(ph >> 32) * 1.4629180792671596e-09f;   // 2 pi / 2^32
     __sincosf(ang, &s, &c);
+#endif
 }
 
 __device__ __forceinline__ uint32_t pack2(float a, float b, bool bf)
@@ -198,7 +215,7 @@ struct TcArgs {
     const uint64_t *ph0;
     const uint64_t *dra, *drb, *dac;   // increments along the row axes and the column axis
     const float *w;
-    double2 *part;
+    float2 *part;
     int32_t *err;
 };
 
@@ -221,9 +238,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcGeom g, const TcAr
     const uint32_t stage_bytes = 4 * TC_A_BYTES + 4 * b_bytes;
     uint64_t *full = reinterpret_cast<uint64_t *>(smem + (size_t)S * stage_bytes);
     uint64_t *empty = full + S;
-    uint64_t *tfull = empty + S;
-    uint64_t *tempty = tfull + 1;
-    uint64_t *drain = tempty + 1;
+    uint64_t *mfull = empty + S;      // [2] main accumulator b ready
+    uint64_t *mempty = mfull + 2;     // [2] main accumulator b drained
+    uint64_t *cfull = mempty + 2;     // correction accumulator ready (end of item)
+    uint64_t *cempty = cfull + 1;     // correction accumulator drained
+    uint64_t *drain = cempty + 1;
     uint32_t *tbase = reinterpret_cast<uint32_t *>(drain + 1);
     volatile int32_t *err = args.err;
     const bool bf = g.bf16 != 0;
@@ -234,8 +253,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcGeom g, const TcAr
             mbar_init(&full[s], TC_PROD_THREADS);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(tfull, 1);
-        mbar_init(tempty, 4 * 32);
+        for (int b = 0; b < 2; b++) {
+            mbar_init(&mfull[b], 1);
+            mbar_init(&mempty[b], 4 * 32);
+        }
+        mbar_init(cfull, 1);
+        mbar_init(cempty, 4 * 32);
         mbar_init(drain, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -339,9 +362,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcGeom g, const TcAr
         const uint32_t fmt = bf ? 1u : 0u;
         const uint32_t idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(N >> 3) << 17) |
                                ((uint32_t)(TC_M >> 4) << 24);
-        const uint32_t idesc_neg = idesc | (1u << 13);     // negate A: the -Ui Vi^T product
-        const uint32_t d_re = tmem, d_im = tmem + (uint32_t)N;
-        uint32_t it = 0, nitem = 0;
+        const uint32_t idesc_neg = idesc | (1u << 13);     // negate A: the -Ui Vi^T products
+        const uint32_t c_re = tmem, c_im = tmem + (uint32_t)N;  // correction accumulator
+        uint32_t it = 0, nitem = 0, nchunk = 0;
         bool ok = true, issued = false;
         for (int64_t item = blockIdx.x; item < g.nitems && ok; item += gridDim.x) {
             int t, ks, nt, mt;
@@ -351,47 +374,62 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcGeom g, const TcAr
             const int64_t cnt = a1 > a0 ? a1 - a0 : 0;
             const int nst = (int)((cnt + TC_KA - 1) / TC_KA);
             if (nst == 0) continue;
-            if (nitem > 0 && !mbar_wait(tempty, (nitem - 1) & 1, err, 2)) { ok = false; break; }
-            tc_fence_after();
-            for (int st = 0; st < nst; st++, it++) {
-                const int s = it % S;
-                if (!mbar_wait(&full[s], (it / S) & 1, err, 3)) { ok = false; break; }
+            // the correction accumulator restarts with this item: previous one drained?
+            if (nitem > 0 && !mbar_wait(cempty, (nitem - 1) & 1, err, 2)) { ok = false; break; }
+            for (int st0 = 0; st0 < nst && ok; st0 += g.flush, nchunk++) {
+                const int b = (int)(nchunk % g.nbuf);
+                const uint32_t use = nchunk / g.nbuf;
+                if (use > 0 && !mbar_wait(&mempty[b], (use - 1) & 1, err, 6)) { ok = false; break; }
                 tc_fence_after();
-                if (lane == 0) {
-                    const uint32_t A = smem_u32(smem + (size_t)s * stage_bytes);
-                    const uint32_t B = A + 4 * TC_A_BYTES;
+                const uint32_t m_re = tmem + 2u * N * (1u + (uint32_t)b), m_im = m_re + (uint32_t)N;
+                const int st1 = min(nst, st0 + g.flush);
+                for (int st = st0; st < st1; st++, it++) {
+                    const int s = it % S;
+                    if (!mbar_wait(&full[s], (it / S) & 1, err, 3)) { ok = false; break; }
+                    tc_fence_after();
+                    if (lane == 0) {
+                        const uint32_t A = smem_u32(smem + (size_t)s * stage_bytes);
+                        const uint32_t B = A + 4 * TC_A_BYTES;
 #pragma unroll
-                    for (int kk = 0; kk < TC_KA / 16; kk++) {
-                        const uint32_t ko = kk * 2 * TC_LBO;
-                        const uint64_t ar[2] = {sdesc(A + 0 * TC_A_BYTES + ko), sdesc(A + 1 * TC_A_BYTES + ko)};
-                        const uint64_t ai[2] = {sdesc(A + 2 * TC_A_BYTES + ko), sdesc(A + 3 * TC_A_BYTES + ko)};
-                        const uint64_t br[2] = {sdesc(B + 0 * b_bytes + ko), sdesc(B + 1 * b_bytes + ko)};
-                        const uint64_t bi[2] = {sdesc(B + 2 * b_bytes + ko), sdesc(B + 3 * b_bytes + ko)};
-#pragma unroll
-                        for (int p = 0; p < 3; p++) {
-                            const int x = p == 2 ? 1 : 0;     // A: hi, hi, lo
-                            const int y = p == 1 ? 1 : 0;     // B: hi, lo, hi
-                            const uint32_t acc = (st > 0 || kk > 0 || p > 0) ? 1u : 0u;
-                            mma_f16(d_re, ar[x], br[y], idesc, acc);
-                            mma_f16(d_re, ai[x], bi[y], idesc_neg, 1u);
-                            mma_f16(d_im, ar[x], bi[y], idesc, acc);
-                            mma_f16(d_im, ai[x], br[y], idesc, 1u);
+                        for (int kk = 0; kk < TC_KA / 16; kk++) {
+                            const uint32_t ko = kk * 2 * TC_LBO;
+                            const uint64_t arh = sdesc(A + 0 * TC_A_BYTES + ko), arl = sdesc(A + 1 * TC_A_BYTES + ko);
+                            const uint64_t aih = sdesc(A + 2 * TC_A_BYTES + ko), ail = sdesc(A + 3 * TC_A_BYTES + ko);
+                            const uint64_t brh = sdesc(B + 0 * b_bytes + ko), brl = sdesc(B + 1 * b_bytes + ko);
+                            const uint64_t bih = sdesc(B + 2 * b_bytes + ko), bil = sdesc(B + 3 * b_bytes + ko);
+                            const uint32_t am = (st > st0 || kk > 0) ? 1u : 0u;   // main restarts per chunk
+                            const uint32_t ac = (st > 0 || kk > 0) ? 1u : 0u;     // correction per item
+                            // main: (hi,hi)
+                            mma_f16(m_re, arh, brh, idesc, am);
+                            mma_f16(m_re, aih, bih, idesc_neg, 1u);
+                            mma_f16(m_im, arh, bih, idesc, am);
+                            mma_f16(m_im, aih, brh, idesc, 1u);
+                            // corrections: (hi,lo) and (lo,hi)
+                            mma_f16(c_re, arh, brl, idesc, ac);
+                            mma_f16(c_re, aih, bil, idesc_neg, 1u);
+                            mma_f16(c_re, arl, brh, idesc, 1u);
+                            mma_f16(c_re, ail, bih, idesc_neg, 1u);
+                            mma_f16(c_im, arh, bil, idesc, ac);
+                            mma_f16(c_im, aih, brl, idesc, 1u);
+                            mma_f16(c_im, arl, bih, idesc, 1u);
+                            mma_f16(c_im, ail, brh, idesc, 1u);
                         }
+                        mma_commit(&empty[s]);
+                        issued = true;
                     }
-                    mma_commit(&empty[s]);
-                    issued = true;
+                    __syncwarp();
                 }
+                if (!ok) break;
+                if (lane == 0) mma_commit(&mfull[b]);
                 __syncwarp();
             }
             if (!ok) break;
-            if (lane == 0) mma_commit(tfull);
+            if (lane == 0) mma_commit(cfull);
             __syncwarp();
             nitem++;
         }
         // make sure no MMA of this CTA is still running before TMEM is freed
-        if (lane == 0 && issued) {
-            mma_commit(drain);
-        }
+        if (lane == 0 && issued) mma_commit(drain);
         __syncwarp();
         if (__shfl_sync(0xffffffffu, issued ? 1 : 0, 0)) mbar_wait(drain, 0, err, 4);
         tc_fence_before();
@@ -399,46 +437,78 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcGeom g, const TcAr
         // ------------------------------------------------------------ epilogue
         const int q = warp & 3;                       // TMEM lane quadrant of this warp
         const int r = q * 32 + lane;
-        uint32_t nitem = 0;
+        uint32_t nitem = 0, nchunk = 0;
         bool ok = true;
         for (int64_t item = blockIdx.x; item < g.nitems && ok; item += gridDim.x) {
             int t, ks, nt, mt;
             decode_item(g, item, t, ks, nt, mt);
             const int64_t a0 = g.ts[t] + (int64_t)ks * g.slice_len;
             const int64_t a1 = min(g.ts[t + 1], a0 + g.slice_len);
-            const bool has = a1 > a0;
-            if (has) {
-                if (!mbar_wait(tfull, nitem & 1, err, 5)) { ok = false; break; }
-                tc_fence_after();
-            }
+            const int64_t cnt = a1 > a0 ? a1 - a0 : 0;
+            const int nst = (int)((cnt + TC_KA - 1) / TC_KA);
             const int64_t rg = (int64_t)mt * TC_M + r;
             const bool rv = rg < g.nrows;
             const int64_t prow = rv ? (rg % g.fra) * g.sra + (rg / g.fra) * g.srb : 0;
-            double2 *out = args.part + ((int64_t)t * g.nslice + ks) * g.pbox + prow;
-            for (int c0 = 0; c0 < N; c0 += 16) {
-                uint32_t vr[16], vi[16];
-                if (has) {
-                    const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
+            float2 *out = args.part + ((int64_t)t * g.nslice + ks) * g.pbox + prow;
+            const int64_t cbase0 = (int64_t)nt * N;
+            if (nst == 0) {
+                if (rv)
+                    for (int c = 0; c < N && cbase0 + c < g.ncols; c++) out[(cbase0 + c) * g.sac] = make_float2(0.f, 0.f);
+                continue;
+            }
+            // main accumulator, one chunk at a time: first chunk stores, later chunks add
+            for (int st0 = 0; st0 < nst; st0 += g.flush, nchunk++) {
+                const int b = (int)(nchunk % g.nbuf);
+                if (!mbar_wait(&mfull[b], (nchunk / g.nbuf) & 1, err, 5)) { ok = false; break; }
+                tc_fence_after();
+                const uint32_t col0 = 2u * N * (1u + (uint32_t)b);
+                for (int c0 = 0; c0 < N; c0 += 16) {
+                    uint32_t vr[16], vi[16];
+                    const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + col0 + (uint32_t)c0;
                     tmem_ld16(ta, vr);
                     tmem_ld16(ta + (uint32_t)N, vi);
                     tmem_wait_ld();
-                } else {
 #pragma unroll
-                    for (int k = 0; k < 16; k++) vr[k] = vi[k] = 0u;
+                    for (int k = 0; k < 16; k++) {
+                        const int64_t cg = cbase0 + c0 + k;
+                        if (rv && cg < g.ncols) {
+                            float2 v = make_float2(__uint_as_float(vr[k]), __uint_as_float(vi[k]));
+                            float2 *o = out + cg * g.sac;
+                            if (st0 > 0) {
+                                float2 old = *o;
+                                v.x += old.x;
+                                v.y += old.y;
+                            }
+                            *o = v;
+                        }
+                    }
                 }
-                const int64_t cbase = (int64_t)nt * N + c0;
+                tc_fence_before();
+                mbar_arrive(&mempty[b]);
+            }
+            if (!ok) break;
+            // correction accumulator of the item
+            if (!mbar_wait(cfull, nitem & 1, err, 7)) { ok = false; break; }
+            tc_fence_after();
+            for (int c0 = 0; c0 < N; c0 += 16) {
+                uint32_t vr[16], vi[16];
+                const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
+                tmem_ld16(ta, vr);
+                tmem_ld16(ta + (uint32_t)N, vi);
+                tmem_wait_ld();
 #pragma unroll
                 for (int k = 0; k < 16; k++) {
-                    if (rv && cbase + k < g.ncols)
-                        out[(cbase + k) * g.sac] =
-                            make_double2((double)__uint_as_float(vr[k]), (double)__uint_as_float(vi[k]));
+                    const int64_t cg = cbase0 + c0 + k;
+                    if (rv && cg < g.ncols) {
+                        float2 *o = out + cg * g.sac;
+                        float2 old = *o;
+                        *o = make_float2(old.x + __uint_as_float(vr[k]), old.y + __uint_as_float(vi[k]));
+                    }
                 }
             }
-            if (has) {
-                tc_fence_before();
-                mbar_arrive(tempty);
-                nitem++;
-            }
+            tc_fence_before();
+            mbar_arrive(cempty);
+            nitem++;
         }
     }
     __syncthreads();
@@ -472,28 +542,30 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
                  const dgpu_opts *op, DevBuf &part, int32_t *nslice_out)
 {
     if (ntype < 1 || ntype > 64) return dgpu_set_error(ctx, DGPU_ERR_ARG, "ntype=%d", ntype);
+    const int want_n = op->tc_tile_n;
+    if (want_n && (want_n % 16 || want_n < 16 || want_n > 128))
+        return dgpu_set_error(ctx, DGPU_ERR_ARG, "tc_tile_n=%d (multiple of 16 in 16..128)", want_n);
     TcGeom g;
     memset(&g, 0, sizeof(g));
     for (int k = 0; k < 3; k++) g.f[k] = box.f[k];
-    // column axis: the one whose tile padding wastes least, longer axis on ties
-    int ac = -1;
-    double best = 1e30;
-    int want_n = op->tc_tile_n;
+    const int64_t npts = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    // column axis and tile width: least padded MMA area, with the operand
+    // generation of the V tile (N per 128 rows) counted as extra work
+    int ac = 0, bestN = 16, best_tiles = 1;
+    double best = 1e300;
     for (int a = 0; a < 3; a++) {
-        if (box.f[a] < 2 && !(box.f[0] * box.f[1] * box.f[2] == box.f[a])) continue;
-        int n = box.f[a];
-        int tiles = (int)dgpu_cdiv(n, 256);
-        int N = (int)dgpu_cdiv(dgpu_cdiv(n, tiles), 16) * 16;
-        if (want_n > 0) {
-            N = want_n;
-            tiles = (int)dgpu_cdiv(n, N);
+        const int n = box.f[a];
+        if (n < 2 && npts != n) continue;
+        const int64_t rows = npts / n;
+        for (int N = 16; N <= 128; N += 16) {
+            if (want_n && N != want_n) continue;
+            const int64_t tiles = dgpu_cdiv(n, N);
+            double area = (double)tiles * N * dgpu_cdiv(rows, TC_M) * TC_M;
+            double cost = area * (1.0 + (double)(TC_M + N) / (TC_M * N) * 24.0);
+            if (6 * N > 512) cost *= 1.10;        // single-buffered main accumulator stalls on drains
+            if (cost < best * (1 - 1e-9)) { best = cost; ac = a; bestN = N; best_tiles = (int)tiles; }
         }
-        int64_t rows = (int64_t)box.f[0] * box.f[1] * box.f[2] / n;
-        double cost = (double)tiles * N * dgpu_cdiv(rows, TC_M) * TC_M;   // padded MMA area
-        cost *= (1.0 + 16.0 / N);                                         // operand-generation overhead
-        if (cost < best - 1e-9) { best = cost; ac = a; }
     }
-    if (ac < 0) ac = 0;
     g.ac = ac;
     g.ra = ac == 0 ? 1 : 0;
     g.rb = 3 - ac - g.ra;
@@ -506,18 +578,14 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
         g.sac = stride[ac];
     }
     g.nrows = box.f[g.ra] * box.f[g.rb];
-    g.n_tiles = (int32_t)dgpu_cdiv(g.ncols, 256);
-    g.N = (int32_t)(dgpu_cdiv(dgpu_cdiv(g.ncols, g.n_tiles), 16) * 16);
-    if (want_n > 0) {
-        if (want_n % 16 || want_n < 16 || want_n > 256)
-            return dgpu_set_error(ctx, DGPU_ERR_ARG, "tc_tile_n=%d (multiple of 16 in 16..256)", want_n);
-        g.N = want_n;
-        g.n_tiles = (int32_t)dgpu_cdiv(g.ncols, g.N);
-    }
+    g.N = bestN;
+    g.n_tiles = best_tiles;
+    g.nbuf = 6 * g.N <= 512 ? 2 : 1;
     g.m_tiles = (int32_t)dgpu_cdiv(g.nrows, TC_M);
-    g.pbox = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    g.pbox = npts;
     g.ntype = ntype;
     g.bf16 = op->split == DGPU_SPLIT_BF16;
+    g.flush = TC_FLUSH_STAGES;
     int64_t maxn = 0;
     for (int t = 0; t < ntype; t++) {
         g.ts[t] = h_type_start[t];
@@ -525,27 +593,28 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
         maxn = n > maxn ? n : maxn;
     }
     g.ts[ntype] = h_type_start[ntype];
-    // K slices: enough work items for all SMs, at most tc_kslice atoms each
-    int64_t tiles = (int64_t)g.m_tiles * g.n_tiles * ntype;
-    int64_t nsl = dgpu_cdiv(4LL * ctx->nsm, tiles);
-    int64_t max_len = op->tc_kslice > 0 ? op->tc_kslice : 32768;
-    if (nsl < dgpu_cdiv(maxn, max_len)) nsl = dgpu_cdiv(maxn, max_len);
-    int64_t min_len = 1024;
-    if (nsl > 1 && dgpu_cdiv(maxn, nsl) < min_len) nsl = dgpu_cdiv(maxn, min_len);
+    // K slices: about 4 work items per SM, or tc_kslice atoms each when given
+    const int64_t tiles = (int64_t)g.m_tiles * g.n_tiles * ntype;
+    int64_t nsl;
+    if (op->tc_kslice > 0) {
+        nsl = dgpu_cdiv(maxn, op->tc_kslice);
+    } else {
+        nsl = dgpu_cdiv(4LL * ctx->nsm, tiles);
+        if (nsl > 1 && dgpu_cdiv(maxn, nsl) < 2048) nsl = dgpu_cdiv(maxn, 2048);
+    }
     if (nsl < 1) nsl = 1;
-    g.slice_len = dgpu_cdiv(maxn > 0 ? maxn : 1, nsl);
-    g.slice_len = dgpu_cdiv(g.slice_len, TC_KA) * TC_KA;
+    g.slice_len = dgpu_cdiv(dgpu_cdiv(maxn > 0 ? maxn : 1, nsl), TC_KA) * TC_KA;
     g.nslice = (int32_t)dgpu_cdiv(maxn > 0 ? maxn : 1, g.slice_len);
     g.nitems = tiles * g.nslice;
     const uint32_t stage_bytes = 4 * TC_A_BYTES + 4u * g.N * TC_KA * 2;
     const uint32_t bar_bytes = 256;
     int stages = (int)((200 * 1024 - bar_bytes) / stage_bytes);
     g.stages = stages > 4 ? 4 : stages;
-    if (g.stages < 2) return dgpu_set_error(ctx, DGPU_ERR_ARG, "tile too large for shared memory");
-    g.tmem_cols = pow2_cols(2 * g.N);
+    g.tmem_cols = pow2_cols(2 * g.N * (1 + g.nbuf));
+    if (g.stages < 2 || g.tmem_cols > 512) return dgpu_set_error(ctx, DGPU_ERR_ARG, "tile does not fit");
     size_t smem = (size_t)g.stages * stage_bytes + bar_bytes;
 
-    DGPU_CUDA(ctx, part.ensure((size_t)ntype * g.nslice * g.pbox * sizeof(double2)));
+    DGPU_CUDA(ctx, part.ensure((size_t)ntype * g.nslice * g.pbox * sizeof(float2)));
     DGPU_CUDA(ctx, ctx->flag.ensure(64));
     int32_t *d_err = ctx->flag.as<int32_t>() + 8;
     DGPU_CUDA(ctx, cudaMemsetAsync(d_err, 0, sizeof(int32_t), ctx->stream));
@@ -556,7 +625,7 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
     args.drb = dd[g.rb];
     args.dac = dd[g.ac];
     args.w = w;
-    args.part = part.as<double2>();
+    args.part = part.as<float2>();
     args.err = d_err;
     static bool attr_set = false;
     if (!attr_set) {

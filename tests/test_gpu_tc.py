@@ -32,7 +32,7 @@ def test_tc_random_vs_oracle(oracle, ctx, inc, natoms):
         assert K.rel_err(r.dsi, dsi, K.incoherent_floor(cr, g, op)) <= TOL
 
 
-@pytest.mark.parametrize("tile_n,kslice", [(16, 1024), (64, 2048), (208, 0), (256, 1024)])
+@pytest.mark.parametrize("tile_n,kslice", [(16, 1024), (64, 2048), (112, 0), (128, 96), (80, 4096)])
 def test_tc_tiles_and_slices(oracle, ctx, tile_n, kslice):
     cr, g = S.perovskite_plane(cells=6)
     op = tc_opts(tc_tile_n=tile_n, tc_kslice=kslice)
