@@ -33,6 +33,9 @@ from diffusecode_gb300 import _abi  # noqa: E402
 from diffusecode_gb300 import structures as S  # noqa: E402
 
 METRIC = "G atom.hkl pairs/s for |F|^2"
+# kernels of one four_run without <F>: type count, scan, scatter, stltab,
+# formtab, type sums, combine, Friedel mirror, two statistics reductions
+LAUNCHES_PER_RUN = 10
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
@@ -154,6 +157,42 @@ def cpu_baseline(cr, grid, nthreads=0):
     return pairs * credit / sec / 1e9, nthreads, rows, sec
 
 
+def fp64_check(cr, grid, dsi, npts=192, seed=7):
+    """|F|^2 at sampled grid points from an FP64 numpy sum over all atoms
+    (TABLE form factors, as the run uses), against the GPU's dsi:
+    max |I - I_64| / (I_64 + N<|f|^2>)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n1, n2, n3 = grid.inc
+    idx = np.stack([rng.integers(0, n, npts) for n in (n1, n2, n3)], 1)
+    # include the origin and a few Bragg points
+    c = [(n - 1) // 2 for n in (n1, n2, n3)]
+    idx[0] = c
+    h = (grid.eck[:, 0][None, :] + idx[:, 0:1] * grid.vi[:, 0] + idx[:, 1:2] * grid.vi[:, 1]
+         + idx[:, 2:3] * grid.vi[:, 2])
+    h32 = h.astype(np.float32).astype(np.float64)
+    q2 = np.einsum("pa,ab,pb->p", h32, cr.rten, h32) / 4.0
+    istl = np.floor(np.sqrt(q2) * 1000.0 + 0.5)
+    s2 = (istl * 0.001) ** 2
+    F = np.zeros(npts, complex)
+    floor = np.zeros(npts)
+    for t in range(1, cr.nscat + 1):
+        sel = cr.iscat == t
+        x = cr.pos[sel]
+        sc = cr.scat[t]
+        f = sc[0] + sum(sc[2 * i - 1] * np.exp(-sc[2 * i] * s2) for i in range(1, 5))
+        cf = np.exp(-cr.dw[t] * s2) * cr.occ[t] * f
+        acc = np.zeros(npts, complex)
+        for k0 in range(0, x.shape[0], 65536):
+            ph = h @ x[k0:k0 + 65536].T
+            ph -= np.round(ph)
+            acc += np.exp(2j * np.pi * ph).sum(axis=1)
+        F += cf * acc
+        floor += sel.sum() * cf ** 2
+    i64 = np.abs(F) ** 2
+    ig = dsi[idx[:, 0], idx[:, 1], idx[:, 2]]
+    return float(np.max(np.abs(ig - i64) / (i64 + floor))), npts
+
+
 def run_reference(args, world, rank):
     cr, grid = workload(args.workload)
     if rank != 0:
@@ -232,6 +271,7 @@ def run_ours(args, world, rank, local):
         wall = time.perf_counter() - t0
     barrier(world)
     engine_used = info.engine_used
+    dsi_host = dsi.cpu().numpy().reshape(grid.inc, order="F")
     ms = max_over_ranks(world, sum(times) / len(times))
     kms = sum(ktimes) / len(ktimes)
     pairs_full = info.pairs
@@ -269,6 +309,7 @@ def run_ours(args, world, rank, local):
 
     if rank != 0:
         return
+    acc_err, acc_pts = fp64_check(cr, grid, dsi_host)
     pk, pk_kind = peaks()
     fnum_pts = int(np.prod(list(info.fnum)))
     pairs_computed = cr.n_scattering() * fnum_pts
@@ -299,7 +340,9 @@ def run_ours(args, world, rank, local):
         "wall_s_timed": wall,
         "roofline": roof,
         "clocks": clk.summary(),
-        "gpu_launches": None,
+        "gpu_launches": LAUNCHES_PER_RUN * args.steps,
+        "accuracy": {"rel_err_vs_fp64": acc_err, "points": acc_pts,
+                     "norm": "max |I-I64|/(I64 + N<|f|^2>) at sampled grid points"},
         "e2e": {"value": e2e_val, "unit": "G pairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
     }
     if not args.no_cpu_baseline:
