@@ -83,6 +83,7 @@ class Opts(C.Structure):
         ("split", C.c_int32),
         ("tc_tile_n", C.c_int32),
         ("tc_kslice", C.c_int32),
+        ("tc_flush", C.c_int32),
         ("cancel", C.POINTER(C.c_int32)),
     ]
 
@@ -143,6 +144,7 @@ def default_opts(**kw):
     o.split = SPLIT_F16
     o.tc_tile_n = 0
     o.tc_kslice = 0
+    o.tc_flush = 0
     o.cancel = C.cast(None, C.POINTER(C.c_int32))
     for k, v in kw.items():
         if k == "aver_cells":

@@ -194,15 +194,24 @@ __device__ __forceinline__ float2 unpack2(uint32_t u, bool bf)
     return __half22float2(v);
 }
 
-// 8 values -> hi (rounded) and lo (remainder, rounded) packed as 16 bytes each
+// 8 values -> hi (rounded) and lo (remainder x 2^12, rounded), 16 bytes each.
+// hi is zero or a normal number; the remainder is scaled by 2^12 so that it
+// stays normal in fp16 as well (tensor-core inputs below 2^-14 would
+// otherwise lose their bits); the correction accumulator, which only ever
+// receives products with one lo factor, is scaled back by 2^-12.
+#define TC_LO_SCALE 4096.0f
+#define TC_LO_UNSCALE (1.0f / 4096.0f)
 __device__ __forceinline__ void split8(const float (&v)[8], uint4 &hi, uint4 &lo, bool bf)
 {
     uint32_t h[4], l[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        h[k] = pack2(v[2 * k], v[2 * k + 1], bf);
+        const float x0 = v[2 * k], x1 = v[2 * k + 1];
+        const float y0 = fabsf(x0) < 6.103515625e-05f ? 0.f : x0;     // 2^-14: smallest normal fp16
+        const float y1 = fabsf(x1) < 6.103515625e-05f ? 0.f : x1;
+        h[k] = pack2(y0, y1, bf);
         float2 b = unpack2(h[k], bf);
-        l[k] = pack2(v[2 * k] - b.x, v[2 * k + 1] - b.y, bf);
+        l[k] = pack2((x0 - b.x) * TC_LO_SCALE, (x1 - b.y) * TC_LO_SCALE, bf);
     }
     hi = make_uint4(h[0], h[1], h[2], h[3]);
     lo = make_uint4(l[0], l[1], l[2], l[3]);
@@ -502,7 +511,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcGeom g, const TcAr
                     if (rv && cg < g.ncols) {
                         float2 *o = out + cg * g.sac;
                         float2 old = *o;
-                        *o = make_float2(old.x + __uint_as_float(vr[k]), old.y + __uint_as_float(vi[k]));
+                        *o = make_float2(fmaf(__uint_as_float(vr[k]), TC_LO_UNSCALE, old.x),
+                                         fmaf(__uint_as_float(vi[k]), TC_LO_UNSCALE, old.y));
                     }
                 }
             }
@@ -585,7 +595,7 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
     g.pbox = npts;
     g.ntype = ntype;
     g.bf16 = op->split == DGPU_SPLIT_BF16;
-    g.flush = TC_FLUSH_STAGES;
+    g.flush = op->tc_flush > 0 ? (int32_t)dgpu_cdiv(op->tc_flush, TC_KA) : TC_FLUSH_STAGES;
     int64_t maxn = 0;
     for (int t = 0; t < ntype; t++) {
         g.ts[t] = h_type_start[t];
