@@ -49,7 +49,7 @@
 #define TC_LBO 128
 #define TC_TIMEOUT_NS 2000000000ull            // 2 s per wait
 #ifndef TC_FLUSH_STAGES
-#define TC_FLUSH_STAGES 16                     // 512 atoms per drain of the main accumulator
+#define TC_FLUSH_STAGES 4                      // 128 atoms per drain of the main accumulator
 #endif
 
 struct TcGeom {
@@ -572,7 +572,7 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
             const int64_t tiles = dgpu_cdiv(n, N);
             double area = (double)tiles * N * dgpu_cdiv(rows, TC_M) * TC_M;
             double cost = area * (1.0 + (double)(TC_M + N) / (TC_M * N) * 24.0);
-            if (6 * N > 512) cost *= 1.10;        // single-buffered main accumulator stalls on drains
+            if (6 * N > 512) cost *= 1.6;         // single-buffered main accumulator stalls on drains
             if (cost < best * (1 - 1e-9)) { best = cost; ac = a; bestN = N; best_tiles = (int)tiles; }
         }
     }

@@ -113,7 +113,7 @@ typedef struct dgpu_opts {
     int32_t split;          /* DGPU_SPLIT_* (tensor-core engine)                    */
     int32_t tc_tile_n;      /* tensor-core N tile in points (0 = autotuned)         */
     int32_t tc_kslice;      /* atoms per tensor-core work item (0 = autotuned)      */
-    int32_t tc_flush;       /* atoms per drain of the main TMEM accumulator (0 = 512) */
+    int32_t tc_flush;       /* atoms per drain of the main TMEM accumulator (0 = 128) */
     volatile int32_t *cancel; /* optional host flag polled between atom types      */
 } dgpu_opts;
 
