@@ -229,7 +229,7 @@ static int four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
     int32_t ncell = 0;
     int64_t pairs_aver = 0;
     float kernel_ms = 0.f;
-    int64_t ts[66];
+    int64_t ts[2 * 64 + 4];
 
     // ---- <F> (four_aver) ----
     if (op->fave != 0.0) {
@@ -252,7 +252,7 @@ static int four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
         rc = engine_sums(ctx, engine, ctx->aph0, ctx->adu, ctx->adv, ctx->adw, ctx->aw, ts, cr->nscat, op, box,
                          ctx->apart, &aref);
         if (rc) return rc;
-        pairs_aver += ts[cr->nscat] * np;
+        for (int t = 0; t < cr->nscat; t++) pairs_aver += ts[cr->nscat + 1 + t] * np;
         // lattice of all cells (four_getav LOT_OFF + four_strucf(0,...) on the full num)
         int32_t lat_nslice = 1, closed = op->phase == DGPU_PHASE_EXACT64;
         if (!closed) {
@@ -320,7 +320,8 @@ static int four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
         for (int k = 0; k < 9; k++) info->off_shift[k] = geo.off[k];
         info->ncell = ncell;
         info->engine_used = engine;
-        info->pairs = ts[cr->nscat] * np;
+        info->pairs = 0;
+        for (int t = 0; t < cr->nscat; t++) info->pairs += ts[cr->nscat + 1 + t] * np;
         info->pairs_aver = pairs_aver;
         for (int k = 0; k < 7; k++) info->res[k] = res[k];
         info->kernel_ms = kernel_ms;
@@ -423,7 +424,7 @@ extern "C" int dgpu_four_strucf(dgpu_ctx *ctx, const double *xat, int64_t nxat, 
         for (int k = 0; k < 3; k++) { geo.vi[k] = uin[k]; geo.vi[3 + k] = vin[k]; geo.vi[6 + k] = win[k]; }
         memcpy(geo.off, off_shift, sizeof(geo.off));
         FoldSpec nofold = {0, 1, {1, 1, 1}, {0, 0, 0}, nullptr};
-        int64_t ts[3];
+        int64_t ts[8];
         int rc = dgpu_prepare_atoms(ctx, ctx->pos.as<double>(), ctx->iscat.as<int32_t>(), nullptr, nxat, 1, geo,
                                     nofold, ctx->ph0, ctx->du, ctx->dv, ctx->dw, ctx->w, ts);
         if (rc) return rc;

@@ -111,7 +111,11 @@ __global__ void k_type_count(const int32_t *iscat, int64_t n, int32_t nscat, Fol
         counts[(int64_t)tt * nblk + blockIdx.x] = hist[tt + 1];
 }
 
-// exclusive scan of len int32 counts into int64 offsets (one CTA)
+// Exclusive scan of the per-(type, block) counts into int64 offsets, one CTA.
+// Each type's range starts on a multiple of TYPE_ALIGN atoms; the gap after a
+// type is padding (zero phase, zero weight) so that every 32-atom group of a
+// type is aligned and complete.
+#define TYPE_ALIGN 32
 __global__ void k_scan_counts(const int32_t *counts, int64_t len, int64_t *offs,
                               int64_t nblk, int32_t nscat, int64_t *type_start)
 {
@@ -120,35 +124,43 @@ __global__ void k_scan_counts(const int32_t *counts, int64_t len, int64_t *offs,
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int64_t base = 0; base < len; base += blockDim.x) {
-        int64_t i = base + threadIdx.x;
-        int64_t v = i < len ? counts[i] : 0;
-        int64_t x = v;
-        for (int o = 1; o < 32; o <<= 1) {
-            int64_t y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
+    for (int t = 0; t < nscat; t++) {
+        if (threadIdx.x == 0) {
+            carry = (carry + TYPE_ALIGN - 1) / TYPE_ALIGN * TYPE_ALIGN;
+            type_start[t] = carry;
         }
-        if (lane == 31) warp_sums[wid] = x;
         __syncthreads();
-        if (wid == 0) {
-            int64_t s = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : 0;
+        const int64_t seg = (int64_t)t * nblk;
+        for (int64_t base = 0; base < nblk; base += blockDim.x) {
+            int64_t i = base + threadIdx.x;
+            int64_t v = i < nblk ? counts[seg + i] : 0;
+            int64_t x = v;
             for (int o = 1; o < 32; o <<= 1) {
-                int64_t y = __shfl_up_sync(0xffffffffu, s, o);
-                if (lane >= o) s += y;
+                int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
             }
-            warp_sums[lane] = s;
+            if (lane == 31) warp_sums[wid] = x;
+            __syncthreads();
+            if (wid == 0) {
+                int64_t s = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : 0;
+                for (int o = 1; o < 32; o <<= 1) {
+                    int64_t y = __shfl_up_sync(0xffffffffu, s, o);
+                    if (lane >= o) s += y;
+                }
+                warp_sums[lane] = s;
+            }
+            __syncthreads();
+            int64_t incl = x + (wid > 0 ? warp_sums[wid - 1] : 0) + carry;
+            if (i < nblk) offs[seg + i] = incl - v;
+            __syncthreads();
+            if (threadIdx.x == blockDim.x - 1) carry = incl;
+            __syncthreads();
         }
-        __syncthreads();
-        int64_t incl = x + (wid > 0 ? warp_sums[wid - 1] : 0) + carry;
-        if (i < len) offs[i] = incl - v;
-        __syncthreads();
-        if (threadIdx.x == blockDim.x - 1) carry = incl;
+        if (threadIdx.x == 0) type_start[nscat + 1 + t] = carry - type_start[t];   // real atoms of type t
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        for (int t = 0; t < nscat; t++) type_start[t] = offs[(int64_t)t * nblk];
-        type_start[nscat] = carry;
-    }
+    if (threadIdx.x == 0) type_start[nscat] = (carry + TYPE_ALIGN - 1) / TYPE_ALIGN * TYPE_ALIGN;
+    (void)len;
 }
 
 __global__ void k_scatter_atoms(const double *pos, const int32_t *iscat, const float *aocc,
@@ -211,13 +223,13 @@ int dgpu_prepare_atoms(dgpu_ctx *ctx, const double *d_pos, const int32_t *d_isca
     DGPU_CUDA(ctx, ctx->counts.ensure(cnt_bytes + (size_t)len * sizeof(int64_t)));
     int32_t *counts = ctx->counts.as<int32_t>();
     int64_t *offs = (int64_t *)((char *)ctx->counts.p + cnt_bytes);
-    DGPU_CUDA(ctx, ctx->type_start.ensure((MAXT + 2) * sizeof(int64_t)));
+    DGPU_CUDA(ctx, ctx->type_start.ensure((2 * MAXT + 4) * sizeof(int64_t)));
     int64_t *d_ts = ctx->type_start.as<int64_t>();
     k_type_count<<<(unsigned)nblk, PREP_BLK, 0, ctx->stream>>>(d_iscat, natoms, nscat, fs, counts, nblk);
     DGPU_CUDA(ctx, cudaGetLastError());
     k_scan_counts<<<1, 1024, 0, ctx->stream>>>(counts, len, offs, nblk, nscat, d_ts);
     DGPU_CUDA(ctx, cudaGetLastError());
-    DGPU_CUDA(ctx, cudaMemcpyAsync(h_type_start, d_ts, (nscat + 1) * sizeof(int64_t),
+    DGPU_CUDA(ctx, cudaMemcpyAsync(h_type_start, d_ts, (2 * nscat + 1) * sizeof(int64_t),
                                    cudaMemcpyDeviceToHost, ctx->stream));
     DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     int64_t total = h_type_start[nscat];
@@ -227,6 +239,12 @@ int dgpu_prepare_atoms(dgpu_ctx *ctx, const double *d_pos, const int32_t *d_isca
     DGPU_CUDA(ctx, dv.ensure(cap * 8));
     DGPU_CUDA(ctx, dw.ensure(cap * 8));
     DGPU_CUDA(ctx, w.ensure(cap * 4));
+    // padding slots: phase 0, weight 0
+    DGPU_CUDA(ctx, cudaMemsetAsync(ph0.p, 0, cap * 8, ctx->stream));
+    DGPU_CUDA(ctx, cudaMemsetAsync(du.p, 0, cap * 8, ctx->stream));
+    DGPU_CUDA(ctx, cudaMemsetAsync(dv.p, 0, cap * 8, ctx->stream));
+    DGPU_CUDA(ctx, cudaMemsetAsync(dw.p, 0, cap * 8, ctx->stream));
+    DGPU_CUDA(ctx, cudaMemsetAsync(w.p, 0, cap * 4, ctx->stream));
     k_scatter_atoms<<<(unsigned)nblk, PREP_BLK, 0, ctx->stream>>>(
         d_pos, d_iscat, d_aocc, natoms, nscat, fs, g, offs, nblk, ph0.as<uint64_t>(),
         du.as<uint64_t>(), dv.as<uint64_t>(), dw.as<uint64_t>(), w.as<float>());

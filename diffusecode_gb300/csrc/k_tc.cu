@@ -48,6 +48,9 @@
 #define TC_SBO ((TC_KA / 8) * 128)
 #define TC_LBO 128
 #define TC_TIMEOUT_NS 2000000000ull            // 2 s per wait
+// phase data of one 32-atom group in shared memory: ph0, d_ra, d_rb, d_ac (u64), w (f32)
+#define TC_ATOM_SLOT (TC_KA * 4 * 8 + TC_KA * 4)
+#define TC_BAR_BYTES 256
 #ifndef TC_FLUSH_STAGES
 #define TC_FLUSH_STAGES 4                      // 128 atoms per drain of the main accumulator
 #endif
@@ -117,6 +120,16 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volati
         }
     }
 }
+
+__device__ __forceinline__ void cp_async16(void *dst, const void *src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+// barrier among the producer warps only
+__device__ __forceinline__ void producers_sync() { asm volatile("bar.sync 1, %0;" ::"n"(TC_PROD_THREADS) : "memory"); }
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -253,6 +266,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcGeom g, const TcAr
     uint64_t *cempty = cfull + 1;     // correction accumulator drained
     uint64_t *drain = cempty + 1;
     uint32_t *tbase = reinterpret_cast<uint32_t *>(drain + 1);
+    uint8_t *aslot = smem + (size_t)S * stage_bytes + TC_BAR_BYTES;   // 2 x TC_ATOM_SLOT
     volatile int32_t *err = args.err;
     const bool bf = g.bf16 != 0;
 
@@ -284,23 +298,50 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcGeom g, const TcAr
 
     if (warp < TC_PROD_WARPS) {
         // ------------------------------------------------------------ producers
+        // Atom groups are complete (type ranges padded to 32 atoms with zero
+        // weight).  Their phase data is staged in shared memory with
+        // cp.async, one group ahead of the generation.
         const int tid = threadIdx.x;
         uint32_t it = 0;
         bool ok = true;
+        const uint64_t *src[4] = {args.ph0, args.dra, args.drb, args.dac};
+        auto issue = [&](int slot, int64_t ab) {
+            uint8_t *dst = aslot + slot * TC_ATOM_SLOT;
+            if (tid < 64) {            // 4 arrays x 16 chunks of 16 B
+                const int arr = tid >> 4, ch = tid & 15;
+                cp_async16(dst + arr * (TC_KA * 8) + ch * 16, src[arr] + ab + ch * 2);
+            } else if (tid < 72) {     // weights: 8 chunks
+                const int ch = tid - 64;
+                cp_async16(dst + 4 * TC_KA * 8 + ch * 16, args.w + ab + ch * 4);
+            }
+            cp_async_commit();
+        };
         for (int64_t item = blockIdx.x; item < g.nitems && ok; item += gridDim.x) {
             int t, ks, nt, mt;
             decode_item(g, item, t, ks, nt, mt);
             const int64_t a0 = g.ts[t] + (int64_t)ks * g.slice_len;
             const int64_t a1 = min(g.ts[t + 1], a0 + g.slice_len);
             const int64_t cnt = a1 > a0 ? a1 - a0 : 0;
-            const int nst = (int)((cnt + TC_KA - 1) / TC_KA);
-            const uint64_t *dra = args.dra, *drb = args.drb, *dac = args.dac;
+            const int nst = (int)(cnt / TC_KA);
+            if (nst == 0) continue;
+            producers_sync();               // previous item's slots are free
+            issue(0, a0);
             for (int st = 0; st < nst; st++, it++) {
                 const int s = it % S;
+                if (st + 1 < nst) {
+                    issue((st + 1) & 1, a0 + (int64_t)(st + 1) * TC_KA);
+                    cp_async_wait1();
+                } else {
+                    cp_async_wait0();
+                }
+                producers_sync();           // group st staged for everybody
                 if (it >= (uint32_t)S && !mbar_wait(&empty[s], ((it / S) - 1) & 1, err, 1)) { ok = false; break; }
+                const uint8_t *as = aslot + (st & 1) * TC_ATOM_SLOT;
+                const uint64_t *s_ph0 = reinterpret_cast<const uint64_t *>(as);
+                const uint64_t *s_dra = s_ph0 + TC_KA, *s_drb = s_dra + TC_KA, *s_dac = s_drb + TC_KA;
+                const float *s_w = reinterpret_cast<const float *>(s_dac + TC_KA);
                 uint8_t *A = smem + (size_t)s * stage_bytes;
                 uint8_t *B = A + 4 * TC_A_BYTES;
-                const int64_t ab = a0 + (int64_t)st * TC_KA;
                 const int units = 4 * TC_M + 4 * N;
                 for (int u = tid; u < units; u += TC_PROD_THREADS) {
                     float re[8], im[8];
@@ -313,20 +354,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcGeom g, const TcAr
                         const bool rv = rg < g.nrows;
                         const uint32_t na = rv ? (uint32_t)(rg % g.fra) : 0u;
                         const uint32_t nb = rv ? (uint32_t)(rg / g.fra) : 0u;
+                        const float wr = rv ? 1.f : 0.f;
 #pragma unroll
                         for (int e = 0; e < 8; e++) {
-                            const int64_t a = ab + q * 8 + e;
-                            if (rv && a < a1) {
-                                uint64_t ph = __ldg(&args.ph0[a]) + na * __ldg(&dra[a]) + nb * __ldg(&drb[a]);
-                                float c, sn;
-                                phasor(ph, c, sn);
-                                const float wj = __ldg(&args.w[a]);
-                                re[e] = wj * c;
-                                im[e] = wj * sn;
-                            } else {
-                                re[e] = 0.f;
-                                im[e] = 0.f;
-                            }
+                            const int k = q * 8 + e;
+                            const uint64_t ph = s_ph0[k] + na * s_dra[k] + nb * s_drb[k];
+                            float c, sn;
+                            phasor(ph, c, sn);
+                            const float wj = s_w[k] * wr;
+                            re[e] = wj * c;
+                            im[e] = wj * sn;
                         }
                         off = core_off(r, q);
                         base = A;
@@ -335,20 +372,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcGeom g, const TcAr
                         const int v = u - 4 * TC_M;
                         const int c = v % N, q = v / N;
                         const int64_t cg = (int64_t)nt * N + c;
-                        const bool cv = cg < g.ncols;
+                        const float wc = cg < g.ncols ? 1.f : 0.f;
                         const uint32_t nc = (uint32_t)cg;
 #pragma unroll
                         for (int e = 0; e < 8; e++) {
-                            const int64_t a = ab + q * 8 + e;
-                            if (cv && a < a1) {
-                                float cs, sn;
-                                phasor(nc * __ldg(&dac[a]), cs, sn);
-                                re[e] = cs;
-                                im[e] = sn;
-                            } else {
-                                re[e] = 0.f;
-                                im[e] = 0.f;
-                            }
+                            float cs, sn;
+                            phasor(nc * s_dac[q * 8 + e], cs, sn);
+                            re[e] = cs * wc;
+                            im[e] = sn * wc;
                         }
                         off = core_off(c, q);
                         base = B;
@@ -365,6 +396,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcGeom g, const TcAr
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 mbar_arrive(&full[s]);
             }
+            cp_async_wait0();
         }
     } else if (warp == TC_MMA_WARP) {
         // ------------------------------------------------------------ MMA issuer
@@ -617,7 +649,7 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
     g.nslice = (int32_t)dgpu_cdiv(maxn > 0 ? maxn : 1, g.slice_len);
     g.nitems = tiles * g.nslice;
     const uint32_t stage_bytes = 4 * TC_A_BYTES + 4u * g.N * TC_KA * 2;
-    const uint32_t bar_bytes = 256;
+    const uint32_t bar_bytes = TC_BAR_BYTES + 2 * TC_ATOM_SLOT;
     int stages = (int)((200 * 1024 - bar_bytes) / stage_bytes);
     g.stages = stages > 4 ? 4 : stages;
     g.tmem_cols = pow2_cols(2 * g.N * (1 + g.nbuf));
