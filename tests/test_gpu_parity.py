@@ -101,7 +101,10 @@ def test_perovskite_plane_parity(oracle, ctx, phase):
     assert list(r.info.lmn) == list(info.lmn)
     floor = K.incoherent_floor(cr, g, op)
     assert K.rel_err(r.dsi, dsi, floor) <= TOL
-    np.testing.assert_allclose(np.array(r.res[1:]), np.array(list(info.res)[1:]), rtol=1e-4)
+    # four_qinfo statistics; minima sit at near-cancellations, so the
+    # tolerance scales with the mean diffuse intensity
+    ref = np.array(list(info.res)[1:])
+    assert np.all(np.abs(np.array(r.res[1:]) - ref) <= 1e-4 * np.abs(ref) + 1e-5 * ref[2])
     assert r.info.pairs == cr.n_scattering() * g.npoints
 
 
