@@ -170,6 +170,27 @@ int dgpu_four_strucf(dgpu_ctx *ctx, const double *xat, int64_t nxat,
                      const int32_t num[3], const int32_t fnum[3],
                      const double *cfact, const int32_t *istl, double *tcsf);
 
+/* Allocation-free variant of dgpu_four_strucf for callers that cannot
+ * allocate device memory: reverse Monte Carlo loops re-evaluating a few atoms
+ * per move (where a cudaMalloc/cudaFree per call would synchronise the
+ * device), code living inside another allocator's memory budget, or code
+ * enqueuing on a stream it does not own.  It has no counterpart in the
+ * reference.  All pointers named d_* are device memory, arrays as in
+ * dgpu_four_strucf (cfact = complex(0:CFPKT) or NULL, istl int32 num points,
+ * tcsf complex num points); stream is a cudaStream_t (NULL = default stream).
+ * The call only enqueues work: the result is ready when the stream reaches it.
+ * Working memory is one fixed __device__ array per GPU (8.5 MiB, held until
+ * process exit): at most 131072 atoms and 262144 computed points
+ * (fnum(1)*fnum(2)*fnum(3)) per call, else DGPU_ERR_SCRATCH_SIZE.  Calls that
+ * overlap on the GPU share that array and race; calls on one stream are safe.
+ * The first call on a device looks the array up (cudaGetSymbolAddress) and
+ * should come before any stream capture.                                     */
+int dgpu_four_strucf_noalloc(void *stream, const double *d_xat, int64_t nxat,
+                             const double uin[3], const double vin[3], const double win[3],
+                             const double off_shift[9], const int32_t lmn[6],
+                             const int32_t num[3], const int32_t fnum[3],
+                             const double *d_cfact, const int32_t *d_istl, double *d_tcsf);
+
 /* ---- tables (each replaces one reference routine; host buffers) ---------- */
 /* fourier_lmn (discus/prog/fourier_lmn_mod.f90:4-280), host quad precision. */
 int dgpu_fourier_lmn(const double eck[12], const double vi[9], const int32_t inc[3],
