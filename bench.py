@@ -193,6 +193,30 @@ def fp64_check(cr, grid, dsi, npts=192, seed=7):
     return float(np.max(np.abs(ig - i64) / (i64 + floor))), npts
 
 
+def adjoint_measure(ctx, engine, steps=3):
+    """bwd/fwd on the gradient workload: rock salt a = 5.64 A, 25x25x20 cells
+    x 8 = 100,000 atoms, 65^3 grid h,k,l in [-3.2,3.2]; target from a seeded
+    perturbed copy (0.05 A, occupancies +-0.1); w = 1/(I_target + 1)."""
+    from diffusecode_gb300 import fourier as FR
+    from diffusecode_gb300.autograd import chi2_grad
+    cr, grid = S.rocksalt_volume()
+    tgt = S.perturbed_copy(cr, 41, 0.05, 5.64, 0.1)
+    op = _abi.default_opts(ldbw=1, phase=_abi.PHASE_EXACT64, engine=engine)
+    it = FR.four_run(tgt, grid, op, ctx=ctx).dsi
+    wt = 1.0 / (it + 1.0)
+    fwd, bwd = [], []
+    for s in range(steps + 1):
+        r = FR.four_run(cr, grid, op, ctx=ctx)
+        c2, gp, go, info = chi2_grad(cr, grid, op, it, wt, ctx=ctx)
+        if s:
+            fwd.append(r.info.kernel_ms)
+            bwd.append(info.total_ms)
+    f, b = min(fwd), min(bwd)
+    return {"workload": "rocksalt-100000-atoms-65^3", "fwd_kernel_ms": f, "adjoint_ms": b,
+            "bwd_over_fwd": b / f, "chi2": c2,
+            "note": "adjoint = per-point weights + per-atom sums (CUDA cores); fwd = type sums of the same engine"}
+
+
 def run_reference(args, world, rank):
     cr, grid = workload(args.workload)
     if rank != 0:
@@ -310,6 +334,7 @@ def run_ours(args, world, rank, local):
     if rank != 0:
         return
     acc_err, acc_pts = fp64_check(cr, grid, dsi_host)
+    adj = None if args.no_adjoint else adjoint_measure(ctx, engine)
     pk, pk_kind = peaks()
     fnum_pts = int(np.prod(list(info.fnum)))
     pairs_computed = cr.n_scattering() * fnum_pts
@@ -340,6 +365,8 @@ def run_ours(args, world, rank, local):
         "wall_s_timed": wall,
         "roofline": roof,
         "clocks": clk.summary(),
+        "adjoint": adj,
+        "tc_config": list(info.tc_config),
         "gpu_launches": LAUNCHES_PER_RUN * args.steps,
         "accuracy": {"rel_err_vs_fp64": acc_err, "points": acc_pts,
                      "norm": "max |I-I64|/(I64 + N<|f|^2>) at sampled grid points"},
@@ -363,6 +390,7 @@ def main():
     ap.add_argument("--engine", default="auto", choices=["auto", "direct", "tc"])
     ap.add_argument("--workload", default="fcc-alloy-101^3")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":

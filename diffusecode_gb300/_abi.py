@@ -101,6 +101,7 @@ class Info(C.Structure):
         ("res", C.c_double * 7),
         ("kernel_ms", C.c_double),
         ("total_ms", C.c_double),
+        ("tc_config", C.c_int32 * 4),
     ]
 
 

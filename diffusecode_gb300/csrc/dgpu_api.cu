@@ -183,7 +183,7 @@ static int engine_sums(dgpu_ctx *ctx, int engine, DevBuf &ph0, DevBuf &du, DevBu
 }
 
 // The whole path with device-resident crystal arrays and outputs.
-static int four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,
+int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,
                         double2 *d_csf, double2 *d_acsf, double *d_dsi, dgpu_info *info)
 {
     int rc = check_inputs(ctx, cr, g, op);
@@ -289,6 +289,7 @@ static int four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
     rc = dgpu_prepare_atoms(ctx, cr->pos, cr->iscat, cr->atom_occ, cr->natoms, cr->nscat, geo, nofold, ctx->ph0,
                             ctx->du, ctx->dv, ctx->dw, ctx->w, ts);
     if (rc) return rc;
+    memcpy(ctx->ts_main, ts, sizeof(int64_t) * (2 * cr->nscat + 1));
     PartRef pref;
     DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
     rc = engine_sums(ctx, engine, ctx->ph0, ctx->du, ctx->dv, ctx->dw, ctx->w, ts, cr->nscat, op, box, ctx->part,
@@ -325,6 +326,7 @@ static int four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
         info->pairs_aver = pairs_aver;
         for (int k = 0; k < 7; k++) info->res[k] = res[k];
         info->kernel_ms = kernel_ms;
+        for (int k = 0; k < 4; k++) info->tc_config[k] = engine == DGPU_ENGINE_TC ? ctx->tc_last[k] : -1;
         float tot = 0.f;
         DGPU_CUDA(ctx, cudaEventElapsedTime(&tot, ctx->ev[0], ctx->ev[1]));
         info->total_ms = tot;
@@ -343,7 +345,7 @@ extern "C" int dgpu_four_run_device(dgpu_ctx *ctx, const dgpu_crystal *cr, const
         DGPU_CUDA(ctx, ctx->acsf.ensure(np * sizeof(double2)));
         acsf = ctx->acsf.as<double2>();
     }
-    return four_run_dev(ctx, cr, grid, opts, (double2 *)d_csf, acsf, d_dsi, info);
+    return dgpu_four_run_dev(ctx, cr, grid, opts, (double2 *)d_csf, acsf, d_dsi, info);
 }
 
 extern "C" int dgpu_four_run(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid, const dgpu_opts *opts,
@@ -370,8 +372,8 @@ extern "C" int dgpu_four_run(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_g
     DGPU_CUDA(ctx, ctx->csf.ensure(np * sizeof(double2)));
     DGPU_CUDA(ctx, ctx->acsf.ensure(np * sizeof(double2)));
     DGPU_CUDA(ctx, ctx->dsi.ensure(np * sizeof(double)));
-    rc = four_run_dev(ctx, &dc, grid, opts, ctx->csf.as<double2>(), ctx->acsf.as<double2>(), ctx->dsi.as<double>(),
-                      info);
+    rc = dgpu_four_run_dev(ctx, &dc, grid, opts, ctx->csf.as<double2>(), ctx->acsf.as<double2>(),
+                           ctx->dsi.as<double>(), info);
     if (rc < 0) return rc;
     DGPU_CUDA(ctx, cudaMemcpyAsync(csf, ctx->csf.p, np * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
     DGPU_CUDA(ctx, cudaMemcpyAsync(dsi, ctx->dsi.p, np * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));

@@ -3,6 +3,9 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <map>
+#include <tuple>
 #include <stdio.h>
 #include <string.h>
 
@@ -47,6 +50,12 @@ struct Tables {
     double2 *cfact;        // [nscat][NTAB]
 };
 
+// one tensor-core launch configuration (chosen by the autotuner)
+struct TcChoice {
+    int32_t axis = -1, N = 0, slice_mult = 4;
+};
+typedef std::tuple<int32_t, int32_t, int32_t, int32_t, int32_t, int32_t, int32_t> TcKey;
+
 struct dgpu_ctx {
     int device = 0;
     int nsm = 0;
@@ -59,9 +68,12 @@ struct dgpu_ctx {
     DevBuf ph0, du, dv, dw, w;          // main atom set
     DevBuf aph0, adu, adv, adw, aw;     // folded atoms for <F>
     DevBuf istl, cfact, part, apart, lat, csf, acsf, dsi, stats, flag;
-    DevBuf tc_part, tc_work;
+    DevBuf tc_part, tc_work, aidx;          // aidx: original atom index of each prepared slot
+    int64_t ts_main[2 * 64 + 4] = {};      // type ranges of the last main atom preparation
     DevBuf gq, gpart, grad, batch_desc, batch_aux;
     double batch_ms = 0.0;
+    std::map<TcKey, TcChoice> tc_tuned;   // autotuner results per problem shape
+    int32_t tc_last[4] = {-1, -1, -1, -1};
 };
 
 // error helpers ---------------------------------------------------------
@@ -169,6 +181,10 @@ int dgpu_friedel_mirror(dgpu_ctx *ctx, const BoxSpec &box, int32_t idim, double2
                         double2 *acsf, double *dsi);
 int dgpu_qinfo(dgpu_ctx *ctx, const double eck[3], const double vi[9], const int32_t num[3],
                const double *dsi, double res[7]);
+
+// the whole four_run with device-resident crystal arrays and outputs
+int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,
+                      double2 *d_csf, double2 *d_acsf, double *d_dsi, dgpu_info *info);
 
 // adjoint.cu / batch.cu ---------------------------------------------------
 int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid,

@@ -1,17 +1,283 @@
-// Adjoint (placeholder).
+// Adjoint of four_run: chi^2 = sum_h wt(h) (I(h) - It(h))^2 over the full
+// grid and its gradient with respect to every atom position (lattice units)
+// and per-atom occupancy weight.  Replaces the finite-difference derivatives
+// REFINE and RMC obtain by re-running whole macros
+// (refine/prog/refine_run.f90:491-759).
+//
+// With I = ds |F|^2, F = sum_t c_t(h) sum_j w_j exp(2 pi i h.r_j):
+//   dchi2/dw_j   = Re T0_j
+//   dchi2/dr_j,k = -2 pi w_j ( eck_k Im T0_j + sum_a vi_a,k Im T_a,j )
+//   T0_j  = sum_h Q_t(h) exp(2 pi i h.r_j),  T_a,j = sum_h n_a(h) Q_t(h) exp(...)
+//   Q_t(h) = 2 ds G(h) conj(F(h)) c_t(h),    G = dchi2/dI = 2 wt (I - It)
+// h = eck + n_0 vi_0 + n_1 vi_1 + n_2 vi_2.  The sums run over the Friedel-
+// reduced box; a box point whose mirror lies outside the box carries the
+// mirror's G as well (I(-h) = I(h) without anomalous scattering).  The phase
+// of every (atom, point) pair is the exact 64-bit fixed point of the forward
+// pass; phasors in FP32, sums in FP32 over 256-point tiles and FP64 across.
+#include <math.h>
+
 #include "dgpu_internal.h"
 
-int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *, const dgpu_grid *, const dgpu_opts *,
-                        const double *, const double *, double *, double *, double *, dgpu_info *)
+#define ADJ_NT 128
+#define ADJ_TP 256
+
+__global__ void k_adj_g(const double *__restrict__ dsi, const double *__restrict__ it,
+                        const double *__restrict__ wt, int64_t np, double *__restrict__ g,
+                        double *__restrict__ chi_part)
 {
-    return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "adjoint not built");
+    __shared__ double sh[256];
+    double acc = 0.0;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += (int64_t)gridDim.x * blockDim.x) {
+        const double d = dsi[p] - it[p];
+        const double w = wt ? wt[p] : 1.0;
+        g[p] = 2.0 * w * d;
+        acc += w * d * d;
+    }
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) chi_part[blockIdx.x] = sh[0];
 }
 
-extern "C" int dgpu_batch_run(dgpu_ctx *ctx, int32_t, const dgpu_crystal *, const dgpu_grid *,
-                              const dgpu_opts *, double *const *, const double *const *,
-                              const double *const *, double *, double *const *, double *const *)
+__global__ void k_adj_chi(const double *part, int n, double *out)
 {
-    return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "batch not built");
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double s = 0.0;
+        for (int k = 0; k < n; k++) s += part[k];
+        *out = s;
+    }
 }
 
-extern "C" double dgpu_batch_last_ms(const dgpu_ctx *ctx) { return ctx ? ctx->batch_ms : 0.0; }
+// Q_t(p) on the box, FP32 complex, layout [t][box point]
+__global__ void k_adj_q(const FormSpec *fs, BoxSpec box, int32_t halved, const double *__restrict__ g,
+                        const double2 *__restrict__ csf, const int32_t *__restrict__ istl,
+                        const double2 *__restrict__ cfact, double sqds, float2 *__restrict__ Q)
+{
+    const int64_t pb = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    if (pb >= nb) return;
+    const int32_t c[3] = {(int32_t)(pb % box.f[0]), (int32_t)((pb / box.f[0]) % box.f[1]),
+                          (int32_t)(pb / ((int64_t)box.f[0] * box.f[1]))};
+    const int32_t *n = box.num;
+    const int64_t idx = c[0] + (int64_t)n[0] * (c[1] + (int64_t)n[1] * c[2]);
+    double G = g[idx];
+    if (halved >= 1 && c[halved - 1] < box.f[halved - 1] - 1) {
+        const int64_t m = (n[0] - 1 - c[0]) + (int64_t)n[0] * ((n[1] - 1 - c[1]) + (int64_t)n[1] * (n[2] - 1 - c[2]));
+        G += g[m];
+    }
+    // conj(F) with F = csf / sqrt(ds):  2 ds G conj(F) c_t = 2 sqrt(ds) G conj(csf) c_t
+    const double2 f = csf[idx];
+    const double sc = 2.0 * sqds * G;
+    double h[3];
+    if (fs->mode != DGPU_FORM_TABLE)
+        for (int k = 0; k < 3; k++)
+            h[k] = __dadd_rn(__dadd_rn(__dadd_rn(fs->eck[k], __dmul_rn(fs->vi[k], (double)c[0])),
+                                       __dmul_rn(fs->vi[3 + k], (double)c[1])),
+                             __dmul_rn(fs->vi[6 + k], (double)c[2]));
+    for (int t = 1; t <= fs->nscat; t++) {
+        double cr, ci;
+        if (fs->mode == DGPU_FORM_TABLE) {
+            const double2 cc = cfact[(int64_t)(t - 1) * DGPU_NTAB + istl[idx]];
+            cr = cc.x;
+            ci = cc.y;
+        } else {
+            const double *r = fs->rten;
+            const double t0 = r[0] * h[0] + r[3] * h[1] + r[6] * h[2];
+            const double t1 = r[1] * h[0] + r[4] * h[1] + r[7] * h[2];
+            const double t2 = r[2] * h[0] + r[5] * h[1] + r[8] * h[2];
+            const double q2 = (h[0] * t0 + h[1] * t1 + h[2] * t2) / 4.0;
+            const double *s = fs->scat + 11 * t;
+            double ff = s[0];
+            if (fs->lxray)
+                for (int i = 1; i <= fs->power; i++) ff += s[2 * i - 1] * exp(-s[2 * i] * q2);
+            const double fp = fs->ano ? fs->delfr[t] : 0.0, fpp = fs->ano ? fs->delfi[t] : 0.0;
+            const double sb = fs->ldbw ? exp(-fs->dw[t] * q2) * fs->occ[t] : fs->occ[t];
+            cr = sb * (ff + fp);
+            ci = sb * fpp;
+        }
+        // conj(f) * c = (fr - i fi)(cr + i ci)
+        const double qr = sc * (f.x * cr + f.y * ci);
+        const double qi = sc * (f.x * ci - f.y * cr);
+        Q[(int64_t)(t - 1) * nb + pb] = make_float2((float)qr, (float)qi);
+    }
+}
+
+struct AdjGeom {
+    int32_t f[3];
+    int64_t pbox;
+    double eck[3], vi[9];
+};
+
+// one thread per prepared atom of one type: sums over all box points
+__global__ void __launch_bounds__(ADJ_NT) k_adj_atoms(const uint64_t *__restrict__ ph0, const uint64_t *__restrict__ du,
+                                                      const uint64_t *__restrict__ dv, const uint64_t *__restrict__ dw,
+                                                      const float *__restrict__ w, const int32_t *__restrict__ aidx,
+                                                      int64_t a_lo, int64_t a_hi, const float2 *__restrict__ Q,
+                                                      AdjGeom g, double *__restrict__ grad_pos,
+                                                      double *__restrict__ grad_occ)
+{
+    __shared__ float2 sq[ADJ_TP];
+    const int64_t a = a_lo + (int64_t)blockIdx.x * ADJ_NT + threadIdx.x;
+    const bool valid = a < a_hi;
+    const uint64_t p0 = valid ? ph0[a] : 0, d0 = valid ? du[a] : 0, d1 = valid ? dv[a] : 0, d2 = valid ? dw[a] : 0;
+    uint64_t ph_plane = p0, ph_row = p0, ph = p0;
+    int32_t i = 0, j = 0, l = 0;
+    double T0r = 0.0, T0i = 0.0, T1 = 0.0, T2 = 0.0, T3 = 0.0;
+    for (int64_t base = 0; base < g.pbox; base += ADJ_TP) {
+        const int cnt = (int)min((int64_t)ADJ_TP, g.pbox - base);
+        __syncthreads();
+        for (int k = threadIdx.x; k < cnt; k += ADJ_NT) sq[k] = Q[base + k];
+        __syncthreads();
+        float a0r = 0.f, a0i = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+        for (int k = 0; k < cnt; k++) {
+            const float2 q = sq[k];
+            float s, c;
+            __sincosf((float)(int32_t)(ph >> 32) * 1.4629180792671596e-09f, &s, &c);
+            const float zr = q.x * c - q.y * s;
+            const float zi = q.x * s + q.y * c;
+            a0r += zr;
+            a0i += zi;
+            a1 = fmaf((float)i, zi, a1);
+            a2 = fmaf((float)j, zi, a2);
+            a3 = fmaf((float)l, zi, a3);
+            // next point of the box, first axis fastest (uniform across the block)
+            ++i;
+            ph += d0;
+            if (i == g.f[0]) {
+                i = 0;
+                ++j;
+                ph_row += d1;
+                if (j == g.f[1]) {
+                    j = 0;
+                    ++l;
+                    ph_plane += d2;
+                    ph_row = ph_plane;
+                }
+                ph = ph_row;
+            }
+        }
+        T0r += a0r;
+        T0i += a0i;
+        T1 += a1;
+        T2 += a2;
+        T3 += a3;
+    }
+    if (!valid) return;
+    const int32_t o = aidx[a];
+    if (o < 0) return;
+    const double wj = (double)w[a];
+    if (grad_occ) grad_occ[o] = T0r;
+    if (grad_pos) {
+        const double zpi = 6.283185307179586476925286766559;
+        for (int k = 0; k < 3; k++)
+            grad_pos[3 * (int64_t)o + k] =
+                -zpi * wj * (g.eck[k] * T0i + g.vi[k] * T1 + g.vi[3 + k] * T2 + g.vi[6 + k] * T3);
+    }
+}
+
+int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid, const dgpu_opts *op,
+                        const double *i_target, const double *weight, double *chi2, double *grad_pos,
+                        double *grad_occ, dgpu_info *info)
+{
+    if (op->fave != 0.0)
+        return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "gradient with <F> subtraction (set aver) is not available");
+    if (op->ano) return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "gradient with anomalous scattering");
+    if (op->phase != DGPU_PHASE_EXACT64)
+        return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "gradient needs EXACT64 phases");
+    const int64_t n = cr->natoms;
+    const int64_t np = (int64_t)grid->inc[0] * grid->inc[1] * grid->inc[2];
+    // forward pass with host inputs
+    DGPU_CUDA(ctx, ctx->pos.ensure(n * 3 * sizeof(double)));
+    DGPU_CUDA(ctx, ctx->iscat.ensure(n * sizeof(int32_t)));
+    DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->pos.p, cr->pos, n * 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->iscat.p, cr->iscat, n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+    dgpu_crystal dc = *cr;
+    dc.pos = ctx->pos.as<double>();
+    dc.iscat = ctx->iscat.as<int32_t>();
+    if (cr->atom_occ) {
+        DGPU_CUDA(ctx, ctx->aocc.ensure(n * sizeof(float)));
+        DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->aocc.p, cr->atom_occ, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+        dc.atom_occ = ctx->aocc.as<float>();
+    }
+    DGPU_CUDA(ctx, ctx->csf.ensure(np * sizeof(double2)));
+    DGPU_CUDA(ctx, ctx->acsf.ensure(np * sizeof(double2)));
+    DGPU_CUDA(ctx, ctx->dsi.ensure(np * sizeof(double)));
+    dgpu_info fwd;
+    int rc = dgpu_four_run_dev(ctx, &dc, grid, op, ctx->csf.as<double2>(), ctx->acsf.as<double2>(),
+                               ctx->dsi.as<double>(), &fwd);
+    if (rc < 0) return rc;
+    DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
+
+    // adjoint weights g(h) and chi^2
+    const int nblk = 512;
+    DGPU_CUDA(ctx, ctx->gq.ensure(np * sizeof(double) * 3 + (size_t)nblk * sizeof(double) + 64));
+    double *d_it = ctx->gq.as<double>();
+    double *d_wt = d_it + np;
+    double *d_g = d_wt + np;
+    double *d_chi = d_g + np;
+    DGPU_CUDA(ctx, cudaMemcpyAsync(d_it, i_target, np * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    if (weight)
+        DGPU_CUDA(ctx, cudaMemcpyAsync(d_wt, weight, np * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    k_adj_g<<<nblk, 256, 0, ctx->stream>>>(ctx->dsi.as<double>(), d_it, weight ? d_wt : nullptr, np, d_g, d_chi);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    k_adj_chi<<<1, 32, 0, ctx->stream>>>(d_chi, nblk, d_chi + nblk);
+    DGPU_CUDA(ctx, cudaGetLastError());
+
+    // Q on the Friedel box
+    BoxSpec box;
+    for (int k = 0; k < 3; k++) {
+        box.f[k] = fwd.fnum[k];
+        box.num[k] = grid->inc[k];
+    }
+    const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    FormSpec fs;
+    dgpu_fill_formspec(ctx, cr, op, grid, fs);
+    DGPU_CUDA(ctx, ctx->stats.ensure(sizeof(FormSpec)));
+    FormSpec *d_fs = ctx->stats.as<FormSpec>();
+    DGPU_CUDA(ctx, cudaMemcpyAsync(d_fs, &fs, sizeof(FormSpec), cudaMemcpyHostToDevice, ctx->stream));
+    DGPU_CUDA(ctx, ctx->gpart.ensure((size_t)cr->nscat * nb * sizeof(float2)));
+    k_adj_q<<<(unsigned)dgpu_cdiv(nb, 256), 256, 0, ctx->stream>>>(
+        d_fs, box, fwd.friedel_dim, d_g, ctx->csf.as<double2>(), ctx->istl.as<int32_t>(), ctx->cfact.as<double2>(),
+        sqrt(op->diff_scale), ctx->gpart.as<float2>());
+    DGPU_CUDA(ctx, cudaGetLastError());
+
+    // per-atom sums (atoms prepared by the forward pass, grouped by type)
+    DGPU_CUDA(ctx, ctx->grad.ensure(n * 4 * sizeof(double)));
+    double *d_gpos = ctx->grad.as<double>();
+    double *d_gocc = d_gpos + 3 * n;
+    DGPU_CUDA(ctx, cudaMemsetAsync(d_gpos, 0, n * 4 * sizeof(double), ctx->stream));
+    AdjGeom ag;
+    for (int k = 0; k < 3; k++) {
+        ag.f[k] = box.f[k];
+        ag.eck[k] = grid->eck[k];
+    }
+    ag.pbox = nb;
+    memcpy(ag.vi, grid->vi, sizeof(ag.vi));
+    const int64_t *ts = ctx->ts_main;
+    for (int t = 0; t < cr->nscat; t++) {
+        const int64_t lo = ts[t], hi = ts[t + 1];
+        if (hi <= lo) continue;
+        k_adj_atoms<<<(unsigned)dgpu_cdiv(hi - lo, ADJ_NT), ADJ_NT, 0, ctx->stream>>>(
+            ctx->ph0.as<uint64_t>(), ctx->du.as<uint64_t>(), ctx->dv.as<uint64_t>(), ctx->dw.as<uint64_t>(),
+            ctx->w.as<float>(), ctx->aidx.as<int32_t>(), lo, hi, ctx->gpart.as<float2>() + (int64_t)t * nb, ag,
+            d_gpos, d_gocc);
+        DGPU_CUDA(ctx, cudaGetLastError());
+    }
+    DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
+    DGPU_CUDA(ctx, cudaMemcpyAsync(chi2, d_chi + nblk, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    if (grad_pos)
+        DGPU_CUDA(ctx, cudaMemcpyAsync(grad_pos, d_gpos, n * 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    if (grad_occ)
+        DGPU_CUDA(ctx, cudaMemcpyAsync(grad_occ, d_gocc, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (info) {
+        *info = fwd;
+        float ms = 0.f;
+        DGPU_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]));
+        info->total_ms = ms;          // adjoint part; the forward's own time is in kernel_ms
+    }
+    return DGPU_OK;
+}

@@ -166,7 +166,7 @@ __global__ void k_scan_counts(const int32_t *counts, int64_t len, int64_t *offs,
 __global__ void k_scatter_atoms(const double *pos, const int32_t *iscat, const float *aocc,
                                 int64_t n, int32_t nscat, FoldSpec fs, PhaseGeom g,
                                 const int64_t *offs, int64_t nblk, uint64_t *ph0, uint64_t *du,
-                                uint64_t *dv, uint64_t *dw, float *w)
+                                uint64_t *dv, uint64_t *dw, float *w, int32_t *idx)
 {
     __shared__ int32_t wcnt[32][MAXT];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -207,6 +207,7 @@ __global__ void k_scatter_atoms(const double *pos, const int32_t *iscat, const f
     dv[dst] = o.dv;
     dw[dst] = o.dw;
     w[dst] = aocc ? aocc[i] : 1.0f;
+    idx[dst] = (int32_t)i;
 }
 
 int dgpu_prepare_atoms(dgpu_ctx *ctx, const double *d_pos, const int32_t *d_iscat,
@@ -245,9 +246,11 @@ int dgpu_prepare_atoms(dgpu_ctx *ctx, const double *d_pos, const int32_t *d_isca
     DGPU_CUDA(ctx, cudaMemsetAsync(dv.p, 0, cap * 8, ctx->stream));
     DGPU_CUDA(ctx, cudaMemsetAsync(dw.p, 0, cap * 8, ctx->stream));
     DGPU_CUDA(ctx, cudaMemsetAsync(w.p, 0, cap * 4, ctx->stream));
+    DGPU_CUDA(ctx, ctx->aidx.ensure(cap * 4));
+    DGPU_CUDA(ctx, cudaMemsetAsync(ctx->aidx.p, 0xFF, cap * 4, ctx->stream));   // padding: -1
     k_scatter_atoms<<<(unsigned)nblk, PREP_BLK, 0, ctx->stream>>>(
         d_pos, d_iscat, d_aocc, natoms, nscat, fs, g, offs, nblk, ph0.as<uint64_t>(),
-        du.as<uint64_t>(), dv.as<uint64_t>(), dw.as<uint64_t>(), w.as<float>());
+        du.as<uint64_t>(), dv.as<uint64_t>(), dw.as<uint64_t>(), w.as<float>(), ctx->aidx.as<int32_t>());
     DGPU_CUDA(ctx, cudaGetLastError());
     return DGPU_OK;
 }

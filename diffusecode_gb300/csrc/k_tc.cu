@@ -579,49 +579,25 @@ static uint32_t pow2_cols(int n)
     return c;
 }
 
-int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const uint64_t *dv, const uint64_t *dw,
-                 const float *w, const int64_t *h_type_start, int32_t ntype, const BoxSpec &box,
-                 const dgpu_opts *op, DevBuf &part, int32_t *nslice_out)
+// Geometry of one launch for a given column axis, tile width and slicing.
+static int tc_setup(dgpu_ctx *ctx, const int64_t *h_type_start, int32_t ntype, const BoxSpec &box,
+                    const dgpu_opts *op, int axis, int N, int slice_mult, TcGeom &g, size_t &smem)
 {
-    if (ntype < 1 || ntype > 64) return dgpu_set_error(ctx, DGPU_ERR_ARG, "ntype=%d", ntype);
-    const int want_n = op->tc_tile_n;
-    if (want_n && (want_n % 16 || want_n < 16 || want_n > 128))
-        return dgpu_set_error(ctx, DGPU_ERR_ARG, "tc_tile_n=%d (multiple of 16 in 16..128)", want_n);
-    TcGeom g;
     memset(&g, 0, sizeof(g));
     for (int k = 0; k < 3; k++) g.f[k] = box.f[k];
     const int64_t npts = (int64_t)box.f[0] * box.f[1] * box.f[2];
-    // column axis and tile width: least padded MMA area, with the operand
-    // generation of the V tile (N per 128 rows) counted as extra work
-    int ac = 0, bestN = 16, best_tiles = 1;
-    double best = 1e300;
-    for (int a = 0; a < 3; a++) {
-        const int n = box.f[a];
-        if (n < 2 && npts != n) continue;
-        const int64_t rows = npts / n;
-        for (int N = 16; N <= 128; N += 16) {
-            if (want_n && N != want_n) continue;
-            const int64_t tiles = dgpu_cdiv(n, N);
-            double area = (double)tiles * N * dgpu_cdiv(rows, TC_M) * TC_M;
-            double cost = area * (1.0 + (double)(TC_M + N) / (TC_M * N) * 24.0);
-            if (6 * N > 512) cost *= 1.6;         // single-buffered main accumulator stalls on drains
-            if (cost < best * (1 - 1e-9)) { best = cost; ac = a; bestN = N; best_tiles = (int)tiles; }
-        }
-    }
-    g.ac = ac;
-    g.ra = ac == 0 ? 1 : 0;
-    g.rb = 3 - ac - g.ra;
-    g.ncols = box.f[ac];
+    g.ac = axis;
+    g.ra = axis == 0 ? 1 : 0;
+    g.rb = 3 - axis - g.ra;
+    g.ncols = box.f[axis];
     g.fra = box.f[g.ra];
-    {
-        const int64_t stride[3] = {1, (int64_t)box.f[0], (int64_t)box.f[0] * box.f[1]};
-        g.sra = stride[g.ra];
-        g.srb = stride[g.rb];
-        g.sac = stride[ac];
-    }
+    const int64_t stride[3] = {1, (int64_t)box.f[0], (int64_t)box.f[0] * box.f[1]};
+    g.sra = stride[g.ra];
+    g.srb = stride[g.rb];
+    g.sac = stride[axis];
     g.nrows = box.f[g.ra] * box.f[g.rb];
-    g.N = bestN;
-    g.n_tiles = best_tiles;
+    g.N = N;
+    g.n_tiles = (int32_t)dgpu_cdiv(g.ncols, N);
     g.nbuf = 6 * g.N <= 512 ? 2 : 1;
     g.m_tiles = (int32_t)dgpu_cdiv(g.nrows, TC_M);
     g.pbox = npts;
@@ -631,17 +607,17 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
     int64_t maxn = 0;
     for (int t = 0; t < ntype; t++) {
         g.ts[t] = h_type_start[t];
-        int64_t n = h_type_start[t + 1] - h_type_start[t];
+        const int64_t n = h_type_start[t + 1] - h_type_start[t];
         maxn = n > maxn ? n : maxn;
     }
     g.ts[ntype] = h_type_start[ntype];
-    // K slices: about 4 work items per SM, or tc_kslice atoms each when given
+    // K slices: about slice_mult work items per SM, or tc_kslice atoms each when given
     const int64_t tiles = (int64_t)g.m_tiles * g.n_tiles * ntype;
     int64_t nsl;
     if (op->tc_kslice > 0) {
         nsl = dgpu_cdiv(maxn, op->tc_kslice);
     } else {
-        nsl = dgpu_cdiv(4LL * ctx->nsm, tiles);
+        nsl = dgpu_cdiv((int64_t)slice_mult * ctx->nsm, tiles);
         if (nsl > 1 && dgpu_cdiv(maxn, nsl) < 2048) nsl = dgpu_cdiv(maxn, 2048);
     }
     if (nsl < 1) nsl = 1;
@@ -650,13 +626,18 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
     g.nitems = tiles * g.nslice;
     const uint32_t stage_bytes = 4 * TC_A_BYTES + 4u * g.N * TC_KA * 2;
     const uint32_t bar_bytes = TC_BAR_BYTES + 2 * TC_ATOM_SLOT;
-    int stages = (int)((200 * 1024 - bar_bytes) / stage_bytes);
+    const int stages = (int)((200 * 1024 - bar_bytes) / stage_bytes);
     g.stages = stages > 4 ? 4 : stages;
     g.tmem_cols = pow2_cols(2 * g.N * (1 + g.nbuf));
     if (g.stages < 2 || g.tmem_cols > 512) return dgpu_set_error(ctx, DGPU_ERR_ARG, "tile does not fit");
-    size_t smem = (size_t)g.stages * stage_bytes + bar_bytes;
+    smem = (size_t)g.stages * stage_bytes + bar_bytes;
+    return DGPU_OK;
+}
 
-    DGPU_CUDA(ctx, part.ensure((size_t)ntype * g.nslice * g.pbox * sizeof(float2)));
+static int tc_launch(dgpu_ctx *ctx, const TcGeom &g, size_t smem, const uint64_t *ph0, const uint64_t *du,
+                     const uint64_t *dv, const uint64_t *dw, const float *w, DevBuf &part)
+{
+    DGPU_CUDA(ctx, part.ensure((size_t)g.ntype * g.nslice * g.pbox * sizeof(float2)));
     DGPU_CUDA(ctx, ctx->flag.ensure(64));
     int32_t *d_err = ctx->flag.as<int32_t>() + 8;
     DGPU_CUDA(ctx, cudaMemsetAsync(d_err, 0, sizeof(int32_t), ctx->stream));
@@ -678,10 +659,111 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
     if (grid < 1) grid = 1;
     k_tc<<<grid, TC_THREADS, smem, ctx->stream>>>(g, args);
     DGPU_CUDA(ctx, cudaGetLastError());
+    return DGPU_OK;
+}
+
+static int tc_check(dgpu_ctx *ctx)
+{
     int32_t herr = 0;
-    DGPU_CUDA(ctx, cudaMemcpyAsync(&herr, d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    DGPU_CUDA(ctx, cudaMemcpyAsync(&herr, ctx->flag.as<int32_t>() + 8, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                   ctx->stream));
     DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (herr) return dgpu_set_error(ctx, DGPU_ERR_TIMEOUT, "tensor-core kernel wait gave up (site %d)", herr);
+    return DGPU_OK;
+}
+
+// Candidate configurations: every column axis and tile width whose padded
+// MMA area is within 25% of the smallest, at two slicings.
+static void tc_candidates(const BoxSpec &box, int want_n, TcChoice *out, int &n)
+{
+    const int64_t npts = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    double best = 1e300, area[3][9];
+    for (int a = 0; a < 3; a++)
+        for (int k = 0; k < 9; k++) {
+            area[a][k] = -1;
+            const int N = 16 * (k + 1) > 128 ? 0 : 16 * (k + 1);
+            if (!N || (want_n && N != want_n)) continue;
+            const int nc = box.f[a];
+            if (nc < 2 && npts != nc) continue;
+            const int64_t rows = npts / nc;
+            area[a][k] = (double)dgpu_cdiv(nc, N) * N * dgpu_cdiv(rows, TC_M) * TC_M;
+            if (N >= 48 && area[a][k] < best) best = area[a][k];
+            if (want_n && area[a][k] < best) best = area[a][k];
+        }
+    n = 0;
+    for (int a = 0; a < 3; a++)
+        for (int k = 0; k < 9; k++) {
+            const int N = 16 * (k + 1);
+            if (area[a][k] < 0 || area[a][k] > 1.25 * best || (N < 48 && !want_n)) continue;
+            for (int m : {4, 8}) {
+                if (n >= 64) return;
+                out[n].axis = a;
+                out[n].N = N;
+                out[n].slice_mult = m;
+                n++;
+            }
+        }
+}
+
+int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const uint64_t *dv, const uint64_t *dw,
+                 const float *w, const int64_t *h_type_start, int32_t ntype, const BoxSpec &box,
+                 const dgpu_opts *op, DevBuf &part, int32_t *nslice_out)
+{
+    if (ntype < 1 || ntype > 64) return dgpu_set_error(ctx, DGPU_ERR_ARG, "ntype=%d", ntype);
+    const int want_n = op->tc_tile_n;
+    if (want_n && (want_n % 16 || want_n < 16 || want_n > 128))
+        return dgpu_set_error(ctx, DGPU_ERR_ARG, "tc_tile_n=%d (multiple of 16 in 16..128)", want_n);
+    int64_t maxn = 0;
+    for (int t = 0; t < ntype; t++) {
+        const int64_t n = h_type_start[t + 1] - h_type_start[t];
+        maxn = n > maxn ? n : maxn;
+    }
+    int lg = 0;
+    while ((1LL << lg) < maxn) lg++;
+    const TcKey key(box.f[0], box.f[1], box.f[2], ntype, lg, op->split * 1000 + want_n,
+                    op->tc_kslice * 7 + op->tc_flush);
+    TcChoice choice;
+    auto hit = ctx->tc_tuned.find(key);
+    if (hit != ctx->tc_tuned.end()) {
+        choice = hit->second;
+    } else {
+        TcChoice cand[64];
+        int nc = 0;
+        tc_candidates(box, want_n, cand, nc);
+        if (nc == 0) return dgpu_set_error(ctx, DGPU_ERR_ARG, "no tensor-core tile fits the box");
+        float best = 1e30f;
+        for (int c = 0; c < nc; c++) {
+            TcGeom g;
+            size_t smem;
+            if (tc_setup(ctx, h_type_start, ntype, box, op, cand[c].axis, cand[c].N, cand[c].slice_mult, g, smem))
+                continue;
+            DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[4], ctx->stream));
+            int rc = tc_launch(ctx, g, smem, ph0, du, dv, dw, w, part);
+            if (rc) return rc;
+            DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[5], ctx->stream));
+            rc = tc_check(ctx);
+            if (rc) return rc;
+            float ms = 0.f;
+            DGPU_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[4], ctx->ev[5]));
+            if (ms < best) {
+                best = ms;
+                choice = cand[c];
+            }
+        }
+        ctx->tc_tuned[key] = choice;
+    }
+    TcGeom g;
+    size_t smem;
+    int rc = tc_setup(ctx, h_type_start, ntype, box, op, choice.axis, choice.N, choice.slice_mult, g, smem);
+    if (rc) return rc;
+    rc = tc_launch(ctx, g, smem, ph0, du, dv, dw, w, part);
+    if (rc) return rc;
+    rc = tc_check(ctx);
+    if (rc) return rc;
+    ctx->tc_last[0] = g.ac;
+    ctx->tc_last[1] = g.N;
+    ctx->tc_last[2] = g.nbuf;
+    ctx->tc_last[3] = (int32_t)g.slice_len;
     *nslice_out = g.nslice;
     return DGPU_OK;
 }

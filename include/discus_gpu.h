@@ -131,6 +131,8 @@ typedef struct dgpu_info {
                                   diffusig, braggmin, braggmax (fourier_sup.f90:2930-2936) */
     double  kernel_ms;         /* device time of the atom x point sums               */
     double  total_ms;          /* device time of the whole call                      */
+    int32_t tc_config[4];      /* tensor-core engine: column axis, N tile, main
+                                  accumulator buffers, atoms per K slice (-1 if unused) */
 } dgpu_info;
 
 /* ---- context ------------------------------------------------------------ */

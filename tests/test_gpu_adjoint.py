@@ -1,0 +1,94 @@
+"""Adjoint (dgpu_chi2_grad): against the oracle's FP64 gradient, against
+central finite differences, and through the autograd wrapper."""
+import numpy as np
+import pytest
+
+import kat_cases as K
+from diffusecode_gb300 import _abi
+from diffusecode_gb300 import fourier as FR
+from diffusecode_gb300 import structures as S
+
+pytestmark = pytest.mark.gpu
+
+
+def _target(cr, grid, ctx, seed=3, sigma=0.05, occ_pm=0.1, a_lat=4.0):
+    tgt = S.perturbed_copy(cr, seed, sigma, a_lat, occ_pm)
+    r = FR.four_run(tgt, grid, K.opts(phase=_abi.PHASE_EXACT64, engine=_abi.ENGINE_DIRECT, friedel=0), ctx=ctx)
+    return r.dsi, 1.0 / (r.dsi + 1.0)
+
+
+@pytest.mark.parametrize("engine", [_abi.ENGINE_DIRECT, _abi.ENGINE_TC])
+def test_gradient_vs_oracle_fp64(oracle, ctx, engine):
+    from diffusecode_gb300.autograd import chi2_grad
+    cr, g = S.small_random(seed=8, natoms=120, nscat=2, inc=(9, 7, 5))
+    cr.atom_occ = np.linspace(0.9, 1.1, cr.natoms).astype(np.float32)
+    it, wt = _target(cr, g, ctx)
+    op = K.opts(phase=_abi.PHASE_EXACT64, engine=engine)
+    c2, gp, go, _ = chi2_grad(cr, g, op, it, wt, ctx=ctx)
+    oc2, ogp, ogo = oracle.chi2_grad(cr, g, op, it, wt)
+    assert abs(c2 - oc2) <= 1e-4 * oc2
+    assert np.max(np.abs(gp - ogp)) <= 2e-4 * np.abs(ogp).max()
+    assert np.max(np.abs(go - ogo)) <= 2e-4 * np.abs(ogo).max()
+    assert np.all(gp[cr.iscat == 0] == 0) and np.all(go[cr.iscat == 0] == 0)
+
+
+def test_gradient_with_friedel_reduction(oracle, ctx):
+    """Centred odd grid: the GPU sums over half the grid with mirror weights."""
+    from diffusecode_gb300.autograd import chi2_grad
+    cr, g = S.perovskite_plane(cells=2)
+    g = S.GridData.from_corners((-2, -2, 0), (2, -2, 0), (-2, 2, 0), inc=(21, 21, 1))
+    it, wt = _target(cr, g, ctx)
+    op = K.opts(phase=_abi.PHASE_EXACT64, engine=_abi.ENGINE_DIRECT)
+    c2, gp, go, info = chi2_grad(cr, g, op, it, wt, ctx=ctx)
+    assert info.friedel_dim == 1
+    oc2, ogp, ogo = oracle.chi2_grad(cr, g, op, it, wt)
+    assert abs(c2 - oc2) <= 1e-4 * oc2
+    assert np.max(np.abs(gp - ogp)) <= 2e-4 * np.abs(ogp).max()
+    assert np.max(np.abs(go - ogo)) <= 2e-4 * np.abs(ogo).max()
+
+
+def test_central_finite_differences(ctx):
+    """d chi2 / d x by central differences with a 1e-4 A step on seeded atoms."""
+    from diffusecode_gb300.autograd import chi2_grad
+    a = 5.64
+    cr, g = S.rocksalt_volume(cells=(3, 3, 3), inc=17, step=0.2)
+    it, wt = _target(cr, g, ctx, a_lat=a)
+    op = K.opts(phase=_abi.PHASE_EXACT64, engine=_abi.ENGINE_DIRECT)
+    c2, gp, go, _ = chi2_grad(cr, g, op, it, wt, ctx=ctx)
+    rng = np.random.Generator(np.random.PCG64(12))
+    h = 1e-4 / a
+    scale = np.abs(gp).max()
+    for atom in rng.choice(cr.natoms, 6, replace=False):
+        for k in range(3):
+            vals = []
+            for sgn in (1, -1):
+                p = cr.pos.copy()
+                p[atom, k] += sgn * h
+                c, _, _, _ = chi2_grad(cr.with_positions(p), g, op, it, wt, ctx=ctx)
+                vals.append(c)
+            fd = (vals[0] - vals[1]) / (2 * h)
+            assert abs(fd - gp[atom, k]) <= 1e-3 * scale + 1e-3 * abs(gp[atom, k])
+
+
+def test_autograd_wrapper(ctx):
+    import torch
+    from diffusecode_gb300.autograd import chi2, chi2_grad
+    cr, g = S.small_random(seed=4, natoms=60, nscat=2, inc=(7, 5, 3))
+    it, wt = _target(cr, g, ctx)
+    op = K.opts(phase=_abi.PHASE_EXACT64, engine=_abi.ENGINE_DIRECT)
+    pos = torch.tensor(cr.pos, requires_grad=True)
+    occ = torch.ones(cr.natoms, dtype=torch.float64, requires_grad=True)
+    val = chi2(pos, occ, cr, g, op, it, wt)
+    val.backward()
+    c2, gp, go, _ = chi2_grad(cr.with_positions(cr.pos, np.ones(cr.natoms, np.float32)), g, op, it, wt, ctx=ctx)
+    assert abs(val.item() - c2) <= 1e-12 * c2
+    np.testing.assert_allclose(pos.grad.numpy(), gp, rtol=1e-12)
+    np.testing.assert_allclose(occ.grad.numpy(), go, rtol=1e-12)
+
+
+def test_gradient_rejects_average(ctx):
+    from diffusecode_gb300.autograd import chi2_grad
+    cr, g = S.small_random(seed=4, natoms=30, inc=(5, 5, 3))
+    with pytest.raises(Exception) as e:
+        chi2_grad(cr, g, K.opts(fave=1.0), np.zeros(g.inc), ctx=ctx)
+    assert getattr(e.value, "code", None) == _abi.DGPU_ERR_UNSUPPORTED

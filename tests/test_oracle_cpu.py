@@ -156,3 +156,23 @@ def test_stl_range_error(oracle):
     big = S.GridData.from_corners((-60, -60, 0), (60, -60, 0), (-60, 60, 0), inc=(5, 5, 1))
     rc, istl = oracle.stltab(big, cr.rten)
     assert rc == _abi.DGPU_ERR_STL_RANGE
+
+
+def test_oracle_gradient_matches_finite_differences(oracle):
+    """The FP64 reference gradient (oc_chi2_grad) against central differences."""
+    cr, g = S.small_random(seed=8, natoms=30, nscat=2, inc=(5, 5, 3))
+    cr.atom_occ = np.linspace(0.9, 1.1, cr.natoms).astype(np.float32)
+    tgt = S.perturbed_copy(cr, 3, 0.05, 4.0, 0.1)
+    op = K.opts(phase=_abi.PHASE_EXACT64, friedel=0)
+    rc, csf, acsf, it, info = oracle.four_run(tgt, g, op)
+    wt = 1.0 / (it + 1.0)
+    c2, gp, go = oracle.chi2_grad(cr, g, op, it, wt)
+    h = 1e-6
+    for a in (1, 7):
+        for k in range(3):
+            p = cr.pos.copy()
+            p[a, k] += h
+            cp, _, _ = oracle.chi2_grad(cr.with_positions(p), g, op, it, wt)
+            p[a, k] -= 2 * h
+            cm, _, _ = oracle.chi2_grad(cr.with_positions(p), g, op, it, wt)
+            assert abs((cp - cm) / (2 * h) - gp[a, k]) <= 1e-6 * np.abs(gp).max()
