@@ -217,6 +217,35 @@ def adjoint_measure(ctx, engine, steps=3):
             "note": "adjoint = per-point weights + per-atom sums (CUDA cores); fwd = type sums of the same engine"}
 
 
+def batch_measure(ctx, steps=3):
+    """Population workload: 64 crystals (cubic / fcc / rock salt), atoms
+    log-uniform in [2000, 200000], each with its own 2D plane of 129^2..257^2
+    points and its own disorder; forward |F|^2 plus chi^2 gradients in one
+    captured graph launch per step (targets: seeded perturbed copies)."""
+    from diffusecode_gb300 import fourier as FR
+    pop = S.population()
+    crs = [c for c, g in pop]
+    grids = [g for c, g in pop]
+    op = _abi.default_opts(ldbw=1, phase=_abi.PHASE_EXACT64, engine=_abi.ENGINE_TC)
+    targets, weights = [], []
+    for i, (cr, g) in enumerate(pop):
+        it = FR.four_run(S.perturbed_copy(cr, 500 + i, 0.02, 4.0, 0.0), g, op, ctx=ctx).dsi
+        targets.append(it)
+        weights.append(1.0 / (it + 1.0))
+    pairs = sum(c.n_scattering() * g.npoints for c, g in pop)
+    fwd_ms, full_ms = [], []
+    for s in range(steps + 1):
+        _, _, _, _, ms_f = FR.batch_run(crs, grids, op, ctx=ctx)
+        _, chi2, gp, go, ms = FR.batch_run(crs, grids, op, targets, weights, ctx=ctx)
+        if s:
+            fwd_ms.append(ms_f)
+            full_ms.append(ms)
+    f, t = min(fwd_ms), min(full_ms)
+    return {"workload": "population-64", "members": len(pop), "atoms": int(sum(c.n_scattering() for c in crs)),
+            "pairs": int(pairs), "fwd_graph_ms": f, "fwd_grad_graph_ms": t,
+            "fwd_G_pairs_per_s": pairs / f / 1e6, "note": "one CUDA graph launch per step; device time"}
+
+
 def run_reference(args, world, rank):
     cr, grid = workload(args.workload)
     if rank != 0:
@@ -335,6 +364,7 @@ def run_ours(args, world, rank, local):
         return
     acc_err, acc_pts = fp64_check(cr, grid, dsi_host)
     adj = None if args.no_adjoint else adjoint_measure(ctx, engine)
+    bat = None if args.no_batch else batch_measure(ctx)
     pk, pk_kind = peaks()
     fnum_pts = int(np.prod(list(info.fnum)))
     pairs_computed = cr.n_scattering() * fnum_pts
@@ -366,6 +396,7 @@ def run_ours(args, world, rank, local):
         "roofline": roof,
         "clocks": clk.summary(),
         "adjoint": adj,
+        "batch": bat,
         "tc_config": list(info.tc_config),
         "gpu_launches": LAUNCHES_PER_RUN * args.steps,
         "accuracy": {"rel_err_vs_fp64": acc_err, "points": acc_pts,
@@ -391,6 +422,7 @@ def main():
     ap.add_argument("--workload", default="fcc-alloy-101^3")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":

@@ -68,6 +68,7 @@ extern "C" int dgpu_ctx_destroy(dgpu_ctx *c)
     if (!c) return DGPU_OK;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
+    dgpu_batch_free(c);
     DevBuf *bufs[] = {&c->pos, &c->iscat, &c->aocc, &c->sel, &c->counts, &c->type_start, &c->ph0, &c->du,
                       &c->dv, &c->dw, &c->w, &c->aph0, &c->adu, &c->adv, &c->adw, &c->aw, &c->istl,
                       &c->cfact, &c->part, &c->apart, &c->lat, &c->csf, &c->acsf, &c->dsi, &c->stats,
@@ -136,7 +137,7 @@ int dgpu_fill_formspec(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *o
 }
 
 // four_test_friedel (fourier_sup.f90:3645-3722)
-static int friedel_test(const dgpu_grid *g, const dgpu_opts *op, int32_t fnum[3])
+int dgpu_friedel_test(const dgpu_grid *g, const dgpu_opts *op, int32_t fnum[3])
 {
     const double eps = (double)1.0e-6f;
     for (int k = 0; k < 3; k++) fnum[k] = g->inc[k];
@@ -215,7 +216,7 @@ int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g,
     if (rc) return rc;
 
     int32_t fnum[3];
-    int idim = friedel_test(g, op, fnum);
+    int idim = dgpu_friedel_test(g, op, fnum);
     BoxSpec box;
     for (int k = 0; k < 3; k++) { box.f[k] = fnum[k]; box.num[k] = num[k]; }
     FormSpec fs;

@@ -56,6 +56,8 @@ struct TcChoice {
 };
 typedef std::tuple<int32_t, int32_t, int32_t, int32_t, int32_t, int32_t, int32_t> TcKey;
 
+struct BatchState;   // k_batch.cu
+
 struct dgpu_ctx {
     int device = 0;
     int nsm = 0;
@@ -73,6 +75,7 @@ struct dgpu_ctx {
     DevBuf gq, gpart, grad, batch_desc, batch_aux;
     double batch_ms = 0.0;
     std::map<TcKey, TcChoice> tc_tuned;   // autotuner results per problem shape
+    BatchState *batch = nullptr;          // captured population graph and its buffers
     int32_t tc_last[4] = {-1, -1, -1, -1};
 };
 
@@ -146,7 +149,57 @@ int dgpu_direct_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du,
                      const BoxSpec &box, DevBuf &part, int32_t *nslice_out);
 
 // tc.cu -----------------------------------------------------------------
-// Partial sums are float2 (FP32, one per work item, RN-accumulated drains).
+// One problem (one crystal's type sums): geometry, atom arrays and the output
+// partials.  Lives in global memory; a launch may cover many problems.
+struct TcProblem {
+    int32_t f[3];
+    int32_t ra, rb, ac, fra;
+    int64_t sra, srb, sac;   // box-index strides of the row and column axes
+    int32_t nrows, ncols;
+    int32_t N;               // columns per tile (multiple of 16, <= TcLaunch::Nmax)
+    int32_t m_tiles, n_tiles, nslice, ntype;
+    int64_t slice_len, nitems, item0, pbox;
+    int64_t ts[65];
+    const uint64_t *ph0, *dra, *drb, *dac;   // phase data along the row axes and the column axis
+    const float *w;
+    float2 *part;
+};
+
+// Launch-wide constants: shared-memory and TMEM layout follow Nmax.
+struct TcLaunch {
+    const TcProblem *probs;
+    const int32_t *item_prob;   // problem index of every work item
+    int64_t nitems;
+    int32_t Nmax, stages, flush, nbuf, bf16;
+    uint32_t tmem_cols;
+    int32_t *err;
+};
+
+#include <vector>
+// One problem's inputs for a tensor-core launch.
+struct TcInput {
+    const uint64_t *ph0, *du, *dv, *dw;
+    const float *w;
+    const int64_t *ts;        // host: padded type ranges (ntype + 1 values)
+    int32_t ntype;
+    BoxSpec box;
+    int32_t axis;             // column axis, -1 = least padding
+};
+// A planned launch: descriptors uploaded, partial buffer allocated.
+struct TcPlan {
+    std::vector<TcProblem> probs;
+    std::vector<int32_t> item_prob;
+    TcLaunch L;
+    size_t smem = 0;
+    std::vector<int64_t> part_off;     // float2 offset of each problem's partials
+    std::vector<int32_t> nslice;
+};
+int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *op, int N, int slice_mult,
+                 TcPlan &plan, DevBuf &part, DevBuf &desc);
+int dgpu_tc_launch(dgpu_ctx *ctx, const TcPlan &plan);          // enqueues the kernel only
+int dgpu_tc_check(dgpu_ctx *ctx);                               // waits, reads the error flag
+// Single problem with autotuned tile; partial sums are float2 (FP32, one per
+// work item, RN-accumulated drains).
 int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const uint64_t *dv,
                  const uint64_t *dw, const float *w, const int64_t *h_type_start,
                  int32_t ntype, const BoxSpec &box, const dgpu_opts *op, DevBuf &part,
@@ -181,6 +234,29 @@ int dgpu_friedel_mirror(dgpu_ctx *ctx, const BoxSpec &box, int32_t idim, double2
                         double2 *acsf, double *dsi);
 int dgpu_qinfo(dgpu_ctx *ctx, const double eck[3], const double vi[9], const int32_t num[3],
                const double *dsi, double res[7]);
+
+// enqueue-only helpers for captured sequences (batch)
+void dgpu_type_ranges(const int32_t *iscat, int64_t n, int32_t nscat, int64_t *ts);
+int64_t dgpu_prepare_blocks(int64_t natoms);
+int dgpu_prepare_async(dgpu_ctx *ctx, const double *d_pos, const int32_t *d_iscat, const float *d_aocc,
+                       int64_t natoms, int32_t nscat, const PhaseGeom &g, int32_t *counts, int64_t *offs,
+                       int64_t *ts_dev, uint64_t *ph0, uint64_t *du, uint64_t *dv, uint64_t *dw, float *w,
+                       int32_t *idx);
+int dgpu_stltab_async(dgpu_ctx *ctx, const double eck[3], const double vi[9], const int32_t num[3],
+                      const double rten[9], int32_t *d_istl, int32_t *d_flag);
+size_t dgpu_formcoef_bytes();
+void dgpu_formcoef_fill(const dgpu_crystal *cr, void *host);
+int dgpu_formtab_async(dgpu_ctx *ctx, const void *d_coef, int32_t nscat, const dgpu_opts *op, double2 *d_cfact);
+int dgpu_combine_async(dgpu_ctx *ctx, const FormSpec *d_fs, const BoxSpec &box, const PartRef &part,
+                       const int32_t *istl, const double2 *cfact, double2 *csf, double *dsi, double diff_scale);
+int dgpu_adjoint_async(dgpu_ctx *ctx, const FormSpec *d_fs, const BoxSpec &box, int32_t friedel_dim,
+                       const dgpu_grid *grid, double diff_scale, int32_t nscat, const int64_t *ts,
+                       const uint64_t *ph0, const uint64_t *du, const uint64_t *dv, const uint64_t *dw,
+                       const float *w, const int32_t *aidx, const double2 *csf, const double *dsi,
+                       const int32_t *istl, const double2 *cfact, const double *it, const double *wt, double *g,
+                       double *chi, float2 *Q, double *gpos, double *gocc);
+int dgpu_friedel_test(const dgpu_grid *g, const dgpu_opts *op, int32_t fnum[3]);
+void dgpu_batch_free(dgpu_ctx *ctx);
 
 // the whole four_run with device-resident crystal arrays and outputs
 int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,

@@ -281,3 +281,37 @@ int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
     }
     return DGPU_OK;
 }
+
+// Enqueue-only adjoint of one crystal whose forward results (csf, dsi, istl,
+// cfact, prepared atoms) are on the device.  g: np doubles, chi: 513 doubles
+// (chi[512] receives chi^2), Q: nscat*pbox float2; gpos (3*natoms) and gocc
+// (natoms) must be zeroed by the caller.
+int dgpu_adjoint_async(dgpu_ctx *ctx, const FormSpec *d_fs, const BoxSpec &box, int32_t friedel_dim,
+                       const dgpu_grid *grid, double diff_scale, int32_t nscat, const int64_t *ts,
+                       const uint64_t *ph0, const uint64_t *du, const uint64_t *dv, const uint64_t *dw,
+                       const float *w, const int32_t *aidx, const double2 *csf, const double *dsi,
+                       const int32_t *istl, const double2 *cfact, const double *it, const double *wt, double *g,
+                       double *chi, float2 *Q, double *gpos, double *gocc)
+{
+    const int64_t np = (int64_t)box.num[0] * box.num[1] * box.num[2];
+    const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    k_adj_g<<<512, 256, 0, ctx->stream>>>(dsi, it, wt, np, g, chi);
+    k_adj_chi<<<1, 32, 0, ctx->stream>>>(chi, 512, chi + 512);
+    k_adj_q<<<(unsigned)dgpu_cdiv(nb, 256), 256, 0, ctx->stream>>>(d_fs, box, friedel_dim, g, csf, istl, cfact,
+                                                                     sqrt(diff_scale), Q);
+    AdjGeom ag;
+    for (int k = 0; k < 3; k++) {
+        ag.f[k] = box.f[k];
+        ag.eck[k] = grid->eck[k];
+    }
+    ag.pbox = nb;
+    memcpy(ag.vi, grid->vi, sizeof(ag.vi));
+    for (int t = 0; t < nscat; t++) {
+        const int64_t lo = ts[t], hi = ts[t + 1];
+        if (hi <= lo) continue;
+        k_adj_atoms<<<(unsigned)dgpu_cdiv(hi - lo, ADJ_NT), ADJ_NT, 0, ctx->stream>>>(
+            ph0, du, dv, dw, w, aidx, lo, hi, Q + (int64_t)t * nb, ag, gpos, gocc);
+    }
+    DGPU_CUDA(ctx, cudaGetLastError());
+    return DGPU_OK;
+}

@@ -1,11 +1,386 @@
-// Batched population (placeholder).
+// Batched population: many independent crystals (a DIFFEV population --
+// diffev/prog/with_mpi.f90:281-510 farms one four_run per member to MPI
+// workers) evaluated together on one GPU.
+//
+// All members' type sums run in ONE persistent tcgen05 launch (a multi-problem
+// work list, k_tc.cu); atom preparation, tables, combine, Friedel mirror and,
+// when targets are given, chi^2 and its gradient are small per-member kernels
+// on the same stream.  The whole sequence -- host-to-device copies from pinned
+// staging, kernels, device-to-host copies -- is captured once per batch shape
+// into a CUDA graph and replayed on later calls (new coordinates, same
+// shapes), so a population step costs one graph launch.
+#include <stdlib.h>
+
+#include <vector>
+
 #include "dgpu_internal.h"
 
-extern "C" int dgpu_batch_run(dgpu_ctx *ctx, int32_t, const dgpu_crystal *, const dgpu_grid *,
-                              const dgpu_opts *, double *const *, const double *const *,
-                              const double *const *, double *, double *const *, double *const *)
+namespace {
+
+struct Member {
+    int64_t natoms, abase, pbase;
+    int32_t nscat, idim;
+    int64_t ts[2 * 64 + 4];
+    int64_t np, nb, nblk;
+    BoxSpec box;
+    PhaseGeom geo;
+    dgpu_grid grid;
+    double ds;
+    double rten[9];
+    int64_t istl_off, cfact_off, pt_off, g_off, q_off, grad_off, cnt_off, offs_off, tsd_off, chi_off;
+};
+
+struct HostPinned {
+    void *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes)
+    {
+        if (bytes <= cap && p) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaHostAlloc(&p, bytes < 256 ? 256 : bytes, cudaHostAllocDefault);
+        if (e == cudaSuccess) cap = bytes < 256 ? 256 : bytes;
+        return e;
+    }
+    ~HostPinned()
+    {
+        if (p) cudaFreeHost(p);
+    }
+};
+
+}  // namespace
+
+struct BatchState {
+    std::vector<int64_t> sig;
+    std::vector<Member> mem;
+    bool targets = false, has_occ = false;
+    int64_t tot_atoms = 0, tot_pad = 0, tot_np = 0;
+    TcPlan plan;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    DevBuf d_pos, d_isc, d_aocc, d_ph0, d_du, d_dv, d_dw, d_w, d_idx, d_cnt, d_offs, d_tsd;
+    DevBuf d_istl, d_cfact, d_csf, d_dsi, d_g, d_q, d_chi, d_grad, d_coef, d_fs, d_it, d_wt, part, desc;
+    HostPinned h_pos, h_isc, h_aocc, h_it, h_wt, h_dsi, h_chi, h_grad;
+    ~BatchState()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        DevBuf *b[] = {&d_pos, &d_isc, &d_aocc, &d_ph0, &d_du, &d_dv, &d_dw, &d_w, &d_idx, &d_cnt, &d_offs,
+                       &d_tsd, &d_istl, &d_cfact, &d_csf, &d_dsi, &d_g, &d_q, &d_chi, &d_grad, &d_coef, &d_fs,
+                       &d_it, &d_wt, &part, &desc};
+        for (DevBuf *x : b) x->release();
+    }
+};
+
+void dgpu_batch_free(dgpu_ctx *ctx)
 {
-    return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "batch not built");
+    delete ctx->batch;
+    ctx->batch = nullptr;
+}
+
+// Everything one population step runs, in stream order (capturable).
+static int batch_enqueue(dgpu_ctx *ctx, BatchState &B, const dgpu_opts *op)
+{
+    cudaStream_t st = ctx->stream;
+    int32_t *flag = ctx->flag.as<int32_t>() + 12;
+    DGPU_CUDA(ctx, cudaMemcpyAsync(B.d_pos.p, B.h_pos.p, B.tot_atoms * 3 * sizeof(double), cudaMemcpyHostToDevice, st));
+    DGPU_CUDA(ctx, cudaMemcpyAsync(B.d_isc.p, B.h_isc.p, B.tot_atoms * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    if (B.has_occ)
+        DGPU_CUDA(ctx, cudaMemcpyAsync(B.d_aocc.p, B.h_aocc.p, B.tot_atoms * sizeof(float), cudaMemcpyHostToDevice, st));
+    if (B.targets) {
+        DGPU_CUDA(ctx, cudaMemcpyAsync(B.d_it.p, B.h_it.p, B.tot_np * sizeof(double), cudaMemcpyHostToDevice, st));
+        DGPU_CUDA(ctx, cudaMemcpyAsync(B.d_wt.p, B.h_wt.p, B.tot_np * sizeof(double), cudaMemcpyHostToDevice, st));
+        DGPU_CUDA(ctx, cudaMemsetAsync(B.d_grad.p, 0, B.tot_atoms * 4 * sizeof(double), st));
+    }
+    const size_t pad = (size_t)B.tot_pad;
+    DGPU_CUDA(ctx, cudaMemsetAsync(B.d_ph0.p, 0, pad * 8, st));
+    DGPU_CUDA(ctx, cudaMemsetAsync(B.d_du.p, 0, pad * 8, st));
+    DGPU_CUDA(ctx, cudaMemsetAsync(B.d_dv.p, 0, pad * 8, st));
+    DGPU_CUDA(ctx, cudaMemsetAsync(B.d_dw.p, 0, pad * 8, st));
+    DGPU_CUDA(ctx, cudaMemsetAsync(B.d_w.p, 0, pad * 4, st));
+    DGPU_CUDA(ctx, cudaMemsetAsync(B.d_idx.p, 0xFF, pad * 4, st));
+    DGPU_CUDA(ctx, cudaMemsetAsync(flag, 0, sizeof(int32_t), st));
+    for (size_t c = 0; c < B.mem.size(); c++) {
+        Member &m = B.mem[c];
+        int rc = dgpu_prepare_async(ctx, B.d_pos.as<double>() + 3 * m.abase, B.d_isc.as<int32_t>() + m.abase,
+                                    B.has_occ ? B.d_aocc.as<float>() + m.abase : nullptr, m.natoms, m.nscat, m.geo,
+                                    B.d_cnt.as<int32_t>() + m.cnt_off, B.d_offs.as<int64_t>() + m.offs_off,
+                                    B.d_tsd.as<int64_t>() + m.tsd_off, B.d_ph0.as<uint64_t>() + m.pbase,
+                                    B.d_du.as<uint64_t>() + m.pbase, B.d_dv.as<uint64_t>() + m.pbase,
+                                    B.d_dw.as<uint64_t>() + m.pbase, B.d_w.as<float>() + m.pbase,
+                                    B.d_idx.as<int32_t>() + m.pbase);
+        if (rc) return rc;
+        rc = dgpu_stltab_async(ctx, m.grid.eck, m.grid.vi, m.grid.inc, m.rten, B.d_istl.as<int32_t>() + m.istl_off,
+                               flag);
+        if (rc) return rc;
+        rc = dgpu_formtab_async(ctx, (const char *)B.d_coef.p + c * dgpu_formcoef_bytes(), m.nscat, op,
+                                B.d_cfact.as<double2>() + m.cfact_off);
+        if (rc) return rc;
+    }
+    int rc = dgpu_tc_launch(ctx, B.plan);
+    if (rc) return rc;
+    for (size_t c = 0; c < B.mem.size(); c++) {
+        Member &m = B.mem[c];
+        const FormSpec *fs = B.d_fs.as<FormSpec>() + c;
+        PartRef pr = {B.part.as<float2>() + B.plan.part_off[c], B.plan.nslice[c], 1};
+        double2 *csf = B.d_csf.as<double2>() + m.pt_off;
+        double *dsi = B.d_dsi.as<double>() + m.pt_off;
+        rc = dgpu_combine_async(ctx, fs, m.box, pr, B.d_istl.as<int32_t>() + m.istl_off,
+                                B.d_cfact.as<double2>() + m.cfact_off, csf, dsi, m.ds);
+        if (rc) return rc;
+        rc = dgpu_friedel_mirror(ctx, m.box, m.idim, csf, nullptr, dsi);
+        if (rc) return rc;
+        if (B.targets) {
+            double *gpos = B.d_grad.as<double>() + m.grad_off;
+            rc = dgpu_adjoint_async(ctx, fs, m.box, m.idim, &m.grid, m.ds, m.nscat, m.ts,
+                                    B.d_ph0.as<uint64_t>() + m.pbase, B.d_du.as<uint64_t>() + m.pbase,
+                                    B.d_dv.as<uint64_t>() + m.pbase, B.d_dw.as<uint64_t>() + m.pbase,
+                                    B.d_w.as<float>() + m.pbase, B.d_idx.as<int32_t>() + m.pbase, csf, dsi,
+                                    B.d_istl.as<int32_t>() + m.istl_off, B.d_cfact.as<double2>() + m.cfact_off,
+                                    B.d_it.as<double>() + m.pt_off, B.d_wt.as<double>() + m.pt_off,
+                                    B.d_g.as<double>() + m.pt_off, B.d_chi.as<double>() + m.chi_off,
+                                    B.d_q.as<float2>() + m.q_off, gpos, gpos + 3 * m.natoms);
+            if (rc) return rc;
+            DGPU_CUDA(ctx, cudaMemcpyAsync((double *)B.h_chi.p + c, B.d_chi.as<double>() + m.chi_off + 512,
+                                           sizeof(double), cudaMemcpyDeviceToHost, st));
+        }
+    }
+    DGPU_CUDA(ctx, cudaMemcpyAsync(B.h_dsi.p, B.d_dsi.p, B.tot_np * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (B.targets)
+        DGPU_CUDA(ctx, cudaMemcpyAsync(B.h_grad.p, B.d_grad.p, B.tot_atoms * 4 * sizeof(double),
+                                       cudaMemcpyDeviceToHost, st));
+    return DGPU_OK;
+}
+
+static int batch_build(dgpu_ctx *ctx, BatchState &B, int32_t nc, const dgpu_crystal *crs, const dgpu_grid *grids,
+                       const dgpu_opts *op)
+{
+    B.mem.assign(nc, Member());
+    int64_t abase = 0, pbase = 0, np_tot = 0, istl = 0, cf = 0, q = 0, cnt = 0, tsd = 0;
+    for (int c = 0; c < nc; c++) {
+        Member &m = B.mem[c];
+        const dgpu_crystal &cr = crs[c];
+        m.natoms = cr.natoms;
+        m.nscat = cr.nscat;
+        m.abase = abase;
+        m.pbase = pbase;
+        m.grid = grids[c];
+        m.ds = op->diff_scale;
+        memcpy(m.rten, cr.rten, sizeof(m.rten));
+        dgpu_type_ranges(cr.iscat, cr.natoms, cr.nscat, m.ts);
+        int32_t fnum[3];
+        m.idim = dgpu_friedel_test(&grids[c], op, fnum);
+        for (int k = 0; k < 3; k++) {
+            m.box.f[k] = fnum[k];
+            m.box.num[k] = grids[c].inc[k];
+        }
+        m.np = (int64_t)grids[c].inc[0] * grids[c].inc[1] * grids[c].inc[2];
+        m.nb = (int64_t)fnum[0] * fnum[1] * fnum[2];
+        m.nblk = dgpu_prepare_blocks(cr.natoms);
+        memset(&m.geo, 0, sizeof(m.geo));
+        m.geo.mode = DGPU_PHASE_EXACT64;
+        for (int k = 0; k < 3; k++) m.geo.eck[k] = grids[c].eck[k];
+        memcpy(m.geo.vi, grids[c].vi, sizeof(m.geo.vi));
+        m.istl_off = istl;
+        m.cfact_off = cf;
+        m.pt_off = np_tot;
+        m.g_off = np_tot;
+        m.q_off = q;
+        m.grad_off = 4 * abase;
+        m.cnt_off = cnt;
+        m.offs_off = cnt;
+        m.tsd_off = tsd;
+        m.chi_off = (int64_t)c * 520;
+        abase += cr.natoms;
+        pbase += m.ts[cr.nscat] > 0 ? m.ts[cr.nscat] : 0;
+        pbase = (pbase + 31) / 32 * 32;
+        np_tot += m.np;
+        istl += m.np;
+        cf += (int64_t)cr.nscat * DGPU_NTAB;
+        q += (int64_t)cr.nscat * m.nb;
+        cnt += m.nblk * cr.nscat;
+        tsd += 2 * cr.nscat + 1;
+    }
+    B.tot_atoms = abase;
+    B.tot_pad = pbase > 0 ? pbase : 32;
+    B.tot_np = np_tot;
+    B.has_occ = false;
+    for (int c = 0; c < nc; c++) B.has_occ = B.has_occ || crs[c].atom_occ;
+    const size_t na = (size_t)(abase > 0 ? abase : 1), npd = (size_t)B.tot_pad;
+    DGPU_CUDA(ctx, B.d_pos.ensure(na * 3 * 8));
+    DGPU_CUDA(ctx, B.d_isc.ensure(na * 4));
+    DGPU_CUDA(ctx, B.d_aocc.ensure(na * 4));
+    DGPU_CUDA(ctx, B.d_ph0.ensure(npd * 8));
+    DGPU_CUDA(ctx, B.d_du.ensure(npd * 8));
+    DGPU_CUDA(ctx, B.d_dv.ensure(npd * 8));
+    DGPU_CUDA(ctx, B.d_dw.ensure(npd * 8));
+    DGPU_CUDA(ctx, B.d_w.ensure(npd * 4));
+    DGPU_CUDA(ctx, B.d_idx.ensure(npd * 4));
+    DGPU_CUDA(ctx, B.d_cnt.ensure((size_t)(cnt > 0 ? cnt : 1) * 4));
+    DGPU_CUDA(ctx, B.d_offs.ensure((size_t)(cnt > 0 ? cnt : 1) * 8));
+    DGPU_CUDA(ctx, B.d_tsd.ensure((size_t)(tsd > 0 ? tsd : 1) * 8));
+    DGPU_CUDA(ctx, B.d_istl.ensure((size_t)istl * 4));
+    DGPU_CUDA(ctx, B.d_cfact.ensure((size_t)cf * 16));
+    DGPU_CUDA(ctx, B.d_csf.ensure((size_t)np_tot * 16));
+    DGPU_CUDA(ctx, B.d_dsi.ensure((size_t)np_tot * 8));
+    DGPU_CUDA(ctx, B.d_g.ensure((size_t)np_tot * 8));
+    DGPU_CUDA(ctx, B.d_q.ensure((size_t)(q > 0 ? q : 1) * 8));
+    DGPU_CUDA(ctx, B.d_chi.ensure((size_t)nc * 520 * 8));
+    DGPU_CUDA(ctx, B.d_grad.ensure(na * 4 * 8));
+    DGPU_CUDA(ctx, B.d_it.ensure((size_t)np_tot * 8));
+    DGPU_CUDA(ctx, B.d_wt.ensure((size_t)np_tot * 8));
+    DGPU_CUDA(ctx, B.h_pos.ensure(na * 3 * 8));
+    DGPU_CUDA(ctx, B.h_isc.ensure(na * 4));
+    DGPU_CUDA(ctx, B.h_aocc.ensure(na * 4));
+    DGPU_CUDA(ctx, B.h_it.ensure((size_t)np_tot * 8));
+    DGPU_CUDA(ctx, B.h_wt.ensure((size_t)np_tot * 8));
+    DGPU_CUDA(ctx, B.h_dsi.ensure((size_t)np_tot * 8));
+    DGPU_CUDA(ctx, B.h_chi.ensure((size_t)nc * 8));
+    DGPU_CUDA(ctx, B.h_grad.ensure(na * 4 * 8));
+    DGPU_CUDA(ctx, ctx->flag.ensure(64));
+    // per-member form-factor coefficients and FormSpecs
+    const size_t cb = dgpu_formcoef_bytes();
+    DGPU_CUDA(ctx, B.d_coef.ensure((size_t)nc * cb));
+    DGPU_CUDA(ctx, B.d_fs.ensure((size_t)nc * sizeof(FormSpec)));
+    std::vector<char> coef((size_t)nc * cb);
+    std::vector<FormSpec> fs(nc);
+    for (int c = 0; c < nc; c++) {
+        dgpu_formcoef_fill(&crs[c], coef.data() + c * cb);
+        dgpu_fill_formspec(ctx, &crs[c], op, &grids[c], fs[c]);
+    }
+    DGPU_CUDA(ctx, cudaMemcpyAsync(B.d_coef.p, coef.data(), coef.size(), cudaMemcpyHostToDevice, ctx->stream));
+    DGPU_CUDA(ctx, cudaMemcpyAsync(B.d_fs.p, fs.data(), fs.size() * sizeof(FormSpec), cudaMemcpyHostToDevice,
+                                   ctx->stream));
+    // one multi-problem tensor-core plan over all members
+    std::vector<TcInput> in(nc);
+    for (int c = 0; c < nc; c++) {
+        Member &m = B.mem[c];
+        in[c].ph0 = B.d_ph0.as<uint64_t>() + m.pbase;
+        in[c].du = B.d_du.as<uint64_t>() + m.pbase;
+        in[c].dv = B.d_dv.as<uint64_t>() + m.pbase;
+        in[c].dw = B.d_dw.as<uint64_t>() + m.pbase;
+        in[c].w = B.d_w.as<float>() + m.pbase;
+        in[c].ts = m.ts;
+        in[c].ntype = m.nscat;
+        in[c].box = m.box;
+        in[c].axis = -1;
+    }
+    const int N = op->tc_tile_n > 0 ? op->tc_tile_n : 64;
+    int rc = dgpu_tc_plan(ctx, nc, in.data(), op, N, 4, B.plan, B.part, B.desc);
+    if (rc) return rc;
+    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return DGPU_OK;
+}
+
+extern "C" int dgpu_batch_run(dgpu_ctx *ctx, int32_t nc, const dgpu_crystal *crs, const dgpu_grid *grids,
+                              const dgpu_opts *op, double *const *dsi, const double *const *i_target,
+                              const double *const *weight, double *chi2, double *const *grad_pos,
+                              double *const *grad_occ)
+{
+    if (!ctx || nc < 1 || !crs || !grids || !op || !dsi) return DGPU_ERR_ARG;
+    if (op->phase != DGPU_PHASE_EXACT64 || op->fave != 0.0 || op->ano)
+        return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "batch: EXACT64 phases, no <F>, no anomalous scattering");
+    if (!dgpu_tc_available(ctx)) return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "batch needs the tensor-core engine");
+    const bool targets = i_target != nullptr;
+    if (targets && !chi2) return dgpu_set_error(ctx, DGPU_ERR_ARG, "chi2 output missing");
+    for (int c = 0; c < nc; c++) {
+        if (crs[c].natoms < 1 || !crs[c].pos || !crs[c].iscat || crs[c].nscat < 1 || crs[c].nscat > 63)
+            return dgpu_set_error(ctx, DGPU_ERR_ARG, "batch member %d: bad crystal", c);
+        if (!dsi[c] || (targets && !i_target[c])) return dgpu_set_error(ctx, DGPU_ERR_ARG, "member %d: buffers", c);
+        for (int k = 0; k < 3; k++)
+            if (grids[c].inc[k] < 1) return dgpu_set_error(ctx, DGPU_ERR_ARG, "member %d: inc", c);
+    }
+    DGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+    // batch shape signature: sizes, types and the options that shape the graph
+    std::vector<int64_t> sig;
+    sig.push_back(nc);
+    sig.push_back(targets);
+    sig.push_back(op->tc_tile_n);
+    sig.push_back(op->form * 16 + op->ldbw * 4 + op->lxray * 2 + op->friedel);
+    sig.push_back(op->power);
+    sig.push_back((int64_t)(op->diff_scale * 1e12));
+    for (int c = 0; c < nc; c++) {
+        sig.push_back(crs[c].natoms);
+        sig.push_back(crs[c].nscat);
+        sig.push_back(crs[c].atom_occ != nullptr);
+        int64_t ts[2 * 64 + 4];
+        dgpu_type_ranges(crs[c].iscat, crs[c].natoms, crs[c].nscat, ts);
+        for (int t = 0; t <= crs[c].nscat; t++) sig.push_back(ts[t]);
+        for (int k = 0; k < 12; k++) sig.push_back((int64_t)(grids[c].eck[k] * 1e9));
+        for (int k = 0; k < 9; k++) sig.push_back((int64_t)(grids[c].vi[k] * 1e12));
+        for (int k = 0; k < 3; k++) sig.push_back(grids[c].inc[k]);
+        for (int t = 0; t <= crs[c].nscat; t++) {
+            for (int i = 0; i < 11; i++) sig.push_back((int64_t)(crs[c].scat[11 * t + i] * 1e9));
+            sig.push_back((int64_t)(crs[c].occ[t] * 1e9));
+            sig.push_back((int64_t)(crs[c].dw[t] * 1e9));
+        }
+        for (int k = 0; k < 9; k++) sig.push_back((int64_t)(crs[c].rten[k] * 1e15));
+    }
+    if (!ctx->batch || ctx->batch->sig != sig) {
+        dgpu_batch_free(ctx);
+        ctx->batch = new BatchState();
+        ctx->batch->sig = sig;
+        ctx->batch->targets = targets;
+        int rc = batch_build(ctx, *ctx->batch, nc, crs, grids, op);
+        if (rc) {
+            dgpu_batch_free(ctx);
+            return rc;
+        }
+    }
+    BatchState &B = *ctx->batch;
+    // stage this step's inputs in pinned memory
+    for (int c = 0; c < nc; c++) {
+        const Member &m = B.mem[c];
+        memcpy((double *)B.h_pos.p + 3 * m.abase, crs[c].pos, m.natoms * 3 * sizeof(double));
+        memcpy((int32_t *)B.h_isc.p + m.abase, crs[c].iscat, m.natoms * sizeof(int32_t));
+        if (B.has_occ) {
+            float *o = (float *)B.h_aocc.p + m.abase;
+            if (crs[c].atom_occ) memcpy(o, crs[c].atom_occ, m.natoms * sizeof(float));
+            else for (int64_t i = 0; i < m.natoms; i++) o[i] = 1.0f;
+        }
+        if (targets) {
+            memcpy((double *)B.h_it.p + m.pt_off, i_target[c], m.np * sizeof(double));
+            double *w = (double *)B.h_wt.p + m.pt_off;
+            if (weight && weight[c]) memcpy(w, weight[c], m.np * sizeof(double));
+            else for (int64_t p = 0; p < m.np; p++) w[p] = 1.0;
+        }
+    }
+    if (!B.exec) {
+        DGPU_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = batch_enqueue(ctx, B, op);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) return dgpu_set_error(ctx, DGPU_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+        B.graph = g;
+        DGPU_CUDA(ctx, cudaGraphInstantiate(&B.exec, B.graph, 0));
+    }
+    DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[4], ctx->stream));
+    DGPU_CUDA(ctx, cudaGraphLaunch(B.exec, ctx->stream));
+    DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[5], ctx->stream));
+    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    float ms = 0.f;
+    DGPU_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[4], ctx->ev[5]));
+    ctx->batch_ms = ms;
+    int32_t flags[8];
+    DGPU_CUDA(ctx, cudaMemcpy(flags, ctx->flag.as<int32_t>() + 8, sizeof(flags), cudaMemcpyDeviceToHost));
+    if (flags[0]) return dgpu_set_error(ctx, DGPU_ERR_TIMEOUT, "tensor-core kernel wait gave up (site %d)", flags[0]);
+    if (flags[4]) return dgpu_set_error(ctx, DGPU_ERR_STL_RANGE, "sin(theta)/lambda beyond the table in a member");
+    for (int c = 0; c < nc; c++) {
+        const Member &m = B.mem[c];
+        memcpy(dsi[c], (double *)B.h_dsi.p + m.pt_off, m.np * sizeof(double));
+        if (targets) {
+            chi2[c] = ((double *)B.h_chi.p)[c];
+            const double *gpos = (double *)B.h_grad.p + m.grad_off;
+            if (grad_pos && grad_pos[c]) memcpy(grad_pos[c], gpos, m.natoms * 3 * sizeof(double));
+            if (grad_occ && grad_occ[c]) memcpy(grad_occ[c], gpos + 3 * m.natoms, m.natoms * sizeof(double));
+        }
+    }
+    return DGPU_OK;
 }
 
 extern "C" double dgpu_batch_last_ms(const dgpu_ctx *ctx) { return ctx ? ctx->batch_ms : 0.0; }

@@ -354,3 +354,19 @@ int dgpu_qinfo(dgpu_ctx *ctx, const double eck[3], const double vi[9], const int
     DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return DGPU_OK;
 }
+
+// enqueue-only combine: FormSpec already in device memory
+int dgpu_combine_async(dgpu_ctx *ctx, const FormSpec *d_fs, const BoxSpec &box, const PartRef &part,
+                       const int32_t *istl, const double2 *cfact, double2 *csf, double *dsi, double diff_scale)
+{
+    const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    const unsigned nblk = (unsigned)dgpu_cdiv(nb, 256);
+    if (part.f32)
+        k_combine<float2><<<nblk, 256, 0, ctx->stream>>>(d_fs, box, (const float2 *)part.p, part.nslice, istl, cfact,
+                                                          nullptr, csf, dsi, diff_scale, sqrt(diff_scale));
+    else
+        k_combine<double2><<<nblk, 256, 0, ctx->stream>>>(d_fs, box, (const double2 *)part.p, part.nslice, istl,
+                                                           cfact, nullptr, csf, dsi, diff_scale, sqrt(diff_scale));
+    DGPU_CUDA(ctx, cudaGetLastError());
+    return DGPU_OK;
+}

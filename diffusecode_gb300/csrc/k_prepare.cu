@@ -422,3 +422,78 @@ int dgpu_increments_dev(dgpu_ctx *ctx, const double *d_xat, int64_t nxat, const 
     }
     return DGPU_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Enqueue-only variants (no host synchronisation; usable under stream capture).
+// counts: int32[nblk*nscat], offs: int64[nblk*nscat], ts_dev: int64[2*nscat+1]
+// scratch; the phase arrays receive the atoms at the type ranges the host
+// computed with the same padding rule (dgpu_type_ranges).
+void dgpu_type_ranges(const int32_t *iscat, int64_t n, int32_t nscat, int64_t *ts)
+{
+    int64_t cnt[MAXT] = {0};
+    for (int64_t i = 0; i < n; i++)
+        if (iscat[i] >= 1 && iscat[i] <= nscat) cnt[iscat[i]]++;
+    int64_t c = 0;
+    for (int t = 0; t < nscat; t++) {
+        c = (c + TYPE_ALIGN - 1) / TYPE_ALIGN * TYPE_ALIGN;
+        ts[t] = c;
+        ts[nscat + 1 + t] = cnt[t + 1];
+        c += cnt[t + 1];
+    }
+    ts[nscat] = (c + TYPE_ALIGN - 1) / TYPE_ALIGN * TYPE_ALIGN;
+}
+
+int64_t dgpu_prepare_blocks(int64_t natoms) { return dgpu_cdiv(natoms > 0 ? natoms : 1, PREP_BLK); }
+
+int dgpu_prepare_async(dgpu_ctx *ctx, const double *d_pos, const int32_t *d_iscat, const float *d_aocc,
+                       int64_t natoms, int32_t nscat, const PhaseGeom &g, int32_t *counts, int64_t *offs,
+                       int64_t *ts_dev, uint64_t *ph0, uint64_t *du, uint64_t *dv, uint64_t *dw, float *w,
+                       int32_t *idx)
+{
+    const int64_t nblk = dgpu_prepare_blocks(natoms);
+    FoldSpec nofold = {0, 1, {1, 1, 1}, {0, 0, 0}, nullptr};
+    k_type_count<<<(unsigned)nblk, PREP_BLK, 0, ctx->stream>>>(d_iscat, natoms, nscat, nofold, counts, nblk);
+    k_scan_counts<<<1, 1024, 0, ctx->stream>>>(counts, nblk * nscat, offs, nblk, nscat, ts_dev);
+    k_scatter_atoms<<<(unsigned)nblk, PREP_BLK, 0, ctx->stream>>>(d_pos, d_iscat, d_aocc, natoms, nscat, nofold, g,
+                                                                  offs, nblk, ph0, du, dv, dw, w, idx);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    return DGPU_OK;
+}
+
+int dgpu_stltab_async(dgpu_ctx *ctx, const double eck[3], const double vi[9], const int32_t num[3],
+                      const double rten[9], int32_t *d_istl, int32_t *d_flag)
+{
+    const int64_t np = (int64_t)num[0] * num[1] * num[2];
+    PhaseGeom vg;
+    memset(&vg, 0, sizeof(vg));
+    memcpy(vg.vi, vi, sizeof(vg.vi));
+    k_stltab<<<(unsigned)dgpu_cdiv(np, 256), 256, 0, ctx->stream>>>(
+        eck[0], eck[1], eck[2], vg, num[0], num[1], num[2], rten[0], rten[1], rten[2], rten[3], rten[4], rten[5],
+        rten[6], rten[7], rten[8], d_istl, d_flag);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    return DGPU_OK;
+}
+
+size_t dgpu_formcoef_bytes() { return sizeof(FormCoef); }
+
+void dgpu_formcoef_fill(const dgpu_crystal *cr, void *host)
+{
+    FormCoef *h = (FormCoef *)host;
+    memset(h, 0, sizeof(FormCoef));
+    for (int t = 0; t <= cr->nscat && t < MAXT; t++) {
+        for (int i = 0; i < 11; i++) h->scat[11 * t + i] = cr->scat[11 * t + i];
+        h->occ[t] = cr->occ[t];
+        h->dw[t] = cr->dw[t];
+        h->delfr[t] = cr->delfr ? cr->delfr[t] : 0.0;
+        h->delfi[t] = cr->delfi ? cr->delfi[t] : 0.0;
+    }
+}
+
+int dgpu_formtab_async(dgpu_ctx *ctx, const void *d_coef, int32_t nscat, const dgpu_opts *op, double2 *d_cfact)
+{
+    const int64_t n = (int64_t)nscat * DGPU_NTAB;
+    k_formtab<<<(unsigned)dgpu_cdiv(n, 256), 256, 0, ctx->stream>>>((const FormCoef *)d_coef, nscat, op->lxray,
+                                                                      op->power, op->ano, op->ldbw, d_cfact);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    return DGPU_OK;
+}

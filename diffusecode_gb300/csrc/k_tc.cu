@@ -55,22 +55,6 @@
 #define TC_FLUSH_STAGES 4                      // 128 atoms per drain of the main accumulator
 #endif
 
-struct TcGeom {
-    int32_t f[3];
-    int32_t ra, rb, ac, fra;
-    int64_t sra, srb, sac;   // box-index strides of the row and column axes
-    int32_t nrows, ncols;
-    int32_t N;               // columns per tile (multiple of 16, <= 128)
-    int32_t m_tiles, n_tiles, nslice, ntype;
-    int64_t slice_len, nitems, pbox;
-    int32_t stages;
-    int32_t flush;           // stages per drain of the main accumulator
-    int32_t nbuf;            // main accumulator buffers in TMEM (1 or 2)
-    int32_t bf16;
-    uint32_t tmem_cols;
-    int64_t ts[65];
-};
-
 // ---------------------------------------------------------------------------
 // PTX helpers
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -233,15 +217,7 @@ __device__ __forceinline__ void split8(const float (&v)[8], uint4 &hi, uint4 &lo
 // byte offset of (row, k-group) in one operand of the canonical layout
 __device__ __forceinline__ uint32_t core_off(int row, int q) { return (row >> 3) * TC_SBO + q * TC_LBO + (row & 7) * 16; }
 
-struct TcArgs {
-    const uint64_t *ph0;
-    const uint64_t *dra, *drb, *dac;   // increments along the row axes and the column axis
-    const float *w;
-    float2 *part;
-    int32_t *err;
-};
-
-__device__ __forceinline__ void decode_item(const TcGeom &g, int64_t item, int &t, int &ks, int &nt, int &mt)
+__device__ __forceinline__ void decode_item(const TcProblem &g, int64_t item, int &t, int &ks, int &nt, int &mt)
 {
     mt = (int)(item % g.m_tiles);
     int64_t r = item / g.m_tiles;
@@ -251,12 +227,12 @@ __device__ __forceinline__ void decode_item(const TcGeom &g, int64_t item, int &
     t = (int)(r / g.nslice);
 }
 
-__global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcGeom g, const TcArgs args)
+__global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
-    const int S = g.stages;
-    const int N = g.N;
-    const uint32_t b_bytes = (uint32_t)N * TC_KA * 2;      // one B operand
+    const int S = L.stages;
+    const int NM = L.Nmax;
+    const uint32_t b_bytes = (uint32_t)NM * TC_KA * 2;     // one B operand
     const uint32_t stage_bytes = 4 * TC_A_BYTES + 4 * b_bytes;
     uint64_t *full = reinterpret_cast<uint64_t *>(smem + (size_t)S * stage_bytes);
     uint64_t *empty = full + S;
@@ -267,8 +243,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcGeom g, const TcAr
     uint64_t *drain = cempty + 1;
     uint32_t *tbase = reinterpret_cast<uint32_t *>(drain + 1);
     uint8_t *aslot = smem + (size_t)S * stage_bytes + TC_BAR_BYTES;   // 2 x TC_ATOM_SLOT
-    volatile int32_t *err = args.err;
-    const bool bf = g.bf16 != 0;
+    volatile int32_t *err = L.err;
+    const bool bf = L.bf16 != 0;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -287,7 +263,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcGeom g, const TcAr
     }
     if (warp == TC_MMA_WARP) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tbase)),
-                     "r"(g.tmem_cols)
+                     "r"(L.tmem_cols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -304,32 +280,34 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcGeom g, const TcAr
         const int tid = threadIdx.x;
         uint32_t it = 0;
         bool ok = true;
-        const uint64_t *src[4] = {args.ph0, args.dra, args.drb, args.dac};
-        auto issue = [&](int slot, int64_t ab) {
+        auto issue = [&](const TcProblem &P, int slot, int64_t ab) {
             uint8_t *dst = aslot + slot * TC_ATOM_SLOT;
             if (tid < 64) {            // 4 arrays x 16 chunks of 16 B
                 const int arr = tid >> 4, ch = tid & 15;
-                cp_async16(dst + arr * (TC_KA * 8) + ch * 16, src[arr] + ab + ch * 2);
+                const uint64_t *src = arr == 0 ? P.ph0 : arr == 1 ? P.dra : arr == 2 ? P.drb : P.dac;
+                cp_async16(dst + arr * (TC_KA * 8) + ch * 16, src + ab + ch * 2);
             } else if (tid < 72) {     // weights: 8 chunks
                 const int ch = tid - 64;
-                cp_async16(dst + 4 * TC_KA * 8 + ch * 16, args.w + ab + ch * 4);
+                cp_async16(dst + 4 * TC_KA * 8 + ch * 16, P.w + ab + ch * 4);
             }
             cp_async_commit();
         };
-        for (int64_t item = blockIdx.x; item < g.nitems && ok; item += gridDim.x) {
+        for (int64_t item = blockIdx.x; item < L.nitems && ok; item += gridDim.x) {
+            const TcProblem &g = L.probs[L.item_prob[item]];
+            const int N = g.N;
             int t, ks, nt, mt;
-            decode_item(g, item, t, ks, nt, mt);
+            decode_item(g, item - g.item0, t, ks, nt, mt);
             const int64_t a0 = g.ts[t] + (int64_t)ks * g.slice_len;
             const int64_t a1 = min(g.ts[t + 1], a0 + g.slice_len);
             const int64_t cnt = a1 > a0 ? a1 - a0 : 0;
             const int nst = (int)(cnt / TC_KA);
             if (nst == 0) continue;
             producers_sync();               // previous item's slots are free
-            issue(0, a0);
+            issue(g, 0, a0);
             for (int st = 0; st < nst; st++, it++) {
                 const int s = it % S;
                 if (st + 1 < nst) {
-                    issue((st + 1) & 1, a0 + (int64_t)(st + 1) * TC_KA);
+                    issue(g, (st + 1) & 1, a0 + (int64_t)(st + 1) * TC_KA);
                     cp_async_wait1();
                 } else {
                     cp_async_wait0();
@@ -401,29 +379,31 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcGeom g, const TcAr
     } else if (warp == TC_MMA_WARP) {
         // ------------------------------------------------------------ MMA issuer
         const uint32_t fmt = bf ? 1u : 0u;
-        const uint32_t idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(N >> 3) << 17) |
-                               ((uint32_t)(TC_M >> 4) << 24);
-        const uint32_t idesc_neg = idesc | (1u << 13);     // negate A: the -Ui Vi^T products
-        const uint32_t c_re = tmem, c_im = tmem + (uint32_t)N;  // correction accumulator
+        const uint32_t c_re = tmem, c_im = tmem + (uint32_t)NM;  // correction accumulator
         uint32_t it = 0, nitem = 0, nchunk = 0;
         bool ok = true, issued = false;
-        for (int64_t item = blockIdx.x; item < g.nitems && ok; item += gridDim.x) {
+        for (int64_t item = blockIdx.x; item < L.nitems && ok; item += gridDim.x) {
+            const TcProblem &g = L.probs[L.item_prob[item]];
+            const int N = g.N;
             int t, ks, nt, mt;
-            decode_item(g, item, t, ks, nt, mt);
+            decode_item(g, item - g.item0, t, ks, nt, mt);
             const int64_t a0 = g.ts[t] + (int64_t)ks * g.slice_len;
             const int64_t a1 = min(g.ts[t + 1], a0 + g.slice_len);
             const int64_t cnt = a1 > a0 ? a1 - a0 : 0;
             const int nst = (int)((cnt + TC_KA - 1) / TC_KA);
             if (nst == 0) continue;
+            const uint32_t idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(N >> 3) << 17) |
+                                   ((uint32_t)(TC_M >> 4) << 24);
+            const uint32_t idesc_neg = idesc | (1u << 13);     // negate A: the -Ui Vi^T products
             // the correction accumulator restarts with this item: previous one drained?
             if (nitem > 0 && !mbar_wait(cempty, (nitem - 1) & 1, err, 2)) { ok = false; break; }
-            for (int st0 = 0; st0 < nst && ok; st0 += g.flush, nchunk++) {
-                const int b = (int)(nchunk % g.nbuf);
-                const uint32_t use = nchunk / g.nbuf;
+            for (int st0 = 0; st0 < nst && ok; st0 += L.flush, nchunk++) {
+                const int b = (int)(nchunk % L.nbuf);
+                const uint32_t use = nchunk / L.nbuf;
                 if (use > 0 && !mbar_wait(&mempty[b], (use - 1) & 1, err, 6)) { ok = false; break; }
                 tc_fence_after();
-                const uint32_t m_re = tmem + 2u * N * (1u + (uint32_t)b), m_im = m_re + (uint32_t)N;
-                const int st1 = min(nst, st0 + g.flush);
+                const uint32_t m_re = tmem + 2u * NM * (1u + (uint32_t)b), m_im = m_re + (uint32_t)NM;
+                const int st1 = min(nst, st0 + L.flush);
                 for (int st = st0; st < st1; st++, it++) {
                     const int s = it % S;
                     if (!mbar_wait(&full[s], (it / S) & 1, err, 3)) { ok = false; break; }
@@ -480,9 +460,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcGeom g, const TcAr
         const int r = q * 32 + lane;
         uint32_t nitem = 0, nchunk = 0;
         bool ok = true;
-        for (int64_t item = blockIdx.x; item < g.nitems && ok; item += gridDim.x) {
+        for (int64_t item = blockIdx.x; item < L.nitems && ok; item += gridDim.x) {
+            const TcProblem &g = L.probs[L.item_prob[item]];
+            const int N = g.N;
             int t, ks, nt, mt;
-            decode_item(g, item, t, ks, nt, mt);
+            decode_item(g, item - g.item0, t, ks, nt, mt);
             const int64_t a0 = g.ts[t] + (int64_t)ks * g.slice_len;
             const int64_t a1 = min(g.ts[t + 1], a0 + g.slice_len);
             const int64_t cnt = a1 > a0 ? a1 - a0 : 0;
@@ -490,7 +472,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcGeom g, const TcAr
             const int64_t rg = (int64_t)mt * TC_M + r;
             const bool rv = rg < g.nrows;
             const int64_t prow = rv ? (rg % g.fra) * g.sra + (rg / g.fra) * g.srb : 0;
-            float2 *out = args.part + ((int64_t)t * g.nslice + ks) * g.pbox + prow;
+            float2 *out = g.part + ((int64_t)t * g.nslice + ks) * g.pbox + prow;
             const int64_t cbase0 = (int64_t)nt * N;
             if (nst == 0) {
                 if (rv)
@@ -498,16 +480,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcGeom g, const TcAr
                 continue;
             }
             // main accumulator, one chunk at a time: first chunk stores, later chunks add
-            for (int st0 = 0; st0 < nst; st0 += g.flush, nchunk++) {
-                const int b = (int)(nchunk % g.nbuf);
-                if (!mbar_wait(&mfull[b], (nchunk / g.nbuf) & 1, err, 5)) { ok = false; break; }
+            for (int st0 = 0; st0 < nst; st0 += L.flush, nchunk++) {
+                const int b = (int)(nchunk % L.nbuf);
+                if (!mbar_wait(&mfull[b], (nchunk / L.nbuf) & 1, err, 5)) { ok = false; break; }
                 tc_fence_after();
-                const uint32_t col0 = 2u * N * (1u + (uint32_t)b);
+                const uint32_t col0 = 2u * NM * (1u + (uint32_t)b);
                 for (int c0 = 0; c0 < N; c0 += 16) {
                     uint32_t vr[16], vi[16];
                     const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + col0 + (uint32_t)c0;
                     tmem_ld16(ta, vr);
-                    tmem_ld16(ta + (uint32_t)N, vi);
+                    tmem_ld16(ta + (uint32_t)NM, vi);
                     tmem_wait_ld();
 #pragma unroll
                     for (int k = 0; k < 16; k++) {
@@ -535,7 +517,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcGeom g, const TcAr
                 uint32_t vr[16], vi[16];
                 const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
                 tmem_ld16(ta, vr);
-                tmem_ld16(ta + (uint32_t)N, vi);
+                tmem_ld16(ta + (uint32_t)NM, vi);
                 tmem_wait_ld();
 #pragma unroll
                 for (int k = 0; k < 16; k++) {
@@ -556,7 +538,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcGeom g, const TcAr
     __syncthreads();
     if (warp == TC_MMA_WARP) {
         tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(g.tmem_cols)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(L.tmem_cols)
                      : "memory");
     }
 }
@@ -579,13 +561,22 @@ static uint32_t pow2_cols(int n)
     return c;
 }
 
-// Geometry of one launch for a given column axis, tile width and slicing.
-static int tc_setup(dgpu_ctx *ctx, const int64_t *h_type_start, int32_t ntype, const BoxSpec &box,
-                    const dgpu_opts *op, int axis, int N, int slice_mult, TcGeom &g, size_t &smem)
+// padded MMA area of a column axis / tile width
+static double tc_area(const BoxSpec &box, int a, int N)
+{
+    const int64_t npts = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    const int nc = box.f[a];
+    if (nc < 2 && npts != nc) return -1.0;
+    return (double)dgpu_cdiv(nc, N) * N * dgpu_cdiv(npts / nc, TC_M) * TC_M;
+}
+
+// Geometry of one problem for a column axis, tile width and slicing.
+static void tc_problem(dgpu_ctx *ctx, const TcInput &in, const dgpu_opts *op, int axis, int N, int slice_mult,
+                       TcProblem &g)
 {
     memset(&g, 0, sizeof(g));
+    const BoxSpec &box = in.box;
     for (int k = 0; k < 3; k++) g.f[k] = box.f[k];
-    const int64_t npts = (int64_t)box.f[0] * box.f[1] * box.f[2];
     g.ac = axis;
     g.ra = axis == 0 ? 1 : 0;
     g.rb = 3 - axis - g.ra;
@@ -598,21 +589,18 @@ static int tc_setup(dgpu_ctx *ctx, const int64_t *h_type_start, int32_t ntype, c
     g.nrows = box.f[g.ra] * box.f[g.rb];
     g.N = N;
     g.n_tiles = (int32_t)dgpu_cdiv(g.ncols, N);
-    g.nbuf = 6 * g.N <= 512 ? 2 : 1;
     g.m_tiles = (int32_t)dgpu_cdiv(g.nrows, TC_M);
-    g.pbox = npts;
-    g.ntype = ntype;
-    g.bf16 = op->split == DGPU_SPLIT_BF16;
-    g.flush = op->tc_flush > 0 ? (int32_t)dgpu_cdiv(op->tc_flush, TC_KA) : TC_FLUSH_STAGES;
+    g.pbox = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    g.ntype = in.ntype;
     int64_t maxn = 0;
-    for (int t = 0; t < ntype; t++) {
-        g.ts[t] = h_type_start[t];
-        const int64_t n = h_type_start[t + 1] - h_type_start[t];
+    for (int t = 0; t < in.ntype; t++) {
+        g.ts[t] = in.ts[t];
+        const int64_t n = in.ts[t + 1] - in.ts[t];
         maxn = n > maxn ? n : maxn;
     }
-    g.ts[ntype] = h_type_start[ntype];
+    g.ts[in.ntype] = in.ts[in.ntype];
     // K slices: about slice_mult work items per SM, or tc_kslice atoms each when given
-    const int64_t tiles = (int64_t)g.m_tiles * g.n_tiles * ntype;
+    const int64_t tiles = (int64_t)g.m_tiles * g.n_tiles * in.ntype;
     int64_t nsl;
     if (op->tc_kslice > 0) {
         nsl = dgpu_cdiv(maxn, op->tc_kslice);
@@ -624,45 +612,88 @@ static int tc_setup(dgpu_ctx *ctx, const int64_t *h_type_start, int32_t ntype, c
     g.slice_len = dgpu_cdiv(dgpu_cdiv(maxn > 0 ? maxn : 1, nsl), TC_KA) * TC_KA;
     g.nslice = (int32_t)dgpu_cdiv(maxn > 0 ? maxn : 1, g.slice_len);
     g.nitems = tiles * g.nslice;
-    const uint32_t stage_bytes = 4 * TC_A_BYTES + 4u * g.N * TC_KA * 2;
-    const uint32_t bar_bytes = TC_BAR_BYTES + 2 * TC_ATOM_SLOT;
-    const int stages = (int)((200 * 1024 - bar_bytes) / stage_bytes);
-    g.stages = stages > 4 ? 4 : stages;
-    g.tmem_cols = pow2_cols(2 * g.N * (1 + g.nbuf));
-    if (g.stages < 2 || g.tmem_cols > 512) return dgpu_set_error(ctx, DGPU_ERR_ARG, "tile does not fit");
-    smem = (size_t)g.stages * stage_bytes + bar_bytes;
-    return DGPU_OK;
+    const uint64_t *dd[3] = {in.du, in.dv, in.dw};
+    g.ph0 = in.ph0;
+    g.dra = dd[g.ra];
+    g.drb = dd[g.rb];
+    g.dac = dd[axis];
+    g.w = in.w;
 }
 
-static int tc_launch(dgpu_ctx *ctx, const TcGeom &g, size_t smem, const uint64_t *ph0, const uint64_t *du,
-                     const uint64_t *dv, const uint64_t *dw, const float *w, DevBuf &part)
+int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *op, int N, int slice_mult,
+                 TcPlan &plan, DevBuf &part, DevBuf &desc)
 {
-    DGPU_CUDA(ctx, part.ensure((size_t)g.ntype * g.nslice * g.pbox * sizeof(float2)));
-    DGPU_CUDA(ctx, ctx->flag.ensure(64));
-    int32_t *d_err = ctx->flag.as<int32_t>() + 8;
-    DGPU_CUDA(ctx, cudaMemsetAsync(d_err, 0, sizeof(int32_t), ctx->stream));
-    TcArgs args;
-    args.ph0 = ph0;
-    const uint64_t *dd[3] = {du, dv, dw};
-    args.dra = dd[g.ra];
-    args.drb = dd[g.rb];
-    args.dac = dd[g.ac];
-    args.w = w;
-    args.part = part.as<float2>();
-    args.err = d_err;
-    static bool attr_set = false;
+    plan.probs.assign(nprob, TcProblem());
+    plan.part_off.assign(nprob, 0);
+    plan.nslice.assign(nprob, 0);
+    int64_t items = 0, elems = 0;
+    for (int p = 0; p < nprob; p++) {
+        int axis = in[p].axis;
+        if (axis < 0) {
+            double best = 1e300;
+            for (int a = 0; a < 3; a++) {
+                const double ar = tc_area(in[p].box, a, N);
+                if (ar >= 0 && ar < best * (1 - 1e-9)) { best = ar; axis = a; }
+            }
+        }
+        if (axis < 0) return dgpu_set_error(ctx, DGPU_ERR_ARG, "no tensor-core tile fits the box");
+        TcProblem &g = plan.probs[p];
+        tc_problem(ctx, in[p], op, axis, N, slice_mult, g);
+        g.item0 = items;
+        items += g.nitems;
+        plan.part_off[p] = elems;
+        plan.nslice[p] = g.nslice;
+        elems += (int64_t)g.ntype * g.nslice * g.pbox;
+    }
+    plan.item_prob.resize(items);
+    for (int p = 0; p < nprob; p++)
+        for (int64_t i = 0; i < plan.probs[p].nitems; i++) plan.item_prob[plan.probs[p].item0 + i] = p;
+    DGPU_CUDA(ctx, part.ensure((size_t)(elems > 0 ? elems : 1) * sizeof(float2)));
+    for (int p = 0; p < nprob; p++) plan.probs[p].part = part.as<float2>() + plan.part_off[p];
+    const size_t pbytes = ((size_t)nprob * sizeof(TcProblem) + 255) & ~(size_t)255;
+    DGPU_CUDA(ctx, desc.ensure(pbytes + (size_t)items * sizeof(int32_t) + 256));
+    DGPU_CUDA(ctx, cudaMemcpyAsync(desc.p, plan.probs.data(), (size_t)nprob * sizeof(TcProblem),
+                                   cudaMemcpyHostToDevice, ctx->stream));
+    DGPU_CUDA(ctx, cudaMemcpyAsync((char *)desc.p + pbytes, plan.item_prob.data(), (size_t)items * sizeof(int32_t),
+                                   cudaMemcpyHostToDevice, ctx->stream));
+    // the host vectors must outlive the copies
+    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    TcLaunch &L = plan.L;
+    L.probs = (const TcProblem *)desc.p;
+    L.item_prob = (const int32_t *)((char *)desc.p + pbytes);
+    L.nitems = items;
+    L.Nmax = N;
+    L.nbuf = 6 * N <= 512 ? 2 : 1;
+    L.flush = op->tc_flush > 0 ? (int32_t)dgpu_cdiv(op->tc_flush, TC_KA) : TC_FLUSH_STAGES;
+    L.bf16 = op->split == DGPU_SPLIT_BF16;
+    const uint32_t stage_bytes = 4 * TC_A_BYTES + 4u * N * TC_KA * 2;
+    const uint32_t bar_bytes = TC_BAR_BYTES + 2 * TC_ATOM_SLOT;
+    const int stages = (int)((200 * 1024 - bar_bytes) / stage_bytes);
+    L.stages = stages > 4 ? 4 : stages;
+    L.tmem_cols = pow2_cols(2 * N * (1 + L.nbuf));
+    if (L.stages < 2 || L.tmem_cols > 512) return dgpu_set_error(ctx, DGPU_ERR_ARG, "tile does not fit");
+    plan.smem = (size_t)L.stages * stage_bytes + bar_bytes;
+    static bool attr_set = false;     // set once, outside any stream capture
     if (!attr_set) {
         DGPU_CUDA(ctx, cudaFuncSetAttribute(k_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
         attr_set = true;
     }
-    int grid = (int)(g.nitems < ctx->nsm ? g.nitems : ctx->nsm);
-    if (grid < 1) grid = 1;
-    k_tc<<<grid, TC_THREADS, smem, ctx->stream>>>(g, args);
+    DGPU_CUDA(ctx, ctx->flag.ensure(64));
+    L.err = ctx->flag.as<int32_t>() + 8;
+    return DGPU_OK;
+}
+
+int dgpu_tc_launch(dgpu_ctx *ctx, const TcPlan &plan)
+{
+    DGPU_CUDA(ctx, cudaMemsetAsync(plan.L.err, 0, sizeof(int32_t), ctx->stream));
+    if (plan.L.nitems < 1) return DGPU_OK;
+    const int grid = (int)(plan.L.nitems < ctx->nsm ? plan.L.nitems : ctx->nsm);
+    k_tc<<<grid, TC_THREADS, plan.smem, ctx->stream>>>(plan.L);
     DGPU_CUDA(ctx, cudaGetLastError());
     return DGPU_OK;
 }
 
-static int tc_check(dgpu_ctx *ctx)
+int dgpu_tc_check(dgpu_ctx *ctx)
 {
     int32_t herr = 0;
     DGPU_CUDA(ctx, cudaMemcpyAsync(&herr, ctx->flag.as<int32_t>() + 8, sizeof(int32_t), cudaMemcpyDeviceToHost,
@@ -676,25 +707,19 @@ static int tc_check(dgpu_ctx *ctx)
 // MMA area is within 25% of the smallest, at two slicings.
 static void tc_candidates(const BoxSpec &box, int want_n, TcChoice *out, int &n)
 {
-    const int64_t npts = (int64_t)box.f[0] * box.f[1] * box.f[2];
-    double best = 1e300, area[3][9];
+    double best = 1e300;
     for (int a = 0; a < 3; a++)
-        for (int k = 0; k < 9; k++) {
-            area[a][k] = -1;
-            const int N = 16 * (k + 1) > 128 ? 0 : 16 * (k + 1);
-            if (!N || (want_n && N != want_n)) continue;
-            const int nc = box.f[a];
-            if (nc < 2 && npts != nc) continue;
-            const int64_t rows = npts / nc;
-            area[a][k] = (double)dgpu_cdiv(nc, N) * N * dgpu_cdiv(rows, TC_M) * TC_M;
-            if (N >= 48 && area[a][k] < best) best = area[a][k];
-            if (want_n && area[a][k] < best) best = area[a][k];
+        for (int N = 16; N <= 128; N += 16) {
+            if ((want_n && N != want_n) || (!want_n && N < 48)) continue;
+            const double ar = tc_area(box, a, N);
+            if (ar >= 0 && ar < best) best = ar;
         }
     n = 0;
     for (int a = 0; a < 3; a++)
-        for (int k = 0; k < 9; k++) {
-            const int N = 16 * (k + 1);
-            if (area[a][k] < 0 || area[a][k] > 1.25 * best || (N < 48 && !want_n)) continue;
+        for (int N = 16; N <= 128; N += 16) {
+            if ((want_n && N != want_n) || (!want_n && N < 48)) continue;
+            const double ar = tc_area(box, a, N);
+            if (ar < 0 || ar > 1.25 * best) continue;
             for (int m : {4, 8}) {
                 if (n >= 64) return;
                 out[n].axis = a;
@@ -722,6 +747,15 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
     while ((1LL << lg) < maxn) lg++;
     const TcKey key(box.f[0], box.f[1], box.f[2], ntype, lg, op->split * 1000 + want_n,
                     op->tc_kslice * 7 + op->tc_flush);
+    TcInput in;
+    in.ph0 = ph0;
+    in.du = du;
+    in.dv = dv;
+    in.dw = dw;
+    in.w = w;
+    in.ts = h_type_start;
+    in.ntype = ntype;
+    in.box = box;
     TcChoice choice;
     auto hit = ctx->tc_tuned.find(key);
     if (hit != ctx->tc_tuned.end()) {
@@ -733,15 +767,14 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
         if (nc == 0) return dgpu_set_error(ctx, DGPU_ERR_ARG, "no tensor-core tile fits the box");
         float best = 1e30f;
         for (int c = 0; c < nc; c++) {
-            TcGeom g;
-            size_t smem;
-            if (tc_setup(ctx, h_type_start, ntype, box, op, cand[c].axis, cand[c].N, cand[c].slice_mult, g, smem))
-                continue;
+            in.axis = cand[c].axis;
+            TcPlan plan;
+            if (dgpu_tc_plan(ctx, 1, &in, op, cand[c].N, cand[c].slice_mult, plan, part, ctx->tc_part)) continue;
             DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[4], ctx->stream));
-            int rc = tc_launch(ctx, g, smem, ph0, du, dv, dw, w, part);
+            int rc = dgpu_tc_launch(ctx, plan);
             if (rc) return rc;
             DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[5], ctx->stream));
-            rc = tc_check(ctx);
+            rc = dgpu_tc_check(ctx);
             if (rc) return rc;
             float ms = 0.f;
             DGPU_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[4], ctx->ev[5]));
@@ -752,18 +785,18 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
         }
         ctx->tc_tuned[key] = choice;
     }
-    TcGeom g;
-    size_t smem;
-    int rc = tc_setup(ctx, h_type_start, ntype, box, op, choice.axis, choice.N, choice.slice_mult, g, smem);
+    in.axis = choice.axis;
+    TcPlan plan;
+    int rc = dgpu_tc_plan(ctx, 1, &in, op, choice.N, choice.slice_mult, plan, part, ctx->tc_part);
     if (rc) return rc;
-    rc = tc_launch(ctx, g, smem, ph0, du, dv, dw, w, part);
+    rc = dgpu_tc_launch(ctx, plan);
     if (rc) return rc;
-    rc = tc_check(ctx);
+    rc = dgpu_tc_check(ctx);
     if (rc) return rc;
-    ctx->tc_last[0] = g.ac;
-    ctx->tc_last[1] = g.N;
-    ctx->tc_last[2] = g.nbuf;
-    ctx->tc_last[3] = (int32_t)g.slice_len;
-    *nslice_out = g.nslice;
+    ctx->tc_last[0] = plan.probs[0].ac;
+    ctx->tc_last[1] = plan.probs[0].N;
+    ctx->tc_last[2] = plan.L.nbuf;
+    ctx->tc_last[3] = (int32_t)plan.probs[0].slice_len;
+    *nslice_out = plan.nslice[0];
     return DGPU_OK;
 }

@@ -130,6 +130,41 @@ def four_strucf(xat, uin, vin, win, off, lmn, num, fnum, cfact=None, istl=None, 
     return _cplx(out, tuple(num))
 
 
+def batch_run(crystals, grids, opts, targets=None, weights=None, ctx=None):
+    """A population of crystals in one captured launch sequence
+    (dgpu_batch_run).  Returns (dsi list, chi2 array or None, grad_pos list,
+    grad_occ list, device ms of the graph launch)."""
+    ctx = ctx or default_context()
+    n = len(crystals)
+    crs = (_abi.Crystal * n)(*[c.to_c() for c in crystals])
+    grs = (_abi.Grid * n)(*[g.to_c() for g in grids])
+    dp = C.POINTER(C.c_double)
+    dsi = [np.zeros(g.npoints) for g in grids]
+    dsi_p = (dp * n)(*[_abi.dptr(d) for d in dsi])
+    it_p = wt_p = gp_p = go_p = None
+    chi2 = None
+    gps, gos = [], []
+    keep = []
+    if targets is not None:
+        its = [np.asfortranarray(np.asarray(t, np.float64)).reshape(-1, order="F").copy() for t in targets]
+        keep += its
+        it_p = (dp * n)(*[_abi.dptr(t) for t in its])
+        if weights is not None:
+            wts = [np.asfortranarray(np.asarray(w, np.float64)).reshape(-1, order="F").copy() for w in weights]
+            keep += wts
+            wt_p = (dp * n)(*[_abi.dptr(w) for w in wts])
+        chi2 = np.zeros(n)
+        gps = [np.zeros(3 * c.natoms) for c in crystals]
+        gos = [np.zeros(c.natoms) for c in crystals]
+        gp_p = (dp * n)(*[_abi.dptr(x) for x in gps])
+        go_p = (dp * n)(*[_abi.dptr(x) for x in gos])
+    ctx.check(ctx.lib.dgpu_batch_run(ctx.h, n, crs, grs, C.byref(opts), dsi_p, it_p, wt_p,
+                                     _abi.dptr(chi2), gp_p, go_p))
+    ms = ctx.lib.dgpu_batch_last_ms(ctx.h)
+    dsi = [d.reshape(g.inc, order="F") for d, g in zip(dsi, grids)]
+    return dsi, chi2, [x.reshape(-1, 3) for x in gps], gos, ms
+
+
 class Fourier:
     """Menu state of `fourier` with its reset defaults (fourier_reset.f90:42-101)."""
 
