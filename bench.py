@@ -42,6 +42,8 @@ PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 def workload(name):
     if name == "fcc-alloy-101^3":
         return S.fcc_alloy_volume()
+    if name == "fcc-alloy-61^3":       # the same alloy at 30^3 cells on a 61^3 grid (profiling case)
+        return S.fcc_alloy_volume(cells=30, inc=61, step=8.0 / 60)
     if name == "perovskite-201^2":
         return S.perovskite_plane()
     if name == "hex-layers-1001^2":

@@ -72,7 +72,7 @@ extern "C" int dgpu_ctx_destroy(dgpu_ctx *c)
     DevBuf *bufs[] = {&c->pos, &c->iscat, &c->aocc, &c->sel, &c->counts, &c->type_start, &c->ph0, &c->du,
                       &c->dv, &c->dw, &c->w, &c->aph0, &c->adu, &c->adv, &c->adw, &c->aw, &c->istl,
                       &c->cfact, &c->part, &c->apart, &c->lat, &c->csf, &c->acsf, &c->dsi, &c->stats,
-                      &c->flag, &c->tc_part, &c->tc_work, &c->gq, &c->gpart, &c->grad, &c->batch_desc,
+                      &c->flag, &c->tc_part, &c->tc_work, &c->tc_mult, &c->gq, &c->gpart, &c->grad, &c->batch_desc,
                       &c->batch_aux};
     for (DevBuf *b : bufs) b->release();
     for (int i = 0; i < 6; i++)
@@ -169,17 +169,15 @@ static int engine_sums(dgpu_ctx *ctx, int engine, DevBuf &ph0, DevBuf &du, DevBu
                        const int64_t *ts, int32_t ntype, const dgpu_opts *op, const BoxSpec &box, DevBuf &part,
                        PartRef *ref)
 {
-    int rc;
-    int32_t nslice = 1;
+    memset(ref, 0, sizeof(*ref));
     if (engine == DGPU_ENGINE_TC)
-        rc = dgpu_tc_sums(ctx, ph0.as<uint64_t>(), du.as<uint64_t>(), dv.as<uint64_t>(), dw.as<uint64_t>(),
-                          w.as<float>(), ts, ntype, box, op, part, &nslice);
-    else
-        rc = dgpu_direct_sums(ctx, ph0.as<uint64_t>(), du.as<uint64_t>(), dv.as<uint64_t>(), dw.as<uint64_t>(),
+        return dgpu_tc_sums(ctx, ph0.as<uint64_t>(), du.as<uint64_t>(), dv.as<uint64_t>(), dw.as<uint64_t>(),
+                            w.as<float>(), ts, ntype, box, op, part, ref);
+    int32_t nslice = 1;
+    int rc = dgpu_direct_sums(ctx, ph0.as<uint64_t>(), du.as<uint64_t>(), dv.as<uint64_t>(), dw.as<uint64_t>(),
                               w.as<float>(), ts, ntype, op->phase == DGPU_PHASE_REF22, box, part, &nslice);
     ref->p = part.p;
     ref->nslice = nslice;
-    ref->f32 = engine == DGPU_ENGINE_TC;
     return rc;
 }
 

@@ -71,6 +71,7 @@ struct dgpu_ctx {
     DevBuf aph0, adu, adv, adw, aw;     // folded atoms for <F>
     DevBuf istl, cfact, part, apart, lat, csf, acsf, dsi, stats, flag;
     DevBuf tc_part, tc_work, aidx;          // aidx: original atom index of each prepared slot
+    DevBuf tc_mult;                         // per-atom step factors of the tensor-core engine
     int64_t ts_main[2 * 64 + 4] = {};      // type ranges of the last main atom preparation
     DevBuf gq, gpart, grad, batch_desc, batch_aux;
     double batch_ms = 0.0;
@@ -153,16 +154,18 @@ int dgpu_direct_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du,
 // partials.  Lives in global memory; a launch may cover many problems.
 struct TcProblem {
     int32_t f[3];
-    int32_t ra, rb, ac, fra;
-    int64_t sra, srb, sac;   // box-index strides of the row and column axes
-    int32_t nrows, ncols;
+    int32_t ra, rb, ac;       // row axes (ra the longer) and column axis
+    int32_t fra, fra_p, frb;  // row extents; ra padded to a multiple of 8
+    int32_t ncols;
     int32_t N;               // columns per tile (multiple of 16, <= TcLaunch::Nmax)
     int32_t m_tiles, n_tiles, nslice, ntype;
-    int64_t slice_len, nitems, item0, pbox;
+    int64_t nrows_p;         // fra_p * frb: rows of the tile space (rg = nb * fra_p + na)
+    int64_t slice_len, nitems, item0, slab;
     int64_t ts[65];
     const uint64_t *ph0, *dra, *drb, *dac;   // phase data along the row axes and the column axis
     const float *w;
-    float2 *part;
+    const float2 *ma, *mc;   // per-atom exp(2 pi i 8 d) along ra and ac
+    float2 *part;            // part[(t*nslice+ks)*slab + c*nrows_p + rg]
 };
 
 // Launch-wide constants: shared-memory and TMEM layout follow Nmax.
@@ -171,6 +174,7 @@ struct TcLaunch {
     const int32_t *item_prob;   // problem index of every work item
     int64_t nitems;
     int32_t Nmax, stages, flush, nbuf, bf16;
+    int32_t tsum;               // running sum of the main accumulator kept in TMEM
     uint32_t tmem_cols;
     int32_t *err;
 };
@@ -180,6 +184,8 @@ struct TcLaunch {
 struct TcInput {
     const uint64_t *ph0, *du, *dv, *dw;
     const float *w;
+    const float2 *mult;       // step factors: mult[axis * mult_stride + atom]
+    int64_t mult_stride;
     const int64_t *ts;        // host: padded type ranges (ntype + 1 values)
     int32_t ntype;
     BoxSpec box;
@@ -198,12 +204,19 @@ int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *o
                  TcPlan &plan, DevBuf &part, DevBuf &desc);
 int dgpu_tc_launch(dgpu_ctx *ctx, const TcPlan &plan);          // enqueues the kernel only
 int dgpu_tc_check(dgpu_ctx *ctx);                               // waits, reads the error flag
+struct PartRef;
+// Per-atom step factors exp(2 pi i 8 d) of du, dv, dw (n atoms) into
+// out[axis * stride + atom]; enqueue only.
+int dgpu_tc_mult_async(dgpu_ctx *ctx, const uint64_t *du, const uint64_t *dv, const uint64_t *dw, int64_t n,
+                       int64_t stride, float2 *out);
+// Layout of a problem's partials for the combine kernels.
+void dgpu_tc_partref(const TcProblem &g, const float2 *p, PartRef &ref);
 // Single problem with autotuned tile; partial sums are float2 (FP32, one per
-// work item, RN-accumulated drains).
+// work item, RN-accumulated drains); ref receives their layout.
 int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const uint64_t *dv,
                  const uint64_t *dw, const float *w, const int64_t *h_type_start,
                  int32_t ntype, const BoxSpec &box, const dgpu_opts *op, DevBuf &part,
-                 int32_t *nslice_out);
+                 PartRef *ref);
 bool dgpu_tc_available(dgpu_ctx *ctx);
 
 // epilogue.cu -----------------------------------------------------------
@@ -217,10 +230,15 @@ struct FormSpec {
     double eck[3], vi[9];
 };
 // Partial sums part[t][s][p] of either engine: double2 (direct) or float2 (TC).
+// Element (point i,j,l of the box, type t, slice k) at
+// (t*nslice + k)*slab + i*s[0] + j*s[1] + l*s[2]; s[0] == 0 means the dense
+// box order (s = 1, f0, f0*f1; slab = f0*f1*f2).
 struct PartRef {
     const void *p;
     int32_t nslice;
     int32_t f32;
+    int64_t s[3];
+    int64_t slab;
 };
 int dgpu_combine(dgpu_ctx *ctx, const FormSpec &fs, const BoxSpec &box, const PartRef &part,
                  const int32_t *istl, const double2 *cfact,

@@ -61,6 +61,7 @@ struct BatchState {
     cudaGraphExec_t exec = nullptr;
     DevBuf d_pos, d_isc, d_aocc, d_ph0, d_du, d_dv, d_dw, d_w, d_idx, d_cnt, d_offs, d_tsd;
     DevBuf d_istl, d_cfact, d_csf, d_dsi, d_g, d_q, d_chi, d_grad, d_coef, d_fs, d_it, d_wt, part, desc;
+    DevBuf d_mult;                         // tensor-core step factors, 3 x tot_pad
     HostPinned h_pos, h_isc, h_aocc, h_it, h_wt, h_dsi, h_chi, h_grad;
     ~BatchState()
     {
@@ -70,6 +71,7 @@ struct BatchState {
                        &d_tsd, &d_istl, &d_cfact, &d_csf, &d_dsi, &d_g, &d_q, &d_chi, &d_grad, &d_coef, &d_fs,
                        &d_it, &d_wt, &part, &desc};
         for (DevBuf *x : b) x->release();
+        d_mult.release();
     }
 };
 
@@ -118,12 +120,16 @@ static int batch_enqueue(dgpu_ctx *ctx, BatchState &B, const dgpu_opts *op)
                                 B.d_cfact.as<double2>() + m.cfact_off);
         if (rc) return rc;
     }
-    int rc = dgpu_tc_launch(ctx, B.plan);
+    int rc = dgpu_tc_mult_async(ctx, B.d_du.as<uint64_t>(), B.d_dv.as<uint64_t>(), B.d_dw.as<uint64_t>(),
+                                B.tot_pad, B.tot_pad, B.d_mult.as<float2>());
+    if (rc) return rc;
+    rc = dgpu_tc_launch(ctx, B.plan);
     if (rc) return rc;
     for (size_t c = 0; c < B.mem.size(); c++) {
         Member &m = B.mem[c];
         const FormSpec *fs = B.d_fs.as<FormSpec>() + c;
-        PartRef pr = {B.part.as<float2>() + B.plan.part_off[c], B.plan.nslice[c], 1};
+        PartRef pr;
+        dgpu_tc_partref(B.plan.probs[c], B.part.as<float2>() + B.plan.part_off[c], pr);
         double2 *csf = B.d_csf.as<double2>() + m.pt_off;
         double *dsi = B.d_dsi.as<double>() + m.pt_off;
         rc = dgpu_combine_async(ctx, fs, m.box, pr, B.d_istl.as<int32_t>() + m.istl_off,
@@ -216,6 +222,7 @@ static int batch_build(dgpu_ctx *ctx, BatchState &B, int32_t nc, const dgpu_crys
     DGPU_CUDA(ctx, B.d_dv.ensure(npd * 8));
     DGPU_CUDA(ctx, B.d_dw.ensure(npd * 8));
     DGPU_CUDA(ctx, B.d_w.ensure(npd * 4));
+    DGPU_CUDA(ctx, B.d_mult.ensure(npd * 3 * sizeof(float2)));
     DGPU_CUDA(ctx, B.d_idx.ensure(npd * 4));
     DGPU_CUDA(ctx, B.d_cnt.ensure((size_t)(cnt > 0 ? cnt : 1) * 4));
     DGPU_CUDA(ctx, B.d_offs.ensure((size_t)(cnt > 0 ? cnt : 1) * 8));
@@ -261,6 +268,8 @@ static int batch_build(dgpu_ctx *ctx, BatchState &B, int32_t nc, const dgpu_crys
         in[c].dv = B.d_dv.as<uint64_t>() + m.pbase;
         in[c].dw = B.d_dw.as<uint64_t>() + m.pbase;
         in[c].w = B.d_w.as<float>() + m.pbase;
+        in[c].mult = B.d_mult.as<float2>() + m.pbase;
+        in[c].mult_stride = B.tot_pad;
         in[c].ts = m.ts;
         in[c].ntype = m.nscat;
         in[c].box = m.box;

@@ -50,9 +50,23 @@ __device__ __forceinline__ double2 ld_part(const float2 *p)
     return make_double2((double)v.x, (double)v.y);
 }
 
+// element offsets of a partial-sum array (see PartRef)
+struct PartLayout {
+    int64_t s0, s1, s2, slab;
+};
+
+static PartLayout layout_of(const PartRef &r, const BoxSpec &box)
+{
+    if (r.s[0] == 0) {
+        const int64_t f0 = box.f[0], f01 = (int64_t)box.f[0] * box.f[1];
+        return PartLayout{1, f0, f01, f01 * box.f[2]};
+    }
+    return PartLayout{r.s[0], r.s[1], r.s[2], r.slab};
+}
+
 template <class P>
 __global__ void k_combine(const FormSpec *fs, BoxSpec box, const P *__restrict__ part,
-                          int32_t nslice, const int32_t *__restrict__ istl,
+                          int32_t nslice, PartLayout lay, const int32_t *__restrict__ istl,
                           const double2 *__restrict__ cfact, const double2 *__restrict__ acsf,
                           double2 *__restrict__ csf, double *__restrict__ dsi, double ds, double sqds)
 {
@@ -67,9 +81,9 @@ __global__ void k_combine(const FormSpec *fs, BoxSpec box, const P *__restrict__
     double2 F = make_double2(0.0, 0.0);
     for (int t = 1; t <= fs->nscat; t++) {
         double2 s = make_double2(0.0, 0.0);
-        const P *pt = part + (int64_t)(t - 1) * nslice * nb + pb;
+        const P *pt = part + (int64_t)(t - 1) * nslice * lay.slab + i * lay.s0 + j * lay.s1 + l * lay.s2;
         for (int k = 0; k < nslice; k++) {
-            double2 v = ld_part(pt + (int64_t)k * nb);
+            double2 v = ld_part(pt + (int64_t)k * lay.slab);
             s.x += v.x;
             s.y += v.y;
         }
@@ -100,7 +114,7 @@ __device__ __forceinline__ double2 geom_series(double x, int32_t n)
 
 template <class P>
 __global__ void k_aver_combine(const FormSpec *fs, BoxSpec box, const P *__restrict__ apart,
-                               int32_t anslice, const int32_t *__restrict__ istl,
+                               int32_t anslice, PartLayout lay, const int32_t *__restrict__ istl,
                                const double2 *__restrict__ cfact, const double2 *__restrict__ lat,
                                int32_t lat_nslice, int32_t lat_closed, int32_t c0, int32_t c1,
                                int32_t c2, double d0, double d1, double d2, double norm,
@@ -118,9 +132,9 @@ __global__ void k_aver_combine(const FormSpec *fs, BoxSpec box, const P *__restr
     double2 A = make_double2(0.0, 0.0);
     for (int t = 1; t <= fs->nscat; t++) {
         double2 s = make_double2(0.0, 0.0);
-        const P *pt = apart + (int64_t)(t - 1) * anslice * nb + pb;
+        const P *pt = apart + (int64_t)(t - 1) * anslice * lay.slab + i * lay.s0 + j * lay.s1 + l * lay.s2;
         for (int k = 0; k < anslice; k++) {
-            double2 v = ld_part(pt + (int64_t)k * nb);
+            double2 v = ld_part(pt + (int64_t)k * lay.slab);
             s.x += v.x;
             s.y += v.y;
         }
@@ -287,12 +301,13 @@ int dgpu_combine(dgpu_ctx *ctx, const FormSpec &fs, const BoxSpec &box, const Pa
     if (rc) return rc;
     int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
     const unsigned nblk = (unsigned)dgpu_cdiv(nb, 256);
+    const PartLayout lay = layout_of(part, box);
     if (part.f32)
-        k_combine<float2><<<nblk, 256, 0, ctx->stream>>>(d, box, (const float2 *)part.p, part.nslice, istl, cfact,
-                                                          acsf_in, csf, dsi, diff_scale, sqrt(diff_scale));
+        k_combine<float2><<<nblk, 256, 0, ctx->stream>>>(d, box, (const float2 *)part.p, part.nslice, lay, istl,
+                                                          cfact, acsf_in, csf, dsi, diff_scale, sqrt(diff_scale));
     else
-        k_combine<double2><<<nblk, 256, 0, ctx->stream>>>(d, box, (const double2 *)part.p, part.nslice, istl, cfact,
-                                                           acsf_in, csf, dsi, diff_scale, sqrt(diff_scale));
+        k_combine<double2><<<nblk, 256, 0, ctx->stream>>>(d, box, (const double2 *)part.p, part.nslice, lay, istl,
+                                                           cfact, acsf_in, csf, dsi, diff_scale, sqrt(diff_scale));
     DGPU_CUDA(ctx, cudaGetLastError());
     DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));   // FormSpec block reused next
     return DGPU_OK;
@@ -308,14 +323,15 @@ int dgpu_aver_combine(dgpu_ctx *ctx, const FormSpec &fs, const BoxSpec &box, con
     if (rc) return rc;
     int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
     const unsigned nblk = (unsigned)dgpu_cdiv(nb, 256);
+    const PartLayout lay = layout_of(apart, box);
     if (apart.f32)
         k_aver_combine<float2><<<nblk, 256, 0, ctx->stream>>>(
-            d, box, (const float2 *)apart.p, apart.nslice, istl, cfact, lat, lat_nslice, lat_closed, icc[0], icc[1],
-            icc[2], dim0[0], dim0[1], dim0[2], norm, acsf);
+            d, box, (const float2 *)apart.p, apart.nslice, lay, istl, cfact, lat, lat_nslice, lat_closed, icc[0],
+            icc[1], icc[2], dim0[0], dim0[1], dim0[2], norm, acsf);
     else
         k_aver_combine<double2><<<nblk, 256, 0, ctx->stream>>>(
-            d, box, (const double2 *)apart.p, apart.nslice, istl, cfact, lat, lat_nslice, lat_closed, icc[0], icc[1],
-            icc[2], dim0[0], dim0[1], dim0[2], norm, acsf);
+            d, box, (const double2 *)apart.p, apart.nslice, lay, istl, cfact, lat, lat_nslice, lat_closed, icc[0],
+            icc[1], icc[2], dim0[0], dim0[1], dim0[2], norm, acsf);
     DGPU_CUDA(ctx, cudaGetLastError());
     DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return DGPU_OK;
@@ -361,12 +377,14 @@ int dgpu_combine_async(dgpu_ctx *ctx, const FormSpec *d_fs, const BoxSpec &box, 
 {
     const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
     const unsigned nblk = (unsigned)dgpu_cdiv(nb, 256);
+    const PartLayout lay = layout_of(part, box);
     if (part.f32)
-        k_combine<float2><<<nblk, 256, 0, ctx->stream>>>(d_fs, box, (const float2 *)part.p, part.nslice, istl, cfact,
-                                                          nullptr, csf, dsi, diff_scale, sqrt(diff_scale));
+        k_combine<float2><<<nblk, 256, 0, ctx->stream>>>(d_fs, box, (const float2 *)part.p, part.nslice, lay, istl,
+                                                          cfact, nullptr, csf, dsi, diff_scale, sqrt(diff_scale));
     else
-        k_combine<double2><<<nblk, 256, 0, ctx->stream>>>(d_fs, box, (const double2 *)part.p, part.nslice, istl,
-                                                           cfact, nullptr, csf, dsi, diff_scale, sqrt(diff_scale));
+        k_combine<double2><<<nblk, 256, 0, ctx->stream>>>(d_fs, box, (const double2 *)part.p, part.nslice, lay,
+                                                           istl, cfact, nullptr, csf, dsi, diff_scale,
+                                                           sqrt(diff_scale));
     DGPU_CUDA(ctx, cudaGetLastError());
     return DGPU_OK;
 }

@@ -2,27 +2,43 @@
 // tcgen05 (sm_100 family), accumulators in TMEM.
 //
 // For the computed box, one grid axis ac is the GEMM's N dimension
-// ("columns") and the other two, flattened, its M dimension ("rows").  The
-// phase of point (row r, column c) and atom j splits exactly:
-//     phase = [ph0_j + n_ra(r) d_ra,j + n_rb(r) d_rb,j] + [n_ac(c) d_ac,j]
-// so  S(r,c) = sum_j U[r,j] V[j,c]  with  U = w_j exp(2 pi i A-phase),
+// ("columns"); the other two, ra (the longer) and rb, flattened with ra padded
+// to a multiple of 8 (fra_p), form its M dimension ("rows": rg = nb*fra_p+na).
+// The phase of point (row, column c) and atom j splits exactly:
+//     phase = [ph0_j + na d_ra,j + nb d_rb,j] + [n_c d_ac,j]
+// so  S(row,c) = sum_j U[row,j] V[j,c]  with  U = w_j exp(2 pi i A-phase),
 // V = exp(2 pi i B-phase); K = the atoms of one type (a slice of them per
-// work item).  Each CTA generates its U (128 rows) and V (N columns) tiles
-// for KA = 32 atoms per stage directly in shared memory from the 64-bit
-// fixed-point phases (no operand traffic in HBM), splits every FP32 phasor
-// value into fp16 (or bf16) hi + lo, and issues per 16 atoms the 12 MMAs
-//     Re += Ur Vr^T - Ui Vi^T ,  Im += Ur Vi^T + Ui Vr^T
-// for the split products (hi,hi), (hi,lo), (lo,hi).
+// work item).
 //
-// Accumulation.  Every MMA truncates its FP32 accumulator by about one ulp,
-// so the error of one TMEM accumulator grows with the number of MMAs chained
-// into it.  The large (hi,hi) products therefore go to a "main" accumulator
-// that is drained every `flush` stages (flush*32 atoms) into the work item's
-// FP32 partial in global memory (round-to-nearest adds on CUDA cores, the
-// partial stays in L2), and the small (hi,lo)+(lo,hi) corrections go to a
-// separate accumulator drained once per work item.  With nbuf = 2 the main
-// accumulator is double-buffered so the drain overlaps the next chunk.  The
-// combine kernel adds the K slices of all work items in FP64.
+// Operand generation.  Each CTA generates its U tile (128 rows) and V tile
+// (N columns) for KA = 32 atoms per stage in shared memory from the 64-bit
+// fixed-point phases.  A producer thread owns 4 atoms and every 8th row (or
+// column) of a run: it evaluates exp(2 pi i phase) at the start of the run
+// (MUFU, exact 64-bit phase) and then steps by the per-atom factor
+// exp(2 pi i 8 d) (computed once per atom to about one ulp); a row run
+// restarts from the exact phase wherever nb changes.  Every FP32 value is
+// split into hi (the value with its mantissa cut to the fp16 / bf16 width,
+// exact in that format) and lo (the exact remainder, rounded).  V is scaled
+// by 2^12 so that its lo parts stay normal fp16 numbers; all accumulators
+// therefore carry 2^12, removed when they are drained.
+//
+// MMA form.  B holds the rows [Vr; Vi; -Vr] (3N rows), so per 16 atoms
+//     D[:, 0:2N] += Ur [Vr;Vi]^T   and   D += (-Ui) [Vi;-Vr]^T
+// give Re (accumulator columns 0..N-1) and Im (N..2N-1) with two MMAs of
+// width 2N.  The (hi,hi) products go to the main accumulator, the (hi,lo) and
+// (lo,hi) products to the correction accumulator.
+//
+// Accumulation.  Every MMA truncates its FP32 accumulator by about one ulp, so
+// the error of one TMEM accumulator grows with the number of MMAs chained into
+// it.  The main accumulator is therefore drained every `flush` stages
+// (flush*32 atoms) and added with round-to-nearest FP32 adds to a running sum
+// (kept in TMEM when N <= 64, otherwise in the work item's partial in global
+// memory); the small corrections accumulate over the whole work item.  With
+// nbuf = 2 the main accumulator is double-buffered so that a drain overlaps the
+// next chunk.  The combine kernel adds the K slices of all work items in FP64.
+//
+// Partials: part[(t*nslice + ks)*slab + c*nrows_p + rg], a column-major image
+// of the tile space (rows with na >= fra are never written).
 //
 // Warp roles (416 threads): warps 0-7 produce operand stages, warp 8 owns
 // TMEM and issues the MMAs (one elected lane), warps 9-12 drain TMEM.  All
@@ -30,7 +46,7 @@
 // the CTA stops issuing, waits for its own MMAs, frees TMEM and returns.
 //
 // Shared-memory operands use the canonical K-major layout without swizzle:
-// 8x8 fp16 core matrices of 128 contiguous bytes, LBO = 128 B between
+// 8x8 16-bit core matrices of 128 contiguous bytes, LBO = 128 B between
 // K-adjacent core matrices, SBO = (KA/8)*128 B between 8-row groups.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -44,16 +60,24 @@
 #define TC_EPI_WARP0 9
 #define TC_THREADS (13 * 32)
 #define TC_PROD_THREADS (TC_PROD_WARPS * 32)
-#define TC_A_BYTES (TC_M * TC_KA * 2)          // one operand (e.g. Ur_hi): 8 KB
+#define TC_A_BYTES (TC_M * TC_KA * 2)          // one A operand (e.g. Ur_hi): 8 KB
 #define TC_SBO ((TC_KA / 8) * 128)
 #define TC_LBO 128
 #define TC_TIMEOUT_NS 2000000000ull            // 2 s per wait
-// phase data of one 32-atom group in shared memory: ph0, d_ra, d_rb, d_ac (u64), w (f32)
-#define TC_ATOM_SLOT (TC_KA * 4 * 8 + TC_KA * 4)
+// phase data of one 32-atom group in shared memory:
+// ph0, d_ra, d_rb, d_ac (u64), w (f32), step factors along ra and ac (float2)
+#define TC_SLOT_W (TC_KA * 32)
+#define TC_SLOT_MA (TC_SLOT_W + TC_KA * 4)
+#define TC_SLOT_MC (TC_SLOT_MA + TC_KA * 8)
+#define TC_ATOM_SLOT (TC_SLOT_MC + TC_KA * 8)
+#define TC_NSLOT 3
 #define TC_BAR_BYTES 256
+#define TC_SMEM_BUDGET (220 * 1024)
 #ifndef TC_FLUSH_STAGES
 #define TC_FLUSH_STAGES 4                      // 128 atoms per drain of the main accumulator
 #endif
+#define TC_V_SCALE 4096.0f
+#define TC_UNSCALE (1.0f / 4096.0f)
 
 // ---------------------------------------------------------------------------
 // PTX helpers
@@ -155,25 +179,39 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16])
         : "r"(taddr));
 }
 
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16])
+{
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+        "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(taddr),
+        "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]),
+        "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+        : "memory");
+}
+
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // ---------------------------------------------------------------------------
 // operand generation
 
-// exp(2 pi i phase) from the top 32 bits of a 64-bit fixed-point turn
-__device__ __forceinline__ void phasor(uint64_t ph, float &c, float &s)
+// exp(2 pi i phase) from the top 32 bits of a 64-bit fixed-point turn (MUFU)
+__device__ __forceinline__ float2 phasor_fast(uint64_t ph)
 {
-#ifdef TC_PHASOR_ACCURATE
-    sincospif((float)(int32_t)(ph >> 32) * 4.656612873077393e-10f, &s, &c);
-#else
-    float ang = (float)(int32_t)(ph >> 32) * 1.4629180792671596e-09f;   // 2 pi / 2^32
-    __sincosf(ang, &s, &c);
-#endif
+    float s, c;
+    __sincosf((float)(int32_t)(ph >> 32) * 1.4629180792671596e-09f, &s, &c);   // 2 pi / 2^32
+    return make_float2(c, s);
 }
 
-__device__ __forceinline__ uint32_t pack2(float a, float b, bool bf)
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b)
 {
-    if (bf) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+
+template <bool BF>
+__device__ __forceinline__ uint32_t pack2(float a, float b)
+{
+    if (BF) {
         __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
         return *reinterpret_cast<uint32_t *>(&v);
     }
@@ -181,41 +219,24 @@ __device__ __forceinline__ uint32_t pack2(float a, float b, bool bf)
     return *reinterpret_cast<uint32_t *>(&v);
 }
 
-__device__ __forceinline__ float2 unpack2(uint32_t u, bool bf)
+// 4 values (4 consecutive atoms of one row) -> hi and lo, 4 x 16 bit each.
+// hi keeps the leading 11 (fp16) or 8 (bf16) significant bits of the FP32
+// value, so it is exact in the operand format (fp16 subnormals aside, which
+// only occur below 2^-14 where the absolute error stays below 2^-25); lo is
+// the exact FP32 remainder, rounded to the operand format.
+template <bool BF>
+__device__ __forceinline__ void split4(float x0, float x1, float x2, float x3, uint2 &hi, uint2 &lo)
 {
-    if (bf) {
-        __nv_bfloat162 v = *reinterpret_cast<__nv_bfloat162 *>(&u);
-        return __bfloat1622float2(v);
-    }
-    __half2 v = *reinterpret_cast<__half2 *>(&u);
-    return __half22float2(v);
+    const uint32_t mask = BF ? 0xFFFF0000u : 0xFFFFE000u;
+    const float h0 = __uint_as_float(__float_as_uint(x0) & mask);
+    const float h1 = __uint_as_float(__float_as_uint(x1) & mask);
+    const float h2 = __uint_as_float(__float_as_uint(x2) & mask);
+    const float h3 = __uint_as_float(__float_as_uint(x3) & mask);
+    hi.x = pack2<BF>(h0, h1);
+    hi.y = pack2<BF>(h2, h3);
+    lo.x = pack2<BF>(x0 - h0, x1 - h1);
+    lo.y = pack2<BF>(x2 - h2, x3 - h3);
 }
-
-// 8 values -> hi (rounded) and lo (remainder x 2^12, rounded), 16 bytes each.
-// hi is zero or a normal number; the remainder is scaled by 2^12 so that it
-// stays normal in fp16 as well (tensor-core inputs below 2^-14 would
-// otherwise lose their bits); the correction accumulator, which only ever
-// receives products with one lo factor, is scaled back by 2^-12.
-#define TC_LO_SCALE 4096.0f
-#define TC_LO_UNSCALE (1.0f / 4096.0f)
-__device__ __forceinline__ void split8(const float (&v)[8], uint4 &hi, uint4 &lo, bool bf)
-{
-    uint32_t h[4], l[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        const float x0 = v[2 * k], x1 = v[2 * k + 1];
-        const float y0 = fabsf(x0) < 6.103515625e-05f ? 0.f : x0;     // 2^-14: smallest normal fp16
-        const float y1 = fabsf(x1) < 6.103515625e-05f ? 0.f : x1;
-        h[k] = pack2(y0, y1, bf);
-        float2 b = unpack2(h[k], bf);
-        l[k] = pack2((x0 - b.x) * TC_LO_SCALE, (x1 - b.y) * TC_LO_SCALE, bf);
-    }
-    hi = make_uint4(h[0], h[1], h[2], h[3]);
-    lo = make_uint4(l[0], l[1], l[2], l[3]);
-}
-
-// byte offset of (row, k-group) in one operand of the canonical layout
-__device__ __forceinline__ uint32_t core_off(int row, int q) { return (row >> 3) * TC_SBO + q * TC_LBO + (row & 7) * 16; }
 
 __device__ __forceinline__ void decode_item(const TcProblem &g, int64_t item, int &t, int &ks, int &nt, int &mt)
 {
@@ -227,13 +248,132 @@ __device__ __forceinline__ void decode_item(const TcProblem &g, int64_t item, in
     t = (int)(r / g.nslice);
 }
 
+// Stage the phase data of the 32-atom group starting at padded atom ab into
+// an atom slot: 104 chunks of 16 bytes, one per thread of tid < 104.
+__device__ __forceinline__ void stage_atoms(const TcProblem &P, uint8_t *dst, int64_t ab, int tid)
+{
+    if (tid < 64) {                     // ph0, d_ra, d_rb, d_ac: 16 chunks each
+        const int arr = tid >> 4, ch = tid & 15;
+        const uint64_t *src = arr == 0 ? P.ph0 : arr == 1 ? P.dra : arr == 2 ? P.drb : P.dac;
+        cp_async16(dst + arr * (TC_KA * 8) + ch * 16, src + ab + ch * 2);
+    } else if (tid < 72) {              // w: 8 chunks
+        const int ch = tid - 64;
+        cp_async16(dst + TC_SLOT_W + ch * 16, P.w + ab + ch * 4);
+    } else if (tid < 104) {             // step factors along ra and ac: 16 chunks each
+        const int arr = (tid - 72) >> 4, ch = (tid - 72) & 15;
+        cp_async16(dst + (arr ? TC_SLOT_MC : TC_SLOT_MA) + ch * 16, (arr ? P.mc : P.ma) + ab + ch * 2);
+    }
+    cp_async_commit();
+}
+
+// U rows of one stage.  Thread (s, j, h) of the first 128 producers: atoms
+// 4j..4j+3, rows 8*(8h+m)+s for m = 0..7 (the rows of one lane of eight core
+// matrices; a warp's stores of one step cover 16 distinct 8-byte bank slots).
+template <bool BF>
+__device__ __forceinline__ void gen_rows(const TcProblem &g, int mt, const uint8_t *as, uint8_t *A, int tid)
+{
+    const int s = tid & 7, j = (tid >> 3) & 7, h = tid >> 6;
+    const uint64_t *s_ph0 = reinterpret_cast<const uint64_t *>(as);
+    const uint64_t *s_dra = s_ph0 + TC_KA, *s_drb = s_dra + TC_KA;
+    const float *s_w = reinterpret_cast<const float *>(as + TC_SLOT_W);
+    const float2 *s_ma = reinterpret_cast<const float2 *>(as + TC_SLOT_MA);
+    const int gpn = g.fra_p >> 3;                   // row groups per nb
+    const int G0 = mt * (TC_M / 8) + 8 * h;
+    int gi = G0 % gpn;
+    uint32_t nb = (uint32_t)(G0 / gpn);
+    const int k0 = 4 * j;
+    float2 x[4], m[4];
+    auto seed = [&](uint32_t na) {
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            const int k = k0 + a;
+            const float2 p = phasor_fast(s_ph0[k] + (uint64_t)na * s_dra[k] + (uint64_t)nb * s_drb[k]);
+            const float wk = s_w[k];
+            x[a] = make_float2(p.x * wk, p.y * wk);
+        }
+    };
+#pragma unroll
+    for (int a = 0; a < 4; a++) m[a] = s_ma[k0 + a];
+    seed((uint32_t)(gi * 8 + s));
+    uint8_t *dst = A + (8 * h) * TC_SBO + (j >> 1) * TC_LBO + s * 16 + (j & 1) * 8;
+#pragma unroll 1
+    for (int mm = 0; mm < 8; mm++) {
+        if (mm > 0) {
+            if (++gi == gpn) {          // next nb: restart from the exact phase (warp-uniform)
+                gi = 0;
+                nb++;
+                seed((uint32_t)s);
+            } else {
+#pragma unroll
+                for (int a = 0; a < 4; a++) x[a] = cmulf(x[a], m[a]);
+            }
+        }
+        uint2 rh, rl, ih, il;
+        split4<BF>(x[0].x, x[1].x, x[2].x, x[3].x, rh, rl);
+        split4<BF>(x[0].y, x[1].y, x[2].y, x[3].y, ih, il);
+        uint8_t *d = dst + mm * TC_SBO;
+        *reinterpret_cast<uint2 *>(d + 0 * TC_A_BYTES) = rh;    // Ur hi
+        *reinterpret_cast<uint2 *>(d + 1 * TC_A_BYTES) = rl;    // Ur lo
+        *reinterpret_cast<uint2 *>(d + 2 * TC_A_BYTES) = ih;    // Ui hi
+        *reinterpret_cast<uint2 *>(d + 3 * TC_A_BYTES) = il;    // Ui lo
+    }
+}
+
+// V columns of one stage: thread (s, j, h) of producers 128..255: atoms
+// 4j..4j+3, columns 8*gc+s for gc in its half of the N/8 column groups.  B
+// rows: Vr at c, Vi at N+c, -Vr at 2N+c, in a hi and a lo operand.
+template <bool BF>
+__device__ __forceinline__ void gen_cols(const TcProblem &g, int nt, const uint8_t *as, uint8_t *Bh,
+                                         uint32_t b_bytes, int t)
+{
+    const int s = t & 7, j = (t >> 3) & 7, h = t >> 6;
+    const int N = g.N;
+    const int ngrp = N >> 3, per = (ngrp + 1) >> 1;
+    const int gc0 = h * per, gc1 = min(ngrp, gc0 + per);
+    if (gc0 >= gc1) return;
+    const uint64_t *s_dac = reinterpret_cast<const uint64_t *>(as) + 3 * TC_KA;
+    const float2 *s_mc = reinterpret_cast<const float2 *>(as + TC_SLOT_MC);
+    const int k0 = 4 * j;
+    const uint32_t nc = (uint32_t)(nt * N + gc0 * 8 + s);
+    float2 x[4], m[4];
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        const float2 p = phasor_fast((uint64_t)nc * s_dac[k0 + a]);
+        x[a] = make_float2(p.x * TC_V_SCALE, p.y * TC_V_SCALE);
+        m[a] = s_mc[k0 + a];
+    }
+    uint8_t *Bl = Bh + b_bytes;
+    const uint32_t blk = (uint32_t)(N >> 3) * TC_SBO;           // N rows further
+    const uint32_t o0 = (j >> 1) * TC_LBO + s * 16 + (j & 1) * 8;
+#pragma unroll 1
+    for (int gc = gc0; gc < gc1; gc++) {
+        if (gc > gc0) {
+#pragma unroll
+            for (int a = 0; a < 4; a++) x[a] = cmulf(x[a], m[a]);
+        }
+        uint2 rh, rl, ih, il;
+        split4<BF>(x[0].x, x[1].x, x[2].x, x[3].x, rh, rl);
+        split4<BF>(x[0].y, x[1].y, x[2].y, x[3].y, ih, il);
+        const uint32_t o = gc * TC_SBO + o0;
+        const uint2 nrh = make_uint2(rh.x ^ 0x80008000u, rh.y ^ 0x80008000u);
+        const uint2 nrl = make_uint2(rl.x ^ 0x80008000u, rl.y ^ 0x80008000u);
+        *reinterpret_cast<uint2 *>(Bh + o) = rh;
+        *reinterpret_cast<uint2 *>(Bl + o) = rl;
+        *reinterpret_cast<uint2 *>(Bh + o + blk) = ih;
+        *reinterpret_cast<uint2 *>(Bl + o + blk) = il;
+        *reinterpret_cast<uint2 *>(Bh + o + 2 * blk) = nrh;
+        *reinterpret_cast<uint2 *>(Bl + o + 2 * blk) = nrl;
+    }
+}
+
+template <bool BF>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     const int S = L.stages;
     const int NM = L.Nmax;
-    const uint32_t b_bytes = (uint32_t)NM * TC_KA * 2;     // one B operand
-    const uint32_t stage_bytes = 4 * TC_A_BYTES + 4 * b_bytes;
+    const uint32_t b_bytes = (uint32_t)3 * NM * TC_KA * 2;      // one B operand: 3N rows
+    const uint32_t stage_bytes = 4 * TC_A_BYTES + 2 * b_bytes;
     uint64_t *full = reinterpret_cast<uint64_t *>(smem + (size_t)S * stage_bytes);
     uint64_t *empty = full + S;
     uint64_t *mfull = empty + S;      // [2] main accumulator b ready
@@ -242,9 +382,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
     uint64_t *cempty = cfull + 1;     // correction accumulator drained
     uint64_t *drain = cempty + 1;
     uint32_t *tbase = reinterpret_cast<uint32_t *>(drain + 1);
-    uint8_t *aslot = smem + (size_t)S * stage_bytes + TC_BAR_BYTES;   // 2 x TC_ATOM_SLOT
+    uint8_t *aslot = smem + (size_t)S * stage_bytes + TC_BAR_BYTES;   // TC_NSLOT x TC_ATOM_SLOT
     volatile int32_t *err = L.err;
-    const bool bf = L.bf16 != 0;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -275,102 +414,38 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
     if (warp < TC_PROD_WARPS) {
         // ------------------------------------------------------------ producers
         // Atom groups are complete (type ranges padded to 32 atoms with zero
-        // weight).  Their phase data is staged in shared memory with
-        // cp.async, one group ahead of the generation.
+        // weight).  Their phase data is staged in shared memory with cp.async
+        // one group ahead; three slots, so that a slot is rewritten only after
+        // every producer has passed the barrier that follows its last use.
         const int tid = threadIdx.x;
         uint32_t it = 0;
         bool ok = true;
-        auto issue = [&](const TcProblem &P, int slot, int64_t ab) {
-            uint8_t *dst = aslot + slot * TC_ATOM_SLOT;
-            if (tid < 64) {            // 4 arrays x 16 chunks of 16 B
-                const int arr = tid >> 4, ch = tid & 15;
-                const uint64_t *src = arr == 0 ? P.ph0 : arr == 1 ? P.dra : arr == 2 ? P.drb : P.dac;
-                cp_async16(dst + arr * (TC_KA * 8) + ch * 16, src + ab + ch * 2);
-            } else if (tid < 72) {     // weights: 8 chunks
-                const int ch = tid - 64;
-                cp_async16(dst + 4 * TC_KA * 8 + ch * 16, P.w + ab + ch * 4);
-            }
-            cp_async_commit();
-        };
         for (int64_t item = blockIdx.x; item < L.nitems && ok; item += gridDim.x) {
             const TcProblem &g = L.probs[L.item_prob[item]];
-            const int N = g.N;
             int t, ks, nt, mt;
             decode_item(g, item - g.item0, t, ks, nt, mt);
             const int64_t a0 = g.ts[t] + (int64_t)ks * g.slice_len;
             const int64_t a1 = min(g.ts[t + 1], a0 + g.slice_len);
-            const int64_t cnt = a1 > a0 ? a1 - a0 : 0;
-            const int nst = (int)(cnt / TC_KA);
+            const int nst = a1 > a0 ? (int)((a1 - a0) / TC_KA) : 0;
             if (nst == 0) continue;
             producers_sync();               // previous item's slots are free
-            issue(g, 0, a0);
+            stage_atoms(g, aslot, a0, tid);
             for (int st = 0; st < nst; st++, it++) {
                 const int s = it % S;
                 if (st + 1 < nst) {
-                    issue(g, (st + 1) & 1, a0 + (int64_t)(st + 1) * TC_KA);
+                    stage_atoms(g, aslot + ((st + 1) % TC_NSLOT) * TC_ATOM_SLOT, a0 + (int64_t)(st + 1) * TC_KA, tid);
                     cp_async_wait1();
                 } else {
                     cp_async_wait0();
                 }
                 producers_sync();           // group st staged for everybody
                 if (it >= (uint32_t)S && !mbar_wait(&empty[s], ((it / S) - 1) & 1, err, 1)) { ok = false; break; }
-                const uint8_t *as = aslot + (st & 1) * TC_ATOM_SLOT;
-                const uint64_t *s_ph0 = reinterpret_cast<const uint64_t *>(as);
-                const uint64_t *s_dra = s_ph0 + TC_KA, *s_drb = s_dra + TC_KA, *s_dac = s_drb + TC_KA;
-                const float *s_w = reinterpret_cast<const float *>(s_dac + TC_KA);
+                const uint8_t *as = aslot + (st % TC_NSLOT) * TC_ATOM_SLOT;
                 uint8_t *A = smem + (size_t)s * stage_bytes;
-                uint8_t *B = A + 4 * TC_A_BYTES;
-                const int units = 4 * TC_M + 4 * N;
-                for (int u = tid; u < units; u += TC_PROD_THREADS) {
-                    float re[8], im[8];
-                    uint32_t off;
-                    uint8_t *base;
-                    uint32_t ostride;
-                    if (u < 4 * TC_M) {
-                        const int r = u % TC_M, q = u / TC_M;
-                        const int64_t rg = (int64_t)mt * TC_M + r;
-                        const bool rv = rg < g.nrows;
-                        const uint32_t na = rv ? (uint32_t)(rg % g.fra) : 0u;
-                        const uint32_t nb = rv ? (uint32_t)(rg / g.fra) : 0u;
-                        const float wr = rv ? 1.f : 0.f;
-#pragma unroll
-                        for (int e = 0; e < 8; e++) {
-                            const int k = q * 8 + e;
-                            const uint64_t ph = s_ph0[k] + na * s_dra[k] + nb * s_drb[k];
-                            float c, sn;
-                            phasor(ph, c, sn);
-                            const float wj = s_w[k] * wr;
-                            re[e] = wj * c;
-                            im[e] = wj * sn;
-                        }
-                        off = core_off(r, q);
-                        base = A;
-                        ostride = TC_A_BYTES;
-                    } else {
-                        const int v = u - 4 * TC_M;
-                        const int c = v % N, q = v / N;
-                        const int64_t cg = (int64_t)nt * N + c;
-                        const float wc = cg < g.ncols ? 1.f : 0.f;
-                        const uint32_t nc = (uint32_t)cg;
-#pragma unroll
-                        for (int e = 0; e < 8; e++) {
-                            float cs, sn;
-                            phasor(nc * s_dac[q * 8 + e], cs, sn);
-                            re[e] = cs * wc;
-                            im[e] = sn * wc;
-                        }
-                        off = core_off(c, q);
-                        base = B;
-                        ostride = b_bytes;
-                    }
-                    uint4 hr, lr, hi_, li;
-                    split8(re, hr, lr, bf);
-                    split8(im, hi_, li, bf);
-                    *reinterpret_cast<uint4 *>(base + 0 * ostride + off) = hr;   // real hi
-                    *reinterpret_cast<uint4 *>(base + 1 * ostride + off) = lr;   // real lo
-                    *reinterpret_cast<uint4 *>(base + 2 * ostride + off) = hi_;  // imag hi
-                    *reinterpret_cast<uint4 *>(base + 3 * ostride + off) = li;   // imag lo
-                }
+                if (tid < 128)
+                    gen_rows<BF>(g, mt, as, A, tid);
+                else
+                    gen_cols<BF>(g, nt, as, A + 4 * TC_A_BYTES, b_bytes, tid - 128);
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 mbar_arrive(&full[s]);
             }
@@ -378,8 +453,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
         }
     } else if (warp == TC_MMA_WARP) {
         // ------------------------------------------------------------ MMA issuer
-        const uint32_t fmt = bf ? 1u : 0u;
-        const uint32_t c_re = tmem, c_im = tmem + (uint32_t)NM;  // correction accumulator
+        const uint32_t fmt = BF ? 1u : 0u;
+        const uint32_t c_acc = tmem;                                  // correction accumulator
         uint32_t it = 0, nitem = 0, nchunk = 0;
         bool ok = true, issued = false;
         for (int64_t item = blockIdx.x; item < L.nitems && ok; item += gridDim.x) {
@@ -389,12 +464,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
             decode_item(g, item - g.item0, t, ks, nt, mt);
             const int64_t a0 = g.ts[t] + (int64_t)ks * g.slice_len;
             const int64_t a1 = min(g.ts[t + 1], a0 + g.slice_len);
-            const int64_t cnt = a1 > a0 ? a1 - a0 : 0;
-            const int nst = (int)((cnt + TC_KA - 1) / TC_KA);
+            const int nst = a1 > a0 ? (int)((a1 - a0) / TC_KA) : 0;
             if (nst == 0) continue;
-            const uint32_t idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(N >> 3) << 17) |
+            // D = 128 x 2N, f32; A and B of the operand format
+            const uint32_t idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)((2 * N) >> 3) << 17) |
                                    ((uint32_t)(TC_M >> 4) << 24);
-            const uint32_t idesc_neg = idesc | (1u << 13);     // negate A: the -Ui Vi^T products
+            const uint32_t idesc_neg = idesc | (1u << 13);     // negate A: the -Ui products
+            const uint32_t b2off = (uint32_t)(N >> 3) * TC_SBO; // B rows N.. : [Vi; -Vr]
             // the correction accumulator restarts with this item: previous one drained?
             if (nitem > 0 && !mbar_wait(cempty, (nitem - 1) & 1, err, 2)) { ok = false; break; }
             for (int st0 = 0; st0 < nst && ok; st0 += L.flush, nchunk++) {
@@ -402,7 +478,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
                 const uint32_t use = nchunk / L.nbuf;
                 if (use > 0 && !mbar_wait(&mempty[b], (use - 1) & 1, err, 6)) { ok = false; break; }
                 tc_fence_after();
-                const uint32_t m_re = tmem + 2u * NM * (1u + (uint32_t)b), m_im = m_re + (uint32_t)NM;
+                const uint32_t m_acc = tmem + 2u * NM * (1u + (uint32_t)b);
                 const int st1 = min(nst, st0 + L.flush);
                 for (int st = st0; st < st1; st++, it++) {
                     const int s = it % S;
@@ -410,30 +486,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
                     tc_fence_after();
                     if (lane == 0) {
                         const uint32_t A = smem_u32(smem + (size_t)s * stage_bytes);
-                        const uint32_t B = A + 4 * TC_A_BYTES;
+                        const uint32_t Bh = A + 4 * TC_A_BYTES, Bl = Bh + b_bytes;
 #pragma unroll
                         for (int kk = 0; kk < TC_KA / 16; kk++) {
                             const uint32_t ko = kk * 2 * TC_LBO;
                             const uint64_t arh = sdesc(A + 0 * TC_A_BYTES + ko), arl = sdesc(A + 1 * TC_A_BYTES + ko);
                             const uint64_t aih = sdesc(A + 2 * TC_A_BYTES + ko), ail = sdesc(A + 3 * TC_A_BYTES + ko);
-                            const uint64_t brh = sdesc(B + 0 * b_bytes + ko), brl = sdesc(B + 1 * b_bytes + ko);
-                            const uint64_t bih = sdesc(B + 2 * b_bytes + ko), bil = sdesc(B + 3 * b_bytes + ko);
+                            const uint64_t b1h = sdesc(Bh + ko), b2h = sdesc(Bh + b2off + ko);
+                            const uint64_t b1l = sdesc(Bl + ko), b2l = sdesc(Bl + b2off + ko);
                             const uint32_t am = (st > st0 || kk > 0) ? 1u : 0u;   // main restarts per chunk
                             const uint32_t ac = (st > 0 || kk > 0) ? 1u : 0u;     // correction per item
                             // main: (hi,hi)
-                            mma_f16(m_re, arh, brh, idesc, am);
-                            mma_f16(m_re, aih, bih, idesc_neg, 1u);
-                            mma_f16(m_im, arh, bih, idesc, am);
-                            mma_f16(m_im, aih, brh, idesc, 1u);
+                            mma_f16(m_acc, arh, b1h, idesc, am);
+                            mma_f16(m_acc, aih, b2h, idesc_neg, 1u);
                             // corrections: (hi,lo) and (lo,hi)
-                            mma_f16(c_re, arh, brl, idesc, ac);
-                            mma_f16(c_re, aih, bil, idesc_neg, 1u);
-                            mma_f16(c_re, arl, brh, idesc, 1u);
-                            mma_f16(c_re, ail, bih, idesc_neg, 1u);
-                            mma_f16(c_im, arh, bil, idesc, ac);
-                            mma_f16(c_im, aih, brl, idesc, 1u);
-                            mma_f16(c_im, arl, bih, idesc, 1u);
-                            mma_f16(c_im, ail, brh, idesc, 1u);
+                            mma_f16(c_acc, arh, b1l, idesc, ac);
+                            mma_f16(c_acc, aih, b2l, idesc_neg, 1u);
+                            mma_f16(c_acc, arl, b1h, idesc, 1u);
+                            mma_f16(c_acc, ail, b2h, idesc_neg, 1u);
                         }
                         mma_commit(&empty[s]);
                         issued = true;
@@ -458,6 +528,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
         // ------------------------------------------------------------ epilogue
         const int q = warp & 3;                       // TMEM lane quadrant of this warp
         const int r = q * 32 + lane;
+        const uint32_t lane_off = (uint32_t)(q * 32) << 16;
+        const uint32_t t_corr = tmem + lane_off;
+        const uint32_t t_sum = tmem + lane_off + 2u * NM * (1u + (uint32_t)L.nbuf);
         uint32_t nitem = 0, nchunk = 0;
         bool ok = true;
         for (int64_t item = blockIdx.x; item < L.nitems && ok; item += gridDim.x) {
@@ -467,71 +540,89 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
             decode_item(g, item - g.item0, t, ks, nt, mt);
             const int64_t a0 = g.ts[t] + (int64_t)ks * g.slice_len;
             const int64_t a1 = min(g.ts[t + 1], a0 + g.slice_len);
-            const int64_t cnt = a1 > a0 ? a1 - a0 : 0;
-            const int nst = (int)((cnt + TC_KA - 1) / TC_KA);
+            const int nst = a1 > a0 ? (int)((a1 - a0) / TC_KA) : 0;
             const int64_t rg = (int64_t)mt * TC_M + r;
-            const bool rv = rg < g.nrows;
-            const int64_t prow = rv ? (rg % g.fra) * g.sra + (rg / g.fra) * g.srb : 0;
-            float2 *out = g.part + ((int64_t)t * g.nslice + ks) * g.pbox + prow;
-            const int64_t cbase0 = (int64_t)nt * N;
+            const bool rv = rg < g.nrows_p && (int)(rg % g.fra_p) < g.fra;
+            const int64_t nrp = g.nrows_p;
+            const int ncv = min(N, g.ncols - nt * N);             // valid columns of this tile
+            float2 *oc = g.part + ((int64_t)t * g.nslice + ks) * g.slab + (int64_t)nt * N * nrp + rg;
             if (nst == 0) {
                 if (rv)
-                    for (int c = 0; c < N && cbase0 + c < g.ncols; c++) out[(cbase0 + c) * g.sac] = make_float2(0.f, 0.f);
+                    for (int c = 0; c < ncv; c++) oc[(int64_t)c * nrp] = make_float2(0.f, 0.f);
                 continue;
             }
-            // main accumulator, one chunk at a time: first chunk stores, later chunks add
             for (int st0 = 0; st0 < nst; st0 += L.flush, nchunk++) {
                 const int b = (int)(nchunk % L.nbuf);
                 if (!mbar_wait(&mfull[b], (nchunk / L.nbuf) & 1, err, 5)) { ok = false; break; }
                 tc_fence_after();
-                const uint32_t col0 = 2u * NM * (1u + (uint32_t)b);
+                const bool first = st0 == 0, last = st0 + L.flush >= nst;
+                if (last) {                                        // the item's corrections
+                    if (!mbar_wait(cfull, nitem & 1, err, 7)) { ok = false; break; }
+                    tc_fence_after();
+                }
+                const uint32_t t_main = tmem + lane_off + 2u * NM * (1u + (uint32_t)b);
+                const bool keep = L.tsum && !last;                 // running sum stays in TMEM
                 for (int c0 = 0; c0 < N; c0 += 16) {
                     uint32_t vr[16], vi[16];
-                    const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + col0 + (uint32_t)c0;
-                    tmem_ld16(ta, vr);
-                    tmem_ld16(ta + (uint32_t)NM, vi);
+                    float fr[16], fi[16];
+                    tmem_ld16(t_main + (uint32_t)c0, vr);
+                    tmem_ld16(t_main + (uint32_t)(N + c0), vi);
                     tmem_wait_ld();
 #pragma unroll
                     for (int k = 0; k < 16; k++) {
-                        const int64_t cg = cbase0 + c0 + k;
-                        if (rv && cg < g.ncols) {
-                            float2 v = make_float2(__uint_as_float(vr[k]), __uint_as_float(vi[k]));
-                            float2 *o = out + cg * g.sac;
-                            if (st0 > 0) {
-                                float2 old = *o;
-                                v.x += old.x;
-                                v.y += old.y;
+                        fr[k] = __uint_as_float(vr[k]);
+                        fi[k] = __uint_as_float(vi[k]);
+                    }
+                    if (L.tsum && !first) {
+                        tmem_ld16(t_sum + (uint32_t)c0, vr);
+                        tmem_ld16(t_sum + (uint32_t)(N + c0), vi);
+                        tmem_wait_ld();
+#pragma unroll
+                        for (int k = 0; k < 16; k++) {
+                            fr[k] += __uint_as_float(vr[k]);
+                            fi[k] += __uint_as_float(vi[k]);
+                        }
+                    }
+                    if (last) {
+                        tmem_ld16(t_corr + (uint32_t)c0, vr);
+                        tmem_ld16(t_corr + (uint32_t)(N + c0), vi);
+                        tmem_wait_ld();
+#pragma unroll
+                        for (int k = 0; k < 16; k++) {
+                            fr[k] += __uint_as_float(vr[k]);
+                            fi[k] += __uint_as_float(vi[k]);
+                        }
+                    }
+                    if (keep) {
+#pragma unroll
+                        for (int k = 0; k < 16; k++) {
+                            vr[k] = __float_as_uint(fr[k]);
+                            vi[k] = __float_as_uint(fi[k]);
+                        }
+                        tmem_st16(t_sum + (uint32_t)c0, vr);
+                        tmem_st16(t_sum + (uint32_t)(N + c0), vi);
+                    } else if (rv) {
+#pragma unroll
+                        for (int k = 0; k < 16; k++) {
+                            if (c0 + k < ncv) {
+                                float2 *o = oc + (int64_t)(c0 + k) * nrp;
+                                float2 v = make_float2(fr[k] * TC_UNSCALE, fi[k] * TC_UNSCALE);
+                                if (!L.tsum && !first) {
+                                    const float2 old = *o;
+                                    v.x += old.x;
+                                    v.y += old.y;
+                                }
+                                *o = v;
                             }
-                            *o = v;
                         }
                     }
                 }
+                if (keep) tmem_wait_st();
                 tc_fence_before();
                 mbar_arrive(&mempty[b]);
+                if (last) mbar_arrive(cempty);
             }
             if (!ok) break;
-            // correction accumulator of the item
-            if (!mbar_wait(cfull, nitem & 1, err, 7)) { ok = false; break; }
-            tc_fence_after();
-            for (int c0 = 0; c0 < N; c0 += 16) {
-                uint32_t vr[16], vi[16];
-                const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
-                tmem_ld16(ta, vr);
-                tmem_ld16(ta + (uint32_t)NM, vi);
-                tmem_wait_ld();
-#pragma unroll
-                for (int k = 0; k < 16; k++) {
-                    const int64_t cg = cbase0 + c0 + k;
-                    if (rv && cg < g.ncols) {
-                        float2 *o = out + cg * g.sac;
-                        float2 old = *o;
-                        *o = make_float2(fmaf(__uint_as_float(vr[k]), TC_LO_UNSCALE, old.x),
-                                         fmaf(__uint_as_float(vi[k]), TC_LO_UNSCALE, old.y));
-                    }
-                }
-            }
-            tc_fence_before();
-            mbar_arrive(cempty);
             nitem++;
         }
     }
@@ -540,6 +631,27 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(L.tmem_cols)
                      : "memory");
+    }
+}
+
+// Per-atom step factors exp(2 pi i 8 d) along the three grid axes, to about
+// one ulp: the turn 8d / 2^64 is split into a float part for sincospif and a
+// small remainder applied to first order.
+__global__ void k_tc_mult(const uint64_t *__restrict__ du, const uint64_t *__restrict__ dv,
+                          const uint64_t *__restrict__ dw, int64_t n, int64_t stride, float2 *__restrict__ out)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint64_t *d[3] = {du, dv, dw};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const int64_t v = (int64_t)(d[a][i] << 3);
+        const double x = (double)v * 0x1p-63;          // turns x 2, in [-1, 1]
+        const float xf = (float)x;
+        const float dth = (float)((x - (double)xf) * 3.141592653589793);
+        float s, c;
+        sincospif(xf, &s, &c);
+        out[a * stride + i] = make_float2(fmaf(-s, dth, c), fmaf(c, dth, s));
     }
 }
 
@@ -561,13 +673,24 @@ static uint32_t pow2_cols(int n)
     return c;
 }
 
+// row axes for a column axis: ra is the longer of the other two
+static void tc_row_axes(const BoxSpec &box, int ac, int &ra, int &rb)
+{
+    const int a = ac == 0 ? 1 : 0, b = 3 - ac - a;
+    if (box.f[b] > box.f[a]) { ra = b; rb = a; }
+    else { ra = a; rb = b; }
+}
+
 // padded MMA area of a column axis / tile width
-static double tc_area(const BoxSpec &box, int a, int N)
+static double tc_area(const BoxSpec &box, int ac, int N)
 {
     const int64_t npts = (int64_t)box.f[0] * box.f[1] * box.f[2];
-    const int nc = box.f[a];
+    const int nc = box.f[ac];
     if (nc < 2 && npts != nc) return -1.0;
-    return (double)dgpu_cdiv(nc, N) * N * dgpu_cdiv(npts / nc, TC_M) * TC_M;
+    int ra, rb;
+    tc_row_axes(box, ac, ra, rb);
+    const int64_t rows = (int64_t)dgpu_cdiv(box.f[ra], 8) * 8 * box.f[rb];
+    return (double)dgpu_cdiv(nc, N) * N * dgpu_cdiv(rows, TC_M) * TC_M;
 }
 
 // Geometry of one problem for a column axis, tile width and slicing.
@@ -578,19 +701,16 @@ static void tc_problem(dgpu_ctx *ctx, const TcInput &in, const dgpu_opts *op, in
     const BoxSpec &box = in.box;
     for (int k = 0; k < 3; k++) g.f[k] = box.f[k];
     g.ac = axis;
-    g.ra = axis == 0 ? 1 : 0;
-    g.rb = 3 - axis - g.ra;
+    tc_row_axes(box, axis, g.ra, g.rb);
     g.ncols = box.f[axis];
     g.fra = box.f[g.ra];
-    const int64_t stride[3] = {1, (int64_t)box.f[0], (int64_t)box.f[0] * box.f[1]};
-    g.sra = stride[g.ra];
-    g.srb = stride[g.rb];
-    g.sac = stride[axis];
-    g.nrows = box.f[g.ra] * box.f[g.rb];
+    g.fra_p = (int32_t)dgpu_cdiv(g.fra, 8) * 8;
+    g.frb = box.f[g.rb];
+    g.nrows_p = (int64_t)g.fra_p * g.frb;
     g.N = N;
     g.n_tiles = (int32_t)dgpu_cdiv(g.ncols, N);
-    g.m_tiles = (int32_t)dgpu_cdiv(g.nrows, TC_M);
-    g.pbox = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    g.m_tiles = (int32_t)dgpu_cdiv(g.nrows_p, TC_M);
+    g.slab = g.nrows_p * g.ncols;
     g.ntype = in.ntype;
     int64_t maxn = 0;
     for (int t = 0; t < in.ntype; t++) {
@@ -618,6 +738,19 @@ static void tc_problem(dgpu_ctx *ctx, const TcInput &in, const dgpu_opts *op, in
     g.drb = dd[g.rb];
     g.dac = dd[axis];
     g.w = in.w;
+    g.ma = in.mult + (int64_t)g.ra * in.mult_stride;
+    g.mc = in.mult + (int64_t)axis * in.mult_stride;
+}
+
+void dgpu_tc_partref(const TcProblem &g, const float2 *p, PartRef &ref)
+{
+    ref.p = p;
+    ref.nslice = g.nslice;
+    ref.f32 = 1;
+    ref.s[g.ra] = 1;
+    ref.s[g.rb] = g.fra_p;
+    ref.s[g.ac] = g.nrows_p;
+    ref.slab = g.slab;
 }
 
 int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *op, int N, int slice_mult,
@@ -643,7 +776,7 @@ int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *o
         items += g.nitems;
         plan.part_off[p] = elems;
         plan.nslice[p] = g.nslice;
-        elems += (int64_t)g.ntype * g.nslice * g.pbox;
+        elems += (int64_t)g.ntype * g.nslice * g.slab;
     }
     plan.item_prob.resize(items);
     for (int p = 0; p < nprob; p++)
@@ -663,19 +796,22 @@ int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *o
     L.item_prob = (const int32_t *)((char *)desc.p + pbytes);
     L.nitems = items;
     L.Nmax = N;
-    L.nbuf = 6 * N <= 512 ? 2 : 1;
+    // TMEM: correction (2N) + main x nbuf (2N each) [+ running sum (2N)]
+    L.nbuf = 2 * N * 3 <= 512 ? 2 : 1;
+    L.tsum = 2 * N * (2 + L.nbuf) <= 512 ? 1 : 0;
     L.flush = op->tc_flush > 0 ? (int32_t)dgpu_cdiv(op->tc_flush, TC_KA) : TC_FLUSH_STAGES;
     L.bf16 = op->split == DGPU_SPLIT_BF16;
-    const uint32_t stage_bytes = 4 * TC_A_BYTES + 4u * N * TC_KA * 2;
-    const uint32_t bar_bytes = TC_BAR_BYTES + 2 * TC_ATOM_SLOT;
-    const int stages = (int)((200 * 1024 - bar_bytes) / stage_bytes);
+    const uint32_t stage_bytes = 4 * TC_A_BYTES + 2u * 3u * N * TC_KA * 2;
+    const uint32_t bar_bytes = TC_BAR_BYTES + TC_NSLOT * TC_ATOM_SLOT;
+    const int stages = (int)((TC_SMEM_BUDGET - bar_bytes) / stage_bytes);
     L.stages = stages > 4 ? 4 : stages;
-    L.tmem_cols = pow2_cols(2 * N * (1 + L.nbuf));
+    L.tmem_cols = pow2_cols(2 * N * (1 + L.nbuf + L.tsum));
     if (L.stages < 2 || L.tmem_cols > 512) return dgpu_set_error(ctx, DGPU_ERR_ARG, "tile does not fit");
     plan.smem = (size_t)L.stages * stage_bytes + bar_bytes;
     static bool attr_set = false;     // set once, outside any stream capture
     if (!attr_set) {
-        DGPU_CUDA(ctx, cudaFuncSetAttribute(k_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+        DGPU_CUDA(ctx, cudaFuncSetAttribute(k_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+        DGPU_CUDA(ctx, cudaFuncSetAttribute(k_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
         attr_set = true;
     }
     DGPU_CUDA(ctx, ctx->flag.ensure(64));
@@ -688,7 +824,10 @@ int dgpu_tc_launch(dgpu_ctx *ctx, const TcPlan &plan)
     DGPU_CUDA(ctx, cudaMemsetAsync(plan.L.err, 0, sizeof(int32_t), ctx->stream));
     if (plan.L.nitems < 1) return DGPU_OK;
     const int grid = (int)(plan.L.nitems < ctx->nsm ? plan.L.nitems : ctx->nsm);
-    k_tc<<<grid, TC_THREADS, plan.smem, ctx->stream>>>(plan.L);
+    if (plan.L.bf16)
+        k_tc<true><<<grid, TC_THREADS, plan.smem, ctx->stream>>>(plan.L);
+    else
+        k_tc<false><<<grid, TC_THREADS, plan.smem, ctx->stream>>>(plan.L);
     DGPU_CUDA(ctx, cudaGetLastError());
     return DGPU_OK;
 }
@@ -703,9 +842,18 @@ int dgpu_tc_check(dgpu_ctx *ctx)
     return DGPU_OK;
 }
 
+int dgpu_tc_mult_async(dgpu_ctx *ctx, const uint64_t *du, const uint64_t *dv, const uint64_t *dw, int64_t n,
+                       int64_t stride, float2 *out)
+{
+    if (n < 1) return DGPU_OK;
+    k_tc_mult<<<(unsigned)dgpu_cdiv(n, 256), 256, 0, ctx->stream>>>(du, dv, dw, n, stride, out);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    return DGPU_OK;
+}
+
 // Candidate configurations: every column axis and tile width whose padded
 // MMA area is within 25% of the smallest, at two slicings.
-static void tc_candidates(const BoxSpec &box, int want_n, TcChoice *out, int &n)
+static void tc_candidates(const BoxSpec &box, int want_n, int kslice, TcChoice *out, int &n)
 {
     double best = 1e300;
     for (int a = 0; a < 3; a++)
@@ -722,6 +870,7 @@ static void tc_candidates(const BoxSpec &box, int want_n, TcChoice *out, int &n)
             if (ar < 0 || ar > 1.25 * best) continue;
             for (int m : {4, 8}) {
                 if (n >= 64) return;
+                if (kslice > 0 && m != 4) continue;     // the slicing is given: one candidate per tile
                 out[n].axis = a;
                 out[n].N = N;
                 out[n].slice_mult = m;
@@ -732,7 +881,7 @@ static void tc_candidates(const BoxSpec &box, int want_n, TcChoice *out, int &n)
 
 int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const uint64_t *dv, const uint64_t *dw,
                  const float *w, const int64_t *h_type_start, int32_t ntype, const BoxSpec &box,
-                 const dgpu_opts *op, DevBuf &part, int32_t *nslice_out)
+                 const dgpu_opts *op, DevBuf &part, PartRef *ref)
 {
     if (ntype < 1 || ntype > 64) return dgpu_set_error(ctx, DGPU_ERR_ARG, "ntype=%d", ntype);
     const int want_n = op->tc_tile_n;
@@ -743,6 +892,10 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
         const int64_t n = h_type_start[t + 1] - h_type_start[t];
         maxn = n > maxn ? n : maxn;
     }
+    const int64_t npad = h_type_start[ntype];
+    DGPU_CUDA(ctx, ctx->tc_mult.ensure((size_t)3 * (npad > 0 ? npad : 1) * sizeof(float2)));
+    int rc = dgpu_tc_mult_async(ctx, du, dv, dw, npad, npad, ctx->tc_mult.as<float2>());
+    if (rc) return rc;
     int lg = 0;
     while ((1LL << lg) < maxn) lg++;
     const TcKey key(box.f[0], box.f[1], box.f[2], ntype, lg, op->split * 1000 + want_n,
@@ -753,6 +906,8 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
     in.dv = dv;
     in.dw = dw;
     in.w = w;
+    in.mult = ctx->tc_mult.as<float2>();
+    in.mult_stride = npad;
     in.ts = h_type_start;
     in.ntype = ntype;
     in.box = box;
@@ -763,15 +918,16 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
     } else {
         TcChoice cand[64];
         int nc = 0;
-        tc_candidates(box, want_n, cand, nc);
+        tc_candidates(box, want_n, op->tc_kslice, cand, nc);
         if (nc == 0) return dgpu_set_error(ctx, DGPU_ERR_ARG, "no tensor-core tile fits the box");
         float best = 1e30f;
-        for (int c = 0; c < nc; c++) {
+        choice = cand[0];
+        for (int c = 0; c < nc && nc > 1; c++) {
             in.axis = cand[c].axis;
             TcPlan plan;
             if (dgpu_tc_plan(ctx, 1, &in, op, cand[c].N, cand[c].slice_mult, plan, part, ctx->tc_part)) continue;
             DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[4], ctx->stream));
-            int rc = dgpu_tc_launch(ctx, plan);
+            rc = dgpu_tc_launch(ctx, plan);
             if (rc) return rc;
             DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[5], ctx->stream));
             rc = dgpu_tc_check(ctx);
@@ -787,7 +943,7 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
     }
     in.axis = choice.axis;
     TcPlan plan;
-    int rc = dgpu_tc_plan(ctx, 1, &in, op, choice.N, choice.slice_mult, plan, part, ctx->tc_part);
+    rc = dgpu_tc_plan(ctx, 1, &in, op, choice.N, choice.slice_mult, plan, part, ctx->tc_part);
     if (rc) return rc;
     rc = dgpu_tc_launch(ctx, plan);
     if (rc) return rc;
@@ -797,6 +953,6 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
     ctx->tc_last[1] = plan.probs[0].N;
     ctx->tc_last[2] = plan.L.nbuf;
     ctx->tc_last[3] = (int32_t)plan.probs[0].slice_len;
-    *nslice_out = plan.nslice[0];
+    dgpu_tc_partref(plan.probs[0], part.as<float2>(), *ref);
     return DGPU_OK;
 }
