@@ -112,19 +112,32 @@ __device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity)
     return ok != 0;
 }
 
+// try_wait that may suspend the thread until the phase completes, at most
+// TC_SUSPEND_NS: a waiting warp takes no issue slots from the producers
+#define TC_SUSPEND_NS 20000
+__device__ __forceinline__ bool mbar_try_suspend(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity), "n"(TC_SUSPEND_NS)
+        : "memory");
+    return ok != 0;
+}
+
 // bounded wait: false if the error flag is up or the wait timed out
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int32_t *err, int code)
 {
     if (mbar_try(bar, parity)) return true;
-    uint64_t t0 = gtimer();
-    for (uint32_t it = 1;; ++it) {
-        if (mbar_try(bar, parity)) return true;
-        if ((it & 63) == 0) {
-            if (*err) return false;
-            if (gtimer() - t0 > TC_TIMEOUT_NS) {
-                atomicCAS((int32_t *)err, 0, code);
-                return false;
-            }
+    const uint64_t t0 = gtimer();
+    for (;;) {
+        if (mbar_try_suspend(bar, parity)) return true;
+        if (*err) return false;
+        if (gtimer() - t0 > TC_TIMEOUT_NS) {
+            atomicCAS((int32_t *)err, 0, code);
+            return false;
         }
     }
 }
@@ -248,9 +261,16 @@ __device__ __forceinline__ void decode_item(const TcProblem &g, int64_t item, in
     t = (int)(r / g.nslice);
 }
 
+// Source arrays of one problem, held in registers by the producers.
+struct TcSrc {
+    const uint64_t *ph0, *dra, *drb, *dac;
+    const float *w;
+    const float2 *ma, *mc;
+};
+
 // Stage the phase data of the 32-atom group starting at padded atom ab into
 // an atom slot: 104 chunks of 16 bytes, one per thread of tid < 104.
-__device__ __forceinline__ void stage_atoms(const TcProblem &P, uint8_t *dst, int64_t ab, int tid)
+__device__ __forceinline__ void stage_atoms(const TcSrc &P, uint8_t *dst, int64_t ab, int tid)
 {
     if (tid < 64) {                     // ph0, d_ra, d_rb, d_ac: 16 chunks each
         const int arr = tid >> 4, ch = tid & 15;
@@ -266,19 +286,20 @@ __device__ __forceinline__ void stage_atoms(const TcProblem &P, uint8_t *dst, in
     cp_async_commit();
 }
 
-// U rows of one stage.  Thread (s, j, h) of the first 128 producers: atoms
-// 4j..4j+3, rows 8*(8h+m)+s for m = 0..7 (the rows of one lane of eight core
-// matrices; a warp's stores of one step cover 16 distinct 8-byte bank slots).
+// U rows of one stage for row groups [q0, q1) of the tile (8 rows each).
+// The thread owns atoms k0..k0+3 and row s of every group: it seeds at the
+// first group from the exact phase and steps by exp(2 pi i 8 d_ra) from group
+// to group, restarting from the exact phase where nb changes (gpn groups per
+// nb).  A warp's stores of one step cover 16 distinct 8-byte bank slots.
 template <bool BF>
-__device__ __forceinline__ void gen_rows(const TcProblem &g, int mt, const uint8_t *as, uint8_t *A, int tid)
+__device__ __forceinline__ void gen_rows(int q0, int q1, int mt, int gpn, const uint8_t *as, uint8_t *A, int s,
+                                         int j)
 {
-    const int s = tid & 7, j = (tid >> 3) & 7, h = tid >> 6;
     const uint64_t *s_ph0 = reinterpret_cast<const uint64_t *>(as);
     const uint64_t *s_dra = s_ph0 + TC_KA, *s_drb = s_dra + TC_KA;
     const float *s_w = reinterpret_cast<const float *>(as + TC_SLOT_W);
     const float2 *s_ma = reinterpret_cast<const float2 *>(as + TC_SLOT_MA);
-    const int gpn = g.fra_p >> 3;                   // row groups per nb
-    const int G0 = mt * (TC_M / 8) + 8 * h;
+    const int G0 = mt * (TC_M / 8) + q0;
     int gi = G0 % gpn;
     uint32_t nb = (uint32_t)(G0 / gpn);
     const int k0 = 4 * j;
@@ -295,10 +316,10 @@ __device__ __forceinline__ void gen_rows(const TcProblem &g, int mt, const uint8
 #pragma unroll
     for (int a = 0; a < 4; a++) m[a] = s_ma[k0 + a];
     seed((uint32_t)(gi * 8 + s));
-    uint8_t *dst = A + (8 * h) * TC_SBO + (j >> 1) * TC_LBO + s * 16 + (j & 1) * 8;
+    uint8_t *dst = A + (j >> 1) * TC_LBO + s * 16 + (j & 1) * 8;
 #pragma unroll 1
-    for (int mm = 0; mm < 8; mm++) {
-        if (mm > 0) {
+    for (int q = q0; q < q1; q++) {
+        if (q > q0) {
             if (++gi == gpn) {          // next nb: restart from the exact phase (warp-uniform)
                 gi = 0;
                 nb++;
@@ -311,7 +332,7 @@ __device__ __forceinline__ void gen_rows(const TcProblem &g, int mt, const uint8
         uint2 rh, rl, ih, il;
         split4<BF>(x[0].x, x[1].x, x[2].x, x[3].x, rh, rl);
         split4<BF>(x[0].y, x[1].y, x[2].y, x[3].y, ih, il);
-        uint8_t *d = dst + mm * TC_SBO;
+        uint8_t *d = dst + q * TC_SBO;
         *reinterpret_cast<uint2 *>(d + 0 * TC_A_BYTES) = rh;    // Ur hi
         *reinterpret_cast<uint2 *>(d + 1 * TC_A_BYTES) = rl;    // Ur lo
         *reinterpret_cast<uint2 *>(d + 2 * TC_A_BYTES) = ih;    // Ui hi
@@ -319,22 +340,17 @@ __device__ __forceinline__ void gen_rows(const TcProblem &g, int mt, const uint8
     }
 }
 
-// V columns of one stage: thread (s, j, h) of producers 128..255: atoms
-// 4j..4j+3, columns 8*gc+s for gc in its half of the N/8 column groups.  B
-// rows: Vr at c, Vi at N+c, -Vr at 2N+c, in a hi and a lo operand.
+// V columns of one stage for column groups [q0, q1) of the tile: atoms
+// k0..k0+3, column 8q+s of every group, stepping by exp(2 pi i 8 d_ac).
+// B rows: Vr at c, Vi at N+c, -Vr at 2N+c, in a hi and a lo operand.
 template <bool BF>
-__device__ __forceinline__ void gen_cols(const TcProblem &g, int nt, const uint8_t *as, uint8_t *Bh,
-                                         uint32_t b_bytes, int t)
+__device__ __forceinline__ void gen_cols(int q0, int q1, int nt, int N, const uint8_t *as, uint8_t *Bh,
+                                         uint32_t b_bytes, int s, int j)
 {
-    const int s = t & 7, j = (t >> 3) & 7, h = t >> 6;
-    const int N = g.N;
-    const int ngrp = N >> 3, per = (ngrp + 1) >> 1;
-    const int gc0 = h * per, gc1 = min(ngrp, gc0 + per);
-    if (gc0 >= gc1) return;
     const uint64_t *s_dac = reinterpret_cast<const uint64_t *>(as) + 3 * TC_KA;
     const float2 *s_mc = reinterpret_cast<const float2 *>(as + TC_SLOT_MC);
     const int k0 = 4 * j;
-    const uint32_t nc = (uint32_t)(nt * N + gc0 * 8 + s);
+    const uint32_t nc = (uint32_t)(nt * N + q0 * 8 + s);
     float2 x[4], m[4];
 #pragma unroll
     for (int a = 0; a < 4; a++) {
@@ -346,15 +362,15 @@ __device__ __forceinline__ void gen_cols(const TcProblem &g, int nt, const uint8
     const uint32_t blk = (uint32_t)(N >> 3) * TC_SBO;           // N rows further
     const uint32_t o0 = (j >> 1) * TC_LBO + s * 16 + (j & 1) * 8;
 #pragma unroll 1
-    for (int gc = gc0; gc < gc1; gc++) {
-        if (gc > gc0) {
+    for (int q = q0; q < q1; q++) {
+        if (q > q0) {
 #pragma unroll
             for (int a = 0; a < 4; a++) x[a] = cmulf(x[a], m[a]);
         }
         uint2 rh, rl, ih, il;
         split4<BF>(x[0].x, x[1].x, x[2].x, x[3].x, rh, rl);
         split4<BF>(x[0].y, x[1].y, x[2].y, x[3].y, ih, il);
-        const uint32_t o = gc * TC_SBO + o0;
+        const uint32_t o = q * TC_SBO + o0;
         const uint2 nrh = make_uint2(rh.x ^ 0x80008000u, rh.y ^ 0x80008000u);
         const uint2 nrl = make_uint2(rl.x ^ 0x80008000u, rl.y ^ 0x80008000u);
         *reinterpret_cast<uint2 *>(Bh + o) = rh;
@@ -417,7 +433,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
         // weight).  Their phase data is staged in shared memory with cp.async
         // one group ahead; three slots, so that a slot is rewritten only after
         // every producer has passed the barrier that follows its last use.
+        // Work split: the 16 row groups of U and the N/8 column groups of V
+        // form one list, cut into four equal ranges; producer thread
+        // (s = lane&7, j = atom quad, u) takes range u for its atom quad.
         const int tid = threadIdx.x;
+        const int s = lane & 7, j = (lane >> 3) + 4 * (warp & 1), u = warp >> 1;
         uint32_t it = 0;
         bool ok = true;
         for (int64_t item = blockIdx.x; item < L.nitems && ok; item += gridDim.x) {
@@ -428,26 +448,31 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
             const int64_t a1 = min(g.ts[t + 1], a0 + g.slice_len);
             const int nst = a1 > a0 ? (int)((a1 - a0) / TC_KA) : 0;
             if (nst == 0) continue;
+            const TcSrc src = {g.ph0, g.dra, g.drb, g.dac, g.w, g.ma, g.mc};
+            const int N = g.N, gpn = g.fra_p >> 3;
+            const int ngr = TC_M / 8, ntot = ngr + (N >> 3), per = (ntot + 3) >> 2;
+            const int r0 = u * per, r1 = min(ntot, r0 + per);
+            const int ra0 = min(r0, ngr), ra1 = min(r1, ngr);           // row groups
+            const int rc0 = max(r0, ngr) - ngr, rc1 = max(r1, ngr) - ngr; // column groups
             producers_sync();               // previous item's slots are free
-            stage_atoms(g, aslot, a0, tid);
+            stage_atoms(src, aslot, a0, tid);
             for (int st = 0; st < nst; st++, it++) {
-                const int s = it % S;
+                const int sb = it % S;
                 if (st + 1 < nst) {
-                    stage_atoms(g, aslot + ((st + 1) % TC_NSLOT) * TC_ATOM_SLOT, a0 + (int64_t)(st + 1) * TC_KA, tid);
+                    stage_atoms(src, aslot + ((st + 1) % TC_NSLOT) * TC_ATOM_SLOT, a0 + (int64_t)(st + 1) * TC_KA,
+                                tid);
                     cp_async_wait1();
                 } else {
                     cp_async_wait0();
                 }
                 producers_sync();           // group st staged for everybody
-                if (it >= (uint32_t)S && !mbar_wait(&empty[s], ((it / S) - 1) & 1, err, 1)) { ok = false; break; }
+                if (it >= (uint32_t)S && !mbar_wait(&empty[sb], ((it / S) - 1) & 1, err, 1)) { ok = false; break; }
                 const uint8_t *as = aslot + (st % TC_NSLOT) * TC_ATOM_SLOT;
-                uint8_t *A = smem + (size_t)s * stage_bytes;
-                if (tid < 128)
-                    gen_rows<BF>(g, mt, as, A, tid);
-                else
-                    gen_cols<BF>(g, nt, as, A + 4 * TC_A_BYTES, b_bytes, tid - 128);
+                uint8_t *A = smem + (size_t)sb * stage_bytes;
+                if (ra0 < ra1) gen_rows<BF>(ra0, ra1, mt, gpn, as, A, s, j);
+                if (rc0 < rc1) gen_cols<BF>(rc0, rc1, nt, N, as, A + 4 * TC_A_BYTES, b_bytes, s, j);
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                mbar_arrive(&full[s]);
+                mbar_arrive(&full[sb]);
             }
             cp_async_wait0();
         }
