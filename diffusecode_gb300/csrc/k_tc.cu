@@ -45,9 +45,10 @@
 // waits are bounded (globaltimer); a wait that gives up sets an error flag,
 // the CTA stops issuing, waits for its own MMAs, frees TMEM and returns.
 //
-// Shared-memory operands use the canonical K-major layout without swizzle:
-// 8x8 16-bit core matrices of 128 contiguous bytes, LBO = 128 B between
-// K-adjacent core matrices, SBO = (KA/8)*128 B between 8-row groups.
+// Shared-memory operands use the canonical K-major layout with the 64-byte
+// swizzle: a row holds the 32 atoms of a stage (64 B), 8-row groups of 512 B
+// are SBO = 512 B apart, and the 16-byte chunk c of row r is stored at
+// chunk c ^ ((r & 7) >> 1).
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -155,13 +156,22 @@ __device__ __forceinline__ void producers_sync() { asm volatile("bar.sync 1, %0;
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
+// K-major operand with the 64-byte swizzle: row r of an 8-row group at
+// (r&7)*64 B, its 16-byte chunk c stored at chunk c ^ ((r&7)>>1); 8-row groups
+// SBO = 512 B apart (each group 512-byte aligned).
+__device__ __forceinline__ uint32_t sw_off(int r, int chunk)
+{
+    return (uint32_t)((r >> 3) * TC_SBO + (r & 7) * 64 + ((chunk ^ ((r & 7) >> 1)) << 4));
+}
+
 __device__ __forceinline__ uint64_t sdesc(uint32_t saddr)
 {
     uint64_t d = 0;
     d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
-    d |= (uint64_t)((TC_LBO >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)1 << 16;                      // leading byte offset: unused for swizzled K-major
     d |= (uint64_t)((TC_SBO >> 4) & 0x3FFFu) << 32;
-    d |= (uint64_t)1 << 46;          // descriptor version of the sm_100 family; no swizzle
+    d |= (uint64_t)1 << 46;                      // descriptor version of the sm_100 family
+    d |= (uint64_t)4 << 61;                      // 64-byte swizzle
     return d;
 }
 
@@ -286,11 +296,80 @@ __device__ __forceinline__ void stage_atoms(const TcSrc &P, uint8_t *dst, int64_
     cp_async_commit();
 }
 
+// Split 4 complex values (4 atoms of one row or column) into the hi and lo
+// operand words of the real and imaginary parts.
+template <bool BF>
+__device__ __forceinline__ void split_c4(const float2 (&x)[4], uint2 &rh, uint2 &rl, uint2 &ih, uint2 &il)
+{
+    split4<BF>(x[0].x, x[1].x, x[2].x, x[3].x, rh, rl);
+    split4<BF>(x[0].y, x[1].y, x[2].y, x[3].y, ih, il);
+}
+
+// U row group q: Ur hi/lo and Ui hi/lo at the thread's row and atom quad
+template <bool BF>
+__device__ __forceinline__ void emit_rows(uint8_t *dst, int q, const float2 (&x)[4])
+{
+    uint2 rh, rl, ih, il;
+    split_c4<BF>(x, rh, rl, ih, il);
+    uint8_t *d = dst + q * TC_SBO;
+    *reinterpret_cast<uint2 *>(d + 0 * TC_A_BYTES) = rh;
+    *reinterpret_cast<uint2 *>(d + 1 * TC_A_BYTES) = rl;
+    *reinterpret_cast<uint2 *>(d + 2 * TC_A_BYTES) = ih;
+    *reinterpret_cast<uint2 *>(d + 3 * TC_A_BYTES) = il;
+}
+
+// V column group q: rows c (Vr), N+c (Vi) and 2N+c (-Vr) of the hi and lo operands
+template <bool BF>
+__device__ __forceinline__ void emit_cols(uint8_t *Bh, uint32_t b_bytes, uint32_t blk, uint32_t o0, int q,
+                                          const float2 (&x)[4])
+{
+    uint2 rh, rl, ih, il;
+    split_c4<BF>(x, rh, rl, ih, il);
+    uint8_t *d = Bh + q * TC_SBO + o0;
+    const uint2 nrh = make_uint2(rh.x ^ 0x80008000u, rh.y ^ 0x80008000u);
+    const uint2 nrl = make_uint2(rl.x ^ 0x80008000u, rl.y ^ 0x80008000u);
+    *reinterpret_cast<uint2 *>(d) = rh;
+    *reinterpret_cast<uint2 *>(d + b_bytes) = rl;
+    *reinterpret_cast<uint2 *>(d + blk) = ih;
+    *reinterpret_cast<uint2 *>(d + blk + b_bytes) = il;
+    *reinterpret_cast<uint2 *>(d + 2 * blk) = nrh;
+    *reinterpret_cast<uint2 *>(d + 2 * blk + b_bytes) = nrl;
+}
+
+// Groups [q, qe) from the value x at group q: two interleaved chains
+// (even groups and odd groups, each stepping by m^2) give the recurrence
+// twice the instruction-level parallelism; the next pair is formed before the
+// current pair is split and stored.
+template <class Emit>
+__device__ __forceinline__ void run_pairs(int q, int qe, float2 (&x0)[4], const float2 (&m)[4],
+                                          const float2 (&m2)[4], Emit emit)
+{
+    float2 x1[4];
+#pragma unroll
+    for (int a = 0; a < 4; a++) x1[a] = cmulf(x0[a], m[a]);
+#pragma unroll 1
+    for (; q < qe; q += 2) {
+        float2 y0[4], y1[4];
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            y0[a] = cmulf(x0[a], m2[a]);
+            y1[a] = cmulf(x1[a], m2[a]);
+        }
+        emit(q, x0);
+        if (q + 1 < qe) emit(q + 1, x1);
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            x0[a] = y0[a];
+            x1[a] = y1[a];
+        }
+    }
+}
+
 // U rows of one stage for row groups [q0, q1) of the tile (8 rows each).
-// The thread owns atoms k0..k0+3 and row s of every group: it seeds at the
-// first group from the exact phase and steps by exp(2 pi i 8 d_ra) from group
-// to group, restarting from the exact phase where nb changes (gpn groups per
-// nb).  A warp's stores of one step cover 16 distinct 8-byte bank slots.
+// The thread owns atoms k0..k0+3 and row s of every group.  Within each
+// segment of constant nb it starts from the exact phase and steps by
+// exp(2 pi i 8 d_ra) from group to group.  A warp's stores of one step cover
+// 16 distinct 8-byte bank slots.
 template <bool BF>
 __device__ __forceinline__ void gen_rows(int q0, int q1, int mt, int gpn, const uint8_t *as, uint8_t *A, int s,
                                          int j)
@@ -303,8 +382,18 @@ __device__ __forceinline__ void gen_rows(int q0, int q1, int mt, int gpn, const 
     int gi = G0 % gpn;
     uint32_t nb = (uint32_t)(G0 / gpn);
     const int k0 = 4 * j;
-    float2 x[4], m[4];
-    auto seed = [&](uint32_t na) {
+    float2 m[4], m2[4];
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        m[a] = s_ma[k0 + a];
+        m2[a] = cmulf(m[a], m[a]);
+    }
+    uint8_t *dst = A + sw_off(s, j >> 1) + (j & 1) * 8;
+    auto emit = [&](int q, const float2 (&x)[4]) { emit_rows<BF>(dst, q, x); };
+    for (int q = q0; q < q1;) {            // segments of constant nb (warp-uniform)
+        const int qe = min(q1, q + (gpn - gi));
+        const uint32_t na = (uint32_t)(gi * 8 + s);
+        float2 x[4];
 #pragma unroll
         for (int a = 0; a < 4; a++) {
             const int k = k0 + a;
@@ -312,31 +401,10 @@ __device__ __forceinline__ void gen_rows(int q0, int q1, int mt, int gpn, const 
             const float wk = s_w[k];
             x[a] = make_float2(p.x * wk, p.y * wk);
         }
-    };
-#pragma unroll
-    for (int a = 0; a < 4; a++) m[a] = s_ma[k0 + a];
-    seed((uint32_t)(gi * 8 + s));
-    uint8_t *dst = A + (j >> 1) * TC_LBO + s * 16 + (j & 1) * 8;
-#pragma unroll 1
-    for (int q = q0; q < q1; q++) {
-        if (q > q0) {
-            if (++gi == gpn) {          // next nb: restart from the exact phase (warp-uniform)
-                gi = 0;
-                nb++;
-                seed((uint32_t)s);
-            } else {
-#pragma unroll
-                for (int a = 0; a < 4; a++) x[a] = cmulf(x[a], m[a]);
-            }
-        }
-        uint2 rh, rl, ih, il;
-        split4<BF>(x[0].x, x[1].x, x[2].x, x[3].x, rh, rl);
-        split4<BF>(x[0].y, x[1].y, x[2].y, x[3].y, ih, il);
-        uint8_t *d = dst + q * TC_SBO;
-        *reinterpret_cast<uint2 *>(d + 0 * TC_A_BYTES) = rh;    // Ur hi
-        *reinterpret_cast<uint2 *>(d + 1 * TC_A_BYTES) = rl;    // Ur lo
-        *reinterpret_cast<uint2 *>(d + 2 * TC_A_BYTES) = ih;    // Ui hi
-        *reinterpret_cast<uint2 *>(d + 3 * TC_A_BYTES) = il;    // Ui lo
+        run_pairs(q, qe, x, m, m2, emit);
+        q = qe;
+        gi = 0;
+        nb++;
     }
 }
 
@@ -351,35 +419,18 @@ __device__ __forceinline__ void gen_cols(int q0, int q1, int nt, int N, const ui
     const float2 *s_mc = reinterpret_cast<const float2 *>(as + TC_SLOT_MC);
     const int k0 = 4 * j;
     const uint32_t nc = (uint32_t)(nt * N + q0 * 8 + s);
-    float2 x[4], m[4];
+    float2 x[4], m[4], m2[4];
 #pragma unroll
     for (int a = 0; a < 4; a++) {
         const float2 p = phasor_fast((uint64_t)nc * s_dac[k0 + a]);
         x[a] = make_float2(p.x * TC_V_SCALE, p.y * TC_V_SCALE);
         m[a] = s_mc[k0 + a];
+        m2[a] = cmulf(m[a], m[a]);
     }
-    uint8_t *Bl = Bh + b_bytes;
     const uint32_t blk = (uint32_t)(N >> 3) * TC_SBO;           // N rows further
-    const uint32_t o0 = (j >> 1) * TC_LBO + s * 16 + (j & 1) * 8;
-#pragma unroll 1
-    for (int q = q0; q < q1; q++) {
-        if (q > q0) {
-#pragma unroll
-            for (int a = 0; a < 4; a++) x[a] = cmulf(x[a], m[a]);
-        }
-        uint2 rh, rl, ih, il;
-        split4<BF>(x[0].x, x[1].x, x[2].x, x[3].x, rh, rl);
-        split4<BF>(x[0].y, x[1].y, x[2].y, x[3].y, ih, il);
-        const uint32_t o = q * TC_SBO + o0;
-        const uint2 nrh = make_uint2(rh.x ^ 0x80008000u, rh.y ^ 0x80008000u);
-        const uint2 nrl = make_uint2(rl.x ^ 0x80008000u, rl.y ^ 0x80008000u);
-        *reinterpret_cast<uint2 *>(Bh + o) = rh;
-        *reinterpret_cast<uint2 *>(Bl + o) = rl;
-        *reinterpret_cast<uint2 *>(Bh + o + blk) = ih;
-        *reinterpret_cast<uint2 *>(Bl + o + blk) = il;
-        *reinterpret_cast<uint2 *>(Bh + o + 2 * blk) = nrh;
-        *reinterpret_cast<uint2 *>(Bl + o + 2 * blk) = nrl;
-    }
+    const uint32_t o0 = sw_off(s, j >> 1) + (j & 1) * 8;
+    auto emit = [&](int q, const float2 (&v)[4]) { emit_cols<BF>(Bh, b_bytes, blk, o0, q, v); };
+    run_pairs(q0, q1, x, m, m2, emit);
 }
 
 template <bool BF>
@@ -404,7 +455,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
         for (int s = 0; s < S; s++) {
-            mbar_init(&full[s], TC_PROD_THREADS);
+            mbar_init(&full[s], TC_PROD_WARPS);
             mbar_init(&empty[s], 1);
         }
         for (int b = 0; b < 2; b++) {
@@ -454,25 +505,30 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
             const int r0 = u * per, r1 = min(ntot, r0 + per);
             const int ra0 = min(r0, ngr), ra1 = min(r1, ngr);           // row groups
             const int rc0 = max(r0, ngr) - ngr, rc1 = max(r1, ngr) - ngr; // column groups
+            // groups st+1 and st+2 are in flight while group st is generated;
+            // the slot of group st+2 was last read for group st-1, before the
+            // barrier of step st
             producers_sync();               // previous item's slots are free
             stage_atoms(src, aslot, a0, tid);
+            if (nst > 1) stage_atoms(src, aslot + TC_ATOM_SLOT, a0 + TC_KA, tid);
+            else cp_async_commit();
             for (int st = 0; st < nst; st++, it++) {
                 const int sb = it % S;
-                if (st + 1 < nst) {
-                    stage_atoms(src, aslot + ((st + 1) % TC_NSLOT) * TC_ATOM_SLOT, a0 + (int64_t)(st + 1) * TC_KA,
+                cp_async_wait1();           // group st has landed (only the newest may be pending)
+                producers_sync();           // ... for every producer; slot of st-1 is free
+                if (st + 2 < nst)
+                    stage_atoms(src, aslot + ((st + 2) % TC_NSLOT) * TC_ATOM_SLOT, a0 + (int64_t)(st + 2) * TC_KA,
                                 tid);
-                    cp_async_wait1();
-                } else {
-                    cp_async_wait0();
-                }
-                producers_sync();           // group st staged for everybody
+                else
+                    cp_async_commit();
                 if (it >= (uint32_t)S && !mbar_wait(&empty[sb], ((it / S) - 1) & 1, err, 1)) { ok = false; break; }
                 const uint8_t *as = aslot + (st % TC_NSLOT) * TC_ATOM_SLOT;
                 uint8_t *A = smem + (size_t)sb * stage_bytes;
                 if (ra0 < ra1) gen_rows<BF>(ra0, ra1, mt, gpn, as, A, s, j);
                 if (rc0 < rc1) gen_cols<BF>(rc0, rc1, nt, N, as, A + 4 * TC_A_BYTES, b_bytes, s, j);
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                mbar_arrive(&full[sb]);
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&full[sb]);   // one arrival per producer warp
             }
             cp_async_wait0();
         }
@@ -514,7 +570,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
                         const uint32_t Bh = A + 4 * TC_A_BYTES, Bl = Bh + b_bytes;
 #pragma unroll
                         for (int kk = 0; kk < TC_KA / 16; kk++) {
-                            const uint32_t ko = kk * 2 * TC_LBO;
+                            const uint32_t ko = kk * 32;        // 16 atoms = 32 bytes of a row
                             const uint64_t arh = sdesc(A + 0 * TC_A_BYTES + ko), arl = sdesc(A + 1 * TC_A_BYTES + ko);
                             const uint64_t aih = sdesc(A + 2 * TC_A_BYTES + ko), ail = sdesc(A + 3 * TC_A_BYTES + ko);
                             const uint64_t b1h = sdesc(Bh + ko), b2h = sdesc(Bh + b2off + ko);
