@@ -72,6 +72,7 @@ struct dgpu_ctx {
     DevBuf istl, cfact, part, apart, lat, csf, acsf, dsi, stats, flag;
     DevBuf tc_part, tc_work, aidx;          // aidx: original atom index of each prepared slot
     DevBuf tc_mult;                         // per-atom step factors of the tensor-core engine
+    DevBuf tc_vimg;                         // V operand images of the tensor-core engine
     int64_t ts_main[2 * 64 + 4] = {};      // type ranges of the last main atom preparation
     DevBuf gq, gpart, grad, batch_desc, batch_aux;
     double batch_ms = 0.0;
@@ -165,6 +166,7 @@ struct TcProblem {
     const uint64_t *ph0, *dra, *drb, *dac;   // phase data along the row axes and the column axis
     const float *w;
     const float2 *ma, *mc;   // per-atom exp(2 pi i 8 d) along ra and ac
+    uint8_t *vimg;           // B rows of every (atom group, column tile), or null: generated in-kernel
     float2 *part;            // part[(t*nslice+ks)*slab + c*nrows_p + rg]
 };
 
@@ -175,6 +177,7 @@ struct TcLaunch {
     int64_t nitems;
     int32_t Nmax, stages, flush, nbuf, bf16;
     int32_t tsum;               // running sum of the main accumulator kept in TMEM
+    int32_t vring;              // V operand streamed from images through a shared-memory ring
     uint32_t tmem_cols;
     int32_t *err;
 };
@@ -199,9 +202,12 @@ struct TcPlan {
     size_t smem = 0;
     std::vector<int64_t> part_off;     // float2 offset of each problem's partials
     std::vector<int32_t> nslice;
+    bool vimg = false;                 // V images generated before the main kernel
 };
+// vimg: buffer for the V images of the launch (null, or too large for the
+// image budget: V is generated inside the kernel instead)
 int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *op, int N, int slice_mult,
-                 TcPlan &plan, DevBuf &part, DevBuf &desc);
+                 TcPlan &plan, DevBuf &part, DevBuf &desc, DevBuf *vimg);
 int dgpu_tc_launch(dgpu_ctx *ctx, const TcPlan &plan);          // enqueues the kernel only
 int dgpu_tc_check(dgpu_ctx *ctx);                               // waits, reads the error flag
 struct PartRef;

@@ -62,6 +62,7 @@ struct BatchState {
     DevBuf d_pos, d_isc, d_aocc, d_ph0, d_du, d_dv, d_dw, d_w, d_idx, d_cnt, d_offs, d_tsd;
     DevBuf d_istl, d_cfact, d_csf, d_dsi, d_g, d_q, d_chi, d_grad, d_coef, d_fs, d_it, d_wt, part, desc;
     DevBuf d_mult;                         // tensor-core step factors, 3 x tot_pad
+    DevBuf d_vimg;                         // tensor-core V images
     HostPinned h_pos, h_isc, h_aocc, h_it, h_wt, h_dsi, h_chi, h_grad;
     ~BatchState()
     {
@@ -72,6 +73,7 @@ struct BatchState {
                        &d_it, &d_wt, &part, &desc};
         for (DevBuf *x : b) x->release();
         d_mult.release();
+        d_vimg.release();
     }
 };
 
@@ -276,7 +278,7 @@ static int batch_build(dgpu_ctx *ctx, BatchState &B, int32_t nc, const dgpu_crys
         in[c].axis = -1;
     }
     const int N = op->tc_tile_n > 0 ? op->tc_tile_n : 64;
-    int rc = dgpu_tc_plan(ctx, nc, in.data(), op, N, 4, B.plan, B.part, B.desc);
+    int rc = dgpu_tc_plan(ctx, nc, in.data(), op, N, 4, B.plan, B.part, B.desc, &B.d_vimg);
     if (rc) return rc;
     DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return DGPU_OK;

@@ -72,6 +72,7 @@
 #define TC_SLOT_MC (TC_SLOT_MA + TC_KA * 8)
 #define TC_ATOM_SLOT (TC_SLOT_MC + TC_KA * 8)
 #define TC_NSLOT 3
+#define TC_VSLOTS 4                            // V ring: images prefetched two stages ahead
 #define TC_BAR_BYTES 256
 #define TC_SMEM_BUDGET (220 * 1024)
 #ifndef TC_FLUSH_STAGES
@@ -143,6 +144,35 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volati
     }
 }
 
+// arrive on a barrier and announce tx bytes that an async copy will complete
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
+                     smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+// one bulk global -> shared copy (16-byte aligned, size a multiple of 16)
+// completing `bytes` of transaction on bar
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// wait that ignores the error flag (time-bounded): used to let the CTA's own
+// bulk copies land before it exits after an error
+__device__ __forceinline__ void mbar_wait_quiet(uint64_t *bar, uint32_t parity)
+{
+    const uint64_t t0 = gtimer();
+    while (!mbar_try_suspend(bar, parity))
+        if (gtimer() - t0 > TC_TIMEOUT_NS) return;
+}
+
 __device__ __forceinline__ void cp_async16(void *dst, const void *src)
 {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
@@ -150,8 +180,20 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-// barrier among the producer warps only
-__device__ __forceinline__ void producers_sync() { asm volatile("bar.sync 1, %0;" ::"n"(TC_PROD_THREADS) : "memory"); }
+// barrier among the producer warps only; returns the OR of `stop` over them,
+// so that all producers leave their loops at the same barrier (a thread that
+// left alone would keep the others waiting at the next one)
+__device__ __forceinline__ bool producers_sync(bool stop)
+{
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.or.pred p, 1, %2, q;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)stop), "n"(TC_PROD_THREADS)
+        : "memory");
+    return r != 0;
+}
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -440,16 +482,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
     const int S = L.stages;
     const int NM = L.Nmax;
     const uint32_t b_bytes = (uint32_t)3 * NM * TC_KA * 2;      // one B operand: 3N rows
-    const uint32_t stage_bytes = 4 * TC_A_BYTES + 2 * b_bytes;
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem + (size_t)S * stage_bytes);
+    // stages hold U (and V when it is generated in-kernel); with V images,
+    // V lives in a ring of TC_VSLOTS slots of 2 * b_bytes after the stages
+    const uint32_t stage_bytes = 4 * TC_A_BYTES + (L.vring ? 0u : 2 * b_bytes);
+    const uint32_t vbytes = 2 * b_bytes;
+    uint8_t *vring = smem + (size_t)S * stage_bytes;
+    uint64_t *full = reinterpret_cast<uint64_t *>(vring + (L.vring ? (size_t)TC_VSLOTS * vbytes : 0));
     uint64_t *empty = full + S;
     uint64_t *mfull = empty + S;      // [2] main accumulator b ready
     uint64_t *mempty = mfull + 2;     // [2] main accumulator b drained
     uint64_t *cfull = mempty + 2;     // correction accumulator ready (end of item)
     uint64_t *cempty = cfull + 1;     // correction accumulator drained
     uint64_t *drain = cempty + 1;
-    uint32_t *tbase = reinterpret_cast<uint32_t *>(drain + 1);
-    uint8_t *aslot = smem + (size_t)S * stage_bytes + TC_BAR_BYTES;   // TC_NSLOT x TC_ATOM_SLOT
+    uint64_t *vfull = drain + 1;      // [TC_VSLOTS] V image of the slot landed
+    uint64_t *vempty = vfull + TC_VSLOTS;   // [TC_VSLOTS] MMAs reading the slot done
+    uint32_t *tbase = reinterpret_cast<uint32_t *>(vempty + TC_VSLOTS);
+    uint8_t *aslot = reinterpret_cast<uint8_t *>(full) + TC_BAR_BYTES;   // TC_NSLOT x TC_ATOM_SLOT
     volatile int32_t *err = L.err;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -465,6 +513,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
         mbar_init(cfull, 1);
         mbar_init(cempty, 4 * 32);
         mbar_init(drain, 1);
+        for (int v = 0; v < TC_VSLOTS; v++) {
+            mbar_init(&vfull[v], 1);
+            mbar_init(&vempty[v], 1);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == TC_MMA_WARP) {
@@ -489,9 +541,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
         // (s = lane&7, j = atom quad, u) takes range u for its atom quad.
         const int tid = threadIdx.x;
         const int s = lane & 7, j = (lane >> 3) + 4 * (warp & 1), u = warp >> 1;
+        uint32_t vnext = 0, vwait = 0;      // thread 0: next stage to copy V for / first not known landed
         uint32_t it = 0;
-        bool ok = true;
-        for (int64_t item = blockIdx.x; item < L.nitems && ok; item += gridDim.x) {
+        bool ok = true;                     // this thread saw no failed wait
+        for (int64_t item = blockIdx.x; item < L.nitems; item += gridDim.x) {
             const TcProblem &g = L.probs[L.item_prob[item]];
             int t, ks, nt, mt;
             decode_item(g, item - g.item0, t, ks, nt, mt);
@@ -499,39 +552,65 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
             const int64_t a1 = min(g.ts[t + 1], a0 + g.slice_len);
             const int nst = a1 > a0 ? (int)((a1 - a0) / TC_KA) : 0;
             if (nst == 0) continue;
+            // previous item's slots are free; everybody stops together after a failure
+            if (producers_sync(!ok)) break;
             const TcSrc src = {g.ph0, g.dra, g.drb, g.dac, g.w, g.ma, g.mc};
             const int N = g.N, gpn = g.fra_p >> 3;
-            const int ngr = TC_M / 8, ntot = ngr + (N >> 3), per = (ntot + 3) >> 2;
+            // with V images the column groups arrive by bulk copy into the ring
+            const uint8_t *vimg = L.vring ? g.vimg : nullptr;
+            const int64_t g0 = a0 / TC_KA;
+            const int ntl = g.n_tiles;
+            const int ngr = TC_M / 8, ntot = ngr + (vimg ? 0 : (N >> 3)), per = (ntot + 3) >> 2;
+            // thread 0: V copy of item stage y (global stage x) once its slot is free
+            auto issue_v = [&](uint32_t x, int y) -> bool {
+                const int v = (int)(x % TC_VSLOTS);
+                if (x >= TC_VSLOTS) {
+                    if (!mbar_wait(&vempty[v], ((x / TC_VSLOTS) - 1) & 1, err, 9)) return false;
+                    vwait = x - TC_VSLOTS + 1;          // the MMAs consumed that copy: it landed
+                }
+                mbar_arrive_tx(&vfull[v], vbytes);
+                bulk_g2s(vring + (size_t)v * vbytes, vimg + ((g0 + y) * ntl + nt) * (int64_t)vbytes, vbytes,
+                         &vfull[v]);
+                vnext = x + 1;
+                return true;
+            };
+            if (vimg && tid == 0)
+                for (int y = 0; y < 2 && y < nst && ok; y++) ok = issue_v(it + y, y);
             const int r0 = u * per, r1 = min(ntot, r0 + per);
             const int ra0 = min(r0, ngr), ra1 = min(r1, ngr);           // row groups
             const int rc0 = max(r0, ngr) - ngr, rc1 = max(r1, ngr) - ngr; // column groups
             // groups st+1 and st+2 are in flight while group st is generated;
             // the slot of group st+2 was last read for group st-1, before the
             // barrier of step st
-            producers_sync();               // previous item's slots are free
             stage_atoms(src, aslot, a0, tid);
             if (nst > 1) stage_atoms(src, aslot + TC_ATOM_SLOT, a0 + TC_KA, tid);
             else cp_async_commit();
             for (int st = 0; st < nst; st++, it++) {
                 const int sb = it % S;
                 cp_async_wait1();           // group st has landed (only the newest may be pending)
-                producers_sync();           // ... for every producer; slot of st-1 is free
+                // one thread waits for the stage buffer, the barrier tells everybody
+                if (tid == 0 && ok && it >= (uint32_t)S) ok = mbar_wait(&empty[sb], ((it / S) - 1) & 1, err, 1);
+                if (producers_sync(!ok)) break;   // staged for every producer; slot of st-1 and stage sb free
                 if (st + 2 < nst)
                     stage_atoms(src, aslot + ((st + 2) % TC_NSLOT) * TC_ATOM_SLOT, a0 + (int64_t)(st + 2) * TC_KA,
                                 tid);
                 else
                     cp_async_commit();
-                if (it >= (uint32_t)S && !mbar_wait(&empty[sb], ((it / S) - 1) & 1, err, 1)) { ok = false; break; }
                 const uint8_t *as = aslot + (st % TC_NSLOT) * TC_ATOM_SLOT;
                 uint8_t *A = smem + (size_t)sb * stage_bytes;
-                if (ra0 < ra1) gen_rows<BF>(ra0, ra1, mt, gpn, as, A, s, j);
-                if (rc0 < rc1) gen_cols<BF>(rc0, rc1, nt, N, as, A + 4 * TC_A_BYTES, b_bytes, s, j);
+                if (ok && vimg && tid == 0 && st + 2 < nst) ok = issue_v(it + 2, st + 2);
+                if (ok && ra0 < ra1) gen_rows<BF>(ra0, ra1, mt, gpn, as, A, s, j);
+                if (ok && rc0 < rc1) gen_cols<BF>(rc0, rc1, nt, N, as, A + 4 * TC_A_BYTES, b_bytes, s, j);
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&full[sb]);   // one arrival per producer warp
             }
             cp_async_wait0();
         }
+        // let this thread's bulk copies land before the CTA can exit (after an
+        // error the MMA side may not have waited for them)
+        if (tid == 0)
+            for (uint32_t x = vwait; x < vnext; x++) mbar_wait_quiet(&vfull[x % TC_VSLOTS], (x / TC_VSLOTS) & 1);
     } else if (warp == TC_MMA_WARP) {
         // ------------------------------------------------------------ MMA issuer
         const uint32_t fmt = BF ? 1u : 0u;
@@ -553,21 +632,39 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
             const uint32_t idesc_neg = idesc | (1u << 13);     // negate A: the -Ui products
             const uint32_t b2off = (uint32_t)(N >> 3) * TC_SBO; // B rows N.. : [Vi; -Vr]
             // the correction accumulator restarts with this item: previous one drained?
-            if (nitem > 0 && !mbar_wait(cempty, (nitem - 1) & 1, err, 2)) { ok = false; break; }
+            if (nitem > 0 &&
+                !__shfl_sync(0xffffffffu, lane == 0 ? mbar_wait(cempty, (nitem - 1) & 1, err, 2) : true, 0)) {
+                ok = false;
+                break;
+            }
             for (int st0 = 0; st0 < nst && ok; st0 += L.flush, nchunk++) {
                 const int b = (int)(nchunk % L.nbuf);
                 const uint32_t use = nchunk / L.nbuf;
-                if (use > 0 && !mbar_wait(&mempty[b], (use - 1) & 1, err, 6)) { ok = false; break; }
+                if (use > 0 &&
+                    !__shfl_sync(0xffffffffu, lane == 0 ? mbar_wait(&mempty[b], (use - 1) & 1, err, 6) : true, 0)) {
+                    ok = false;
+                    break;
+                }
                 tc_fence_after();
                 const uint32_t m_acc = tmem + 2u * NM * (1u + (uint32_t)b);
                 const int st1 = min(nst, st0 + L.flush);
                 for (int st = st0; st < st1; st++, it++) {
                     const int s = it % S;
-                    if (!mbar_wait(&full[s], (it / S) & 1, err, 3)) { ok = false; break; }
+                    bool got = true;
+                    if (lane == 0) {
+                        got = mbar_wait(&full[s], (it / S) & 1, err, 3);
+                        if (got && L.vring) got = mbar_wait(&vfull[it % TC_VSLOTS], (it / TC_VSLOTS) & 1, err, 8);
+                    }
+                    if (!__shfl_sync(0xffffffffu, got, 0)) {
+                        ok = false;
+                        break;
+                    }
                     tc_fence_after();
                     if (lane == 0) {
                         const uint32_t A = smem_u32(smem + (size_t)s * stage_bytes);
-                        const uint32_t Bh = A + 4 * TC_A_BYTES, Bl = Bh + b_bytes;
+                        const uint32_t Bh =
+                            L.vring ? smem_u32(vring) + (it % TC_VSLOTS) * vbytes : A + 4 * TC_A_BYTES;
+                        const uint32_t Bl = Bh + b_bytes;
 #pragma unroll
                         for (int kk = 0; kk < TC_KA / 16; kk++) {
                             const uint32_t ko = kk * 32;        // 16 atoms = 32 bytes of a row
@@ -587,6 +684,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
                             mma_f16(c_acc, ail, b2h, idesc_neg, 1u);
                         }
                         mma_commit(&empty[s]);
+                        if (L.vring) mma_commit(&vempty[it % TC_VSLOTS]);
                         issued = true;
                     }
                     __syncwarp();
@@ -603,7 +701,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
         // make sure no MMA of this CTA is still running before TMEM is freed
         if (lane == 0 && issued) mma_commit(drain);
         __syncwarp();
-        if (__shfl_sync(0xffffffffu, issued ? 1 : 0, 0)) mbar_wait(drain, 0, err, 4);
+        if (__shfl_sync(0xffffffffu, issued ? 1 : 0, 0)) mbar_wait_quiet(drain, 0);
         tc_fence_before();
     } else {
         // ------------------------------------------------------------ epilogue
@@ -634,11 +732,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
             }
             for (int st0 = 0; st0 < nst; st0 += L.flush, nchunk++) {
                 const int b = (int)(nchunk % L.nbuf);
-                if (!mbar_wait(&mfull[b], (nchunk / L.nbuf) & 1, err, 5)) { ok = false; break; }
+                if (!__shfl_sync(0xffffffffu, lane == 0 ? mbar_wait(&mfull[b], (nchunk / L.nbuf) & 1, err, 5) : true,
+                                 0)) {
+                    ok = false;
+                    break;
+                }
                 tc_fence_after();
                 const bool first = st0 == 0, last = st0 + L.flush >= nst;
                 if (last) {                                        // the item's corrections
-                    if (!mbar_wait(cfull, nitem & 1, err, 7)) { ok = false; break; }
+                    if (!__shfl_sync(0xffffffffu, lane == 0 ? mbar_wait(cfull, nitem & 1, err, 7) : true, 0)) {
+                        ok = false;
+                        break;
+                    }
                     tc_fence_after();
                 }
                 const uint32_t t_main = tmem + lane_off + 2u * NM * (1u + (uint32_t)b);
@@ -733,6 +838,41 @@ __global__ void k_tc_mult(const uint64_t *__restrict__ du, const uint64_t *__res
         float s, c;
         sincospif(xf, &s, &c);
         out[a * stride + i] = make_float2(fmaf(-s, dth, c), fmaf(c, dth, s));
+    }
+}
+
+// V images of one problem: for every 32-atom group gi and column tile nt the
+// B rows [Vr; Vi; -Vr] of a stage, hi then lo, exactly as the producers lay
+// them out in shared memory (384 N bytes).  Each value is evaluated from its
+// exact 64-bit phase; grid: one block per (gi, nt).
+template <bool BF>
+__global__ void __launch_bounds__(256) k_tc_vgen(const uint64_t *__restrict__ dac, int N, int n_tiles,
+                                                  uint8_t *__restrict__ vimg)
+{
+    const int64_t gi = blockIdx.x / n_tiles;
+    const int nt = (int)(blockIdx.x % n_tiles);
+    const uint32_t vbytes = (uint32_t)N * 384u;
+    uint8_t *img = vimg + (int64_t)blockIdx.x * vbytes;
+    const uint32_t half = vbytes / 2, blk = (uint32_t)(N >> 3) * TC_SBO;
+    for (int u = threadIdx.x; u < N * 8; u += blockDim.x) {
+        const int c = u % N, jq = u / N;                       // column, atom quad
+        const uint32_t nc = (uint32_t)(nt * N + c);
+        float2 x[4];
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            const float2 p = phasor_fast((uint64_t)nc * dac[gi * TC_KA + 4 * jq + a]);
+            x[a] = make_float2(p.x * TC_V_SCALE, p.y * TC_V_SCALE);
+        }
+        uint2 rh, rl, ih, il;
+        split4<BF>(x[0].x, x[1].x, x[2].x, x[3].x, rh, rl);
+        split4<BF>(x[0].y, x[1].y, x[2].y, x[3].y, ih, il);
+        uint8_t *d = img + sw_off(c, jq >> 1) + (jq & 1) * 8;
+        *reinterpret_cast<uint2 *>(d) = rh;
+        *reinterpret_cast<uint2 *>(d + half) = rl;
+        *reinterpret_cast<uint2 *>(d + blk) = ih;
+        *reinterpret_cast<uint2 *>(d + blk + half) = il;
+        *reinterpret_cast<uint2 *>(d + 2 * blk) = make_uint2(rh.x ^ 0x80008000u, rh.y ^ 0x80008000u);
+        *reinterpret_cast<uint2 *>(d + 2 * blk + half) = make_uint2(rl.x ^ 0x80008000u, rl.y ^ 0x80008000u);
     }
 }
 
@@ -834,8 +974,10 @@ void dgpu_tc_partref(const TcProblem &g, const float2 *p, PartRef &ref)
     ref.slab = g.slab;
 }
 
+#define TC_VIMG_BUDGET ((int64_t)1 << 30)     // bytes of V images per launch
+
 int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *op, int N, int slice_mult,
-                 TcPlan &plan, DevBuf &part, DevBuf &desc)
+                 TcPlan &plan, DevBuf &part, DevBuf &desc, DevBuf *vimg)
 {
     plan.probs.assign(nprob, TcProblem());
     plan.part_off.assign(nprob, 0);
@@ -864,6 +1006,18 @@ int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *o
         for (int64_t i = 0; i < plan.probs[p].nitems; i++) plan.item_prob[plan.probs[p].item0 + i] = p;
     DGPU_CUDA(ctx, part.ensure((size_t)(elems > 0 ? elems : 1) * sizeof(float2)));
     for (int p = 0; p < nprob; p++) plan.probs[p].part = part.as<float2>() + plan.part_off[p];
+    // V images: one per (32-atom group, column tile) of every problem
+    std::vector<int64_t> voff(nprob, 0);
+    int64_t vtot = 0;
+    for (int p = 0; p < nprob; p++) {
+        voff[p] = vtot;
+        vtot += in[p].ts[in[p].ntype] / TC_KA * plan.probs[p].n_tiles * (int64_t)N * 384;
+    }
+    plan.vimg = vimg && vtot > 0 && vtot <= TC_VIMG_BUDGET;
+    if (plan.vimg) {
+        DGPU_CUDA(ctx, vimg->ensure((size_t)vtot));
+        for (int p = 0; p < nprob; p++) plan.probs[p].vimg = vimg->as<uint8_t>() + voff[p];
+    }
     const size_t pbytes = ((size_t)nprob * sizeof(TcProblem) + 255) & ~(size_t)255;
     DGPU_CUDA(ctx, desc.ensure(pbytes + (size_t)items * sizeof(int32_t) + 256));
     DGPU_CUDA(ctx, cudaMemcpyAsync(desc.p, plan.probs.data(), (size_t)nprob * sizeof(TcProblem),
@@ -882,13 +1036,21 @@ int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *o
     L.tsum = 2 * N * (2 + L.nbuf) <= 512 ? 1 : 0;
     L.flush = op->tc_flush > 0 ? (int32_t)dgpu_cdiv(op->tc_flush, TC_KA) : TC_FLUSH_STAGES;
     L.bf16 = op->split == DGPU_SPLIT_BF16;
-    const uint32_t stage_bytes = 4 * TC_A_BYTES + 2u * 3u * N * TC_KA * 2;
+    const uint32_t vbytes = 2u * 3u * N * TC_KA * 2;
     const uint32_t bar_bytes = TC_BAR_BYTES + TC_NSLOT * TC_ATOM_SLOT;
-    const int stages = (int)((TC_SMEM_BUDGET - bar_bytes) / stage_bytes);
+    // V images stream through a ring when it leaves room for two U stages
+    const int64_t room = (int64_t)TC_SMEM_BUDGET - bar_bytes - (int64_t)TC_VSLOTS * vbytes;
+    if (plan.vimg && room < 2 * 4 * TC_A_BYTES) plan.vimg = false;
+    if (!plan.vimg)
+        for (TcProblem &g : plan.probs) g.vimg = nullptr;
+    L.vring = plan.vimg ? 1 : 0;
+    const uint32_t stage_bytes = 4 * TC_A_BYTES + (L.vring ? 0u : vbytes);
+    const int stages = (int)(((int64_t)TC_SMEM_BUDGET - bar_bytes - (L.vring ? (int64_t)TC_VSLOTS * vbytes : 0)) /
+                             stage_bytes);
     L.stages = stages > 4 ? 4 : stages;
     L.tmem_cols = pow2_cols(2 * N * (1 + L.nbuf + L.tsum));
     if (L.stages < 2 || L.tmem_cols > 512) return dgpu_set_error(ctx, DGPU_ERR_ARG, "tile does not fit");
-    plan.smem = (size_t)L.stages * stage_bytes + bar_bytes;
+    plan.smem = (size_t)L.stages * stage_bytes + (L.vring ? (size_t)TC_VSLOTS * vbytes : 0) + bar_bytes;
     static bool attr_set = false;     // set once, outside any stream capture
     if (!attr_set) {
         DGPU_CUDA(ctx, cudaFuncSetAttribute(k_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
@@ -904,6 +1066,15 @@ int dgpu_tc_launch(dgpu_ctx *ctx, const TcPlan &plan)
 {
     DGPU_CUDA(ctx, cudaMemsetAsync(plan.L.err, 0, sizeof(int32_t), ctx->stream));
     if (plan.L.nitems < 1) return DGPU_OK;
+    if (plan.vimg)
+        for (const TcProblem &g : plan.probs) {
+            const int64_t nimg = (g.ts[g.ntype] / TC_KA) * g.n_tiles;
+            if (nimg < 1) continue;
+            if (plan.L.bf16)
+                k_tc_vgen<true><<<(unsigned)nimg, 256, 0, ctx->stream>>>(g.dac, g.N, g.n_tiles, g.vimg);
+            else
+                k_tc_vgen<false><<<(unsigned)nimg, 256, 0, ctx->stream>>>(g.dac, g.N, g.n_tiles, g.vimg);
+        }
     const int grid = (int)(plan.L.nitems < ctx->nsm ? plan.L.nitems : ctx->nsm);
     if (plan.L.bf16)
         k_tc<true><<<grid, TC_THREADS, plan.smem, ctx->stream>>>(plan.L);
@@ -1006,7 +1177,9 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
         for (int c = 0; c < nc && nc > 1; c++) {
             in.axis = cand[c].axis;
             TcPlan plan;
-            if (dgpu_tc_plan(ctx, 1, &in, op, cand[c].N, cand[c].slice_mult, plan, part, ctx->tc_part)) continue;
+            if (dgpu_tc_plan(ctx, 1, &in, op, cand[c].N, cand[c].slice_mult, plan, part, ctx->tc_part,
+                             &ctx->tc_vimg))
+                continue;
             DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[4], ctx->stream));
             rc = dgpu_tc_launch(ctx, plan);
             if (rc) return rc;
@@ -1024,7 +1197,7 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
     }
     in.axis = choice.axis;
     TcPlan plan;
-    rc = dgpu_tc_plan(ctx, 1, &in, op, choice.N, choice.slice_mult, plan, part, ctx->tc_part);
+    rc = dgpu_tc_plan(ctx, 1, &in, op, choice.N, choice.slice_mult, plan, part, ctx->tc_part, &ctx->tc_vimg);
     if (rc) return rc;
     rc = dgpu_tc_launch(ctx, plan);
     if (rc) return rc;
