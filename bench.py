@@ -216,7 +216,7 @@ def adjoint_measure(ctx, engine, steps=3):
     f, b = min(fwd), min(bwd)
     return {"workload": "rocksalt-100000-atoms-65^3", "fwd_kernel_ms": f, "adjoint_ms": b,
             "bwd_over_fwd": b / f, "chi2": c2,
-            "note": "adjoint = per-point weights + per-atom sums (CUDA cores); fwd = type sums of the same engine"}
+            "note": "adjoint = per-point weights + per-atom sums (tensor cores for the TC engine); fwd = type sums of the same engine"}
 
 
 def batch_measure(ctx, steps=3):

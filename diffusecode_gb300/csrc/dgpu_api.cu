@@ -72,7 +72,7 @@ extern "C" int dgpu_ctx_destroy(dgpu_ctx *c)
     DevBuf *bufs[] = {&c->pos, &c->iscat, &c->aocc, &c->sel, &c->counts, &c->type_start, &c->ph0, &c->du,
                       &c->dv, &c->dw, &c->w, &c->aph0, &c->adu, &c->adv, &c->adw, &c->aw, &c->istl,
                       &c->cfact, &c->part, &c->apart, &c->lat, &c->csf, &c->acsf, &c->dsi, &c->stats,
-                      &c->flag, &c->tc_part, &c->tc_work, &c->tc_mult, &c->tc_vimg, &c->gq, &c->gpart, &c->grad, &c->batch_desc,
+                      &c->flag, &c->tc_part, &c->tc_work, &c->tc_mult, &c->tc_vimg, &c->adj_qimg, &c->adj_items, &c->gq, &c->gpart, &c->grad, &c->batch_desc,
                       &c->batch_aux};
     for (DevBuf *b : bufs) b->release();
     for (int i = 0; i < 6; i++)

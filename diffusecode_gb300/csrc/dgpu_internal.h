@@ -73,6 +73,7 @@ struct dgpu_ctx {
     DevBuf tc_part, tc_work, aidx;          // aidx: original atom index of each prepared slot
     DevBuf tc_mult;                         // per-atom step factors of the tensor-core engine
     DevBuf tc_vimg;                         // V operand images of the tensor-core engine
+    DevBuf adj_qimg, adj_items;             // tensor-core adjoint: Q images, work items
     int64_t ts_main[2 * 64 + 4] = {};      // type ranges of the last main atom preparation
     DevBuf gq, gpart, grad, batch_desc, batch_aux;
     double batch_ms = 0.0;
@@ -280,6 +281,12 @@ int dgpu_adjoint_async(dgpu_ctx *ctx, const FormSpec *d_fs, const BoxSpec &box, 
                        const int32_t *istl, const double2 *cfact, const double *it, const double *wt, double *g,
                        double *chi, float2 *Q, double *gpos, double *gocc);
 int dgpu_friedel_test(const dgpu_grid *g, const dgpu_opts *op, int32_t fnum[3]);
+// Tensor-core adjoint sums (k_adjtc.cu): adds the gradient of every prepared
+// atom of the ntype type ranges ts (host) to gpos / gocc (device, indexed by
+// aidx); Q: nscat * box points, FP32 complex, dense box order.
+int dgpu_adjtc_sums(dgpu_ctx *ctx, const BoxSpec &box, const dgpu_grid *grid, int32_t nscat, const int64_t *ts,
+                    const uint64_t *ph0, const uint64_t *du, const uint64_t *dv, const uint64_t *dw, const float *w,
+                    const int32_t *aidx, const float2 *Q, double *gpos, double *gocc);
 void dgpu_batch_free(dgpu_ctx *ctx);
 
 // the whole four_run with device-resident crystal arrays and outputs

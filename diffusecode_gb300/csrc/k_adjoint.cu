@@ -257,14 +257,22 @@ int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
     ag.pbox = nb;
     memcpy(ag.vi, grid->vi, sizeof(ag.vi));
     const int64_t *ts = ctx->ts_main;
-    for (int t = 0; t < cr->nscat; t++) {
-        const int64_t lo = ts[t], hi = ts[t + 1];
-        if (hi <= lo) continue;
-        k_adj_atoms<<<(unsigned)dgpu_cdiv(hi - lo, ADJ_NT), ADJ_NT, 0, ctx->stream>>>(
-            ctx->ph0.as<uint64_t>(), ctx->du.as<uint64_t>(), ctx->dv.as<uint64_t>(), ctx->dw.as<uint64_t>(),
-            ctx->w.as<float>(), ctx->aidx.as<int32_t>(), lo, hi, ctx->gpart.as<float2>() + (int64_t)t * nb, ag,
-            d_gpos, d_gocc);
-        DGPU_CUDA(ctx, cudaGetLastError());
+    if (fwd.engine_used == DGPU_ENGINE_TC) {
+        // same sums on the tensor cores, with the forward pass's engine
+        rc = dgpu_adjtc_sums(ctx, box, grid, cr->nscat, ts, ctx->ph0.as<uint64_t>(), ctx->du.as<uint64_t>(),
+                             ctx->dv.as<uint64_t>(), ctx->dw.as<uint64_t>(), ctx->w.as<float>(),
+                             ctx->aidx.as<int32_t>(), ctx->gpart.as<float2>(), d_gpos, d_gocc);
+        if (rc) return rc;
+    } else {
+        for (int t = 0; t < cr->nscat; t++) {
+            const int64_t lo = ts[t], hi = ts[t + 1];
+            if (hi <= lo) continue;
+            k_adj_atoms<<<(unsigned)dgpu_cdiv(hi - lo, ADJ_NT), ADJ_NT, 0, ctx->stream>>>(
+                ctx->ph0.as<uint64_t>(), ctx->du.as<uint64_t>(), ctx->dv.as<uint64_t>(), ctx->dw.as<uint64_t>(),
+                ctx->w.as<float>(), ctx->aidx.as<int32_t>(), lo, hi, ctx->gpart.as<float2>() + (int64_t)t * nb, ag,
+                d_gpos, d_gocc);
+            DGPU_CUDA(ctx, cudaGetLastError());
+        }
     }
     DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
     DGPU_CUDA(ctx, cudaMemcpyAsync(chi2, d_chi + nblk, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));

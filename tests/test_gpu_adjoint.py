@@ -32,6 +32,30 @@ def test_gradient_vs_oracle_fp64(oracle, ctx, engine):
     assert np.all(gp[cr.iscat == 0] == 0) and np.all(go[cr.iscat == 0] == 0)
 
 
+@pytest.mark.parametrize("inc", [(97, 5, 3), (9, 71, 69)], ids=["two-column-chunks", "many-rows"])
+def test_tc_adjoint_shapes(oracle, ctx, inc):
+    """Tensor-core adjoint on boxes with more than 64 columns on every axis
+    choice (two column chunks) and with many row tiles, three atom types,
+    against the oracle's FP64 gradient."""
+    from diffusecode_gb300.autograd import chi2_grad
+    cr, _ = S.small_random(seed=21, natoms=300, nscat=3, span=4.0)
+    st = [4.0 / (n - 1) for n in inc]              # about 4 reciprocal units along every axis
+    vi = np.array([[st[0], 0.2 * st[1], 0.1 * st[2]],
+                   [0.1 * st[0], st[1], -0.1 * st[2]],
+                   [0.05 * st[0], 0.1 * st[1], st[2]]])
+    eck = np.zeros((3, 4))
+    eck[:, 0] = -0.5 * (vi @ (np.asarray(inc) - 1)) + np.array([0.013, -0.021, 0.017])
+    g = S.GridData(eck=eck, vi=vi, inc=inc)
+    cr.atom_occ = np.linspace(0.8, 1.2, cr.natoms).astype(np.float32)
+    it, wt = _target(cr, g, ctx)
+    op = K.opts(phase=_abi.PHASE_EXACT64, engine=_abi.ENGINE_TC, friedel=0)
+    c2, gp, go, _ = chi2_grad(cr, g, op, it, wt, ctx=ctx)
+    oc2, ogp, ogo = oracle.chi2_grad(cr, g, op, it, wt)
+    assert abs(c2 - oc2) <= 1e-4 * oc2
+    assert np.max(np.abs(gp - ogp)) <= 2e-4 * np.abs(ogp).max()
+    assert np.max(np.abs(go - ogo)) <= 2e-4 * np.abs(ogo).max()
+
+
 def test_gradient_with_friedel_reduction(oracle, ctx):
     """Centred odd grid: the GPU sums over half the grid with mirror weights."""
     from diffusecode_gb300.autograd import chi2_grad
@@ -47,13 +71,14 @@ def test_gradient_with_friedel_reduction(oracle, ctx):
     assert np.max(np.abs(go - ogo)) <= 2e-4 * np.abs(ogo).max()
 
 
-def test_central_finite_differences(ctx):
+@pytest.mark.parametrize("engine", [_abi.ENGINE_DIRECT, _abi.ENGINE_TC])
+def test_central_finite_differences(ctx, engine):
     """d chi2 / d x by central differences with a 1e-4 A step on seeded atoms."""
     from diffusecode_gb300.autograd import chi2_grad
     a = 5.64
     cr, g = S.rocksalt_volume(cells=(3, 3, 3), inc=17, step=0.2)
     it, wt = _target(cr, g, ctx, a_lat=a)
-    op = K.opts(phase=_abi.PHASE_EXACT64, engine=_abi.ENGINE_DIRECT)
+    op = K.opts(phase=_abi.PHASE_EXACT64, engine=engine)
     c2, gp, go, _ = chi2_grad(cr, g, op, it, wt, ctx=ctx)
     rng = np.random.Generator(np.random.PCG64(12))
     h = 1e-4 / a
