@@ -279,8 +279,44 @@ int dgpu_adjoint_async(dgpu_ctx *ctx, const FormSpec *d_fs, const BoxSpec &box, 
                        const uint64_t *ph0, const uint64_t *du, const uint64_t *dv, const uint64_t *dw,
                        const float *w, const int32_t *aidx, const double2 *csf, const double *dsi,
                        const int32_t *istl, const double2 *cfact, const double *it, const double *wt, double *g,
-                       double *chi, float2 *Q, double *gpos, double *gocc);
+                       double *chi, float2 *Q, double *gpos, double *gocc, bool cuda_core_sums = true);
 int dgpu_friedel_test(const dgpu_grid *g, const dgpu_opts *op, int32_t fnum[3]);
+// One work item: an atom tile of one type, a column chunk and a row range.
+struct AdjItem {
+    int64_t a0;          // first padded atom of the tile
+    int64_t a_end;       // end of the type's atom range
+    int32_t t;           // type (0-based)
+    int32_t kc;          // column chunk
+    int32_t rt0, rt1;    // row tiles
+};
+
+// Geometry of one tensor-core adjoint launch.
+struct AdjTcGeom {
+    int32_t f[3];
+    int32_t ra, rb, ac, fra, frb, ncols;
+    int32_t rtiles, nstage;        // row tiles, 32-column stages over all columns
+    int64_t rows, pbox;
+    int32_t ec;                    // n_c V' scaled by 2^ec
+    int64_t sra, srb, sac;         // box-order strides of the row and column axes
+    double eck[3], vi[9];
+};
+
+// A planned tensor-core adjoint: geometry, work items, number of Q images.
+struct AdjTcPlan {
+    AdjTcGeom g;
+    std::vector<AdjItem> items;
+    int64_t nimg = 0;
+    int32_t nscat = 0;
+};
+void dgpu_adjtc_plan(dgpu_ctx *ctx, const BoxSpec &box, const dgpu_grid *grid, int32_t nscat, const int64_t *ts,
+                     AdjTcPlan &plan);
+size_t dgpu_adjtc_img_bytes(const AdjTcPlan &plan);
+// Enqueue only: Q scale, Q images, main kernel (d_items: the plan's items on
+// the device; err: zeroed by the caller, read after the stream).
+int dgpu_adjtc_enqueue(dgpu_ctx *ctx, const AdjTcPlan &plan, const AdjItem *d_items, uint8_t *d_img,
+                       uint32_t *d_qmax, const uint64_t *ph0, const uint64_t *du, const uint64_t *dv,
+                       const uint64_t *dw, const float *w, const int32_t *aidx, const float2 *Q, double *gpos,
+                       double *gocc, int32_t *err);
 // Tensor-core adjoint sums (k_adjtc.cu): adds the gradient of every prepared
 // atom of the ntype type ranges ts (host) to gpos / gocc (device, indexed by
 // aidx); Q: nscat * box points, FP32 complex, dense box order.

@@ -293,13 +293,14 @@ int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
 // Enqueue-only adjoint of one crystal whose forward results (csf, dsi, istl,
 // cfact, prepared atoms) are on the device.  g: np doubles, chi: 513 doubles
 // (chi[512] receives chi^2), Q: nscat*pbox float2; gpos (3*natoms) and gocc
-// (natoms) must be zeroed by the caller.
+// (natoms) must be zeroed by the caller.  With cuda_core_sums false only g,
+// chi^2 and Q are produced (the tensor-core sums follow from Q).
 int dgpu_adjoint_async(dgpu_ctx *ctx, const FormSpec *d_fs, const BoxSpec &box, int32_t friedel_dim,
                        const dgpu_grid *grid, double diff_scale, int32_t nscat, const int64_t *ts,
                        const uint64_t *ph0, const uint64_t *du, const uint64_t *dv, const uint64_t *dw,
                        const float *w, const int32_t *aidx, const double2 *csf, const double *dsi,
                        const int32_t *istl, const double2 *cfact, const double *it, const double *wt, double *g,
-                       double *chi, float2 *Q, double *gpos, double *gocc)
+                       double *chi, float2 *Q, double *gpos, double *gocc, bool cuda_core_sums)
 {
     const int64_t np = (int64_t)box.num[0] * box.num[1] * box.num[2];
     const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
@@ -307,6 +308,8 @@ int dgpu_adjoint_async(dgpu_ctx *ctx, const FormSpec *d_fs, const BoxSpec &box, 
     k_adj_chi<<<1, 32, 0, ctx->stream>>>(chi, 512, chi + 512);
     k_adj_q<<<(unsigned)dgpu_cdiv(nb, 256), 256, 0, ctx->stream>>>(d_fs, box, friedel_dim, g, csf, istl, cfact,
                                                                      sqrt(diff_scale), Q);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    if (!cuda_core_sums) return DGPU_OK;      // the caller runs the per-atom sums on the tensor cores
     AdjGeom ag;
     for (int k = 0; k < 3; k++) {
         ag.f[k] = box.f[k];

@@ -54,26 +54,6 @@
 #define AT_SMEM (AT_A_BYTES + AT_QSLOTS * AT_Q_BYTES + AT_BAR_BYTES)
 #define AT_V_SCALE 4096.0f
 
-// One work item: an atom tile of one type, a column chunk and a row range.
-struct AdjItem {
-    int64_t a0;          // first padded atom of the tile
-    int64_t a_end;       // end of the type's atom range
-    int32_t t;           // type (0-based)
-    int32_t kc;          // column chunk
-    int32_t rt0, rt1;    // row tiles
-};
-
-// Geometry shared by the kernels of one launch.
-struct AdjTcGeom {
-    int32_t f[3];
-    int32_t ra, rb, ac, fra, frb, ncols;
-    int32_t rtiles, nstage;        // row tiles, 32-column stages over all columns
-    int64_t rows, pbox;
-    int32_t ec;                    // n_c V' scaled by 2^ec
-    int64_t sra, srb, sac;         // box-order strides of the row and column axes
-    double eck[3], vi[9];
-};
-
 // max |component| of Q over all types (bits of a non-negative float)
 __global__ void k_adjtc_qmax(const float2 *__restrict__ Q, int64_t n, uint32_t *__restrict__ out)
 {
@@ -482,12 +462,10 @@ static double adjtc_cost(const int32_t f[3], int ac)
     return rtiles * c;
 }
 
-int dgpu_adjtc_sums(dgpu_ctx *ctx, const BoxSpec &box, const dgpu_grid *grid, int32_t nscat, const int64_t *ts,
-                    const uint64_t *ph0, const uint64_t *du, const uint64_t *dv, const uint64_t *dw, const float *w,
-                    const int32_t *aidx, const float2 *Q, double *gpos, double *gocc)
+void dgpu_adjtc_plan(dgpu_ctx *ctx, const BoxSpec &box, const dgpu_grid *grid, int32_t nscat, const int64_t *ts,
+                     AdjTcPlan &plan)
 {
-    if (nscat < 1 || nscat > 64) return dgpu_set_error(ctx, DGPU_ERR_ARG, "nscat=%d", nscat);
-    AdjTcGeom g;
+    AdjTcGeom &g = plan.g;
     memset(&g, 0, sizeof(g));
     for (int k = 0; k < 3; k++) {
         g.f[k] = box.f[k];
@@ -522,14 +500,13 @@ int dgpu_adjtc_sums(dgpu_ctx *ctx, const BoxSpec &box, const dgpu_grid *grid, in
     while ((1 << lg) < g.ncols) lg++;
     g.ec = 14 - lg;                                // n_c < ncols <= 2^lg
     const int kch = (int)dgpu_cdiv(g.ncols, AT_KC);
-
     // work items: atom tiles x column chunks x row parts
     int64_t tiles = 0;
     for (int t = 0; t < nscat; t++) tiles += dgpu_cdiv(ts[t + 1] - ts[t], AT_M);
     int64_t rp = tiles * kch > 0 ? dgpu_cdiv((int64_t)4 * ctx->nsm, tiles * kch) : 1;
     if (rp > g.rtiles) rp = g.rtiles;
     if (rp < 1) rp = 1;
-    std::vector<AdjItem> items;
+    plan.items.clear();
     for (int t = 0; t < nscat; t++)
         for (int64_t a0 = ts[t]; a0 < ts[t + 1]; a0 += AT_M)
             for (int kc = 0; kc < kch; kc++)
@@ -541,28 +518,33 @@ int dgpu_adjtc_sums(dgpu_ctx *ctx, const BoxSpec &box, const dgpu_grid *grid, in
                     it.kc = kc;
                     it.rt0 = (int32_t)(g.rtiles * p / rp);
                     it.rt1 = (int32_t)(g.rtiles * (p + 1) / rp);
-                    if (it.rt1 > it.rt0) items.push_back(it);
+                    if (it.rt1 > it.rt0) plan.items.push_back(it);
                 }
-    if (items.empty()) return DGPU_OK;
+    plan.nimg = (int64_t)nscat * g.rtiles * g.nstage;
+    plan.nscat = nscat;
+    static bool attr_set = false;     // set once, outside any stream capture
+    if (!attr_set && cudaFuncSetAttribute(k_adjtc, cudaFuncAttributeMaxDynamicSharedMemorySize, AT_SMEM) == cudaSuccess)
+        attr_set = true;
+}
 
-    // Q images and the scale of Q
-    const int64_t nimg = (int64_t)nscat * g.rtiles * g.nstage;
-    const size_t ibytes = ((size_t)items.size() * sizeof(AdjItem) + 255) & ~(size_t)255;
-    DGPU_CUDA(ctx, ctx->adj_qimg.ensure((size_t)nimg * AT_Q_BYTES));
-    DGPU_CUDA(ctx, ctx->adj_items.ensure(ibytes + 256));
-    uint32_t *qmax = reinterpret_cast<uint32_t *>(ctx->adj_items.as<uint8_t>() + ibytes);
-    DGPU_CUDA(ctx, cudaMemsetAsync(qmax, 0, sizeof(uint32_t), ctx->stream));
-    k_adjtc_qmax<<<4 * ctx->nsm, 256, 0, ctx->stream>>>(Q, (int64_t)nscat * g.pbox, qmax);
-    DGPU_CUDA(ctx, cudaGetLastError());
-    k_adjtc_qimg<<<(unsigned)nimg, 256, 0, ctx->stream>>>(Q, g, qmax, ctx->adj_qimg.as<uint8_t>());
-    DGPU_CUDA(ctx, cudaGetLastError());
-    DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->adj_items.p, items.data(), items.size() * sizeof(AdjItem),
-                                   cudaMemcpyHostToDevice, ctx->stream));
+size_t dgpu_adjtc_img_bytes(const AdjTcPlan &plan) { return (size_t)plan.nimg * AT_Q_BYTES; }
 
+int dgpu_adjtc_enqueue(dgpu_ctx *ctx, const AdjTcPlan &plan, const AdjItem *d_items, uint8_t *d_img,
+                       uint32_t *d_qmax, const uint64_t *ph0, const uint64_t *du, const uint64_t *dv,
+                       const uint64_t *dw, const float *w, const int32_t *aidx, const float2 *Q, double *gpos,
+                       double *gocc, int32_t *err)
+{
+    if (plan.items.empty()) return DGPU_OK;
+    const AdjTcGeom &g = plan.g;
+    DGPU_CUDA(ctx, cudaMemsetAsync(d_qmax, 0, sizeof(uint32_t), ctx->stream));
+    k_adjtc_qmax<<<4 * ctx->nsm, 256, 0, ctx->stream>>>(Q, (int64_t)plan.nscat * g.pbox, d_qmax);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    k_adjtc_qimg<<<(unsigned)plan.nimg, 256, 0, ctx->stream>>>(Q, g, d_qmax, d_img);
+    DGPU_CUDA(ctx, cudaGetLastError());
     const uint64_t *dd[3] = {du, dv, dw};
     AdjTcLaunch L;
-    L.items = ctx->adj_items.as<AdjItem>();
-    L.nitems = (int64_t)items.size();
+    L.items = d_items;
+    L.nitems = (int64_t)plan.items.size();
     L.g = g;
     L.ph0 = ph0;
     L.dra = dd[g.ra];
@@ -570,24 +552,40 @@ int dgpu_adjtc_sums(dgpu_ctx *ctx, const BoxSpec &box, const dgpu_grid *grid, in
     L.dac = dd[g.ac];
     L.w = w;
     L.aidx = aidx;
-    L.qimg = ctx->adj_qimg.as<uint8_t>();
-    L.qmax = qmax;
+    L.qimg = d_img;
+    L.qmax = d_qmax;
     L.gpos = gpos;
     L.gocc = gocc;
-    DGPU_CUDA(ctx, ctx->flag.ensure(64));
-    L.err = ctx->flag.as<int32_t>() + 10;
-    DGPU_CUDA(ctx, cudaMemsetAsync(L.err, 0, sizeof(int32_t), ctx->stream));
-    static bool attr_set = false;
-    if (!attr_set) {
-        DGPU_CUDA(ctx, cudaFuncSetAttribute(k_adjtc, cudaFuncAttributeMaxDynamicSharedMemorySize, AT_SMEM));
-        attr_set = true;
-    }
+    L.err = err;
     const int grid_n = (int)(L.nitems < ctx->nsm ? L.nitems : ctx->nsm);
     k_adjtc<<<grid_n, AT_THREADS, AT_SMEM, ctx->stream>>>(L);
     DGPU_CUDA(ctx, cudaGetLastError());
+    return DGPU_OK;
+}
+
+int dgpu_adjtc_sums(dgpu_ctx *ctx, const BoxSpec &box, const dgpu_grid *grid, int32_t nscat, const int64_t *ts,
+                    const uint64_t *ph0, const uint64_t *du, const uint64_t *dv, const uint64_t *dw, const float *w,
+                    const int32_t *aidx, const float2 *Q, double *gpos, double *gocc)
+{
+    if (nscat < 1 || nscat > 64) return dgpu_set_error(ctx, DGPU_ERR_ARG, "nscat=%d", nscat);
+    AdjTcPlan plan;
+    dgpu_adjtc_plan(ctx, box, grid, nscat, ts, plan);
+    if (plan.items.empty()) return DGPU_OK;
+    const size_t ibytes = ((size_t)plan.items.size() * sizeof(AdjItem) + 255) & ~(size_t)255;
+    DGPU_CUDA(ctx, ctx->adj_qimg.ensure(dgpu_adjtc_img_bytes(plan)));
+    DGPU_CUDA(ctx, ctx->adj_items.ensure(ibytes + 256));
+    uint32_t *qmax = reinterpret_cast<uint32_t *>(ctx->adj_items.as<uint8_t>() + ibytes);
+    DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->adj_items.p, plan.items.data(), plan.items.size() * sizeof(AdjItem),
+                                   cudaMemcpyHostToDevice, ctx->stream));
+    DGPU_CUDA(ctx, ctx->flag.ensure(64));
+    int32_t *err = ctx->flag.as<int32_t>() + 10;
+    DGPU_CUDA(ctx, cudaMemsetAsync(err, 0, sizeof(int32_t), ctx->stream));
+    int rc = dgpu_adjtc_enqueue(ctx, plan, ctx->adj_items.as<AdjItem>(), ctx->adj_qimg.as<uint8_t>(), qmax, ph0, du,
+                                dv, dw, w, aidx, Q, gpos, gocc, err);
+    if (rc) return rc;
     // the item table must outlive its copy; the error flag is read here
     int32_t herr = 0;
-    DGPU_CUDA(ctx, cudaMemcpyAsync(&herr, L.err, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    DGPU_CUDA(ctx, cudaMemcpyAsync(&herr, err, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
     DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (herr) return dgpu_set_error(ctx, DGPU_ERR_TIMEOUT, "tensor-core adjoint wait gave up (site %d)", herr);
     return DGPU_OK;

@@ -28,6 +28,8 @@ struct Member {
     double ds;
     double rten[9];
     int64_t istl_off, cfact_off, pt_off, g_off, q_off, grad_off, cnt_off, offs_off, tsd_off, chi_off;
+    int64_t adj_item_off, adj_img_off;     // tensor-core adjoint: item and image offsets
+    AdjTcPlan adj;
 };
 
 struct HostPinned {
@@ -55,6 +57,7 @@ struct BatchState {
     std::vector<int64_t> sig;
     std::vector<Member> mem;
     bool targets = false, has_occ = false;
+    int64_t adj_qmax_off = 0;              // byte offset of the members' Q scales in d_adj_items
     int64_t tot_atoms = 0, tot_pad = 0, tot_np = 0;
     TcPlan plan;
     cudaGraph_t graph = nullptr;
@@ -63,6 +66,7 @@ struct BatchState {
     DevBuf d_istl, d_cfact, d_csf, d_dsi, d_g, d_q, d_chi, d_grad, d_coef, d_fs, d_it, d_wt, part, desc;
     DevBuf d_mult;                         // tensor-core step factors, 3 x tot_pad
     DevBuf d_vimg;                         // tensor-core V images
+    DevBuf d_adj_items, d_adj_img;         // tensor-core adjoint: items (+ Q scales), Q images
     HostPinned h_pos, h_isc, h_aocc, h_it, h_wt, h_dsi, h_chi, h_grad;
     ~BatchState()
     {
@@ -74,6 +78,8 @@ struct BatchState {
         for (DevBuf *x : b) x->release();
         d_mult.release();
         d_vimg.release();
+        d_adj_items.release();
+        d_adj_img.release();
     }
 };
 
@@ -105,6 +111,7 @@ static int batch_enqueue(dgpu_ctx *ctx, BatchState &B, const dgpu_opts *op)
     DGPU_CUDA(ctx, cudaMemsetAsync(B.d_w.p, 0, pad * 4, st));
     DGPU_CUDA(ctx, cudaMemsetAsync(B.d_idx.p, 0xFF, pad * 4, st));
     DGPU_CUDA(ctx, cudaMemsetAsync(flag, 0, sizeof(int32_t), st));
+    DGPU_CUDA(ctx, cudaMemsetAsync(ctx->flag.as<int32_t>() + 10, 0, sizeof(int32_t), st));   // adjoint
     for (size_t c = 0; c < B.mem.size(); c++) {
         Member &m = B.mem[c];
         int rc = dgpu_prepare_async(ctx, B.d_pos.as<double>() + 3 * m.abase, B.d_isc.as<int32_t>() + m.abase,
@@ -148,7 +155,16 @@ static int batch_enqueue(dgpu_ctx *ctx, BatchState &B, const dgpu_opts *op)
                                     B.d_istl.as<int32_t>() + m.istl_off, B.d_cfact.as<double2>() + m.cfact_off,
                                     B.d_it.as<double>() + m.pt_off, B.d_wt.as<double>() + m.pt_off,
                                     B.d_g.as<double>() + m.pt_off, B.d_chi.as<double>() + m.chi_off,
-                                    B.d_q.as<float2>() + m.q_off, gpos, gpos + 3 * m.natoms);
+                                    B.d_q.as<float2>() + m.q_off, gpos, gpos + 3 * m.natoms, false);
+            if (rc) return rc;
+            uint32_t *qmax = reinterpret_cast<uint32_t *>(B.d_adj_items.as<uint8_t>() + B.adj_qmax_off) + c;
+            rc = dgpu_adjtc_enqueue(ctx, m.adj,
+                                    reinterpret_cast<const AdjItem *>(B.d_adj_items.as<uint8_t>()) + m.adj_item_off,
+                                    B.d_adj_img.as<uint8_t>() + m.adj_img_off, qmax, B.d_ph0.as<uint64_t>() + m.pbase,
+                                    B.d_du.as<uint64_t>() + m.pbase, B.d_dv.as<uint64_t>() + m.pbase,
+                                    B.d_dw.as<uint64_t>() + m.pbase, B.d_w.as<float>() + m.pbase,
+                                    B.d_idx.as<int32_t>() + m.pbase, B.d_q.as<float2>() + m.q_off, gpos,
+                                    gpos + 3 * m.natoms, ctx->flag.as<int32_t>() + 10);
             if (rc) return rc;
             DGPU_CUDA(ctx, cudaMemcpyAsync((double *)B.h_chi.p + c, B.d_chi.as<double>() + m.chi_off + 512,
                                            sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -280,6 +296,25 @@ static int batch_build(dgpu_ctx *ctx, BatchState &B, int32_t nc, const dgpu_crys
     const int N = op->tc_tile_n > 0 ? op->tc_tile_n : 64;
     int rc = dgpu_tc_plan(ctx, nc, in.data(), op, N, 4, B.plan, B.part, B.desc, &B.d_vimg);
     if (rc) return rc;
+    // tensor-core adjoint plans: items and Q images of every member
+    if (B.targets) {
+        std::vector<AdjItem> items;
+        int64_t img = 0;
+        for (int c = 0; c < nc; c++) {
+            Member &m = B.mem[c];
+            dgpu_adjtc_plan(ctx, m.box, &m.grid, m.nscat, m.ts, m.adj);
+            m.adj_item_off = (int64_t)items.size();
+            items.insert(items.end(), m.adj.items.begin(), m.adj.items.end());
+            m.adj_img_off = img;
+            img += (int64_t)dgpu_adjtc_img_bytes(m.adj);
+        }
+        B.adj_qmax_off = (int64_t)((items.size() * sizeof(AdjItem) + 255) & ~(size_t)255);
+        DGPU_CUDA(ctx, B.d_adj_items.ensure((size_t)B.adj_qmax_off + (size_t)nc * sizeof(uint32_t) + 256));
+        DGPU_CUDA(ctx, B.d_adj_img.ensure((size_t)(img > 0 ? img : 256)));
+        if (!items.empty())
+            DGPU_CUDA(ctx, cudaMemcpy(B.d_adj_items.p, items.data(), items.size() * sizeof(AdjItem),
+                                      cudaMemcpyHostToDevice));
+    }
     DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return DGPU_OK;
 }
@@ -380,6 +415,7 @@ extern "C" int dgpu_batch_run(dgpu_ctx *ctx, int32_t nc, const dgpu_crystal *crs
     int32_t flags[8];
     DGPU_CUDA(ctx, cudaMemcpy(flags, ctx->flag.as<int32_t>() + 8, sizeof(flags), cudaMemcpyDeviceToHost));
     if (flags[0]) return dgpu_set_error(ctx, DGPU_ERR_TIMEOUT, "tensor-core kernel wait gave up (site %d)", flags[0]);
+    if (flags[2]) return dgpu_set_error(ctx, DGPU_ERR_TIMEOUT, "tensor-core adjoint wait gave up (site %d)", flags[2]);
     if (flags[4]) return dgpu_set_error(ctx, DGPU_ERR_STL_RANGE, "sin(theta)/lambda beyond the table in a member");
     for (int c = 0; c < nc; c++) {
         const Member &m = B.mem[c];
