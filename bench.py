@@ -33,9 +33,13 @@ from diffusecode_gb300 import _abi  # noqa: E402
 from diffusecode_gb300 import structures as S  # noqa: E402
 
 METRIC = "G atom.hkl pairs/s for |F|^2"
-# kernels of one four_run without <F>: type count, scan, scatter, stltab,
-# formtab, type sums, combine, Friedel mirror, two statistics reductions
-LAUNCHES_PER_RUN = 10
+# kernels of one four_run without <F>, by engine: type count, scan, scatter,
+# stltab, formtab, type sums, combine, Friedel mirror, two statistics
+# reductions; the tensor-core engine adds its step-factor and V-image kernels
+LAUNCHES_PER_RUN = {1: 10, 2: 12}
+# DRAM bytes per atom of one tensor-core type-sum launch (ncu capture on the
+# 108 000-atom, 61^3 alloy: 100.4 MB read + written)
+TC_DRAM_BYTES_PER_ATOM = 100.38e6 / 108000
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
@@ -306,22 +310,23 @@ def run_ours(args, world, rank, local):
         ctx.check(ctx.lib.dgpu_four_run_device(ctx.h, C.byref(c), C.byref(g), C.byref(op),
                                                C.c_void_p(csf.data_ptr()), C.c_void_p(acsf.data_ptr()),
                                                C.c_void_p(dsi.data_ptr()), C.byref(info)))
-        return info.total_ms, info.kernel_ms
+        return info.total_ms, info.kernel_ms, ctx.lib.dgpu_tc_last_kernel_ms(ctx.h)
 
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
     barrier(world)
-    times, ktimes = [], []
+    times, ktimes, tctimes = [], [], []
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(args.steps):
             flush.fill_(1.0)
             torch.cuda.synchronize()
-            tt, kt = step()
+            tt, kt, tk = step()
             times.append(tt)
             ktimes.append(kt)
+            tctimes.append(tk)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
     barrier(world)
@@ -371,12 +376,17 @@ def run_ours(args, world, rank, local):
     fnum_pts = int(np.prod(list(info.fnum)))
     pairs_computed = cr.n_scattering() * fnum_pts
     if engine_used == _abi.ENGINE_TC:
+        # the tensor-core kernel alone, CUDA events on its stream, averaged over the timed steps
+        tcms = sum(tctimes) / len(tctimes)
         flops = 24.0 * pairs_computed
-        achieved = flops / (kms * 1e-3) / 1e12
+        achieved = flops / (tcms * 1e-3) / 1e12
         peak = pk.get("bf16_tflops", 1900.0)
         roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": None,
-                "note": f"24 tensor flops per computed pair (3 split products x 8); peak {pk_kind}"}
+                "frac": achieved / peak, "traffic": TC_DRAM_BYTES_PER_ATOM * cr.n_scattering(),
+                "kernel_ms": tcms,
+                "note": f"24 tensor flops per computed pair (3 split products x 8); peak {pk_kind}; traffic: "
+                        "DRAM bytes of one ncu capture of the same kernel on the 108 000-atom alloy, scaled by "
+                        "the atom count (the bytes are the V operand images, which grow with the atoms)"}
     else:
         # direct engine: FP32 pipe; 4 flops/pair of accumulation + phasor
         flops = 4.0 * pairs_computed
@@ -400,7 +410,7 @@ def run_ours(args, world, rank, local):
         "adjoint": adj,
         "batch": bat,
         "tc_config": list(info.tc_config),
-        "gpu_launches": LAUNCHES_PER_RUN * args.steps,
+        "gpu_launches": LAUNCHES_PER_RUN.get(engine_used, 10) * args.steps,
         "accuracy": {"rel_err_vs_fp64": acc_err, "points": acc_pts,
                      "norm": "max |I-I64|/(I64 + N<|f|^2>) at sampled grid points"},
         "e2e": {"value": e2e_val, "unit": "G pairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

@@ -57,7 +57,7 @@ extern "C" int dgpu_ctx_create(int device, dgpu_ctx **out)
     if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) { delete c; return DGPU_ERR_CUDA; }
     c->nsm = prop.multiProcessorCount;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { delete c; return DGPU_ERR_CUDA; }
-    for (int i = 0; i < 6; i++)
+    for (int i = 0; i < 8; i++)
         if (cudaEventCreate(&c->ev[i]) != cudaSuccess) { delete c; return DGPU_ERR_CUDA; }
     *out = c;
     return DGPU_OK;
@@ -72,10 +72,10 @@ extern "C" int dgpu_ctx_destroy(dgpu_ctx *c)
     DevBuf *bufs[] = {&c->pos, &c->iscat, &c->aocc, &c->sel, &c->counts, &c->type_start, &c->ph0, &c->du,
                       &c->dv, &c->dw, &c->w, &c->aph0, &c->adu, &c->adv, &c->adw, &c->aw, &c->istl,
                       &c->cfact, &c->part, &c->apart, &c->lat, &c->csf, &c->acsf, &c->dsi, &c->stats,
-                      &c->flag, &c->tc_part, &c->tc_work, &c->tc_mult, &c->tc_vimg, &c->adj_qimg, &c->adj_items, &c->gq, &c->gpart, &c->grad, &c->batch_desc,
-                      &c->batch_aux};
+                      &c->flag, &c->tc_part, &c->tc_work, &c->tc_mult, &c->tc_vimg, &c->adj_qimg,
+                      &c->adj_items, &c->gq, &c->gpart, &c->grad, &c->batch_desc, &c->batch_aux};
     for (DevBuf *b : bufs) b->release();
-    for (int i = 0; i < 6; i++)
+    for (int i = 0; i < 8; i++)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;

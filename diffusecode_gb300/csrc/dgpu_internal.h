@@ -62,7 +62,7 @@ struct dgpu_ctx {
     int device = 0;
     int nsm = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev[6] = {};
+    cudaEvent_t ev[8] = {};
     char err[512] = {0};
     // cached buffers
     DevBuf pos, iscat, aocc, sel;
@@ -77,6 +77,7 @@ struct dgpu_ctx {
     int64_t ts_main[2 * 64 + 4] = {};      // type ranges of the last main atom preparation
     DevBuf gq, gpart, grad, batch_desc, batch_aux;
     double batch_ms = 0.0;
+    double tc_kernel_ms = 0.0;              // duration of the last single-problem tensor-core launch
     std::map<TcKey, TcChoice> tc_tuned;   // autotuner results per problem shape
     BatchState *batch = nullptr;          // captured population graph and its buffers
     int32_t tc_last[4] = {-1, -1, -1, -1};
@@ -209,7 +210,9 @@ struct TcPlan {
 // image budget: V is generated inside the kernel instead)
 int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *op, int N, int slice_mult,
                  TcPlan &plan, DevBuf &part, DevBuf &desc, DevBuf *vimg);
-int dgpu_tc_launch(dgpu_ctx *ctx, const TcPlan &plan);          // enqueues the kernel only
+// Enqueues the V images and the kernel only; timed: events ev[6], ev[7]
+// around the main kernel.
+int dgpu_tc_launch(dgpu_ctx *ctx, const TcPlan &plan, bool timed = false);
 int dgpu_tc_check(dgpu_ctx *ctx);                               // waits, reads the error flag
 struct PartRef;
 // Per-atom step factors exp(2 pi i 8 d) of du, dv, dw (n atoms) into

@@ -852,7 +852,7 @@ int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *o
     return DGPU_OK;
 }
 
-int dgpu_tc_launch(dgpu_ctx *ctx, const TcPlan &plan)
+int dgpu_tc_launch(dgpu_ctx *ctx, const TcPlan &plan, bool timed)
 {
     DGPU_CUDA(ctx, cudaMemsetAsync(plan.L.err, 0, sizeof(int32_t), ctx->stream));
     if (plan.L.nitems < 1) return DGPU_OK;
@@ -866,11 +866,13 @@ int dgpu_tc_launch(dgpu_ctx *ctx, const TcPlan &plan)
                 k_tc_vgen<false><<<(unsigned)nimg, 256, 0, ctx->stream>>>(g.dac, g.N, g.n_tiles, g.vimg);
         }
     const int grid = (int)(plan.L.nitems < ctx->nsm ? plan.L.nitems : ctx->nsm);
+    if (timed) DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[6], ctx->stream));
     if (plan.L.bf16)
         k_tc<true><<<grid, TC_THREADS, plan.smem, ctx->stream>>>(plan.L);
     else
         k_tc<false><<<grid, TC_THREADS, plan.smem, ctx->stream>>>(plan.L);
     DGPU_CUDA(ctx, cudaGetLastError());
+    if (timed) DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[7], ctx->stream));
     return DGPU_OK;
 }
 
@@ -920,6 +922,8 @@ static void tc_candidates(const BoxSpec &box, int want_n, int kslice, TcChoice *
             }
         }
 }
+
+extern "C" double dgpu_tc_last_kernel_ms(const dgpu_ctx *ctx) { return ctx ? ctx->tc_kernel_ms : 0.0; }
 
 int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const uint64_t *dv, const uint64_t *dw,
                  const float *w, const int64_t *h_type_start, int32_t ntype, const BoxSpec &box,
@@ -989,10 +993,15 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
     TcPlan plan;
     rc = dgpu_tc_plan(ctx, 1, &in, op, choice.N, choice.slice_mult, plan, part, ctx->tc_part, &ctx->tc_vimg);
     if (rc) return rc;
-    rc = dgpu_tc_launch(ctx, plan);
+    rc = dgpu_tc_launch(ctx, plan, true);
     if (rc) return rc;
     rc = dgpu_tc_check(ctx);
     if (rc) return rc;
+    {
+        float ms = 0.f;
+        DGPU_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]));
+        ctx->tc_kernel_ms = ms;
+    }
     ctx->tc_last[0] = plan.probs[0].ac;
     ctx->tc_last[1] = plan.probs[0].N;
     ctx->tc_last[2] = plan.L.nbuf;

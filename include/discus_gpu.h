@@ -235,6 +235,12 @@ int dgpu_batch_run(dgpu_ctx *ctx, int32_t ncrystal, const dgpu_crystal *crystals
 /* Device time of the last dgpu_batch_run call's persistent launch, ms. */
 double dgpu_batch_last_ms(const dgpu_ctx *ctx);
 
+/* Device time of the tensor-core type-sum kernel alone in the last
+ * dgpu_four_run / dgpu_four_run_device call that used the tensor-core
+ * engine, ms (CUDA events on the context's stream around that launch).
+ * Measurement aid; no counterpart in the reference. */
+double dgpu_tc_last_kernel_ms(const dgpu_ctx *ctx);
+
 #ifdef __cplusplus
 }
 #endif
