@@ -43,6 +43,10 @@ TC_DRAM_BYTES_PER_ATOM = 100.38e6 / 108000
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
+# workloads run with the average structure factor subtracted (set aver 1)
+WORKLOAD_FAVE = {"hex-layers-1001^2": 1.0}
+
+
 def workload(name):
     if name == "fcc-alloy-101^3":
         return S.fcc_alloy_volume()
@@ -163,10 +167,13 @@ def cpu_baseline(cr, grid, nthreads=0):
     return pairs * credit / sec / 1e9, nthreads, rows, sec
 
 
-def fp64_check(cr, grid, dsi, npts=192, seed=7):
+def fp64_check(cr, grid, dsi, npts=192, seed=7, fave=0.0):
     """|F|^2 at sampled grid points from an FP64 numpy sum over all atoms
     (TABLE form factors, as the run uses), against the GPU's dsi:
-    max |I - I_64| / (I_64 + N<|f|^2>)."""
+    max |I - I_64| / (I_64 + N<|f|^2>).  With fave = 1 the average structure
+    factor of four_aver is subtracted first: every cell's atoms folded into
+    one cell (x - cell - dim0), times the lattice sum over all cells, over the
+    number of cells."""
     rng = np.random.Generator(np.random.PCG64(seed))
     n1, n2, n3 = grid.inc
     idx = np.stack([rng.integers(0, n, npts) for n in (n1, n2, n3)], 1)
@@ -179,21 +186,35 @@ def fp64_check(cr, grid, dsi, npts=192, seed=7):
     q2 = np.einsum("pa,ab,pb->p", h32, cr.rten, h32) / 4.0
     istl = np.floor(np.sqrt(q2) * 1000.0 + 0.5)
     s2 = (istl * 0.001) ** 2
-    F = np.zeros(npts, complex)
-    floor = np.zeros(npts)
-    for t in range(1, cr.nscat + 1):
-        sel = cr.iscat == t
-        x = cr.pos[sel]
-        sc = cr.scat[t]
-        f = sc[0] + sum(sc[2 * i - 1] * np.exp(-sc[2 * i] * s2) for i in range(1, 5))
-        cf = np.exp(-cr.dw[t] * s2) * cr.occ[t] * f
+    def phase_sum(x):
         acc = np.zeros(npts, complex)
         for k0 in range(0, x.shape[0], 65536):
             ph = h @ x[k0:k0 + 65536].T
             ph -= np.round(ph)
             acc += np.exp(2j * np.pi * ph).sum(axis=1)
-        F += cf * acc
+        return acc
+
+    F = np.zeros(npts, complex)
+    Fav = np.zeros(npts, complex)
+    floor = np.zeros(npts)
+    if fave:
+        icc = np.asarray(cr.icc)
+        cell = np.arange(cr.natoms) // cr.ncatoms
+        cidx = np.stack([cell % icc[0], (cell // icc[0]) % icc[1], cell // (icc[0] * icc[1])], 1)
+        fold = cr.pos - cidx - np.asarray(cr.dim0)[None, :]
+        ncell = int(np.prod(icc))
+        g0, g1, g2 = np.meshgrid(*(np.arange(n) for n in icc), indexing="ij")
+        lat = phase_sum(np.stack([g0.ravel(), g1.ravel(), g2.ravel()], 1) + np.asarray(cr.dim0)[None, :])
+    for t in range(1, cr.nscat + 1):
+        sel = cr.iscat == t
+        sc = cr.scat[t]
+        f = sc[0] + sum(sc[2 * i - 1] * np.exp(-sc[2 * i] * s2) for i in range(1, 5))
+        cf = np.exp(-cr.dw[t] * s2) * cr.occ[t] * f
+        F += cf * phase_sum(cr.pos[sel])
+        if fave:
+            Fav += cf * phase_sum(fold[sel]) * lat / ncell
         floor += sel.sum() * cf ** 2
+    F -= Fav
     i64 = np.abs(F) ** 2
     ig = dsi[idx[:, 0], idx[:, 1], idx[:, 2]]
     return float(np.max(np.abs(ig - i64) / (i64 + floor))), npts
@@ -221,6 +242,34 @@ def adjoint_measure(ctx, engine, steps=3):
     return {"workload": "rocksalt-100000-atoms-65^3", "fwd_kernel_ms": f, "adjoint_ms": b,
             "bwd_over_fwd": b / f, "chi2": c2,
             "note": "adjoint = per-point weights + per-atom sums (tensor cores for the TC engine); fwd = type sums of the same engine"}
+
+
+def plain_measure(ctx, c, g, op_tc, csf, acsf, dsi, flush, cr, grid, fave, pairs, steps=2):
+    """The plain form on the same workload: the CUDA-core FP32 engine (exact
+    64-bit phases, FP32 sincospi, FP64 across chunks), device-resident, L2
+    flushed before each step; its FP64 accuracy and the tensor-core speed-up."""
+    import torch
+    op = _abi.Opts()
+    C.memmove(C.byref(op), C.byref(op_tc), C.sizeof(op))
+    op.engine = _abi.ENGINE_DIRECT
+    info = _abi.Info()
+
+    def run():
+        ctx.check(ctx.lib.dgpu_four_run_device(ctx.h, C.byref(c), C.byref(g), C.byref(op),
+                                               C.c_void_p(csf.data_ptr()), C.c_void_p(acsf.data_ptr()),
+                                               C.c_void_p(dsi.data_ptr()), C.byref(info)))
+        return info.total_ms
+
+    run()
+    ts = []
+    for _ in range(steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        ts.append(run())
+    ms = sum(ts) / len(ts)
+    err, npt = fp64_check(cr, grid, dsi.cpu().numpy().reshape(grid.inc, order="F"), fave=fave)
+    return {"value": pairs / (ms * 1e-3) / 1e9, "unit": "G pairs/s", "ms_per_step": ms, "steps": steps,
+            "rel_err_vs_fp64": err, "engine": "direct (CUDA cores, FP32 phasors)"}
 
 
 def batch_measure(ctx, steps=3):
@@ -293,7 +342,8 @@ def run_ours(args, world, rank, local):
     cr, grid = workload(args.workload)
     ctx = _lib.Context(local)
     engine = {"auto": _abi.ENGINE_AUTO, "direct": _abi.ENGINE_DIRECT, "tc": _abi.ENGINE_TC}[args.engine]
-    op = _abi.default_opts(ldbw=1, phase=_abi.PHASE_EXACT64, form=_abi.FORM_TABLE, engine=engine)
+    fave = WORKLOAD_FAVE.get(args.workload, 0.0)
+    op = _abi.default_opts(ldbw=1, phase=_abi.PHASE_EXACT64, form=_abi.FORM_TABLE, engine=engine, fave=fave)
     npnt = grid.npoints
     pos = torch.from_numpy(cr.pos).to(dev)
     isc = torch.from_numpy(cr.iscat).to(dev)
@@ -369,7 +419,9 @@ def run_ours(args, world, rank, local):
 
     if rank != 0:
         return
-    acc_err, acc_pts = fp64_check(cr, grid, dsi_host)
+    acc_err, acc_pts = fp64_check(cr, grid, dsi_host, fave=fave)
+    plain = None if (args.no_plain or engine_used != _abi.ENGINE_TC) else plain_measure(
+        ctx, c, g, op, csf, acsf, dsi, flush, cr, grid, fave, info.pairs)
     adj = None if args.no_adjoint else adjoint_measure(ctx, engine)
     bat = None if args.no_batch else batch_measure(ctx)
     pk, pk_kind = peaks()
@@ -400,13 +452,15 @@ def run_ours(args, world, rank, local):
         "vs_baseline": None, "dtype": "f32-phasor/f64-reduce" if engine_used != _abi.ENGINE_TC else "f16x3-split",
         "data": "synthetic",
         "config": {"workload": args.workload, "atoms": cr.n_scattering(), "grid": list(grid.inc),
-                   "pairs_per_step": pairs_full, "friedel_points": fnum_pts,
+                   "pairs_per_step": pairs_full, "friedel_points": fnum_pts, "fave": fave,
+                   "aver_pairs_per_step": int(info.pairs_aver),
                    "engine": {1: "direct", 2: "tc"}.get(engine_used, str(engine_used)),
                    "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas{world}"},
         "kernel_ms_per_step": kms,
         "wall_s_timed": wall,
         "roofline": roof,
         "clocks": clk.summary(),
+        "plain_fp32": dict(plain, tc_over_plain=value / plain["value"]) if plain else None,
         "adjoint": adj,
         "batch": bat,
         "tc_config": list(info.tc_config),
@@ -435,6 +489,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":
