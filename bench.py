@@ -167,7 +167,7 @@ def cpu_baseline(cr, grid, nthreads=0):
     return pairs * credit / sec / 1e9, nthreads, rows, sec
 
 
-def fp64_check(cr, grid, dsi, npts=192, seed=7, fave=0.0):
+def fp64_check(cr, grid, dsi, npts=192, seed=7, fave=0.0, split=False):
     """|F|^2 at sampled grid points from an FP64 numpy sum over all atoms
     (TABLE form factors, as the run uses), against the GPU's dsi:
     max |I - I_64| / (I_64 + N<|f|^2>).  With fave = 1 the average structure
@@ -217,7 +217,12 @@ def fp64_check(cr, grid, dsi, npts=192, seed=7, fave=0.0):
     F -= Fav
     i64 = np.abs(F) ** 2
     ig = dsi[idx[:, 0], idx[:, 1], idx[:, 2]]
-    return float(np.max(np.abs(ig - i64) / (i64 + floor))), npts
+    rel = np.abs(ig - i64) / (i64 + floor)
+    if split:
+        bragg = np.all(np.abs(h - np.round(h)) < 1e-6, axis=1)
+        return (float(np.max(rel)), npts, float(np.max(rel[~bragg])) if (~bragg).any() else 0.0,
+                float(np.max(rel[bragg])) if bragg.any() else 0.0, int(bragg.sum()))
+    return float(np.max(rel)), npts
 
 
 def adjoint_measure(ctx, engine, steps=3):
@@ -343,7 +348,8 @@ def run_ours(args, world, rank, local):
     ctx = _lib.Context(local)
     engine = {"auto": _abi.ENGINE_AUTO, "direct": _abi.ENGINE_DIRECT, "tc": _abi.ENGINE_TC}[args.engine]
     fave = WORKLOAD_FAVE.get(args.workload, 0.0)
-    op = _abi.default_opts(ldbw=1, phase=_abi.PHASE_EXACT64, form=_abi.FORM_TABLE, engine=engine, fave=fave)
+    op = _abi.default_opts(ldbw=1, phase=_abi.PHASE_EXACT64, form=_abi.FORM_TABLE, engine=engine, fave=fave,
+                           tc_flush=args.tc_flush)
     npnt = grid.npoints
     pos = torch.from_numpy(cr.pos).to(dev)
     isc = torch.from_numpy(cr.iscat).to(dev)
@@ -419,7 +425,7 @@ def run_ours(args, world, rank, local):
 
     if rank != 0:
         return
-    acc_err, acc_pts = fp64_check(cr, grid, dsi_host, fave=fave)
+    acc_err, acc_pts, acc_diffuse, acc_bragg, n_bragg = fp64_check(cr, grid, dsi_host, fave=fave, split=True)
     plain = None if (args.no_plain or engine_used != _abi.ENGINE_TC) else plain_measure(
         ctx, c, g, op, csf, acsf, dsi, flush, cr, grid, fave, info.pairs)
     adj = None if args.no_adjoint else adjoint_measure(ctx, engine)
@@ -466,6 +472,7 @@ def run_ours(args, world, rank, local):
         "tc_config": list(info.tc_config),
         "gpu_launches": LAUNCHES_PER_RUN.get(engine_used, 10) * args.steps,
         "accuracy": {"rel_err_vs_fp64": acc_err, "points": acc_pts,
+                     "non_bragg": acc_diffuse, "bragg": acc_bragg, "bragg_points": n_bragg,
                      "norm": "max |I-I64|/(I64 + N<|f|^2>) at sampled grid points"},
         "e2e": {"value": e2e_val, "unit": "G pairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
     }
@@ -490,6 +497,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--tc-flush", type=int, default=0, help="atoms per main-accumulator drain (0: default)")
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":

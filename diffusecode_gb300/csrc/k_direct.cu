@@ -71,9 +71,12 @@ k_direct(const uint64_t *__restrict__ ph0, const uint64_t *__restrict__ du,
             s_w[threadIdx.x] = w[a];
         }
         __syncthreads();
-        float accf[DIR_Q][2];
+        // FP32 sums over the chunk with Fast2Sum compensation: a coherent sum
+        // of nearly equal terms would otherwise round with a bias that grows
+        // with the chunk length (~ n 2^-24 of the sum)
+        float accf[DIR_Q][2], cmpf[DIR_Q][2];
 #pragma unroll
-        for (int k = 0; k < DIR_Q; k++) accf[k][0] = accf[k][1] = 0.f;
+        for (int k = 0; k < DIR_Q; k++) accf[k][0] = accf[k][1] = cmpf[k][0] = cmpf[k][1] = 0.f;
         for (int j = 0; j < cnt; j++) {
             const uint64_t d0 = s_d0[j];
             uint64_t ph = s_b[j] + m0 * d0 + m1 * s_d1[j] + m2 * s_d2[j];
@@ -84,15 +87,19 @@ k_direct(const uint64_t *__restrict__ ph0, const uint64_t *__restrict__ du,
                 float x = (float)(int32_t)(q >> 32) * 4.656612873077393e-10f;   // turns * 2
                 float sn, cs;
                 sincospif(x, &sn, &cs);
-                accf[k][0] = fmaf(wj, cs, accf[k][0]);
-                accf[k][1] = fmaf(wj, sn, accf[k][1]);
+                const float y0 = wj * cs, y1 = wj * sn;
+                const float t0 = accf[k][0] + y0, t1 = accf[k][1] + y1;
+                cmpf[k][0] += y0 - (t0 - accf[k][0]);
+                cmpf[k][1] += y1 - (t1 - accf[k][1]);
+                accf[k][0] = t0;
+                accf[k][1] = t1;
                 ph += d0;
             }
         }
 #pragma unroll
         for (int k = 0; k < DIR_Q; k++) {
-            accd[k][0] += (double)accf[k][0];
-            accd[k][1] += (double)accf[k][1];
+            accd[k][0] += (double)accf[k][0] + (double)cmpf[k][0];
+            accd[k][1] += (double)accf[k][1] + (double)cmpf[k][1];
         }
     }
     if (!valid) return;
