@@ -34,6 +34,9 @@ ENGINE_DIRECT = 1
 ENGINE_TC = 2
 SPLIT_F16 = 0
 SPLIT_BF16 = 1
+LOT_OFF = 1
+LOT_BOX = 2
+LOT_ELI = 3
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
@@ -56,6 +59,12 @@ class Crystal(C.Structure):
         ("dw", _dp),
         ("delfr", _dp),
         ("delfi", _dp),
+        ("is_anis", C.c_int32),
+        ("nanis", C.c_int32),
+        ("ianis", _ip),
+        ("anis_full", _dp),
+        ("ar", C.c_double * 3),
+        ("dim_lo", C.c_double * 3),
     ]
 
 
@@ -85,6 +94,12 @@ class Opts(C.Structure):
         ("tc_kslice", C.c_int32),
         ("tc_flush", C.c_int32),
         ("cancel", C.POINTER(C.c_int32)),
+        ("ilots", C.c_int32),
+        ("nlots", C.c_int32),
+        ("ls_xyz", C.c_int32 * 3),
+        ("lot_all", C.c_int32),
+        ("lperiod", C.c_int32),
+        ("lot_origins", _ip),
     ]
 
 
@@ -147,8 +162,19 @@ def default_opts(**kw):
     o.tc_kslice = 0
     o.tc_flush = 0
     o.cancel = C.cast(None, C.POINTER(C.c_int32))
+    o.ilots = LOT_OFF
+    o.nlots = 1
+    for k in range(3):
+        o.ls_xyz[k] = 5
+    o.lot_all = 0
+    o.lperiod = 1
+    o.lot_origins = C.cast(None, _ip)
     for k, v in kw.items():
-        if k == "aver_cells":
+        if k in ("aver_cells", "lot_origins"):
+            continue
+        if k == "ls_xyz":
+            for i in range(3):
+                o.ls_xyz[i] = int(v[i])
             continue
         setattr(o, k, v)
     return o

@@ -1,16 +1,21 @@
 // C-ABI entry points and the four_run orchestration on the device.
 //
 // dgpu_four_run replaces four_run (discus/prog/fourier_sup.f90:11-323) for
-// LOT_OFF crystals with isotropic ADPs.  The order of work follows it:
+// the independent atom model.  The order of work follows it:
 // four_layer/fourier_lmn (:71,:82), four_stltab (:84), four_formtab (:120),
-// four_test_friedel (:132), four_aver (:134), the loop over atom types
-// (:224-244), csf -= acsf and dsi += |csf|^2 (:250-254), four_apply_friedel
-// (:256), scaling (:281-282) and four_qinfo (:294).
+// four_nanis (:131), four_test_friedel (:132), four_aver (:134), the loop
+// over lots (:136-257) and over atom types or (type, ADP type) groups
+// (:195-244), csf -= acsf and dsi += |csf|^2 (:250-254), four_apply_friedel
+// (:256, once after the lots: it only copies the computed half), the lot
+// normalisation (:273-277), scaling (:281-282) and four_qinfo (:294).
 #include <math.h>
 #include <stdarg.h>
 #include <stdlib.h>
 
+#include <vector>
+
 #include "dgpu_internal.h"
+#include "dgpu_lots.h"
 
 int dgpu_set_error(dgpu_ctx *ctx, int code, const char *fmt, ...)
 {
@@ -41,6 +46,12 @@ extern "C" void dgpu_default_opts(dgpu_opts *o)
     o->engine = DGPU_ENGINE_AUTO;
     o->split = DGPU_SPLIT_F16;
     o->cancel = nullptr;
+    o->ilots = DGPU_LOT_OFF;
+    o->nlots = 1;
+    for (int k = 0; k < 3; k++) o->ls_xyz[k] = 5;
+    o->lot_all = 0;
+    o->lperiod = 1;
+    o->lot_origins = nullptr;
 }
 
 extern "C" int dgpu_ctx_create(int device, dgpu_ctx **out)
@@ -73,8 +84,10 @@ extern "C" int dgpu_ctx_destroy(dgpu_ctx *c)
                       &c->dv, &c->dw, &c->w, &c->aph0, &c->adu, &c->adv, &c->adw, &c->aw, &c->istl,
                       &c->cfact, &c->part, &c->apart, &c->lat, &c->csf, &c->acsf, &c->dsi, &c->stats,
                       &c->flag, &c->tc_part, &c->tc_work, &c->tc_mult, &c->tc_vimg, &c->adj_qimg,
-                      &c->adj_items, &c->gq, &c->gpart, &c->grad, &c->batch_desc, &c->batch_aux};
+                      &c->adj_items, &c->gq, &c->gpart, &c->grad, &c->batch_desc, &c->batch_aux,
+                      &c->ianis, &c->geff, &c->ghist, &c->lpos, &c->ltype, &c->locc, &c->lplan, &c->lfac};
     for (DevBuf *b : bufs) b->release();
+    delete c->fs_main;
     for (int i = 0; i < 8; i++)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -109,6 +122,27 @@ static int check_inputs(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
     if (op->fave > 0.0 && op->fave < 1.0 && !op->aver_cells)
         return dgpu_set_error(ctx, DGPU_ERR_ARG, "0<fave<1 needs the caller's cell selection");
     if (op->diff_scale < 0.0) return dgpu_set_error(ctx, DGPU_ERR_ARG, "diff_scale<0");
+    if (cr->is_anis && (cr->nanis < 1 || !cr->ianis || !cr->anis_full))
+        return dgpu_set_error(ctx, DGPU_ERR_ARG, "anisotropic crystal without nanis/ianis/anis_full");
+    // lots: the checks of the lots command (fourier.f90:490-497) and the origins' range
+    const bool lots = dgpu_lots_on(op);
+    if (op->ilots != 0 && op->ilots != DGPU_LOT_OFF && !lots)
+        return dgpu_set_error(ctx, DGPU_ERR_ARG, "ilots=%d", op->ilots);
+    if (lots || !op->lperiod)
+        for (int k = 0; k < 3; k++)
+            if (op->ls_xyz[k] < 1 || op->ls_xyz[k] > cr->icc[k])
+                return dgpu_set_error(ctx, DGPU_ERR_ARG, "ls_xyz(%d)=%d outside 1..icc", k + 1, op->ls_xyz[k]);
+    if (lots && !op->lot_all) {
+        if (op->nlots < 1 || !op->lot_origins)
+            return dgpu_set_error(ctx, DGPU_ERR_ARG, "lots need nlots>0 origins (or lot_all)");
+        int32_t cs[3];
+        dgpu_csize(cr, op, cs);
+        for (int64_t l = 0; l < op->nlots; l++)
+            for (int k = 0; k < 3; k++)
+                if (op->lot_origins[3 * l + k] < 1 || op->lot_origins[3 * l + k] > cs[k])
+                    return dgpu_set_error(ctx, DGPU_ERR_ARG, "lot %lld origin(%d)=%d outside 1..%d", (long long)l + 1,
+                                          k + 1, op->lot_origins[3 * l + k], cs[k]);
+    }
     return DGPU_OK;
 }
 
@@ -121,7 +155,9 @@ int dgpu_fill_formspec(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *o
     fs.lxray = op->lxray;
     fs.power = op->power;
     fs.ano = op->ano;
-    fs.ldbw = op->ldbw;
+    fs.ldbw = op->ldbw && !cr->is_anis;
+    fs.ngroup = cr->nscat;
+    for (int t = 1; t <= cr->nscat; t++) fs.gtype[t] = t;
     for (int t = 0; t <= cr->nscat; t++) {
         for (int i = 0; i < 11; i++) fs.scat[11 * t + i] = cr->scat[11 * t + i];
         fs.occ[t] = cr->occ[t];
@@ -224,22 +260,50 @@ int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g,
     DGPU_CUDA(ctx, cudaMemsetAsync(d_dsi, 0, np * sizeof(double), ctx->stream));
     DGPU_CUDA(ctx, cudaMemsetAsync(d_acsf, 0, np * sizeof(double2), ctx->stream));
 
+    // partial-sum groups: the types, or the (type, ADP type) pairs (four_nanis)
+    FormSpec fsm = fs;
+    const int32_t *eiscat = cr->iscat;
+    int32_t ngroup = cr->nscat;
+    if (cr->is_anis) {
+        rc = dgpu_anis_groups(ctx, cr, op, fsm, &ngroup);
+        if (rc) return rc;
+        eiscat = ctx->geff.as<int32_t>();
+    }
+    const bool lots = dgpu_lots_on(op);
+    int32_t cs[3];
+    dgpu_csize(cr, op, cs);
+    LotPlan lp;
+    if (lots) {
+        rc = dgpu_lot_plan(ctx, cr, op, ngroup, lp);
+        if (rc) return rc;
+    }
+
     int warn = 0;
     int32_t ncell = 0;
-    int64_t pairs_aver = 0;
+    int64_t pairs_aver = 0, pairs = 0;
     float kernel_ms = 0.f;
     int64_t ts[2 * 64 + 4];
 
-    // ---- <F> (four_aver) ----
+    // ---- <F> (four_aver): cells drawn over csize, lattice of the crystal or of a lot ----
     if (op->fave != 0.0) {
         const int64_t ncells = (int64_t)cr->icc[0] * cr->icc[1] * cr->icc[2];
         FoldSpec fold = {1, cr->ncatoms, {cr->icc[0], cr->icc[1], cr->icc[2]},
                          {cr->dim0[0], cr->dim0[1], cr->dim0[2]}, nullptr};
-        if (op->fave < 1.0) {
+        const bool whole = cs[0] == cr->icc[0] && cs[1] == cr->icc[1] && cs[2] == cr->icc[2];
+        if (op->fave < 1.0 || !whole) {
+            std::vector<uint8_t> sel((size_t)ncells, 0);
+            for (int32_t kk = 0; kk < cs[2]; kk++)
+                for (int32_t jj = 0; jj < cs[1]; jj++)
+                    for (int32_t ii = 0; ii < cs[0]; ii++) {
+                        const int64_t s = ii + (int64_t)cs[0] * (jj + (int64_t)cs[1] * kk);
+                        const bool on = op->fave >= 1.0 || op->aver_cells[s] != 0;
+                        sel[ii + (int64_t)cr->icc[0] * (jj + (int64_t)cr->icc[1] * kk)] = on ? 1 : 0;
+                        ncell += on ? 1 : 0;
+                    }
             DGPU_CUDA(ctx, ctx->sel.ensure(ncells));
-            DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->sel.p, op->aver_cells, ncells, cudaMemcpyHostToDevice, ctx->stream));
+            DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->sel.p, sel.data(), ncells, cudaMemcpyHostToDevice, ctx->stream));
+            DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));      // sel is a host temporary
             fold.sel = ctx->sel.as<uint8_t>();
-            for (int64_t c = 0; c < ncells; c++) ncell += op->aver_cells[c] ? 1 : 0;
         } else {
             ncell = (int32_t)ncells;
         }
@@ -252,19 +316,49 @@ int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g,
                          ctx->apart, &aref);
         if (rc) return rc;
         for (int t = 0; t < cr->nscat; t++) pairs_aver += ts[cr->nscat + 1 + t] * np;
-        // lattice of all cells (four_getav LOT_OFF + four_strucf(0,...) on the full num)
-        int32_t lat_nslice = 1, closed = op->phase == DGPU_PHASE_EXACT64;
+        // four_getav (fourier_sup.f90:2440-2510) + four_strucf(0, ...) on the full num:
+        // a box (all cells at dim0, or a box lot at 0) has a closed form in EXACT64
+        int32_t lat_n[3];
+        double lat_d[3];
+        for (int k = 0; k < 3; k++) {
+            lat_n[k] = lots ? op->ls_xyz[k] : cr->icc[k];
+            lat_d[k] = lots ? 0.0 : cr->dim0[k];
+        }
+        int32_t lat_nslice = 1;
+        const int32_t closed = op->phase == DGPU_PHASE_EXACT64 && op->ilots != DGPU_LOT_ELI;
         if (!closed) {
-            rc = dgpu_prepare_lattice(ctx, cr->icc, cr->dim0, geo, ctx->ph0, ctx->du, ctx->dv, ctx->dw, ctx->w);
-            if (rc) return rc;
-            int64_t lts[2] = {0, ncells};
+            int64_t lts[2 * 1 + 4];
+            int64_t nlat;
+            if (op->ilots == DGPU_LOT_ELI) {
+                nlat = (int64_t)lp.shape.size() / 3;
+                std::vector<double> pts((size_t)nlat * 3);
+                std::vector<int32_t> ones((size_t)nlat, 1);
+                for (int64_t m = 0; m < 3 * nlat; m++) pts[m] = (double)lp.shape[m];
+                DGPU_CUDA(ctx, ctx->lpos.ensure((size_t)nlat * 3 * sizeof(double)));
+                DGPU_CUDA(ctx, ctx->ltype.ensure((size_t)nlat * sizeof(int32_t)));
+                DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->lpos.p, pts.data(), pts.size() * sizeof(double),
+                                               cudaMemcpyHostToDevice, ctx->stream));
+                DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->ltype.p, ones.data(), ones.size() * sizeof(int32_t),
+                                               cudaMemcpyHostToDevice, ctx->stream));
+                DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // host temporaries
+                FoldSpec nofold = {0, 1, {1, 1, 1}, {0, 0, 0}, nullptr};
+                rc = dgpu_prepare_atoms(ctx, ctx->lpos.as<double>(), ctx->ltype.as<int32_t>(), nullptr, nlat, 1, geo,
+                                        nofold, ctx->ph0, ctx->du, ctx->dv, ctx->dw, ctx->w, lts);
+                if (rc) return rc;
+            } else {
+                nlat = (int64_t)lat_n[0] * lat_n[1] * lat_n[2];
+                rc = dgpu_prepare_lattice(ctx, lat_n, lat_d, geo, ctx->ph0, ctx->du, ctx->dv, ctx->dw, ctx->w);
+                if (rc) return rc;
+                lts[0] = 0;
+                lts[1] = nlat;
+            }
             BoxSpec full;
             for (int k = 0; k < 3; k++) { full.f[k] = num[k]; full.num[k] = num[k]; }
             rc = dgpu_direct_sums(ctx, ctx->ph0.as<uint64_t>(), ctx->du.as<uint64_t>(), ctx->dv.as<uint64_t>(),
-                                  ctx->dw.as<uint64_t>(), ctx->w.as<float>(), lts, 1, 1, full, ctx->lat,
-                                  &lat_nslice);
+                                  ctx->dw.as<uint64_t>(), ctx->w.as<float>(), lts, 1, op->phase == DGPU_PHASE_REF22,
+                                  full, ctx->lat, &lat_nslice);
             if (rc) return rc;
-            pairs_aver += ncells * np;
+            pairs_aver += nlat * np;
         }
         DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
         double norm = 0.0;
@@ -275,7 +369,7 @@ int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g,
         }
         rc = dgpu_aver_combine(ctx, fs, box, aref, ctx->istl.as<int32_t>(),
                                ctx->cfact.as<double2>(), closed ? nullptr : ctx->lat.as<double2>(), lat_nslice,
-                               closed, cr->icc, cr->dim0, norm, d_acsf);
+                               closed, lat_n, lat_d, norm, d_acsf);
         if (rc) return rc;
         float ms = 0.f;
         DGPU_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]));
@@ -283,26 +377,76 @@ int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g,
         if (cancelled(op)) return dgpu_set_error(ctx, DGPU_ERR_CANCELLED, "cancelled");
     }
 
-    // ---- type sums (fourier_sup.f90:224-244) ----
-    FoldSpec nofold = {0, cr->ncatoms, {cr->icc[0], cr->icc[1], cr->icc[2]}, {0, 0, 0}, nullptr};
-    rc = dgpu_prepare_atoms(ctx, cr->pos, cr->iscat, cr->atom_occ, cr->natoms, cr->nscat, geo, nofold, ctx->ph0,
-                            ctx->du, ctx->dv, ctx->dw, ctx->w, ts);
-    if (rc) return rc;
-    memcpy(ctx->ts_main, ts, sizeof(int64_t) * (2 * cr->nscat + 1));
-    PartRef pref;
-    DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
-    rc = engine_sums(ctx, engine, ctx->ph0, ctx->du, ctx->dv, ctx->dw, ctx->w, ts, cr->nscat, op, box, ctx->part,
-                     &pref);
-    if (rc) return rc;
-    DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
-    rc = dgpu_combine(ctx, fs, box, pref, ctx->istl.as<int32_t>(),
-                      ctx->cfact.as<double2>(), op->fave != 0.0 ? d_acsf : nullptr, d_csf, d_dsi, op->diff_scale);
-    if (rc) return rc;
-    {
+    const double2 *acsf_in = op->fave != 0.0 ? d_acsf : nullptr;
+    if (!lots) {
+        // ---- type or group sums (fourier_sup.f90:195-244) ----
+        FoldSpec nofold = {0, cr->ncatoms, {cr->icc[0], cr->icc[1], cr->icc[2]}, {0, 0, 0}, nullptr};
+        rc = dgpu_prepare_atoms(ctx, cr->pos, eiscat, cr->atom_occ, cr->natoms, ngroup, geo, nofold, ctx->ph0,
+                                ctx->du, ctx->dv, ctx->dw, ctx->w, ts);
+        if (rc) return rc;
+        memcpy(ctx->ts_main, ts, sizeof(int64_t) * (2 * ngroup + 1));
+        PartRef pref;
+        DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
+        rc = engine_sums(ctx, engine, ctx->ph0, ctx->du, ctx->dv, ctx->dw, ctx->w, ts, ngroup, op, box, ctx->part,
+                         &pref);
+        if (rc) return rc;
+        DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
+        rc = dgpu_combine(ctx, fsm, box, pref, ctx->istl.as<int32_t>(), ctx->cfact.as<double2>(), acsf_in, d_csf,
+                          d_dsi, op->diff_scale);
+        if (rc) return rc;
         float ms = 0.f;
         DGPU_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]));
         kernel_ms += ms;
+        for (int t = 0; t < ngroup; t++) pairs += ts[ngroup + 1 + t] * np;
+    } else {
+        // ---- lots (fourier_sup.f90:136-257): chunks of lots, one engine launch each ----
+        const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
+        DGPU_CUDA(ctx, ctx->lfac.ensure((size_t)ngroup * nb * sizeof(double2)));
+        rc = dgpu_group_factors(ctx, fsm, box, ctx->istl.as<int32_t>(), ctx->cfact.as<double2>(),
+                                ctx->lfac.as<double2>());
+        if (rc) return rc;
+        for (int64_t lot0 = 0; lot0 < lp.nlots; lot0 += lp.per_chunk) {
+            const int32_t nl = (int32_t)(lp.nlots - lot0 < lp.per_chunk ? lp.nlots - lot0 : lp.per_chunk);
+            const int32_t ntype = nl * ngroup;
+            int64_t m = 0;
+            rc = dgpu_lot_gather(ctx, lp, lot0, nl, cr->pos, eiscat, cr->atom_occ, &m);
+            if (rc) return rc;
+            FoldSpec nofold = {0, 1, {1, 1, 1}, {0, 0, 0}, nullptr};
+            rc = dgpu_prepare_atoms(ctx, ctx->lpos.as<double>(), ctx->ltype.as<int32_t>(),
+                                    cr->atom_occ ? ctx->locc.as<float>() : nullptr, m, ntype, geo, nofold, ctx->ph0,
+                                    ctx->du, ctx->dv, ctx->dw, ctx->w, ts);
+            if (rc) return rc;
+            int64_t nat = 0;
+            for (int t = 0; t < ntype; t++) nat += ts[ntype + 1 + t];
+            pairs += nat * np;
+            PartRef pref;
+            memset(&pref, 0, sizeof(pref));
+            DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
+            if (nat > 0) {
+                rc = engine_sums(ctx, engine, ctx->ph0, ctx->du, ctx->dv, ctx->dw, ctx->w, ts, ntype, op, box,
+                                 ctx->part, &pref);
+                if (rc) return rc;
+            }
+            DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
+            const int32_t last = lot0 + nl == lp.nlots ? nl - 1 : -1;
+            rc = dgpu_lot_combine(ctx, ngroup, nl, box, nat > 0 ? &pref : nullptr, ctx->lfac.as<double2>(), acsf_in,
+                                  d_csf, d_dsi, last);
+            if (rc) return rc;
+            DGPU_CUDA(ctx, cudaEventSynchronize(ctx->ev[3]));
+            float ms = 0.f;
+            DGPU_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]));
+            kernel_ms += ms;
+            if (cancelled(op)) return dgpu_set_error(ctx, DGPU_ERR_CANCELLED, "cancelled");
+        }
+        // dsi * icc1*icc2*icc3 / (ncell*nlots) when nlots != 1 (fourier_sup.f90:273-277)
+        double dnorm = 1.0;
+        if (lp.nlots != 1)
+            dnorm = (double)((int64_t)cr->icc[0] * cr->icc[1] * cr->icc[2]) / (double)((int64_t)lp.ncell * lp.nlots);
+        rc = dgpu_lot_scale(ctx, box, d_csf, d_dsi, dnorm * op->diff_scale, sqrt(op->diff_scale));
+        if (rc) return rc;
     }
+    if (!ctx->fs_main) ctx->fs_main = new FormSpec();
+    *ctx->fs_main = fsm;
     if (cancelled(op)) return dgpu_set_error(ctx, DGPU_ERR_CANCELLED, "cancelled");
     rc = dgpu_friedel_mirror(ctx, box, idim, d_csf, d_acsf, d_dsi);
     if (rc) return rc;
@@ -320,8 +464,7 @@ int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g,
         for (int k = 0; k < 9; k++) info->off_shift[k] = geo.off[k];
         info->ncell = ncell;
         info->engine_used = engine;
-        info->pairs = 0;
-        for (int t = 0; t < cr->nscat; t++) info->pairs += ts[cr->nscat + 1 + t] * np;
+        info->pairs = pairs;
         info->pairs_aver = pairs_aver;
         for (int k = 0; k < 7; k++) info->res[k] = res[k];
         info->kernel_ms = kernel_ms;
@@ -367,6 +510,11 @@ extern "C" int dgpu_four_run(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_g
         DGPU_CUDA(ctx, ctx->aocc.ensure(n * sizeof(float)));
         DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->aocc.p, cr->atom_occ, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
         dc.atom_occ = ctx->aocc.as<float>();
+    }
+    if (cr->is_anis) {
+        DGPU_CUDA(ctx, ctx->ianis.ensure(n * sizeof(int32_t)));
+        DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->ianis.p, cr->ianis, n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+        dc.ianis = ctx->ianis.as<int32_t>();
     }
     DGPU_CUDA(ctx, ctx->csf.ensure(np * sizeof(double2)));
     DGPU_CUDA(ctx, ctx->acsf.ensure(np * sizeof(double2)));
@@ -452,6 +600,8 @@ extern "C" int dgpu_four_strucf(dgpu_ctx *ctx, const double *xat, int64_t nxat, 
         memset(&fs, 0, sizeof(fs));
         fs.mode = DGPU_FORM_TABLE;
         fs.nscat = 1;
+        fs.ngroup = 1;
+        fs.gtype[1] = 1;
         PartRef pref = {ctx->part.p, nslice, 0};
         rc = dgpu_combine(ctx, fs, box, pref, ctx->istl.as<int32_t>(),
                           ctx->cfact.as<double2>(), nullptr, ctx->csf.as<double2>(), ctx->dsi.as<double>(), 1.0);

@@ -57,6 +57,7 @@ struct TcChoice {
 typedef std::tuple<int32_t, int32_t, int32_t, int32_t, int32_t, int32_t, int32_t> TcKey;
 
 struct BatchState;   // k_batch.cu
+struct FormSpec;
 
 struct dgpu_ctx {
     int device = 0;
@@ -75,6 +76,9 @@ struct dgpu_ctx {
     DevBuf tc_vimg;                         // V operand images of the tensor-core engine
     DevBuf adj_qimg, adj_items;             // tensor-core adjoint: Q images, work items
     int64_t ts_main[2 * 64 + 4] = {};      // type ranges of the last main atom preparation
+    DevBuf ianis, geff, ghist;              // ADP types, group of every atom, (type, ADP) histogram
+    DevBuf lpos, ltype, locc, lplan, lfac;  // lot crystals, lot plan, group factors
+    FormSpec *fs_main = nullptr;            // host copy of the last main combine's FormSpec
     DevBuf gq, gpart, grad, batch_desc, batch_aux;
     double batch_ms = 0.0;
     double tc_kernel_ms = 0.0;              // duration of the last single-problem tensor-core launch
@@ -230,14 +234,24 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
 bool dgpu_tc_available(dgpu_ctx *ctx);
 
 // epilogue.cu -----------------------------------------------------------
+// Form factors of the combine and adjoint kernels.  The partial sums come
+// per group g = 1..ngroup: a scattering type (isotropic crystal, gtype[g] = g)
+// or a (type, ADP type) pair of an anisotropic crystal, whose factor is
+// cfact(gtype[g]) times, when adbw, exp(-2 pi^2 h^T (a*_i a*_j U_ij) h) with
+// the group's U (four_dbwtab, fourier_sup.f90:2809-2831).  ldbw here is the
+// isotropic term inside cfact: off for an anisotropic crystal (:2729).
 struct FormSpec {
     int32_t mode;          // DGPU_FORM_*
     int32_t nscat;
     int32_t lxray, power, ano, ldbw;
+    int32_t ngroup, adbw;
+    int32_t gtype[64];     // group -> scattering type
     double scat[64 * 11];  // per type coefficients (types 1..nscat, <=63)
     double occ[64], dw[64], delfr[64], delfi[64];
     double rten[9];
     double eck[3], vi[9];
+    double gU[64 * 6];     // U11, U22, U33, U23, U13, U12 of each group (A^2)
+    double ar[3];          // reciprocal cell lengths (1/A)
 };
 // Partial sums part[t][s][p] of either engine: double2 (direct) or float2 (TC).
 // Element (point i,j,l of the box, type t, slice k) at

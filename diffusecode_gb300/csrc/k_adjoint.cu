@@ -4,7 +4,9 @@
 // REFINE and RMC obtain by re-running whole macros
 // (refine/prog/refine_run.f90:491-759).
 //
-// With I = ds |F|^2, F = sum_t c_t(h) sum_j w_j exp(2 pi i h.r_j):
+// With I = ds |F|^2, F = sum_t c_t(h) sum_j w_j exp(2 pi i h.r_j) (t runs over
+// the forward pass's groups: types, or (type, ADP type) pairs whose c_t
+// carries the anisotropic Debye-Waller term):
 //   dchi2/dw_j   = Re T0_j
 //   dchi2/dr_j,k = -2 pi w_j ( eck_k Im T0_j + sum_a vi_a,k Im T_a,j )
 //   T0_j  = sum_h Q_t(h) exp(2 pi i h.r_j),  T_a,j = sum_h n_a(h) Q_t(h) exp(...)
@@ -16,7 +18,7 @@
 // pass; phasors in FP32, sums in FP32 over 256-point tiles and FP64 across.
 #include <math.h>
 
-#include "dgpu_internal.h"
+#include "dgpu_form.cuh"
 
 #define ADJ_NT 128
 #define ADJ_TP 256
@@ -72,32 +74,10 @@ __global__ void k_adj_q(const FormSpec *fs, BoxSpec box, int32_t halved, const d
     const double2 f = csf[idx];
     const double sc = 2.0 * sqds * G;
     double h[3];
-    if (fs->mode != DGPU_FORM_TABLE)
-        for (int k = 0; k < 3; k++)
-            h[k] = __dadd_rn(__dadd_rn(__dadd_rn(fs->eck[k], __dmul_rn(fs->vi[k], (double)c[0])),
-                                       __dmul_rn(fs->vi[3 + k], (double)c[1])),
-                             __dmul_rn(fs->vi[6 + k], (double)c[2]));
-    for (int t = 1; t <= fs->nscat; t++) {
-        double cr, ci;
-        if (fs->mode == DGPU_FORM_TABLE) {
-            const double2 cc = cfact[(int64_t)(t - 1) * DGPU_NTAB + istl[idx]];
-            cr = cc.x;
-            ci = cc.y;
-        } else {
-            const double *r = fs->rten;
-            const double t0 = r[0] * h[0] + r[3] * h[1] + r[6] * h[2];
-            const double t1 = r[1] * h[0] + r[4] * h[1] + r[7] * h[2];
-            const double t2 = r[2] * h[0] + r[5] * h[1] + r[8] * h[2];
-            const double q2 = (h[0] * t0 + h[1] * t1 + h[2] * t2) / 4.0;
-            const double *s = fs->scat + 11 * t;
-            double ff = s[0];
-            if (fs->lxray)
-                for (int i = 1; i <= fs->power; i++) ff += s[2 * i - 1] * exp(-s[2 * i] * q2);
-            const double fp = fs->ano ? fs->delfr[t] : 0.0, fpp = fs->ano ? fs->delfi[t] : 0.0;
-            const double sb = fs->ldbw ? exp(-fs->dw[t] * q2) * fs->occ[t] : fs->occ[t];
-            cr = sb * (ff + fp);
-            ci = sb * fpp;
-        }
+    if (form_needs_h(fs)) form_hvec(fs, c[0], c[1], c[2], h);
+    for (int t = 1; t <= fs->ngroup; t++) {
+        const double2 cc = form_group(fs, cfact, istl[idx], t, h);
+        const double cr = cc.x, ci = cc.y;
         // conj(f) * c = (fr - i fi)(cr + i ci)
         const double qr = sc * (f.x * cr + f.y * ci);
         const double qi = sc * (f.x * ci - f.y * cr);
@@ -187,6 +167,8 @@ int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
     if (op->ano) return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "gradient with anomalous scattering");
     if (op->phase != DGPU_PHASE_EXACT64)
         return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "gradient needs EXACT64 phases");
+    if (op->ilots == DGPU_LOT_BOX || op->ilots == DGPU_LOT_ELI)
+        return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "gradient with lots");
     const int64_t n = cr->natoms;
     const int64_t np = (int64_t)grid->inc[0] * grid->inc[1] * grid->inc[2];
     // forward pass with host inputs
@@ -201,6 +183,11 @@ int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
         DGPU_CUDA(ctx, ctx->aocc.ensure(n * sizeof(float)));
         DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->aocc.p, cr->atom_occ, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
         dc.atom_occ = ctx->aocc.as<float>();
+    }
+    if (cr->is_anis) {
+        DGPU_CUDA(ctx, ctx->ianis.ensure(n * sizeof(int32_t)));
+        DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->ianis.p, cr->ianis, n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+        dc.ianis = ctx->ianis.as<int32_t>();
     }
     DGPU_CUDA(ctx, ctx->csf.ensure(np * sizeof(double2)));
     DGPU_CUDA(ctx, ctx->acsf.ensure(np * sizeof(double2)));
@@ -233,12 +220,13 @@ int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
         box.num[k] = grid->inc[k];
     }
     const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
-    FormSpec fs;
-    dgpu_fill_formspec(ctx, cr, op, grid, fs);
+    // the forward pass's groups: types, or (type, ADP type) pairs
+    const FormSpec fs = *ctx->fs_main;
+    const int32_t ngroup = fs.ngroup;
     DGPU_CUDA(ctx, ctx->stats.ensure(sizeof(FormSpec)));
     FormSpec *d_fs = ctx->stats.as<FormSpec>();
     DGPU_CUDA(ctx, cudaMemcpyAsync(d_fs, &fs, sizeof(FormSpec), cudaMemcpyHostToDevice, ctx->stream));
-    DGPU_CUDA(ctx, ctx->gpart.ensure((size_t)cr->nscat * nb * sizeof(float2)));
+    DGPU_CUDA(ctx, ctx->gpart.ensure((size_t)ngroup * nb * sizeof(float2)));
     k_adj_q<<<(unsigned)dgpu_cdiv(nb, 256), 256, 0, ctx->stream>>>(
         d_fs, box, fwd.friedel_dim, d_g, ctx->csf.as<double2>(), ctx->istl.as<int32_t>(), ctx->cfact.as<double2>(),
         sqrt(op->diff_scale), ctx->gpart.as<float2>());
@@ -259,12 +247,12 @@ int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
     const int64_t *ts = ctx->ts_main;
     if (fwd.engine_used == DGPU_ENGINE_TC) {
         // same sums on the tensor cores, with the forward pass's engine
-        rc = dgpu_adjtc_sums(ctx, box, grid, cr->nscat, ts, ctx->ph0.as<uint64_t>(), ctx->du.as<uint64_t>(),
+        rc = dgpu_adjtc_sums(ctx, box, grid, ngroup, ts, ctx->ph0.as<uint64_t>(), ctx->du.as<uint64_t>(),
                              ctx->dv.as<uint64_t>(), ctx->dw.as<uint64_t>(), ctx->w.as<float>(),
                              ctx->aidx.as<int32_t>(), ctx->gpart.as<float2>(), d_gpos, d_gocc);
         if (rc) return rc;
     } else {
-        for (int t = 0; t < cr->nscat; t++) {
+        for (int t = 0; t < ngroup; t++) {
             const int64_t lo = ts[t], hi = ts[t + 1];
             if (hi <= lo) continue;
             k_adj_atoms<<<(unsigned)dgpu_cdiv(hi - lo, ADJ_NT), ADJ_NT, 0, ctx->stream>>>(

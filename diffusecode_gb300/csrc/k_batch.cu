@@ -327,12 +327,16 @@ extern "C" int dgpu_batch_run(dgpu_ctx *ctx, int32_t nc, const dgpu_crystal *crs
     if (!ctx || nc < 1 || !crs || !grids || !op || !dsi) return DGPU_ERR_ARG;
     if (op->phase != DGPU_PHASE_EXACT64 || op->fave != 0.0 || op->ano)
         return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "batch: EXACT64 phases, no <F>, no anomalous scattering");
+    if (op->ilots == DGPU_LOT_BOX || op->ilots == DGPU_LOT_ELI)
+        return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "batch: lots are run by dgpu_four_run");
     if (!dgpu_tc_available(ctx)) return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "batch needs the tensor-core engine");
     const bool targets = i_target != nullptr;
     if (targets && !chi2) return dgpu_set_error(ctx, DGPU_ERR_ARG, "chi2 output missing");
     for (int c = 0; c < nc; c++) {
         if (crs[c].natoms < 1 || !crs[c].pos || !crs[c].iscat || crs[c].nscat < 1 || crs[c].nscat > 63)
             return dgpu_set_error(ctx, DGPU_ERR_ARG, "batch member %d: bad crystal", c);
+        if (crs[c].is_anis)
+            return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "batch member %d: anisotropic ADPs are run by dgpu_four_run", c);
         if (!dsi[c] || (targets && !i_target[c])) return dgpu_set_error(ctx, DGPU_ERR_ARG, "member %d: buffers", c);
         for (int k = 0; k < 3; k++)
             if (grids[c].inc[k] < 1) return dgpu_set_error(ctx, DGPU_ERR_ARG, "member %d: inc", c);

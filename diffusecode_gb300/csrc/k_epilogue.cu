@@ -1,7 +1,10 @@
-// Epilogue kernels of four_run (discus/prog/fourier_sup.f90:224-294):
-//   * combine: csf = sum_t cfact_t(point) * S_t - acsf ; dsi = |csf|^2
-//     (tcsf_form_iso, fourier_form.f90:147-177; fourier_sup.f90:232,250-254),
-//     with diff_scale applied (fourier_sup.f90:281-282);
+// Epilogue kernels of four_run (discus/prog/fourier_sup.f90:136-294):
+//   * combine: csf = sum_g factor_g(point) * S_g - acsf ; dsi = |csf|^2
+//     (tcsf_form_iso / tcsf_form_aniso, fourier_form.f90:106-177;
+//     fourier_sup.f90:205,232,250-254), with diff_scale applied
+//     (fourier_sup.f90:281-282);
+//   * lots: the same per lot of a chunk, dsi accumulated over the lots and
+//     normalised by icc1*icc2*icc3 / (ncell*nlots) (fourier_sup.f90:136-277);
 //   * <F>: acsf = (sum_t cfact_t * Savg_t) * lattice / ncell
 //     (four_aver, fourier_sup.f90:1194-1357); the lattice sum is either the
 //     direct sum over all cells or its closed form (a product of three
@@ -9,34 +12,8 @@
 //   * Friedel mirror (four_apply_friedel, fourier_sup.f90:3726-3757), with the
 //     net effect of its sequential in-place loop on the middle slab;
 //   * four_qinfo statistics (fourier_sup.f90:2859-2942).
-#include "dgpu_internal.h"
-
-__device__ __forceinline__ void hvec(const FormSpec *fs, int64_t i, int64_t j, int64_t l, double h[3])
-{
-    for (int k = 0; k < 3; k++)
-        h[k] = __dadd_rn(__dadd_rn(__dadd_rn(fs->eck[k], __dmul_rn(fs->vi[k], (double)i)),
-                                   __dmul_rn(fs->vi[3 + k], (double)j)),
-                         __dmul_rn(fs->vi[6 + k], (double)l));
-}
-
-// cfact of type t (1-based) at a point: table or exact sin(theta)/lambda
-__device__ __forceinline__ double2 cfact_at(const FormSpec *fs, const double2 *cfact, int32_t istl,
-                                            int t, const double h[3])
-{
-    if (fs->mode == DGPU_FORM_TABLE) return cfact[(int64_t)(t - 1) * DGPU_NTAB + istl];
-    const double *r = fs->rten;
-    double t0 = __dadd_rn(__dadd_rn(__dmul_rn(r[0], h[0]), __dmul_rn(r[3], h[1])), __dmul_rn(r[6], h[2]));
-    double t1 = __dadd_rn(__dadd_rn(__dmul_rn(r[1], h[0]), __dmul_rn(r[4], h[1])), __dmul_rn(r[7], h[2]));
-    double t2 = __dadd_rn(__dadd_rn(__dmul_rn(r[2], h[0]), __dmul_rn(r[5], h[1])), __dmul_rn(r[8], h[2]));
-    double q2 = __dadd_rn(__dadd_rn(__dmul_rn(h[0], t0), __dmul_rn(h[1], t1)), __dmul_rn(h[2], t2)) / 4.0;
-    const double *sc = fs->scat + 11 * t;
-    double f = sc[0];
-    if (fs->lxray)
-        for (int i = 1; i <= fs->power; i++) f = __dadd_rn(f, __dmul_rn(sc[2 * i - 1], exp(-__dmul_rn(sc[2 * i], q2))));
-    double fp = fs->ano ? fs->delfr[t] : 0.0, fpp = fs->ano ? fs->delfi[t] : 0.0;
-    double sb = fs->ldbw ? __dmul_rn(exp(-__dmul_rn(fs->dw[t], q2)), fs->occ[t]) : fs->occ[t];
-    return make_double2(__dmul_rn(sb, __dadd_rn(f, fp)), __dmul_rn(sb, fpp));
-}
+#include "dgpu_form.cuh"
+#include "dgpu_lots.h"
 
 __device__ __forceinline__ double2 cmul(double2 a, double2 b)
 {
@@ -76,10 +53,10 @@ __global__ void k_combine(const FormSpec *fs, BoxSpec box, const P *__restrict__
     int64_t i = pb % box.f[0], j = (pb / box.f[0]) % box.f[1], l = pb / ((int64_t)box.f[0] * box.f[1]);
     int64_t idx = i + (int64_t)box.num[0] * (j + (int64_t)box.num[1] * l);
     double h[3];
-    if (fs->mode != DGPU_FORM_TABLE) hvec(fs, i, j, l, h);
+    if (form_needs_h(fs)) form_hvec(fs, i, j, l, h);
     int32_t q = istl ? istl[idx] : 0;
     double2 F = make_double2(0.0, 0.0);
-    for (int t = 1; t <= fs->nscat; t++) {
+    for (int t = 1; t <= fs->ngroup; t++) {
         double2 s = make_double2(0.0, 0.0);
         const P *pt = part + (int64_t)(t - 1) * nslice * lay.slab + i * lay.s0 + j * lay.s1 + l * lay.s2;
         for (int k = 0; k < nslice; k++) {
@@ -87,7 +64,7 @@ __global__ void k_combine(const FormSpec *fs, BoxSpec box, const P *__restrict__
             s.x += v.x;
             s.y += v.y;
         }
-        double2 c = cfact_at(fs, cfact, q, t, h);
+        double2 c = form_group(fs, cfact, q, t, h);
         double2 m = cmul(s, c);
         F.x += m.x;
         F.y += m.y;
@@ -127,7 +104,7 @@ __global__ void k_aver_combine(const FormSpec *fs, BoxSpec box, const P *__restr
     int64_t idx = i + (int64_t)box.num[0] * (j + (int64_t)box.num[1] * l);
     int64_t nfull = (int64_t)box.num[0] * box.num[1] * box.num[2];
     double h[3];
-    hvec(fs, i, j, l, h);
+    form_hvec(fs, i, j, l, h);
     int32_t q = istl ? istl[idx] : 0;
     double2 A = make_double2(0.0, 0.0);
     for (int t = 1; t <= fs->nscat; t++) {
@@ -138,7 +115,7 @@ __global__ void k_aver_combine(const FormSpec *fs, BoxSpec box, const P *__restr
             s.x += v.x;
             s.y += v.y;
         }
-        double2 m = cmul(s, cfact_at(fs, cfact, q, t, h));
+        double2 m = cmul(s, form_cfact(fs, cfact, q, t, h));
         A.x += m.x;
         A.y += m.y;
     }
@@ -385,6 +362,119 @@ int dgpu_combine_async(dgpu_ctx *ctx, const FormSpec *d_fs, const BoxSpec &box, 
         k_combine<double2><<<nblk, 256, 0, ctx->stream>>>(d_fs, box, (const double2 *)part.p, part.nslice, lay,
                                                            istl, cfact, nullptr, csf, dsi, diff_scale,
                                                            sqrt(diff_scale));
+    DGPU_CUDA(ctx, cudaGetLastError());
+    return DGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Lots (fourier_sup.f90:136-277).  The group factors do not depend on the
+// lot: they are tabulated once per run on the box, fac[(g-1)*nb + box point].
+__global__ void k_group_factors(const FormSpec *fs, BoxSpec box, const int32_t *__restrict__ istl,
+                                const double2 *__restrict__ cfact, double2 *__restrict__ fac)
+{
+    const int64_t pb = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    if (pb >= nb) return;
+    const int64_t i = pb % box.f[0], j = (pb / box.f[0]) % box.f[1], l = pb / ((int64_t)box.f[0] * box.f[1]);
+    const int64_t idx = i + (int64_t)box.num[0] * (j + (int64_t)box.num[1] * l);
+    double h[3];
+    if (form_needs_h(fs)) form_hvec(fs, i, j, l, h);
+    const int32_t q = istl ? istl[idx] : 0;
+    for (int g = 1; g <= fs->ngroup; g++) fac[(int64_t)(g - 1) * nb + pb] = form_group(fs, cfact, q, g, h);
+}
+
+// One chunk of nlot lots whose partial sums come as nlot*ngroup types (lot-
+// major): dsi += sum_L |sum_g fac_g S_{L,g} - acsf|^2 (unscaled) and, for the
+// chunk's lot `last` (-1: none), csf = its F - acsf (unscaled).  part == null:
+// the chunk has no atoms.
+template <class P>
+__global__ void k_lot_combine(int32_t ngroup, int32_t nlot, BoxSpec box, const P *__restrict__ part,
+                              int32_t nslice, PartLayout lay, const double2 *__restrict__ fac,
+                              const double2 *__restrict__ acsf, double2 *__restrict__ csf,
+                              double *__restrict__ dsi, int32_t last)
+{
+    const int64_t pb = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    if (pb >= nb) return;
+    const int64_t i = pb % box.f[0], j = (pb / box.f[0]) % box.f[1], l = pb / ((int64_t)box.f[0] * box.f[1]);
+    const int64_t idx = i + (int64_t)box.num[0] * (j + (int64_t)box.num[1] * l);
+    const double2 a = acsf ? acsf[idx] : make_double2(0.0, 0.0);
+    const int64_t off = i * lay.s0 + j * lay.s1 + l * lay.s2;
+    double acc = 0.0;
+    for (int L = 0; L < nlot; L++) {
+        double2 F = make_double2(0.0, 0.0);
+        if (part)
+            for (int g = 0; g < ngroup; g++) {
+                const P *pt = part + (int64_t)(L * ngroup + g) * nslice * lay.slab + off;
+                double2 s = make_double2(0.0, 0.0);
+                for (int k = 0; k < nslice; k++) {
+                    const double2 v = ld_part(pt + (int64_t)k * lay.slab);
+                    s.x += v.x;
+                    s.y += v.y;
+                }
+                const double2 m = cmul(s, fac[(int64_t)g * nb + pb]);
+                F.x += m.x;
+                F.y += m.y;
+            }
+        F.x -= a.x;
+        F.y -= a.y;
+        acc += F.x * F.x + F.y * F.y;
+        if (L == last) csf[idx] = F;
+    }
+    dsi[idx] += acc;
+}
+
+// dsi *= dscale, csf *= cscale on the box (lot normalisation and diff_scale)
+__global__ void k_lot_scale(BoxSpec box, double2 *__restrict__ csf, double *__restrict__ dsi, double dscale,
+                            double cscale)
+{
+    const int64_t pb = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    if (pb >= nb) return;
+    const int64_t i = pb % box.f[0], j = (pb / box.f[0]) % box.f[1], l = pb / ((int64_t)box.f[0] * box.f[1]);
+    const int64_t idx = i + (int64_t)box.num[0] * (j + (int64_t)box.num[1] * l);
+    dsi[idx] *= dscale;
+    const double2 c = csf[idx];
+    csf[idx] = make_double2(c.x * cscale, c.y * cscale);
+}
+
+int dgpu_group_factors(dgpu_ctx *ctx, const FormSpec &fs, const BoxSpec &box, const int32_t *istl,
+                       const double2 *cfact, double2 *fac)
+{
+    FormSpec *d;
+    int rc = upload_formspec(ctx, fs, &d);
+    if (rc) return rc;
+    const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    k_group_factors<<<(unsigned)dgpu_cdiv(nb, 256), 256, 0, ctx->stream>>>(d, box, istl, cfact, fac);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));   // FormSpec block reused next
+    return DGPU_OK;
+}
+
+int dgpu_lot_combine(dgpu_ctx *ctx, int32_t ngroup, int32_t nlot, const BoxSpec &box, const PartRef *part,
+                     const double2 *fac, const double2 *acsf, double2 *csf, double *dsi, int32_t last)
+{
+    const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    const unsigned nblk = (unsigned)dgpu_cdiv(nb, 256);
+    PartRef none;
+    memset(&none, 0, sizeof(none));
+    const PartRef &r = part ? *part : none;
+    const PartLayout lay = layout_of(r, box);
+    const int32_t nslice = r.nslice > 0 ? r.nslice : 1;
+    if (r.f32)
+        k_lot_combine<float2><<<nblk, 256, 0, ctx->stream>>>(ngroup, nlot, box, (const float2 *)r.p, nslice, lay,
+                                                              fac, acsf, csf, dsi, last);
+    else
+        k_lot_combine<double2><<<nblk, 256, 0, ctx->stream>>>(ngroup, nlot, box, (const double2 *)r.p, nslice,
+                                                               lay, fac, acsf, csf, dsi, last);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    return DGPU_OK;
+}
+
+int dgpu_lot_scale(dgpu_ctx *ctx, const BoxSpec &box, double2 *csf, double *dsi, double dscale, double cscale)
+{
+    const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    k_lot_scale<<<(unsigned)dgpu_cdiv(nb, 256), 256, 0, ctx->stream>>>(box, csf, dsi, dscale, cscale);
     DGPU_CUDA(ctx, cudaGetLastError());
     return DGPU_OK;
 }

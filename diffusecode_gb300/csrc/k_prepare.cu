@@ -384,7 +384,7 @@ int dgpu_formtab_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *op,
     DGPU_CUDA(ctx, cudaMemcpyAsync(d, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->stream));
     int64_t n = (int64_t)cr->nscat * DGPU_NTAB;
     k_formtab<<<(unsigned)dgpu_cdiv(n, 256), 256, 0, ctx->stream>>>(d, cr->nscat, op->lxray, op->power,
-                                                                      op->ano, op->ldbw, d_cfact);
+                                                                      op->ano, op->ldbw && !cr->is_anis, d_cfact);
     DGPU_CUDA(ctx, cudaGetLastError());
     // the coefficient block lives in ctx->stats: finish before it is reused
     DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

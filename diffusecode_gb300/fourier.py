@@ -41,7 +41,25 @@ def _cplx(buf, shape):
     return (buf[0::2] + 1j * buf[1::2]).reshape(shape, order="F")
 
 
-def four_run(cr: CrystalData, grid: GridData, opts: _abi.Opts, ctx=None, aver_cells=None):
+def attach_selections(opts: _abi.Opts, aver_cells=None, lot_origins=None):
+    """Points opts at the caller's random draws: the <F> cell selection
+    cells(csize1,csize2,csize3) (fourier_sup.f90:1235-1241) and the lot origins
+    lbeg(3,nlots), 1-based (four_ranloc, fourier_sup.f90:2513-2530).  Returns
+    the arrays, which must stay alive while opts is used."""
+    keep = []
+    if aver_cells is not None:
+        a = np.ascontiguousarray(np.asarray(aver_cells, dtype=np.uint8).reshape(-1, order="F"))
+        opts.aver_cells = a.ctypes.data_as(C.POINTER(C.c_uint8))
+        keep.append(a)
+    if lot_origins is not None:
+        o = np.ascontiguousarray(np.asarray(lot_origins, dtype=np.int32).reshape(-1, 3))
+        opts.lot_origins = _abi.iptr(o)
+        opts.nlots = o.shape[0]
+        keep.append(o)
+    return keep
+
+
+def four_run(cr: CrystalData, grid: GridData, opts: _abi.Opts, ctx=None, aver_cells=None, lot_origins=None):
     """four_run (discus/prog/fourier_sup.f90:11-323) on the GPU."""
     ctx = ctx or default_context()
     np_ = grid.npoints
@@ -51,10 +69,7 @@ def four_run(cr: CrystalData, grid: GridData, opts: _abi.Opts, ctx=None, aver_ce
     info = _abi.Info()
     c = cr.to_c()
     g = grid.to_c()
-    keep = None
-    if aver_cells is not None:
-        keep = np.ascontiguousarray(np.asarray(aver_cells, dtype=np.uint8).reshape(-1, order="F"))
-        opts.aver_cells = keep.ctypes.data_as(C.POINTER(C.c_uint8))
+    keep = attach_selections(opts, aver_cells, lot_origins)
     rc = ctx.check(ctx.lib.dgpu_four_run(ctx.h, C.byref(c), C.byref(g), C.byref(opts), _abi.dptr(csf),
                                          _abi.dptr(acsf), _abi.dptr(dsi), C.byref(info)))
     del keep

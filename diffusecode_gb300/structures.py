@@ -56,6 +56,11 @@ class CrystalData:
     delfi: np.ndarray | None = None
     atom_occ: np.ndarray | None = None   # (natoms,) float32, not part of DISCUS
     name: str = ""
+    # anisotropic ADPs (crystal_mod cr_is_anis, cr_iscat(3,:), cr_anis_full, cr_ar)
+    ianis: np.ndarray | None = None      # (natoms,) int32, ADP type 1..nanis
+    anis_full: np.ndarray | None = None  # (nanis, 6) U11 U22 U33 U23 U13 U12, A^2
+    ar: tuple = (0.0, 0.0, 0.0)          # reciprocal cell lengths, 1/A
+    dim_lo: tuple | None = None          # cr_dim(:,1); None = min over the positions
     _keep: list = field(default_factory=list, repr=False)
 
     def __post_init__(self):
@@ -71,6 +76,15 @@ class CrystalData:
             self.delfi = np.zeros(self.nscat + 1)
         if self.atom_occ is not None:
             self.atom_occ = np.ascontiguousarray(self.atom_occ, dtype=np.float32)
+        if self.ianis is not None:
+            self.ianis = np.ascontiguousarray(self.ianis, dtype=np.int32)
+            self.anis_full = np.ascontiguousarray(np.asarray(self.anis_full, dtype=np.float64).reshape(-1, 6))
+        if self.dim_lo is None:
+            self.dim_lo = tuple(float(x) for x in self.pos.min(axis=0)) if len(self.pos) else (0.0, 0.0, 0.0)
+
+    @property
+    def is_anis(self):
+        return self.ianis is not None
 
     @property
     def natoms(self):
@@ -79,7 +93,7 @@ class CrystalData:
     def n_scattering(self):
         return int(np.count_nonzero((self.iscat >= 1) & (self.iscat <= self.nscat)))
 
-    def to_c(self, pos_ptr=None, iscat_ptr=None, occ_ptr=None):
+    def to_c(self, pos_ptr=None, iscat_ptr=None, occ_ptr=None, ianis_ptr=None):
         """Fill a dgpu_crystal; pointer overrides allow device arrays."""
         cr = _abi.Crystal()
         cr.natoms = self.natoms
@@ -102,6 +116,14 @@ class CrystalData:
         cr.dw = _abi.dptr(self.dw)
         cr.delfr = _abi.dptr(self.delfr)
         cr.delfi = _abi.dptr(self.delfi)
+        for k in range(3):
+            cr.ar[k] = float(self.ar[k])
+            cr.dim_lo[k] = float(self.dim_lo[k])
+        if self.ianis is not None:
+            cr.is_anis = 1
+            cr.nanis = int(self.anis_full.shape[0])
+            cr.ianis = ianis_ptr if ianis_ptr is not None else _abi.iptr(self.ianis)
+            cr.anis_full = _abi.dptr(self.anis_full)
         return cr
 
     def with_positions(self, pos, atom_occ=None):
@@ -109,7 +131,8 @@ class CrystalData:
                            icc=self.icc, rten=self.rten, scat=self.scat, occ=self.occ,
                            dw=self.dw, dim0=self.dim0, delfr=self.delfr, delfi=self.delfi,
                            atom_occ=self.atom_occ if atom_occ is None else atom_occ,
-                           name=self.name)
+                           name=self.name, ianis=self.ianis, anis_full=self.anis_full, ar=self.ar,
+                           dim_lo=self.dim_lo)
 
 
 @dataclass
@@ -406,4 +429,56 @@ def small_random(seed=0, natoms=64, nscat=2, inc=(9, 7, 3), span=3.0):
     cr = CrystalData(pos=pos, iscat=iscat, nscat=nscat, ncatoms=1, icc=(natoms, 1, 1),
                      rten=reciprocal_metric(4.1, 4.3, 5.2, 88, 92, 95), scat=scat, occ=occ, dw=dw,
                      name="small-random")
+    return cr, grid
+
+
+def small_lots_anis(seed=7, icc=(5, 4, 3), nextra=4, inc=(13, 11, 5), anis=True, lxray=True):
+    """Small orthorhombic crystal (a, b, c = 4.0, 4.5, 5.0 A) for the ADP and
+    lot paths: two sites per cell, two types, one VOID site, cell origins from
+    dim0 = (-2, -2, -1); with anis, three ADP types (type 1 split over ADPs 1
+    and 3); nextra interstitial atoms stored after the periodic block (the
+    atoms four_getatm places in lots by INT(pos)).  The grid is centred on 0
+    with odd counts, so Friedel halving applies."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    a_lat = np.array([4.0, 4.5, 5.0])
+    dim0 = (-2.0, -2.0, -1.0)
+    sites = [[0.1, 0.2, 0.3], [0.55, 0.45, 0.6]]
+    pos, iscat = build_periodic(sites, [1, 2], icc, a_lat, rng, sigma_ang=0.05)
+    pos = pos + np.asarray(dim0)
+    iscat[rng.integers(0, iscat.shape[0])] = 0
+    ncell = int(np.prod(icc))
+    if nextra:
+        cells = rng.integers(0, ncell, size=nextra)
+        cx = np.stack([cells % icc[0], (cells // icc[0]) % icc[1], cells // (icc[0] * icc[1])], axis=1)
+        extra = cx + np.asarray(dim0) + rng.uniform(0.05, 0.95, size=(nextra, 3))
+        pos = np.concatenate([pos, extra])
+        iscat = np.concatenate([iscat, rng.integers(1, 3, size=nextra).astype(np.int32)])
+    scat, occ, dw = random_form_factors(rng, 2, b_iso=0.6)
+    occ[1:] = [0.9, 0.75]
+    if not lxray:
+        scat[:, 1:] = 0.0
+    cr = CrystalData(pos=pos, iscat=iscat.astype(np.int32), nscat=2, ncatoms=2, icc=icc,
+                     rten=reciprocal_metric(*a_lat, 90, 90, 90), scat=scat, occ=occ, dw=dw, dim0=dim0,
+                     ar=tuple(1.0 / a_lat), name="small-lots-anis")
+    if anis:
+        ianis = np.where(iscat == 2, 2, 1).astype(np.int32)
+        ianis[(iscat == 1) & (rng.random(iscat.shape[0]) < 0.4)] = 3
+        U = np.array([[0.010, 0.014, 0.008, 0.002, -0.001, 0.003],
+                      [0.020, 0.012, 0.016, -0.003, 0.002, 0.001],
+                      [0.006, 0.006, 0.006, 0.0, 0.0, 0.0]])
+        cr.ianis = ianis
+        cr.anis_full = U
+    lo = np.array([-1.2, -1.0, -0.8])
+    vi = np.diag([2.4 / (inc[0] - 1), 2.0 / (inc[1] - 1), 1.6 / (inc[2] - 1)])
+    vi[0, 1] = 0.03
+    vi[1, 0] = -0.02
+    eck = np.stack([lo, lo + vi[:, 0] * (inc[0] - 1), lo + vi[:, 1] * (inc[1] - 1), lo + vi[:, 2] * (inc[2] - 1)],
+                   axis=1)
+    # the corners must sum to 0 for Friedel: shift ll so that ll + (n-1) v = -ll
+    far = eck[:, 0] + vi @ (np.asarray(inc) - 1)
+    eck[:, 0] = eck[:, 0] - (eck[:, 0] + far) / 2
+    eck[:, 1] = eck[:, 0] + vi[:, 0] * (inc[0] - 1)
+    eck[:, 2] = eck[:, 0] + vi[:, 1] * (inc[1] - 1)
+    eck[:, 3] = eck[:, 0] + vi[:, 2] * (inc[2] - 1)
+    grid = GridData(eck=eck, vi=vi, inc=inc)
     return cr, grid

@@ -64,6 +64,11 @@ extern "C" {
 #define DGPU_ENGINE_DIRECT  1   /* FP32 direct sum on CUDA cores                 */
 #define DGPU_ENGINE_TC      2   /* tcgen05 split-precision complex GEMM          */
 
+/* Lots (diffuse_mod.f90:10-12): sub-volumes whose intensities are averaged. */
+#define DGPU_LOT_OFF        1   /* whole crystal (0 is read as OFF as well)      */
+#define DGPU_LOT_BOX        2   /* ls_xyz box of unit cells                      */
+#define DGPU_LOT_ELI        3   /* ellipsoid inscribed in that box               */
+
 /* Operand split of the tensor-core engine. */
 #define DGPU_SPLIT_F16      0   /* fp16 hi + fp16 lo, 3 products  (default)      */
 #define DGPU_SPLIT_BF16     1   /* bf16 hi + bf16 lo, 3 products                 */
@@ -87,6 +92,19 @@ typedef struct dgpu_crystal {
     const double  *dw;         /* cr_dw(0:nscat), isotropic B in A^2                     */
     const double  *delfr;      /* cr_delfr(0:nscat), f', used only when ano != 0         */
     const double  *delfi;      /* cr_delfi(0:nscat), f'', used only when ano != 0        */
+    /* Anisotropic ADPs (crystal_mod.f90:47,94,103,118).  is_anis == 0: the
+       crystal is isotropic (cr_dw in cfact) and ianis/anis_full are ignored.
+       is_anis != 0: cfact carries no Debye-Waller term and each (type, ADP)
+       group is multiplied by exp(-2 pi^2 h^T (a*_i a*_j U_ij) h) at every
+       point (four_dbwtab, fourier_sup.f90:2747-2855) when ldbw is set.      */
+    int32_t        is_anis;    /* cr_is_anis                                             */
+    int32_t        nanis;      /* cr_nanis                                               */
+    const int32_t *ianis;      /* cr_iscat(3,:), ADP type 1..nanis of each atom          */
+    const double  *anis_full;  /* cr_anis_full(6,nanis): U11,U22,U33,U23,U13,U12 in A^2  */
+    double         ar[3];      /* cr_ar, reciprocal cell lengths in 1/A                  */
+    double         dim_lo[3];  /* cr_dim(:,1), lower corner of the atom positions; lots
+                                  use it to place atoms stored after the
+                                  ncatoms*icc(1)*icc(2)*icc(3) block (fourier_sup.f90:1886-1899) */
 } dgpu_crystal;
 
 /* The reciprocal-space grid: diffuse_mod eck/vi/inc (diffuse_mod.f90:100,113-119). */
@@ -104,8 +122,9 @@ typedef struct dgpu_opts {
     int32_t ldbw;           /* 'temp use': isotropic Debye-Waller in cfact          */
     int32_t friedel;        /* four_friedel: halve the grid when allowed            */
     double  fave;           /* 'set aver': 0 off, 1 all cells; 0<fave<1 needs cells  */
-    const uint8_t *aver_cells; /* cell selection for 0<fave<1, cells(icc1,icc2,icc3),
-                                  drawn by the caller's ran1 stream (fourier_sup.f90:1235-1241) */
+    const uint8_t *aver_cells; /* cell selection for 0<fave<1, cells(csize1,csize2,csize3)
+                                  (csize = icc for a periodic crystal), drawn by the
+                                  caller's ran1 stream (fourier_sup.f90:1235-1241)   */
     double  diff_scale;     /* intensity scale (fourier_sup.f90:281-282), default 1  */
     int32_t phase;          /* DGPU_PHASE_*                                         */
     int32_t form;           /* DGPU_FORM_*                                          */
@@ -115,6 +134,15 @@ typedef struct dgpu_opts {
     int32_t tc_kslice;      /* atoms per tensor-core work item (0 = autotuned)      */
     int32_t tc_flush;       /* atoms per drain of the main TMEM accumulator (0 = 128) */
     volatile int32_t *cancel; /* optional host flag polled between atom types      */
+    /* Lots (fourier.f90:467-531, diffuse_mod.f90:75-82, defaults fourier_reset.f90:44-51). */
+    int32_t ilots;          /* DGPU_LOT_*                                           */
+    int32_t nlots;          /* number of lots (ignored with lot_all)                */
+    int32_t ls_xyz[3];      /* lot size in unit cells, 1..icc (default 5)           */
+    int32_t lot_all;        /* every origin of csize once, in DISCUS order          */
+    int32_t lperiod;        /* periodic crystal: csize = icc, else max(1,icc-ls+1)  */
+    const int32_t *lot_origins; /* lbeg(3,nlots), 1-based origin cells 1..csize, drawn
+                                  by the caller's ran1 stream as four_ranloc does
+                                  (fourier_sup.f90:2513-2530); unused with lot_all  */
 } dgpu_opts;
 
 /* What four_run reports besides the arrays. */
@@ -142,11 +170,12 @@ const char *dgpu_last_error(const dgpu_ctx *ctx);
 void dgpu_default_opts(dgpu_opts *opts);   /* fourier_reset.f90 defaults + engine AUTO */
 
 /* ---- the whole path ----------------------------------------------------- */
-/* Replaces four_run (discus/prog/fourier_sup.f90:11-323) for LOT_OFF with
- * isotropic ADPs: tables, Friedel reduction, <F> (four_aver), the per-type
- * structure-factor sums, csf -= acsf, dsi += |csf|^2, mirror, scale and
+/* Replaces four_run (discus/prog/fourier_sup.f90:11-323) for the independent
+ * atom model: tables, Friedel reduction, <F> (four_aver), the loop over lots,
+ * the per-type (isotropic) or per-(type, ADP) (anisotropic) structure-factor
+ * sums, csf -= acsf, dsi += |csf|^2, lot normalisation, mirror, scale and
  * four_qinfo statistics.  Host buffers: csf/acsf are complex num(1)*num(2)*num(3),
- * dsi is real.  acsf may be NULL.                                          */
+ * dsi is real.  acsf may be NULL.  With lots, csf is that of the last lot.  */
 int dgpu_four_run(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid,
                   const dgpu_opts *opts, double *csf, double *acsf, double *dsi,
                   dgpu_info *info);

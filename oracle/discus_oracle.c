@@ -243,14 +243,15 @@ static double oc_form(const double *scat, int t, int lxray, double h2, int power
 }
 
 /* cfact for one type at sin(theta)/lambda squared q2, four_formtab body
- * (fourier_sup.f90:2716-2736) */
+ * (fourier_sup.f90:2716-2736): the isotropic Debye-Waller term only when all
+ * ADPs are isotropic (:2729) */
 static void oc_cfact_at(const dgpu_crystal *cr, const dgpu_opts *op, int t, double q2,
                         double *re, double *im)
 {
     double sf = oc_form(cr->scat, t, op->lxray, q2, op->power);
     double sfp = 0, sfpp = 0, sb;
     if (op->ano) { sfp = cr->delfr ? cr->delfr[t] : 0; sfpp = cr->delfi ? cr->delfi[t] : 0; }
-    if (op->ldbw) sb = exp(-(cr->dw[t] * q2)) * cr->occ[t];
+    if (op->ldbw && !cr->is_anis) sb = exp(-(cr->dw[t] * q2)) * cr->occ[t];
     else sb = 1.0 * cr->occ[t];
     *re = sb * (sf + sfp);
     *im = sb * sfpp;
@@ -497,26 +498,148 @@ static void oc_qinfo(const dgpu_grid *g, const double *dsi, double res[7])
     res[5] = bmin; res[6] = bmax;
 }
 
-/* Gather atoms of one type (four_getatm LOT_OFF, fourier_sup.f90:1839-1848). */
-static int64_t oc_getatm(const dgpu_crystal *cr, int t, double *xat, float *w)
+/* four_csize, fourier_sup.f90:2533-2555: origins available to a lot */
+static void oc_csize(const dgpu_crystal *cr, const dgpu_opts *op, int32_t cs[3])
 {
-    int64_t n = 0;
-    for (int64_t i = 0; i < cr->natoms; i++)
-        if (cr->iscat[i] == t) n++;
+    for (int k = 0; k < 3; k++) {
+        int32_t c = cr->icc[k] - op->ls_xyz[k] + 1;
+        cs[k] = op->lperiod ? cr->icc[k] : (c > 1 ? c : 1);
+    }
+}
+
+static int oc_lots_on(const dgpu_opts *op)
+{
+    return op->ilots == DGPU_LOT_BOX || op->ilots == DGPU_LOT_ELI;
+}
+
+/* Cell (ii,jj,kk) of the ls_xyz box belongs to the lot: always for a box,
+ * inside the inscribed ellipsoid for LOT_ELI (fourier_sup.f90:1908-1937,
+ * four_getav :2488-2500), summed in the reference's order x1 + x2 + x3. */
+static int oc_in_lot(const dgpu_opts *op, int32_t ii, int32_t jj, int32_t kk)
+{
+    if (op->ilots != DGPU_LOT_ELI) return 1;
+    double x0[3], xt[3];
+    int32_t d[3] = {ii, jj, kk};
+    for (int k = 0; k < 3; k++) {
+        x0[k] = (double)op->ls_xyz[k] / 2.0;
+        double u = (double)d[k] - x0[k] + 0.5;
+        xt[k] = u * u / (x0[k] * x0[k]);
+    }
+    return (xt[0] + xt[1] + xt[2]) <= 1.0;
+}
+
+/* Atom i is of type t and, when a > 0, of ADP type a. */
+static int oc_match(const dgpu_crystal *cr, int64_t i, int t, int a)
+{
+    if (cr->iscat[i] != t) return 0;
+    return a <= 0 || cr->ianis[i] == a;
+}
+
+/* Gather the atoms of type t (ADP a, or any when a == 0) of one lot:
+ * four_getatm / four_getatm_anis (fourier_sup.f90:1806-1970, 1975-2140).
+ * LOT_OFF takes every atom at its position; a box or ellipsoid lot walks
+ * its cells from lbeg (1-based, wrapped once at icc), takes the ncatoms
+ * sites of each cell (celltoindex, celltoindex.f90:21-23) and the atoms
+ * stored after the periodic block whose INT(pos) is that cell, all shifted
+ * by the lot origin.  xat == NULL counts only; xat is SoA with stride n.
+ * *ncell receives the cells of the lot. */
+static int64_t oc_getatm_lot(const dgpu_crystal *cr, const dgpu_opts *op, int t, int a,
+                             const int32_t lbeg[3], double *xat, float *w, int64_t n,
+                             int32_t *ncell)
+{
     int64_t m = 0;
-    for (int64_t i = 0; i < cr->natoms; i++)
-        if (cr->iscat[i] == t) {
-            for (int k = 0; k < 3; k++) xat[k * n + m] = cr->pos[3 * i + k];
-            if (w) w[m] = cr->atom_occ ? cr->atom_occ[i] : 1.0f;
-            m++;
-        }
+    if (!oc_lots_on(op)) {
+        *ncell = cr->icc[0] * cr->icc[1] * cr->icc[2];
+        for (int64_t i = 0; i < cr->natoms; i++)
+            if (oc_match(cr, i, t, a)) {
+                if (xat) {
+                    for (int k = 0; k < 3; k++) xat[k * n + m] = cr->pos[3 * i + k];
+                    if (w) w[m] = cr->atom_occ ? cr->atom_occ[i] : 1.0f;
+                }
+                m++;
+            }
+        return m;
+    }
+    const int64_t cr_end = (int64_t)cr->ncatoms * cr->icc[0] * cr->icc[1] * cr->icc[2];
+    int32_t nc = 0;
+    for (int32_t kk = 0; kk < op->ls_xyz[2]; kk++)
+        for (int32_t jj = 0; jj < op->ls_xyz[1]; jj++)
+            for (int32_t ii = 0; ii < op->ls_xyz[0]; ii++) {
+                int32_t d[3] = {ii, jj, kk}, icell[3];
+                double off[3];
+                for (int k = 0; k < 3; k++) {
+                    icell[k] = d[k] + lbeg[k];
+                    off[k] = cr->dim0[k] + lbeg[k] - 1;
+                    if (icell[k] > cr->icc[k]) {
+                        icell[k] -= cr->icc[k];
+                        off[k] -= (double)cr->icc[k];
+                    }
+                }
+                if (!oc_in_lot(op, ii, jj, kk)) continue;
+                nc++;
+                int64_t c = (icell[2] - 1) * (int64_t)cr->icc[0] * cr->icc[1]
+                          + (icell[1] - 1) * (int64_t)cr->icc[0] + (icell[0] - 1);
+                for (int32_t is = 0; is < cr->ncatoms; is++) {
+                    int64_t ia = c * cr->ncatoms + is;
+                    if (ia >= cr->natoms || !oc_match(cr, ia, t, a)) continue;
+                    if (xat) {
+                        for (int k = 0; k < 3; k++) xat[k * n + m] = cr->pos[3 * ia + k] - off[k];
+                        if (w) w[m] = cr->atom_occ ? cr->atom_occ[ia] : 1.0f;
+                    }
+                    m++;
+                }
+                int64_t jc[3];
+                for (int k = 0; k < 3; k++) jc[k] = icell[k] + lround(cr->dim_lo[k]) - 1;
+                for (int64_t ir = cr_end; ir < cr->natoms; ir++) {
+                    if ((int64_t)cr->pos[3 * ir] != jc[0] || (int64_t)cr->pos[3 * ir + 1] != jc[1] ||
+                        (int64_t)cr->pos[3 * ir + 2] != jc[2] || !oc_match(cr, ir, t, a))
+                        continue;
+                    if (xat) {
+                        for (int k = 0; k < 3; k++) xat[k * n + m] = cr->pos[3 * ir + k] - off[k];
+                        if (w) w[m] = cr->atom_occ ? cr->atom_occ[ir] : 1.0f;
+                    }
+                    m++;
+                }
+            }
+    *ncell = nc;
+    return m;
+}
+
+/* four_nanis, fourier_sup.f90:4294-4326: the ADP types met among the atoms
+ * of type t, in order of first appearance. */
+static int oc_anis_list(const dgpu_crystal *cr, int t, int32_t *list)
+{
+    int n = 0;
+    for (int64_t i = 0; i < cr->natoms; i++) {
+        if (cr->iscat[i] != t) continue;
+        int seen = 0;
+        for (int j = 0; j < n && !seen; j++) seen = list[j] == cr->ianis[i];
+        if (!seen) list[n++] = cr->ianis[i];
+    }
     return n;
 }
 
-/* Multiply by the form factor on fnum (tcsf_form_iso, fourier_form.f90:147-177),
- * by table (istl) or at the exact sin(theta)/lambda. */
+/* four_dbw of ADP type a at h, four_dbwtab (fourier_sup.f90:2809-2831),
+ * zpi*pi = 2 pi^2 (lib_f90/wink_mod.f90:10-11). */
+static double oc_dbw(const dgpu_crystal *cr, int a, const double h[3])
+{
+    const double pi = 3.1415926535897932384626433832795028841971693993751;
+    const double *u = cr->anis_full + 6 * (int64_t)(a - 1), *r = cr->ar;
+    double arg = ((h[0] * h[0] * r[0] * r[0] * u[0]) +
+                  (h[1] * h[1] * r[1] * r[1] * u[1]) +
+                  (h[2] * h[2] * r[2] * r[2] * u[2]) +
+                  (h[1] * h[2] * r[1] * r[2] * u[3]) * 2.0 +
+                  (h[0] * h[2] * r[0] * r[2] * u[4]) * 2.0 +
+                  (h[0] * h[1] * r[0] * r[1] * u[5]) * 2.0) * (2.0 * pi) * pi;
+    return exp(-arg);
+}
+
+/* Multiply by the form factor on fnum, by table (istl) or at the exact
+ * sin(theta)/lambda: tcsf_form_iso (fourier_form.f90:147-177), or, for ADP
+ * type a > 0, tcsf_form_aniso (fourier_form.f90:106-143) with four_dbw = 1
+ * unless ldbw (fourier_sup.f90:2797-2800). */
 static void oc_apply_form(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,
-                          int t, const double *cfact, const int32_t *istl,
+                          int t, int a, const double *cfact, const int32_t *istl,
                           const int32_t fnum[3], double *tcsf)
 {
     const int32_t *num = g->inc;
@@ -524,21 +647,27 @@ static void oc_apply_form(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu
         for (int32_t j = 0; j < fnum[1]; j++)
             for (int32_t i = 0; i < fnum[0]; i++) {
                 int64_t p = i + (int64_t)num[0] * (j + (int64_t)num[1] * l);
-                double br, bi;
+                double br, bi, h[3];
+                oc_hvec(g->eck, g->vi, i, j, l, h);
                 if (op->form == DGPU_FORM_TABLE) {
                     const double *c = cfact + 2 * ((int64_t)(t - 1) * NTAB + istl[p]);
                     br = c[0]; bi = c[1];
                 } else {
-                    double h[3], tt[3];
-                    oc_hvec(g->eck, g->vi, i, j, l, h);
-                    for (int a = 0; a < 3; a++)
-                        tt[a] = M3(cr->rten,a,0) * h[0] + M3(cr->rten,a,1) * h[1] + M3(cr->rten,a,2) * h[2];
+                    double tt[3];
+                    for (int k = 0; k < 3; k++)
+                        tt[k] = M3(cr->rten,k,0) * h[0] + M3(cr->rten,k,1) * h[1] + M3(cr->rten,k,2) * h[2];
                     double q2 = (h[0] * tt[0] + h[1] * tt[1] + h[2] * tt[2]) / 4.0;
                     oc_cfact_at(cr, op, t, q2, &br, &bi);
                 }
                 double ar = tcsf[2 * p], ai = tcsf[2 * p + 1];
-                tcsf[2 * p] = ar * br - ai * bi;
-                tcsf[2 * p + 1] = ar * bi + ai * br;
+                double xr = ar * br - ai * bi, xi = ar * bi + ai * br;
+                if (a > 0 && op->ldbw) {
+                    double d = oc_dbw(cr, a, h);
+                    xr *= d;
+                    xi *= d;
+                }
+                tcsf[2 * p] = xr;
+                tcsf[2 * p + 1] = xi;
             }
 }
 
@@ -558,16 +687,42 @@ static void oc_strucf_mode(const dgpu_grid *g, const dgpu_opts *op, const double
         oc_strucf_exact(xat, w, nxat, g->eck, g->vi, num, fnum, nthreads, tcsf);
 }
 
-/* four_run for LOT_OFF and isotropic ADPs, fourier_sup.f90:11-323 */
+/* Checks of the lot options, the lots command's own (fourier.f90:490-497)
+ * plus the range of the caller's origins. */
+static int oc_check_lots(const dgpu_crystal *cr, const dgpu_opts *op, const int32_t cs[3])
+{
+    int lots = oc_lots_on(op);
+    if (op->ilots != 0 && op->ilots != DGPU_LOT_OFF && !lots) return DGPU_ERR_ARG;
+    if (!lots && op->lperiod) return 0;
+    for (int k = 0; k < 3; k++)
+        if (op->ls_xyz[k] < 1 || op->ls_xyz[k] > cr->icc[k]) return DGPU_ERR_ARG;
+    if (!lots) return 0;
+    if (!op->lot_all) {
+        if (op->nlots < 1 || !op->lot_origins) return DGPU_ERR_ARG;
+        for (int64_t l = 0; l < op->nlots; l++)
+            for (int k = 0; k < 3; k++)
+                if (op->lot_origins[3 * l + k] < 1 || op->lot_origins[3 * l + k] > cs[k]) return DGPU_ERR_ARG;
+    }
+    return 0;
+}
+
+/* four_run for the independent atom model, fourier_sup.f90:11-323: lots
+ * (LOT_OFF, box, ellipsoid) and isotropic or anisotropic ADPs. */
 int oc_four_run(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,
                 double *csf, double *acsf_out, double *dsi, dgpu_info *info, int nthreads)
 {
     const int32_t *num = g->inc;
     int64_t np = (int64_t)num[0] * num[1] * num[2];
-    int32_t lmn[6], fnum[3];
+    int32_t lmn[6], fnum[3], cs[3];
     double off[9];
     int rc, warn = 0;
     if (cr->natoms < 1) return DGPU_ERR_NO_ATOMS;
+    if (cr->is_anis && (cr->nanis < 1 || !cr->ianis || !cr->anis_full)) return DGPU_ERR_ARG;
+    oc_csize(cr, op, cs);
+    rc = oc_check_lots(cr, op, cs);
+    if (rc) return rc;
+    const int lots = oc_lots_on(op);
+    const int64_t nlots = !lots ? 1 : op->lot_all ? (int64_t)cs[0] * cs[1] * cs[2] : op->nlots;
 
     memset(csf, 0, sizeof(double) * 2 * np);
     memset(dsi, 0, sizeof(double) * np);
@@ -578,6 +733,8 @@ int oc_four_run(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,
     double *cex = (double *)malloc(sizeof(double) * 2 * DGPU_I2PI);
     double *xat = (double *)malloc(sizeof(double) * 3 * cr->natoms);
     float *w = (float *)malloc(sizeof(float) * cr->natoms);
+    int32_t *alist = (int32_t *)malloc(sizeof(int32_t) * (cr->is_anis ? cr->natoms : 1));
+    int64_t pairs = 0;
 
     rc = oc_fourier_lmn(g->eck, g->vi, g->inc, lmn, off);
     if (rc) goto done;
@@ -588,65 +745,72 @@ int oc_four_run(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,
     oc_formtab(cr, op, cfact);
     int idim = oc_test_friedel(g, op, fnum);
 
-    /* four_aver, fourier_sup.f90:1194-1357 */
+    /* four_aver, fourier_sup.f90:1194-1357: cells drawn over csize */
     int32_t ncell = 0;
     if (op->fave != 0.0) {
-        int64_t ncells = (int64_t)cr->icc[0] * cr->icc[1] * cr->icc[2];
         for (int t = 1; t <= cr->nscat; t++) {
             int64_t nx = 0;
-            for (int32_t ii = 0; ii < cr->icc[0]; ii++)
-                for (int32_t jj = 0; jj < cr->icc[1]; jj++)
-                    for (int32_t kk = 0; kk < cr->icc[2]; kk++) {
-                        int64_t c = ii + (int64_t)cr->icc[0] * (jj + (int64_t)cr->icc[1] * kk);
-                        int sel = op->fave >= 1.0 ? 1 : (op->aver_cells ? op->aver_cells[c] != 0 : 0);
-                        if (!sel) continue;
-                        ncell++;
-                        for (int32_t is = 0; is < cr->ncatoms; is++) {
-                            int64_t ia = c * cr->ncatoms + is;              /* celltoindex */
-                            if (ia >= cr->natoms || cr->iscat[ia] != t) continue;
-                            nx++;
+            for (int pass = 0; pass < 2; pass++) {
+                int64_t m = 0;
+                double *xa = pass ? xat : NULL;
+                for (int32_t ii = 0; ii < cs[0]; ii++)
+                    for (int32_t jj = 0; jj < cs[1]; jj++)
+                        for (int32_t kk = 0; kk < cs[2]; kk++) {
+                            int64_t s = ii + (int64_t)cs[0] * (jj + (int64_t)cs[1] * kk);
+                            int sel = op->fave >= 1.0 ? 1 : (op->aver_cells ? op->aver_cells[s] != 0 : 0);
+                            if (!sel) continue;
+                            if (pass) ncell++;
+                            int32_t icell[3] = {ii, jj, kk};
+                            int64_t c = ii + (int64_t)cr->icc[0] * (jj + (int64_t)cr->icc[1] * kk);
+                            for (int32_t is = 0; is < cr->ncatoms; is++) {
+                                int64_t ia = c * cr->ncatoms + is;              /* celltoindex */
+                                if (ia >= cr->natoms || cr->iscat[ia] != t) continue;
+                                if (xa) {
+                                    for (int k = 0; k < 3; k++)
+                                        xa[k * nx + m] = cr->pos[3 * ia + k] - (double)icell[k] - cr->dim0[k];
+                                    w[m] = cr->atom_occ ? cr->atom_occ[ia] : 1.0f;
+                                }
+                                m++;
+                            }
                         }
-                    }
-            double *xa = (double *)malloc(sizeof(double) * 3 * (nx > 0 ? nx : 1));
-            float *wa = (float *)malloc(sizeof(float) * (nx > 0 ? nx : 1));
-            int64_t m = 0;
-            for (int32_t ii = 0; ii < cr->icc[0]; ii++)
-                for (int32_t jj = 0; jj < cr->icc[1]; jj++)
-                    for (int32_t kk = 0; kk < cr->icc[2]; kk++) {
-                        int64_t c = ii + (int64_t)cr->icc[0] * (jj + (int64_t)cr->icc[1] * kk);
-                        int sel = op->fave >= 1.0 ? 1 : (op->aver_cells ? op->aver_cells[c] != 0 : 0);
-                        if (!sel) continue;
-                        int32_t icell[3] = {ii, jj, kk};
-                        for (int32_t is = 0; is < cr->ncatoms; is++) {
-                            int64_t ia = c * cr->ncatoms + is;
-                            if (ia >= cr->natoms || cr->iscat[ia] != t) continue;
-                            for (int k = 0; k < 3; k++)
-                                xa[k * nx + m] = cr->pos[3 * ia + k] - (double)icell[k] - cr->dim0[k];
-                            wa[m] = cr->atom_occ ? cr->atom_occ[ia] : 1.0f;
-                            m++;
-                        }
-                    }
-            oc_strucf_mode(g, op, xa, cr->atom_occ ? wa : NULL, nx, lmn, off, fnum, cex, nthreads, tcsf);
-            oc_apply_form(cr, g, op, t, cfact, istl, fnum, tcsf);
+                nx = m;
+            }
+            oc_strucf_mode(g, op, xat, cr->atom_occ ? w : NULL, nx, lmn, off, fnum, cex, nthreads, tcsf);
+            oc_apply_form(cr, g, op, t, 0, cfact, istl, fnum, tcsf);
             for (int64_t p = 0; p < 2 * np; p++) acsf[p] += tcsf[p];
-            free(xa); free(wa);
-            (void)ncells;
         }
         ncell = ncell / cr->nscat;
-        /* four_getav LOT_OFF (fourier_sup.f90:2457-2466), summed on the full num */
-        int64_t nl = (int64_t)cr->icc[0] * cr->icc[1] * cr->icc[2];
-        double *xl = (double *)malloc(sizeof(double) * 3 * nl);
-        int64_t m = 0;
-        for (int32_t ii = 0; ii < cr->icc[0]; ii++)
-            for (int32_t jj = 0; jj < cr->icc[1]; jj++)
-                for (int32_t kk = 0; kk < cr->icc[2]; kk++) {
-                    xl[m] = (double)ii + cr->dim0[0];
-                    xl[nl + m] = (double)jj + cr->dim0[1];
-                    xl[2 * nl + m] = (double)kk + cr->dim0[2];
-                    m++;
-                }
+        /* four_getav (fourier_sup.f90:2440-2510): the lattice of the whole
+         * crystal or of one lot, summed on the full num */
+        int64_t nl = 0;
+        double *xl = (double *)malloc(sizeof(double) * 3 * ((int64_t)cr->icc[0] * cr->icc[1] * cr->icc[2] + 1));
+        int64_t cap = (int64_t)cr->icc[0] * cr->icc[1] * cr->icc[2];
+        double *xs = (double *)malloc(sizeof(double) * 3 * (cap > 0 ? cap : 1));
+        if (!lots) {
+            for (int32_t ii = 0; ii < cr->icc[0]; ii++)
+                for (int32_t jj = 0; jj < cr->icc[1]; jj++)
+                    for (int32_t kk = 0; kk < cr->icc[2]; kk++) {
+                        xs[3 * nl] = (double)ii + cr->dim0[0];
+                        xs[3 * nl + 1] = (double)jj + cr->dim0[1];
+                        xs[3 * nl + 2] = (double)kk + cr->dim0[2];
+                        nl++;
+                    }
+        } else {
+            for (int32_t kk = 0; kk < op->ls_xyz[2]; kk++)
+                for (int32_t jj = 0; jj < op->ls_xyz[1]; jj++)
+                    for (int32_t ii = 0; ii < op->ls_xyz[0]; ii++) {
+                        if (!oc_in_lot(op, ii, jj, kk)) continue;
+                        xs[3 * nl] = ii;
+                        xs[3 * nl + 1] = jj;
+                        xs[3 * nl + 2] = kk;
+                        nl++;
+                    }
+        }
+        for (int64_t m = 0; m < nl; m++)
+            for (int k = 0; k < 3; k++) xl[k * nl + m] = xs[3 * m + k];
         oc_strucf_mode(g, op, xl, NULL, nl, lmn, off, num, cex, nthreads, tcsf);
         free(xl);
+        free(xs);
         double norm = 0.0;
         if (ncell > 0) norm = 1.0 / ncell; else warn = DGPU_WARN_NO_CELL;
         for (int64_t p = 0; p < np; p++) {
@@ -658,21 +822,48 @@ int oc_four_run(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,
         }
     }
 
-    /* loop over types (fourier_sup.f90:224-244) */
-    for (int t = 1; t <= cr->nscat; t++) {
-        int64_t nx = oc_getatm(cr, t, xat, w);
-        if (nx <= 0) continue;
-        oc_strucf_mode(g, op, xat, cr->atom_occ ? w : NULL, nx, lmn, off, fnum, cex, nthreads, tcsf);
-        oc_apply_form(cr, g, op, t, cfact, istl, fnum, tcsf);
-        for (int64_t p = 0; p < 2 * np; p++) csf[p] += tcsf[p];
-        if (op->cancel && *op->cancel) { rc = DGPU_ERR_CANCELLED; goto done; }
+    /* loop over lots and atom types (fourier_sup.f90:136-257) */
+    int32_t lcell = 0;
+    for (int64_t lot = 0; lot < nlots; lot++) {
+        int32_t lbeg[3] = {1, 1, 1};
+        if (lots && op->lot_all) {
+            int64_t ii = lot;
+            lbeg[2] = (int32_t)(ii / ((int64_t)cs[0] * cs[1])) + 1;
+            ii -= (int64_t)(lbeg[2] - 1) * cs[0] * cs[1];
+            lbeg[1] = (int32_t)(ii / cs[0]) + 1;
+            ii -= (int64_t)(lbeg[1] - 1) * cs[0];
+            lbeg[0] = (int32_t)(ii % cs[0]) + 1;
+        } else if (lots) {
+            for (int k = 0; k < 3; k++) lbeg[k] = op->lot_origins[3 * lot + k];
+        }
+        memset(csf, 0, sizeof(double) * 2 * np);
+        for (int t = 1; t <= cr->nscat; t++) {
+            int na = 1;
+            if (cr->is_anis) na = oc_anis_list(cr, t, alist);
+            for (int j = 0; j < na; j++) {
+                int a = cr->is_anis ? alist[j] : 0;
+                int64_t nx = oc_getatm_lot(cr, op, t, a, lbeg, NULL, NULL, 0, &lcell);
+                if (nx <= 0) continue;
+                oc_getatm_lot(cr, op, t, a, lbeg, xat, w, nx, &lcell);
+                pairs += nx * np;
+                oc_strucf_mode(g, op, xat, cr->atom_occ ? w : NULL, nx, lmn, off, fnum, cex, nthreads, tcsf);
+                oc_apply_form(cr, g, op, t, a, cfact, istl, fnum, tcsf);
+                for (int64_t p = 0; p < 2 * np; p++) csf[p] += tcsf[p];
+                if (op->cancel && *op->cancel) { rc = DGPU_ERR_CANCELLED; goto done; }
+            }
+        }
+        for (int64_t p = 0; p < np; p++) {
+            csf[2 * p] -= acsf[2 * p];
+            csf[2 * p + 1] -= acsf[2 * p + 1];
+            dsi[p] = dsi[p] + (csf[2 * p] * csf[2 * p] + csf[2 * p + 1] * csf[2 * p + 1]);
+        }
+        if (idim) oc_apply_friedel(num, fnum, acsf, csf, dsi);
     }
-    for (int64_t p = 0; p < np; p++) {
-        csf[2 * p] -= acsf[2 * p];
-        csf[2 * p + 1] -= acsf[2 * p + 1];
-        dsi[p] = dsi[p] + (csf[2 * p] * csf[2 * p] + csf[2 * p + 1] * csf[2 * p + 1]);
+    if (nlots != 1) {
+        /* fourier_sup.f90:273-277 */
+        double dnorm = (double)((int64_t)cr->icc[0] * cr->icc[1] * cr->icc[2]) / (double)(lcell * nlots);
+        for (int64_t p = 0; p < np; p++) dsi[p] = dnorm * dsi[p];
     }
-    if (idim) oc_apply_friedel(num, fnum, acsf, csf, dsi);
     {
         double sq = sqrt(op->diff_scale);
         for (int64_t p = 0; p < 2 * np; p++) csf[p] *= sq;
@@ -685,22 +876,20 @@ int oc_four_run(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,
         for (int k = 0; k < 6; k++) info->lmn[k] = lmn[k];
         for (int k = 0; k < 9; k++) info->off_shift[k] = off[k];
         info->ncell = ncell;
-        int64_t nat = 0;
-        for (int64_t i = 0; i < cr->natoms; i++) if (cr->iscat[i] >= 1 && cr->iscat[i] <= cr->nscat) nat++;
-        info->pairs = nat * np;
+        info->pairs = pairs;
         oc_qinfo(g, dsi, info->res);
     }
     if (acsf_out) memcpy(acsf_out, acsf, sizeof(double) * 2 * np);
     rc = warn;
 done:
-    free(acsf); free(tcsf); free(istl); free(cfact); free(cex); free(xat); free(w);
+    free(acsf); free(tcsf); free(istl); free(cfact); free(cex); free(xat); free(w); free(alist);
     return rc;
 }
-
 /* ---------------------------------------------------------------------- */
 /* chi^2 = sum_h wt(h) (I(h) - It(h))^2 and its gradient, exact FP64, full
  * grid, fave = 0, no Friedel reduction.  I = diff_scale |F|^2 with
- * F = sum_t cf_t(h) sum_j w_j exp(2 pi i h.r_j).                            */
+ * F = sum_j cf_t(j)(h) D_a(j)(h) w_j exp(2 pi i h.r_j), D the anisotropic
+ * Debye-Waller term of atom j's ADP type (1 for an isotropic crystal).      */
 int oc_chi2_grad(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,
                  const double *it, const double *wt, double *chi2, double *grad_pos,
                  double *grad_occ, int nthreads)
@@ -715,6 +904,8 @@ int oc_chi2_grad(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op
     double *H = (double *)malloc(sizeof(double) * 3 * np);
     int32_t *istl = (int32_t *)malloc(sizeof(int32_t) * np);
     double *cfact = (double *)malloc(sizeof(double) * 2 * NTAB * (ns > 0 ? ns : 1));
+    const int anis = cr->is_anis && op->ldbw;
+    double *D = (double *)malloc(sizeof(double) * np * (anis ? cr->nanis : 1));
     (void)nthreads;
     oc_stltab(g->eck, g->vi, num, cr->rten, istl);
     oc_formtab(cr, op, cfact);
@@ -725,6 +916,8 @@ int oc_chi2_grad(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op
                 double h[3], tt[3];
                 oc_hvec(g->eck, g->vi, i, j, l, h);
                 for (int k = 0; k < 3; k++) H[3 * p + k] = h[k];
+                if (anis)
+                    for (int a = 1; a <= cr->nanis; a++) D[(int64_t)(a - 1) * np + p] = oc_dbw(cr, a, h);
                 for (int a = 0; a < 3; a++)
                     tt[a] = M3(cr->rten,a,0) * h[0] + M3(cr->rten,a,1) * h[1] + M3(cr->rten,a,2) * h[2];
                 double q2 = (h[0] * tt[0] + h[1] * tt[1] + h[2] * tt[2]) / 4.0;
@@ -748,6 +941,7 @@ int oc_chi2_grad(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op
             if (t < 1 || t > ns) continue;
             double ph = oc_frac_dot(H + 3 * p, cr->pos[3 * a], cr->pos[3 * a + 1], cr->pos[3 * a + 2]);
             double wa = cr->atom_occ ? (double)cr->atom_occ[a] : 1.0;
+            if (anis) wa *= D[(int64_t)(cr->ianis[a] - 1) * np + p];
             double c = cos(zpi * ph) * wa, s = sin(zpi * ph) * wa;
             double br = cf[2 * ((int64_t)(t - 1) * np + p)], bi = cf[2 * ((int64_t)(t - 1) * np + p) + 1];
             fr += br * c - bi * s;
@@ -780,6 +974,11 @@ int oc_chi2_grad(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op
                 double ph = oc_frac_dot(H + 3 * p, cr->pos[3 * a], cr->pos[3 * a + 1], cr->pos[3 * a + 2]);
                 double c = cos(zpi * ph), s = sin(zpi * ph);
                 double qr = Q[2 * ((int64_t)(t - 1) * np + p)], qi = Q[2 * ((int64_t)(t - 1) * np + p) + 1];
+                if (anis) {
+                    double d = D[(int64_t)(cr->ianis[a] - 1) * np + p];
+                    qr *= d;
+                    qi *= d;
+                }
                 double zr = qr * c - qi * s, zi = qr * s + qi * c;
                 go += zr;
                 for (int k = 0; k < 3; k++) gx[k] += H[3 * p + k] * zi;
@@ -789,7 +988,7 @@ int oc_chi2_grad(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op
         if (grad_occ) grad_occ[a] = go;
         if (grad_pos) for (int k = 0; k < 3; k++) grad_pos[3 * a + k] = -zpi * wa * gx[k];
     }
-    free(cf); free(F); free(Q); free(H); free(istl); free(cfact);
+    free(cf); free(F); free(Q); free(H); free(istl); free(cfact); free(D);
     return DGPU_OK;
 }
 
@@ -814,8 +1013,13 @@ double oc_time_ref_rows(const dgpu_crystal *cr, const dgpu_grid *g, int32_t row_
     t0 = omp_get_wtime();
 #endif
     for (int t = 1; t <= cr->nscat; t++) {
-        int64_t nx = oc_getatm(cr, t, xat, NULL);
+        dgpu_opts whole;
+        memset(&whole, 0, sizeof(whole));
+        whole.ilots = DGPU_LOT_OFF;
+        int32_t nc;
+        int64_t nx = oc_getatm_lot(cr, &whole, t, 0, NULL, NULL, NULL, 0, &nc);
         if (nx <= 0) continue;
+        oc_getatm_lot(cr, &whole, t, 0, NULL, xat, NULL, nx, &nc);
         oc_strucf_ref(xat, NULL, nx, g->vi, g->vi + 3, g->vi + 6, off, lmn, num, fnum, cex,
                       row_lo, row_hi, nthreads, tcsf);
         pairs += nx * (int64_t)(row_hi - row_lo) * num[1] * num[2];

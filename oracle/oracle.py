@@ -116,10 +116,20 @@ def four_strucf(xat, uin, vin, win, off, lmn, num, fnum, cfact=None, istl=None):
     return (out[0::2] + 1j * out[1::2]).reshape(num, order="F")
 
 
-def four_run(cr, grid, opts, nthreads=0):
+def four_run(cr, grid, opts, nthreads=0, aver_cells=None, lot_origins=None):
     """Returns (rc, csf, acsf, dsi, info); arrays shaped grid.inc (Fortran order)."""
     if nthreads <= 0:
         nthreads = os.cpu_count() or 1
+    keep = []
+    if aver_cells is not None:
+        a = np.ascontiguousarray(np.asarray(aver_cells, dtype=np.uint8).reshape(-1, order="F"))
+        opts.aver_cells = a.ctypes.data_as(C.POINTER(C.c_uint8))
+        keep.append(a)
+    if lot_origins is not None:
+        o = np.ascontiguousarray(np.asarray(lot_origins, dtype=np.int32).reshape(-1, 3))
+        opts.lot_origins = _i(o)
+        opts.nlots = o.shape[0]
+        keep.append(o)
     c = cr.to_c()
     g = grid.to_c()
     np_ = grid.npoints
@@ -129,6 +139,7 @@ def four_run(cr, grid, opts, nthreads=0):
     info = _abi.Info()
     rc = lib().oc_four_run(C.byref(c), C.byref(g), C.byref(opts), _d(csf), _d(acsf), _d(dsi),
                            C.byref(info), nthreads)
+    del keep
     shp = grid.inc
     return (rc, (csf[0::2] + 1j * csf[1::2]).reshape(shp, order="F"),
             (acsf[0::2] + 1j * acsf[1::2]).reshape(shp, order="F"),

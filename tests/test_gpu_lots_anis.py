@@ -1,0 +1,132 @@
+"""Anisotropic ADPs and lots on the GPU against the oracle.
+
+Cases: (type, ADP type) groups with the anisotropic Debye-Waller term
+(four_dbwtab, tcsf_form_aniso), box and ellipsoid lots with periodic wrap,
+interstitial atoms, lot_all over a non-periodic csize and <F> with the lot
+lattice (fourier_sup.f90:136-277, 1194-1357, 1806-2140).  Intensities are
+compared as max |I - I_ref| / (I_ref + N<|f|^2>) <= 1e-5 (both engines),
+csf and acsf relative to their maxima.
+"""
+import numpy as np
+import pytest
+
+import kat_cases as K
+from diffusecode_gb300 import _abi
+from diffusecode_gb300 import fourier as FR
+from diffusecode_gb300 import structures as S
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+CASES = {
+    "anis": dict(anis=True, opts=dict(ldbw=1)),
+    "anis-nodbw": dict(anis=True, opts=dict(ldbw=0, fave=1.0)),
+    "anis-box-aver": dict(anis=True, opts=dict(ldbw=1, ilots=_abi.LOT_BOX, ls_xyz=(3, 2, 2), fave=1.0),
+                          origins=[(1, 1, 1), (4, 3, 2), (5, 4, 3)]),
+    "iso-eli-all-nonperiodic": dict(anis=False, opts=dict(ilots=_abi.LOT_ELI, ls_xyz=(3, 3, 2), lot_all=1,
+                                                          lperiod=0, fave=0.5)),
+    "anis-eli-origins": dict(anis=True, opts=dict(ldbw=1, ilots=_abi.LOT_ELI, ls_xyz=(4, 3, 3), diff_scale=2.5),
+                             origins=[(2, 1, 1), (5, 4, 1)]),
+    "iso-box-all": dict(anis=False, opts=dict(ilots=_abi.LOT_BOX, ls_xyz=(2, 2, 1), lot_all=1, fave=1.0)),
+}
+
+
+def _cells(cr, op, seed=3):
+    if not 0 < op.fave < 1:
+        return None
+    cs = [cr.icc[k] if op.lperiod else max(1, cr.icc[k] - op.ls_xyz[k] + 1) for k in range(3)]
+    return (np.random.default_rng(seed).random(cs) < op.fave).astype(np.uint8)
+
+
+@pytest.mark.parametrize("engine", [_abi.ENGINE_DIRECT, _abi.ENGINE_TC], ids=["direct", "tc"])
+@pytest.mark.parametrize("form", [_abi.FORM_TABLE, _abi.FORM_ANALYTIC], ids=["table", "analytic"])
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_lots_anis_vs_oracle(oracle, ctx, name, form, engine):
+    case = CASES[name]
+    cr, g = S.small_lots_anis(anis=case["anis"])
+    op = K.opts(phase=_abi.PHASE_EXACT64, form=form, engine=engine, **case["opts"])
+    cells = _cells(cr, op)
+    origins = case.get("origins")
+    rc, csf, acsf, dsi, info = oracle.four_run(cr, g, op, aver_cells=cells, lot_origins=origins)
+    r = FR.four_run(cr, g, op, ctx=ctx, aver_cells=cells, lot_origins=origins)
+    assert rc == 0 and r.status == 0
+    assert r.info.engine_used == engine
+    assert r.info.friedel_dim == info.friedel_dim == 1
+    floor = K.incoherent_floor(cr, g, K.opts(ldbw=0))
+    assert K.rel_err(r.dsi, dsi, floor) <= TOL
+    assert np.abs(r.csf - csf).max() <= 3e-5 * np.abs(csf).max()
+    if op.fave:
+        assert np.abs(r.acsf - acsf).max() <= 3e-5 * np.abs(acsf).max()
+        assert r.info.ncell == info.ncell
+    assert r.info.pairs == info.pairs
+
+
+@pytest.mark.parametrize("name", ["anis", "anis-box-aver", "iso-eli-all-nonperiodic"])
+def test_lots_anis_ref22(oracle, ctx, name):
+    """The reference's integer phases (CUDA-core engine) on the same cases."""
+    case = CASES[name]
+    cr, g = S.small_lots_anis(anis=case["anis"])
+    op = K.opts(phase=_abi.PHASE_REF22, engine=_abi.ENGINE_DIRECT, **case["opts"])
+    cells = _cells(cr, op)
+    origins = case.get("origins")
+    rc, csf, acsf, dsi, info = oracle.four_run(cr, g, op, aver_cells=cells, lot_origins=origins)
+    r = FR.four_run(cr, g, op, ctx=ctx, aver_cells=cells, lot_origins=origins)
+    assert rc == 0 and r.status == 0
+    assert K.rel_err(r.dsi, dsi, K.incoherent_floor(cr, g, K.opts(ldbw=0))) <= TOL
+
+
+def test_many_lots_chunked(oracle, ctx):
+    """More (lot, group) pairs than one engine launch takes (63): 40 lots of
+    3 groups run in two chunks."""
+    cr, g = S.small_lots_anis(anis=True, icc=(6, 5, 4), inc=(9, 9, 5))
+    rng = np.random.default_rng(11)
+    origins = np.stack([rng.integers(1, cr.icc[k] + 1, size=40) for k in range(3)], axis=1)
+    for engine in (_abi.ENGINE_DIRECT, _abi.ENGINE_TC):
+        op = K.opts(phase=_abi.PHASE_EXACT64, engine=engine, ilots=_abi.LOT_BOX, ls_xyz=(3, 3, 2), fave=1.0)
+        rc, csf, acsf, dsi, info = oracle.four_run(cr, g, op, lot_origins=origins)
+        r = FR.four_run(cr, g, op, ctx=ctx, lot_origins=origins)
+        assert rc == 0 and r.status == 0
+        assert K.rel_err(r.dsi, dsi, K.incoherent_floor(cr, g, K.opts(ldbw=0))) <= TOL
+        assert np.abs(r.csf - csf).max() <= 3e-5 * np.abs(csf).max()
+
+
+def test_lot_and_adp_argument_errors(ctx):
+    cr, g = S.small_lots_anis(anis=True)
+    op = K.opts(ilots=_abi.LOT_BOX, ls_xyz=(9, 1, 1))
+    r = FR.four_run(cr, g, op, ctx=ctx, lot_origins=[(1, 1, 1)])
+    assert r.status == _abi.DGPU_ERR_ARG
+    op = K.opts(ilots=_abi.LOT_BOX, ls_xyz=(2, 2, 2))
+    r = FR.four_run(cr, g, op, ctx=ctx, lot_origins=[(0, 1, 1)])
+    assert r.status == _abi.DGPU_ERR_ARG
+    bad = cr.ianis.copy()
+    bad[5] = 9
+    cr.ianis = bad
+    if cr.iscat[5] != 0:
+        r = FR.four_run(cr, g, K.opts(), ctx=ctx)
+        assert r.status == _abi.DGPU_ERR_ARG
+
+
+@pytest.mark.parametrize("engine", [_abi.ENGINE_DIRECT, _abi.ENGINE_TC], ids=["direct", "tc"])
+def test_gradient_anisotropic(oracle, ctx, engine):
+    """chi^2 gradient of an anisotropic crystal: the adjoint weights carry
+    each group's Debye-Waller term."""
+    from diffusecode_gb300.autograd import chi2_grad
+    cr, g = S.small_lots_anis(anis=True, inc=(11, 9, 5))
+    cr.atom_occ = np.linspace(0.9, 1.1, cr.natoms).astype(np.float32)
+    op = K.opts(phase=_abi.PHASE_EXACT64, engine=engine, ldbw=1)
+    tgt = S.perturbed_copy(cr, 3, 0.05, 4.5, 0.1)
+    tgt.ianis, tgt.anis_full, tgt.ar = cr.ianis, cr.anis_full, cr.ar
+    it = FR.four_run(tgt, g, K.opts(phase=_abi.PHASE_EXACT64, engine=_abi.ENGINE_DIRECT, ldbw=1), ctx=ctx).dsi
+    wt = 1.0 / (it + 1.0)
+    c2, gp, go, _ = chi2_grad(cr, g, op, it, wt, ctx=ctx)
+    oc2, ogp, ogo = oracle.chi2_grad(cr, g, op, it, wt)
+    assert abs(c2 - oc2) <= 1e-4 * oc2
+    assert np.max(np.abs(gp - ogp)) <= 2e-4 * np.abs(ogp).max()
+    assert np.max(np.abs(go - ogo)) <= 2e-4 * np.abs(ogo).max()
+
+
+def test_batch_rejects_lots_and_adps(ctx):
+    cr, g = S.small_lots_anis(anis=True)
+    with pytest.raises(Exception) as e:
+        FR.batch_run([cr], [g], K.opts(phase=_abi.PHASE_EXACT64), ctx=ctx)
+    assert getattr(e.value, "code", None) == _abi.DGPU_ERR_UNSUPPORTED
