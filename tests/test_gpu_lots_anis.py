@@ -5,7 +5,8 @@ Cases: (type, ADP type) groups with the anisotropic Debye-Waller term
 interstitial atoms, lot_all over a non-periodic csize and <F> with the lot
 lattice (fourier_sup.f90:136-277, 1194-1357, 1806-2140).  Intensities are
 compared as max |I - I_ref| / (I_ref + N<|f|^2>) <= 1e-5 (both engines),
-csf and acsf relative to their maxima.
+csf within 3e-5 of max |csf| + max |acsf| (its size before the <F>
+subtraction), acsf within 3e-5 of its maximum.
 """
 import numpy as np
 import pytest
@@ -54,7 +55,8 @@ def test_lots_anis_vs_oracle(oracle, ctx, name, form, engine):
     assert r.info.friedel_dim == info.friedel_dim == 1
     floor = K.incoherent_floor(cr, g, K.opts(ldbw=0))
     assert K.rel_err(r.dsi, dsi, floor) <= TOL
-    assert np.abs(r.csf - csf).max() <= 3e-5 * np.abs(csf).max()
+    # csf = F - <F>: the error scales with |F| before the subtraction
+    assert np.abs(r.csf - csf).max() <= 3e-5 * (np.abs(csf).max() + np.abs(acsf).max())
     if op.fave:
         assert np.abs(r.acsf - acsf).max() <= 3e-5 * np.abs(acsf).max()
         assert r.info.ncell == info.ncell
@@ -87,23 +89,27 @@ def test_many_lots_chunked(oracle, ctx):
         r = FR.four_run(cr, g, op, ctx=ctx, lot_origins=origins)
         assert rc == 0 and r.status == 0
         assert K.rel_err(r.dsi, dsi, K.incoherent_floor(cr, g, K.opts(ldbw=0))) <= TOL
-        assert np.abs(r.csf - csf).max() <= 3e-5 * np.abs(csf).max()
+        assert np.abs(r.csf - csf).max() <= 3e-5 * (np.abs(csf).max() + np.abs(acsf).max())
+
+
+def _status(fn):
+    try:
+        return fn().status
+    except Exception as e:          # the host wrapper raises on errors
+        return getattr(e, "code", None)
 
 
 def test_lot_and_adp_argument_errors(ctx):
     cr, g = S.small_lots_anis(anis=True)
     op = K.opts(ilots=_abi.LOT_BOX, ls_xyz=(9, 1, 1))
-    r = FR.four_run(cr, g, op, ctx=ctx, lot_origins=[(1, 1, 1)])
-    assert r.status == _abi.DGPU_ERR_ARG
+    assert _status(lambda: FR.four_run(cr, g, op, ctx=ctx, lot_origins=[(1, 1, 1)])) == _abi.DGPU_ERR_ARG
     op = K.opts(ilots=_abi.LOT_BOX, ls_xyz=(2, 2, 2))
-    r = FR.four_run(cr, g, op, ctx=ctx, lot_origins=[(0, 1, 1)])
-    assert r.status == _abi.DGPU_ERR_ARG
+    assert _status(lambda: FR.four_run(cr, g, op, ctx=ctx, lot_origins=[(0, 1, 1)])) == _abi.DGPU_ERR_ARG
     bad = cr.ianis.copy()
-    bad[5] = 9
+    k = int(np.flatnonzero(cr.iscat > 0)[0])
+    bad[k] = 9
     cr.ianis = bad
-    if cr.iscat[5] != 0:
-        r = FR.four_run(cr, g, K.opts(), ctx=ctx)
-        assert r.status == _abi.DGPU_ERR_ARG
+    assert _status(lambda: FR.four_run(cr, g, K.opts(), ctx=ctx)) == _abi.DGPU_ERR_ARG
 
 
 @pytest.mark.parametrize("engine", [_abi.ENGINE_DIRECT, _abi.ENGINE_TC], ids=["direct", "tc"])
