@@ -277,6 +277,48 @@ def plain_measure(ctx, c, g, op_tc, csf, acsf, dsi, flush, cr, grid, fave, pairs
             "rel_err_vs_fp64": err, "engine": "direct (CUDA cores, FP32 phasors)"}
 
 
+def lots_measure(ctx, c, g, op_main, csf, acsf, dsi, flush, cr, grid, steps=2, nlots=100, ls=10):
+    """Lots on the headline crystal (four_run's box lots, fourier_sup.f90:
+    136-277): nlots boxes of ls^3 unit cells at seeded random origins (numpy
+    PCG64 standing in for the caller's ran1 stream), device-resident, L2
+    flushed before each step.  The lots of one engine launch are as many as
+    fit 63 (lot, type) partial sums."""
+    import torch
+    op = _abi.Opts()
+    C.memmove(C.byref(op), C.byref(op_main), C.sizeof(op))
+    op.fave = 0.0
+    op.ilots = _abi.LOT_BOX
+    for k in range(3):
+        op.ls_xyz[k] = ls
+    rng = np.random.Generator(np.random.PCG64(17))
+    origins = np.ascontiguousarray(np.stack([rng.integers(1, cr.icc[k] + 1, size=nlots) for k in range(3)],
+                                            axis=1).astype(np.int32))
+    op.nlots = nlots
+    op.lot_origins = _abi.iptr(origins)
+    info = _abi.Info()
+
+    def run():
+        ctx.check(ctx.lib.dgpu_four_run_device(ctx.h, C.byref(c), C.byref(g), C.byref(op),
+                                               C.c_void_p(csf.data_ptr()), C.c_void_p(acsf.data_ptr()),
+                                               C.c_void_p(dsi.data_ptr()), C.byref(info)))
+        return info.total_ms, info.kernel_ms
+
+    run()
+    ts, ks = [], []
+    for _ in range(steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t, k = run()
+        ts.append(t)
+        ks.append(k)
+    ms = sum(ts) / len(ts)
+    per_launch = 63 // max(1, cr.nscat)
+    return {"workload": f"{nlots} box lots of {ls}^3 cells of the headline crystal, grid {list(grid.inc)}",
+            "pairs": int(info.pairs), "ms_per_step": ms, "kernel_ms": sum(ks) / len(ks),
+            "G_pairs_per_s": info.pairs / (ms * 1e-3) / 1e9, "lots_per_launch": per_launch,
+            "launches": -(-nlots // per_launch), "engine": {1: "direct", 2: "tc"}.get(info.engine_used)}
+
+
 def batch_measure(ctx, steps=3):
     """Population workload: 64 crystals (cubic / fcc / rock salt), atoms
     log-uniform in [2000, 200000], each with its own 2D plane of 129^2..257^2
@@ -430,6 +472,7 @@ def run_ours(args, world, rank, local):
         ctx, c, g, op, csf, acsf, dsi, flush, cr, grid, fave, info.pairs)
     adj = None if args.no_adjoint else adjoint_measure(ctx, engine)
     bat = None if args.no_batch else batch_measure(ctx)
+    lots = None if args.no_lots else lots_measure(ctx, c, g, op, csf, acsf, dsi, flush, cr, grid)
     pk, pk_kind = peaks()
     fnum_pts = int(np.prod(list(info.fnum)))
     pairs_computed = cr.n_scattering() * fnum_pts
@@ -469,6 +512,7 @@ def run_ours(args, world, rank, local):
         "plain_fp32": dict(plain, tc_over_plain=value / plain["value"]) if plain else None,
         "adjoint": adj,
         "batch": bat,
+        "lots": lots,
         "tc_config": list(info.tc_config),
         "gpu_launches": LAUNCHES_PER_RUN.get(engine_used, 10) * args.steps,
         "accuracy": {"rel_err_vs_fp64": acc_err, "points": acc_pts,
@@ -497,6 +541,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-lots", action="store_true")
     ap.add_argument("--tc-flush", type=int, default=0, help="atoms per main-accumulator drain (0: default)")
     args = ap.parse_args()
     world, rank, local = dist_init()
