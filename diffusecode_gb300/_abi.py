@@ -20,6 +20,7 @@ DGPU_ERR_TIMEOUT = -7
 DGPU_ERR_CANCELLED = -14
 DGPU_ERR_NO_ATOMS = -198
 DGPU_ERR_SCRATCH_SIZE = -20
+DGPU_ERR_NO_ACCUM = -175
 
 CFPKT = 9999
 CFINC = 0.001
@@ -34,6 +35,10 @@ ENGINE_DIRECT = 1
 ENGINE_TC = 2
 SPLIT_F16 = 0
 SPLIT_BF16 = 1
+ACCUM_INIT = -1
+ACCUM_SINGLE = 0
+ACCUM_ACCUM = 1
+ACCUM_FINISHED = 2
 LOT_OFF = 1
 LOT_BOX = 2
 LOT_ELI = 3

@@ -18,6 +18,7 @@ EXPORTS = [
     "dgpu_four_run", "dgpu_four_run_device", "dgpu_four_strucf", "dgpu_fourier_lmn",
     "dgpu_four_stltab", "dgpu_four_formtab", "dgpu_four_increments", "dgpu_chi2_grad",
     "dgpu_batch_run", "dgpu_batch_last_ms", "dgpu_four_strucf_noalloc", "dgpu_tc_last_kernel_ms",
+    "dgpu_four_weight", "dgpu_four_weight_device", "dgpu_four_accumulate",
 ]
 
 
@@ -60,6 +61,9 @@ def load():
     L.dgpu_tc_last_kernel_ms.argtypes = [vp]
     L.dgpu_tc_last_kernel_ms.restype = C.c_double
     L.dgpu_four_strucf_noalloc.argtypes = [vp, vp, C.c_int64, dp, dp, dp, dp, ip, ip, ip, vp, vp, vp]
+    L.dgpu_four_weight.argtypes = [vp, CR, GR, OP, dp, dp]
+    L.dgpu_four_weight_device.argtypes = [vp, CR, GR, OP, vp, vp]
+    L.dgpu_four_accumulate.argtypes = [vp, C.c_int32, C.c_int32, GR, C.c_double, dp, dp]
     _lib = L
     return L
 

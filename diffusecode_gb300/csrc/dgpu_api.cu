@@ -85,7 +85,8 @@ extern "C" int dgpu_ctx_destroy(dgpu_ctx *c)
                       &c->cfact, &c->part, &c->apart, &c->lat, &c->csf, &c->acsf, &c->dsi, &c->stats,
                       &c->flag, &c->tc_part, &c->tc_work, &c->tc_mult, &c->tc_vimg, &c->adj_qimg,
                       &c->adj_items, &c->gq, &c->gpart, &c->grad, &c->batch_desc, &c->batch_aux,
-                      &c->ianis, &c->geff, &c->ghist, &c->lpos, &c->ltype, &c->locc, &c->lplan, &c->lfac};
+                      &c->ianis, &c->geff, &c->ghist, &c->lpos, &c->ltype, &c->locc, &c->lplan, &c->lfac,
+                      &c->wbuf, &c->acc_csf, &c->acc_dsi};
     for (DevBuf *b : bufs) b->release();
     delete c->fs_main;
     for (int i = 0; i < 8; i++)

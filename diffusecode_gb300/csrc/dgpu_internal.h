@@ -79,6 +79,8 @@ struct dgpu_ctx {
     DevBuf ianis, geff, ghist;              // ADP types, group of every atom, (type, ADP) histogram
     DevBuf lpos, ltype, locc, lplan, lfac;  // lot crystals, lot plan, group factors
     FormSpec *fs_main = nullptr;            // host copy of the last main combine's FormSpec
+    DevBuf wbuf, acc_csf, acc_dsi;          // four_weight staging; four_accumulate sums
+    int64_t acc_np = 0;                     // points of the accumulated sums (0: none)
     DevBuf gq, gpart, grad, batch_desc, batch_aux;
     double batch_ms = 0.0;
     double tc_kernel_ms = 0.0;              // duration of the last single-problem tensor-core launch

@@ -1,0 +1,293 @@
+// Epilogue steps of four_run after the structure-factor sums:
+//  * four_weight (discus/prog/fourier_sup.f90:1428-1643): the dsi3d copy of
+//    dsi whose Bragg points are divided by the ratio of the grid's voxel to
+//    the reciprocal volume per unit cell of the crystal (or lot);
+//  * four_accumulate (fourier_sup.f90:3784-3840) with four_fill_csf /
+//    four_fill_dsi (:3844-4044): sums of csf and dsi over runs, kept in
+//    device memory, and the Bragg-point fill of a finished sum.
+#include <math.h>
+
+#include <complex>
+#include <vector>
+
+#include "dgpu_internal.h"
+#include "dgpu_lots.h"
+
+// ---------------------------------------------------------------------------
+// four_weight
+
+// u^T G v with the reciprocal metric (skalpro, discus/prog/metric.f90)
+static double skal(const double u[3], const double v[3], const double *g)
+{
+    double s = 0.0;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) s += u[i] * g[3 * j + i] * v[j];
+    return s;
+}
+
+// do_bang (metric.f90:35-): angle in degrees between u and w seen from the
+// origin, with the reference's single-precision degree conversion
+static double bang_deg(const double u[3], const double w[3], const double *g)
+{
+    const double xx = sqrt(skal(u, u, g)), yy = sqrt(skal(w, w, g)), xy = skal(u, w, g);
+    if (!(xx > 0.0 && yy > 0.0)) return 0.0;
+    const double arg = xy / (xx * yy);
+    if (fabs(arg) < 1.0) return acos(arg) / (double)(float)(M_PI / 180.0);
+    return arg >= 1.0 ? 0.0 : 180.0;
+}
+
+// do_volume(.FALSE., u, v, w) (metric.f90:576-605): volume spanned in the
+// reciprocal metric from lengths and the cosines of the angles
+static double recip_volume(const double u[3], const double v[3], const double w[3], const double *g)
+{
+    const double l0 = sqrt(skal(u, u, g)), l1 = sqrt(skal(v, v, g)), l2 = sqrt(skal(w, w, g));
+    const double rad = M_PI / 180.0;
+    const double c0 = cos(bang_deg(v, w, g) * rad), c1 = cos(bang_deg(u, w, g) * rad),
+                 c2 = cos(bang_deg(u, v, g) * rad);
+    const double q = 1.0 - c0 * c0 - c1 * c1 - c2 * c2 + 2.0 * c0 * c1 * c2;
+    return l0 * l1 * l2 * sqrt(q);
+}
+
+// scalef of four_weight; 1 when no correction applies (fave != 0, zero voxel)
+static double weight_scale(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op)
+{
+    if (op->fave != 0.0) return 1.0;
+    const int32_t *num = g->inc;
+    const double *uin = g->vi, *vin = g->vi + 3, *win = g->vi + 6;
+    int isdim = 3;
+    for (int k = 0; k < 3; k++)
+        if (num[k] == 1) isdim--;
+    // lot sizes when several lots ran, else the crystal's cells
+    const bool lots = dgpu_lots_on(op);
+    int64_t nlots = 1;
+    if (lots) {
+        int32_t cs[3];
+        dgpu_csize(cr, op, cs);
+        nlots = op->lot_all ? (int64_t)cs[0] * cs[1] * cs[2] : op->nlots;
+    }
+    const int32_t *n = nlots == 1 ? cr->icc : op->ls_xyz;
+    double b[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};   // b[column][component]
+    int64_t ncells = 1;
+    if (isdim == 1) {
+        // the reference tests num(1)/=1, then num(2)==1, then num(3)==1
+        int col = -1;
+        const double *vec = nullptr;
+        if (num[0] != 1) { col = 0; vec = uin; ncells = n[0]; }
+        else if (num[1] == 1) { col = 1; vec = vin; ncells = n[1]; }
+        else if (num[2] == 1) { col = 2; vec = win; ncells = n[2]; }
+        if (col >= 0) {
+            for (int k = 0; k < 3; k++) b[col][k] = vec[k];
+            // unit vectors on the remaining columns, chosen by the first
+            // non-zero component of the vector (fourier_sup.f90:1462-1504);
+            // the volume does not depend on which column holds which
+            const int o1 = (col + 1) % 3, o2 = (col + 2) % 3;
+            if (vec[0] != 0.0) { b[o1][1] = 1.0; b[o2][2] = 1.0; }
+            else if (vec[1] != 0.0) { b[o1][2] = 1.0; b[o2][0] = 1.0; }
+            else if (vec[2] != 0.0) { b[o1][0] = 1.0; b[o2][1] = 1.0; }
+        }
+    } else if (isdim == 2) {
+        // planes: the flat axis gets (1,1,1) with the components used by the
+        // two grid vectors zeroed.  The reference's third test repeats
+        // num(3)==1, so a plane with num(1)==1 reaches no branch there and
+        // its bases stay undefined; this build takes the evident intent.
+        int flat = num[2] == 1 ? 2 : num[1] == 1 ? 1 : 0;
+        const int a0 = flat == 0 ? 1 : 0, a1 = flat == 2 ? 1 : 2;
+        const double *vv[3] = {uin, vin, win};
+        for (int k = 0; k < 3; k++) {
+            b[a0][k] = vv[a0][k];
+            b[a1][k] = vv[a1][k];
+            b[flat][k] = (vv[a0][k] != 0.0 || vv[a1][k] != 0.0) ? 0.0 : 1.0;
+        }
+        ncells = (int64_t)n[a0] * n[a1];
+    } else if (isdim == 3) {
+        for (int k = 0; k < 3; k++) {
+            b[0][k] = uin[k];
+            b[1][k] = vin[k];
+            b[2][k] = win[k];
+        }
+        ncells = (int64_t)n[0] * n[1] * n[2];
+    }
+    const double voxel = recip_volume(b[0], b[1], b[2], cr->rten);
+    if (!(voxel > 0.0)) return 1.0;
+    // cr_vr, the reciprocal cell volume: sqrt(det G*)
+    const double *r = cr->rten;
+    const double det = r[0] * (r[4] * r[8] - r[7] * r[5]) - r[3] * (r[1] * r[8] - r[7] * r[2]) +
+                       r[6] * (r[1] * r[5] - r[4] * r[2]);
+    const double vr = sqrt(det);
+    return (double)(float)ncells / vr * voxel;
+}
+
+__global__ void k_weight(int32_t n0, int32_t n1, int32_t n2, double e0, double e1, double e2, PhaseGeom vg,
+                         const double *__restrict__ dsi, double *__restrict__ dsi3d, double scalef, int32_t apply)
+{
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t np = (int64_t)n0 * n1 * n2;
+    if (p >= np) return;
+    double v = dsi[p];
+    if (apply) {
+        const int64_t i = p % n0, j = (p / n0) % n1, k = p / ((int64_t)n0 * n1);
+        const double e[3] = {e0, e1, e2};
+        bool bragg = true;
+        for (int c = 0; c < 3; c++) {
+            const double h = __dadd_rn(__dadd_rn(__dadd_rn(e[c], __dmul_rn(vg.vi[c], (double)i)),
+                                                 __dmul_rn(vg.vi[3 + c], (double)j)),
+                                       __dmul_rn(vg.vi[6 + c], (double)k));
+            bragg = bragg && fabs(h - round(h)) < (double)1.0e-4f;
+        }
+        if (bragg) v = v / scalef;
+    }
+    dsi3d[p] = v;
+}
+
+extern "C" int dgpu_four_weight_device(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid,
+                                       const dgpu_opts *opts, const double *d_dsi, double *d_dsi3d)
+{
+    if (!ctx || !cr || !grid || !opts || !d_dsi || !d_dsi3d) return DGPU_ERR_ARG;
+    for (int k = 0; k < 3; k++)
+        if (grid->inc[k] < 1) return dgpu_set_error(ctx, DGPU_ERR_ARG, "inc(%d)=%d", k + 1, grid->inc[k]);
+    DGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+    const double scalef = weight_scale(cr, grid, opts);
+    const int32_t apply = opts->fave == 0.0 && fabs(scalef - 1.0) > (double)1.0e-5f;
+    PhaseGeom vg;
+    memset(&vg, 0, sizeof(vg));
+    memcpy(vg.vi, grid->vi, sizeof(vg.vi));
+    const int64_t np = (int64_t)grid->inc[0] * grid->inc[1] * grid->inc[2];
+    k_weight<<<(unsigned)dgpu_cdiv(np, 256), 256, 0, ctx->stream>>>(grid->inc[0], grid->inc[1], grid->inc[2],
+                                                                     grid->eck[0], grid->eck[1], grid->eck[2], vg,
+                                                                     d_dsi, d_dsi3d, scalef, apply);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    return DGPU_OK;
+}
+
+extern "C" int dgpu_four_weight(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid,
+                                const dgpu_opts *opts, const double *dsi, double *dsi3d)
+{
+    if (!ctx || !cr || !grid || !opts || !dsi || !dsi3d) return DGPU_ERR_ARG;
+    DGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int64_t np = (int64_t)grid->inc[0] * grid->inc[1] * grid->inc[2];
+    DGPU_CUDA(ctx, ctx->wbuf.ensure((size_t)np * 2 * sizeof(double)));
+    double *d_in = ctx->wbuf.as<double>(), *d_out = d_in + np;
+    DGPU_CUDA(ctx, cudaMemcpyAsync(d_in, dsi, np * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    int rc = dgpu_four_weight_device(ctx, cr, grid, opts, d_in, d_out);
+    if (rc) return rc;
+    DGPU_CUDA(ctx, cudaMemcpyAsync(dsi3d, d_out, np * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return DGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// four_accumulate
+
+__global__ void k_accum_add(int64_t np, const double *__restrict__ csf, const double *__restrict__ dsi,
+                            double *__restrict__ csf_sum, double *__restrict__ dsi_sum)
+{
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    csf_sum[2 * p] += csf[2 * p];
+    csf_sum[2 * p + 1] += csf[2 * p + 1];
+    dsi_sum[p] += dsi[p];
+}
+
+// four_fill_csf / four_fill_dsi with fave < 0: every Bragg point takes the
+// mean of its (up to six) grid neighbours, in place and in the reference's
+// loop order (h slowest, l fastest), so that a neighbour filled earlier is
+// seen filled.
+template <class T>
+static void fill_bragg(const dgpu_grid *g, T *a)
+{
+    const int32_t *num = g->inc;
+    const double *vi = g->vi, *eck = g->eck;
+    double step[3];
+    for (int c = 0; c < 3; c++) {
+        double m = vi[c];
+        if (vi[3 + c] > m) m = vi[3 + c];
+        if (vi[6 + c] > m) m = vi[6 + c];
+        step[c] = m * (double)0.005f;
+        if (num[c] == 1) step[c] = (double)0.0001f;
+    }
+    auto at = [&](int h, int k, int l) -> T & {
+        return a[(h - 1) + (int64_t)num[0] * ((k - 1) + (int64_t)num[1] * (l - 1))];
+    };
+    for (int h = 1; h <= num[0]; h++)
+        for (int k = 1; k <= num[1]; k++)
+            for (int l = 1; l <= num[2]; l++) {
+                bool bragg = true;
+                for (int c = 0; c < 3; c++) {
+                    const double x = eck[c] + (h - 1) * vi[c] + (k - 1) * vi[3 + c] + (l - 1) * vi[6 + c];
+                    bragg = bragg && fabs(x - round(x)) < step[c];
+                }
+                if (!bragg) continue;
+                T s = T(0);
+                int n = 0;
+                if (h > 1) { s += at(h - 1, k, l); n++; }
+                if (h < num[0]) { s += at(h + 1, k, l); n++; }
+                if (k > 1) { s += at(h, k - 1, l); n++; }
+                if (k < num[1]) { s += at(h, k + 1, l); n++; }
+                if (l > 1) { s += at(h, k, l - 1); n++; }
+                if (l < num[2]) { s += at(h, k, l + 1); n++; }
+                if (n > 0) at(h, k, l) = s / (double)(float)n;
+            }
+}
+
+extern "C" int dgpu_four_accumulate(dgpu_ctx *ctx, int32_t mode, int32_t symm, const dgpu_grid *grid, double fave,
+                                    double *csf, double *dsi)
+{
+    if (!ctx || !grid) return DGPU_ERR_ARG;
+    DGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int64_t np = (int64_t)grid->inc[0] * grid->inc[1] * grid->inc[2];
+    switch (mode) {
+    case DGPU_ACCUM_SINGLE:
+        if (symm) return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "reciprocal-space symmetry averaging");
+        return DGPU_OK;
+    case DGPU_ACCUM_INIT:
+        ctx->acc_csf.release();
+        ctx->acc_dsi.release();
+        ctx->acc_np = 0;
+        return DGPU_OK;
+    case DGPU_ACCUM_ACCUM: {
+        if (!csf || !dsi) return DGPU_ERR_ARG;
+        if (ctx->acc_np == 0) {
+            DGPU_CUDA(ctx, ctx->acc_csf.ensure((size_t)np * 2 * sizeof(double)));
+            DGPU_CUDA(ctx, ctx->acc_dsi.ensure((size_t)np * sizeof(double)));
+            DGPU_CUDA(ctx, cudaMemsetAsync(ctx->acc_csf.p, 0, (size_t)np * 2 * sizeof(double), ctx->stream));
+            DGPU_CUDA(ctx, cudaMemsetAsync(ctx->acc_dsi.p, 0, (size_t)np * sizeof(double), ctx->stream));
+            ctx->acc_np = np;
+        } else if (ctx->acc_np != np) {
+            return dgpu_set_error(ctx, DGPU_ERR_ARG, "accumulated grid has %lld points, this one %lld",
+                                  (long long)ctx->acc_np, (long long)np);
+        }
+        DGPU_CUDA(ctx, ctx->wbuf.ensure((size_t)np * 3 * sizeof(double)));
+        double *d_c = ctx->wbuf.as<double>(), *d_d = d_c + 2 * np;
+        DGPU_CUDA(ctx, cudaMemcpyAsync(d_c, csf, np * 2 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        DGPU_CUDA(ctx, cudaMemcpyAsync(d_d, dsi, np * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        k_accum_add<<<(unsigned)dgpu_cdiv(np, 256), 256, 0, ctx->stream>>>(np, d_c, d_d, ctx->acc_csf.as<double>(),
+                                                                           ctx->acc_dsi.as<double>());
+        DGPU_CUDA(ctx, cudaGetLastError());
+        DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));      // the host arrays may change after return
+        return DGPU_OK;
+    }
+    case DGPU_ACCUM_FINISHED: {
+        if (!csf || !dsi) return DGPU_ERR_ARG;
+        if (ctx->acc_np == 0)
+            return dgpu_set_error(ctx, DGPU_ERR_NO_ACCUM, "accumulation finished without accumulated sums");
+        if (symm) return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "reciprocal-space symmetry averaging");
+        if (ctx->acc_np != np)
+            return dgpu_set_error(ctx, DGPU_ERR_ARG, "accumulated grid has %lld points, this one %lld",
+                                  (long long)ctx->acc_np, (long long)np);
+        DGPU_CUDA(ctx, cudaMemcpyAsync(csf, ctx->acc_csf.p, np * 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                                       ctx->stream));
+        DGPU_CUDA(ctx, cudaMemcpyAsync(dsi, ctx->acc_dsi.p, np * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (fave < 0.0) {
+            fill_bragg(grid, reinterpret_cast<std::complex<double> *>(csf));
+            fill_bragg(grid, dsi);
+        }
+        ctx->acc_csf.release();
+        ctx->acc_dsi.release();
+        ctx->acc_np = 0;
+        return DGPU_OK;
+    }
+    default:
+        return dgpu_set_error(ctx, DGPU_ERR_ARG, "accumulate mode %d", mode);
+    }
+}

@@ -77,6 +77,37 @@ def four_run(cr: CrystalData, grid: GridData, opts: _abi.Opts, ctx=None, aver_ce
     return FourierResult(_cplx(csf, shp), _cplx(acsf, shp), dsi.reshape(shp, order="F"), info, rc)
 
 
+def four_weight(cr: CrystalData, grid: GridData, dsi, opts: _abi.Opts, ctx=None):
+    """four_weight (fourier_sup.f90:1428-1643): the dsi3d copy of dsi with
+    the Bragg points re-weighted."""
+    ctx = ctx or default_context()
+    d = np.asfortranarray(dsi, dtype=np.float64).reshape(-1, order="F").copy()
+    out = np.zeros_like(d)
+    c = cr.to_c()
+    g = grid.to_c()
+    ctx.check(ctx.lib.dgpu_four_weight(ctx.h, C.byref(c), C.byref(g), C.byref(opts), _abi.dptr(d),
+                                       _abi.dptr(out)))
+    return out.reshape(grid.inc, order="F")
+
+
+def four_accumulate(mode, grid: GridData, csf=None, dsi=None, fave=0.0, symm=0, ctx=None):
+    """four_accumulate (fourier_sup.f90:3784-3840).  ACCUM adds csf/dsi to the
+    context's sums; FINISHED returns (csf_sum, dsi_sum) and clears them."""
+    ctx = ctx or default_context()
+    g = grid.to_c()
+    np_ = grid.npoints
+    if csf is None:
+        cbuf, dbuf = np.zeros(2 * np_), np.zeros(np_)
+    else:
+        z = np.asfortranarray(csf).reshape(-1, order="F")
+        cbuf = np.empty(2 * np_)
+        cbuf[0::2], cbuf[1::2] = z.real, z.imag
+        dbuf = np.asfortranarray(dsi, dtype=np.float64).reshape(-1, order="F").copy()
+    ctx.check(ctx.lib.dgpu_four_accumulate(ctx.h, int(mode), int(symm), C.byref(g), float(fave),
+                                           _abi.dptr(cbuf), _abi.dptr(dbuf)))
+    return _cplx(cbuf, grid.inc), dbuf.reshape(grid.inc, order="F")
+
+
 def fourier_lmn(eck, vi, inc, ctx=None):
     """fourier_lmn (discus/prog/fourier_lmn_mod.f90:4-280): (rc, lmn[6], off_shift(3,3))."""
     ctx = ctx or default_context()

@@ -39,6 +39,7 @@ extern "C" {
 #define DGPU_ERR_CANCELLED   (-14)  /* cancel flag seen (ier_num=-14, ER_COMM, like ier_ctrlc)  */
 #define DGPU_ERR_NO_ATOMS   (-198)  /* cr_natoms < 1 (ier_num=-198, ER_APPL)                   */
 #define DGPU_ERR_SCRATCH_SIZE (-20) /* request exceeds a fixed scratch capacity                */
+#define DGPU_ERR_NO_ACCUM   (-175)  /* accumulation finished without sums (ier_num=-175, ER_APPL) */
 
 /* ---- tables (discus/prog/discus_config_mod.f90:27-28, diffuse_mod.f90:20-21) */
 #define DGPU_CFPKT   9999          /* last index of the sin(theta)/lambda table              */
@@ -237,6 +238,33 @@ int dgpu_four_formtab(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *op
 int dgpu_four_increments(dgpu_ctx *ctx, const double *xat, int64_t nxat,
                          const double uin[3], const double vin[3], const double win[3],
                          const double off_shift[9], int64_t *inc_out);
+
+/* ---- epilogue steps of four_run after the sums --------------------------- */
+/* four_weight (fourier_sup.f90:1428-1643): dsi3d = dsi, except that with
+ * fave == 0 the Bragg points (h, k, l all within 1e-4 of integers) are
+ * divided by scalef = ncells * voxel / V*, the number of unit cells (or lot
+ * cells) along the grid's dimensions times the reciprocal volume of one grid
+ * step over that of the cell, when |scalef - 1| > 1e-5.  cr supplies icc and
+ * rten; opts supplies fave and the lot size.  Host arrays of num points.   */
+int dgpu_four_weight(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid,
+                     const dgpu_opts *opts, const double *dsi, double *dsi3d);
+/* Same with device arrays; enqueued on the context's stream. */
+int dgpu_four_weight_device(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid,
+                            const dgpu_opts *opts, const double *d_dsi, double *d_dsi3d);
+
+/* four_accumulate (fourier_sup.f90:3784-3840): sums of csf and dsi over
+ * several runs, kept in the context's device memory.  mode (diffuse_mod.f90:
+ * 154-157): INIT clears the sums, ACCUM adds csf/dsi (host arrays of the
+ * grid), FINISHED writes the sums into csf/dsi and clears them (with
+ * fave < 0 the Bragg points first take the mean of their grid neighbours,
+ * four_fill_csf/four_fill_dsi :3844-4044), SINGLE does nothing.  symm != 0
+ * (reciprocal-space symmetry averaging) is DGPU_ERR_UNSUPPORTED.            */
+#define DGPU_ACCUM_INIT      (-1)
+#define DGPU_ACCUM_SINGLE      0
+#define DGPU_ACCUM_ACCUM       1
+#define DGPU_ACCUM_FINISHED    2
+int dgpu_four_accumulate(dgpu_ctx *ctx, int32_t mode, int32_t symm, const dgpu_grid *grid, double fave,
+                         double *csf, double *dsi);
 
 /* ---- adjoint: chi^2 and its gradient ------------------------------------- */
 /* chi2 = sum_h w(h) (I(h) - I_target(h))^2 over the full grid, I = diff_scale*|csf|^2

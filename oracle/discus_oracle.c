@@ -1031,3 +1031,158 @@ double oc_time_ref_rows(const dgpu_crystal *cr, const dgpu_grid *g, int32_t row_
     if (pairs_out) *pairs_out = pairs;
     return t1 - t0;
 }
+
+/* ---------------------------------------------------------------------- */
+/* four_weight, fourier_sup.f90:1428-1643, with do_volume / do_bang /
+ * do_blen (discus/prog/metric.f90:6-60, 576-605) in the reciprocal metric. */
+static double oc_skal(const double *u, const double *v, const double *g)
+{
+    double s = 0;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) s += u[i] * M3(g, i, j) * v[j];
+    return s;
+}
+
+static double oc_bang(const double *u, const double *w, const double *g)
+{
+    double xx = sqrt(oc_skal(u, u, g)), yy = sqrt(oc_skal(w, w, g)), xy = oc_skal(u, w, g);
+    if (!(xx > 0 && yy > 0)) return 0.0;
+    double arg = xy / (xx * yy);
+    const float rad_sp = (float)(3.1415926535897932384626433832795028841971693993751 / 180.0);
+    if (fabs(arg) < 1.0) return acos(arg) / (double)rad_sp;
+    return arg >= 1.0 ? 0.0 : 180.0;
+}
+
+static double oc_volume(const double *u, const double *v, const double *w, const double *g)
+{
+    const double rad = 3.1415926535897932384626433832795028841971693993751 / 180.0;
+    double l1 = sqrt(oc_skal(u, u, g)), l2 = sqrt(oc_skal(v, v, g)), l3 = sqrt(oc_skal(w, w, g));
+    double c1 = cos(oc_bang(v, w, g) * rad), c2 = cos(oc_bang(u, w, g) * rad), c3 = cos(oc_bang(u, v, g) * rad);
+    return l1 * l2 * l3 * sqrt(1.0 - c1 * c1 - c2 * c2 - c3 * c3 + 2.0 * c1 * c2 * c3);
+}
+
+int oc_four_weight(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op, const double *dsi,
+                   double *dsi3d, double *scalef_out)
+{
+    const int32_t *num = g->inc;
+    const double *uin = g->vi, *vin = g->vi + 3, *win = g->vi + 6;
+    int64_t np = (int64_t)num[0] * num[1] * num[2];
+    double scalef = 1.0;
+    if (op->fave == 0.0) {
+        int isdim = 3;
+        for (int k = 0; k < 3; k++) if (num[k] == 1) isdim--;
+        int32_t cs[3];
+        oc_csize(cr, op, cs);
+        int64_t nlots = !oc_lots_on(op) ? 1 : op->lot_all ? (int64_t)cs[0] * cs[1] * cs[2] : op->nlots;
+        const int32_t *n = nlots == 1 ? cr->icc : op->ls_xyz;
+        double B[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};     /* bases(3,3), column-major */
+        int64_t ncells = 1;
+        if (isdim == 1) {
+            if (num[0] != 1) {
+                for (int k = 0; k < 3; k++) B[k] = uin[k];
+                if (B[0] != 0) { B[3 + 1] = 1; B[6 + 2] = 1; }
+                else if (B[1] != 0) { B[3 + 2] = 1; B[6 + 0] = 1; }
+                else if (B[2] != 0) { B[3 + 0] = 1; B[6 + 1] = 1; }
+                ncells = n[0];
+            } else if (num[1] == 1) {
+                for (int k = 0; k < 3; k++) B[3 + k] = vin[k];
+                if (B[3] != 0) { B[0 + 1] = 1; B[6 + 2] = 1; }
+                else if (B[4] != 0) { B[0 + 2] = 1; B[6 + 0] = 1; }
+                else if (B[5] != 0) { B[0 + 0] = 1; B[6 + 1] = 1; }
+                ncells = n[1];
+            } else if (num[2] == 1) {
+                for (int k = 0; k < 3; k++) B[6 + k] = win[k];
+                if (B[6] != 0) { B[0 + 1] = 1; B[3 + 2] = 1; }
+                else if (B[7] != 0) { B[0 + 2] = 1; B[3 + 0] = 1; }
+                else if (B[8] != 0) { B[0 + 0] = 1; B[3 + 1] = 1; }
+                ncells = n[2];
+            }
+        } else if (isdim == 2) {
+            if (num[2] == 1) {
+                for (int k = 0; k < 3; k++) { B[k] = uin[k]; B[3 + k] = vin[k]; B[6 + k] = 1.0; }
+                for (int k = 0; k < 3; k++) if (B[k] != 0 || B[3 + k] != 0) B[6 + k] = 0.0;
+                ncells = (int64_t)n[0] * n[1];
+            } else if (num[1] == 1) {
+                for (int k = 0; k < 3; k++) { B[k] = uin[k]; B[3 + k] = 1.0; B[6 + k] = win[k]; }
+                for (int k = 0; k < 3; k++) if (B[k] != 0 || B[6 + k] != 0) B[3 + k] = 0.0;
+                ncells = (int64_t)n[0] * n[2];
+            } else {
+                /* the reference's third test repeats num(3)==1 and leaves
+                 * bases undefined here; the evident intent: */
+                for (int k = 0; k < 3; k++) { B[k] = 1.0; B[3 + k] = vin[k]; B[6 + k] = win[k]; }
+                for (int k = 0; k < 3; k++) if (B[3 + k] != 0 || B[6 + k] != 0) B[k] = 0.0;
+                ncells = (int64_t)n[1] * n[2];
+            }
+        } else if (isdim == 3) {
+            for (int k = 0; k < 3; k++) { B[k] = uin[k]; B[3 + k] = vin[k]; B[6 + k] = win[k]; }
+            ncells = (int64_t)n[0] * n[1] * n[2];
+        }
+        double voxel = oc_volume(B, B + 3, B + 6, cr->rten);
+        if (voxel > 0.0) {
+            const double *r = cr->rten;
+            double det = M3(r,0,0) * (M3(r,1,1) * M3(r,2,2) - M3(r,1,2) * M3(r,2,1))
+                       - M3(r,0,1) * (M3(r,1,0) * M3(r,2,2) - M3(r,1,2) * M3(r,2,0))
+                       + M3(r,0,2) * (M3(r,1,0) * M3(r,2,1) - M3(r,1,1) * M3(r,2,0));
+            scalef = (double)(float)ncells / sqrt(det) * voxel;
+        }
+    }
+    if (scalef_out) *scalef_out = scalef;
+    if (op->fave == 0.0 && fabs(scalef - 1.0) > (double)1.0e-5f) {
+        int64_t ii = 0;
+        for (int32_t k = 0; k < num[2]; k++)
+            for (int32_t j = 0; j < num[1]; j++)
+                for (int32_t i = 0; i < num[0]; i++, ii++) {
+                    int bragg = 1;
+                    for (int c = 0; c < 3; c++) {
+                        double h = g->eck[c] + g->vi[c] * i + g->vi[3 + c] * j + g->vi[6 + c] * k;
+                        bragg = bragg && fabs(h - (double)llround(h)) < (double)1.0e-4f;
+                    }
+                    dsi3d[ii] = bragg ? dsi[ii] / scalef : dsi[ii];
+                }
+    } else {
+        memcpy(dsi3d, dsi, sizeof(double) * np);
+    }
+    return 0;
+}
+
+/* four_fill_csf / four_fill_dsi with fave < 0 (fourier_sup.f90:3844-4044):
+ * in place, h slowest; comp = 2 for interleaved complex, 1 for real. */
+void oc_fill_bragg(const dgpu_grid *g, double *a, int comp)
+{
+    const int32_t *num = g->inc;
+    const double *vi = g->vi;
+    double step[3];
+    for (int c = 0; c < 3; c++) {
+        double m = vi[c];
+        if (vi[3 + c] > m) m = vi[3 + c];
+        if (vi[6 + c] > m) m = vi[6 + c];
+        step[c] = m * (double)0.005f;
+        if (num[c] == 1) step[c] = (double)0.0001f;
+    }
+#define AT(h, k, l) (a + comp * ((int64_t)((h) - 1) + (int64_t)num[0] * (((k) - 1) + (int64_t)num[1] * ((l) - 1))))
+    for (int32_t h = 1; h <= num[0]; h++)
+        for (int32_t k = 1; k <= num[1]; k++)
+            for (int32_t l = 1; l <= num[2]; l++) {
+                int bragg = 1;
+                for (int c = 0; c < 3; c++) {
+                    double x = g->eck[c] + (h - 1) * vi[c] + (k - 1) * vi[3 + c] + (l - 1) * vi[6 + c];
+                    bragg = bragg && fabs(x - (double)llround(x)) < step[c];
+                }
+                if (!bragg) continue;
+                double s[2] = {0, 0};
+                int np = 0;
+                const int nb[6][3] = {{h - 1, k, l}, {h + 1, k, l}, {h, k - 1, l}, {h, k + 1, l}, {h, k, l - 1}, {h, k, l + 1}};
+                const int ok[6] = {h > 1, h < num[0], k > 1, k < num[1], l > 1, l < num[2]};
+                for (int q = 0; q < 6; q++)
+                    if (ok[q]) {
+                        const double *v = AT(nb[q][0], nb[q][1], nb[q][2]);
+                        for (int c = 0; c < comp; c++) s[c] += v[c];
+                        np++;
+                    }
+                if (np > 0) {
+                    double *t = AT(h, k, l);
+                    for (int c = 0; c < comp; c++) t[c] = s[c] / (double)(float)np;
+                }
+            }
+#undef AT
+}

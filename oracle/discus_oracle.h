@@ -52,6 +52,9 @@ int  oc_four_run(const dgpu_crystal *cr, const dgpu_grid *grid, const dgpu_opts 
 int  oc_chi2_grad(const dgpu_crystal *cr, const dgpu_grid *grid, const dgpu_opts *op,
                   const double *i_target, const double *weight, double *chi2,
                   double *grad_pos, double *grad_occ, int nthreads);
+int  oc_four_weight(const dgpu_crystal *cr, const dgpu_grid *grid, const dgpu_opts *op,
+                    const double *dsi, double *dsi3d, double *scalef);
+void oc_fill_bragg(const dgpu_grid *grid, double *a, int comp);
 double oc_time_ref_rows(const dgpu_crystal *cr, const dgpu_grid *grid, int32_t row_lo,
                         int32_t row_hi, int nthreads, int64_t *pairs_out);
 

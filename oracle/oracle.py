@@ -41,6 +41,10 @@ def lib():
         L.oc_time_ref_rows.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Grid), C.c_int32,
                                        C.c_int32, C.c_int, C.POINTER(C.c_int64)]
         L.oc_time_ref_rows.restype = C.c_double
+        L.oc_four_weight.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Grid), C.POINTER(_abi.Opts),
+                                     dp, dp, dp]
+        L.oc_fill_bragg.argtypes = [C.POINTER(_abi.Grid), dp, C.c_int]
+        L.oc_fill_bragg.restype = None
         _lib = L
     return _lib
 
@@ -172,3 +176,28 @@ def time_ref_rows(cr, grid, row_lo, row_hi, nthreads=0):
     sec = lib().oc_time_ref_rows(C.byref(c), C.byref(g), int(row_lo), int(row_hi), int(nthreads),
                                  C.byref(pairs))
     return sec, int(pairs.value)
+
+
+def four_weight(cr, grid, dsi, opts):
+    """(dsi3d, scalef) of four_weight."""
+    c = cr.to_c()
+    g = grid.to_c()
+    d = np.asfortranarray(dsi, dtype=np.float64).reshape(-1, order="F").copy()
+    out = np.zeros_like(d)
+    sc = np.zeros(1)
+    lib().oc_four_weight(C.byref(c), C.byref(g), C.byref(opts), _d(d), _d(out), _d(sc))
+    return out.reshape(grid.inc, order="F"), float(sc[0])
+
+
+def fill_bragg(grid, arr):
+    """four_fill_csf / four_fill_dsi (fave < 0) on a copy of arr."""
+    g = grid.to_c()
+    if np.iscomplexobj(arr):
+        z = np.asfortranarray(arr).reshape(-1, order="F")
+        buf = np.empty(2 * z.size)
+        buf[0::2], buf[1::2] = z.real, z.imag
+        lib().oc_fill_bragg(C.byref(g), _d(buf), 2)
+        return (buf[0::2] + 1j * buf[1::2]).reshape(grid.inc, order="F")
+    buf = np.asfortranarray(arr, dtype=np.float64).reshape(-1, order="F").copy()
+    lib().oc_fill_bragg(C.byref(g), _d(buf), 1)
+    return buf.reshape(grid.inc, order="F")

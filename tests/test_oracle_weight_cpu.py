@@ -1,0 +1,93 @@
+"""four_weight and the Bragg fill of four_accumulate in the oracle, against
+closed forms (CPU only).
+
+The voxel of four_weight is the reciprocal volume of the grid steps
+(do_volume from lengths and angles); divided by the reciprocal cell volume
+it is |det(bases)| exactly, so scalef = ncells * |det(bases)| up to the
+reference's single-precision degree conversion (1e-6 here).
+"""
+import numpy as np
+
+from diffusecode_gb300 import _abi
+from diffusecode_gb300.structures import GridData, reciprocal_metric, small_lots_anis
+from oracle import oracle as O
+
+
+def _grid(vi, inc, lo=(-1.0, -1.0, 0.0)):
+    vi = np.asarray(vi, dtype=np.float64)
+    lo = np.asarray(lo, dtype=np.float64)
+    eck = np.stack([lo, lo + vi[:, 0] * (inc[0] - 1), lo + vi[:, 1] * (inc[1] - 1), lo + vi[:, 2] * (inc[2] - 1)],
+                   axis=1)
+    return GridData(eck=eck, vi=vi, inc=inc)
+
+
+def _crystal(icc, rten):
+    cr, _ = small_lots_anis(anis=False, icc=icc)
+    cr.rten = rten
+    return cr
+
+
+def test_weight_scale_closed_forms():
+    rt = reciprocal_metric(4.1, 4.6, 5.3, 90, 103, 90)
+    cr = _crystal((5, 4, 3), rt)
+    cases = [
+        # 3D, oblique steps: bases = vi
+        (np.array([[0.1, 0.02, 0.0], [0.0, 0.2, 0.01], [0.03, 0.0, 0.25]]), (9, 7, 5), 60),
+        # hk0 plane: the flat column is (0, 0, 1)
+        (np.array([[0.05, 0.0, 0.0], [0.0, 0.05, 0.0], [0.0, 0.0, 0.0]]), (21, 21, 1), 20),
+        # h0l plane
+        (np.array([[0.05, 0.0, 0.0], [0.0, 0.0, 0.0], [0.0, 0.0, 0.04]]), (21, 1, 21), 15),
+        # row along a*: columns v, e2, e3
+        (np.array([[0.05, 0.0, 0.0], [0.0, 0.0, 0.0], [0.0, 0.0, 0.0]]), (41, 1, 1), 5),
+    ]
+    for vi, inc, ncells in cases:
+        g = _grid(vi, inc)
+        B = vi.copy()
+        if inc[2] == 1 and inc[1] > 1:
+            B[:, 2] = [0, 0, 1]
+        elif inc[1] == 1 and inc[2] > 1:
+            B[:, 1] = [0, 1, 0]
+        elif inc[1] == 1 and inc[2] == 1:
+            B[:, 1], B[:, 2] = [0, 1, 0], [0, 0, 1]
+        dsi = np.random.default_rng(1).random(inc) + 1.0
+        d3, scalef = O.four_weight(cr, g, dsi, _abi.default_opts())
+        assert abs(scalef - ncells * abs(np.linalg.det(B))) <= 1e-6 * scalef, (inc, scalef)
+        hkl = g.hkl()
+        bragg = np.all(np.abs(hkl - np.rint(hkl)) < np.float32(1e-4), axis=0)
+        assert bragg.any()
+        np.testing.assert_allclose(d3[bragg], dsi[bragg] / scalef, rtol=1e-15)
+        np.testing.assert_array_equal(d3[~bragg], dsi[~bragg])
+
+
+def test_weight_lots_and_aver():
+    cr = _crystal((6, 5, 4), reciprocal_metric(4, 4, 4, 90, 90, 90))
+    g = _grid(np.diag([0.1, 0.1, 0.1]), (11, 11, 11))
+    dsi = np.ones(g.inc)
+    _, s_all = O.four_weight(cr, g, dsi, _abi.default_opts())
+    op = _abi.default_opts(ilots=_abi.LOT_BOX, ls_xyz=(3, 2, 2), nlots=7)
+    _, s_lot = O.four_weight(cr, g, dsi, op)
+    assert abs(s_all - 120 * 1e-3) < 1e-9 and abs(s_lot - 12 * 1e-3) < 1e-9
+    d3, s = O.four_weight(cr, g, dsi, _abi.default_opts(fave=1.0))
+    assert s == 1.0 and np.array_equal(d3, dsi)
+
+
+def test_fill_bragg_neighbour_mean():
+    g = _grid(np.diag([0.25, 0.25, 0.0]), (9, 9, 1), lo=(-1.0, -1.0, 0.0))
+    rng = np.random.default_rng(2)
+    d = rng.random(g.inc)
+    out = O.fill_bragg(g, d)
+    z = d + 1j * rng.random(g.inc)
+    zout = O.fill_bragg(g, z)
+    hkl = g.hkl()
+    ref, zref = d.copy(), z.copy()
+    for h in range(9):                      # reference order: h slowest (no Bragg neighbours here)
+        for k in range(9):
+            x = hkl[:, h, k, 0]
+            if np.all(np.abs(x - np.rint(x)) < [0.25 * np.float32(0.005)] * 2 + [np.float32(1e-4)]):
+                nb = [(h + a, k + b) for a, b in ((-1, 0), (1, 0), (0, -1), (0, 1))
+                      if 0 <= h + a < 9 and 0 <= k + b < 9]
+                ref[h, k, 0] = np.mean([ref[p, q, 0] for p, q in nb])
+                zref[h, k, 0] = np.mean([zref[p, q, 0] for p, q in nb])
+    np.testing.assert_allclose(out, ref, rtol=1e-14)
+    np.testing.assert_allclose(zout, zref, rtol=1e-14)
+    assert not np.array_equal(out, d)
