@@ -119,7 +119,6 @@ static int check_inputs(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
         return dgpu_set_error(ctx, DGPU_ERR_ARG, "phase=%d", op->phase);
     if (op->form != DGPU_FORM_TABLE && op->form != DGPU_FORM_ANALYTIC)
         return dgpu_set_error(ctx, DGPU_ERR_ARG, "form=%d", op->form);
-    if (op->fave < 0.0) return dgpu_set_error(ctx, DGPU_ERR_ARG, "fave=%g", op->fave);
     if (op->fave > 0.0 && op->fave < 1.0 && !op->aver_cells)
         return dgpu_set_error(ctx, DGPU_ERR_ARG, "0<fave<1 needs the caller's cell selection");
     if (op->diff_scale < 0.0) return dgpu_set_error(ctx, DGPU_ERR_ARG, "diff_scale<0");
@@ -286,7 +285,11 @@ int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g,
     int64_t ts[2 * 64 + 4];
 
     // ---- <F> (four_aver): cells drawn over csize, lattice of the crystal or of a lot ----
-    if (op->fave != 0.0) {
+    if (op->fave < 0.0) {
+        // ran1 <= fave never holds: no cell, <F> = 0 and the +1 warning (fourier_sup.f90:1235-1241,1323-1331)
+        warn = DGPU_WARN_NO_CELL;
+        dgpu_set_error(ctx, DGPU_WARN_NO_CELL, "no unit cell selected for <F>");
+    } else if (op->fave != 0.0) {
         const int64_t ncells = (int64_t)cr->icc[0] * cr->icc[1] * cr->icc[2];
         FoldSpec fold = {1, cr->ncatoms, {cr->icc[0], cr->icc[1], cr->icc[2]},
                          {cr->dim0[0], cr->dim0[1], cr->dim0[2]}, nullptr};
@@ -378,7 +381,7 @@ int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g,
         if (cancelled(op)) return dgpu_set_error(ctx, DGPU_ERR_CANCELLED, "cancelled");
     }
 
-    const double2 *acsf_in = op->fave != 0.0 ? d_acsf : nullptr;
+    const double2 *acsf_in = op->fave > 0.0 ? d_acsf : nullptr;
     if (!lots) {
         // ---- type or group sums (fourier_sup.f90:195-244) ----
         FoldSpec nofold = {0, cr->ncatoms, {cr->icc[0], cr->icc[1], cr->icc[2]}, {0, 0, 0}, nullptr};

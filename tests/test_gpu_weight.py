@@ -64,3 +64,16 @@ def test_four_accumulate(oracle, ctx):
         with pytest.raises(Exception) as e:
             FR.four_accumulate(mode, g, runs[0][0], runs[0][1], ctx=ctx, **kw)
         assert getattr(e.value, "code", None) == code
+
+
+def test_negative_fave_is_no_cell(oracle, ctx):
+    """fave < 0: four_aver draws no cell (<F> = 0, warning +1), as the
+    reference does; the Bragg fill of four_accumulate keys on it."""
+    cr, g = S.small_lots_anis(anis=False)
+    op = K.opts(phase=_abi.PHASE_EXACT64, fave=-1.0)
+    rc, csf, acsf, dsi, info = oracle.four_run(cr, g, op)
+    r = FR.four_run(cr, g, op, ctx=ctx)
+    assert rc == r.status == _abi.DGPU_WARN_NO_CELL
+    assert not np.any(r.acsf) and not np.any(acsf)
+    r0 = FR.four_run(cr, g, K.opts(phase=_abi.PHASE_EXACT64), ctx=ctx)
+    np.testing.assert_allclose(r.dsi, r0.dsi, rtol=1e-12)
