@@ -40,8 +40,9 @@
 // Partials: part[(t*nslice + ks)*slab + c*nrows_p + rg], a column-major image
 // of the tile space (rows with na >= fra are never written).
 //
-// Warp roles (416 threads): warps 0-7 produce operand stages, warp 8 owns
-// TMEM and issues the MMAs (one elected lane), warps 9-12 drain TMEM.  All
+// Warp roles (448 threads): warps 0-7 produce operand stages, warp 8 owns
+// TMEM and issues the MMAs (one elected lane), warps 9-12 drain TMEM, warp 13
+// streams the V operand images into their ring (one lane).  All
 // waits are bounded (globaltimer); a wait that gives up sets an error flag,
 // the CTA stops issuing, waits for its own MMAs, frees TMEM and returns.
 //
@@ -56,7 +57,8 @@
 #define TC_PROD_WARPS 8
 #define TC_MMA_WARP 8
 #define TC_EPI_WARP0 9
-#define TC_THREADS (13 * 32)
+#define TC_COPY_WARP 13
+#define TC_THREADS (14 * 32)
 #define TC_PROD_THREADS (TC_PROD_WARPS * 32)
 #define TC_A_BYTES (TC_M * TC_KA * 2)          // one A operand (e.g. Ur_hi): 8 KB
 // phase data of one 32-atom group in shared memory:
@@ -240,6 +242,126 @@ __device__ __forceinline__ void gen_rows(int q0, int q1, int mt, int gpn, const 
     }
 }
 
+// 2 complex values (2 consecutive atoms of one row) -> the hi and lo words of
+// the real and imaginary parts, low half = first atom.
+template <bool BF>
+__device__ __forceinline__ void split_c2(const float2 (&x)[2], uint32_t &rh, uint32_t &rl, uint32_t &ih,
+                                         uint32_t &il)
+{
+    const uint32_t mask = BF ? 0xFFFF0000u : 0xFFFFE000u;
+    const float hr0 = __uint_as_float(__float_as_uint(x[0].x) & mask);
+    const float hr1 = __uint_as_float(__float_as_uint(x[1].x) & mask);
+    const float hi0 = __uint_as_float(__float_as_uint(x[0].y) & mask);
+    const float hi1 = __uint_as_float(__float_as_uint(x[1].y) & mask);
+    rh = pack2<BF>(hr0, hr1);
+    rl = pack2<BF>(x[0].x - hr0, x[1].x - hr1);
+    ih = pack2<BF>(hi0, hi1);
+    il = pack2<BF>(x[0].y - hi0, x[1].y - hi1);
+}
+
+// U rows of one stage, stored with stmatrix: warp w generates atom chunk
+// c = w & 3 (atoms 8c..8c+7) of row groups 8 (w >> 2) .. 8 (w >> 2) + 7; lane
+// l owns row l >> 2 of each group and atoms 8c + 2 (l & 3) + {0, 1}, the
+// fragment layout of an 8x8 b16 matrix, so that one stmatrix.x4 stores four
+// row groups of one operand array.  Values step from group to group by
+// exp(2 pi i 8 d_ra) on two chains (even and odd groups, by its square) and
+// restart from the exact phase at every group that begins a new nb.
+template <bool BF>
+__device__ __forceinline__ void gen_rows_stm(int mt, int gpn, const uint8_t *as, uint8_t *A, int lane, int warp)
+{
+    const uint64_t *s_ph0 = reinterpret_cast<const uint64_t *>(as);
+    const uint64_t *s_dra = s_ph0 + TC_KA, *s_drb = s_dra + TC_KA;
+    const float *s_w = reinterpret_cast<const float *>(as + TC_SLOT_W);
+    const float2 *s_ma = reinterpret_cast<const float2 *>(as + TC_SLOT_MA);
+    const int c = warp & 3;
+    const int q0 = (warp >> 2) * 8;
+    const int s = lane >> 2;
+    const int k0 = 8 * c + 2 * (lane & 3);
+    const uint32_t adr = smem_u32(A) + (uint32_t)(q0 + (lane >> 3)) * TC_SBO + sw_off(lane & 7, c);
+    uint64_t ph0[2], dra[2], drb[2];
+    float w[2];
+    float2 m[2], m2[2];
+#pragma unroll
+    for (int a = 0; a < 2; a++) {
+        ph0[a] = s_ph0[k0 + a];
+        dra[a] = s_dra[k0 + a];
+        drb[a] = s_drb[k0 + a];
+        w[a] = s_w[k0 + a];
+        m[a] = s_ma[k0 + a];
+        m2[a] = cmulf(m[a], m[a]);
+    }
+    // segments of constant nb: bit o of bmask marks group G0 + o as the first
+    // of a segment (one division per stage, no other)
+    const int G0 = mt * (TC_M / 8) + q0;
+    const int gi0 = G0 % gpn;
+    const uint32_t nb0 = (uint32_t)(G0 / gpn);
+    uint32_t bmask = 0;
+    {
+        int gi = gi0;
+#pragma unroll
+        for (int o = 0; o < 8; o++) {
+            if (o > 0 && gi == 0) bmask |= 1u << o;
+            if (++gi == gpn) gi = 0;
+        }
+    }
+    // exact value at group G0 + o: offset 0, or the start of a segment
+    auto seed = [&](int o, float2 (&x)[2]) {
+        const uint32_t na = (uint32_t)((o == 0 ? gi0 * 8 : 0) + s);
+        const uint32_t nb = nb0 + (uint32_t)__popc(bmask & ((2u << o) - 1u));
+#pragma unroll
+        for (int a = 0; a < 2; a++) {
+            const float2 p = phasor_fast(ph0[a] + (uint64_t)na * dra[a] + (uint64_t)nb * drb[a]);
+            x[a] = make_float2(p.x * w[a], p.y * w[a]);
+        }
+    };
+    auto starts = [&](int o) { return ((bmask >> o) & 1u) != 0u; };
+    float2 e[2], o[2];                 // groups G0 + 2p (even chain) and G0 + 2p + 1 (odd chain)
+    seed(0, e);
+    if (starts(1)) seed(1, o);
+    else {
+#pragma unroll
+        for (int a = 0; a < 2; a++) o[a] = cmulf(e[a], m[a]);
+    }
+    uint32_t R[4][4];                  // [operand array][matrix = group within four]
+#pragma unroll
+    for (int p = 0; p < 4; p++) {
+        const int i = (2 * p) & 3;
+        split_c2<BF>(e, R[0][i], R[1][i], R[2][i], R[3][i]);
+        split_c2<BF>(o, R[0][i + 1], R[1][i + 1], R[2][i + 1], R[3][i + 1]);
+        if (p & 1) {
+            const uint32_t base = adr + (uint32_t)(2 * (p - 1)) * TC_SBO;
+#pragma unroll
+            for (int arr = 0; arr < 4; arr++)
+                stmatrix_x4(base + arr * TC_A_BYTES, R[arr][0], R[arr][1], R[arr][2], R[arr][3]);
+        }
+        if (p < 3) {
+            const int ge = 2 * p + 2, go = ge + 1;      // offsets of the next pair
+            float2 ne[2], no[2];
+            if (starts(ge)) seed(ge, ne);
+            else if (starts(ge - 1)) {
+#pragma unroll
+                for (int a = 0; a < 2; a++) ne[a] = cmulf(o[a], m[a]);
+            } else {
+#pragma unroll
+                for (int a = 0; a < 2; a++) ne[a] = cmulf(e[a], m2[a]);
+            }
+            if (starts(go)) seed(go, no);
+            else if (starts(ge)) {
+#pragma unroll
+                for (int a = 0; a < 2; a++) no[a] = cmulf(ne[a], m[a]);
+            } else {
+#pragma unroll
+                for (int a = 0; a < 2; a++) no[a] = cmulf(o[a], m2[a]);
+            }
+#pragma unroll
+            for (int a = 0; a < 2; a++) {
+                e[a] = ne[a];
+                o[a] = no[a];
+            }
+        }
+    }
+}
+
 // V columns of one stage for column groups [q0, q1) of the tile: atoms
 // k0..k0+3, column 8q+s of every group, stepping by exp(2 pi i 8 d_ac).
 // B rows: Vr at c, Vi at N+c, -Vr at 2N+c, in a hi and a lo operand.
@@ -331,7 +453,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
         // (s = lane&7, j = atom quad, u) takes range u for its atom quad.
         const int tid = threadIdx.x;
         const int s = lane & 7, j = (lane >> 3) + 4 * (warp & 1), u = warp >> 1;
-        uint32_t vnext = 0, vwait = 0;      // thread 0: next stage to copy V for / first not known landed
         uint32_t it = 0;
         bool ok = true;                     // this thread saw no failed wait
         for (int64_t item = blockIdx.x; item < L.nitems; item += gridDim.x) {
@@ -348,24 +469,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
             const int N = g.N, gpn = g.fra_p >> 3;
             // with V images the column groups arrive by bulk copy into the ring
             const uint8_t *vimg = L.vring ? g.vimg : nullptr;
-            const int64_t g0 = a0 / TC_KA;
-            const int ntl = g.n_tiles;
             const int ngr = TC_M / 8, ntot = ngr + (vimg ? 0 : (N >> 3)), per = (ntot + 3) >> 2;
-            // thread 0: V copy of item stage y (global stage x) once its slot is free
-            auto issue_v = [&](uint32_t x, int y) -> bool {
-                const int v = (int)(x % TC_VSLOTS);
-                if (x >= TC_VSLOTS) {
-                    if (!mbar_wait(&vempty[v], ((x / TC_VSLOTS) - 1) & 1, err, 9)) return false;
-                    vwait = x - TC_VSLOTS + 1;          // the MMAs consumed that copy: it landed
-                }
-                mbar_arrive_tx(&vfull[v], vbytes);
-                bulk_g2s(vring + (size_t)v * vbytes, vimg + ((g0 + y) * ntl + nt) * (int64_t)vbytes, vbytes,
-                         &vfull[v]);
-                vnext = x + 1;
-                return true;
-            };
-            if (vimg && tid == 0)
-                for (int y = 0; y < 2 && y < nst && ok; y++) ok = issue_v(it + y, y);
             const int r0 = u * per, r1 = min(ntot, r0 + per);
             const int ra0 = min(r0, ngr), ra1 = min(r1, ngr);           // row groups
             const int rc0 = max(r0, ngr) - ngr, rc1 = max(r1, ngr) - ngr; // column groups
@@ -388,19 +492,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
                     cp_async_commit();
                 const uint8_t *as = aslot + (st % TC_NSLOT) * TC_ATOM_SLOT;
                 uint8_t *A = smem + (size_t)sb * stage_bytes;
-                if (ok && vimg && tid == 0 && st + 2 < nst) ok = issue_v(it + 2, st + 2);
-                if (ok && ra0 < ra1) gen_rows<BF>(ra0, ra1, mt, gpn, as, A, s, j);
-                if (ok && rc0 < rc1) gen_cols<BF>(rc0, rc1, nt, N, as, A + 4 * TC_A_BYTES, b_bytes, s, j);
+                if (vimg) {
+                    gen_rows_stm<BF>(mt, gpn, as, A, lane, warp);     // rows only, by stmatrix
+                } else {
+                    if (ok && ra0 < ra1) gen_rows<BF>(ra0, ra1, mt, gpn, as, A, s, j);
+                    if (ok && rc0 < rc1) gen_cols<BF>(rc0, rc1, nt, N, as, A + 4 * TC_A_BYTES, b_bytes, s, j);
+                }
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&full[sb]);   // one arrival per producer warp
             }
             cp_async_wait0();
         }
-        // let this thread's bulk copies land before the CTA can exit (after an
-        // error the MMA side may not have waited for them)
-        if (tid == 0)
-            for (uint32_t x = vwait; x < vnext; x++) mbar_wait_quiet(&vfull[x % TC_VSLOTS], (x / TC_VSLOTS) & 1);
     } else if (warp == TC_MMA_WARP) {
         // ------------------------------------------------------------ MMA issuer
         const uint32_t fmt = BF ? 1u : 0u;
@@ -493,7 +596,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
         __syncwarp();
         if (__shfl_sync(0xffffffffu, issued ? 1 : 0, 0)) mbar_wait_quiet(drain, 0);
         tc_fence_before();
-    } else {
+    } else if (warp < TC_COPY_WARP) {
         // ------------------------------------------------------------ epilogue
         const int q = warp & 3;                       // TMEM lane quadrant of this warp
         const int r = q * 32 + lane;
@@ -601,6 +704,42 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
             if (!ok) break;
             nitem++;
         }
+    } else {
+        // ------------------------------------------------------------ V copies
+        // Lane 0 streams the V operand images of every stage into the ring, up
+        // to TC_VSLOTS stages ahead of the MMAs: a slot is refilled once the
+        // MMAs that read it have completed.  Off the producers' path, so that
+        // their stage barrier never waits for a slot.
+        if (L.vring && lane == 0) {
+            uint32_t x = 0, landed = 0;       // copies issued / first copy not known to have landed
+            bool ok = true;
+            for (int64_t item = blockIdx.x; item < L.nitems && ok; item += gridDim.x) {
+                const TcProblem &g = L.probs[L.item_prob[item]];
+                int t, ks, nt, mt;
+                decode_item(g, item - g.item0, t, ks, nt, mt);
+                const int64_t a0 = g.ts[t] + (int64_t)ks * g.slice_len;
+                const int64_t a1 = min(g.ts[t + 1], a0 + g.slice_len);
+                const int nst = a1 > a0 ? (int)((a1 - a0) / TC_KA) : 0;
+                const int64_t g0 = a0 / TC_KA;
+                for (int y = 0; y < nst; y++, x++) {
+                    const int v = (int)(x % TC_VSLOTS);
+                    if (x >= TC_VSLOTS) {
+                        if (!mbar_wait(&vempty[v], ((x / TC_VSLOTS) - 1) & 1, err, 9)) {
+                            ok = false;
+                            break;
+                        }
+                        landed = x - TC_VSLOTS + 1;       // the MMAs consumed that copy: it landed
+                    }
+                    mbar_arrive_tx(&vfull[v], vbytes);
+                    bulk_g2s(vring + (size_t)v * vbytes, g.vimg + ((g0 + y) * g.n_tiles + nt) * (int64_t)vbytes,
+                             vbytes, &vfull[v]);
+                }
+            }
+            // copies still in flight land before the CTA can exit (after an
+            // error the MMA side may not have waited for them)
+            for (uint32_t y = landed; y < x; y++) mbar_wait_quiet(&vfull[y % TC_VSLOTS], (y / TC_VSLOTS) & 1);
+        }
+        __syncwarp();
     }
     __syncthreads();
     if (warp == TC_MMA_WARP) {

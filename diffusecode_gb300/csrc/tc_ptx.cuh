@@ -116,6 +116,16 @@ __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::
 // K-major operand with the 64-byte swizzle: row r of an 8-row group at
 // (r&7)*64 B, its 16-byte chunk c stored at chunk c ^ ((r&7)>>1); 8-row groups
 // SBO = 512 B apart (each group 512-byte aligned).
+// four 8x8 b16 matrices from registers to shared memory: lane l gives the
+// address of row (l & 7) of matrix (l >> 3); register i of lane l holds
+// row l >> 2, columns 2 (l & 3) and 2 (l & 3) + 1 of matrix i (low half first)
+__device__ __forceinline__ void stmatrix_x4(uint32_t addr, uint32_t r0, uint32_t r1, uint32_t r2, uint32_t r3)
+{
+    asm volatile("stmatrix.sync.aligned.m8n8.x4.shared.b16 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(r0), "r"(r1),
+                 "r"(r2), "r"(r3)
+                 : "memory");
+}
+
 __device__ __forceinline__ uint32_t sw_off(int r, int chunk)
 {
     return (uint32_t)((r >> 3) * TC_SBO + (r & 7) * 64 + ((chunk ^ ((r & 7) >> 1)) << 4));
