@@ -266,30 +266,37 @@ __device__ __forceinline__ void split_c2(const float2 (&x)[2], uint32_t &rh, uin
 // row groups of one operand array.  Values step from group to group by
 // exp(2 pi i 8 d_ra) on two chains (even and odd groups, by its square) and
 // restart from the exact phase at every group that begins a new nb.
-template <bool BF>
-__device__ __forceinline__ void gen_rows_stm(int mt, int gpn, const uint8_t *as, uint8_t *A, int lane, int warp)
+// Phase data of the thread's two atoms for one stage, loaded from global
+// memory one stage ahead (16-byte loads: the atoms are consecutive and even).
+struct AtomPair {
+    ulonglong2 ph0, dra, drb;
+    float2 w;
+    float4 m;               // step factors exp(2 pi i 8 d_ra) of the two atoms
+};
+
+__device__ __forceinline__ void load_pair(AtomPair &r, const TcSrc &P, int64_t k)
 {
-    const uint64_t *s_ph0 = reinterpret_cast<const uint64_t *>(as);
-    const uint64_t *s_dra = s_ph0 + TC_KA, *s_drb = s_dra + TC_KA;
-    const float *s_w = reinterpret_cast<const float *>(as + TC_SLOT_W);
-    const float2 *s_ma = reinterpret_cast<const float2 *>(as + TC_SLOT_MA);
+    r.ph0 = __ldg(reinterpret_cast<const ulonglong2 *>(P.ph0 + k));
+    r.dra = __ldg(reinterpret_cast<const ulonglong2 *>(P.dra + k));
+    r.drb = __ldg(reinterpret_cast<const ulonglong2 *>(P.drb + k));
+    r.w = __ldg(reinterpret_cast<const float2 *>(P.w + k));
+    r.m = __ldg(reinterpret_cast<const float4 *>(P.ma + k));
+}
+
+template <bool BF>
+__device__ __forceinline__ void gen_rows_stm(int mt, int gpn, const AtomPair &ap, uint8_t *A, int lane, int warp)
+{
     const int c = warp & 3;
     const int q0 = (warp >> 2) * 8;
     const int s = lane >> 2;
-    const int k0 = 8 * c + 2 * (lane & 3);
     const uint32_t adr = smem_u32(A) + (uint32_t)(q0 + (lane >> 3)) * TC_SBO + sw_off(lane & 7, c);
-    uint64_t ph0[2], dra[2], drb[2];
-    float w[2];
+    const uint64_t ph0[2] = {ap.ph0.x, ap.ph0.y}, dra[2] = {ap.dra.x, ap.dra.y}, drb[2] = {ap.drb.x, ap.drb.y};
+    const float w[2] = {ap.w.x, ap.w.y};
     float2 m[2], m2[2];
+    m[0] = make_float2(ap.m.x, ap.m.y);
+    m[1] = make_float2(ap.m.z, ap.m.w);
 #pragma unroll
-    for (int a = 0; a < 2; a++) {
-        ph0[a] = s_ph0[k0 + a];
-        dra[a] = s_dra[k0 + a];
-        drb[a] = s_drb[k0 + a];
-        w[a] = s_w[k0 + a];
-        m[a] = s_ma[k0 + a];
-        m2[a] = cmulf(m[a], m[a]);
-    }
+    for (int a = 0; a < 2; a++) m2[a] = cmulf(m[a], m[a]);
     // segments of constant nb: bit o of bmask marks group G0 + o as the first
     // of a segment (one division per stage, no other)
     const int G0 = mt * (TC_M / 8) + q0;
@@ -442,7 +449,44 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
     tc_fence_after();
     const uint32_t tmem = *tbase;
 
-    if (warp < TC_PROD_WARPS) {
+    if (warp < TC_PROD_WARPS && L.vring) {
+        // ------------------------------------------------ producers (V images)
+        // Every producer warp runs on its own: its lane 0 waits for the stage
+        // buffer, the warp writes its quarter-chunk of U rows (gen_rows_stm) and
+        // arrives on the stage's full barrier; the phase data of its atoms is
+        // loaded one stage ahead into registers.  No barrier among producers.
+        uint32_t it = 0;
+        bool ok = true;
+        const int kq = 8 * (warp & 3) + 2 * (lane & 3);     // the thread's first atom in a stage
+        for (int64_t item = blockIdx.x; item < L.nitems && ok; item += gridDim.x) {
+            const TcProblem &g = L.probs[L.item_prob[item]];
+            int t, ks, nt, mt;
+            decode_item(g, item - g.item0, t, ks, nt, mt);
+            const int64_t a0 = g.ts[t] + (int64_t)ks * g.slice_len;
+            const int64_t a1 = min(g.ts[t + 1], a0 + g.slice_len);
+            const int nst = a1 > a0 ? (int)((a1 - a0) / TC_KA) : 0;
+            if (nst == 0) continue;
+            const TcSrc src = {g.ph0, g.dra, g.drb, g.dac, g.w, g.ma, g.mc};
+            const int gpn = g.fra_p >> 3;
+            AtomPair cur, nxt;
+            load_pair(cur, src, a0 + kq);
+            for (int st = 0; st < nst; st++, it++) {
+                if (st + 1 < nst) load_pair(nxt, src, a0 + (int64_t)(st + 1) * TC_KA + kq);
+                const int sb = it % S;
+                bool got = true;
+                if (lane == 0 && it >= (uint32_t)S) got = mbar_wait(&empty[sb], ((it / S) - 1) & 1, err, 1);
+                if (!__shfl_sync(0xffffffffu, got, 0)) {
+                    ok = false;
+                    break;
+                }
+                gen_rows_stm<BF>(mt, gpn, cur, smem + (size_t)sb * stage_bytes, lane, warp);
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&full[sb]);   // one arrival per producer warp
+                cur = nxt;
+            }
+        }
+    } else if (warp < TC_PROD_WARPS) {
         // ------------------------------------------------------------ producers
         // Atom groups are complete (type ranges padded to 32 atoms with zero
         // weight).  Their phase data is staged in shared memory with cp.async
@@ -492,12 +536,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
                     cp_async_commit();
                 const uint8_t *as = aslot + (st % TC_NSLOT) * TC_ATOM_SLOT;
                 uint8_t *A = smem + (size_t)sb * stage_bytes;
-                if (vimg) {
-                    gen_rows_stm<BF>(mt, gpn, as, A, lane, warp);     // rows only, by stmatrix
-                } else {
-                    if (ok && ra0 < ra1) gen_rows<BF>(ra0, ra1, mt, gpn, as, A, s, j);
-                    if (ok && rc0 < rc1) gen_cols<BF>(rc0, rc1, nt, N, as, A + 4 * TC_A_BYTES, b_bytes, s, j);
-                }
+                if (ok && ra0 < ra1) gen_rows<BF>(ra0, ra1, mt, gpn, as, A, s, j);
+                if (ok && rc0 < rc1) gen_cols<BF>(rc0, rc1, nt, N, as, A + 4 * TC_A_BYTES, b_bytes, s, j);
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&full[sb]);   // one arrival per producer warp
