@@ -71,6 +71,7 @@
 #define TC_VSLOTS 4                            // V ring: images prefetched two stages ahead
 #define TC_BAR_BYTES 256
 #define TC_SMEM_BUDGET (220 * 1024)
+#define TC_SMEM_MAX (227 * 1024)                // the opt-in maximum of one CTA
 #ifndef TC_FLUSH_STAGES
 #define TC_FLUSH_STAGES 4                      // 128 atoms per drain of the main accumulator
 #endif
@@ -1006,16 +1007,18 @@ int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *o
     L.flush = op->tc_flush > 0 ? (int32_t)dgpu_cdiv(op->tc_flush, TC_KA) : TC_FLUSH_STAGES;
     L.bf16 = op->split == DGPU_SPLIT_BF16;
     const uint32_t vbytes = 2u * 3u * N * TC_KA * 2;
-    const uint32_t bar_bytes = TC_BAR_BYTES + TC_NSLOT * TC_ATOM_SLOT;
-    // V images stream through a ring when it leaves room for two U stages
-    const int64_t room = (int64_t)TC_SMEM_BUDGET - bar_bytes - (int64_t)TC_VSLOTS * vbytes;
+    // V images stream through a ring when it leaves room for two U stages; the
+    // producers of that path hold their atoms' phase data in registers, so it
+    // needs no atom slots and may use the whole shared memory of the SM
+    const int64_t room = (int64_t)TC_SMEM_MAX - TC_BAR_BYTES - (int64_t)TC_VSLOTS * vbytes;
     if (plan.vimg && room < 2 * 4 * TC_A_BYTES) plan.vimg = false;
     if (!plan.vimg)
         for (TcProblem &g : plan.probs) g.vimg = nullptr;
     L.vring = plan.vimg ? 1 : 0;
+    const uint32_t bar_bytes = TC_BAR_BYTES + (L.vring ? 0u : (uint32_t)(TC_NSLOT * TC_ATOM_SLOT));
+    const int64_t budget = L.vring ? TC_SMEM_MAX : TC_SMEM_BUDGET;
     const uint32_t stage_bytes = 4 * TC_A_BYTES + (L.vring ? 0u : vbytes);
-    const int stages = (int)(((int64_t)TC_SMEM_BUDGET - bar_bytes - (L.vring ? (int64_t)TC_VSLOTS * vbytes : 0)) /
-                             stage_bytes);
+    const int stages = (int)((budget - bar_bytes - (L.vring ? (int64_t)TC_VSLOTS * vbytes : 0)) / stage_bytes);
     L.stages = stages > 4 ? 4 : stages;
     L.tmem_cols = pow2_cols(2 * N * (1 + L.nbuf + L.tsum));
     if (L.stages < 2 || L.tmem_cols > 512) return dgpu_set_error(ctx, DGPU_ERR_ARG, "tile does not fit");
