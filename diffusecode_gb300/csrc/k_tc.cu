@@ -814,15 +814,18 @@ __global__ void k_tc_mult(const uint64_t *__restrict__ du, const uint64_t *__res
 // V images of one problem: for every 32-atom group gi and column tile nt the
 // B rows [Vr; Vi; -Vr] of a stage, hi then lo, exactly as the producers lay
 // them out in shared memory (384 N bytes).  Each value is evaluated from its
-// exact 64-bit phase; grid: one block per (gi, nt).
+// exact 64-bit phase; grid: one block per (gi, nt).  The image is built in
+// shared memory (N * 384 bytes, at most 48 KB) and written out in 16-byte
+// coalesced stores.
 template <bool BF>
 __global__ void __launch_bounds__(256) k_tc_vgen(const uint64_t *__restrict__ dac, int N, int n_tiles,
                                                   uint8_t *__restrict__ vimg)
 {
+    extern __shared__ __align__(16) uint8_t vs[];
     const int64_t gi = blockIdx.x / n_tiles;
     const int nt = (int)(blockIdx.x % n_tiles);
     const uint32_t vbytes = (uint32_t)N * 384u;
-    uint8_t *img = vimg + (int64_t)blockIdx.x * vbytes;
+    uint8_t *img = vs;                 // built in shared memory, then written out coalesced
     const uint32_t half = vbytes / 2, blk = (uint32_t)(N >> 3) * TC_SBO;
     for (int u = threadIdx.x; u < N * 8; u += blockDim.x) {
         const int c = u % N, jq = u / N;                       // column, atom quad
@@ -844,6 +847,10 @@ __global__ void __launch_bounds__(256) k_tc_vgen(const uint64_t *__restrict__ da
         *reinterpret_cast<uint2 *>(d + 2 * blk) = make_uint2(rh.x ^ 0x80008000u, rh.y ^ 0x80008000u);
         *reinterpret_cast<uint2 *>(d + 2 * blk + half) = make_uint2(rl.x ^ 0x80008000u, rl.y ^ 0x80008000u);
     }
+    __syncthreads();
+    uint4 *out = reinterpret_cast<uint4 *>(vimg + (int64_t)blockIdx.x * vbytes);
+    const uint4 *src = reinterpret_cast<const uint4 *>(vs);
+    for (uint32_t i = threadIdx.x; i < vbytes / 16u; i += blockDim.x) out[i] = src[i];
 }
 
 // ---------------------------------------------------------------------------
@@ -944,7 +951,7 @@ void dgpu_tc_partref(const TcProblem &g, const float2 *p, PartRef &ref)
     ref.slab = g.slab;
 }
 
-#define TC_VIMG_BUDGET ((int64_t)1 << 30)     // bytes of V images per launch
+#define TC_VIMG_BUDGET ((int64_t)16 << 30)    // bytes of V images per launch
 
 int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *op, int N, int slice_mult,
                  TcPlan &plan, DevBuf &part, DevBuf &desc, DevBuf *vimg)
@@ -1043,9 +1050,11 @@ int dgpu_tc_launch(dgpu_ctx *ctx, const TcPlan &plan, bool timed)
             const int64_t nimg = (g.ts[g.ntype] / TC_KA) * g.n_tiles;
             if (nimg < 1) continue;
             if (plan.L.bf16)
-                k_tc_vgen<true><<<(unsigned)nimg, 256, 0, ctx->stream>>>(g.dac, g.N, g.n_tiles, g.vimg);
+                k_tc_vgen<true><<<(unsigned)nimg, 256, (size_t)g.N * 384, ctx->stream>>>(g.dac, g.N, g.n_tiles,
+                                                                                          g.vimg);
             else
-                k_tc_vgen<false><<<(unsigned)nimg, 256, 0, ctx->stream>>>(g.dac, g.N, g.n_tiles, g.vimg);
+                k_tc_vgen<false><<<(unsigned)nimg, 256, (size_t)g.N * 384, ctx->stream>>>(g.dac, g.N, g.n_tiles,
+                                                                                           g.vimg);
         }
     const int grid = (int)(plan.L.nitems < ctx->nsm ? plan.L.nitems : ctx->nsm);
     if (timed) DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[6], ctx->stream));

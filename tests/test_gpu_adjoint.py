@@ -73,7 +73,10 @@ def test_gradient_with_friedel_reduction(oracle, ctx):
 
 @pytest.mark.parametrize("engine", [_abi.ENGINE_DIRECT, _abi.ENGINE_TC])
 def test_central_finite_differences(ctx, engine):
-    """d chi2 / d x by central differences with a 1e-4 A step on seeded atoms."""
+    """d chi2 / d x by central differences on seeded atoms: a 1e-4 A step for
+    the CUDA-core engine; 1e-3 A for the tensor-core engine, whose ~1e-6
+    relative noise in chi2 would otherwise dominate the difference (the
+    truncation error of the central difference stays ~1e-6 relative)."""
     from diffusecode_gb300.autograd import chi2_grad
     a = 5.64
     cr, g = S.rocksalt_volume(cells=(3, 3, 3), inc=17, step=0.2)
@@ -81,7 +84,7 @@ def test_central_finite_differences(ctx, engine):
     op = K.opts(phase=_abi.PHASE_EXACT64, engine=engine)
     c2, gp, go, _ = chi2_grad(cr, g, op, it, wt, ctx=ctx)
     rng = np.random.Generator(np.random.PCG64(12))
-    h = 1e-4 / a
+    h = (1e-4 if engine == _abi.ENGINE_DIRECT else 1e-3) / a
     scale = np.abs(gp).max()
     for atom in rng.choice(cr.natoms, 6, replace=False):
         for k in range(3):
