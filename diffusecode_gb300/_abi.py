@@ -105,6 +105,7 @@ class Opts(C.Structure):
         ("lot_all", C.c_int32),
         ("lperiod", C.c_int32),
         ("lot_origins", _ip),
+        ("tc_vimg", C.c_int32),
     ]
 
 
@@ -174,6 +175,7 @@ def default_opts(**kw):
     o.lot_all = 0
     o.lperiod = 1
     o.lot_origins = C.cast(None, _ip)
+    o.tc_vimg = 0
     for k, v in kw.items():
         if k in ("aver_cells", "lot_origins"):
             continue

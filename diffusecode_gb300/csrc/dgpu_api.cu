@@ -52,6 +52,7 @@ extern "C" void dgpu_default_opts(dgpu_opts *o)
     o->lot_all = 0;
     o->lperiod = 1;
     o->lot_origins = nullptr;
+    o->tc_vimg = 0;
 }
 
 extern "C" int dgpu_ctx_create(int device, dgpu_ctx **out)

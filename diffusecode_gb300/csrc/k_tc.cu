@@ -990,7 +990,16 @@ int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *o
         voff[p] = vtot;
         vtot += in[p].ts[in[p].ntype] / TC_KA * plan.probs[p].n_tiles * (int64_t)N * 384;
     }
-    plan.vimg = vimg && vtot > 0 && vtot <= TC_VIMG_BUDGET;
+    // images pay when every one is re-read by several row tiles (a 3D grid);
+    // thin planes with one or two row tiles generate V in the kernel
+    double reads = 0.0, imgs = 0.0;
+    for (int p = 0; p < nprob; p++) {
+        const double ni = (double)(in[p].ts[in[p].ntype] / TC_KA) * plan.probs[p].n_tiles;
+        imgs += ni;
+        reads += ni * plan.probs[p].m_tiles;
+    }
+    const bool reuse = imgs > 0 && reads >= 4.0 * imgs;
+    plan.vimg = vimg && vtot > 0 && vtot <= TC_VIMG_BUDGET && op->tc_vimg >= 0 && (reuse || op->tc_vimg > 0);
     if (plan.vimg) {
         DGPU_CUDA(ctx, vimg->ensure((size_t)vtot));
         for (int p = 0; p < nprob; p++) plan.probs[p].vimg = vimg->as<uint8_t>() + voff[p];

@@ -144,6 +144,8 @@ typedef struct dgpu_opts {
     const int32_t *lot_origins; /* lbeg(3,nlots), 1-based origin cells 1..csize, drawn
                                   by the caller's ran1 stream as four_ranloc does
                                   (fourier_sup.f90:2513-2530); unused with lot_all  */
+    int32_t tc_vimg;        /* tensor-core V operand: 0 auto (images when each is
+                               re-read by 4+ row tiles), 1 images, -1 in-kernel  */
 } dgpu_opts;
 
 /* What four_run reports besides the arrays. */

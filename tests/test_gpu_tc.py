@@ -20,22 +20,26 @@ def tc_opts(**kw):
     return K.opts(**base)
 
 
+@pytest.mark.parametrize("vimg", [1, -1], ids=["v-images", "v-in-kernel"])
 @pytest.mark.parametrize("inc,natoms", [((13, 11, 7), 300), ((37, 5, 3), 1000), ((3, 129, 2), 77),
                                         ((201, 1, 1), 40)])
-def test_tc_random_vs_oracle(oracle, ctx, inc, natoms):
+def test_tc_random_vs_oracle(oracle, ctx, inc, natoms, vimg):
+    """Both V operand paths: images streamed by the copy warp (independent
+    stmatrix producers) and V generated in the kernel (producer barrier)."""
     cr, g = S.small_random(seed=31, natoms=natoms, nscat=3, inc=inc)
     for form in (_abi.FORM_TABLE, _abi.FORM_ANALYTIC):
-        op = tc_opts(form=form)
+        op = tc_opts(form=form, tc_vimg=vimg)
         rc, csf, acsf, dsi, info = oracle.four_run(cr, g, op)
         r = FR.four_run(cr, g, op, ctx=ctx)
         assert r.info.engine_used == _abi.ENGINE_TC
         assert K.rel_err(r.dsi, dsi, K.incoherent_floor(cr, g, op)) <= TOL
 
 
+@pytest.mark.parametrize("vimg", [1, -1], ids=["v-images", "v-in-kernel"])
 @pytest.mark.parametrize("tile_n,kslice", [(16, 1024), (64, 2048), (112, 0), (128, 96), (80, 4096)])
-def test_tc_tiles_and_slices(oracle, ctx, tile_n, kslice):
+def test_tc_tiles_and_slices(oracle, ctx, tile_n, kslice, vimg):
     cr, g = S.perovskite_plane(cells=6)
-    op = tc_opts(tc_tile_n=tile_n, tc_kslice=kslice)
+    op = tc_opts(tc_tile_n=tile_n, tc_kslice=kslice, tc_vimg=vimg)
     rc, csf, acsf, dsi, info = oracle.four_run(cr, g, op)
     r = FR.four_run(cr, g, op, ctx=ctx)
     assert K.rel_err(r.dsi, dsi, K.incoherent_floor(cr, g, op)) <= TOL
