@@ -35,6 +35,20 @@ ENGINE_DIRECT = 1
 ENGINE_TC = 2
 SPLIT_F16 = 0
 SPLIT_BF16 = 1
+VAL_INTEN = 1
+VAL_AMPLI = 2
+VAL_PHASE = 3
+VAL_REAL = 4
+VAL_IMAG = 5
+VAL_RANPH = 6
+VAL_SQ = 7
+VAL_F2AVER = 9
+VAL_FAVER2 = 10
+VAL_FAVER = 11
+VAL_IQ = 13
+VAL_F2AVERB = 17
+VAL_FAVER2B = 18
+VAL_FAVERB = 19
 ACCUM_INIT = -1
 ACCUM_SINGLE = 0
 ACCUM_ACCUM = 1

@@ -108,6 +108,30 @@ def four_accumulate(mode, grid: GridData, csf=None, dsi=None, fave=0.0, symm=0, 
     return _cplx(cbuf, grid.inc), dbuf.reshape(grid.inc, order="F")
 
 
+def _interleave(z):
+    z = np.asfortranarray(z).reshape(-1, order="F")
+    b = np.empty(2 * z.size)
+    b[0::2], b[1::2] = z.real, z.imag
+    return b
+
+
+def qval(cr: CrystalData, grid: GridData, opts: _abi.Opts, value, result: FourierResult, laver=False,
+         rand=None, ctx=None):
+    """qval (discus/prog/qval.f90:65-290) on the device: the output value of
+    every grid point from a FourierResult (csf, acsf, dsi)."""
+    ctx = ctx or default_context()
+    c = cr.to_c()
+    g = grid.to_c()
+    csf = _interleave(result.csf)
+    acsf = _interleave(result.acsf)
+    dsi = np.asfortranarray(result.dsi, dtype=np.float64).reshape(-1, order="F").copy()
+    rnd = None if rand is None else np.asfortranarray(rand, dtype=np.float64).reshape(-1, order="F").copy()
+    out = np.zeros(grid.npoints)
+    ctx.check(ctx.lib.dgpu_qval(ctx.h, C.byref(c), C.byref(g), C.byref(opts), int(value), int(bool(laver)),
+                                _abi.dptr(csf), _abi.dptr(acsf), _abi.dptr(dsi), _abi.dptr(rnd), _abi.dptr(out)))
+    return out.reshape(grid.inc, order="F")
+
+
 def fourier_lmn(eck, vi, inc, ctx=None):
     """fourier_lmn (discus/prog/fourier_lmn_mod.f90:4-280): (rc, lmn[6], off_shift(3,3))."""
     ctx = ctx or default_context()

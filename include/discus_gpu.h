@@ -268,6 +268,33 @@ int dgpu_four_weight_device(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_gr
 int dgpu_four_accumulate(dgpu_ctx *ctx, int32_t mode, int32_t symm, const dgpu_grid *grid, double fave,
                          double *csf, double *dsi);
 
+/* ---- output values ------------------------------------------------------- */
+/* qval (discus/prog/qval.f90:65-290): the value the output menu writes at a
+ * grid point, from the arrays of the last four_run.  value (qval.f90:3-21):  */
+#define DGPU_VAL_INTEN     1   /* dsi, or |acsf|^2 with laver                    */
+#define DGPU_VAL_AMPLI     2   /* |F|                                            */
+#define DGPU_VAL_PHASE     3   /* atan2(Im F, Re F) in degrees, 0 for F = 0      */
+#define DGPU_VAL_REAL      4
+#define DGPU_VAL_IMAG      5
+#define DGPU_VAL_RANPH     6   /* phase at integer hkl, else (r - 0.5)*360       */
+#define DGPU_VAL_SQ        7   /* S(Q) = I/<f>^2/N + 1 - exp(-Q^2 <u^2>)         */
+#define DGPU_VAL_F2AVER    9   /* <f^2>, from cfact without Debye-Waller/occ     */
+#define DGPU_VAL_FAVER2   10   /* <f>^2                                          */
+#define DGPU_VAL_FAVER    11   /* <f>                                            */
+#define DGPU_VAL_IQ       13   /* I/N                                            */
+#define DGPU_VAL_F2AVERB  17   /* the same three from cfact (Debye-Waller, occ)  */
+#define DGPU_VAL_FAVER2B  18
+#define DGPU_VAL_FAVERB   19
+/* out receives num(1)*num(2)*num(3) values; F = csf, or acsf with laver != 0.
+ * csf/acsf/dsi are host arrays as dgpu_four_run returns them (acsf may be NULL
+ * without laver); rand (RANPH only) holds one value in [0,1) per point, drawn
+ * by the caller's ran1 stream.  The per-type sums use cr (types, scattering
+ * tables, dw), opts (lxray, power, ano, ldbw) and istl(i, j, 1) / istl(i, 1, 1)
+ * exactly as qval indexes them.  PDF values (14-16) are DGPU_ERR_UNSUPPORTED. */
+int dgpu_qval(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid, const dgpu_opts *opts,
+              int32_t value, int32_t laver, const double *csf, const double *acsf, const double *dsi,
+              const double *rand, double *out);
+
 /* ---- adjoint: chi^2 and its gradient ------------------------------------- */
 /* chi2 = sum_h w(h) (I(h) - I_target(h))^2 over the full grid, I = diff_scale*|csf|^2
  * as dgpu_four_run computes it (EXACT64 phase, ANALYTIC or TABLE form).

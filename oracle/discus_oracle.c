@@ -1186,3 +1186,92 @@ void oc_fill_bragg(const dgpu_grid *g, double *a, int comp)
             }
 #undef AT
 }
+
+/* ---------------------------------------------------------------------- */
+/* qval, discus/prog/qval.f90:65-290, with cr_amount / cr_n_real_atoms /
+ * cr_u2aver of chem_aver (chem_aver_mod.f90:495-537).  Indexing as in the
+ * reference: istl(i,j,1) for the form-factor sums, istl(i,1,1) for S(Q)'s
+ * Q^2; the sign of <f> from cfact_pure(1,l); the <f> values keep sign 1. */
+int oc_qval(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op, int value, int laver,
+            const double *csf, const double *acsf, const double *dsi, const double *rnd, double *out)
+{
+    const double pi = 3.1415926535897932384626433832795028841971693993751, rad = pi / 180.0;
+    const int32_t *num = g->inc;
+    int64_t np = (int64_t)num[0] * num[1] * num[2];
+    int ns = cr->nscat;
+    int tables = value == 7 || value >= 9;
+    int32_t *istl = NULL;
+    double *cf = NULL, *cfp = NULL, amount[64], signum[64], nreal = 0, u2 = 0;
+    if (tables) {
+        istl = (int32_t *)malloc(sizeof(int32_t) * np);
+        if (oc_stltab(g->eck, g->vi, num, cr->rten, istl)) { free(istl); return DGPU_ERR_STL_RANGE; }
+        cf = (double *)malloc(sizeof(double) * 2 * NTAB * ns);
+        cfp = (double *)malloc(sizeof(double) * 2 * NTAB * ns);
+        oc_formtab(cr, op, cf);
+        double *ones = (double *)malloc(sizeof(double) * (ns + 1));
+        for (int l = 0; l <= ns; l++) ones[l] = 1.0;
+        dgpu_crystal pc = *cr;
+        pc.occ = ones;
+        dgpu_opts po = *op;
+        po.ldbw = 0;
+        oc_formtab(&pc, &po, cfp);
+        free(ones);
+        for (int l = 0; l <= ns; l++) amount[l] = 0;
+        for (int64_t a = 0; a < cr->natoms; a++)
+            if (cr->iscat[a] >= 0 && cr->iscat[a] <= ns) amount[cr->iscat[a]] += 1;
+        for (int l = 0; l <= ns; l++) {
+            u2 = u2 + cr->dw[l] * amount[l];
+            if (l > 0) nreal += amount[l];
+        }
+        u2 = u2 / nreal / 8.0 / (double)(float)(pi * pi);
+        for (int l = 1; l <= ns; l++) signum[l] = cfp[2 * ((int64_t)(l - 1) * NTAB + 1)] < 0.0 ? -1.0 : 1.0;
+    } else if (value == 13) {
+        for (int64_t a = 0; a < cr->natoms; a++)
+            if (cr->iscat[a] >= 1 && cr->iscat[a] <= ns) nreal += 1;
+    }
+    for (int32_t k = 0; k < num[2]; k++)
+        for (int32_t j = 0; j < num[1]; j++)
+            for (int32_t i = 0; i < num[0]; i++) {
+                int64_t p = i + (int64_t)num[0] * (j + (int64_t)num[1] * k);
+                const double *fz = laver ? acsf + 2 * p : csf + 2 * p;
+                double fr = fz[0], fi = fz[1], f2 = fr * fr + fi * fi, r = 0;
+                double I = laver ? f2 : (dsi ? dsi[p] : 0.0);
+                if (value == 1) r = I;
+                else if (value == 2) r = sqrt(f2);
+                else if (value == 3) r = (fr == 0 && fi == 0) ? 0.0 : atan2(fi, fr) / rad;
+                else if (value == 4) r = fr;
+                else if (value == 5) r = fi;
+                else if (value == 6) {
+                    int bragg = 1;
+                    for (int l = 0; l < 3; l++) {
+                        double h = g->eck[l] + g->vi[l] * (double)(float)i + g->vi[3 + l] * (double)(float)j;
+                        bragg = bragg && fabs(h - (double)llround(h)) < 0.000001;
+                    }
+                    r = bragg ? ((fr == 0 && fi == 0) ? 0.0 : atan2(fi, fr) / rad) : (rnd[p] - 0.5) * 360.0;
+                } else if (value == 13) r = I / nreal;
+                else {
+                    int32_t s = istl[i + (int64_t)num[0] * j];
+                    int pure = value == 7 || value == 9 || value == 10 || value == 11;
+                    const double *tab = pure ? cfp : cf;
+                    double sum = 0;
+                    for (int l = 1; l <= ns; l++) {
+                        const double *c = tab + 2 * ((int64_t)(l - 1) * NTAB + s);
+                        double a2 = c[0] * c[0] + c[1] * c[1];
+                        if (value == 9 || value == 17) sum += a2 * amount[l];
+                        else if (value == 11 || value == 19) sum += sqrt(a2) * amount[l];
+                        else sum += sqrt(a2) * amount[l] * signum[l];
+                    }
+                    if (value == 7) {
+                        double st = 2.0 * (double)istl[i] * DGPU_CFINC;
+                        double q2 = (double)(float)((2 * pi) * (2 * pi) * (st * st));
+                        r = I / (sum * sum) / nreal + 1.0 - exp(-q2 * u2);
+                    } else if (value == 10 || value == 18) {
+                        double t = sum / nreal;
+                        r = t * t;
+                    } else r = sum / nreal;
+                }
+                out[p] = r;
+            }
+    free(istl); free(cf); free(cfp);
+    return 0;
+}

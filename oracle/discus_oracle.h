@@ -55,6 +55,8 @@ int  oc_chi2_grad(const dgpu_crystal *cr, const dgpu_grid *grid, const dgpu_opts
 int  oc_four_weight(const dgpu_crystal *cr, const dgpu_grid *grid, const dgpu_opts *op,
                     const double *dsi, double *dsi3d, double *scalef);
 void oc_fill_bragg(const dgpu_grid *grid, double *a, int comp);
+int  oc_qval(const dgpu_crystal *cr, const dgpu_grid *grid, const dgpu_opts *op, int value, int laver,
+             const double *csf, const double *acsf, const double *dsi, const double *rnd, double *out);
 double oc_time_ref_rows(const dgpu_crystal *cr, const dgpu_grid *grid, int32_t row_lo,
                         int32_t row_hi, int nthreads, int64_t *pairs_out);
 

@@ -45,6 +45,8 @@ def lib():
                                      dp, dp, dp]
         L.oc_fill_bragg.argtypes = [C.POINTER(_abi.Grid), dp, C.c_int]
         L.oc_fill_bragg.restype = None
+        L.oc_qval.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Grid), C.POINTER(_abi.Opts), C.c_int,
+                              C.c_int, dp, dp, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -201,3 +203,21 @@ def fill_bragg(grid, arr):
     buf = np.asfortranarray(arr, dtype=np.float64).reshape(-1, order="F").copy()
     lib().oc_fill_bragg(C.byref(g), _d(buf), 1)
     return buf.reshape(grid.inc, order="F")
+
+
+def qval(cr, grid, opts, value, csf, acsf, dsi, laver=False, rand=None):
+    """qval of every grid point (arrays shaped grid.inc, Fortran order)."""
+    c = cr.to_c()
+    g = grid.to_c()
+    def il(z):
+        z = np.asfortranarray(z).reshape(-1, order="F")
+        b = np.empty(2 * z.size)
+        b[0::2], b[1::2] = z.real, z.imag
+        return b
+    cs, ac = il(csf), il(acsf)
+    d = np.asfortranarray(dsi, dtype=np.float64).reshape(-1, order="F").copy()
+    rn = None if rand is None else np.asfortranarray(rand, dtype=np.float64).reshape(-1, order="F").copy()
+    out = np.zeros(grid.npoints)
+    rc = lib().oc_qval(C.byref(c), C.byref(g), C.byref(opts), int(value), int(bool(laver)), _d(cs), _d(ac),
+                       _d(d), _d(rn) if rn is not None else None, _d(out))
+    return rc, out.reshape(grid.inc, order="F")
