@@ -186,3 +186,122 @@ extern "C" int dgpu_qval(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid 
     DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));      // q and the host arrays are read by now
     return DGPU_OK;
 }
+
+// ---------------------------------------------------------------------------
+// calc_hkl (discus/prog/fourier_sup.f90:3230-3549): F at listed reflections
+
+struct HklSpec {
+    int32_t lo[3], n[3];
+    double ncells, scale, exti, rlambda;
+    double rten[9];
+};
+
+__global__ void k_calc_hkl(HklSpec s, const int32_t *__restrict__ hkl, int64_t nrefl, const double2 *__restrict__ csf,
+                           double *__restrict__ out)
+{
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrefl) return;
+    const int32_t h = hkl[3 * r], k = hkl[3 * r + 1], l = hkl[3 * r + 2];
+    double ic = 0.0, sg = 0.0, ph = 0.0;
+    if (h != 0 || k != 0 || l != 0) {
+        const int64_t idx = (h - s.lo[0]) + (int64_t)s.n[0] * ((k - s.lo[1]) + (int64_t)s.n[1] * (l - s.lo[2]));
+        const double2 f = csf[idx];
+        const double qq = sqrt(f.x * f.x + f.y * f.y) / s.ncells;
+        // d* = do_blen(.false., hkl, 0): sqrt(h^T G* h)
+        const double hv[3] = {(double)h, (double)k, (double)l};
+        double d2 = 0.0;
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) d2 += hv[a] * s.rten[3 * b + a] * hv[b];
+        const double rad = 3.1415926535897932384626433832795028841971693993751 / 180.0;
+        const double tth = 2.0 * (asin(0.5 * s.rlambda * sqrt(d2)) / rad);       // 2 asind(...) in degrees
+        const double ext = pow(1.0 / (1.0 + 0.001 * s.exti * qq * qq * s.rlambda * s.rlambda * s.rlambda /
+                                                sin(tth * rad)),
+                               0.25);
+        ph = atan2(f.y, f.x) / rad;
+        const double e = qq * ext;
+        ic = e * e * s.scale;
+        sg = sqrt(fabs(ic));
+    }
+    out[r] = ic;
+    out[nrefl + r] = sg;
+    out[2 * nrefl + r] = ph;
+}
+
+extern "C" int dgpu_calc_hkl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *opts, const int32_t *hkl,
+                             int64_t nrefl, double scale, double exti, double rlambda, double *icalc, double *sigi,
+                             double *phase)
+{
+    if (!ctx || !cr || !opts || !hkl || nrefl < 0 || !icalc || !sigi) return DGPU_ERR_ARG;
+    if (nrefl == 0) return DGPU_OK;
+    int32_t lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};          // the reference's extrema start at 0
+    for (int64_t r = 0; r < nrefl; r++)
+        for (int a = 0; a < 3; a++) {
+            lo[a] = hkl[3 * r + a] < lo[a] ? hkl[3 * r + a] : lo[a];
+            hi[a] = hkl[3 * r + a] > hi[a] ? hkl[3 * r + a] : hi[a];
+        }
+    dgpu_grid g;
+    memset(&g, 0, sizeof(g));
+    for (int a = 0; a < 3; a++) {
+        g.inc[a] = hi[a] - lo[a] + 1;
+        g.vi[4 * a] = 1.0;                                  // vi = identity
+        for (int c = 0; c < 4; c++) g.eck[3 * c + a] = lo[a];
+        g.eck[3 * (a + 1) + a] = hi[a];                     // corners lr, ul, tl along h, k, l
+    }
+    const int64_t np = (int64_t)g.inc[0] * g.inc[1] * g.inc[2];
+    DGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+    // the crystal to the device, as dgpu_four_run does
+    const int64_t n = cr->natoms;
+    if (n < 1 || !cr->pos || !cr->iscat) return dgpu_set_error(ctx, DGPU_ERR_NO_ATOMS, "no atoms");
+    DGPU_CUDA(ctx, ctx->pos.ensure(n * 3 * sizeof(double)));
+    DGPU_CUDA(ctx, ctx->iscat.ensure(n * sizeof(int32_t)));
+    DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->pos.p, cr->pos, n * 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->iscat.p, cr->iscat, n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+    dgpu_crystal dc = *cr;
+    dc.pos = ctx->pos.as<double>();
+    dc.iscat = ctx->iscat.as<int32_t>();
+    if (cr->atom_occ) {
+        DGPU_CUDA(ctx, ctx->aocc.ensure(n * sizeof(float)));
+        DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->aocc.p, cr->atom_occ, n * sizeof(float), cudaMemcpyHostToDevice,
+                                       ctx->stream));
+        dc.atom_occ = ctx->aocc.as<float>();
+    }
+    if (cr->is_anis) {
+        DGPU_CUDA(ctx, ctx->ianis.ensure(n * sizeof(int32_t)));
+        DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->ianis.p, cr->ianis, n * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                       ctx->stream));
+        dc.ianis = ctx->ianis.as<int32_t>();
+    }
+    DGPU_CUDA(ctx, ctx->csf.ensure(np * sizeof(double2)));
+    DGPU_CUDA(ctx, ctx->acsf.ensure(np * sizeof(double2)));
+    DGPU_CUDA(ctx, ctx->dsi.ensure(np * sizeof(double)));
+    int rc = dgpu_four_run_dev(ctx, &dc, &g, opts, ctx->csf.as<double2>(), ctx->acsf.as<double2>(),
+                               ctx->dsi.as<double>(), nullptr);
+    if (rc < 0) return rc;
+    HklSpec s;
+    memset(&s, 0, sizeof(s));
+    for (int a = 0; a < 3; a++) {
+        s.lo[a] = lo[a];
+        s.n[a] = g.inc[a];
+    }
+    s.ncells = (double)cr->icc[0] * cr->icc[1] * cr->icc[2];
+    s.scale = scale;
+    s.exti = exti;
+    s.rlambda = rlambda;
+    memcpy(s.rten, cr->rten, sizeof(s.rten));
+    DGPU_CUDA(ctx, ctx->wbuf.ensure((size_t)nrefl * (3 * sizeof(double) + 3 * sizeof(int32_t)) + 256));
+    double *d_out = ctx->wbuf.as<double>();
+    int32_t *d_hkl = reinterpret_cast<int32_t *>(d_out + 3 * nrefl);
+    DGPU_CUDA(ctx, cudaMemcpyAsync(d_hkl, hkl, (size_t)nrefl * 3 * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                   ctx->stream));
+    k_calc_hkl<<<(unsigned)dgpu_cdiv(nrefl, 256), 256, 0, ctx->stream>>>(s, d_hkl, nrefl, ctx->csf.as<double2>(),
+                                                                          d_out);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    DGPU_CUDA(ctx, cudaMemcpyAsync(icalc, d_out, (size_t)nrefl * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    DGPU_CUDA(ctx, cudaMemcpyAsync(sigi, d_out + nrefl, (size_t)nrefl * sizeof(double), cudaMemcpyDeviceToHost,
+                                   ctx->stream));
+    if (phase)
+        DGPU_CUDA(ctx, cudaMemcpyAsync(phase, d_out + 2 * nrefl, (size_t)nrefl * sizeof(double),
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return rc;
+}

@@ -132,6 +132,19 @@ def qval(cr: CrystalData, grid: GridData, opts: _abi.Opts, value, result: Fourie
     return out.reshape(grid.inc, order="F")
 
 
+def calc_hkl(cr: CrystalData, opts: _abi.Opts, hkl, scale=1.0, exti=0.0, rlambda=0.70932, ctx=None):
+    """calc_hkl (fourier_sup.f90:3230-3549) core on the device: (icalc, sigi,
+    phase) at the integer reflections hkl (n, 3)."""
+    ctx = ctx or default_context()
+    h = np.ascontiguousarray(np.asarray(hkl, dtype=np.int32).reshape(-1, 3))
+    n = h.shape[0]
+    ic, sg, ph = np.zeros(n), np.zeros(n), np.zeros(n)
+    c = cr.to_c()
+    ctx.check(ctx.lib.dgpu_calc_hkl(ctx.h, C.byref(c), C.byref(opts), _abi.iptr(h), n, float(scale), float(exti),
+                                    float(rlambda), _abi.dptr(ic), _abi.dptr(sg), _abi.dptr(ph)))
+    return ic, sg, ph
+
+
 def fourier_lmn(eck, vi, inc, ctx=None):
     """fourier_lmn (discus/prog/fourier_lmn_mod.f90:4-280): (rc, lmn[6], off_shift(3,3))."""
     ctx = ctx or default_context()

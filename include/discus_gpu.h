@@ -295,6 +295,20 @@ int dgpu_qval(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid, cons
               int32_t value, int32_t laver, const double *csf, const double *acsf, const double *dsi,
               const double *rand, double *out);
 
+/* calc_hkl (discus/prog/fourier_sup.f90:3230-3549), the numeric core: F at
+ * a list of integer reflections hkl(3,nrefl).  four_run runs on the integer
+ * box from min(0, h_min) to max(0, h_max) (same for k, l) with vi = identity
+ * and the caller's crystal and options; for every reflection
+ *   |F| = |csf(h,k,l)| / (icc1 icc2 icc3),
+ *   ext = (1 / (1 + 0.001 exti |F|^2 rlambda^3 / sin(2 asin(0.5 rlambda dstar))))^(1/4)
+ *   with dstar the length of (h,k,l) in the reciprocal metric,
+ *   icalc = (|F| ext)^2 scale,  sigi = sqrt(|icalc|),  phase = atan2d(Im, Re) of csf;
+ * the reflection 0 0 0 gives zeros.  Host arrays of nrefl values; phase may be
+ * NULL.  Reading and writing the HKLF4/CIF files stays with the caller.      */
+int dgpu_calc_hkl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *opts, const int32_t *hkl,
+                  int64_t nrefl, double scale, double exti, double rlambda, double *icalc, double *sigi,
+                  double *phase);
+
 /* ---- adjoint: chi^2 and its gradient ------------------------------------- */
 /* chi2 = sum_h w(h) (I(h) - I_target(h))^2 over the full grid, I = diff_scale*|csf|^2
  * as dgpu_four_run computes it (EXACT64 phase, ANALYTIC or TABLE form).

@@ -1275,3 +1275,54 @@ int oc_qval(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op, int
     free(istl); free(cf); free(cfp);
     return 0;
 }
+
+/* calc_hkl (fourier_sup.f90:3230-3549), the numeric core: four_run on the
+ * integer box of the listed reflections (extrema starting at 0, vi =
+ * identity), then per reflection the extinction-corrected intensity, its
+ * square root and the phase (:3491-3535). */
+int oc_calc_hkl(const dgpu_crystal *cr, const dgpu_opts *op, const int32_t *hkl, int64_t nrefl, double scale,
+                double exti, double rlambda, double *icalc, double *sigi, double *phase, int nthreads)
+{
+    const double pi = 3.1415926535897932384626433832795028841971693993751, rad = pi / 180.0;
+    int32_t lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    for (int64_t r = 0; r < nrefl; r++)
+        for (int a = 0; a < 3; a++) {
+            if (hkl[3 * r + a] < lo[a]) lo[a] = hkl[3 * r + a];
+            if (hkl[3 * r + a] > hi[a]) hi[a] = hkl[3 * r + a];
+        }
+    dgpu_grid g;
+    memset(&g, 0, sizeof(g));
+    for (int a = 0; a < 3; a++) {
+        g.inc[a] = hi[a] - lo[a] + 1;
+        M3(g.vi, a, a) = 1.0;
+        g.eck[a] = g.eck[3 + a] = g.eck[6 + a] = g.eck[9 + a] = lo[a];
+    }
+    g.eck[3 + 0] = hi[0];                        /* eck(1,2) = h_max */
+    g.eck[6 + 1] = hi[1];                        /* eck(2,3) = k_max */
+    g.eck[9 + 2] = hi[2];                        /* eck(3,4) = l_max */
+    int64_t np = (int64_t)g.inc[0] * g.inc[1] * g.inc[2];
+    double *csf = (double *)malloc(sizeof(double) * 2 * np);
+    double *acsf = (double *)malloc(sizeof(double) * 2 * np);
+    double *dsi = (double *)malloc(sizeof(double) * np);
+    int rc = oc_four_run(cr, &g, op, csf, acsf, dsi, NULL, nthreads);
+    if (rc >= 0) {
+        double ncells = (double)cr->icc[0] * cr->icc[1] * cr->icc[2];
+        for (int64_t r = 0; r < nrefl; r++) {
+            int32_t h = hkl[3 * r], k = hkl[3 * r + 1], l = hkl[3 * r + 2];
+            if (h == 0 && k == 0 && l == 0) { icalc[r] = sigi[r] = 0; if (phase) phase[r] = 0; continue; }
+            int64_t p = (h - lo[0]) + (int64_t)g.inc[0] * ((k - lo[1]) + (int64_t)g.inc[1] * (l - lo[2]));
+            double fr = csf[2 * p], fi = csf[2 * p + 1];
+            double qq = sqrt(fr * fr + fi * fi) / ncells;
+            double hv[3] = {h, k, l};
+            double ds = sqrt(oc_skal(hv, hv, cr->rten));
+            double tth = 2.0 * (asin(0.5 * rlambda * ds) / rad);
+            double ext = pow(1.0 / (1.0 + 0.001 * exti * qq * qq * rlambda * rlambda * rlambda / sin(tth * rad)), 0.25);
+            double e = qq * ext;
+            icalc[r] = e * e * scale;
+            sigi[r] = sqrt(fabs(icalc[r]));
+            if (phase) phase[r] = atan2(fi, fr) / rad;
+        }
+    }
+    free(csf); free(acsf); free(dsi);
+    return rc;
+}

@@ -57,6 +57,8 @@ int  oc_four_weight(const dgpu_crystal *cr, const dgpu_grid *grid, const dgpu_op
 void oc_fill_bragg(const dgpu_grid *grid, double *a, int comp);
 int  oc_qval(const dgpu_crystal *cr, const dgpu_grid *grid, const dgpu_opts *op, int value, int laver,
              const double *csf, const double *acsf, const double *dsi, const double *rnd, double *out);
+int  oc_calc_hkl(const dgpu_crystal *cr, const dgpu_opts *op, const int32_t *hkl, int64_t nrefl, double scale,
+                 double exti, double rlambda, double *icalc, double *sigi, double *phase, int nthreads);
 double oc_time_ref_rows(const dgpu_crystal *cr, const dgpu_grid *grid, int32_t row_lo,
                         int32_t row_hi, int nthreads, int64_t *pairs_out);
 

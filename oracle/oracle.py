@@ -45,6 +45,8 @@ def lib():
                                      dp, dp, dp]
         L.oc_fill_bragg.argtypes = [C.POINTER(_abi.Grid), dp, C.c_int]
         L.oc_fill_bragg.restype = None
+        L.oc_calc_hkl.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Opts), C.POINTER(C.c_int32), C.c_int64,
+                                  C.c_double, C.c_double, C.c_double, dp, dp, dp, C.c_int]
         L.oc_qval.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Grid), C.POINTER(_abi.Opts), C.c_int,
                               C.c_int, dp, dp, dp, dp, dp]
         _lib = L
@@ -221,3 +223,16 @@ def qval(cr, grid, opts, value, csf, acsf, dsi, laver=False, rand=None):
     rc = lib().oc_qval(C.byref(c), C.byref(g), C.byref(opts), int(value), int(bool(laver)), _d(cs), _d(ac),
                        _d(d), _d(rn) if rn is not None else None, _d(out))
     return rc, out.reshape(grid.inc, order="F")
+
+
+def calc_hkl(cr, opts, hkl, scale=1.0, exti=0.0, rlambda=0.70932, nthreads=0):
+    """(rc, icalc, sigi, phase) at the reflections hkl (n, 3)."""
+    if nthreads <= 0:
+        nthreads = os.cpu_count() or 1
+    h = np.ascontiguousarray(np.asarray(hkl, dtype=np.int32).reshape(-1, 3))
+    n = h.shape[0]
+    ic, sg, ph = np.zeros(n), np.zeros(n), np.zeros(n)
+    c = cr.to_c()
+    rc = lib().oc_calc_hkl(C.byref(c), C.byref(opts), h.ctypes.data_as(C.POINTER(C.c_int32)), n, float(scale),
+                           float(exti), float(rlambda), _d(ic), _d(sg), _d(ph), nthreads)
+    return rc, ic, sg, ph
