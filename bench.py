@@ -319,6 +319,60 @@ def lots_measure(ctx, c, g, op_main, csf, acsf, dsi, flush, cr, grid, steps=2, n
             "launches": -(-nlots // per_launch), "engine": {1: "direct", 2: "tc"}.get(info.engine_used)}
 
 
+POWDER = dict(hkl_del=(0.05, 0.05, 0.02), ds_max=0.8, qmin=0.5, qmax=5.0, deltaq=0.001, l_all=True)
+
+
+def powder_measure(ctx, cr, flush, steps=2, cpu=True):
+    """Powder complete mode (powder_complete, powder.f90:1829-2593) on the
+    headline crystal: rods of dH = dK = 0.05, dL = 0.02 inside d* <= 0.8 1/A,
+    binned on Q = 0.5..5 1/A in 0.001 steps, X-ray form factors with
+    Debye-Waller.  Through the host API (crystal upload and pattern download
+    inside the timed call), L2 flushed before each step.  Pairs are atoms x
+    rod points, the reference's work; the device also evaluates the rest of
+    each slab box (grid_points)."""
+    import torch
+    from diffusecode_gb300 import fourier as FR
+    pw = S.PowderSpec.for_lattice(3.6, 3.6, 3.6, **POWDER)
+    op = _abi.default_opts(ldbw=1, phase=_abi.PHASE_EXACT64)
+    FR.powder_complete(cr, pw, op, ctx=ctx)
+    ts, ks = [], []
+    info = None
+    for _ in range(steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, info = FR.powder_complete(cr, pw, op, ctx=ctx)
+        ts.append(time.perf_counter() - t0)
+        ks.append(info.kernel_ms)
+    wall = sum(ts) / len(ts)
+    natoms = cr.n_scattering()
+    pairs = natoms * info.rod_points
+    out = {"workload": f"powder complete, {natoms} atoms, dhkl {list(POWDER['hkl_del'])}, ds_max "
+                       f"{POWDER['ds_max']}, Q {POWDER['qmin']}..{POWDER['qmax']} step {POWDER['deltaq']}",
+           "rods": int(info.rods), "rod_points": int(info.rod_points), "grid_points": int(info.grid_points),
+           "slabs": int(info.nslab), "binned": int(info.binned), "ms_per_call": wall * 1e3,
+           "device_ms": info.total_ms, "kernel_ms": sum(ks) / len(ks),
+           "G_pairs_per_s": pairs / wall / 1e9, "pairs": int(pairs)}
+    if cpu:
+        from oracle import oracle as O
+        # the oracle's literal rod loop with the reference's REF22 arithmetic on a
+        # contiguous block of rods from the middle of the loop, about 8 s
+        op_ref = _abi.default_opts(ldbw=1, phase=_abi.PHASE_REF22)
+        nth = os.cpu_count() or 1
+        mid = int(info.rods) // 2
+        t0 = time.perf_counter()
+        _, _, _, n0 = O.powder_complete(cr, pw, op_ref, mid, mid + nth, nthreads=nth)
+        t_cal = time.perf_counter() - t0
+        nrod = max(nth, min(int(info.rods) - mid, int(nth * 8.0 / max(t_cal, 1e-3))))
+        t0 = time.perf_counter()
+        _, _, _, npts = O.powder_complete(cr, pw, op_ref, mid, mid + nrod, nthreads=nth)
+        sec = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": natoms * npts / sec / 1e9, "unit": "G pairs/s", "cores": nth,
+                               "kind": "port", "sample": f"oracle rod loop (REF22), rods {mid}..{mid + nrod} "
+                                                         f"({npts} points), {sec:.1f} s"}
+    return out
+
+
 def batch_measure(ctx, steps=3):
     """Population workload: 64 crystals (cubic / fcc / rock salt), atoms
     log-uniform in [2000, 200000], each with its own 2D plane of 129^2..257^2
@@ -473,6 +527,7 @@ def run_ours(args, world, rank, local):
     adj = None if args.no_adjoint else adjoint_measure(ctx, engine)
     bat = None if args.no_batch else batch_measure(ctx)
     lots = None if args.no_lots else lots_measure(ctx, c, g, op, csf, acsf, dsi, flush, cr, grid)
+    powder = None if args.no_powder else powder_measure(ctx, cr, flush, cpu=not args.no_cpu_baseline)
     pk, pk_kind = peaks()
     fnum_pts = int(np.prod(list(info.fnum)))
     pairs_computed = cr.n_scattering() * fnum_pts
@@ -513,6 +568,7 @@ def run_ours(args, world, rank, local):
         "adjoint": adj,
         "batch": bat,
         "lots": lots,
+        "powder": powder,
         "tc_config": list(info.tc_config),
         "gpu_launches": LAUNCHES_PER_RUN.get(engine_used, 10) * args.steps,
         "accuracy": {"rel_err_vs_fp64": acc_err, "points": acc_pts,
@@ -542,6 +598,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-lots", action="store_true")
+    ap.add_argument("--no-powder", action="store_true")
     ap.add_argument("--tc-flush", type=int, default=0, help="atoms per main-accumulator drain (0: default)")
     args = ap.parse_args()
     world, rank, local = dist_init()

@@ -56,6 +56,9 @@ ACCUM_FINISHED = 2
 LOT_OFF = 1
 LOT_BOX = 2
 LOT_ELI = 3
+PREF_NONE = 0
+PREF_RIETVELD = 1
+PREF_MARCH = 2
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
@@ -137,6 +140,38 @@ class Info(C.Structure):
         ("kernel_ms", C.c_double),
         ("total_ms", C.c_double),
         ("tc_config", C.c_int32 * 4),
+    ]
+
+
+class Powder(C.Structure):
+    _fields_ = [
+        ("hkl_del", C.c_double * 3),
+        ("hkl_shift", C.c_double * 3),
+        ("a0", C.c_double * 3),
+        ("gten", C.c_double * 9),
+        ("ds_max", C.c_double),
+        ("qmin", C.c_double),
+        ("qmax", C.c_double),
+        ("deltaq", C.c_double),
+        ("l_all", C.c_int32),
+        ("pref_type", C.c_int32),
+        ("pref_hkl", C.c_double * 3),
+        ("pref_g1", C.c_double),
+        ("pref_g2", C.c_double),
+    ]
+
+
+class PowderInfo(C.Structure):
+    _fields_ = [
+        ("n_pkt", C.c_int32),
+        ("nslab", C.c_int32),
+        ("rods", C.c_int64),
+        ("rod_points", C.c_int64),
+        ("grid_points", C.c_int64),
+        ("binned", C.c_int64),
+        ("pairs", C.c_int64),
+        ("kernel_ms", C.c_double),
+        ("total_ms", C.c_double),
     ]
 
 

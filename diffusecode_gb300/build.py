@@ -17,7 +17,7 @@ LIB = os.path.join(OUT_DIR, "libdiscus_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-Xptxas", "-warn-spills"]
-CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17"]
+CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off"]
 
 
 def _nvcc():

@@ -69,7 +69,7 @@ extern "C" int dgpu_ctx_create(int device, dgpu_ctx **out)
     if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) { delete c; return DGPU_ERR_CUDA; }
     c->nsm = prop.multiProcessorCount;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { delete c; return DGPU_ERR_CUDA; }
-    for (int i = 0; i < 8; i++)
+    for (int i = 0; i < DGPU_NEV; i++)
         if (cudaEventCreate(&c->ev[i]) != cudaSuccess) { delete c; return DGPU_ERR_CUDA; }
     *out = c;
     return DGPU_OK;
@@ -90,7 +90,7 @@ extern "C" int dgpu_ctx_destroy(dgpu_ctx *c)
                       &c->wbuf, &c->acc_csf, &c->acc_dsi};
     for (DevBuf *b : bufs) b->release();
     delete c->fs_main;
-    for (int i = 0; i < 8; i++)
+    for (int i = 0; i < DGPU_NEV; i++)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -495,20 +495,17 @@ extern "C" int dgpu_four_run_device(dgpu_ctx *ctx, const dgpu_crystal *cr, const
     return dgpu_four_run_dev(ctx, cr, grid, opts, (double2 *)d_csf, acsf, d_dsi, info);
 }
 
-extern "C" int dgpu_four_run(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid, const dgpu_opts *opts,
-                             double *csf, double *acsf, double *dsi, dgpu_info *info)
+// The per-atom arrays of a host crystal to the context's device buffers
+// (enqueued on its stream); dc is the crystal with those device pointers.
+int dgpu_stage_crystal(dgpu_ctx *ctx, const dgpu_crystal *cr, dgpu_crystal &dc)
 {
-    if (!ctx || !cr || !grid || !opts || !csf || !dsi) return DGPU_ERR_ARG;
-    int rc = check_inputs(ctx, cr, grid, opts);
-    if (rc) return rc;
-    DGPU_CUDA(ctx, cudaSetDevice(ctx->device));
     const int64_t n = cr->natoms;
-    const int64_t np = (int64_t)grid->inc[0] * grid->inc[1] * grid->inc[2];
+    if (n < 1 || !cr->pos || !cr->iscat) return dgpu_set_error(ctx, DGPU_ERR_NO_ATOMS, "no atoms");
     DGPU_CUDA(ctx, ctx->pos.ensure(n * 3 * sizeof(double)));
     DGPU_CUDA(ctx, ctx->iscat.ensure(n * sizeof(int32_t)));
     DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->pos.p, cr->pos, n * 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->iscat.p, cr->iscat, n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
-    dgpu_crystal dc = *cr;
+    dc = *cr;
     dc.pos = ctx->pos.as<double>();
     dc.iscat = ctx->iscat.as<int32_t>();
     if (cr->atom_occ) {
@@ -516,11 +513,25 @@ extern "C" int dgpu_four_run(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_g
         DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->aocc.p, cr->atom_occ, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
         dc.atom_occ = ctx->aocc.as<float>();
     }
-    if (cr->is_anis) {
+    if (cr->is_anis && cr->ianis) {
         DGPU_CUDA(ctx, ctx->ianis.ensure(n * sizeof(int32_t)));
         DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->ianis.p, cr->ianis, n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
         dc.ianis = ctx->ianis.as<int32_t>();
     }
+    return DGPU_OK;
+}
+
+extern "C" int dgpu_four_run(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid, const dgpu_opts *opts,
+                             double *csf, double *acsf, double *dsi, dgpu_info *info)
+{
+    if (!ctx || !cr || !grid || !opts || !csf || !dsi) return DGPU_ERR_ARG;
+    int rc = check_inputs(ctx, cr, grid, opts);
+    if (rc) return rc;
+    DGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int64_t np = (int64_t)grid->inc[0] * grid->inc[1] * grid->inc[2];
+    dgpu_crystal dc;
+    rc = dgpu_stage_crystal(ctx, cr, dc);
+    if (rc) return rc;
     DGPU_CUDA(ctx, ctx->csf.ensure(np * sizeof(double2)));
     DGPU_CUDA(ctx, ctx->acsf.ensure(np * sizeof(double2)));
     DGPU_CUDA(ctx, ctx->dsi.ensure(np * sizeof(double)));

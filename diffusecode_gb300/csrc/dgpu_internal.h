@@ -59,11 +59,12 @@ typedef std::tuple<int32_t, int32_t, int32_t, int32_t, int32_t, int32_t, int32_t
 struct BatchState;   // k_batch.cu
 struct FormSpec;
 
+#define DGPU_NEV 10
 struct dgpu_ctx {
     int device = 0;
     int nsm = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev[8] = {};
+    cudaEvent_t ev[DGPU_NEV] = {};   // 0-1 four_run, 2-3 sums, 4-7 tensor core, 8-9 powder
     char err[512] = {0};
     // cached buffers
     DevBuf pos, iscat, aocc, sel;
@@ -345,6 +346,7 @@ int dgpu_adjtc_sums(dgpu_ctx *ctx, const BoxSpec &box, const dgpu_grid *grid, in
 void dgpu_batch_free(dgpu_ctx *ctx);
 
 // the whole four_run with device-resident crystal arrays and outputs
+int dgpu_stage_crystal(dgpu_ctx *ctx, const dgpu_crystal *cr, dgpu_crystal &dc);
 int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,
                       double2 *d_csf, double2 *d_acsf, double *d_dsi, dgpu_info *info);
 

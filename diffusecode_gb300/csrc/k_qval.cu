@@ -249,33 +249,14 @@ extern "C" int dgpu_calc_hkl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_o
     }
     const int64_t np = (int64_t)g.inc[0] * g.inc[1] * g.inc[2];
     DGPU_CUDA(ctx, cudaSetDevice(ctx->device));
-    // the crystal to the device, as dgpu_four_run does
-    const int64_t n = cr->natoms;
-    if (n < 1 || !cr->pos || !cr->iscat) return dgpu_set_error(ctx, DGPU_ERR_NO_ATOMS, "no atoms");
-    DGPU_CUDA(ctx, ctx->pos.ensure(n * 3 * sizeof(double)));
-    DGPU_CUDA(ctx, ctx->iscat.ensure(n * sizeof(int32_t)));
-    DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->pos.p, cr->pos, n * 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->iscat.p, cr->iscat, n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
-    dgpu_crystal dc = *cr;
-    dc.pos = ctx->pos.as<double>();
-    dc.iscat = ctx->iscat.as<int32_t>();
-    if (cr->atom_occ) {
-        DGPU_CUDA(ctx, ctx->aocc.ensure(n * sizeof(float)));
-        DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->aocc.p, cr->atom_occ, n * sizeof(float), cudaMemcpyHostToDevice,
-                                       ctx->stream));
-        dc.atom_occ = ctx->aocc.as<float>();
-    }
-    if (cr->is_anis) {
-        DGPU_CUDA(ctx, ctx->ianis.ensure(n * sizeof(int32_t)));
-        DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->ianis.p, cr->ianis, n * sizeof(int32_t), cudaMemcpyHostToDevice,
-                                       ctx->stream));
-        dc.ianis = ctx->ianis.as<int32_t>();
-    }
+    dgpu_crystal dc;
+    int rc = dgpu_stage_crystal(ctx, cr, dc);
+    if (rc) return rc;
     DGPU_CUDA(ctx, ctx->csf.ensure(np * sizeof(double2)));
     DGPU_CUDA(ctx, ctx->acsf.ensure(np * sizeof(double2)));
     DGPU_CUDA(ctx, ctx->dsi.ensure(np * sizeof(double)));
-    int rc = dgpu_four_run_dev(ctx, &dc, &g, opts, ctx->csf.as<double2>(), ctx->acsf.as<double2>(),
-                               ctx->dsi.as<double>(), nullptr);
+    rc = dgpu_four_run_dev(ctx, &dc, &g, opts, ctx->csf.as<double2>(), ctx->acsf.as<double2>(),
+                           ctx->dsi.as<double>(), nullptr);
     if (rc < 0) return rc;
     HklSpec s;
     memset(&s, 0, sizeof(s));

@@ -20,7 +20,7 @@ import numpy as np
 
 from . import _abi
 from ._lib import default_context
-from .structures import CrystalData, GridData
+from .structures import CrystalData, GridData, PowderSpec
 
 
 @dataclass
@@ -143,6 +143,22 @@ def calc_hkl(cr: CrystalData, opts: _abi.Opts, hkl, scale=1.0, exti=0.0, rlambda
     ctx.check(ctx.lib.dgpu_calc_hkl(ctx.h, C.byref(c), C.byref(opts), _abi.iptr(h), n, float(scale), float(exti),
                                     float(rlambda), _abi.dptr(ic), _abi.dptr(sg), _abi.dptr(ph)))
     return ic, sg, ph
+
+
+def powder_complete(cr: CrystalData, pw: PowderSpec, opts: _abi.Opts, ctx=None):
+    """powder_complete (discus/prog/powder.f90:1829-2593), pow_four_mode =
+    fourier, on the device: (pow_qsp[0..n_pkt], info)."""
+    ctx = ctx or default_context()
+    p = pw.to_c()
+    n = ctx.lib.dgpu_powder_npkt(C.byref(p))
+    if n < 0:
+        raise ValueError("invalid Q range")
+    qsp = np.zeros(n + 1)
+    info = _abi.PowderInfo()
+    c = cr.to_c()
+    ctx.check(ctx.lib.dgpu_powder_complete(ctx.h, C.byref(c), C.byref(p), C.byref(opts), _abi.dptr(qsp),
+                                           C.byref(info)))
+    return qsp, info
 
 
 def fourier_lmn(eck, vi, inc, ctx=None):

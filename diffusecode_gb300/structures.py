@@ -40,6 +40,66 @@ def reciprocal_metric(a, b, c, alpha, beta, gamma):
     return g
 
 
+def direct_metric(a, b, c, alpha, beta, gamma):
+    """cr_gten from lattice constants (spcgr_apply.f90:3538-3658): a_i a_j cos."""
+    a0 = (a, b, c)
+    cw = [math.cos(math.radians(x)) for x in (alpha, beta, gamma)]
+    g = np.empty((3, 3))
+    for i in range(3):
+        for j in range(3):
+            g[i, j] = a0[i] * a0[i] if i == j else a0[i] * a0[j] * cw[3 - i - j]
+    return g
+
+
+@dataclass
+class PowderSpec:
+    """The powder menu state powder_complete reads (powder_mod.f90): steps and
+    shift along h, k, l, the d* sphere, the Q scale and the preferred
+    orientation.  a0/gten are the crystal's cr_a0/cr_gten."""
+    a0: tuple
+    gten: np.ndarray
+    hkl_del: tuple = (0.05, 0.05, 0.05)
+    hkl_shift: tuple = (0.0, 0.0, 0.0)
+    ds_max: float = 0.8
+    qmin: float = 0.5
+    qmax: float = 5.0
+    deltaq: float = 0.001
+    l_all: bool = True
+    pref_type: int = 0
+    pref_hkl: tuple = (0.0, 0.0, 1.0)
+    pref_g1: float = 0.0
+    pref_g2: float = 0.0
+
+    @classmethod
+    def for_lattice(cls, a, b, c, alpha=90.0, beta=90.0, gamma=90.0, **kw):
+        return cls(a0=(a, b, c), gten=direct_metric(a, b, c, alpha, beta, gamma), **kw)
+
+    def to_c(self):
+        p = _abi.Powder()
+        for k in range(3):
+            p.hkl_del[k] = float(self.hkl_del[k])
+            p.hkl_shift[k] = float(self.hkl_shift[k])
+            p.a0[k] = float(self.a0[k])
+            p.pref_hkl[k] = float(self.pref_hkl[k])
+        for k, v in enumerate(np.asarray(self.gten, dtype=np.float64).reshape(-1, order="F")):
+            p.gten[k] = float(v)
+        p.ds_max, p.qmin, p.qmax, p.deltaq = float(self.ds_max), float(self.qmin), float(self.qmax), float(self.deltaq)
+        p.l_all = 1 if self.l_all else 0
+        p.pref_type = int(self.pref_type)
+        p.pref_g1, p.pref_g2 = float(self.pref_g1), float(self.pref_g2)
+        return p
+
+    @property
+    def n_pkt(self):
+        """powder.f90:1957: NINT((qmax + deltaq - qmin) / deltaq) + 2."""
+        x = (self.qmax + self.deltaq - self.qmin) / self.deltaq
+        return int(math.floor(x + 0.5)) + 2
+
+    def q(self):
+        """Q of pow_qsp(0:n_pkt)."""
+        return self.qmin + self.deltaq * np.arange(self.n_pkt + 1)
+
+
 @dataclass
 class CrystalData:
     pos: np.ndarray            # (natoms, 3) float64, lattice units

@@ -309,6 +309,73 @@ int dgpu_calc_hkl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *opts, 
                   int64_t nrefl, double scale, double exti, double rlambda, double *icalc, double *sigi,
                   double *phase);
 
+/* ---- powder pattern, "complete" mode -------------------------------------- */
+/* powder_complete (discus/prog/powder.f90:1829-2593) with pow_four_mode =
+ * fourier: the structure factor four_run_powder (powder.f90:3143-3206) along
+ * every (h, k) rod inside the d* <= ds_max sphere, binned onto the Q scale by
+ * powder_split (powder.f90:2975-3008).
+ *
+ *   h:  ih = h_start..h_end, h_start = ano ? -int(a0(1) ds_max / dH) : 0,
+ *       hh = ih dH + shift(1);
+ *   k:  the range of the circle d* = ds_max in the plane hh as do_proj
+ *       (metric.f90:337-548) returns it for "hh,0,0, 1,0,0, rdrr" and
+ *       "0,1,0, 1,0,0, ddrr" (its parallel part is v / (u.v) / |v|^2, which
+ *       is what the reference enumerates), k = 0.. in the plane h = 0 without ano;
+ *   l:  int(l_lo / dL) .. int(l_hi / dL), l_lo/l_hi the roots of
+ *       d*(hh, kk, l) = ds_max, from l = 0 on the rod h = k = 0 without ano;
+ *   every point with pow_l_all, or with h, k or l more than 0.51 steps from
+ *       an integer, and qmin <= Q = 2 pi d* <= qmax + deltaq adds
+ *       |F|^2 x calc_preferred (powder.f90:3332-3376) to pow_qsp(itth1) and
+ *       pow_qsp(itth1 + 1), split linearly, itth1 = int((Q - qmin) / deltaq);
+ *   without ano the pattern is doubled at the end.
+ * F is four_run's sum over all atoms and types: no <F> subtraction, no lots,
+ * no diff_scale; cfact from (lxray, power, ano, ldbw) of opts, and, as
+ * four_run_powder passes is_anis = .false. while four_formtab drops the
+ * isotropic term of an anisotropic crystal, no Debye-Waller factor at all for
+ * an anisotropic crystal.  The device evaluates F on h-slabs of the (h, k, l)
+ * box that holds the rods (EXACT64 phases, either engine) and bins only the
+ * rod points.  Not covered: stacking-fault crystals (scale_diffuse,
+ * set_scale_mode) and the structure transformation trans_to_short: dL must
+ * be the smallest of the three steps (else DGPU_ERR_UNSUPPORTED).  The
+ * form-factor averages pow_f2aver/pow_faver2 are computed afterwards, in
+ * phases_set_mod, and stay with the caller.                                 */
+#define DGPU_PREF_NONE      0
+#define DGPU_PREF_RIETVELD  1   /* g2 + (1 - g2) exp(g1 alpha^2), alpha in degrees */
+#define DGPU_PREF_MARCH     2   /* g2 + (1 - g2) ((g1 cos alpha)^2 + sin^2 alpha / g1)^(-3/2) */
+typedef struct dgpu_powder {
+    double  hkl_del[3];    /* pow_hkl_del: dH, dK, dL                                */
+    double  hkl_shift[3];  /* pow_hkl_shift                                          */
+    double  a0[3];         /* cr_a0, A (pow_hkl_max = a0 ds_max)                      */
+    double  gten[9];       /* cr_gten, direct metric tensor, column-major            */
+    double  ds_max;        /* pow_ds_max, 1/A                                         */
+    double  qmin;          /* pow_qmin, 1/A                                           */
+    double  qmax;          /* pow_qmax                                               */
+    double  deltaq;        /* pow_deltaq                                             */
+    int32_t l_all;         /* pow_l_all: integer (Bragg) points are binned as well   */
+    int32_t pref_type;     /* DGPU_PREF_*                                            */
+    double  pref_hkl[3];   /* pow_pref_hkl                                           */
+    double  pref_g1;       /* pow_pref_g1                                            */
+    double  pref_g2;       /* pow_pref_g2                                            */
+} dgpu_powder;
+
+typedef struct dgpu_powder_info {
+    int32_t n_pkt;         /* pow_npkt: pow_qsp has n_pkt + 1 values, itth 0..n_pkt  */
+    int32_t nslab;         /* device grids evaluated                                 */
+    int64_t rods;          /* (h, k) rods of powder_complete                         */
+    int64_t rod_points;    /* points on those rods (four_run_powder's points)        */
+    int64_t grid_points;   /* points evaluated on the device                         */
+    int64_t binned;        /* points added to pow_qsp                                */
+    int64_t pairs;         /* atom x evaluated-point pairs                           */
+    double  kernel_ms;     /* device time of the atom x point sums                   */
+    double  total_ms;      /* device time of the whole call                          */
+} dgpu_powder_info;
+
+/* n_pkt = NINT((qmax + deltaq - qmin) / deltaq) + 2 (powder.f90:1957), or <0. */
+int32_t dgpu_powder_npkt(const dgpu_powder *pw);
+/* pow_qsp: host array of n_pkt + 1 doubles (overwritten).  info may be NULL. */
+int dgpu_powder_complete(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_powder *pw,
+                         const dgpu_opts *opts, double *pow_qsp, dgpu_powder_info *info);
+
 /* ---- adjoint: chi^2 and its gradient ------------------------------------- */
 /* chi2 = sum_h w(h) (I(h) - I_target(h))^2 over the full grid, I = diff_scale*|csf|^2
  * as dgpu_four_run computes it (EXACT64 phase, ANALYTIC or TABLE form).

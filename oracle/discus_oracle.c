@@ -1326,3 +1326,243 @@ int oc_calc_hkl(const dgpu_crystal *cr, const dgpu_opts *op, const int32_t *hkl,
     free(csf); free(acsf); free(dsi);
     return rc;
 }
+
+/* ---- powder "complete" mode ------------------------------------------------
+ * powder_complete (discus/prog/powder.f90:1829-2593) with pow_four_mode =
+ * fourier: the literal rod loop, four_run_powder (:3143-3206) per rod as a
+ * four_run over the rod's line of points (all atoms, no <F>, no lots; the
+ * anisotropic crystal gets no Debye-Waller factor, since four_strucf is called
+ * with is_anis = .false. and four_formtab leaves it out of cfact), binned by
+ * powder_split (:2975-3008) in the reference's order. */
+
+static void pw_matvec(const double *t, const double *x, double *y)   /* matmul(t, x) */
+{
+    for (int i = 0; i < 3; i++) y[i] = (M3(t, i, 0) * x[0] + M3(t, i, 1) * x[1]) + M3(t, i, 2) * x[2];
+}
+
+static double pw_dot(const double *a, const double *b) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+
+static double pw_skalpro(const double *a, const double *b, const double *t)   /* metric.f90:90-105 */
+{
+    double m[3];
+    pw_matvec(t, b, m);
+    return pw_dot(a, m);
+}
+
+/* do_proj (metric.f90:337-548): res[0..2] and res[3..5] as the command
+ * returns them in res_para(1:6) for the four space letters sp. */
+static int pw_do_proj(const double *uin, const double *vin, const char *sp, const double *rten,
+                      const double *gten, double *res)
+{
+    double u[3], v[3], w[3], h[3], x[3];
+    memcpy(u, uin, sizeof u);
+    memcpy(v, vin, sizeof v);
+    if (sp[0] == 'r') { pw_matvec(rten, u, w); memcpy(u, w, sizeof u); }
+    if (sp[1] == 'r') { pw_matvec(rten, v, w); memcpy(v, w, sizeof v); }
+    double uv = pw_skalpro(u, v, gten);
+    double vv = pw_skalpro(v, v, gten);
+    if (vv == 0.0) return -1;
+    for (int i = 0; i < 3; i++) w[i] = v[i] / uv / vv;
+    if (sp[2] == 'r') { pw_matvec(gten, w, x); memcpy(w, x, sizeof w); }
+    memcpy(res, w, sizeof w);
+    pw_matvec(gten, v, h);
+    double uh = pw_dot(u, h);
+    double hh = pw_skalpro(h, h, rten);
+    if (hh == 0.0) return -1;
+    for (int i = 0; i < 3; i++) w[i] = u[i] - uh * v[i] / hh;
+    if (sp[3] == 'r') { pw_matvec(gten, w, x); memcpy(w, x, sizeof w); }
+    memcpy(res + 3, w, sizeof w);
+    return 0;
+}
+
+/* calc_preferred (powder.f90:3332-3376) with do_bang (metric.f90:35-86):
+ * lspace = .true., so the angle between hkl and pref_hkl is taken in the
+ * direct metric; acos is divided by REAL(rad), rad in single precision. */
+static double pw_preferred(const double *hkl, const dgpu_powder *pw)
+{
+    const double pi = 3.1415926535897932384626433832795028841971693993751, rad = pi / 180.0;
+    double x[3], y[3];
+    for (int i = 0; i < 3; i++) { x[i] = 0.0 - hkl[i]; y[i] = 0.0 - pw->pref_hkl[i]; }
+    double xx = sqrt(pw_skalpro(x, x, pw->gten)), xy = pw_skalpro(x, y, pw->gten), yy = sqrt(pw_skalpro(y, y, pw->gten));
+    double alpha = 0.0;
+    if (xx > 0 && yy > 0) {
+        double arg = xy / (xx * yy);
+        if (fabs(arg) < 1.0) alpha = acos(arg) / (double)(float)rad;
+        else if (arg >= 1.0) alpha = 0.0;
+        else alpha = 180.0;
+    }
+    if (pw->pref_type == DGPU_PREF_RIETVELD) {
+        double a2 = alpha <= 90.0 ? alpha * alpha : (180 - alpha) * (180 - alpha);
+        return pw->pref_g2 + (1. - pw->pref_g2) * exp(pw->pref_g1 * a2);
+    }
+    if (pw->pref_type == DGPU_PREF_MARCH) {
+        double c = pw->pref_g1 * cos(alpha * rad), s = sin(alpha * rad);
+        return pw->pref_g2 + (1. - pw->pref_g2) * pow(c * c + s * s / pw->pref_g1, -1.5);
+    }
+    return 1.0;
+}
+
+typedef struct { int32_t ih, ik, l_start, n; double hh, kk, e31; int hreal, kreal; } pw_rod;
+
+/* The rods of powder_complete in loop order; returns their count (rods may
+ * be NULL to count only), or -1. */
+static int64_t pw_rods(const dgpu_crystal *cr, const dgpu_powder *pw, int ano, pw_rod *rods)
+{
+    const double *del = pw->hkl_del, *sh = pw->hkl_shift, *rten = cr->rten;
+    double hkl_max1 = pw->a0[0] * pw->ds_max;
+    int32_t h_start = ano ? -(int32_t)(hkl_max1 / del[0]) : 0;
+    int32_t h_end = (int32_t)(hkl_max1 / del[0]);
+    int64_t nr = 0;
+    double v[3], res[6];
+    const double e1[3] = {1, 0, 0}, e2[3] = {0, 1, 0};
+    for (int32_t ih = h_start; ih <= h_end; ih++) {
+        double hh = ih * del[0] + sh[0];
+        int hreal = fabs((round(hh) - hh) / del[0]) > 0.51;
+        double u[3], u2;
+        if (hh == 0.0) {
+            u[0] = u[1] = u[2] = 0.0;
+            u2 = 0.0;
+        } else {
+            double hv[3] = {hh, 0, 0};
+            if (pw_do_proj(hv, e1, "rdrr", rten, pw->gten, res)) return -1;
+            memcpy(u, res, sizeof u);
+            u2 = pw_skalpro(u, u, rten);
+        }
+        if (pw_do_proj(e2, e1, "ddrr", rten, pw->gten, res)) return -1;
+        memcpy(v, res + 3, sizeof v);
+        double vv = sqrt(pw_skalpro(v, v, rten));
+        for (int i = 0; i < 3; i++) v[i] = v[i] / vv;
+        double rr = pw->ds_max * pw->ds_max - u2;
+        double wmin[3], wmax[3];
+        if (rr >= 0.0)
+            for (int i = 0; i < 3; i++) {
+                wmin[i] = u[i] - sqrt(rr) * v[i];
+                wmax[i] = u[i] + sqrt(rr) * v[i];
+            }
+        if (!(rr > 0.0)) continue;
+        int32_t k_start = (!ano && ih == 0) ? 0 : (int32_t)(wmin[1] / del[1]);
+        int32_t k_end = (int32_t)(wmax[1] / del[1]);
+        for (int32_t ik = k_start; ik <= k_end; ik++) {
+            double kk = ik * del[1] + sh[1];
+            int kreal = fabs((round(kk) - kk) / del[1]) > 0.51;
+            double aaa = M3(rten, 2, 2);
+            double bbb = 2.0 * (M3(rten, 0, 2) * hh + M3(rten, 1, 2) * kk);
+            double ccc = M3(rten, 0, 0) * (hh * hh) + 2.0 * M3(rten, 0, 1) * hh * kk + M3(rten, 1, 1) * (kk * kk) -
+                         pw->ds_max * pw->ds_max;
+            double rrr = bbb * bbb - 4.0 * aaa * ccc;
+            int32_t l_start = 0, l_end = 0;
+            if (rrr >= 0.0) {
+                double llstart = (-bbb - sqrt(rrr)) / 2. / aaa;
+                double llend = (-bbb + sqrt(rrr)) / 2. / aaa;
+                if (!ano && ih == 0 && ik == 0) {
+                    l_start = 0;
+                    l_end = (int32_t)(llend / del[2]);
+                } else {
+                    l_start = (int32_t)(llstart / del[2]);
+                    l_end = (int32_t)(llend / del[2]);
+                }
+            }
+            if (!(rrr > 0.0)) continue;
+            double e31 = l_start * del[2] + sh[2], e32 = l_end * del[2] + sh[2];
+            int32_t n = (int32_t)lround((e32 - e31) / del[2]) + 1;
+            if (rods) {
+                pw_rod *r = rods + nr;
+                r->ih = ih; r->ik = ik; r->l_start = l_start; r->n = n;
+                r->hh = hh; r->kk = kk; r->e31 = e31; r->hreal = hreal; r->kreal = kreal;
+            }
+            nr++;
+        }
+    }
+    return nr;
+}
+
+int oc_powder_npkt(const dgpu_powder *pw)
+{
+    if (!(pw->deltaq > 0.0) || !(pw->qmax >= pw->qmin)) return -1;
+    return (int)lround((pw->qmax + pw->deltaq - pw->qmin) / pw->deltaq) + 2;   /* powder.f90:1957 */
+}
+
+int oc_powder_complete(const dgpu_crystal *cr, const dgpu_powder *pw, const dgpu_opts *op, int64_t rod_lo,
+                       int64_t rod_hi, double *qsp, int64_t *nrods_out, int64_t *npoints_out, int nthreads)
+{
+    const double pi = 3.1415926535897932384626433832795028841971693993751, zpi = 2.0 * pi;
+    int n_pkt = oc_powder_npkt(pw);
+    if (n_pkt < 0) return DGPU_ERR_ARG;
+    if (!(pw->hkl_del[2] <= pw->hkl_del[0] && pw->hkl_del[2] <= pw->hkl_del[1])) return DGPU_ERR_UNSUPPORTED;
+    int64_t nr = pw_rods(cr, pw, op->ano, NULL);
+    if (nr < 0) return DGPU_ERR_ARG;
+    pw_rod *rods = (pw_rod *)malloc(sizeof(pw_rod) * (nr > 0 ? nr : 1));
+    pw_rods(cr, pw, op->ano, rods);
+    if (rod_lo < 0) rod_lo = 0;
+    if (rod_hi < 0 || rod_hi > nr) rod_hi = nr;
+    if (nrods_out) *nrods_out = nr;
+    int64_t *first = (int64_t *)malloc(sizeof(int64_t) * (nr + 1));
+    first[0] = 0;
+    for (int64_t r = 0; r < nr; r++) first[r + 1] = first[r] + (r >= rod_lo && r < rod_hi ? rods[r].n : 0);
+    if (npoints_out) *npoints_out = first[nr];
+    double *csf = (double *)malloc(sizeof(double) * 2 * (first[nr] > 0 ? first[nr] : 1));
+    dgpu_crystal c2 = *cr;
+    c2.is_anis = 0;
+    dgpu_opts o2 = *op;
+    o2.fave = 0.0;
+    o2.aver_cells = NULL;
+    o2.ilots = DGPU_LOT_OFF;
+    o2.lot_all = 0;
+    o2.lperiod = 1;
+    o2.diff_scale = 1.0;
+    o2.ldbw = (op->ldbw && !cr->is_anis) ? 1 : 0;
+    int rc = 0;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads > 0 ? nthreads : 1)
+    for (int64_t r = rod_lo; r < rod_hi; r++) {
+        /* four_run_powder on the rod: eck(:,1) = (hh, kk, l_start dL + shift3),
+           vi(:,1) = (0, 0, dL), inc = (n, 1, 1) (powder.f90:2305-2319) */
+        const pw_rod *d = rods + r;
+        dgpu_grid g;
+        memset(&g, 0, sizeof(g));
+        for (int c = 0; c < 4; c++) { g.eck[3 * c] = d->hh; g.eck[3 * c + 1] = d->kk; g.eck[3 * c + 2] = d->e31; }
+        g.eck[3 * 1 + 2] = (d->l_start + d->n - 1) * pw->hkl_del[2] + pw->hkl_shift[2];
+        M3(g.vi, 2, 0) = pw->hkl_del[2];
+        g.inc[0] = d->n;
+        g.inc[1] = g.inc[2] = 1;
+        double *acsf = (double *)malloc(sizeof(double) * 2 * d->n);
+        double *dsi = (double *)malloc(sizeof(double) * d->n);
+        int rr = oc_four_run(&c2, &g, &o2, csf + 2 * first[r], acsf, dsi, NULL, 1);
+        if (rr < 0) {
+#pragma omp critical
+            rc = rr;
+        }
+        free(acsf);
+        free(dsi);
+    }
+    if (rc >= 0) {
+        memset(qsp, 0, sizeof(double) * (n_pkt + 1));
+        for (int64_t r = rod_lo; r < rod_hi; r++) {
+            const pw_rod *d = rods + r;
+            for (int32_t i = 1; i <= d->n; i++) {
+                double hkl[3] = {d->hh, d->kk, d->e31 + (i - 1) * pw->hkl_del[2]};
+                double ll = hkl[2];
+                int lreal = fabs((round(ll) - ll) / pw->hkl_del[2]) > 0.51;
+                if (!(pw->l_all || d->hreal || d->kreal || lreal)) continue;
+                double dstar = sqrt(pw_skalpro(hkl, hkl, cr->rten));
+                double q = zpi * dstar;
+                if (!(pw->qmin <= q && q <= pw->qmax + pw->deltaq)) continue;
+                const double *f = csf + 2 * (first[r] + i - 1);
+                double inten = (f[0] * f[0] - f[1] * (-f[1])) * 1.0;           /* DBLE(csf conjg(csf)) */
+                if (pw->pref_type != DGPU_PREF_NONE) inten = inten * pw_preferred(hkl, pw);
+                /* powder_split */
+                int32_t it1 = (int32_t)((q - pw->qmin) / pw->deltaq);
+                double frac1 = 1.0 - ((q - pw->qmin) / pw->deltaq - (int32_t)((q - pw->qmin) / pw->deltaq));
+                double frac2 = ((q - pw->qmin) / pw->deltaq - (int32_t)((q - pw->qmin) / pw->deltaq));
+                if (it1 < 0 || it1 + 1 > n_pkt) continue;
+                qsp[it1] += inten * frac1;
+                qsp[it1 + 1] += inten * frac2;
+            }
+        }
+        if (!op->ano)
+            for (int i = 0; i <= n_pkt; i++) qsp[i] = qsp[i] * 2.0;   /* half-volume correction */
+    }
+    free(csf);
+    free(first);
+    free(rods);
+    return rc;
+}

@@ -59,6 +59,9 @@ int  oc_qval(const dgpu_crystal *cr, const dgpu_grid *grid, const dgpu_opts *op,
              const double *csf, const double *acsf, const double *dsi, const double *rnd, double *out);
 int  oc_calc_hkl(const dgpu_crystal *cr, const dgpu_opts *op, const int32_t *hkl, int64_t nrefl, double scale,
                  double exti, double rlambda, double *icalc, double *sigi, double *phase, int nthreads);
+int  oc_powder_npkt(const dgpu_powder *pw);
+int  oc_powder_complete(const dgpu_crystal *cr, const dgpu_powder *pw, const dgpu_opts *op, int64_t rod_lo,
+                        int64_t rod_hi, double *qsp, int64_t *nrods, int64_t *npoints, int nthreads);
 double oc_time_ref_rows(const dgpu_crystal *cr, const dgpu_grid *grid, int32_t row_lo,
                         int32_t row_hi, int nthreads, int64_t *pairs_out);
 

@@ -49,6 +49,10 @@ def lib():
                                   C.c_double, C.c_double, C.c_double, dp, dp, dp, C.c_int]
         L.oc_qval.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Grid), C.POINTER(_abi.Opts), C.c_int,
                               C.c_int, dp, dp, dp, dp, dp]
+        L.oc_powder_npkt.argtypes = [C.POINTER(_abi.Powder)]
+        L.oc_powder_complete.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Powder), C.POINTER(_abi.Opts),
+                                         C.c_int64, C.c_int64, dp, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                         C.c_int]
         _lib = L
     return _lib
 
@@ -236,3 +240,22 @@ def calc_hkl(cr, opts, hkl, scale=1.0, exti=0.0, rlambda=0.70932, nthreads=0):
     rc = lib().oc_calc_hkl(C.byref(c), C.byref(opts), h.ctypes.data_as(C.POINTER(C.c_int32)), n, float(scale),
                            float(exti), float(rlambda), _d(ic), _d(sg), _d(ph), nthreads)
     return rc, ic, sg, ph
+
+
+def powder_complete(cr, pw, opts, rod_lo=-1, rod_hi=-1, nthreads=0):
+    """powder_complete (powder.f90:1829-2593), literal rod loop: (rc, pow_qsp,
+    rods, rod points evaluated).  rod_lo/rod_hi restrict the evaluation to
+    the rods [rod_lo, rod_hi) of the reference's loop order (a bounded CPU
+    sample); the half-volume doubling is applied either way."""
+    if nthreads <= 0:
+        nthreads = os.cpu_count() or 1
+    p = pw.to_c()
+    n = lib().oc_powder_npkt(C.byref(p))
+    if n < 0:
+        return -1, None, 0, 0
+    qsp = np.zeros(n + 1)
+    c = cr.to_c()
+    nr, npts = C.c_int64(0), C.c_int64(0)
+    rc = lib().oc_powder_complete(C.byref(c), C.byref(p), C.byref(opts), int(rod_lo), int(rod_hi), _d(qsp),
+                                  C.byref(nr), C.byref(npts), nthreads)
+    return rc, qsp, nr.value, npts.value
