@@ -158,6 +158,7 @@ class Powder(C.Structure):
         ("pref_hkl", C.c_double * 3),
         ("pref_g1", C.c_double),
         ("pref_g2", C.c_double),
+        ("slabs", C.c_int32),
     ]
 
 

@@ -69,6 +69,7 @@ class PowderSpec:
     pref_hkl: tuple = (0.0, 0.0, 1.0)
     pref_g1: float = 0.0
     pref_g2: float = 0.0
+    slabs: int = 0                       # device h-slabs, 0 = automatic (no DISCUS counterpart)
 
     @classmethod
     def for_lattice(cls, a, b, c, alpha=90.0, beta=90.0, gamma=90.0, **kw):
@@ -87,6 +88,7 @@ class PowderSpec:
         p.l_all = 1 if self.l_all else 0
         p.pref_type = int(self.pref_type)
         p.pref_g1, p.pref_g2 = float(self.pref_g1), float(self.pref_g2)
+        p.slabs = int(self.slabs)
         return p
 
     @property

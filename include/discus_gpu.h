@@ -356,6 +356,8 @@ typedef struct dgpu_powder {
     double  pref_hkl[3];   /* pow_pref_hkl                                           */
     double  pref_g1;       /* pow_pref_g1                                            */
     double  pref_g2;       /* pow_pref_g2                                            */
+    int32_t slabs;         /* h-slabs the device evaluates, 0 = automatic; no
+                              counterpart in the reference                        */
 } dgpu_powder;
 
 typedef struct dgpu_powder_info {
