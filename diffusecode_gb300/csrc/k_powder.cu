@@ -247,7 +247,7 @@ extern "C" int dgpu_powder_complete(dgpu_ctx *ctx, const dgpu_crystal *cr, const
     DGPU_CUDA(ctx, cudaMemcpyAsync(&nb, d_cnt, sizeof(nb), cudaMemcpyDeviceToHost, ctx->stream));
     DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[9], ctx->stream));
     DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    // half-volume correction (powder.f90:2553)
+    // half-volume correction (powder.f90:2549)
     if (!opts->ano)
         for (int32_t i = 0; i <= n_pkt; i++) pow_qsp[i] *= 2.0;
     if (info) {

@@ -69,7 +69,7 @@ int dgpu_powder_plan(const double rten[9], const dgpu_powder *pw, int ano, int m
     const double ds2 = pw->ds_max * pw->ds_max;
 
     // do_proj "0,1,0, 1,0,0, ddrr" (metric.f90:337-548): the part of b normal
-    // to a, in reciprocal coordinates, then normalised (powder.f90:2036-2047)
+    // to a, in reciprocal coordinates, then normalised (powder.f90:2045-2057)
     double v[3];
     {
         const double e1[3] = {1.0, 0.0, 0.0}, e2[3] = {0.0, 1.0, 0.0};
