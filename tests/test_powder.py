@@ -321,3 +321,20 @@ def test_powder_errors(ctx):
     assert code(pref_type=7) == _abi.DGPU_ERR_ARG
     assert code(pref_type=_abi.PREF_MARCH, pref_g1=0.0) == _abi.DGPU_ERR_ARG
     assert code(ds_max=-1.0) == _abi.DGPU_ERR_ARG
+
+
+@pytest.mark.gpu
+def test_powder_slab_count_invariance(ctx):
+    """The slab partition is a device detail: 1, 3, 8 and one slab per plane
+    give the same pattern (FP64 atomics only reorder the bin sums)."""
+    from diffusecode_gb300 import fourier as FR
+    cr, pw, op, _ = _case("hex-ano-shift")
+    op.engine = _abi.ENGINE_DIRECT
+    out = []
+    for n in (1, 3, 8, 1000):
+        pw.slabs = n
+        q, info = FR.powder_complete(cr, pw, op, ctx=ctx)
+        assert info.nslab <= n
+        out.append(q)
+    for q in out[1:]:
+        np.testing.assert_allclose(q, out[0], rtol=1e-6, atol=1e-9 * out[0].max())
