@@ -290,38 +290,39 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_adjtc(const AdjTcLaunch L)
             for (uint32_t x = qland; x < qnext; x++) mbar_wait_quiet(&qfull[x % AT_QSLOTS], (x / AT_QSLOTS) & 1);
     } else if (warp == AT_MMA_WARP) {
         // ------------------------------------------------------------ MMA issuer
+        // Lane 0 alone waits, issues and commits; the other lanes join it at
+        // the end, so that no warp-wide step sits between two stages.
         // D = 128 atoms x 128 (Re | Im of 64 rows), f32; A and B fp16
-        const uint32_t idesc = (1u << 4) | ((uint32_t)(128 >> 3) << 17) | ((uint32_t)(AT_M >> 4) << 24);
-        const uint32_t idesc_neg = idesc | (1u << 13);
-        uint32_t qn = 0, nrt = 0, nit = 0;
-        bool ok = true, issued = false;
-        for (int64_t item = blockIdx.x; item < L.nitems && ok; item += gridDim.x) {
-            const AdjItem I = L.items[item];
-            const int nks = adj_nks(G, I.kc);
-            if (!__shfl_sync(0xffffffffu, lane == 0 ? mbar_wait(afull, nit & 1, err, 23) : true, 0)) {
-                ok = false;
-                break;
-            }
-            tc_fence_after();
-            for (int rt = I.rt0; rt < I.rt1 && ok; rt++, nrt++) {
-                const int b = (int)(nrt & 1);
-                const uint32_t use = nrt >> 1;
-                if (use > 0 &&
-                    !__shfl_sync(0xffffffffu, lane == 0 ? mbar_wait(&xempty[b], (use - 1) & 1, err, 24) : true, 0)) {
+        bool issued = false;
+        if (lane == 0) {
+            const uint32_t idesc = (1u << 4) | ((uint32_t)(128 >> 3) << 17) | ((uint32_t)(AT_M >> 4) << 24);
+            const uint32_t idesc_neg = idesc | (1u << 13);
+            uint32_t qn = 0, nrt = 0, nit = 0;
+            bool ok = true;
+            for (int64_t item = blockIdx.x; item < L.nitems && ok; item += gridDim.x) {
+                const AdjItem I = L.items[item];
+                const int nks = adj_nks(G, I.kc);
+                if (!mbar_wait(afull, nit & 1, err, 23)) {
                     ok = false;
                     break;
                 }
                 tc_fence_after();
-                const uint32_t dX = tmem + 256u * b, dXc = dX + 128u;
-                for (int s = 0; s < nks; s++, qn++) {
-                    const int slot = (int)(qn % AT_QSLOTS);
-                    if (!__shfl_sync(0xffffffffu,
-                                     lane == 0 ? mbar_wait(&qfull[slot], (qn / AT_QSLOTS) & 1, err, 25) : true, 0)) {
+                for (int rt = I.rt0; rt < I.rt1 && ok; rt++, nrt++) {
+                    const int b = (int)(nrt & 1);
+                    const uint32_t use = nrt >> 1;
+                    if (use > 0 && !mbar_wait(&xempty[b], (use - 1) & 1, err, 24)) {
                         ok = false;
                         break;
                     }
                     tc_fence_after();
-                    if (lane == 0) {
+                    const uint32_t dX = tmem + 256u * b, dXc = dX + 128u;
+                    for (int s = 0; s < nks; s++, qn++) {
+                        const int slot = (int)(qn % AT_QSLOTS);
+                        if (!mbar_wait(&qfull[slot], (qn / AT_QSLOTS) & 1, err, 25)) {
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
                         const uint32_t A = smem_u32(Asm), Bh = smem_u32(Qsm) + slot * AT_Q_BYTES;
                         const uint32_t Bl = Bh + AT_QH_BYTES, b2 = (AT_R / 8) * TC_SBO;
 #pragma unroll
@@ -348,20 +349,20 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_adjtc(const AdjTcLaunch L)
                         mma_commit(&qempty[slot]);
                         issued = true;
                     }
-                    __syncwarp();
+                    if (!ok) break;
+                    mma_commit(&xfull[b]);
                 }
                 if (!ok) break;
-                if (lane == 0) mma_commit(&xfull[b]);
-                __syncwarp();
+                mma_commit(aempty);
+                nit++;
             }
-            if (!ok) break;
-            if (lane == 0) mma_commit(aempty);
-            __syncwarp();
-            nit++;
+            // no MMA of this CTA may still run when TMEM is freed
+            if (issued) {
+                mma_commit(drain);
+                mbar_wait_quiet(drain, 0);
+            }
         }
-        if (lane == 0 && issued) mma_commit(drain);
         __syncwarp();
-        if (__shfl_sync(0xffffffffu, issued ? 1 : 0, 0)) mbar_wait_quiet(drain, 0);
         tc_fence_before();
     } else {
         // ------------------------------------------------------------ drain: one atom per thread

@@ -41,7 +41,7 @@
 // of the tile space (rows with na >= fra are never written).
 //
 // Warp roles (448 threads): warps 0-7 produce operand stages, warp 8 owns
-// TMEM and issues the MMAs (one elected lane), warps 9-12 drain TMEM, warp 13
+// TMEM and issues the MMAs (its lane 0 alone), warps 9-12 drain TMEM, warp 13
 // streams the V operand images into their ring (one lane).  All
 // waits are bounded (globaltimer); a wait that gives up sets an error flag,
 // the CTA stops issuing, waits for its own MMAs, frees TMEM and returns.
@@ -284,8 +284,31 @@ __device__ __forceinline__ void load_pair(AtomPair &r, const TcSrc &P, int64_t k
     r.m = __ldg(reinterpret_cast<const float4 *>(P.ma + k));
 }
 
+// Where the warp's 8 row groups of a tile start (group G0 = 16 mt + q0 at
+// gi0, nb0) and which of them begin a new nb (bit o: group G0 + o): fixed
+// for all stages of a work item.
+struct RowSeg {
+    uint32_t gi0, nb0, bmask;
+};
+
+__device__ __forceinline__ RowSeg row_segments(int mt, int gpn, int warp)
+{
+    const int G0 = mt * (TC_M / 8) + (warp >> 2) * 8;
+    RowSeg r;
+    r.gi0 = (uint32_t)(G0 % gpn);
+    r.nb0 = (uint32_t)(G0 / gpn);
+    r.bmask = 0;
+    int gi = (int)r.gi0;
+#pragma unroll
+    for (int o = 0; o < 8; o++) {
+        if (o > 0 && gi == 0) r.bmask |= 1u << o;
+        if (++gi == gpn) gi = 0;
+    }
+    return r;
+}
+
 template <bool BF>
-__device__ __forceinline__ void gen_rows_stm(int mt, int gpn, const AtomPair &ap, uint8_t *A, int lane, int warp)
+__device__ __forceinline__ void gen_rows_stm(const RowSeg &rs, const AtomPair &ap, uint8_t *A, int lane, int warp)
 {
     const int c = warp & 3;
     const int q0 = (warp >> 2) * 8;
@@ -299,19 +322,8 @@ __device__ __forceinline__ void gen_rows_stm(int mt, int gpn, const AtomPair &ap
 #pragma unroll
     for (int a = 0; a < 2; a++) m2[a] = cmulf(m[a], m[a]);
     // segments of constant nb: bit o of bmask marks group G0 + o as the first
-    // of a segment (one division per stage, no other)
-    const int G0 = mt * (TC_M / 8) + q0;
-    const int gi0 = G0 % gpn;
-    const uint32_t nb0 = (uint32_t)(G0 / gpn);
-    uint32_t bmask = 0;
-    {
-        int gi = gi0;
-#pragma unroll
-        for (int o = 0; o < 8; o++) {
-            if (o > 0 && gi == 0) bmask |= 1u << o;
-            if (++gi == gpn) gi = 0;
-        }
-    }
+    // of a segment
+    const uint32_t gi0 = rs.gi0, nb0 = rs.nb0, bmask = rs.bmask;
     // exact value at group G0 + o: offset 0, or the start of a segment
     auto seed = [&](int o, float2 (&x)[2]) {
         const uint32_t na = (uint32_t)((o == 0 ? gi0 * 8 : 0) + s);
@@ -452,11 +464,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
 
     if (warp < TC_PROD_WARPS && L.vring) {
         // ------------------------------------------------ producers (V images)
-        // Every producer warp runs on its own: its lane 0 waits for the stage
-        // buffer, the warp writes its quarter-chunk of U rows (gen_rows_stm) and
-        // arrives on the stage's full barrier; the phase data of its atoms is
-        // loaded one stage ahead into registers.  No barrier among producers.
-        uint32_t it = 0;
+        // Every producer warp runs on its own: its lanes wait for the stage
+        // buffer (a vote keeps the warp together if a wait gives up), the warp
+        // writes its quarter-chunk of U rows (gen_rows_stm) and lane 0 arrives
+        // on the stage's full barrier; the phase data of its atoms is loaded
+        // one stage ahead into registers.  No barrier among producers.  Stage
+        // index and round are counted, not divided out of `it` (S is a
+        // run-time value, and these loops are latency-bound).
+        uint32_t it = 0, sb = 0, round = 0;  // it = round * S + sb
         bool ok = true;
         const int kq = 8 * (warp & 3) + 2 * (lane & 3);     // the thread's first atom in a stage
         for (int64_t item = blockIdx.x; item < L.nitems && ok; item += gridDim.x) {
@@ -468,23 +483,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
             const int nst = a1 > a0 ? (int)((a1 - a0) / TC_KA) : 0;
             if (nst == 0) continue;
             const TcSrc src = {g.ph0, g.dra, g.drb, g.dac, g.w, g.ma, g.mc};
-            const int gpn = g.fra_p >> 3;
+            const RowSeg rs = row_segments(mt, g.fra_p >> 3, warp);
             AtomPair cur, nxt;
             load_pair(cur, src, a0 + kq);
             for (int st = 0; st < nst; st++, it++) {
                 if (st + 1 < nst) load_pair(nxt, src, a0 + (int64_t)(st + 1) * TC_KA + kq);
-                const int sb = it % S;
-                bool got = true;
-                if (lane == 0 && it >= (uint32_t)S) got = mbar_wait(&empty[sb], ((it / S) - 1) & 1, err, 1);
-                if (!__shfl_sync(0xffffffffu, got, 0)) {
+                const bool got = round == 0 || mbar_wait(&empty[sb], (round - 1) & 1, err, 1);
+                if (!__all_sync(0xffffffffu, got)) {
                     ok = false;
                     break;
                 }
-                gen_rows_stm<BF>(mt, gpn, cur, smem + (size_t)sb * stage_bytes, lane, warp);
+                gen_rows_stm<BF>(rs, cur, smem + (size_t)sb * stage_bytes, lane, warp);
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&full[sb]);   // one arrival per producer warp
                 cur = nxt;
+                if (++sb == (uint32_t)S) {
+                    sb = 0;
+                    round++;
+                }
             }
         }
     } else if (warp < TC_PROD_WARPS) {
@@ -498,7 +515,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
         // (s = lane&7, j = atom quad, u) takes range u for its atom quad.
         const int tid = threadIdx.x;
         const int s = lane & 7, j = (lane >> 3) + 4 * (warp & 1), u = warp >> 1;
-        uint32_t it = 0;
+        uint32_t it = 0, sb = 0, round = 0;   // it = round * S + sb
         bool ok = true;                     // this thread saw no failed wait
         for (int64_t item = blockIdx.x; item < L.nitems; item += gridDim.x) {
             const TcProblem &g = L.probs[L.item_prob[item]];
@@ -525,10 +542,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
             if (nst > 1) stage_atoms(src, aslot + TC_ATOM_SLOT, a0 + TC_KA, tid);
             else cp_async_commit();
             for (int st = 0; st < nst; st++, it++) {
-                const int sb = it % S;
                 cp_async_wait1();           // group st has landed (only the newest may be pending)
                 // one thread waits for the stage buffer, the barrier tells everybody
-                if (tid == 0 && ok && it >= (uint32_t)S) ok = mbar_wait(&empty[sb], ((it / S) - 1) & 1, err, 1);
+                if (tid == 0 && ok && round > 0) ok = mbar_wait(&empty[sb], (round - 1) & 1, err, 1);
                 if (producers_sync(!ok)) break;   // staged for every producer; slot of st-1 and stage sb free
                 if (st + 2 < nst)
                     stage_atoms(src, aslot + ((st + 2) % TC_NSLOT) * TC_ATOM_SLOT, a0 + (int64_t)(st + 2) * TC_KA,
@@ -542,70 +558,75 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&full[sb]);   // one arrival per producer warp
+                if (++sb == (uint32_t)S) {
+                    sb = 0;
+                    round++;
+                }
             }
             cp_async_wait0();
         }
     } else if (warp == TC_MMA_WARP) {
         // ------------------------------------------------------------ MMA issuer
-        const uint32_t fmt = BF ? 1u : 0u;
-        const uint32_t c_acc = tmem;                                  // correction accumulator
-        uint32_t it = 0, nitem = 0, nchunk = 0;
-        bool ok = true, issued = false;
-        for (int64_t item = blockIdx.x; item < L.nitems && ok; item += gridDim.x) {
-            const TcProblem &g = L.probs[L.item_prob[item]];
-            const int N = g.N;
-            int t, ks, nt, mt;
-            decode_item(g, item - g.item0, t, ks, nt, mt);
-            const int64_t a0 = g.ts[t] + (int64_t)ks * g.slice_len;
-            const int64_t a1 = min(g.ts[t + 1], a0 + g.slice_len);
-            const int nst = a1 > a0 ? (int)((a1 - a0) / TC_KA) : 0;
-            if (nst == 0) continue;
-            // D = 128 x 2N, f32; A and B of the operand format
-            const uint32_t idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)((2 * N) >> 3) << 17) |
-                                   ((uint32_t)(TC_M >> 4) << 24);
-            const uint32_t idesc_neg = idesc | (1u << 13);     // negate A: the -Ui products
-            const uint32_t b2off = (uint32_t)(N >> 3) * TC_SBO; // B rows N.. : [Vi; -Vr]
-            // the correction accumulator restarts with this item: previous one drained?
-            if (nitem > 0 &&
-                !__shfl_sync(0xffffffffu, lane == 0 ? mbar_wait(cempty, (nitem - 1) & 1, err, 2) : true, 0)) {
-                ok = false;
-                break;
-            }
-            for (int st0 = 0; st0 < nst && ok; st0 += L.flush, nchunk++) {
-                const int b = (int)(nchunk % L.nbuf);
-                const uint32_t use = nchunk / L.nbuf;
-                if (use > 0 &&
-                    !__shfl_sync(0xffffffffu, lane == 0 ? mbar_wait(&mempty[b], (use - 1) & 1, err, 6) : true, 0)) {
+        // One thread (lane 0) waits, issues and commits; the other lanes of
+        // the warp only join it at the end, so that no warp-wide step sits
+        // between two stages.
+        bool issued = false;
+        if (lane == 0) {
+            const uint32_t fmt = BF ? 1u : 0u;
+            const uint32_t c_acc = tmem;                                  // correction accumulator
+            uint32_t it = 0, nitem = 0, nchunk = 0, s = 0, round = 0;   // it = round * S + s
+            bool ok = true;
+            for (int64_t item = blockIdx.x; item < L.nitems && ok; item += gridDim.x) {
+                const TcProblem &g = L.probs[L.item_prob[item]];
+                const int N = g.N;
+                int t, ks, nt, mt;
+                decode_item(g, item - g.item0, t, ks, nt, mt);
+                const int64_t a0 = g.ts[t] + (int64_t)ks * g.slice_len;
+                const int64_t a1 = min(g.ts[t + 1], a0 + g.slice_len);
+                const int nst = a1 > a0 ? (int)((a1 - a0) / TC_KA) : 0;
+                if (nst == 0) continue;
+                // D = 128 x 2N, f32; A and B of the operand format
+                const uint32_t idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)((2 * N) >> 3) << 17) |
+                                       ((uint32_t)(TC_M >> 4) << 24);
+                const uint32_t idesc_neg = idesc | (1u << 13);     // negate A: the -Ui products
+                const uint32_t b2off = (uint32_t)(N >> 3) * TC_SBO; // B rows N.. : [Vi; -Vr]
+                // the correction accumulator restarts with this item: previous one drained?
+                if (nitem > 0 && !mbar_wait(cempty, (nitem - 1) & 1, err, 2)) {
                     ok = false;
                     break;
                 }
-                tc_fence_after();
-                const uint32_t m_acc = tmem + 2u * NM * (1u + (uint32_t)b);
-                const int st1 = min(nst, st0 + L.flush);
-                for (int st = st0; st < st1; st++, it++) {
-                    const int s = it % S;
-                    bool got = true;
-                    if (lane == 0) {
-                        got = mbar_wait(&full[s], (it / S) & 1, err, 3);
-                        if (got && L.vring) got = mbar_wait(&vfull[it % TC_VSLOTS], (it / TC_VSLOTS) & 1, err, 8);
-                    }
-                    if (!__shfl_sync(0xffffffffu, got, 0)) {
+                for (int st0 = 0; st0 < nst && ok; st0 += L.flush, nchunk++) {
+                    const int b = (int)(nchunk % L.nbuf);
+                    const uint32_t use = nchunk / L.nbuf;
+                    if (use > 0 && !mbar_wait(&mempty[b], (use - 1) & 1, err, 6)) {
                         ok = false;
                         break;
                     }
                     tc_fence_after();
-                    if (lane == 0) {
+                    const uint32_t m_acc = tmem + 2u * NM * (1u + (uint32_t)b);
+                    const int st1 = min(nst, st0 + L.flush);
+                    for (int st = st0; st < st1; st++, it++) {
+                        if (!mbar_wait(&full[s], round & 1, err, 3) ||
+                            (L.vring && !mbar_wait(&vfull[it % TC_VSLOTS], (it / TC_VSLOTS) & 1, err, 8))) {
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
                         const uint32_t A = smem_u32(smem + (size_t)s * stage_bytes);
                         const uint32_t Bh =
                             L.vring ? smem_u32(vring) + (it % TC_VSLOTS) * vbytes : A + 4 * TC_A_BYTES;
-                        const uint32_t Bl = Bh + b_bytes;
+                        // descriptors: the start-address field (addr >> 4, 14 bits) is the
+                        // low field, and every operand lies below 256 KB, so an offset is a
+                        // plain add to the base descriptor
+                        const uint64_t dA = sdesc(A), dB = sdesc(Bh);
+                        const uint64_t bl_off = b_bytes >> 4, b2_off = b2off >> 4;
 #pragma unroll
                         for (int kk = 0; kk < TC_KA / 16; kk++) {
-                            const uint32_t ko = kk * 32;        // 16 atoms = 32 bytes of a row
-                            const uint64_t arh = sdesc(A + 0 * TC_A_BYTES + ko), arl = sdesc(A + 1 * TC_A_BYTES + ko);
-                            const uint64_t aih = sdesc(A + 2 * TC_A_BYTES + ko), ail = sdesc(A + 3 * TC_A_BYTES + ko);
-                            const uint64_t b1h = sdesc(Bh + ko), b2h = sdesc(Bh + b2off + ko);
-                            const uint64_t b1l = sdesc(Bl + ko), b2l = sdesc(Bl + b2off + ko);
+                            const uint64_t ko = (uint64_t)(kk * 32) >> 4;   // 16 atoms = 32 bytes of a row
+                            const uint64_t arh = dA + ko, arl = dA + (TC_A_BYTES >> 4) + ko;
+                            const uint64_t aih = dA + (2 * TC_A_BYTES >> 4) + ko, ail = dA + (3 * TC_A_BYTES >> 4) + ko;
+                            const uint64_t b1h = dB + ko, b2h = dB + b2_off + ko;
+                            const uint64_t b1l = dB + bl_off + ko, b2l = dB + bl_off + b2_off + ko;
                             const uint32_t am = (st > st0 || kk > 0) ? 1u : 0u;   // main restarts per chunk
                             const uint32_t ac = (st > 0 || kk > 0) ? 1u : 0u;     // correction per item
                             // main: (hi,hi)
@@ -620,22 +641,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
                         mma_commit(&empty[s]);
                         if (L.vring) mma_commit(&vempty[it % TC_VSLOTS]);
                         issued = true;
+                        if (++s == (uint32_t)S) {
+                            s = 0;
+                            round++;
+                        }
                     }
-                    __syncwarp();
+                    if (!ok) break;
+                    mma_commit(&mfull[b]);
                 }
                 if (!ok) break;
-                if (lane == 0) mma_commit(&mfull[b]);
-                __syncwarp();
+                mma_commit(cfull);
+                nitem++;
             }
-            if (!ok) break;
-            if (lane == 0) mma_commit(cfull);
-            __syncwarp();
-            nitem++;
+            // make sure no MMA of this CTA is still running before TMEM is freed
+            if (issued) {
+                mma_commit(drain);
+                mbar_wait_quiet(drain, 0);
+            }
         }
-        // make sure no MMA of this CTA is still running before TMEM is freed
-        if (lane == 0 && issued) mma_commit(drain);
         __syncwarp();
-        if (__shfl_sync(0xffffffffu, issued ? 1 : 0, 0)) mbar_wait_quiet(drain, 0);
         tc_fence_before();
     } else if (warp < TC_COPY_WARP) {
         // ------------------------------------------------------------ epilogue
