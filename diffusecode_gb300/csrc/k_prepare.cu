@@ -113,9 +113,9 @@ __global__ void k_type_count(const int32_t *iscat, int64_t n, int32_t nscat, Fol
 
 // Exclusive scan of the per-(type, block) counts into int64 offsets, one CTA.
 // Each type's range starts on a multiple of TYPE_ALIGN atoms; the gap after a
-// type is padding (zero phase, zero weight) so that every 32-atom group of a
-// type is aligned and complete.
-#define TYPE_ALIGN 32
+// type is padding (zero phase, zero weight) so that every 64-atom group of a
+// type (one tensor-core stage) is aligned and complete.
+#define TYPE_ALIGN 64
 __global__ void k_scan_counts(const int32_t *counts, int64_t len, int64_t *offs,
                               int64_t nblk, int32_t nscat, int64_t *type_start)
 {

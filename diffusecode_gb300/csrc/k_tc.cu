@@ -52,7 +52,8 @@
 // chunk c ^ ((r & 7) >> 1).
 #include "dgpu_internal.h"
 
-#define TC_KA 32
+#define TC_KA 32                               // atoms per stage, V generated in the kernel (64-byte rows)
+#define TC_KB 64                               // atoms per stage, V from images (128-byte rows)
 #define TC_M 128
 #define TC_PROD_WARPS 8
 #define TC_MMA_WARP 8
@@ -61,6 +62,7 @@
 #define TC_THREADS (14 * 32)
 #define TC_PROD_THREADS (TC_PROD_WARPS * 32)
 #define TC_A_BYTES (TC_M * TC_KA * 2)          // one A operand (e.g. Ur_hi): 8 KB
+#define TC_B_BYTES (TC_M * TC_KB * 2)          // one A operand on the V-image path: 16 KB
 // phase data of one 32-atom group in shared memory:
 // ph0, d_ra, d_rb, d_ac (u64), w (f32), step factors along ra and ac (float2)
 #define TC_SLOT_W (TC_KA * 32)
@@ -68,12 +70,12 @@
 #define TC_SLOT_MC (TC_SLOT_MA + TC_KA * 8)
 #define TC_ATOM_SLOT (TC_SLOT_MC + TC_KA * 8)
 #define TC_NSLOT 3
-#define TC_VSLOTS 4                            // V ring: images prefetched two stages ahead
+#define TC_VSLOTS 2                            // V ring: 64-atom images, one stage ahead
 #define TC_BAR_BYTES 256
 #define TC_SMEM_BUDGET (220 * 1024)
 #define TC_SMEM_MAX (227 * 1024)                // the opt-in maximum of one CTA
 #ifndef TC_FLUSH_STAGES
-#define TC_FLUSH_STAGES 4                      // 128 atoms per drain of the main accumulator
+#define TC_FLUSH_STAGES 4                      // 128 atoms per drain of the main accumulator (32-atom stages)
 #endif
 #define TC_V_SCALE 4096.0f
 #define TC_UNSCALE (1.0f / 4096.0f)
@@ -260,13 +262,6 @@ __device__ __forceinline__ void split_c2(const float2 (&x)[2], uint32_t &rh, uin
     il = pack2<BF>(x[0].y - hi0, x[1].y - hi1);
 }
 
-// U rows of one stage, stored with stmatrix: warp w generates atom chunk
-// c = w & 3 (atoms 8c..8c+7) of row groups 8 (w >> 2) .. 8 (w >> 2) + 7; lane
-// l owns row l >> 2 of each group and atoms 8c + 2 (l & 3) + {0, 1}, the
-// fragment layout of an 8x8 b16 matrix, so that one stmatrix.x4 stores four
-// row groups of one operand array.  Values step from group to group by
-// exp(2 pi i 8 d_ra) on two chains (even and odd groups, by its square) and
-// restart from the exact phase at every group that begins a new nb.
 // Phase data of the thread's two atoms for one stage, loaded from global
 // memory one stage ahead (16-byte loads: the atoms are consecutive and even).
 struct AtomPair {
@@ -284,36 +279,48 @@ __device__ __forceinline__ void load_pair(AtomPair &r, const TcSrc &P, int64_t k
     r.m = __ldg(reinterpret_cast<const float4 *>(P.ma + k));
 }
 
-// Where the warp's 8 row groups of a tile start (group G0 = 16 mt + q0 at
-// gi0, nb0) and which of them begin a new nb (bit o: group G0 + o): fixed
-// for all stages of a work item.
+// Where the 16 row groups of tile mt start (group G0 = 16 mt at gi0, nb0)
+// and which of them begin a new nb (bit o: group G0 + o): fixed for all
+// stages of a work item.
 struct RowSeg {
     uint32_t gi0, nb0, bmask;
 };
 
-__device__ __forceinline__ RowSeg row_segments(int mt, int gpn, int warp)
+__device__ __forceinline__ RowSeg row_segments(int mt, int gpn)
 {
-    const int G0 = mt * (TC_M / 8) + (warp >> 2) * 8;
+    const int G0 = mt * (TC_M / 8);
     RowSeg r;
     r.gi0 = (uint32_t)(G0 % gpn);
     r.nb0 = (uint32_t)(G0 / gpn);
     r.bmask = 0;
     int gi = (int)r.gi0;
 #pragma unroll
-    for (int o = 0; o < 8; o++) {
+    for (int o = 0; o < TC_M / 8; o++) {
         if (o > 0 && gi == 0) r.bmask |= 1u << o;
         if (++gi == gpn) gi = 0;
     }
     return r;
 }
 
-template <bool BF>
-__device__ __forceinline__ void gen_rows_stm(const RowSeg &rs, const AtomPair &ap, uint8_t *A, int lane, int warp)
+// The thread's stmatrix address within a stage: row (lane & 7) of matrix
+// (lane >> 3), i.e. of row group lane >> 3, in atom chunk warp.
+__device__ __forceinline__ uint32_t stm_offset(int lane, int warp)
 {
-    const int c = warp & 3;
-    const int q0 = (warp >> 2) * 8;
+    return (uint32_t)(lane >> 3) * TC_SBO128 + sw128_off(lane & 7, warp);
+}
+
+// U rows of one 64-atom stage (128-byte rows), stored with stmatrix: warp w
+// generates atom chunk w (atoms 8w..8w+7) of all 16 row groups; lane l owns
+// row l >> 2 of each group and atoms 8w + 2 (l & 3) + {0, 1}, the fragment
+// layout of an 8x8 b16 matrix, so that one stmatrix.x4 stores four row
+// groups of one operand array.  Values step from group to group by
+// exp(2 pi i 8 d_ra) on two chains (even and odd groups, by its square) and
+// restart from the exact phase at every group that begins a new nb.
+
+template <bool BF>
+__device__ __forceinline__ void gen_rows_stm(const RowSeg &rs, const AtomPair &ap, uint32_t adr, int lane)
+{
     const int s = lane >> 2;
-    const uint32_t adr = smem_u32(A) + (uint32_t)(q0 + (lane >> 3)) * TC_SBO + sw_off(lane & 7, c);
     const uint64_t ph0[2] = {ap.ph0.x, ap.ph0.y}, dra[2] = {ap.dra.x, ap.dra.y}, drb[2] = {ap.drb.x, ap.drb.y};
     const float w[2] = {ap.w.x, ap.w.y};
     float2 m[2], m2[2];
@@ -344,17 +351,17 @@ __device__ __forceinline__ void gen_rows_stm(const RowSeg &rs, const AtomPair &a
     }
     uint32_t R[4][4];                  // [operand array][matrix = group within four]
 #pragma unroll
-    for (int p = 0; p < 4; p++) {
+    for (int p = 0; p < TC_M / 16; p++) {
         const int i = (2 * p) & 3;
         split_c2<BF>(e, R[0][i], R[1][i], R[2][i], R[3][i]);
         split_c2<BF>(o, R[0][i + 1], R[1][i + 1], R[2][i + 1], R[3][i + 1]);
         if (p & 1) {
-            const uint32_t base = adr + (uint32_t)(2 * (p - 1)) * TC_SBO;
+            const uint32_t base = adr + (uint32_t)(2 * (p - 1)) * TC_SBO128;
 #pragma unroll
             for (int arr = 0; arr < 4; arr++)
-                stmatrix_x4(base + arr * TC_A_BYTES, R[arr][0], R[arr][1], R[arr][2], R[arr][3]);
+                stmatrix_x4(base + arr * TC_B_BYTES, R[arr][0], R[arr][1], R[arr][2], R[arr][3]);
         }
-        if (p < 3) {
+        if (p < TC_M / 16 - 1) {
             const int ge = 2 * p + 2, go = ge + 1;      // offsets of the next pair
             float2 ne[2], no[2];
             if (starts(ge)) seed(ge, ne);
@@ -413,10 +420,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
     extern __shared__ __align__(1024) uint8_t smem[];
     const int S = L.stages;
     const int NM = L.Nmax;
-    const uint32_t b_bytes = (uint32_t)3 * NM * TC_KA * 2;      // one B operand: 3N rows
+    // atoms per stage: 64 (128-byte rows) with V images, 32 (64-byte rows)
+    // when V is generated in the kernel
+    const int KS = L.vring ? TC_KB : TC_KA;
+    const uint32_t b_bytes = (uint32_t)3 * NM * KS * 2;         // one B operand: 3N rows
     // stages hold U (and V when it is generated in-kernel); with V images,
     // V lives in a ring of TC_VSLOTS slots of 2 * b_bytes after the stages
-    const uint32_t stage_bytes = 4 * TC_A_BYTES + (L.vring ? 0u : 2 * b_bytes);
+    const uint32_t stage_bytes = 4u * TC_M * KS * 2 + (L.vring ? 0u : 2 * b_bytes);
     const uint32_t vbytes = 2 * b_bytes;
     uint8_t *vring = smem + (size_t)S * stage_bytes;
     uint64_t *full = reinterpret_cast<uint64_t *>(vring + (L.vring ? (size_t)TC_VSLOTS * vbytes : 0));
@@ -466,34 +476,35 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
         // ------------------------------------------------ producers (V images)
         // Every producer warp runs on its own: its lanes wait for the stage
         // buffer (a vote keeps the warp together if a wait gives up), the warp
-        // writes its quarter-chunk of U rows (gen_rows_stm) and lane 0 arrives
+        // writes its 8-atom chunk of U rows (gen_rows_stm) and lane 0 arrives
         // on the stage's full barrier; the phase data of its atoms is loaded
         // one stage ahead into registers.  No barrier among producers.  Stage
         // index and round are counted, not divided out of `it` (S is a
         // run-time value, and these loops are latency-bound).
         uint32_t it = 0, sb = 0, round = 0;  // it = round * S + sb
         bool ok = true;
-        const int kq = 8 * (warp & 3) + 2 * (lane & 3);     // the thread's first atom in a stage
+        const int kq = 8 * warp + 2 * (lane & 3);           // the thread's first atom in a stage
+        const uint32_t adr0 = smem_u32(smem) + stm_offset(lane, warp);
         for (int64_t item = blockIdx.x; item < L.nitems && ok; item += gridDim.x) {
             const TcProblem &g = L.probs[L.item_prob[item]];
             int t, ks, nt, mt;
             decode_item(g, item - g.item0, t, ks, nt, mt);
             const int64_t a0 = g.ts[t] + (int64_t)ks * g.slice_len;
             const int64_t a1 = min(g.ts[t + 1], a0 + g.slice_len);
-            const int nst = a1 > a0 ? (int)((a1 - a0) / TC_KA) : 0;
+            const int nst = a1 > a0 ? (int)((a1 - a0) / TC_KB) : 0;
             if (nst == 0) continue;
             const TcSrc src = {g.ph0, g.dra, g.drb, g.dac, g.w, g.ma, g.mc};
-            const RowSeg rs = row_segments(mt, g.fra_p >> 3, warp);
+            const RowSeg rs = row_segments(mt, g.fra_p >> 3);
             AtomPair cur, nxt;
             load_pair(cur, src, a0 + kq);
             for (int st = 0; st < nst; st++, it++) {
-                if (st + 1 < nst) load_pair(nxt, src, a0 + (int64_t)(st + 1) * TC_KA + kq);
+                if (st + 1 < nst) load_pair(nxt, src, a0 + (int64_t)(st + 1) * TC_KB + kq);
                 const bool got = round == 0 || mbar_wait(&empty[sb], (round - 1) & 1, err, 1);
                 if (!__all_sync(0xffffffffu, got)) {
                     ok = false;
                     break;
                 }
-                gen_rows_stm<BF>(rs, cur, smem + (size_t)sb * stage_bytes, lane, warp);
+                gen_rows_stm<BF>(rs, cur, adr0 + sb * stage_bytes, lane);
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&full[sb]);   // one arrival per producer warp
@@ -583,13 +594,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
                 decode_item(g, item - g.item0, t, ks, nt, mt);
                 const int64_t a0 = g.ts[t] + (int64_t)ks * g.slice_len;
                 const int64_t a1 = min(g.ts[t + 1], a0 + g.slice_len);
-                const int nst = a1 > a0 ? (int)((a1 - a0) / TC_KA) : 0;
+                const int nst = a1 > a0 ? (int)((a1 - a0) / KS) : 0;
                 if (nst == 0) continue;
                 // D = 128 x 2N, f32; A and B of the operand format
                 const uint32_t idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)((2 * N) >> 3) << 17) |
                                        ((uint32_t)(TC_M >> 4) << 24);
                 const uint32_t idesc_neg = idesc | (1u << 13);     // negate A: the -Ui products
-                const uint32_t b2off = (uint32_t)(N >> 3) * TC_SBO; // B rows N.. : [Vi; -Vr]
+                // B rows N.. : [Vi; -Vr]
+                const uint32_t b2off = (uint32_t)(N >> 3) * (L.vring ? TC_SBO128 : TC_SBO);
                 // the correction accumulator restarts with this item: previous one drained?
                 if (nitem > 0 && !mbar_wait(cempty, (nitem - 1) & 1, err, 2)) {
                     ok = false;
@@ -617,27 +629,30 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
                             L.vring ? smem_u32(vring) + (it % TC_VSLOTS) * vbytes : A + 4 * TC_A_BYTES;
                         // descriptors: the start-address field (addr >> 4, 14 bits) is the
                         // low field, and every operand lies below 256 KB, so an offset is a
-                        // plain add to the base descriptor
-                        const uint64_t dA = sdesc(A), dB = sdesc(Bh);
+                        // plain add to the base descriptor; a K step of 16 atoms is 32 bytes
                         const uint64_t bl_off = b_bytes >> 4, b2_off = b2off >> 4;
-#pragma unroll
-                        for (int kk = 0; kk < TC_KA / 16; kk++) {
-                            const uint64_t ko = (uint64_t)(kk * 32) >> 4;   // 16 atoms = 32 bytes of a row
-                            const uint64_t arh = dA + ko, arl = dA + (TC_A_BYTES >> 4) + ko;
-                            const uint64_t aih = dA + (2 * TC_A_BYTES >> 4) + ko, ail = dA + (3 * TC_A_BYTES >> 4) + ko;
-                            const uint64_t b1h = dB + ko, b2h = dB + b2_off + ko;
-                            const uint64_t b1l = dB + bl_off + ko, b2l = dB + bl_off + b2_off + ko;
-                            const uint32_t am = (st > st0 || kk > 0) ? 1u : 0u;   // main restarts per chunk
-                            const uint32_t ac = (st > 0 || kk > 0) ? 1u : 0u;     // correction per item
-                            // main: (hi,hi)
-                            mma_f16(m_acc, arh, b1h, idesc, am);
-                            mma_f16(m_acc, aih, b2h, idesc_neg, 1u);
-                            // corrections: (hi,lo) and (lo,hi)
-                            mma_f16(c_acc, arh, b1l, idesc, ac);
-                            mma_f16(c_acc, aih, b2l, idesc_neg, 1u);
-                            mma_f16(c_acc, arl, b1h, idesc, 1u);
-                            mma_f16(c_acc, ail, b2h, idesc_neg, 1u);
-                        }
+                        auto issue = [&](uint64_t dA, uint64_t dB, uint32_t a_bytes, int nk) {
+#pragma unroll 4
+                            for (int kk = 0; kk < nk; kk++) {
+                                const uint64_t ko = (uint64_t)kk * 2;
+                                const uint64_t arh = dA + ko, arl = dA + (a_bytes >> 4) + ko;
+                                const uint64_t aih = dA + (2 * a_bytes >> 4) + ko, ail = dA + (3 * a_bytes >> 4) + ko;
+                                const uint64_t b1h = dB + ko, b2h = dB + b2_off + ko;
+                                const uint64_t b1l = dB + bl_off + ko, b2l = dB + bl_off + b2_off + ko;
+                                const uint32_t am = (st > st0 || kk > 0) ? 1u : 0u;   // main restarts per chunk
+                                const uint32_t ac = (st > 0 || kk > 0) ? 1u : 0u;     // correction per item
+                                // main: (hi,hi)
+                                mma_f16(m_acc, arh, b1h, idesc, am);
+                                mma_f16(m_acc, aih, b2h, idesc_neg, 1u);
+                                // corrections: (hi,lo) and (lo,hi)
+                                mma_f16(c_acc, arh, b1l, idesc, ac);
+                                mma_f16(c_acc, aih, b2l, idesc_neg, 1u);
+                                mma_f16(c_acc, arl, b1h, idesc, 1u);
+                                mma_f16(c_acc, ail, b2h, idesc_neg, 1u);
+                            }
+                        };
+                        if (L.vring) issue(sdesc128(A), sdesc128(Bh), TC_B_BYTES, TC_KB / 16);
+                        else issue(sdesc(A), sdesc(Bh), TC_A_BYTES, TC_KA / 16);
                         mma_commit(&empty[s]);
                         if (L.vring) mma_commit(&vempty[it % TC_VSLOTS]);
                         issued = true;
@@ -677,7 +692,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
             decode_item(g, item - g.item0, t, ks, nt, mt);
             const int64_t a0 = g.ts[t] + (int64_t)ks * g.slice_len;
             const int64_t a1 = min(g.ts[t + 1], a0 + g.slice_len);
-            const int nst = a1 > a0 ? (int)((a1 - a0) / TC_KA) : 0;
+            const int nst = a1 > a0 ? (int)((a1 - a0) / KS) : 0;
             const int64_t rg = (int64_t)mt * TC_M + r;
             const bool rv = rg < g.nrows_p && (int)(rg % g.fra_p) < g.fra;
             const int64_t nrp = g.nrows_p;
@@ -784,8 +799,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
                 decode_item(g, item - g.item0, t, ks, nt, mt);
                 const int64_t a0 = g.ts[t] + (int64_t)ks * g.slice_len;
                 const int64_t a1 = min(g.ts[t + 1], a0 + g.slice_len);
-                const int nst = a1 > a0 ? (int)((a1 - a0) / TC_KA) : 0;
-                const int64_t g0 = a0 / TC_KA;
+                const int nst = a1 > a0 ? (int)((a1 - a0) / TC_KB) : 0;
+                const int64_t g0 = a0 / TC_KB;
                 for (int y = 0; y < nst; y++, x++) {
                     const int v = (int)(x % TC_VSLOTS);
                     if (x >= TC_VSLOTS) {
@@ -835,35 +850,34 @@ __global__ void k_tc_mult(const uint64_t *__restrict__ du, const uint64_t *__res
     }
 }
 
-// V images of one problem: for every 32-atom group gi and column tile nt the
-// B rows [Vr; Vi; -Vr] of a stage, hi then lo, exactly as the producers lay
-// them out in shared memory (384 N bytes).  Each value is evaluated from its
-// exact 64-bit phase; grid: one block per (gi, nt).  The image is built in
-// shared memory (N * 384 bytes, at most 48 KB) and written out in 16-byte
-// coalesced stores.
+// V operand images: for every (64-atom group gi, column tile nt) the B rows
+// [Vr; Vi; -Vr] (hi operand, then lo) of the tile's N columns, in the
+// 128-byte-swizzled K-major layout the MMAs read (768 N bytes).  Each value is
+// evaluated from its exact 64-bit phase; grid: one block per (gi, nt).  The
+// image is built in shared memory and written out in 16-byte coalesced stores.
 template <bool BF>
 __global__ void __launch_bounds__(256) k_tc_vgen(const uint64_t *__restrict__ dac, int N, int n_tiles,
                                                   uint8_t *__restrict__ vimg)
 {
-    extern __shared__ __align__(16) uint8_t vs[];
+    extern __shared__ __align__(1024) uint8_t vs[];
     const int64_t gi = blockIdx.x / n_tiles;
     const int nt = (int)(blockIdx.x % n_tiles);
-    const uint32_t vbytes = (uint32_t)N * 384u;
+    const uint32_t vbytes = (uint32_t)N * 768u;
     uint8_t *img = vs;                 // built in shared memory, then written out coalesced
-    const uint32_t half = vbytes / 2, blk = (uint32_t)(N >> 3) * TC_SBO;
-    for (int u = threadIdx.x; u < N * 8; u += blockDim.x) {
+    const uint32_t half = vbytes / 2, blk = (uint32_t)(N >> 3) * TC_SBO128;
+    for (int u = threadIdx.x; u < N * (TC_KB / 4); u += blockDim.x) {
         const int c = u % N, jq = u / N;                       // column, atom quad
         const uint32_t nc = (uint32_t)(nt * N + c);
         float2 x[4];
 #pragma unroll
         for (int a = 0; a < 4; a++) {
-            const float2 p = phasor_fast((uint64_t)nc * dac[gi * TC_KA + 4 * jq + a]);
+            const float2 p = phasor_fast((uint64_t)nc * dac[gi * TC_KB + 4 * jq + a]);
             x[a] = make_float2(p.x * TC_V_SCALE, p.y * TC_V_SCALE);
         }
         uint2 rh, rl, ih, il;
         split4<BF>(x[0].x, x[1].x, x[2].x, x[3].x, rh, rl);
         split4<BF>(x[0].y, x[1].y, x[2].y, x[3].y, ih, il);
-        uint8_t *d = img + sw_off(c, jq >> 1) + (jq & 1) * 8;
+        uint8_t *d = img + sw128_off(c, jq >> 1) + (jq & 1) * 8;
         *reinterpret_cast<uint2 *>(d) = rh;
         *reinterpret_cast<uint2 *>(d + half) = rl;
         *reinterpret_cast<uint2 *>(d + blk) = ih;
@@ -951,7 +965,7 @@ static void tc_problem(dgpu_ctx *ctx, const TcInput &in, const dgpu_opts *op, in
         if (nsl > 1 && dgpu_cdiv(maxn, nsl) < 2048) nsl = dgpu_cdiv(maxn, 2048);
     }
     if (nsl < 1) nsl = 1;
-    g.slice_len = dgpu_cdiv(dgpu_cdiv(maxn > 0 ? maxn : 1, nsl), TC_KA) * TC_KA;
+    g.slice_len = dgpu_cdiv(dgpu_cdiv(maxn > 0 ? maxn : 1, nsl), TC_KB) * TC_KB;   // whole stages of either path
     g.nslice = (int32_t)dgpu_cdiv(maxn > 0 ? maxn : 1, g.slice_len);
     g.nitems = tiles * g.nslice;
     const uint64_t *dd[3] = {in.du, in.dv, in.dw};
@@ -1007,18 +1021,18 @@ int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *o
         for (int64_t i = 0; i < plan.probs[p].nitems; i++) plan.item_prob[plan.probs[p].item0 + i] = p;
     DGPU_CUDA(ctx, part.ensure((size_t)(elems > 0 ? elems : 1) * sizeof(float2)));
     for (int p = 0; p < nprob; p++) plan.probs[p].part = part.as<float2>() + plan.part_off[p];
-    // V images: one per (32-atom group, column tile) of every problem
+    // V images: one per (64-atom group, column tile) of every problem
     std::vector<int64_t> voff(nprob, 0);
     int64_t vtot = 0;
     for (int p = 0; p < nprob; p++) {
         voff[p] = vtot;
-        vtot += in[p].ts[in[p].ntype] / TC_KA * plan.probs[p].n_tiles * (int64_t)N * 384;
+        vtot += in[p].ts[in[p].ntype] / TC_KB * plan.probs[p].n_tiles * (int64_t)N * 768;
     }
     // images pay when every one is re-read by several row tiles (a 3D grid);
     // thin planes with one or two row tiles generate V in the kernel
     double reads = 0.0, imgs = 0.0;
     for (int p = 0; p < nprob; p++) {
-        const double ni = (double)(in[p].ts[in[p].ntype] / TC_KA) * plan.probs[p].n_tiles;
+        const double ni = (double)(in[p].ts[in[p].ntype] / TC_KB) * plan.probs[p].n_tiles;
         imgs += ni;
         reads += ni * plan.probs[p].m_tiles;
     }
@@ -1044,20 +1058,24 @@ int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *o
     // TMEM: correction (2N) + main x nbuf (2N each) [+ running sum (2N)]
     L.nbuf = 2 * N * 3 <= 512 ? 2 : 1;
     L.tsum = 2 * N * (2 + L.nbuf) <= 512 ? 1 : 0;
-    L.flush = op->tc_flush > 0 ? (int32_t)dgpu_cdiv(op->tc_flush, TC_KA) : TC_FLUSH_STAGES;
     L.bf16 = op->split == DGPU_SPLIT_BF16;
-    const uint32_t vbytes = 2u * 3u * N * TC_KA * 2;
-    // V images stream through a ring when it leaves room for two U stages; the
-    // producers of that path hold their atoms' phase data in registers, so it
-    // needs no atom slots and may use the whole shared memory of the SM
-    const int64_t room = (int64_t)TC_SMEM_MAX - TC_BAR_BYTES - (int64_t)TC_VSLOTS * vbytes;
-    if (plan.vimg && room < 2 * 4 * TC_A_BYTES) plan.vimg = false;
+    // V images stream through a ring of 64-atom slots when it leaves room for
+    // two U stages; the producers of that path hold their atoms' phase data in
+    // registers, so it needs no atom slots and may use the whole shared
+    // memory of the SM
+    const uint32_t vbytes_img = 2u * 3u * N * TC_KB * 2;
+    const int64_t room = (int64_t)TC_SMEM_MAX - TC_BAR_BYTES - (int64_t)TC_VSLOTS * vbytes_img;
+    if (plan.vimg && room < 2 * 4 * TC_B_BYTES) plan.vimg = false;
     if (!plan.vimg)
         for (TcProblem &g : plan.probs) g.vimg = nullptr;
     L.vring = plan.vimg ? 1 : 0;
+    const int ks_atoms = L.vring ? TC_KB : TC_KA;                 // atoms per stage
+    L.flush = op->tc_flush > 0 ? (int32_t)dgpu_cdiv(op->tc_flush, ks_atoms)
+                               : TC_FLUSH_STAGES * TC_KA / ks_atoms;   // 128 atoms
+    const uint32_t vbytes = 2u * 3u * N * ks_atoms * 2;
     const uint32_t bar_bytes = TC_BAR_BYTES + (L.vring ? 0u : (uint32_t)(TC_NSLOT * TC_ATOM_SLOT));
     const int64_t budget = L.vring ? TC_SMEM_MAX : TC_SMEM_BUDGET;
-    const uint32_t stage_bytes = 4 * TC_A_BYTES + (L.vring ? 0u : vbytes);
+    const uint32_t stage_bytes = 4u * TC_M * ks_atoms * 2 + (L.vring ? 0u : vbytes);
     const int stages = (int)((budget - bar_bytes - (L.vring ? (int64_t)TC_VSLOTS * vbytes : 0)) / stage_bytes);
     L.stages = stages > 4 ? 4 : stages;
     L.tmem_cols = pow2_cols(2 * N * (1 + L.nbuf + L.tsum));
@@ -1067,6 +1085,10 @@ int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *o
     if (!attr_set) {
         DGPU_CUDA(ctx, cudaFuncSetAttribute(k_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
         DGPU_CUDA(ctx, cudaFuncSetAttribute(k_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+        DGPU_CUDA(ctx, cudaFuncSetAttribute(k_tc_vgen<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            227 * 1024));
+        DGPU_CUDA(ctx, cudaFuncSetAttribute(k_tc_vgen<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            227 * 1024));
         attr_set = true;
     }
     DGPU_CUDA(ctx, ctx->flag.ensure(64));
@@ -1080,13 +1102,13 @@ int dgpu_tc_launch(dgpu_ctx *ctx, const TcPlan &plan, bool timed)
     if (plan.L.nitems < 1) return DGPU_OK;
     if (plan.vimg)
         for (const TcProblem &g : plan.probs) {
-            const int64_t nimg = (g.ts[g.ntype] / TC_KA) * g.n_tiles;
+            const int64_t nimg = (g.ts[g.ntype] / TC_KB) * g.n_tiles;
             if (nimg < 1) continue;
             if (plan.L.bf16)
-                k_tc_vgen<true><<<(unsigned)nimg, 256, (size_t)g.N * 384, ctx->stream>>>(g.dac, g.N, g.n_tiles,
+                k_tc_vgen<true><<<(unsigned)nimg, 256, (size_t)g.N * 768, ctx->stream>>>(g.dac, g.N, g.n_tiles,
                                                                                           g.vimg);
             else
-                k_tc_vgen<false><<<(unsigned)nimg, 256, (size_t)g.N * 384, ctx->stream>>>(g.dac, g.N, g.n_tiles,
+                k_tc_vgen<false><<<(unsigned)nimg, 256, (size_t)g.N * 768, ctx->stream>>>(g.dac, g.N, g.n_tiles,
                                                                                            g.vimg);
         }
     const int grid = (int)(plan.L.nitems < ctx->nsm ? plan.L.nitems : ctx->nsm);

@@ -131,6 +131,15 @@ __device__ __forceinline__ uint32_t sw_off(int r, int chunk)
     return (uint32_t)((r >> 3) * TC_SBO + (r & 7) * 64 + ((chunk ^ ((r & 7) >> 1)) << 4));
 }
 
+// K-major operand with the 128-byte swizzle: rows of 128 bytes (64 16-bit
+// values), 8-row groups of 1024 B, the 16-byte chunk c of row r stored at
+// chunk c ^ (r & 7).  The buffer must start on a 1024-byte boundary.
+#define TC_SBO128 1024
+__device__ __forceinline__ uint32_t sw128_off(int r, int chunk)
+{
+    return (uint32_t)((r >> 3) * TC_SBO128 + (r & 7) * 128 + ((chunk ^ (r & 7)) << 4));
+}
+
 __device__ __forceinline__ uint64_t sdesc(uint32_t saddr)
 {
     uint64_t d = 0;
@@ -139,6 +148,18 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr)
     d |= (uint64_t)((TC_SBO >> 4) & 0x3FFFu) << 32;
     d |= (uint64_t)1 << 46;                      // descriptor version of the sm_100 family
     d |= (uint64_t)4 << 61;                      // 64-byte swizzle
+    return d;
+}
+
+// descriptor of the 128-byte-swizzled K-major layout (layout type 2)
+__device__ __forceinline__ uint64_t sdesc128(uint32_t saddr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)1 << 16;                      // leading byte offset: unused for swizzled K-major
+    d |= (uint64_t)((TC_SBO128 >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;                      // descriptor version of the sm_100 family
+    d |= (uint64_t)2 << 61;                      // 128-byte swizzle
     return d;
 }
 
