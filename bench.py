@@ -38,8 +38,8 @@ METRIC = "G atom.hkl pairs/s for |F|^2"
 # reductions; the tensor-core engine adds its step-factor and V-image kernels
 LAUNCHES_PER_RUN = {1: 10, 2: 12}
 # DRAM bytes per atom of one tensor-core type-sum launch (ncu capture on the
-# 108 000-atom, 61^3 alloy: 99.85 MB read + written)
-TC_DRAM_BYTES_PER_ATOM = (87.490816e6 + 12.354560e6) / 108000
+# 108 000-atom, 61^3 alloy: 98.30 MB read + written)
+TC_DRAM_BYTES_PER_ATOM = (87.424000e6 + 10.878464e6) / 108000
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
