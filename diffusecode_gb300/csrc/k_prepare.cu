@@ -28,27 +28,33 @@ __device__ __forceinline__ int64_t inc22(double x)
     return (int64_t)llround(__dmul_rn(4194304.0, fr));
 }
 
-// frac(a.x) as a 64-bit fixed-point turn, from error-free FP64 products
+// frac(a x) as a 64-bit fixed-point turn, exactly (truncated to 2^-64): the
+// two 53-bit significands are multiplied as integers (106-bit product) and
+// shifted by the exponents; a negative product is negated modulo 2^64.
+// Integer arithmetic, because this part's FP64 rate is low.
+__device__ __forceinline__ uint64_t fx64_mul(double a, double x)
+{
+    const uint64_t ba = (uint64_t)__double_as_longlong(a), bx = (uint64_t)__double_as_longlong(x);
+    const int ea = (int)((ba >> 52) & 0x7FF), ex = (int)((bx >> 52) & 0x7FF);
+    const uint64_t ma = (ba & 0xFFFFFFFFFFFFFull) | (ea ? (1ull << 52) : 0ull);
+    const uint64_t mx = (bx & 0xFFFFFFFFFFFFFull) | (ex ? (1ull << 52) : 0ull);
+    // a x = ma mx 2^(e_a + e_x); the fixed point wants that times 2^64, modulo 2^64
+    const int s = (ea ? ea - 1075 : -1074) + (ex ? ex - 1075 : -1074) + 64;
+    const uint64_t lo = ma * mx, hi = __umul64hi(ma, mx);
+    uint64_t r;
+    if (s >= 64) r = 0;
+    else if (s >= 0) r = lo << s;
+    else if (s > -64) r = (lo >> -s) | (hi << (64 + s));
+    else if (s > -128) r = hi >> (-s - 64);
+    else r = 0;
+    return ((ba ^ bx) >> 63) ? 0ull - r : r;
+}
+
+// frac(a.x) as a 64-bit fixed-point turn (the sum of the three exact terms
+// modulo one turn)
 __device__ __forceinline__ uint64_t frac64_dot(const double *a, double x0, double x1, double x2)
 {
-    double p0 = __dmul_rn(a[0], x0), e0 = fma(a[0], x0, -p0);
-    double p1 = __dmul_rn(a[1], x1), e1 = fma(a[1], x1, -p1);
-    double p2 = __dmul_rn(a[2], x2), e2 = fma(a[2], x2, -p2);
-    double s = __dadd_rn(p0, p1);
-    double z = __dsub_rn(s, p0);
-    double es = __dadd_rn(__dsub_rn(p0, __dsub_rn(s, z)), __dsub_rn(p1, z));
-    double t = __dadd_rn(s, p2);
-    z = __dsub_rn(t, s);
-    double et = __dadd_rn(__dsub_rn(s, __dsub_rn(t, z)), __dsub_rn(p2, z));
-    double hi = __dsub_rn(t, floor(t));
-    double lo = __dadd_rn(__dadd_rn(__dadd_rn(es, et), __dadd_rn(e0, e1)), e2);
-    double v = __dadd_rn(hi, lo);
-    double a32 = __dmul_rn(v, 4294967296.0);
-    double ah = floor(a32);
-    double rem = __dsub_rn(a32, ah);
-    uint64_t h32 = (uint64_t)(int64_t)ah;
-    uint64_t l32 = (uint64_t)llrint(__dmul_rn(rem, 4294967296.0));
-    return (h32 << 32) + l32;
+    return fx64_mul(a[0], x0) + fx64_mul(a[1], x1) + fx64_mul(a[2], x2);
 }
 
 struct PhaseOut {
