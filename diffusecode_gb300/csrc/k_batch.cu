@@ -8,12 +8,18 @@
 // on the same stream.  The whole sequence -- host-to-device copies from pinned
 // staging, kernels, device-to-host copies -- is captured once per batch shape
 // into a CUDA graph and replayed on later calls (new coordinates, same
-// shapes), so a population step costs one graph launch.
+// shapes), so a population step costs one graph launch.  The members' small
+// kernels are spread over BATCH_STREAMS side streams in the capture (fork
+// before the per-member stages, join before the tensor-core launch and before
+// the final copies), so the graph runs members side by side instead of one
+// small kernel after another.
 #include <stdlib.h>
 
 #include <vector>
 
 #include "dgpu_internal.h"
+
+#define BATCH_STREAMS 8
 
 namespace {
 
@@ -68,10 +74,19 @@ struct BatchState {
     DevBuf d_vimg;                         // tensor-core V images
     DevBuf d_adj_items, d_adj_img;         // tensor-core adjoint: items (+ Q scales), Q images
     HostPinned h_pos, h_isc, h_aocc, h_it, h_wt, h_dsi, h_chi, h_grad;
+    cudaStream_t aux[BATCH_STREAMS] = {};                          // side streams of the capture
+    cudaEvent_t fork[2] = {}, join[2][BATCH_STREAMS] = {};
     ~BatchState()
     {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
+        for (int k = 0; k < BATCH_STREAMS; k++) {
+            if (aux[k]) cudaStreamDestroy(aux[k]);
+            for (int f = 0; f < 2; f++)
+                if (join[f][k]) cudaEventDestroy(join[f][k]);
+        }
+        for (int f = 0; f < 2; f++)
+            if (fork[f]) cudaEventDestroy(fork[f]);
         DevBuf *b[] = {&d_pos, &d_isc, &d_aocc, &d_ph0, &d_du, &d_dv, &d_dw, &d_w, &d_idx, &d_cnt, &d_offs,
                        &d_tsd, &d_istl, &d_cfact, &d_csf, &d_dsi, &d_g, &d_q, &d_chi, &d_grad, &d_coef, &d_fs,
                        &d_it, &d_wt, &part, &desc};
@@ -89,7 +104,33 @@ void dgpu_batch_free(dgpu_ctx *ctx)
     ctx->batch = nullptr;
 }
 
-// Everything one population step runs, in stream order (capturable).
+// Restores the context's stream when a member stage leaves early.
+struct StreamSwap {
+    dgpu_ctx *ctx;
+    cudaStream_t main;
+    ~StreamSwap() { ctx->stream = main; }
+};
+
+// fork: every side stream waits for what the main stream enqueued so far
+static int batch_fork(dgpu_ctx *ctx, BatchState &B, int f, cudaStream_t st)
+{
+    DGPU_CUDA(ctx, cudaEventRecord(B.fork[f], st));
+    for (int k = 0; k < BATCH_STREAMS; k++) DGPU_CUDA(ctx, cudaStreamWaitEvent(B.aux[k], B.fork[f], 0));
+    return DGPU_OK;
+}
+
+// join: the main stream waits for everything the side streams enqueued
+static int batch_join(dgpu_ctx *ctx, BatchState &B, int f, cudaStream_t st)
+{
+    for (int k = 0; k < BATCH_STREAMS; k++) {
+        DGPU_CUDA(ctx, cudaEventRecord(B.join[f][k], B.aux[k]));
+        DGPU_CUDA(ctx, cudaStreamWaitEvent(st, B.join[f][k], 0));
+    }
+    return DGPU_OK;
+}
+
+// Everything one population step runs, in stream order (capturable); member
+// c's stages run on side stream c % BATCH_STREAMS.
 static int batch_enqueue(dgpu_ctx *ctx, BatchState &B, const dgpu_opts *op)
 {
     cudaStream_t st = ctx->stream;
@@ -112,9 +153,13 @@ static int batch_enqueue(dgpu_ctx *ctx, BatchState &B, const dgpu_opts *op)
     DGPU_CUDA(ctx, cudaMemsetAsync(B.d_idx.p, 0xFF, pad * 4, st));
     DGPU_CUDA(ctx, cudaMemsetAsync(flag, 0, sizeof(int32_t), st));
     DGPU_CUDA(ctx, cudaMemsetAsync(ctx->flag.as<int32_t>() + 10, 0, sizeof(int32_t), st));   // adjoint
+    int rc = batch_fork(ctx, B, 0, st);
+    if (rc) return rc;
     for (size_t c = 0; c < B.mem.size(); c++) {
         Member &m = B.mem[c];
-        int rc = dgpu_prepare_async(ctx, B.d_pos.as<double>() + 3 * m.abase, B.d_isc.as<int32_t>() + m.abase,
+        StreamSwap sw{ctx, st};
+        ctx->stream = B.aux[c % BATCH_STREAMS];
+        rc = dgpu_prepare_async(ctx, B.d_pos.as<double>() + 3 * m.abase, B.d_isc.as<int32_t>() + m.abase,
                                     B.has_occ ? B.d_aocc.as<float>() + m.abase : nullptr, m.natoms, m.nscat, m.geo,
                                     B.d_cnt.as<int32_t>() + m.cnt_off, B.d_offs.as<int64_t>() + m.offs_off,
                                     B.d_tsd.as<int64_t>() + m.tsd_off, B.d_ph0.as<uint64_t>() + m.pbase,
@@ -129,13 +174,19 @@ static int batch_enqueue(dgpu_ctx *ctx, BatchState &B, const dgpu_opts *op)
                                 B.d_cfact.as<double2>() + m.cfact_off);
         if (rc) return rc;
     }
-    int rc = dgpu_tc_mult_async(ctx, B.d_du.as<uint64_t>(), B.d_dv.as<uint64_t>(), B.d_dw.as<uint64_t>(),
+    rc = batch_join(ctx, B, 0, st);
+    if (rc) return rc;
+    rc = dgpu_tc_mult_async(ctx, B.d_du.as<uint64_t>(), B.d_dv.as<uint64_t>(), B.d_dw.as<uint64_t>(),
                                 B.tot_pad, B.tot_pad, B.d_mult.as<float2>());
     if (rc) return rc;
     rc = dgpu_tc_launch(ctx, B.plan);
     if (rc) return rc;
+    rc = batch_fork(ctx, B, 1, st);
+    if (rc) return rc;
     for (size_t c = 0; c < B.mem.size(); c++) {
         Member &m = B.mem[c];
+        StreamSwap sw{ctx, st};
+        ctx->stream = B.aux[c % BATCH_STREAMS];
         const FormSpec *fs = B.d_fs.as<FormSpec>() + c;
         PartRef pr;
         dgpu_tc_partref(B.plan.probs[c], B.part.as<float2>() + B.plan.part_off[c], pr);
@@ -167,9 +218,11 @@ static int batch_enqueue(dgpu_ctx *ctx, BatchState &B, const dgpu_opts *op)
                                     gpos + 3 * m.natoms, ctx->flag.as<int32_t>() + 10);
             if (rc) return rc;
             DGPU_CUDA(ctx, cudaMemcpyAsync((double *)B.h_chi.p + c, B.d_chi.as<double>() + m.chi_off + 512,
-                                           sizeof(double), cudaMemcpyDeviceToHost, st));
+                                           sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
         }
     }
+    rc = batch_join(ctx, B, 1, st);
+    if (rc) return rc;
     DGPU_CUDA(ctx, cudaMemcpyAsync(B.h_dsi.p, B.d_dsi.p, B.tot_np * sizeof(double), cudaMemcpyDeviceToHost, st));
     if (B.targets)
         DGPU_CUDA(ctx, cudaMemcpyAsync(B.h_grad.p, B.d_grad.p, B.tot_atoms * 4 * sizeof(double),
@@ -180,6 +233,11 @@ static int batch_enqueue(dgpu_ctx *ctx, BatchState &B, const dgpu_opts *op)
 static int batch_build(dgpu_ctx *ctx, BatchState &B, int32_t nc, const dgpu_crystal *crs, const dgpu_grid *grids,
                        const dgpu_opts *op)
 {
+    for (int k = 0; k < BATCH_STREAMS; k++) {
+        DGPU_CUDA(ctx, cudaStreamCreateWithFlags(&B.aux[k], cudaStreamNonBlocking));
+        for (int f = 0; f < 2; f++) DGPU_CUDA(ctx, cudaEventCreateWithFlags(&B.join[f][k], cudaEventDisableTiming));
+    }
+    for (int f = 0; f < 2; f++) DGPU_CUDA(ctx, cudaEventCreateWithFlags(&B.fork[f], cudaEventDisableTiming));
     B.mem.assign(nc, Member());
     int64_t abase = 0, pbase = 0, np_tot = 0, istl = 0, cf = 0, q = 0, cnt = 0, tsd = 0;
     for (int c = 0; c < nc; c++) {
