@@ -380,6 +380,8 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_adjtc(const AdjTcLaunch L)
             const uint64_t p0 = valid ? L.ph0[a] : 0ull, d0 = valid ? L.dra[a] : 0ull, d1 = valid ? L.drb[a] : 0ull;
             const float2 step = valid ? phasor_accurate(d0) : make_float2(1.f, 0.f);
             float t0r = 0.f, t0i = 0.f, tra = 0.f, trb = 0.f, tac = 0.f;
+            // (na, nb) of the first row of each row tile, advanced by AT_R rows per tile
+            int64_t na_t = ((int64_t)I.rt0 * AT_R) % G.fra, nb_t = ((int64_t)I.rt0 * AT_R) / G.fra;
             for (int rt = I.rt0; rt < I.rt1; rt++, nrt++) {
                 const int b = (int)(nrt & 1);
                 if (!__shfl_sync(0xffffffffu, lane == 0 ? mbar_wait(&xfull[b], (nrt >> 1) & 1, err, 26) : true, 0)) {
@@ -388,7 +390,12 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_adjtc(const AdjTcLaunch L)
                 }
                 tc_fence_after();
                 const int64_t rg0 = (int64_t)rt * AT_R;
-                uint32_t na = (uint32_t)(rg0 % G.fra), nb = (uint32_t)(rg0 / G.fra);
+                uint32_t na = (uint32_t)na_t, nb = (uint32_t)nb_t;
+                na_t += AT_R;
+                while (na_t >= G.fra) {
+                    na_t -= G.fra;
+                    nb_t++;
+                }
                 float2 u = valid ? phasor_fast(p0 + (uint64_t)na * d0 + (uint64_t)nb * d1) : make_float2(0.f, 0.f);
                 const uint32_t tb = tmem + lane_off + 256u * b;
                 for (int c16 = 0; c16 < AT_R / 16; c16++) {
