@@ -136,7 +136,7 @@ extern "C" int dgpu_powder_complete(dgpu_ctx *ctx, const dgpu_crystal *cr, const
     char msg[256] = {0};
     const int64_t max_points = (int64_t)1 << 26;
     if (pw->slabs < 0) return dgpu_set_error(ctx, DGPU_ERR_ARG, "slabs=%d", pw->slabs);
-    int rc = dgpu_powder_plan(cr->rten, pw, opts->ano, pw->slabs ? pw->slabs : 8, max_points, plan, msg,
+    int rc = dgpu_powder_plan(cr->rten, pw, opts->ano, pw->slabs ? pw->slabs : 1, max_points, plan, msg,
                               sizeof msg);
     if (rc) return dgpu_set_error(ctx, rc, "%s", msg);
     const int32_t n_pkt = plan.n_pkt;
