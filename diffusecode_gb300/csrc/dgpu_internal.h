@@ -81,6 +81,7 @@ struct dgpu_ctx {
     DevBuf lpos, ltype, locc, lplan, lfac;  // lot crystals, lot plan, group factors
     FormSpec *fs_main = nullptr;            // host copy of the last main combine's FormSpec
     DevBuf wbuf, acc_csf, acc_dsi;          // four_weight staging; four_accumulate sums
+    DevBuf slab_ph0;                        // powder: per-slab origin phases of the atoms
     int64_t acc_np = 0;                     // points of the accumulated sums (0: none)
     DevBuf gq, gpart, grad, batch_desc, batch_aux;
     double batch_ms = 0.0;
@@ -169,13 +170,15 @@ struct TcProblem {
     int32_t ncols;
     int32_t N;               // columns per tile (multiple of 16, <= TcLaunch::Nmax)
     int32_t m_tiles, n_tiles, nslice, ntype;
+    int32_t vstride;         // column tiles per atom group in the V images (n_tiles, or more when shared)
     int64_t nrows_p;         // fra_p * frb: rows of the tile space (rg = nb * fra_p + na)
     int64_t slice_len, nitems, item0, slab;
     int64_t ts[65];
     const uint64_t *ph0, *dra, *drb, *dac;   // phase data along the row axes and the column axis
     const float *w;
     const float2 *ma, *mc;   // per-atom exp(2 pi i 8 d) along ra and ac
-    uint8_t *vimg;           // B rows of every (atom group, column tile), or null: generated in-kernel
+    uint8_t *vimg;           // B rows of every (atom group, column tile), or null: generated in-kernel;
+                             // problems with the same atoms and column steps share one set
     float2 *part;            // part[(t*nslice+ks)*slab + c*nrows_p + rg]
 };
 
@@ -212,6 +215,7 @@ struct TcPlan {
     std::vector<int64_t> part_off;     // float2 offset of each problem's partials
     std::vector<int32_t> nslice;
     bool vimg = false;                 // V images generated before the main kernel
+    bool vshared = false;              // one image set serves every problem
 };
 // vimg: buffer for the V images of the launch (null, or too large for the
 // image budget: V is generated inside the kernel instead)

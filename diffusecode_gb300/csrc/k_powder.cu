@@ -118,7 +118,155 @@ __global__ void k_powder_bin(BinSpec s, const double2 *__restrict__ csf, double 
     if ((threadIdx.x & 31) == 0 && b) atomicAdd(nbinned, (unsigned long long)__popc(b));
 }
 
+// origin phase of the atoms for a box shifted by (sl, sk, sh) steps along the
+// axes l, k, h: ph0 + sl du + sk dv + sh dw, modulo one turn (exact)
+__global__ void k_slab_phase(const uint64_t *__restrict__ ph0, const uint64_t *__restrict__ du,
+                             const uint64_t *__restrict__ dv, const uint64_t *__restrict__ dw, int64_t n, int64_t sl,
+                             int64_t sk, int64_t sh, uint64_t *__restrict__ out)
+{
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    out[j] = ph0[j] + (uint64_t)sl * du[j] + (uint64_t)sk * dv[j] + (uint64_t)sh * dw[j];
+}
+
 }  // namespace
+
+// The (l, k, h) box of a slab as a grid: axis 0 = l, axis 1 = k, axis 2 = h.
+static void slab_grid(const PowderSlab &s, const dgpu_powder *pw, dgpu_grid &g)
+{
+    memset(&g, 0, sizeof(g));
+    g.inc[0] = s.nl;
+    g.inc[1] = s.nk;
+    g.inc[2] = s.nh;
+    g.vi[2] = pw->hkl_del[2];
+    g.vi[3 + 1] = pw->hkl_del[1];
+    g.vi[6 + 0] = pw->hkl_del[0];
+    const double e0[3] = {s.h0 * pw->hkl_del[0] + pw->hkl_shift[0], s.k0 * pw->hkl_del[1] + pw->hkl_shift[1],
+                          s.l0 * pw->hkl_del[2] + pw->hkl_shift[2]};
+    for (int c = 0; c < 4; c++)
+        for (int a = 0; a < 3; a++) g.eck[3 * c + a] = e0[a];
+    g.eck[3 * 1 + 2] += (s.nl - 1) * pw->hkl_del[2];  // lower right: last l
+    g.eck[3 * 2 + 1] += (s.nk - 1) * pw->hkl_del[1];  // upper left: last k
+    g.eck[3 * 3 + 0] += (s.nh - 1) * pw->hkl_del[0];  // top left: last h
+}
+
+// The type sums of all slabs in ONE tensor-core launch: the atoms are
+// prepared once for the union box, each slab's origin phase is shifted from
+// it exactly, and the slabs (same atoms, same column axis l) share one set of
+// V images; then per slab the combine and the binning.
+static int powder_tc_slabs(dgpu_ctx *ctx, const dgpu_crystal &dc, const dgpu_opts &op, const dgpu_powder *pw,
+                           const PowderPlan &plan, BinSpec bs, const int2 *d_tab, double *d_qsp,
+                           unsigned long long *d_cnt, double &kernel_ms, int64_t &pairs)
+{
+    const int nsl = (int)plan.slabs.size();
+    if (nsl == 0) return DGPU_OK;
+    PowderSlab u = plan.slabs[0];                      // union box
+    int32_t h1 = u.h0 + u.nh, k1 = u.k0 + u.nk, l1 = u.l0 + u.nl;
+    int64_t maxnp = 1;
+    for (const PowderSlab &s : plan.slabs) {
+        u.h0 = std::min(u.h0, s.h0);
+        u.k0 = std::min(u.k0, s.k0);
+        u.l0 = std::min(u.l0, s.l0);
+        h1 = std::max(h1, s.h0 + s.nh);
+        k1 = std::max(k1, s.k0 + s.nk);
+        l1 = std::max(l1, s.l0 + s.nl);
+        maxnp = std::max(maxnp, (int64_t)s.nh * s.nk * s.nl);
+    }
+    u.nh = h1 - u.h0;
+    u.nk = k1 - u.k0;
+    u.nl = l1 - u.l0;
+    dgpu_grid gu;
+    slab_grid(u, pw, gu);
+    PhaseGeom geo;
+    memset(&geo, 0, sizeof(geo));
+    geo.mode = DGPU_PHASE_EXACT64;
+    for (int k = 0; k < 3; k++) geo.eck[k] = gu.eck[k];
+    memcpy(geo.vi, gu.vi, sizeof(geo.vi));
+    const int32_t nscat = dc.nscat;
+    int64_t ts[2 * 64 + 4];
+    FoldSpec nofold = {0, dc.ncatoms, {dc.icc[0], dc.icc[1], dc.icc[2]}, {0, 0, 0}, nullptr};
+    int rc = dgpu_prepare_atoms(ctx, dc.pos, dc.iscat, dc.atom_occ, dc.natoms, nscat, geo, nofold, ctx->ph0, ctx->du,
+                                ctx->dv, ctx->dw, ctx->w, ts);
+    if (rc) return rc;
+    const int64_t npad = ts[nscat];
+    int64_t natoms = 0;
+    for (int t = 0; t < nscat; t++) natoms += ts[nscat + 1 + t];
+    DGPU_CUDA(ctx, ctx->slab_ph0.ensure((size_t)nsl * (npad > 0 ? npad : 1) * sizeof(uint64_t)));
+    DGPU_CUDA(ctx, ctx->tc_mult.ensure((size_t)3 * (npad > 0 ? npad : 1) * sizeof(float2)));
+    rc = dgpu_tc_mult_async(ctx, ctx->du.as<uint64_t>(), ctx->dv.as<uint64_t>(), ctx->dw.as<uint64_t>(), npad, npad,
+                            ctx->tc_mult.as<float2>());
+    if (rc) return rc;
+    std::vector<TcInput> in((size_t)nsl);
+    for (int i = 0; i < nsl; i++) {
+        const PowderSlab &s = plan.slabs[i];
+        uint64_t *p = ctx->slab_ph0.as<uint64_t>() + (int64_t)i * npad;
+        if (npad > 0)
+            k_slab_phase<<<(unsigned)dgpu_cdiv(npad, 256), 256, 0, ctx->stream>>>(
+                ctx->ph0.as<uint64_t>(), ctx->du.as<uint64_t>(), ctx->dv.as<uint64_t>(), ctx->dw.as<uint64_t>(), npad,
+                s.l0 - u.l0, s.k0 - u.k0, s.h0 - u.h0, p);
+        TcInput &t = in[(size_t)i];
+        t.ph0 = p;
+        t.du = ctx->du.as<uint64_t>();
+        t.dv = ctx->dv.as<uint64_t>();
+        t.dw = ctx->dw.as<uint64_t>();
+        t.w = ctx->w.as<float>();
+        t.mult = ctx->tc_mult.as<float2>();
+        t.mult_stride = npad;
+        t.ts = ts;
+        t.ntype = nscat;
+        t.box.f[0] = t.box.num[0] = s.nl;
+        t.box.f[1] = t.box.num[1] = s.nk;
+        t.box.f[2] = t.box.num[2] = s.nh;
+        t.axis = 0;                                    // columns along l: every slab the same, images shared
+        pairs += natoms * ((int64_t)s.nh * s.nk * s.nl);
+    }
+    DGPU_CUDA(ctx, cudaGetLastError());
+    TcPlan tp;
+    const int N = op.tc_tile_n > 0 ? op.tc_tile_n : 64;
+    rc = dgpu_tc_plan(ctx, nsl, in.data(), &op, N, 4, tp, ctx->part, ctx->tc_part, &ctx->tc_vimg);
+    if (rc) return rc;
+    DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
+    rc = dgpu_tc_launch(ctx, tp);
+    if (rc) return rc;
+    DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
+    rc = dgpu_tc_check(ctx);
+    if (rc) return rc;
+    float ms = 0.f;
+    DGPU_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]));
+    kernel_ms += ms;
+    // tables, combine and binning, slab by slab
+    DGPU_CUDA(ctx, ctx->istl.ensure(maxnp * sizeof(int32_t)));
+    DGPU_CUDA(ctx, ctx->cfact.ensure((size_t)nscat * DGPU_NTAB * sizeof(double2)));
+    rc = dgpu_formtab_dev(ctx, &dc, &op, ctx->cfact.as<double2>());
+    if (rc) return rc;
+    for (int i = 0; i < nsl; i++) {
+        const PowderSlab &s = plan.slabs[i];
+        dgpu_grid g;
+        slab_grid(s, pw, g);
+        rc = dgpu_stltab_dev(ctx, g.eck, g.vi, g.inc, dc.rten, ctx->istl.as<int32_t>());
+        if (rc) return rc;
+        FormSpec fs;
+        dgpu_fill_formspec(ctx, &dc, &op, &g, fs);
+        PartRef ref;
+        dgpu_tc_partref(tp.probs[(size_t)i], ctx->part.as<float2>() + tp.part_off[(size_t)i], ref);
+        BoxSpec box;
+        for (int k = 0; k < 3; k++) box.f[k] = box.num[k] = g.inc[k];
+        rc = dgpu_combine(ctx, fs, box, ref, ctx->istl.as<int32_t>(), ctx->cfact.as<double2>(), nullptr,
+                          ctx->csf.as<double2>(), ctx->dsi.as<double>(), 1.0);
+        if (rc) return rc;
+        bs.h0 = s.h0;
+        bs.nh = s.nh;
+        bs.k0 = s.k0;
+        bs.nk = s.nk;
+        bs.l0 = s.l0;
+        bs.nl = s.nl;
+        bs.tab = d_tab + s.tab_off;
+        const int64_t np = (int64_t)s.nh * s.nk * s.nl;
+        k_powder_bin<<<(unsigned)dgpu_cdiv(np, 256), 256, 0, ctx->stream>>>(bs, ctx->csf.as<double2>(), d_qsp, d_cnt);
+        DGPU_CUDA(ctx, cudaGetLastError());
+    }
+    return DGPU_OK;
+}
 
 extern "C" int32_t dgpu_powder_npkt(const dgpu_powder *pw) { return dgpu_powder_npkt_host(pw); }
 
@@ -136,7 +284,15 @@ extern "C" int dgpu_powder_complete(dgpu_ctx *ctx, const dgpu_crystal *cr, const
     char msg[256] = {0};
     const int64_t max_points = (int64_t)1 << 26;
     if (pw->slabs < 0) return dgpu_set_error(ctx, DGPU_ERR_ARG, "slabs=%d", pw->slabs);
-    int rc = dgpu_powder_plan(cr->rten, pw, opts->ano, pw->slabs ? pw->slabs : 1, max_points, plan, msg,
+    if (cr->natoms < 1) return dgpu_set_error(ctx, DGPU_ERR_NO_ATOMS, "no atoms: no powder pattern will be calculated");
+    if (!cr->pos || !cr->iscat || !cr->scat || !cr->occ || !cr->dw)
+        return dgpu_set_error(ctx, DGPU_ERR_ARG, "crystal arrays missing");
+    if (cr->nscat < 1 || cr->nscat > 63)
+        return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "nscat=%d outside 1..63", cr->nscat);
+    // the tensor-core engine evaluates all slabs in one launch, the CUDA-core
+    // engine one slab after another
+    const bool tc_multi = opts->engine != DGPU_ENGINE_DIRECT && dgpu_tc_available(ctx);
+    int rc = dgpu_powder_plan(cr->rten, pw, opts->ano, pw->slabs ? pw->slabs : 8, max_points, plan, msg,
                               sizeof msg);
     if (rc) return dgpu_set_error(ctx, rc, "%s", msg);
     const int32_t n_pkt = plan.n_pkt;
@@ -206,24 +362,17 @@ extern "C" int dgpu_powder_complete(dgpu_ctx *ctx, const dgpu_crystal *cr, const
     double kernel_ms = 0.0;
     int64_t pairs = 0;
     int warn = 0;
+    if (opts->cancel && *opts->cancel) return dgpu_set_error(ctx, DGPU_ERR_CANCELLED, "cancelled");
+    if (tc_multi) {
+        rc = powder_tc_slabs(ctx, dc, op, pw, plan, bs, d_tab, d_qsp, d_cnt, kernel_ms, pairs);
+        if (rc) return rc;
+    }
     for (const PowderSlab &s : plan.slabs) {
+        if (tc_multi) break;
         if (opts->cancel && *opts->cancel)
             return dgpu_set_error(ctx, DGPU_ERR_CANCELLED, "cancelled");
         dgpu_grid g;
-        memset(&g, 0, sizeof(g));
-        g.inc[0] = s.nl;
-        g.inc[1] = s.nk;
-        g.inc[2] = s.nh;
-        g.vi[2] = pw->hkl_del[2];                       // axis 0: l
-        g.vi[3 + 1] = pw->hkl_del[1];                   // axis 1: k
-        g.vi[6 + 0] = pw->hkl_del[0];                   // axis 2: h
-        const double e0[3] = {s.h0 * pw->hkl_del[0] + pw->hkl_shift[0], s.k0 * pw->hkl_del[1] + pw->hkl_shift[1],
-                              s.l0 * pw->hkl_del[2] + pw->hkl_shift[2]};
-        for (int c = 0; c < 4; c++)
-            for (int a = 0; a < 3; a++) g.eck[3 * c + a] = e0[a];
-        g.eck[3 * 1 + 2] += (s.nl - 1) * pw->hkl_del[2];  // lower right: last l
-        g.eck[3 * 2 + 1] += (s.nk - 1) * pw->hkl_del[1];  // upper left: last k
-        g.eck[3 * 3 + 0] += (s.nh - 1) * pw->hkl_del[0];  // top left: last h
+        slab_grid(s, pw, g);
         dgpu_info fi;
         rc = dgpu_four_run_dev(ctx, &dc, &g, &op, ctx->csf.as<double2>(), ctx->acsf.as<double2>(),
                                ctx->dsi.as<double>(), &fi);

@@ -811,7 +811,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
                         landed = x - TC_VSLOTS + 1;       // the MMAs consumed that copy: it landed
                     }
                     mbar_arrive_tx(&vfull[v], vbytes);
-                    bulk_g2s(vring + (size_t)v * vbytes, g.vimg + ((g0 + y) * g.n_tiles + nt) * (int64_t)vbytes,
+                    bulk_g2s(vring + (size_t)v * vbytes, g.vimg + ((g0 + y) * g.vstride + nt) * (int64_t)vbytes,
                              vbytes, &vfull[v]);
                 }
             }
@@ -945,6 +945,7 @@ static void tc_problem(dgpu_ctx *ctx, const TcInput &in, const dgpu_opts *op, in
     g.nrows_p = (int64_t)g.fra_p * g.frb;
     g.N = N;
     g.n_tiles = (int32_t)dgpu_cdiv(g.ncols, N);
+    g.vstride = g.n_tiles;
     g.m_tiles = (int32_t)dgpu_cdiv(g.nrows_p, TC_M);
     g.slab = g.nrows_p * g.ncols;
     g.ntype = in.ntype;
@@ -1021,26 +1022,41 @@ int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *o
         for (int64_t i = 0; i < plan.probs[p].nitems; i++) plan.item_prob[plan.probs[p].item0 + i] = p;
     DGPU_CUDA(ctx, part.ensure((size_t)(elems > 0 ? elems : 1) * sizeof(float2)));
     for (int p = 0; p < nprob; p++) plan.probs[p].part = part.as<float2>() + plan.part_off[p];
-    // V images: one per (64-atom group, column tile) of every problem
+    // V images: one per (64-atom group, column tile) of every problem.  The
+    // images depend only on the atoms' column steps and the column index, so
+    // problems over the same atoms with the same column axis (boxes of one
+    // grid at different origins) share one set, as wide as the widest.
+    bool share = nprob > 1;
+    int32_t wide = 0;
+    for (int p = 0; p < nprob; p++) {
+        const TcProblem &g = plan.probs[p];
+        share = share && g.dac == plan.probs[0].dac && in[p].ts == in[0].ts && in[p].ntype == in[0].ntype;
+        wide = g.n_tiles > wide ? g.n_tiles : wide;
+    }
     std::vector<int64_t> voff(nprob, 0);
     int64_t vtot = 0;
     for (int p = 0; p < nprob; p++) {
-        voff[p] = vtot;
-        vtot += in[p].ts[in[p].ntype] / TC_KB * plan.probs[p].n_tiles * (int64_t)N * 768;
+        voff[p] = share ? 0 : vtot;
+        if (!share || p == 0)
+            vtot += in[p].ts[in[p].ntype] / TC_KB * (share ? wide : plan.probs[p].n_tiles) * (int64_t)N * 768;
     }
     // images pay when every one is re-read by several row tiles (a 3D grid);
     // thin planes with one or two row tiles generate V in the kernel
     double reads = 0.0, imgs = 0.0;
     for (int p = 0; p < nprob; p++) {
         const double ni = (double)(in[p].ts[in[p].ntype] / TC_KB) * plan.probs[p].n_tiles;
-        imgs += ni;
+        if (!share || p == 0) imgs += share ? (double)(in[p].ts[in[p].ntype] / TC_KB) * wide : ni;
         reads += ni * plan.probs[p].m_tiles;
     }
     const bool reuse = imgs > 0 && reads >= 4.0 * imgs;
     plan.vimg = vimg && vtot > 0 && vtot <= TC_VIMG_BUDGET && op->tc_vimg >= 0 && (reuse || op->tc_vimg > 0);
+    plan.vshared = share;
     if (plan.vimg) {
         DGPU_CUDA(ctx, vimg->ensure((size_t)vtot));
-        for (int p = 0; p < nprob; p++) plan.probs[p].vimg = vimg->as<uint8_t>() + voff[p];
+        for (int p = 0; p < nprob; p++) {
+            plan.probs[p].vimg = vimg->as<uint8_t>() + voff[p];
+            if (share) plan.probs[p].vstride = wide;
+        }
     }
     const size_t pbytes = ((size_t)nprob * sizeof(TcProblem) + 255) & ~(size_t)255;
     DGPU_CUDA(ctx, desc.ensure(pbytes + (size_t)items * sizeof(int32_t) + 256));
@@ -1102,14 +1118,15 @@ int dgpu_tc_launch(dgpu_ctx *ctx, const TcPlan &plan, bool timed)
     if (plan.L.nitems < 1) return DGPU_OK;
     if (plan.vimg)
         for (const TcProblem &g : plan.probs) {
-            const int64_t nimg = (g.ts[g.ntype] / TC_KB) * g.n_tiles;
+            const int64_t nimg = (g.ts[g.ntype] / TC_KB) * g.vstride;
             if (nimg < 1) continue;
             if (plan.L.bf16)
-                k_tc_vgen<true><<<(unsigned)nimg, 256, (size_t)g.N * 768, ctx->stream>>>(g.dac, g.N, g.n_tiles,
+                k_tc_vgen<true><<<(unsigned)nimg, 256, (size_t)g.N * 768, ctx->stream>>>(g.dac, g.N, g.vstride,
                                                                                           g.vimg);
             else
-                k_tc_vgen<false><<<(unsigned)nimg, 256, (size_t)g.N * 768, ctx->stream>>>(g.dac, g.N, g.n_tiles,
+                k_tc_vgen<false><<<(unsigned)nimg, 256, (size_t)g.N * 768, ctx->stream>>>(g.dac, g.N, g.vstride,
                                                                                            g.vimg);
+            if (plan.vshared) break;                        // one set for all problems
         }
     const int grid = (int)(plan.L.nitems < ctx->nsm ? plan.L.nitems : ctx->nsm);
     if (timed) DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[6], ctx->stream));
