@@ -10,13 +10,15 @@
 // V = exp(2 pi i B-phase); K = the atoms of one type (a slice of them per
 // work item).
 //
-// Operand generation.  Each CTA generates its U tile (128 rows) and V tile
-// (N columns) for KA = 32 atoms per stage in shared memory from the 64-bit
-// fixed-point phases.  A producer thread owns 4 atoms and every 8th row (or
-// column) of a run: it evaluates exp(2 pi i phase) at the start of the run
-// (MUFU, exact 64-bit phase) and then steps by the per-atom factor
-// exp(2 pi i 8 d) (computed once per atom to about one ulp); a row run
-// restarts from the exact phase wherever nb changes.  Every FP32 value is
+// Operand generation.  Each CTA generates its U tile (128 rows) in shared
+// memory from the 64-bit fixed-point phases, and V either the same way (V
+// generated in the kernel, 32-atom stages) or not at all: with V images
+// (k_tc_vgen, written once per launch) a copy warp streams them into a ring
+// (64-atom stages).  A producer thread evaluates exp(2 pi i phase) at the
+// start of a run of rows (or columns) (MUFU, exact 64-bit phase) and then
+// steps by the per-atom factor exp(2 pi i 8 d) (computed once per atom to
+// about one ulp); a row run restarts from the exact phase wherever nb
+// changes.  Every FP32 value is
 // split into hi (the value with its mantissa cut to the fp16 / bf16 width,
 // exact in that format) and lo (the exact remainder, rounded).  V is scaled
 // by 2^12 so that its lo parts stay normal fp16 numbers; all accumulators
@@ -31,7 +33,7 @@
 // Accumulation.  Every MMA truncates its FP32 accumulator by about one ulp, so
 // the error of one TMEM accumulator grows with the number of MMAs chained into
 // it.  The main accumulator is therefore drained every `flush` stages
-// (flush*32 atoms) and added with round-to-nearest FP32 adds to a running sum
+// (128 atoms) and added with round-to-nearest FP32 adds to a running sum
 // (kept in TMEM when N <= 64, otherwise in the work item's partial in global
 // memory); the small corrections accumulate over the whole work item.  With
 // nbuf = 2 the main accumulator is double-buffered so that a drain overlaps the
@@ -46,10 +48,11 @@
 // waits are bounded (globaltimer); a wait that gives up sets an error flag,
 // the CTA stops issuing, waits for its own MMAs, frees TMEM and returns.
 //
-// Shared-memory operands use the canonical K-major layout with the 64-byte
-// swizzle: a row holds the 32 atoms of a stage (64 B), 8-row groups of 512 B
-// are SBO = 512 B apart, and the 16-byte chunk c of row r is stored at
-// chunk c ^ ((r & 7) >> 1).
+// Shared-memory operands use the canonical K-major layouts: with V images, a
+// row holds the 64 atoms of a stage (128 B) with the 128-byte swizzle (8-row
+// groups 1024 B apart, the 16-byte chunk c of row r at chunk c ^ (r & 7));
+// with V generated in the kernel, 32 atoms (64 B) with the 64-byte swizzle
+// (8-row groups 512 B apart, chunk c of row r at c ^ ((r & 7) >> 1)).
 #include "dgpu_internal.h"
 
 #define TC_KA 32                               // atoms per stage, V generated in the kernel (64-byte rows)
