@@ -342,3 +342,32 @@ def test_powder_slab_count_invariance(ctx, engine):
     t = 1e-6 if engine == _abi.ENGINE_DIRECT else 2e-5
     for q in out[1:]:
         np.testing.assert_allclose(q, out[0], rtol=10 * t, atol=t * out[0].max())
+
+
+def test_oracle_powder_empty():
+    """Only the origin inside a tiny sphere (its Q = 0 is below qmin), or every
+    Q outside the range: a zero pattern of n_pkt + 1 points."""
+    cr, pw, op, _ = _case("ortho")
+    pw.ds_max = 1e-3
+    rc, q, nr, npts = O.powder_complete(cr, pw, op)
+    assert rc == 0 and nr == 1 and npts == 1 and q.shape == (pw.n_pkt + 1,) and not q.any()
+    cr, pw, op, _ = _case("ortho")
+    pw.qmin, pw.qmax = 20.0, 21.0
+    rc, q, nr, npts = O.powder_complete(cr, pw, op)
+    assert rc == 0 and nr > 0 and not q.any()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("engine", [_abi.ENGINE_DIRECT, _abi.ENGINE_TC])
+def test_powder_empty(ctx, engine):
+    from diffusecode_gb300 import fourier as FR
+    cr, pw, op, _ = _case("ortho")
+    op.engine = engine
+    pw.ds_max = 1e-3
+    q, info = FR.powder_complete(cr, pw, op, ctx=ctx)
+    assert info.rods == 1 and info.binned == 0 and q.shape == (pw.n_pkt + 1,) and not q.any()
+    cr, pw, op, _ = _case("ortho")
+    op.engine = engine
+    pw.qmin, pw.qmax = 20.0, 21.0
+    q, info = FR.powder_complete(cr, pw, op, ctx=ctx)
+    assert info.rods > 0 and info.binned == 0 and not q.any()
