@@ -289,6 +289,9 @@ extern "C" int dgpu_powder_complete(dgpu_ctx *ctx, const dgpu_crystal *cr, const
         return dgpu_set_error(ctx, DGPU_ERR_ARG, "crystal arrays missing");
     if (cr->nscat < 1 || cr->nscat > 63)
         return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "nscat=%d outside 1..63", cr->nscat);
+    if (opts->power < 0 || opts->power > 5) return dgpu_set_error(ctx, DGPU_ERR_ARG, "power=%d", opts->power);
+    if (opts->form != DGPU_FORM_TABLE && opts->form != DGPU_FORM_ANALYTIC)
+        return dgpu_set_error(ctx, DGPU_ERR_ARG, "form=%d", opts->form);
     // the tensor-core engine evaluates all slabs in one launch, the CUDA-core
     // engine one slab after another
     const bool tc_multi = opts->engine != DGPU_ENGINE_DIRECT && dgpu_tc_available(ctx);

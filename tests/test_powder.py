@@ -321,6 +321,8 @@ def test_powder_errors(ctx):
     assert code(pref_type=7) == _abi.DGPU_ERR_ARG
     assert code(pref_type=_abi.PREF_MARCH, pref_g1=0.0) == _abi.DGPU_ERR_ARG
     assert code(ds_max=-1.0) == _abi.DGPU_ERR_ARG
+    assert code(power=9) == _abi.DGPU_ERR_ARG
+    assert code(form=5) == _abi.DGPU_ERR_ARG
 
 
 @pytest.mark.gpu
