@@ -28,17 +28,61 @@ __device__ __forceinline__ double2 ld_part(const float2 *p)
 }
 
 // element offsets of a partial-sum array (see PartRef)
+// Strides of the partial sums along the box axes, and the order in which the
+// combine kernels walk them: thread r takes slot r of the partials' own layout
+// (axis a0 innermost), so that the reads of the partials -- the bulk of the
+// traffic -- are coalesced; padding slots of the tensor-core layout idle.
 struct PartLayout {
     int64_t s0, s1, s2, slab;
+    int64_t m1, m2, nthr;      // strides of axes a1, a2; slots walked
+    int32_t a0, a1, a2;        // box axes from innermost to outermost
 };
 
 static PartLayout layout_of(const PartRef &r, const BoxSpec &box)
 {
+    PartLayout L;
+    int64_t s[3];
     if (r.s[0] == 0) {
-        const int64_t f0 = box.f[0], f01 = (int64_t)box.f[0] * box.f[1];
-        return PartLayout{1, f0, f01, f01 * box.f[2]};
+        s[0] = 1;
+        s[1] = box.f[0];
+        s[2] = (int64_t)box.f[0] * box.f[1];
+        L.slab = s[2] * box.f[2];
+    } else {
+        for (int k = 0; k < 3; k++) s[k] = r.s[k];
+        L.slab = r.slab;
     }
-    return PartLayout{r.s[0], r.s[1], r.s[2], r.slab};
+    L.s0 = s[0];
+    L.s1 = s[1];
+    L.s2 = s[2];
+    // axes by stride; of two equal strides the axis of extent 1 goes first
+    int a[3] = {0, 1, 2};
+    auto before = [&](int x, int y) { return s[x] < s[y] || (s[x] == s[y] && box.f[x] == 1 && box.f[y] != 1); };
+    for (int p = 0; p < 3; p++)
+        for (int q = p + 1; q < 3; q++)
+            if (before(a[q], a[p])) {
+                const int t = a[p];
+                a[p] = a[q];
+                a[q] = t;
+            }
+    L.a0 = a[0];
+    L.a1 = a[1];
+    L.a2 = a[2];
+    L.m1 = s[a[1]];
+    L.m2 = s[a[2]];
+    L.nthr = L.m2 * box.f[a[2]];
+    return L;
+}
+
+// box point of layout slot r, false for a padding slot
+__device__ __forceinline__ bool part_point(const PartLayout &L, const BoxSpec &box, int64_t r, int64_t &i,
+                                           int64_t &j, int64_t &l)
+{
+    const int64_t c2 = r / L.m2, rem = r - c2 * L.m2, c1 = L.m1 > 0 ? rem / L.m1 : 0, c0 = rem - c1 * L.m1;
+    if (c0 >= box.f[L.a0] || c1 >= box.f[L.a1] || c2 >= box.f[L.a2]) return false;
+    i = L.a0 == 0 ? c0 : L.a1 == 0 ? c1 : c2;
+    j = L.a0 == 1 ? c0 : L.a1 == 1 ? c1 : c2;
+    l = L.a0 == 2 ? c0 : L.a1 == 2 ? c1 : c2;
+    return true;
 }
 
 template <class P>
@@ -47,10 +91,9 @@ __global__ void k_combine(const FormSpec *fs, BoxSpec box, const P *__restrict__
                           const double2 *__restrict__ cfact, const double2 *__restrict__ acsf,
                           double2 *__restrict__ csf, double *__restrict__ dsi, double ds, double sqds)
 {
-    int64_t pb = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
-    if (pb >= nb) return;
-    int64_t i = pb % box.f[0], j = (pb / box.f[0]) % box.f[1], l = pb / ((int64_t)box.f[0] * box.f[1]);
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t i, j, l;
+    if (r >= lay.nthr || !part_point(lay, box, r, i, j, l)) return;
     int64_t idx = i + (int64_t)box.num[0] * (j + (int64_t)box.num[1] * l);
     double h[3];
     if (form_needs_h(fs)) form_hvec(fs, i, j, l, h);
@@ -97,10 +140,9 @@ __global__ void k_aver_combine(const FormSpec *fs, BoxSpec box, const P *__restr
                                int32_t c2, double d0, double d1, double d2, double norm,
                                double2 *__restrict__ acsf)
 {
-    int64_t pb = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
-    if (pb >= nb) return;
-    int64_t i = pb % box.f[0], j = (pb / box.f[0]) % box.f[1], l = pb / ((int64_t)box.f[0] * box.f[1]);
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t i, j, l;
+    if (r >= lay.nthr || !part_point(lay, box, r, i, j, l)) return;
     int64_t idx = i + (int64_t)box.num[0] * (j + (int64_t)box.num[1] * l);
     int64_t nfull = (int64_t)box.num[0] * box.num[1] * box.num[2];
     double h[3];
@@ -139,8 +181,8 @@ __global__ void k_aver_combine(const FormSpec *fs, BoxSpec box, const P *__restr
             L.y += v.y;
         }
     }
-    double2 r = cmul(A, L);
-    acsf[idx] = make_double2(r.x * norm, r.y * norm);
+    const double2 av = cmul(A, L);
+    acsf[idx] = make_double2(av.x * norm, av.y * norm);
 }
 
 // four_apply_friedel: points past the halved axis' middle take the conjugate
@@ -276,9 +318,8 @@ int dgpu_combine(dgpu_ctx *ctx, const FormSpec &fs, const BoxSpec &box, const Pa
     FormSpec *d;
     int rc = upload_formspec(ctx, fs, &d);
     if (rc) return rc;
-    int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
-    const unsigned nblk = (unsigned)dgpu_cdiv(nb, 256);
     const PartLayout lay = layout_of(part, box);
+    const unsigned nblk = (unsigned)dgpu_cdiv(lay.nthr, 256);
     if (part.f32)
         k_combine<float2><<<nblk, 256, 0, ctx->stream>>>(d, box, (const float2 *)part.p, part.nslice, lay, istl,
                                                           cfact, acsf_in, csf, dsi, diff_scale, sqrt(diff_scale));
@@ -298,9 +339,8 @@ int dgpu_aver_combine(dgpu_ctx *ctx, const FormSpec &fs, const BoxSpec &box, con
     FormSpec *d;
     int rc = upload_formspec(ctx, fs, &d);
     if (rc) return rc;
-    int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
-    const unsigned nblk = (unsigned)dgpu_cdiv(nb, 256);
     const PartLayout lay = layout_of(apart, box);
+    const unsigned nblk = (unsigned)dgpu_cdiv(lay.nthr, 256);
     if (apart.f32)
         k_aver_combine<float2><<<nblk, 256, 0, ctx->stream>>>(
             d, box, (const float2 *)apart.p, apart.nslice, lay, istl, cfact, lat, lat_nslice, lat_closed, icc[0],
@@ -352,9 +392,8 @@ int dgpu_qinfo(dgpu_ctx *ctx, const double eck[3], const double vi[9], const int
 int dgpu_combine_async(dgpu_ctx *ctx, const FormSpec *d_fs, const BoxSpec &box, const PartRef &part,
                        const int32_t *istl, const double2 *cfact, double2 *csf, double *dsi, double diff_scale)
 {
-    const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
-    const unsigned nblk = (unsigned)dgpu_cdiv(nb, 256);
     const PartLayout lay = layout_of(part, box);
+    const unsigned nblk = (unsigned)dgpu_cdiv(lay.nthr, 256);
     if (part.f32)
         k_combine<float2><<<nblk, 256, 0, ctx->stream>>>(d_fs, box, (const float2 *)part.p, part.nslice, lay, istl,
                                                           cfact, nullptr, csf, dsi, diff_scale, sqrt(diff_scale));
@@ -393,10 +432,11 @@ __global__ void k_lot_combine(int32_t ngroup, int32_t nlot, BoxSpec box, const P
                               const double2 *__restrict__ acsf, double2 *__restrict__ csf,
                               double *__restrict__ dsi, int32_t last)
 {
-    const int64_t pb = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t i, j, l;
+    if (r >= lay.nthr || !part_point(lay, box, r, i, j, l)) return;
     const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
-    if (pb >= nb) return;
-    const int64_t i = pb % box.f[0], j = (pb / box.f[0]) % box.f[1], l = pb / ((int64_t)box.f[0] * box.f[1]);
+    const int64_t pb = i + (int64_t)box.f[0] * (j + (int64_t)box.f[1] * l);
     const int64_t idx = i + (int64_t)box.num[0] * (j + (int64_t)box.num[1] * l);
     const double2 a = acsf ? acsf[idx] : make_double2(0.0, 0.0);
     const int64_t off = i * lay.s0 + j * lay.s1 + l * lay.s2;
@@ -454,12 +494,11 @@ int dgpu_group_factors(dgpu_ctx *ctx, const FormSpec &fs, const BoxSpec &box, co
 int dgpu_lot_combine(dgpu_ctx *ctx, int32_t ngroup, int32_t nlot, const BoxSpec &box, const PartRef *part,
                      const double2 *fac, const double2 *acsf, double2 *csf, double *dsi, int32_t last)
 {
-    const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
-    const unsigned nblk = (unsigned)dgpu_cdiv(nb, 256);
     PartRef none;
     memset(&none, 0, sizeof(none));
     const PartRef &r = part ? *part : none;
     const PartLayout lay = layout_of(r, box);
+    const unsigned nblk = (unsigned)dgpu_cdiv(lay.nthr, 256);
     const int32_t nslice = r.nslice > 0 ? r.nslice : 1;
     if (r.f32)
         k_lot_combine<float2><<<nblk, 256, 0, ctx->stream>>>(ngroup, nlot, box, (const float2 *)r.p, nslice, lay,
