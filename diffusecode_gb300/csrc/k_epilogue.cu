@@ -441,25 +441,62 @@ __global__ void k_lot_combine(int32_t ngroup, int32_t nlot, BoxSpec box, const P
     const double2 a = acsf ? acsf[idx] : make_double2(0.0, 0.0);
     const int64_t off = i * lay.s0 + j * lay.s1 + l * lay.s2;
     double acc = 0.0;
-    for (int L = 0; L < nlot; L++) {
-        double2 F = make_double2(0.0, 0.0);
-        if (part)
-            for (int g = 0; g < ngroup; g++) {
-                const P *pt = part + (int64_t)(L * ngroup + g) * nslice * lay.slab + off;
-                double2 s = make_double2(0.0, 0.0);
-                for (int k = 0; k < nslice; k++) {
-                    const double2 v = ld_part(pt + (int64_t)k * lay.slab);
-                    s.x += v.x;
-                    s.y += v.y;
+    if constexpr (sizeof(P) == sizeof(float2)) {
+        // FP32 partials (tensor-core engine): the group products in FP32 --
+        // the partials carry FP32 rounding already -- with the group factors
+        // of the point loaded once; F - <F> and |.|^2 in FP64
+        constexpr int GMAX = 8;
+        float2 fg[GMAX];
+#pragma unroll
+        for (int g = 0; g < GMAX; g++) {
+            const double2 f = g < ngroup ? fac[(int64_t)g * nb + pb] : make_double2(0.0, 0.0);
+            fg[g] = make_float2((float)f.x, (float)f.y);
+        }
+        for (int L = 0; L < nlot; L++) {
+            float fr = 0.f, fi = 0.f;
+            if (part)
+                for (int g = 0; g < ngroup; g++) {
+                    const P *pt = part + (int64_t)(L * ngroup + g) * nslice * lay.slab + off;
+                    float sr = 0.f, si = 0.f;
+                    for (int k = 0; k < nslice; k++) {
+                        const float2 v = *reinterpret_cast<const float2 *>(pt + (int64_t)k * lay.slab);
+                        sr += v.x;
+                        si += v.y;
+                    }
+                    float2 f;
+                    if (g < GMAX) f = fg[g];
+                    else {
+                        const double2 fd = fac[(int64_t)g * nb + pb];
+                        f = make_float2((float)fd.x, (float)fd.y);
+                    }
+                    fr = fmaf(sr, f.x, fmaf(-si, f.y, fr));
+                    fi = fmaf(sr, f.y, fmaf(si, f.x, fi));
                 }
-                const double2 m = cmul(s, fac[(int64_t)g * nb + pb]);
-                F.x += m.x;
-                F.y += m.y;
-            }
-        F.x -= a.x;
-        F.y -= a.y;
-        acc += F.x * F.x + F.y * F.y;
-        if (L == last) csf[idx] = F;
+            const double2 F = make_double2((double)fr - a.x, (double)fi - a.y);
+            acc += F.x * F.x + F.y * F.y;
+            if (L == last) csf[idx] = F;
+        }
+    } else {
+        for (int L = 0; L < nlot; L++) {
+            double2 F = make_double2(0.0, 0.0);
+            if (part)
+                for (int g = 0; g < ngroup; g++) {
+                    const P *pt = part + (int64_t)(L * ngroup + g) * nslice * lay.slab + off;
+                    double2 s = make_double2(0.0, 0.0);
+                    for (int k = 0; k < nslice; k++) {
+                        const double2 v = ld_part(pt + (int64_t)k * lay.slab);
+                        s.x += v.x;
+                        s.y += v.y;
+                    }
+                    const double2 m = cmul(s, fac[(int64_t)g * nb + pb]);
+                    F.x += m.x;
+                    F.y += m.y;
+                }
+            F.x -= a.x;
+            F.y -= a.y;
+            acc += F.x * F.x + F.y * F.y;
+            if (L == last) csf[idx] = F;
+        }
     }
     dsi[idx] += acc;
 }
