@@ -81,7 +81,7 @@ extern "C" int dgpu_ctx_destroy(dgpu_ctx *c)
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     dgpu_batch_free(c);
-    DevBuf *bufs[] = {&c->pos, &c->iscat, &c->aocc, &c->sel, &c->counts, &c->type_start, &c->ph0, &c->du,
+    DevBuf *bufs[] = {&c->pos, &c->iscat, &c->aocc, &c->sel, &c->counts, &c->ph0, &c->du,
                       &c->dv, &c->dw, &c->w, &c->aph0, &c->adu, &c->adv, &c->adw, &c->aw, &c->istl,
                       &c->cfact, &c->part, &c->apart, &c->lat, &c->csf, &c->acsf, &c->dsi, &c->stats,
                       &c->flag, &c->tc_part, &c->tc_work, &c->tc_mult, &c->tc_vimg, &c->adj_qimg,
@@ -89,6 +89,8 @@ extern "C" int dgpu_ctx_destroy(dgpu_ctx *c)
                       &c->ianis, &c->geff, &c->ghist, &c->lpos, &c->ltype, &c->locc, &c->lplan, &c->lfac,
                       &c->wbuf, &c->acc_csf, &c->acc_dsi, &c->slab_ph0};
     for (DevBuf *b : bufs) b->release();
+    c->stage.release();
+    for (cudaEvent_t e : c->run_ev) cudaEventDestroy(e);
     delete c->fs_main;
     for (int i = 0; i < DGPU_NEV; i++)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
@@ -216,6 +218,127 @@ static int engine_sums(dgpu_ctx *ctx, int engine, DevBuf &ph0, DevBuf &du, DevBu
     ref->p = part.p;
     ref->nslice = nslice;
     return rc;
+}
+
+// The lots' engine launches (fourier_sup.f90:136-257), a chunk of lots per
+// launch, in batches of chunks: every chunk of a batch is gathered and its
+// (lot, group) types counted first, so that one host wait yields all their
+// type ranges; scatter, engine launch and lot combine of the chunks then
+// follow one another on the stream with no host wait between them (the
+// tensor-core engine in its deferred mode, its error flag read once per
+// batch).
+#define LOT_BATCH_SLOTS ((int64_t)1 << 24)     // lot atom slots gathered per batch
+
+namespace {
+struct LotChunk {
+    int64_t lot0, slot0, m;
+    int32_t nl, ntype;
+    size_t reg;                        // offset of the chunk's count region
+    int64_t ts[2 * 64 + 4];
+};
+struct DeferGuard {
+    dgpu_ctx *c;
+    explicit DeferGuard(dgpu_ctx *x) : c(x) { c->tc_defer = 1; }
+    ~DeferGuard() { c->tc_defer = 0; }
+};
+}  // namespace
+
+static int lots_sums(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *op, const LotPlan &lp, int32_t ngroup,
+                     const int32_t *eiscat, const PhaseGeom &geo, const BoxSpec &box, int engine, int64_t np,
+                     const double2 *acsf_in, double2 *d_csf, double *d_dsi, int64_t *pairs, float *kernel_ms)
+{
+    const int64_t per_lot = lp.geo.per_lot;
+    const int64_t nchunk = dgpu_cdiv(lp.nlots, lp.per_chunk);
+    const int64_t chunk_slots = (int64_t)lp.per_chunk * per_lot;
+    const int64_t cpb = chunk_slots > 0 && LOT_BATCH_SLOTS / chunk_slots > 1 ? LOT_BATCH_SLOTS / chunk_slots : 1;
+    const FoldSpec nofold = {0, 1, {1, 1, 1}, {0, 0, 0}, nullptr};
+    int rc;
+    for (int64_t c0 = 0; c0 < nchunk; c0 += cpb) {
+        const int64_t nc = nchunk - c0 < cpb ? nchunk - c0 : cpb;
+        std::vector<LotChunk> ch((size_t)nc);
+        int64_t slots = 0;
+        size_t rbytes = 0;
+        for (int64_t i = 0; i < nc; i++) {
+            LotChunk &k = ch[(size_t)i];
+            k.lot0 = (c0 + i) * lp.per_chunk;
+            k.nl = (int32_t)(lp.nlots - k.lot0 < lp.per_chunk ? lp.nlots - k.lot0 : lp.per_chunk);
+            k.ntype = k.nl * ngroup;
+            k.m = (int64_t)k.nl * per_lot;
+            k.slot0 = slots;
+            slots += k.m;
+            k.reg = rbytes;
+            rbytes += dgpu_prepare_region_bytes(k.m, k.ntype);
+        }
+        const size_t ns = (size_t)(slots > 0 ? slots : 1);
+        DGPU_CUDA(ctx, ctx->lpos.ensure(ns * 3 * sizeof(double)));
+        DGPU_CUDA(ctx, ctx->ltype.ensure(ns * sizeof(int32_t)));
+        DGPU_CUDA(ctx, ctx->locc.ensure(ns * sizeof(float)));
+        DGPU_CUDA(ctx, ctx->counts.ensure(rbytes));
+        for (LotChunk &k : ch) {
+            int64_t m = 0;
+            rc = dgpu_lot_gather(ctx, lp, k.lot0, k.nl, cr->pos, eiscat, cr->atom_occ, k.slot0, &m);
+            if (rc) return rc;
+            const PrepRegion r = dgpu_prepare_region((char *)ctx->counts.p + k.reg, k.m, k.ntype);
+            rc = dgpu_prepare_count(ctx, ctx->ltype.as<int32_t>() + k.slot0, k.m, k.ntype, nofold, r);
+            if (rc) return rc;
+            DGPU_CUDA(ctx, cudaMemcpyAsync(k.ts, r.d_ts, (2 * k.ntype + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost,
+                                           ctx->stream));
+        }
+        DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));        // the type ranges of every chunk
+        ctx->stage.reset();
+        // the largest chunk sizes the atom buffers before the run
+        int64_t most = 1;
+        for (const LotChunk &k : ch) most = k.ts[k.ntype] > most ? k.ts[k.ntype] : most;
+        DGPU_CUDA(ctx, ctx->ph0.ensure((size_t)most * 8));
+        DGPU_CUDA(ctx, ctx->du.ensure((size_t)most * 8));
+        DGPU_CUDA(ctx, ctx->dv.ensure((size_t)most * 8));
+        DGPU_CUDA(ctx, ctx->dw.ensure((size_t)most * 8));
+        DGPU_CUDA(ctx, ctx->w.ensure((size_t)most * 4));
+        DGPU_CUDA(ctx, ctx->aidx.ensure((size_t)most * 4));
+        DGPU_CUDA(ctx, ctx->flag.ensure(64));
+        DGPU_CUDA(ctx, cudaMemsetAsync(ctx->flag.as<int32_t>() + 8, 0, sizeof(int32_t), ctx->stream));
+        while (ctx->run_ev.size() < 2 * (size_t)nc) {
+            cudaEvent_t e;
+            DGPU_CUDA(ctx, cudaEventCreate(&e));
+            ctx->run_ev.push_back(e);
+        }
+        {
+            DeferGuard defer(ctx);
+            for (int64_t i = 0; i < nc; i++) {
+                const LotChunk &k = ch[(size_t)i];
+                const PrepRegion r = dgpu_prepare_region((char *)ctx->counts.p + k.reg, k.m, k.ntype);
+                rc = dgpu_prepare_scatter(ctx, ctx->lpos.as<double>() + 3 * k.slot0, ctx->ltype.as<int32_t>() + k.slot0,
+                                          cr->atom_occ ? ctx->locc.as<float>() + k.slot0 : nullptr, k.m, k.ntype, geo,
+                                          nofold, r, k.ts[k.ntype], ctx->ph0, ctx->du, ctx->dv, ctx->dw, ctx->w);
+                if (rc) return rc;
+                int64_t nat = 0;
+                for (int t = 0; t < k.ntype; t++) nat += k.ts[k.ntype + 1 + t];
+                *pairs += nat * np;
+                PartRef pref;
+                memset(&pref, 0, sizeof(pref));
+                DGPU_CUDA(ctx, cudaEventRecord(ctx->run_ev[2 * i], ctx->stream));
+                if (nat > 0) {
+                    rc = engine_sums(ctx, engine, ctx->ph0, ctx->du, ctx->dv, ctx->dw, ctx->w, k.ts, k.ntype, op, box,
+                                     ctx->part, &pref);
+                    if (rc) return rc;
+                }
+                DGPU_CUDA(ctx, cudaEventRecord(ctx->run_ev[2 * i + 1], ctx->stream));
+                const int32_t last = k.lot0 + k.nl == lp.nlots ? k.nl - 1 : -1;
+                rc = dgpu_lot_combine(ctx, ngroup, k.nl, box, nat > 0 ? &pref : nullptr, ctx->lfac.as<double2>(),
+                                      acsf_in, d_csf, d_dsi, last);
+                if (rc) return rc;
+                if (cancelled(op)) return dgpu_set_error(ctx, DGPU_ERR_CANCELLED, "cancelled");
+            }
+        }
+        rc = dgpu_tc_check(ctx);                                    // waits for the batch
+        if (rc) return rc;
+        for (int64_t i = 0; i < nc; i++) {
+            float ms = 0.f;
+            DGPU_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->run_ev[2 * i], ctx->run_ev[2 * i + 1]));
+            *kernel_ms += ms;
+        }
+    }
+    return DGPU_OK;
 }
 
 // The whole path with device-resident crystal arrays and outputs.
@@ -410,39 +533,9 @@ int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g,
         rc = dgpu_group_factors(ctx, fsm, box, ctx->istl.as<int32_t>(), ctx->cfact.as<double2>(),
                                 ctx->lfac.as<double2>());
         if (rc) return rc;
-        for (int64_t lot0 = 0; lot0 < lp.nlots; lot0 += lp.per_chunk) {
-            const int32_t nl = (int32_t)(lp.nlots - lot0 < lp.per_chunk ? lp.nlots - lot0 : lp.per_chunk);
-            const int32_t ntype = nl * ngroup;
-            int64_t m = 0;
-            rc = dgpu_lot_gather(ctx, lp, lot0, nl, cr->pos, eiscat, cr->atom_occ, &m);
-            if (rc) return rc;
-            FoldSpec nofold = {0, 1, {1, 1, 1}, {0, 0, 0}, nullptr};
-            rc = dgpu_prepare_atoms(ctx, ctx->lpos.as<double>(), ctx->ltype.as<int32_t>(),
-                                    cr->atom_occ ? ctx->locc.as<float>() : nullptr, m, ntype, geo, nofold, ctx->ph0,
-                                    ctx->du, ctx->dv, ctx->dw, ctx->w, ts);
-            if (rc) return rc;
-            int64_t nat = 0;
-            for (int t = 0; t < ntype; t++) nat += ts[ntype + 1 + t];
-            pairs += nat * np;
-            PartRef pref;
-            memset(&pref, 0, sizeof(pref));
-            DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
-            if (nat > 0) {
-                rc = engine_sums(ctx, engine, ctx->ph0, ctx->du, ctx->dv, ctx->dw, ctx->w, ts, ntype, op, box,
-                                 ctx->part, &pref);
-                if (rc) return rc;
-            }
-            DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
-            const int32_t last = lot0 + nl == lp.nlots ? nl - 1 : -1;
-            rc = dgpu_lot_combine(ctx, ngroup, nl, box, nat > 0 ? &pref : nullptr, ctx->lfac.as<double2>(), acsf_in,
-                                  d_csf, d_dsi, last);
-            if (rc) return rc;
-            DGPU_CUDA(ctx, cudaEventSynchronize(ctx->ev[3]));
-            float ms = 0.f;
-            DGPU_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]));
-            kernel_ms += ms;
-            if (cancelled(op)) return dgpu_set_error(ctx, DGPU_ERR_CANCELLED, "cancelled");
-        }
+        rc = lots_sums(ctx, cr, op, lp, ngroup, eiscat, geo, box, engine, np, acsf_in, d_csf, d_dsi, &pairs,
+                       &kernel_ms);
+        if (rc) return rc;
         // dsi * icc1*icc2*icc3 / (ncell*nlots) when nlots != 1 (fourier_sup.f90:273-277)
         double dnorm = 1.0;
         if (lp.nlots != 1)

@@ -6,6 +6,7 @@
 
 #include <map>
 #include <tuple>
+#include <vector>
 #include <stdio.h>
 #include <string.h>
 
@@ -34,6 +35,42 @@ struct DevBuf {
         cap = 0;
     }
     template <class T> T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+// Pinned host memory handed out in order and taken back all at once after a
+// host wait: the source of asynchronous uploads whose host copy must outlive
+// the call that enqueues them.
+struct HostArena {
+    char *p = nullptr;
+    size_t cap = 0, used = 0;
+    std::vector<char *> old;              // outgrown blocks, freed at the next reset
+    void *take(size_t bytes) {
+        bytes = (bytes + 255) & ~(size_t)255;
+        if (used + bytes > cap) {
+            size_t want = cap * 2 > bytes ? cap * 2 : bytes;
+            if (want < ((size_t)1 << 20)) want = (size_t)1 << 20;
+            char *q = nullptr;
+            if (cudaMallocHost(reinterpret_cast<void **>(&q), want) != cudaSuccess) return nullptr;
+            if (p) old.push_back(p);
+            p = q;
+            cap = want;
+            used = 0;
+        }
+        void *r = p + used;
+        used += bytes;
+        return r;
+    }
+    void reset() {                        // only after the uploads from it have completed
+        for (char *q : old) cudaFreeHost(q);
+        old.clear();
+        used = 0;
+    }
+    void release() {
+        reset();
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+    }
 };
 
 // Per-atom phase data, grouped by type (SoA).  Phases are 64-bit fixed point
@@ -68,7 +105,7 @@ struct dgpu_ctx {
     char err[512] = {0};
     // cached buffers
     DevBuf pos, iscat, aocc, sel;
-    DevBuf counts, type_start;
+    DevBuf counts;                      // per-block type counts, their scan, type starts
     DevBuf ph0, du, dv, dw, w;          // main atom set
     DevBuf aph0, adu, adv, adw, aw;     // folded atoms for <F>
     DevBuf istl, cfact, part, apart, lat, csf, acsf, dsi, stats, flag;
@@ -89,6 +126,12 @@ struct dgpu_ctx {
     std::map<TcKey, TcChoice> tc_tuned;   // autotuner results per problem shape
     BatchState *batch = nullptr;          // captured population graph and its buffers
     int32_t tc_last[4] = {-1, -1, -1, -1};
+    // Deferred tensor-core launches (a run of launches with one host wait at
+    // its end): plans are uploaded from the pinned arena, the error flag is
+    // cleared once before the run and read after it.
+    int tc_defer = 0;
+    HostArena stage;
+    std::vector<cudaEvent_t> run_ev;        // event pairs around the launches of such a run
 };
 
 // error helpers ---------------------------------------------------------
@@ -134,6 +177,23 @@ int dgpu_prepare_atoms(dgpu_ctx *ctx, const double *d_pos, const int32_t *d_isca
                        const float *d_aocc, int64_t natoms, int32_t nscat,
                        const PhaseGeom &g, const FoldSpec &fs, DevBuf &ph0, DevBuf &du,
                        DevBuf &dv, DevBuf &dw, DevBuf &w, int64_t *h_type_start);
+// The same in two phases, for callers that learn the type starts of several
+// atom sets with one host wait: the count phase (per-block type counts,
+// their scan and the type starts d_ts, device only) into a region of
+// dgpu_prepare_region_bytes, then the scatter with the padded total.
+struct PrepRegion {
+    int32_t *counts;
+    int64_t *offs;
+    int64_t *d_ts;         // 2*nscat+1 values as h_type_start
+    int64_t nblk;
+};
+size_t dgpu_prepare_region_bytes(int64_t natoms, int32_t nscat);
+PrepRegion dgpu_prepare_region(void *base, int64_t natoms, int32_t nscat);
+int dgpu_prepare_count(dgpu_ctx *ctx, const int32_t *d_iscat, int64_t natoms, int32_t nscat, const FoldSpec &fs,
+                       const PrepRegion &r);
+int dgpu_prepare_scatter(dgpu_ctx *ctx, const double *d_pos, const int32_t *d_iscat, const float *d_aocc,
+                         int64_t natoms, int32_t nscat, const PhaseGeom &g, const FoldSpec &fs, const PrepRegion &r,
+                         int64_t total, DevBuf &ph0, DevBuf &du, DevBuf &dv, DevBuf &dw, DevBuf &w);
 // Lattice points of all cells (four_getav LOT_OFF) as one atom set.
 int dgpu_prepare_lattice(dgpu_ctx *ctx, const int32_t icc[3], const double dim0[3],
                          const PhaseGeom &g, DevBuf &ph0, DevBuf &du, DevBuf &dv,
@@ -233,7 +293,9 @@ int dgpu_tc_mult_async(dgpu_ctx *ctx, const uint64_t *du, const uint64_t *dv, co
 // Layout of a problem's partials for the combine kernels.
 void dgpu_tc_partref(const TcProblem &g, const float2 *p, PartRef &ref);
 // Single problem with autotuned tile; partial sums are float2 (FP32, one per
-// work item, RN-accumulated drains); ref receives their layout.
+// work item, RN-accumulated drains); ref receives their layout.  With
+// ctx->tc_defer set (and the tile already tuned) it enqueues without a host
+// wait, and the caller reads the error flag with dgpu_tc_check after the run.
 int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const uint64_t *dv,
                  const uint64_t *dw, const float *w, const int64_t *h_type_start,
                  int32_t ntype, const BoxSpec &box, const dgpu_opts *op, DevBuf &part,

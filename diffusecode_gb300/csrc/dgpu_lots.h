@@ -33,10 +33,11 @@ struct LotPlan {
     std::vector<int32_t> shape;        // host copy of the shape's cells (3 per cell)
 };
 int dgpu_lot_plan(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *op, int32_t ngroup, LotPlan &lp);
-// Atoms of lots [lot0, lot0+nlot) into ctx->lpos / ltype / locc, types
-// L*ngroup + group (0 = empty slot); *nslots = nlot * per_lot.
+// Atoms of lots [lot0, lot0+nlot) into ctx->lpos / ltype / locc from slot
+// slot0 on (the caller sizes the buffers), types L*ngroup + group (0 = empty
+// slot); *nslots = nlot * per_lot.
 int dgpu_lot_gather(dgpu_ctx *ctx, const LotPlan &lp, int64_t lot0, int32_t nlot, const double *pos,
-                    const int32_t *geff, const float *aocc, int64_t *nslots);
+                    const int32_t *geff, const float *aocc, int64_t slot0, int64_t *nslots);
 
 // epilogue of the lots
 int dgpu_group_factors(dgpu_ctx *ctx, const FormSpec &fs, const BoxSpec &box, const int32_t *istl,

@@ -273,17 +273,17 @@ __global__ void k_lot_gather(LotGeom g, int64_t lot0, int32_t nlot, const int32_
 }
 
 int dgpu_lot_gather(dgpu_ctx *ctx, const LotPlan &lp, int64_t lot0, int32_t nlot, const double *pos,
-                    const int32_t *geff, const float *aocc, int64_t *nslots)
+                    const int32_t *geff, const float *aocc, int64_t slot0, int64_t *nslots)
 {
     const int64_t m = (int64_t)nlot * lp.geo.per_lot;
     *nslots = m;
-    DGPU_CUDA(ctx, ctx->lpos.ensure((size_t)(m > 0 ? m : 1) * 3 * sizeof(double)));
-    DGPU_CUDA(ctx, ctx->ltype.ensure((size_t)(m > 0 ? m : 1) * sizeof(int32_t)));
-    DGPU_CUDA(ctx, ctx->locc.ensure((size_t)(m > 0 ? m : 1) * sizeof(float)));
     if (m == 0) return DGPU_OK;
+    if ((size_t)(slot0 + m) * 3 * sizeof(double) > ctx->lpos.cap ||
+        (size_t)(slot0 + m) * sizeof(int32_t) > ctx->ltype.cap || (size_t)(slot0 + m) * sizeof(float) > ctx->locc.cap)
+        return dgpu_set_error(ctx, DGPU_ERR_ARG, "lot buffers hold fewer than %lld slots", (long long)(slot0 + m));
     k_lot_gather<<<(unsigned)dgpu_cdiv(m, 256), 256, 0, ctx->stream>>>(
-        lp.geo, lot0, nlot, lp.d_orig, lp.d_shape, lp.d_member, pos, geff, aocc, ctx->lpos.as<double>(),
-        ctx->ltype.as<int32_t>(), ctx->locc.as<float>());
+        lp.geo, lot0, nlot, lp.d_orig, lp.d_shape, lp.d_member, pos, geff, aocc, ctx->lpos.as<double>() + 3 * slot0,
+        ctx->ltype.as<int32_t>() + slot0, ctx->locc.as<float>() + slot0);
     DGPU_CUDA(ctx, cudaGetLastError());
     return DGPU_OK;
 }

@@ -216,30 +216,42 @@ __global__ void k_scatter_atoms(const double *pos, const int32_t *iscat, const f
     idx[dst] = (int32_t)i;
 }
 
-int dgpu_prepare_atoms(dgpu_ctx *ctx, const double *d_pos, const int32_t *d_iscat,
-                       const float *d_aocc, int64_t natoms, int32_t nscat, const PhaseGeom &g,
-                       const FoldSpec &fs, DevBuf &ph0, DevBuf &du, DevBuf &dv, DevBuf &dw,
-                       DevBuf &w, int64_t *h_type_start)
+size_t dgpu_prepare_region_bytes(int64_t natoms, int32_t nscat)
+{
+    const int64_t nblk = natoms > PREP_BLK ? dgpu_cdiv(natoms, PREP_BLK) : 1;
+    const size_t cnt = ((size_t)(nblk * nscat) * sizeof(int32_t) + 255) & ~(size_t)255;
+    const size_t off = ((size_t)(nblk * nscat) * sizeof(int64_t) + 255) & ~(size_t)255;
+    return cnt + off + (((2 * MAXT + 4) * sizeof(int64_t) + 255) & ~(size_t)255);
+}
+
+PrepRegion dgpu_prepare_region(void *base, int64_t natoms, int32_t nscat)
+{
+    PrepRegion r;
+    r.nblk = natoms > PREP_BLK ? dgpu_cdiv(natoms, PREP_BLK) : 1;
+    const size_t cnt = ((size_t)(r.nblk * nscat) * sizeof(int32_t) + 255) & ~(size_t)255;
+    const size_t off = ((size_t)(r.nblk * nscat) * sizeof(int64_t) + 255) & ~(size_t)255;
+    r.counts = (int32_t *)base;
+    r.offs = (int64_t *)((char *)base + cnt);
+    r.d_ts = (int64_t *)((char *)base + cnt + off);
+    return r;
+}
+
+int dgpu_prepare_count(dgpu_ctx *ctx, const int32_t *d_iscat, int64_t natoms, int32_t nscat, const FoldSpec &fs,
+                       const PrepRegion &r)
 {
     if (nscat < 1 || nscat >= MAXT)
         return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "nscat=%d outside 1..%d", nscat, MAXT - 1);
-    int64_t nblk = dgpu_cdiv(natoms, PREP_BLK);
-    if (nblk < 1) nblk = 1;
-    int64_t len = nblk * nscat;
-    size_t cnt_bytes = ((size_t)len * sizeof(int32_t) + 255) & ~(size_t)255;
-    DGPU_CUDA(ctx, ctx->counts.ensure(cnt_bytes + (size_t)len * sizeof(int64_t)));
-    int32_t *counts = ctx->counts.as<int32_t>();
-    int64_t *offs = (int64_t *)((char *)ctx->counts.p + cnt_bytes);
-    DGPU_CUDA(ctx, ctx->type_start.ensure((2 * MAXT + 4) * sizeof(int64_t)));
-    int64_t *d_ts = ctx->type_start.as<int64_t>();
-    k_type_count<<<(unsigned)nblk, PREP_BLK, 0, ctx->stream>>>(d_iscat, natoms, nscat, fs, counts, nblk);
+    k_type_count<<<(unsigned)r.nblk, PREP_BLK, 0, ctx->stream>>>(d_iscat, natoms, nscat, fs, r.counts, r.nblk);
     DGPU_CUDA(ctx, cudaGetLastError());
-    k_scan_counts<<<1, 1024, 0, ctx->stream>>>(counts, len, offs, nblk, nscat, d_ts);
+    k_scan_counts<<<1, 1024, 0, ctx->stream>>>(r.counts, r.nblk * nscat, r.offs, r.nblk, nscat, r.d_ts);
     DGPU_CUDA(ctx, cudaGetLastError());
-    DGPU_CUDA(ctx, cudaMemcpyAsync(h_type_start, d_ts, (2 * nscat + 1) * sizeof(int64_t),
-                                   cudaMemcpyDeviceToHost, ctx->stream));
-    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    int64_t total = h_type_start[nscat];
+    return DGPU_OK;
+}
+
+int dgpu_prepare_scatter(dgpu_ctx *ctx, const double *d_pos, const int32_t *d_iscat, const float *d_aocc,
+                         int64_t natoms, int32_t nscat, const PhaseGeom &g, const FoldSpec &fs, const PrepRegion &r,
+                         int64_t total, DevBuf &ph0, DevBuf &du, DevBuf &dv, DevBuf &dw, DevBuf &w)
+{
     size_t cap = (size_t)(total > 0 ? total : 1);
     DGPU_CUDA(ctx, ph0.ensure(cap * 8));
     DGPU_CUDA(ctx, du.ensure(cap * 8));
@@ -254,11 +266,29 @@ int dgpu_prepare_atoms(dgpu_ctx *ctx, const double *d_pos, const int32_t *d_isca
     DGPU_CUDA(ctx, cudaMemsetAsync(w.p, 0, cap * 4, ctx->stream));
     DGPU_CUDA(ctx, ctx->aidx.ensure(cap * 4));
     DGPU_CUDA(ctx, cudaMemsetAsync(ctx->aidx.p, 0xFF, cap * 4, ctx->stream));   // padding: -1
-    k_scatter_atoms<<<(unsigned)nblk, PREP_BLK, 0, ctx->stream>>>(
-        d_pos, d_iscat, d_aocc, natoms, nscat, fs, g, offs, nblk, ph0.as<uint64_t>(),
+    k_scatter_atoms<<<(unsigned)r.nblk, PREP_BLK, 0, ctx->stream>>>(
+        d_pos, d_iscat, d_aocc, natoms, nscat, fs, g, r.offs, r.nblk, ph0.as<uint64_t>(),
         du.as<uint64_t>(), dv.as<uint64_t>(), dw.as<uint64_t>(), w.as<float>(), ctx->aidx.as<int32_t>());
     DGPU_CUDA(ctx, cudaGetLastError());
     return DGPU_OK;
+}
+
+int dgpu_prepare_atoms(dgpu_ctx *ctx, const double *d_pos, const int32_t *d_iscat,
+                       const float *d_aocc, int64_t natoms, int32_t nscat, const PhaseGeom &g,
+                       const FoldSpec &fs, DevBuf &ph0, DevBuf &du, DevBuf &dv, DevBuf &dw,
+                       DevBuf &w, int64_t *h_type_start)
+{
+    if (nscat < 1 || nscat >= MAXT)
+        return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "nscat=%d outside 1..%d", nscat, MAXT - 1);
+    DGPU_CUDA(ctx, ctx->counts.ensure(dgpu_prepare_region_bytes(natoms, nscat)));
+    const PrepRegion r = dgpu_prepare_region(ctx->counts.p, natoms, nscat);
+    int rc = dgpu_prepare_count(ctx, d_iscat, natoms, nscat, fs, r);
+    if (rc) return rc;
+    DGPU_CUDA(ctx, cudaMemcpyAsync(h_type_start, r.d_ts, (2 * nscat + 1) * sizeof(int64_t),
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return dgpu_prepare_scatter(ctx, d_pos, d_iscat, d_aocc, natoms, nscat, g, fs, r, h_type_start[nscat], ph0, du,
+                                dv, dw, w);
 }
 
 __global__ void k_lattice(int64_t ncell, int32_t i0, int32_t i1, double d0, double d1, double d2,

@@ -1063,12 +1063,22 @@ int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *o
     }
     const size_t pbytes = ((size_t)nprob * sizeof(TcProblem) + 255) & ~(size_t)255;
     DGPU_CUDA(ctx, desc.ensure(pbytes + (size_t)items * sizeof(int32_t) + 256));
-    DGPU_CUDA(ctx, cudaMemcpyAsync(desc.p, plan.probs.data(), (size_t)nprob * sizeof(TcProblem),
-                                   cudaMemcpyHostToDevice, ctx->stream));
-    DGPU_CUDA(ctx, cudaMemcpyAsync((char *)desc.p + pbytes, plan.item_prob.data(), (size_t)items * sizeof(int32_t),
-                                   cudaMemcpyHostToDevice, ctx->stream));
-    // the host vectors must outlive the copies
-    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (ctx->tc_defer) {
+        // one copy from pinned memory that stays valid until the run's host wait
+        char *h = static_cast<char *>(ctx->stage.take(pbytes + (size_t)items * sizeof(int32_t)));
+        if (!h) return dgpu_set_error(ctx, DGPU_ERR_NOMEM, "pinned staging memory");
+        memcpy(h, plan.probs.data(), (size_t)nprob * sizeof(TcProblem));
+        memcpy(h + pbytes, plan.item_prob.data(), (size_t)items * sizeof(int32_t));
+        DGPU_CUDA(ctx, cudaMemcpyAsync(desc.p, h, pbytes + (size_t)items * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                       ctx->stream));
+    } else {
+        DGPU_CUDA(ctx, cudaMemcpyAsync(desc.p, plan.probs.data(), (size_t)nprob * sizeof(TcProblem),
+                                       cudaMemcpyHostToDevice, ctx->stream));
+        DGPU_CUDA(ctx, cudaMemcpyAsync((char *)desc.p + pbytes, plan.item_prob.data(),
+                                       (size_t)items * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+        // the host vectors must outlive the copies
+        DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
     TcLaunch &L = plan.L;
     L.probs = (const TcProblem *)desc.p;
     L.item_prob = (const int32_t *)((char *)desc.p + pbytes);
@@ -1117,7 +1127,7 @@ int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *o
 
 int dgpu_tc_launch(dgpu_ctx *ctx, const TcPlan &plan, bool timed)
 {
-    DGPU_CUDA(ctx, cudaMemsetAsync(plan.L.err, 0, sizeof(int32_t), ctx->stream));
+    if (!ctx->tc_defer) DGPU_CUDA(ctx, cudaMemsetAsync(plan.L.err, 0, sizeof(int32_t), ctx->stream));
     if (plan.L.nitems < 1) return DGPU_OK;
     if (plan.vimg)
         for (const TcProblem &g : plan.probs) {
@@ -1259,11 +1269,11 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
     TcPlan plan;
     rc = dgpu_tc_plan(ctx, 1, &in, op, choice.N, choice.slice_mult, plan, part, ctx->tc_part, &ctx->tc_vimg);
     if (rc) return rc;
-    rc = dgpu_tc_launch(ctx, plan, true);
+    rc = dgpu_tc_launch(ctx, plan, !ctx->tc_defer);
     if (rc) return rc;
-    rc = dgpu_tc_check(ctx);
-    if (rc) return rc;
-    {
+    if (!ctx->tc_defer) {
+        rc = dgpu_tc_check(ctx);
+        if (rc) return rc;
         float ms = 0.f;
         DGPU_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]));
         ctx->tc_kernel_ms = ms;
