@@ -250,7 +250,12 @@ static int lots_sums(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *op,
     const int64_t per_lot = lp.geo.per_lot;
     const int64_t nchunk = dgpu_cdiv(lp.nlots, lp.per_chunk);
     const int64_t chunk_slots = (int64_t)lp.per_chunk * per_lot;
-    const int64_t cpb = chunk_slots > 0 && LOT_BATCH_SLOTS / chunk_slots > 1 ? LOT_BATCH_SLOTS / chunk_slots : 1;
+    int64_t batch_slots = LOT_BATCH_SLOTS;
+    if (const char *e = getenv("DGPU_LOT_BATCH_SLOTS")) {      // smaller batches (results are the same)
+        const long long v = atoll(e);
+        if (v > 0) batch_slots = v;
+    }
+    const int64_t cpb = chunk_slots > 0 && batch_slots / chunk_slots > 1 ? batch_slots / chunk_slots : 1;
     const FoldSpec nofold = {0, 1, {1, 1, 1}, {0, 0, 0}, nullptr};
     int rc;
     for (int64_t c0 = 0; c0 < nchunk; c0 += cpb) {

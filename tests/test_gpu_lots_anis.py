@@ -77,9 +77,10 @@ def test_lots_anis_ref22(oracle, ctx, name):
     assert K.rel_err(r.dsi, dsi, K.incoherent_floor(cr, g, K.opts(ldbw=0))) <= TOL
 
 
-def test_many_lots_chunked(oracle, ctx):
+def test_many_lots_chunked(oracle, ctx, monkeypatch):
     """More (lot, group) pairs than one engine launch takes (63): 40 lots of
-    3 groups run in two chunks."""
+    3 groups run in two chunks, counted together in one batch, or (a batch
+    limit of one slot) as one batch each, with the same result."""
     cr, g = S.small_lots_anis(anis=True, icc=(6, 5, 4), inc=(9, 9, 5))
     rng = np.random.default_rng(11)
     origins = np.stack([rng.integers(1, cr.icc[k] + 1, size=40) for k in range(3)], axis=1)
@@ -90,6 +91,11 @@ def test_many_lots_chunked(oracle, ctx):
         assert rc == 0 and r.status == 0
         assert K.rel_err(r.dsi, dsi, K.incoherent_floor(cr, g, K.opts(ldbw=0))) <= TOL
         assert np.abs(r.csf - csf).max() <= 3e-5 * (np.abs(csf).max() + np.abs(acsf).max())
+        monkeypatch.setenv("DGPU_LOT_BATCH_SLOTS", "1")
+        r1 = FR.four_run(cr, g, op, ctx=ctx, lot_origins=origins)
+        monkeypatch.delenv("DGPU_LOT_BATCH_SLOTS")
+        assert r1.status == 0 and r1.info.pairs == r.info.pairs
+        assert np.array_equal(r1.dsi, r.dsi) and np.array_equal(r1.csf, r.csf)
 
 
 def _status(fn):
