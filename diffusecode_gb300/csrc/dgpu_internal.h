@@ -131,6 +131,10 @@ struct dgpu_ctx {
     // cleared once before the run and read after it.
     int tc_defer = 0;
     HostArena stage;
+    // per-device facts set on first use by this context (a process may hold
+    // contexts on several GPUs): tensor cores present, shared-memory opt-ins
+    int tc_avail = -1;
+    bool tc_attr = false, adj_attr = false;
     std::vector<cudaEvent_t> run_ev;        // event pairs around the launches of such a run
 };
 

@@ -530,9 +530,10 @@ void dgpu_adjtc_plan(dgpu_ctx *ctx, const BoxSpec &box, const dgpu_grid *grid, i
                 }
     plan.nimg = (int64_t)nscat * g.rtiles * g.nstage;
     plan.nscat = nscat;
-    static bool attr_set = false;     // set once, outside any stream capture
-    if (!attr_set && cudaFuncSetAttribute(k_adjtc, cudaFuncAttributeMaxDynamicSharedMemorySize, AT_SMEM) == cudaSuccess)
-        attr_set = true;
+    // once per context (and device), outside any stream capture
+    if (!ctx->adj_attr &&
+        cudaFuncSetAttribute(k_adjtc, cudaFuncAttributeMaxDynamicSharedMemorySize, AT_SMEM) == cudaSuccess)
+        ctx->adj_attr = true;
 }
 
 size_t dgpu_adjtc_img_bytes(const AdjTcPlan &plan) { return (size_t)plan.nimg * AT_Q_BYTES; }

@@ -897,12 +897,11 @@ __global__ void __launch_bounds__(256) k_tc_vgen(const uint64_t *__restrict__ da
 // ---------------------------------------------------------------------------
 bool dgpu_tc_available(dgpu_ctx *ctx)
 {
-    static int cached = -1;
-    if (cached < 0) {
+    if (ctx->tc_avail < 0) {
         cudaDeviceProp p;
-        cached = (cudaGetDeviceProperties(&p, ctx->device) == cudaSuccess && p.major == 10) ? 1 : 0;
+        ctx->tc_avail = (cudaGetDeviceProperties(&p, ctx->device) == cudaSuccess && p.major == 10) ? 1 : 0;
     }
-    return cached == 1;
+    return ctx->tc_avail == 1;
 }
 
 static uint32_t pow2_cols(int n)
@@ -1110,15 +1109,14 @@ int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *o
     L.tmem_cols = pow2_cols(2 * N * (1 + L.nbuf + L.tsum));
     if (L.stages < 2 || L.tmem_cols > 512) return dgpu_set_error(ctx, DGPU_ERR_ARG, "tile does not fit");
     plan.smem = (size_t)L.stages * stage_bytes + (L.vring ? (size_t)TC_VSLOTS * vbytes : 0) + bar_bytes;
-    static bool attr_set = false;     // set once, outside any stream capture
-    if (!attr_set) {
+    if (!ctx->tc_attr) {              // once per context (and device), outside any stream capture
         DGPU_CUDA(ctx, cudaFuncSetAttribute(k_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
         DGPU_CUDA(ctx, cudaFuncSetAttribute(k_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
         DGPU_CUDA(ctx, cudaFuncSetAttribute(k_tc_vgen<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             227 * 1024));
         DGPU_CUDA(ctx, cudaFuncSetAttribute(k_tc_vgen<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             227 * 1024));
-        attr_set = true;
+        ctx->tc_attr = true;
     }
     DGPU_CUDA(ctx, ctx->flag.ensure(64));
     L.err = ctx->flag.as<int32_t>() + 8;
