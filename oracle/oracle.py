@@ -174,11 +174,14 @@ def chi2_grad(cr, grid, opts, i_target, weight=None, nthreads=0):
     return float(chi2[0]), gp.reshape(-1, 3), go
 
 
-def time_ref_rows(cr, grid, row_lo, row_hi, nthreads=0):
-    """Seconds and pairs for the REF22 type sums over abscissa rows [lo,hi)."""
+def time_ref_rows(cr, grid, row_lo, row_hi, nthreads=0, natoms=None):
+    """Seconds and pairs for the REF22 type sums over abscissa rows [lo,hi)
+    (over the first natoms atoms when given)."""
     if nthreads <= 0:
         nthreads = os.cpu_count() or 1
     c = cr.to_c()
+    if natoms is not None:
+        c.natoms = min(int(natoms), int(c.natoms))
     g = grid.to_c()
     pairs = C.c_int64(0)
     sec = lib().oc_time_ref_rows(C.byref(c), C.byref(g), int(row_lo), int(row_hi), int(nthreads),
