@@ -168,7 +168,7 @@ int dgpu_lmn_host(const double eck[12], const double vi[9], const int32_t inc[3]
 // Stable gather of atoms by type into phase data.  If fold != 0, atoms are
 // folded into their unit cell (four_aver) and only selected cells are kept.
 // h_type_start receives 2*nscat+1 values: the start of each type's range
-// (multiples of 32; the gaps are zero-weight padding), the padded total, and
+// (multiples of 64; the gaps are zero-weight padding), the padded total, and
 // the real atom count of each type.
 struct FoldSpec {
     int32_t fold;
