@@ -520,7 +520,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
         }
     } else if (warp < TC_PROD_WARPS) {
         // ------------------------------------------------------------ producers
-        // Atom groups are complete (type ranges padded to 32 atoms with zero
+        // Atom groups are complete (type ranges padded to 64 atoms with zero
         // weight).  Their phase data is staged in shared memory with cp.async
         // one group ahead; three slots, so that a slot is rewritten only after
         // every producer has passed the barrier that follows its last use.
