@@ -3,7 +3,7 @@
 Tolerances: integer work (increments, istl, lmn) is bit-exact; tables are
 FP64 (1e-14); type sums use FP32 phasors with FP64 reduction, so
 intensities are compared as max |I - I_ref| / (I_ref + N<|f|^2>) <= 1e-5
-(the BASELINE accuracy target) -- REF22 against the oracle's REF22 (same
+(the headline metric's accuracy bound) -- REF22 against the oracle's REF22 (same
 2^-16-turn phase table), EXACT64 against the oracle's exact FP64 sums.
 """
 import ctypes as C
