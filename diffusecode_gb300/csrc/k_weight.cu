@@ -89,7 +89,7 @@ static double weight_scale(const dgpu_crystal *cr, const dgpu_grid *g, const dgp
         // planes: the flat axis gets (1,1,1) with the components used by the
         // two grid vectors zeroed.  The reference's third test repeats
         // num(3)==1, so a plane with num(1)==1 reaches no branch there and
-        // its bases stay undefined; this build takes the evident intent.
+        // its bases stay undefined; here the plane takes the evident intent.
         int flat = num[2] == 1 ? 2 : num[1] == 1 ? 1 : 0;
         const int a0 = flat == 0 ? 1 : 0, a1 = flat == 2 ? 1 : 2;
         const double *vv[3] = {uin, vin, win};

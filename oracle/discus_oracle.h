@@ -2,8 +2,8 @@
  * CPU oracle of DISCUS's Fourier path -- TEST INFRASTRUCTURE ONLY.
  *
  * Only tests/, __graft_entry__.smoke() and bench.py (cpu_baseline leg and the
- * --impl reference arm) may load this library, and only as the checker or the
- * timed CPU baseline.  The product path (diffusecode_gb300) never calls it.
+ * --impl reference arm) may load this library, and only as the reference for
+ * comparisons or the timed CPU baseline.  The product path (diffusecode_gb300) never calls it.
  *
  * PARITY UNPINNED: the reference (Fortran) cannot be compiled in this
  * environment (no Fortran compiler) and ships no tests, golden vectors or

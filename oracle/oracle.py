@@ -1,7 +1,7 @@
 """ctypes wrapper of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
 
 Used by tests/, __graft_entry__.smoke() and bench.py's CPU legs as the
-checker / timed CPU baseline; never by the product package.
+reference for comparisons / timed CPU baseline; never by the product package.
 Parity unpinned (see discus_oracle.h).
 """
 import ctypes as C
