@@ -279,17 +279,24 @@ static int lots_sums(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *op,
         DGPU_CUDA(ctx, ctx->ltype.ensure(ns * sizeof(int32_t)));
         DGPU_CUDA(ctx, ctx->locc.ensure(ns * sizeof(float)));
         DGPU_CUDA(ctx, ctx->counts.ensure(rbytes));
-        for (LotChunk &k : ch) {
+        // type ranges land in pinned memory, so that their copies do not wait for the stream one by one
+        const size_t tsn = sizeof(LotChunk::ts) / sizeof(int64_t);
+        int64_t *hts = static_cast<int64_t *>(ctx->stage.take((size_t)nc * tsn * sizeof(int64_t)));
+        if (!hts) return dgpu_set_error(ctx, DGPU_ERR_NOMEM, "pinned staging memory");
+        for (int64_t i = 0; i < nc; i++) {
+            const LotChunk &k = ch[(size_t)i];
             int64_t m = 0;
             rc = dgpu_lot_gather(ctx, lp, k.lot0, k.nl, cr->pos, eiscat, cr->atom_occ, k.slot0, &m);
             if (rc) return rc;
             const PrepRegion r = dgpu_prepare_region((char *)ctx->counts.p + k.reg, k.m, k.ntype);
             rc = dgpu_prepare_count(ctx, ctx->ltype.as<int32_t>() + k.slot0, k.m, k.ntype, nofold, r);
             if (rc) return rc;
-            DGPU_CUDA(ctx, cudaMemcpyAsync(k.ts, r.d_ts, (2 * k.ntype + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost,
-                                           ctx->stream));
+            DGPU_CUDA(ctx, cudaMemcpyAsync(hts + i * tsn, r.d_ts, (2 * k.ntype + 1) * sizeof(int64_t),
+                                           cudaMemcpyDeviceToHost, ctx->stream));
         }
         DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));        // the type ranges of every chunk
+        for (int64_t i = 0; i < nc; i++)
+            memcpy(ch[(size_t)i].ts, hts + i * tsn, (2 * ch[(size_t)i].ntype + 1) * sizeof(int64_t));
         ctx->stage.reset();
         // the largest chunk sizes the atom buffers before the run
         int64_t most = 1;
