@@ -501,6 +501,59 @@ __global__ void k_lot_combine(int32_t ngroup, int32_t nlot, BoxSpec box, const P
     dsi[idx] += acc;
 }
 
+// k_lot_combine for FP32 partials with nq = ngroup * nslice partials per lot
+// known at compile time: partial q = g * nslice + k of lot L sits at
+// (L * NQ + q) * slab, and LB lots' partials are loaded before any is used,
+// so that each thread keeps about eight loads in flight (the kernel reads
+// nlot * nq partials per point and is bound by those reads).  For nslice = 1
+// the arithmetic is the generic kernel's, operation for operation.
+template <int NQ>
+__global__ void k_lot_combine_f32(int32_t nslice, int32_t nlot, BoxSpec box, const float2 *__restrict__ part,
+                                  PartLayout lay, const double2 *__restrict__ fac, const double2 *__restrict__ acsf,
+                                  double2 *__restrict__ csf, double *__restrict__ dsi, int32_t last)
+{
+    constexpr int LB = NQ >= 8 ? 1 : 8 / NQ;
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t i, j, l;
+    if (r >= lay.nthr || !part_point(lay, box, r, i, j, l)) return;
+    const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    const int64_t pb = i + (int64_t)box.f[0] * (j + (int64_t)box.f[1] * l);
+    const int64_t idx = i + (int64_t)box.num[0] * (j + (int64_t)box.num[1] * l);
+    const double2 a = acsf ? acsf[idx] : make_double2(0.0, 0.0);
+    const float2 *p0 = part + i * lay.s0 + j * lay.s1 + l * lay.s2;
+    const int64_t slab = lay.slab;
+    float2 fq[NQ];                         // the group factor of each partial of a lot
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+        const double2 f = fac[(int64_t)(q / nslice) * nb + pb];
+        fq[q] = make_float2((float)f.x, (float)f.y);
+    }
+    double acc = 0.0;
+    for (int L0 = 0; L0 < nlot; L0 += LB) {
+        float2 v[LB][NQ];
+#pragma unroll
+        for (int b = 0; b < LB; b++)
+#pragma unroll
+            for (int q = 0; q < NQ; q++)
+                v[b][q] = L0 + b < nlot ? __ldg(p0 + ((int64_t)(L0 + b) * NQ + q) * slab) : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int b = 0; b < LB; b++) {
+            if (L0 + b < nlot) {
+                float fr = 0.f, fi = 0.f;
+#pragma unroll
+                for (int q = 0; q < NQ; q++) {
+                    fr = fmaf(v[b][q].x, fq[q].x, fmaf(-v[b][q].y, fq[q].y, fr));
+                    fi = fmaf(v[b][q].x, fq[q].y, fmaf(v[b][q].y, fq[q].x, fi));
+                }
+                const double2 F = make_double2((double)fr - a.x, (double)fi - a.y);
+                acc += F.x * F.x + F.y * F.y;
+                if (L0 + b == last) csf[idx] = F;
+            }
+        }
+    }
+    dsi[idx] += acc;
+}
+
 // dsi *= dscale, csf *= cscale on the box (lot normalisation and diff_scale)
 __global__ void k_lot_scale(BoxSpec box, double2 *__restrict__ csf, double *__restrict__ dsi, double dscale,
                             double cscale)
@@ -537,7 +590,18 @@ int dgpu_lot_combine(dgpu_ctx *ctx, int32_t ngroup, int32_t nlot, const BoxSpec 
     const PartLayout lay = layout_of(r, box);
     const unsigned nblk = (unsigned)dgpu_cdiv(lay.nthr, 256);
     const int32_t nslice = r.nslice > 0 ? r.nslice : 1;
-    if (r.f32)
+    const int32_t nq = ngroup * nslice;
+    if (r.f32 && r.p && nq >= 1 && nq <= 8) {
+        const float2 *p = (const float2 *)r.p;
+        switch (nq) {
+#define LOT_F32(Q)                                                                                              \
+    case Q:                                                                                                     \
+        k_lot_combine_f32<Q><<<nblk, 256, 0, ctx->stream>>>(nslice, nlot, box, p, lay, fac, acsf, csf, dsi, last); \
+        break;
+            LOT_F32(1) LOT_F32(2) LOT_F32(3) LOT_F32(4) LOT_F32(5) LOT_F32(6) LOT_F32(7) LOT_F32(8)
+#undef LOT_F32
+        }
+    } else if (r.f32)
         k_lot_combine<float2><<<nblk, 256, 0, ctx->stream>>>(ngroup, nlot, box, (const float2 *)r.p, nslice, lay,
                                                               fac, acsf, csf, dsi, last);
     else
