@@ -102,10 +102,18 @@ __global__ void k_combine(const FormSpec *fs, BoxSpec box, const P *__restrict__
     for (int t = 1; t <= fs->ngroup; t++) {
         double2 s = make_double2(0.0, 0.0);
         const P *pt = part + (int64_t)(t - 1) * nslice * lay.slab + i * lay.s0 + j * lay.s1 + l * lay.s2;
-        for (int k = 0; k < nslice; k++) {
-            double2 v = ld_part(pt + (int64_t)k * lay.slab);
-            s.x += v.x;
-            s.y += v.y;
+        // eight slices loaded before any is added (loads in flight), added in slice order
+        for (int k0 = 0; k0 < nslice; k0 += 8) {
+            double2 v[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++)
+                v[u] = k0 + u < nslice ? ld_part(pt + (int64_t)(k0 + u) * lay.slab) : make_double2(0.0, 0.0);
+#pragma unroll
+            for (int u = 0; u < 8; u++)
+                if (k0 + u < nslice) {
+                    s.x += v[u].x;
+                    s.y += v[u].y;
+                }
         }
         double2 c = form_group(fs, cfact, q, t, h);
         double2 m = cmul(s, c);
