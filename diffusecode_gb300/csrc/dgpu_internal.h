@@ -241,6 +241,7 @@ struct TcProblem {
     const uint64_t *ph0, *dra, *drb, *dac;   // phase data along the row axes and the column axis
     const float *w;
     const float2 *ma, *mc;   // per-atom exp(2 pi i 8 d) along ra and ac
+    const float2 *ma2, *mc2; // per-atom exp(2 pi i 16 d) along ra and ac
     uint8_t *vimg;           // B rows of every (atom group, column tile), or null: generated in-kernel;
                              // problems with the same atoms and column steps share one set
     float2 *part;            // part[(t*nslice+ks)*slab + c*nrows_p + rg]
@@ -259,11 +260,14 @@ struct TcLaunch {
 };
 
 #include <vector>
+// Step factors per atom: exp(2 pi i 8 d) along the three grid axes, then
+// exp(2 pi i 16 d) along them (dgpu_tc_mult_async).
+#define TC_MULT_ARRAYS 6
 // One problem's inputs for a tensor-core launch.
 struct TcInput {
     const uint64_t *ph0, *du, *dv, *dw;
     const float *w;
-    const float2 *mult;       // step factors: mult[axis * mult_stride + atom]
+    const float2 *mult;       // step factors: mult[k * mult_stride + atom], k < TC_MULT_ARRAYS
     int64_t mult_stride;
     const int64_t *ts;        // host: padded type ranges (ntype + 1 values)
     int32_t ntype;

@@ -298,7 +298,7 @@ static int batch_build(dgpu_ctx *ctx, BatchState &B, int32_t nc, const dgpu_crys
     DGPU_CUDA(ctx, B.d_dv.ensure(npd * 8));
     DGPU_CUDA(ctx, B.d_dw.ensure(npd * 8));
     DGPU_CUDA(ctx, B.d_w.ensure(npd * 4));
-    DGPU_CUDA(ctx, B.d_mult.ensure(npd * 3 * sizeof(float2)));
+    DGPU_CUDA(ctx, B.d_mult.ensure(npd * TC_MULT_ARRAYS * sizeof(float2)));
     DGPU_CUDA(ctx, B.d_idx.ensure(npd * 4));
     DGPU_CUDA(ctx, B.d_cnt.ensure((size_t)(cnt > 0 ? cnt : 1) * 4));
     DGPU_CUDA(ctx, B.d_offs.ensure((size_t)(cnt > 0 ? cnt : 1) * 8));

@@ -192,7 +192,7 @@ static int powder_tc_slabs(dgpu_ctx *ctx, const dgpu_crystal &dc, const dgpu_opt
     int64_t natoms = 0;
     for (int t = 0; t < nscat; t++) natoms += ts[nscat + 1 + t];
     DGPU_CUDA(ctx, ctx->slab_ph0.ensure((size_t)nsl * (npad > 0 ? npad : 1) * sizeof(uint64_t)));
-    DGPU_CUDA(ctx, ctx->tc_mult.ensure((size_t)3 * (npad > 0 ? npad : 1) * sizeof(float2)));
+    DGPU_CUDA(ctx, ctx->tc_mult.ensure((size_t)TC_MULT_ARRAYS * (npad > 0 ? npad : 1) * sizeof(float2)));
     rc = dgpu_tc_mult_async(ctx, ctx->du.as<uint64_t>(), ctx->dv.as<uint64_t>(), ctx->dw.as<uint64_t>(), npad, npad,
                             ctx->tc_mult.as<float2>());
     if (rc) return rc;

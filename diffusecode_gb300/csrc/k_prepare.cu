@@ -169,10 +169,41 @@ __global__ void k_scan_counts(const int32_t *counts, int64_t len, int64_t *offs,
     (void)len;
 }
 
+// A fixed pseudo-random bijection of [0, n): a four-round Feistel network on
+// the smallest even number of bits that covers n, cycle-walked back into
+// [0, n).  The atoms of a type are summed in this order rather than in the
+// crystal's: every K slice and every accumulator chain of the engines is then
+// a random sample of the crystal, so a partial sum is large only where the
+// whole sum is (near a Bragg position, atoms stored cell after cell give
+// partial sums that are coherent and cancel only in the total).
+__device__ __forceinline__ uint32_t slot_perm(uint32_t x, uint32_t n)
+{
+    if (n <= 2) return x;
+    int b = 32 - __clz(n - 1);
+    b += b & 1;
+    const int h = b >> 1;
+    const uint32_t m = (1u << h) - 1u;
+    do {
+        uint32_t l = x >> h, r = x & m;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            uint32_t f = r * 0x9E3779B1u + 0x85EBCA77u * (uint32_t)(k + 1);
+            f ^= f >> 15;
+            f *= 0x2C1B3C6Du;
+            f ^= f >> 12;
+            const uint32_t t = r;
+            r = l ^ (f & m);
+            l = t;
+        }
+        x = (l << h) | r;
+    } while (x >= n);
+    return x;
+}
+
 __global__ void k_scatter_atoms(const double *pos, const int32_t *iscat, const float *aocc,
                                 int64_t n, int32_t nscat, FoldSpec fs, PhaseGeom g,
-                                const int64_t *offs, int64_t nblk, uint64_t *ph0, uint64_t *du,
-                                uint64_t *dv, uint64_t *dw, float *w, int32_t *idx)
+                                const int64_t *offs, int64_t nblk, const int64_t *ts, uint64_t *ph0,
+                                uint64_t *du, uint64_t *dv, uint64_t *dw, float *w, int32_t *idx)
 {
     __shared__ int32_t wcnt[32][MAXT];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -195,7 +226,9 @@ __global__ void k_scatter_atoms(const double *pos, const int32_t *iscat, const f
     }
     __syncthreads();
     if (!t) return;
-    int64_t dst = offs[(int64_t)(t - 1) * nblk + blockIdx.x] + wcnt[wid][t] + rank;
+    // stable rank within the type, then the type's summation order
+    const int64_t rk = offs[(int64_t)(t - 1) * nblk + blockIdx.x] + wcnt[wid][t] + rank - ts[t - 1];
+    const int64_t dst = ts[t - 1] + slot_perm((uint32_t)rk, (uint32_t)ts[nscat + t]);
     double x0 = pos[3 * i], x1 = pos[3 * i + 1], x2 = pos[3 * i + 2];
     if (fs.fold) {
         int64_t c = i / fs.ncatoms;
@@ -267,7 +300,7 @@ int dgpu_prepare_scatter(dgpu_ctx *ctx, const double *d_pos, const int32_t *d_is
     DGPU_CUDA(ctx, ctx->aidx.ensure(cap * 4));
     DGPU_CUDA(ctx, cudaMemsetAsync(ctx->aidx.p, 0xFF, cap * 4, ctx->stream));   // padding: -1
     k_scatter_atoms<<<(unsigned)r.nblk, PREP_BLK, 0, ctx->stream>>>(
-        d_pos, d_iscat, d_aocc, natoms, nscat, fs, g, r.offs, r.nblk, ph0.as<uint64_t>(),
+        d_pos, d_iscat, d_aocc, natoms, nscat, fs, g, r.offs, r.nblk, r.d_ts, ph0.as<uint64_t>(),
         du.as<uint64_t>(), dv.as<uint64_t>(), dw.as<uint64_t>(), w.as<float>(), ctx->aidx.as<int32_t>());
     DGPU_CUDA(ctx, cudaGetLastError());
     return DGPU_OK;
@@ -491,7 +524,7 @@ int dgpu_prepare_async(dgpu_ctx *ctx, const double *d_pos, const int32_t *d_isca
     k_type_count<<<(unsigned)nblk, PREP_BLK, 0, ctx->stream>>>(d_iscat, natoms, nscat, nofold, counts, nblk);
     k_scan_counts<<<1, 1024, 0, ctx->stream>>>(counts, nblk * nscat, offs, nblk, nscat, ts_dev);
     k_scatter_atoms<<<(unsigned)nblk, PREP_BLK, 0, ctx->stream>>>(d_pos, d_iscat, d_aocc, natoms, nscat, nofold, g,
-                                                                  offs, nblk, ph0, du, dv, dw, w, idx);
+                                                                  offs, nblk, ts_dev, ph0, du, dv, dw, w, idx);
     DGPU_CUDA(ctx, cudaGetLastError());
     return DGPU_OK;
 }

@@ -15,10 +15,13 @@
 // generated in the kernel, 32-atom stages) or not at all: with V images
 // (k_tc_vgen, written once per launch) a copy warp streams them into a ring
 // (64-atom stages).  A producer thread evaluates exp(2 pi i phase) at the
-// start of a run of rows (or columns) (MUFU, exact 64-bit phase) and then
-// steps by the per-atom factor exp(2 pi i 8 d) (computed once per atom to
-// about one ulp); a row run restarts from the exact phase wherever nb
-// changes.  Every FP32 value is
+// start of a run of rows (or columns) (from the exact 64-bit phase) and then
+// steps by the per-atom factors exp(2 pi i 8 d) and exp(2 pi i 16 d)
+// (computed once per atom, rounded stochastically); a row run restarts from
+// the exact phase wherever nb changes.  U is evaluated at phase + rot_j and V
+// at phase - rot_j, a pseudo-random offset per atom (tc_rot): the product is
+// the same, but the evaluation errors of atoms at equivalent positions no
+// longer coincide (they would add up coherently).  Every FP32 value is
 // split into hi (the value with its mantissa cut to the fp16 / bf16 width,
 // exact in that format) and lo (the exact remainder, rounded).  V is scaled
 // by 2^12 so that its lo parts stay normal fp16 numbers; all accumulators
@@ -67,11 +70,14 @@
 #define TC_A_BYTES (TC_M * TC_KA * 2)          // one A operand (e.g. Ur_hi): 8 KB
 #define TC_B_BYTES (TC_M * TC_KB * 2)          // one A operand on the V-image path: 16 KB
 // phase data of one 32-atom group in shared memory:
-// ph0, d_ra, d_rb, d_ac (u64), w (f32), step factors along ra and ac (float2)
+// ph0, d_ra, d_rb, d_ac (u64), w (f32), step factors along ra and ac and
+// their squares (float2)
 #define TC_SLOT_W (TC_KA * 32)
 #define TC_SLOT_MA (TC_SLOT_W + TC_KA * 4)
 #define TC_SLOT_MC (TC_SLOT_MA + TC_KA * 8)
-#define TC_ATOM_SLOT (TC_SLOT_MC + TC_KA * 8)
+#define TC_SLOT_MA2 (TC_SLOT_MC + TC_KA * 8)
+#define TC_SLOT_MC2 (TC_SLOT_MA2 + TC_KA * 8)
+#define TC_ATOM_SLOT (TC_SLOT_MC2 + TC_KA * 8)
 #define TC_NSLOT 3
 #define TC_VSLOTS 2                            // V ring: 64-atom images, one stage ahead
 #define TC_BAR_BYTES 256
@@ -115,11 +121,11 @@ __device__ __forceinline__ void decode_item(const TcProblem &g, int64_t item, in
 struct TcSrc {
     const uint64_t *ph0, *dra, *drb, *dac;
     const float *w;
-    const float2 *ma, *mc;
+    const float2 *ma, *mc, *ma2, *mc2;
 };
 
 // Stage the phase data of the 32-atom group starting at padded atom ab into
-// an atom slot: 104 chunks of 16 bytes, one per thread of tid < 104.
+// an atom slot: 136 chunks of 16 bytes, one per thread of tid < 136.
 __device__ __forceinline__ void stage_atoms(const TcSrc &P, uint8_t *dst, int64_t ab, int tid)
 {
     if (tid < 64) {                     // ph0, d_ra, d_rb, d_ac: 16 chunks each
@@ -129,9 +135,11 @@ __device__ __forceinline__ void stage_atoms(const TcSrc &P, uint8_t *dst, int64_
     } else if (tid < 72) {              // w: 8 chunks
         const int ch = tid - 64;
         cp_async16(dst + TC_SLOT_W + ch * 16, P.w + ab + ch * 4);
-    } else if (tid < 104) {             // step factors along ra and ac: 16 chunks each
+    } else if (tid < 136) {             // step factors along ra and ac and their squares: 16 chunks each
         const int arr = (tid - 72) >> 4, ch = (tid - 72) & 15;
-        cp_async16(dst + (arr ? TC_SLOT_MC : TC_SLOT_MA) + ch * 16, (arr ? P.mc : P.ma) + ab + ch * 2);
+        const int off = arr == 0 ? TC_SLOT_MA : arr == 1 ? TC_SLOT_MC : arr == 2 ? TC_SLOT_MA2 : TC_SLOT_MC2;
+        const float2 *src = arr == 0 ? P.ma : arr == 1 ? P.mc : arr == 2 ? P.ma2 : P.mc2;
+        cp_async16(dst + off + ch * 16, src + ab + ch * 2);
     }
     cp_async_commit();
 }
@@ -212,12 +220,13 @@ __device__ __forceinline__ void run_pairs(int q, int qe, float2 (&x0)[4], const 
 // 16 distinct 8-byte bank slots.
 template <bool BF>
 __device__ __forceinline__ void gen_rows(int q0, int q1, int mt, int gpn, const uint8_t *as, uint8_t *A, int s,
-                                         int j)
+                                         int j, int64_t ab)
 {
     const uint64_t *s_ph0 = reinterpret_cast<const uint64_t *>(as);
     const uint64_t *s_dra = s_ph0 + TC_KA, *s_drb = s_dra + TC_KA;
     const float *s_w = reinterpret_cast<const float *>(as + TC_SLOT_W);
     const float2 *s_ma = reinterpret_cast<const float2 *>(as + TC_SLOT_MA);
+    const float2 *s_ma2 = reinterpret_cast<const float2 *>(as + TC_SLOT_MA2);
     const int G0 = mt * (TC_M / 8) + q0;
     int gi = G0 % gpn;
     uint32_t nb = (uint32_t)(G0 / gpn);
@@ -226,7 +235,7 @@ __device__ __forceinline__ void gen_rows(int q0, int q1, int mt, int gpn, const 
 #pragma unroll
     for (int a = 0; a < 4; a++) {
         m[a] = s_ma[k0 + a];
-        m2[a] = cmulf(m[a], m[a]);
+        m2[a] = s_ma2[k0 + a];
     }
     uint8_t *dst = A + sw_off(s, j >> 1) + (j & 1) * 8;
     auto emit = [&](int q, const float2 (&x)[4]) { emit_rows<BF>(dst, q, x); };
@@ -237,7 +246,8 @@ __device__ __forceinline__ void gen_rows(int q0, int q1, int mt, int gpn, const 
 #pragma unroll
         for (int a = 0; a < 4; a++) {
             const int k = k0 + a;
-            const float2 p = phasor_fast(s_ph0[k] + (uint64_t)na * s_dra[k] + (uint64_t)nb * s_drb[k]);
+            const float2 p =
+                phasor_fast(tc_rot((uint64_t)(ab + k)) + s_ph0[k] + (uint64_t)na * s_dra[k] + (uint64_t)nb * s_drb[k]);
             const float wk = s_w[k];
             x[a] = make_float2(p.x * wk, p.y * wk);
         }
@@ -271,6 +281,8 @@ struct AtomPair {
     ulonglong2 ph0, dra, drb;
     float2 w;
     float4 m;               // step factors exp(2 pi i 8 d_ra) of the two atoms
+    float4 m2;              // and exp(2 pi i 16 d_ra)
+    uint64_t rot0, rot1;    // the atoms' phase offsets (tc_rot)
 };
 
 __device__ __forceinline__ void load_pair(AtomPair &r, const TcSrc &P, int64_t k)
@@ -280,6 +292,9 @@ __device__ __forceinline__ void load_pair(AtomPair &r, const TcSrc &P, int64_t k
     r.drb = __ldg(reinterpret_cast<const ulonglong2 *>(P.drb + k));
     r.w = __ldg(reinterpret_cast<const float2 *>(P.w + k));
     r.m = __ldg(reinterpret_cast<const float4 *>(P.ma + k));
+    r.m2 = __ldg(reinterpret_cast<const float4 *>(P.ma2 + k));
+    r.rot0 = tc_rot((uint64_t)k);
+    r.rot1 = tc_rot((uint64_t)k + 1);
 }
 
 // Where the 16 row groups of tile mt start (group G0 = 16 mt at gi0, nb0)
@@ -326,11 +341,12 @@ __device__ __forceinline__ void gen_rows_stm(const RowSeg &rs, const AtomPair &a
     const int s = lane >> 2;
     const uint64_t ph0[2] = {ap.ph0.x, ap.ph0.y}, dra[2] = {ap.dra.x, ap.dra.y}, drb[2] = {ap.drb.x, ap.drb.y};
     const float w[2] = {ap.w.x, ap.w.y};
+    const uint64_t rot[2] = {ap.rot0, ap.rot1};
     float2 m[2], m2[2];
     m[0] = make_float2(ap.m.x, ap.m.y);
     m[1] = make_float2(ap.m.z, ap.m.w);
-#pragma unroll
-    for (int a = 0; a < 2; a++) m2[a] = cmulf(m[a], m[a]);
+    m2[0] = make_float2(ap.m2.x, ap.m2.y);
+    m2[1] = make_float2(ap.m2.z, ap.m2.w);
     // segments of constant nb: bit o of bmask marks group G0 + o as the first
     // of a segment
     const uint32_t gi0 = rs.gi0, nb0 = rs.nb0, bmask = rs.bmask;
@@ -340,7 +356,7 @@ __device__ __forceinline__ void gen_rows_stm(const RowSeg &rs, const AtomPair &a
         const uint32_t nb = nb0 + (uint32_t)__popc(bmask & ((2u << o) - 1u));
 #pragma unroll
         for (int a = 0; a < 2; a++) {
-            const float2 p = phasor_fast(ph0[a] + (uint64_t)na * dra[a] + (uint64_t)nb * drb[a]);
+            const float2 p = phasor_fast(rot[a] + ph0[a] + (uint64_t)na * dra[a] + (uint64_t)nb * drb[a]);
             x[a] = make_float2(p.x * w[a], p.y * w[a]);
         }
     };
@@ -397,19 +413,20 @@ __device__ __forceinline__ void gen_rows_stm(const RowSeg &rs, const AtomPair &a
 // B rows: Vr at c, Vi at N+c, -Vr at 2N+c, in a hi and a lo operand.
 template <bool BF>
 __device__ __forceinline__ void gen_cols(int q0, int q1, int nt, int N, const uint8_t *as, uint8_t *Bh,
-                                         uint32_t b_bytes, int s, int j)
+                                         uint32_t b_bytes, int s, int j, int64_t ab)
 {
     const uint64_t *s_dac = reinterpret_cast<const uint64_t *>(as) + 3 * TC_KA;
     const float2 *s_mc = reinterpret_cast<const float2 *>(as + TC_SLOT_MC);
+    const float2 *s_mc2 = reinterpret_cast<const float2 *>(as + TC_SLOT_MC2);
     const int k0 = 4 * j;
     const uint32_t nc = (uint32_t)(nt * N + q0 * 8 + s);
     float2 x[4], m[4], m2[4];
 #pragma unroll
     for (int a = 0; a < 4; a++) {
-        const float2 p = phasor_fast((uint64_t)nc * s_dac[k0 + a]);
+        const float2 p = phasor_fast((uint64_t)nc * s_dac[k0 + a] - tc_rot((uint64_t)(ab + k0 + a)));
         x[a] = make_float2(p.x * TC_V_SCALE, p.y * TC_V_SCALE);
         m[a] = s_mc[k0 + a];
-        m2[a] = cmulf(m[a], m[a]);
+        m2[a] = s_mc2[k0 + a];
     }
     const uint32_t blk = (uint32_t)(N >> 3) * TC_SBO;           // N rows further
     const uint32_t o0 = sw_off(s, j >> 1) + (j & 1) * 8;
@@ -496,7 +513,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
             const int64_t a1 = min(g.ts[t + 1], a0 + g.slice_len);
             const int nst = a1 > a0 ? (int)((a1 - a0) / TC_KB) : 0;
             if (nst == 0) continue;
-            const TcSrc src = {g.ph0, g.dra, g.drb, g.dac, g.w, g.ma, g.mc};
+            const TcSrc src = {g.ph0, g.dra, g.drb, g.dac, g.w, g.ma, g.mc, g.ma2, g.mc2};
             const RowSeg rs = row_segments(mt, g.fra_p >> 3);
             AtomPair cur, nxt;
             load_pair(cur, src, a0 + kq);
@@ -541,7 +558,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
             if (nst == 0) continue;
             // previous item's slots are free; everybody stops together after a failure
             if (producers_sync(!ok)) break;
-            const TcSrc src = {g.ph0, g.dra, g.drb, g.dac, g.w, g.ma, g.mc};
+            const TcSrc src = {g.ph0, g.dra, g.drb, g.dac, g.w, g.ma, g.mc, g.ma2, g.mc2};
             const int N = g.N, gpn = g.fra_p >> 3;
             // with V images the column groups arrive by bulk copy into the ring
             const uint8_t *vimg = L.vring ? g.vimg : nullptr;
@@ -567,8 +584,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
                     cp_async_commit();
                 const uint8_t *as = aslot + (st % TC_NSLOT) * TC_ATOM_SLOT;
                 uint8_t *A = smem + (size_t)sb * stage_bytes;
-                if (ok && ra0 < ra1) gen_rows<BF>(ra0, ra1, mt, gpn, as, A, s, j);
-                if (ok && rc0 < rc1) gen_cols<BF>(rc0, rc1, nt, N, as, A + 4 * TC_A_BYTES, b_bytes, s, j);
+                const int64_t ab = a0 + (int64_t)st * TC_KA;        // the stage's first atom
+                if (ok && ra0 < ra1) gen_rows<BF>(ra0, ra1, mt, gpn, as, A, s, j, ab);
+                if (ok && rc0 < rc1) gen_cols<BF>(rc0, rc1, nt, N, as, A + 4 * TC_A_BYTES, b_bytes, s, j, ab);
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&full[sb]);   // one arrival per producer warp
@@ -832,9 +850,31 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
     }
 }
 
-// Per-atom step factors exp(2 pi i 8 d) along the three grid axes, to about
-// one ulp: the turn 8d / 2^64 is split into a float part for sincospif and a
-// small remainder applied to first order.
+// FP64 -> FP32 with stochastic rounding: y rounds up with probability equal
+// to its distance from the lower neighbour in units of the spacing (u is a
+// uniform 32-bit draw), so the rounding error has mean zero over draws.
+__device__ __forceinline__ float round_stochastic(double y, uint32_t u)
+{
+    const float lo = __double2float_rd(y), hi = __double2float_ru(y);
+    if (lo == hi) return lo;
+    const double p = (y - (double)lo) / ((double)hi - (double)lo);
+    return (double)u * 0x1p-32 < p ? hi : lo;
+}
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z)
+{
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// Per-atom step factors exp(2 pi i 8 d) and exp(2 pi i 16 d) along the three
+// grid axes: FP64 sincospi of the exact turn, rounded stochastically to FP32
+// (a draw per atom and component).  The producers step a row by these
+// factors up to 16 times, so a factor's rounding error recurs in every value
+// of the chain; atoms at equivalent positions have identical increments, and
+// with round-to-nearest their chains would share one error and add it up
+// coherently.  Stochastic rounding gives each atom its own, zero-mean error.
 __global__ void k_tc_mult(const uint64_t *__restrict__ du, const uint64_t *__restrict__ dv,
                           const uint64_t *__restrict__ dw, int64_t n, int64_t stride, float2 *__restrict__ out)
 {
@@ -843,13 +883,15 @@ __global__ void k_tc_mult(const uint64_t *__restrict__ du, const uint64_t *__res
     const uint64_t *d[3] = {du, dv, dw};
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        const int64_t v = (int64_t)(d[a][i] << 3);
-        const double x = (double)v * 0x1p-63;          // turns x 2, in [-1, 1]
-        const float xf = (float)x;
-        const float dth = (float)((x - (double)xf) * 3.141592653589793);
-        float s, c;
-        sincospif(xf, &s, &c);
-        out[a * stride + i] = make_float2(fmaf(-s, dth, c), fmaf(c, dth, s));
+#pragma unroll
+        for (int k = 0; k < 2; k++) {                   // 8 d, then 16 d
+            const int64_t v = (int64_t)(d[a][i] << (3 + k));
+            double s, c;
+            sincospi((double)v * 0x1p-63, &s, &c);     // angle pi x, x = 2 turns in [-1, 1)
+            const uint64_t r = mix64((uint64_t)i * 8u + (uint64_t)(2 * a + k) + 0x9E3779B97F4A7C15ull);
+            out[(3 * k + a) * stride + i] =
+                make_float2(round_stochastic(c, (uint32_t)r), round_stochastic(s, (uint32_t)(r >> 32)));
+        }
     }
 }
 
@@ -874,7 +916,8 @@ __global__ void __launch_bounds__(256) k_tc_vgen(const uint64_t *__restrict__ da
         float2 x[4];
 #pragma unroll
         for (int a = 0; a < 4; a++) {
-            const float2 p = phasor_fast((uint64_t)nc * dac[gi * TC_KB + 4 * jq + a]);
+            const int64_t j = gi * TC_KB + 4 * jq + a;
+            const float2 p = phasor_acc((uint64_t)nc * dac[j] - tc_rot((uint64_t)j));
             x[a] = make_float2(p.x * TC_V_SCALE, p.y * TC_V_SCALE);
         }
         uint2 rh, rl, ih, il;
@@ -979,6 +1022,8 @@ static void tc_problem(dgpu_ctx *ctx, const TcInput &in, const dgpu_opts *op, in
     g.w = in.w;
     g.ma = in.mult + (int64_t)g.ra * in.mult_stride;
     g.mc = in.mult + (int64_t)axis * in.mult_stride;
+    g.ma2 = in.mult + (int64_t)(3 + g.ra) * in.mult_stride;
+    g.mc2 = in.mult + (int64_t)(3 + axis) * in.mult_stride;
 }
 
 void dgpu_tc_partref(const TcProblem &g, const float2 *p, PartRef &ref)
@@ -1213,7 +1258,7 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
         maxn = n > maxn ? n : maxn;
     }
     const int64_t npad = h_type_start[ntype];
-    DGPU_CUDA(ctx, ctx->tc_mult.ensure((size_t)3 * (npad > 0 ? npad : 1) * sizeof(float2)));
+    DGPU_CUDA(ctx, ctx->tc_mult.ensure((size_t)TC_MULT_ARRAYS * (npad > 0 ? npad : 1) * sizeof(float2)));
     int rc = dgpu_tc_mult_async(ctx, du, dv, dw, npad, npad, ctx->tc_mult.as<float2>());
     if (rc) return rc;
     int lg = 0;

@@ -214,6 +214,31 @@ __device__ __forceinline__ float2 phasor_fast(uint64_t ph)
     return make_float2(c, s);
 }
 
+// A per-atom phase offset (a Weyl sequence over the atom's slot index, in
+// 2^-64 turns).  The tensor-core engine evaluates U at phase + rot and V at
+// phase - rot, so that their product is unchanged while the rounding and
+// approximation errors of the evaluated values differ from atom to atom:
+// atoms at equivalent positions (a perfect lattice, one layer) would
+// otherwise carry identical errors, which add up coherently in their sum.
+__device__ __forceinline__ uint64_t tc_rot(uint64_t j) { return j * 0x9E3779B97F4A7C15ull; }
+
+// exp(2 pi i phase) of a 64-bit fixed-point turn to about one FP32 ulp: the
+// signed phase as x = 2 turns in [-1, 1) splits into its top 24 bits (exact
+// in FP32, evaluated by sincospif) and a remainder below 2^-23 applied as a
+// first-order rotation.  Used where a value is evaluated once per launch (the
+// V operand images); the kernels' seeds use the hardware approximation above,
+// whose error (a few 1e-7, a smooth function of the phase) tc_rot makes
+// random from atom to atom.
+__device__ __forceinline__ float2 phasor_acc(uint64_t ph)
+{
+    const int64_t v = (int64_t)ph;
+    const float xf = (float)(int32_t)(v >> 40) * 0x1p-23f;
+    const float dth = (float)((uint64_t)v & 0xFFFFFFFFFFull) * (3.14159265358979f * 0x1p-63f);
+    float s, c;
+    sincospif(xf, &s, &c);
+    return make_float2(fmaf(-s, dth, c), fmaf(c, dth, s));
+}
+
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b)
 {
     return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
