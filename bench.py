@@ -236,6 +236,163 @@ def fp64_check(cr, grid, dsi, npts=192, seed=7, fave=0.0, split=False):
     return float(np.max(rel)), npts
 
 
+def incoherent_floor(cr, grid, ldbw=1, power=4):
+    """N <|f|^2> at every grid point: sum_t N_t |f_t(s) exp(-B_t s^2) occ_t|^2
+    with the analytic form factor (the normaliser of the accuracy figures)."""
+    h = grid.hkl()
+    s2 = np.einsum("a...,ab,b...->...", h, cr.rten, h) / 4.0
+    tot = np.zeros(grid.inc)
+    for t in range(1, cr.nscat + 1):
+        n_t = np.count_nonzero(cr.iscat == t)
+        if n_t == 0:
+            continue
+        sc = cr.scat[t]
+        f = sc[0] + sum(sc[2 * i - 1] * np.exp(-sc[2 * i] * s2) for i in range(1, power + 1))
+        sb = np.exp(-cr.dw[t] * s2) * cr.occ[t] if ldbw else cr.occ[t]
+        tot += n_t * (sb * f) ** 2
+    return tot
+
+
+def full_grid_error(i_test, i_ref, floor):
+    """Every point: |I - I_ref| / (I_ref + N<|f|^2>); max, quantiles, and the
+    points whose reference intensity is at least the incoherent level."""
+    rel = np.abs(i_test - i_ref) / (i_ref + floor)
+    strict = i_ref >= floor
+    return {"points": int(rel.size), "max": float(rel.max()), "p99": float(np.quantile(rel, 0.99)),
+            "p999": float(np.quantile(rel, 0.999)), "n_gt_1e-5": int((rel > 1e-5).sum()),
+            "strict_points": int(strict.sum()),
+            "strict_max": float(rel[strict].max()) if strict.any() else 0.0,
+            "strict_max_relative": float((np.abs(i_test - i_ref)[strict] / i_ref[strict]).max())
+            if strict.any() else 0.0}
+
+
+def parity_ref22(ctx):
+    """The tensor-core engine (EXACT64) against the oracle's restatement of
+    the reference's own arithmetic (REF22: 2^-22 increments, 2^-16-turn
+    table) on the 5000-site perovskite plane and on a 12^3-cell fcc alloy on
+    the 101^3 grid, within the table's floor (lut_floor_tol)."""
+    from diffusecode_gb300 import fourier as FR
+    from oracle import oracle as O
+    out = {}
+    for name, (cr, grid) in (("perovskite-201^2", S.perovskite_plane()),
+                             ("fcc-alloy-12^3-cells-101^3", S.fcc_alloy_volume(cells=12))):
+        op_t = _abi.default_opts(ldbw=1, phase=_abi.PHASE_EXACT64, engine=_abi.ENGINE_TC)
+        op_r = _abi.default_opts(ldbw=1, phase=_abi.PHASE_REF22)
+        r = FR.four_run(cr, grid, op_t, ctx=ctx)
+        rc, csf, acsf, dsi, info = O.four_run(cr, grid, op_r)
+        fl = incoherent_floor(cr, grid)
+        e = full_grid_error(r.dsi, dsi, fl)
+        out[name] = {"max": e["max"], "p99": e["p99"], "tol": O.lut_floor_tol(grid, list(info.lmn)),
+                     "engine": {1: "direct", 2: "tc"}.get(r.info.engine_used)}
+    return out
+
+
+def c3_measure(ctx, flush, steps=3):
+    """The large 2D layer with the average structure subtracted: hexagonal
+    a = 2.46, c = 6.7 A, 200 x 200 x 20 cells x 2 atoms, stacking faults
+    p = 0.1, 2% vacancies; h0l plane 1001 x 1001 over [-10, 10]; fave = 1.
+    Device-resident, L2 flushed before each step.  Error: every point against
+    the CUDA-core engine, and both engines against FP64 at 48 points, half of
+    them on the rods of the average lattice where <F> cancels most of F."""
+    import torch
+    from diffusecode_gb300 import fourier as FR
+    cr, grid = S.hex_layers_plane()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    npnt = grid.npoints
+    pos = torch.from_numpy(cr.pos).to(dev)
+    isc = torch.from_numpy(cr.iscat).to(dev)
+    csf = torch.zeros(2 * npnt, dtype=torch.float64, device=dev)
+    acsf = torch.zeros_like(csf)
+    dsi = torch.zeros(npnt, dtype=torch.float64, device=dev)
+    c = cr.to_c(pos_ptr=C.cast(pos.data_ptr(), C.POINTER(C.c_double)),
+                iscat_ptr=C.cast(isc.data_ptr(), C.POINTER(C.c_int32)))
+    g = grid.to_c()
+    op = _abi.default_opts(ldbw=1, phase=_abi.PHASE_EXACT64, engine=_abi.ENGINE_TC, fave=1.0)
+    info = _abi.Info()
+
+    def run():
+        ctx.check(ctx.lib.dgpu_four_run_device(ctx.h, C.byref(c), C.byref(g), C.byref(op),
+                                               C.c_void_p(csf.data_ptr()), C.c_void_p(acsf.data_ptr()),
+                                               C.c_void_p(dsi.data_ptr()), C.byref(info)))
+        return info.total_ms
+
+    run()
+    ts = []
+    for _ in range(steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        ts.append(run())
+    ms = sum(ts) / len(ts)
+    i_tc = dsi.cpu().numpy().reshape(grid.inc, order="F")
+    refined = int(info.refined)
+    d = FR.four_run(cr, grid, _abi.default_opts(ldbw=1, phase=_abi.PHASE_EXACT64, engine=_abi.ENGINE_DIRECT,
+                                                fave=1.0), ctx=ctx)
+    fl = incoherent_floor(cr, grid)
+    e = full_grid_error(i_tc, d.dsi, fl)
+    # FP64 at rod points (integer h, where the average lattice is) and random points
+    rng = np.random.Generator(np.random.PCG64(11))
+    n1 = grid.inc[0]
+    hh = grid.hkl()[0][:, 0, 0]
+    rods = [int(np.argmin(np.abs(hh - v))) for v in range(-9, 10, 3)] + [int(np.argmin(np.abs(hh - v)))
+                                                                         for v in (-8, -4, 2, 5, 7)]
+    idx = [(rods[k % len(rods)], int(rng.integers(0, grid.inc[1])), 0) for k in range(24)]
+    idx += [(int(rng.integers(0, n1)), int(rng.integers(0, grid.inc[1])), 0) for _ in range(24)]
+    idx = np.array(idx)
+    i64, floor64 = fp64_points(cr, grid, idx, fave=1.0)
+    sel = (idx[:, 0], idx[:, 1], idx[:, 2])
+    e64_tc = np.abs(i_tc[sel] - i64) / (i64 + floor64)
+    e64_d = np.abs(d.dsi[sel] - i64) / (i64 + floor64)
+    return {"workload": "hex-layers-1001^2 (fave 1)", "atoms": cr.n_scattering(), "ms_per_step": ms,
+            "pairs": int(info.pairs), "aver_pairs": int(info.pairs_aver),
+            "G_pairs_per_s": info.pairs / (ms * 1e-3) / 1e9, "refined_points": refined,
+            "direct_ms": d.info.total_ms, "tc_over_plain": d.info.total_ms / ms,
+            "tc_vs_direct_full_grid": e,
+            "fp64_points": {"points": int(len(idx)), "tc_max": float(e64_tc.max()),
+                            "direct_max": float(e64_d.max())}}
+
+
+def fp64_points(cr, grid, idx, fave=0.0):
+    """FP64 numpy |F - <F>|^2 and N<|f|^2> at the given grid indices (TABLE
+    form factors, as the runs use)."""
+    h = (grid.eck[:, 0][None, :] + idx[:, 0:1] * grid.vi[:, 0] + idx[:, 1:2] * grid.vi[:, 1]
+         + idx[:, 2:3] * grid.vi[:, 2])
+    npts = h.shape[0]
+    h32 = h.astype(np.float32).astype(np.float64)
+    q2 = np.einsum("pa,ab,pb->p", h32, cr.rten, h32) / 4.0
+    istl = np.floor(np.sqrt(q2) * 1000.0 + 0.5)
+    s2 = (istl * 0.001) ** 2
+
+    def phase_sum(x):
+        acc = np.zeros(npts, complex)
+        for k0 in range(0, x.shape[0], 65536):
+            ph = h @ x[k0:k0 + 65536].T
+            ph -= np.round(ph)
+            acc += np.exp(2j * np.pi * ph).sum(axis=1)
+        return acc
+
+    F = np.zeros(npts, complex)
+    Fav = np.zeros(npts, complex)
+    floor = np.zeros(npts)
+    if fave:
+        icc = np.asarray(cr.icc)
+        cell = np.arange(cr.natoms) // cr.ncatoms
+        cidx = np.stack([cell % icc[0], (cell // icc[0]) % icc[1], cell // (icc[0] * icc[1])], 1)
+        fold = cr.pos - cidx - np.asarray(cr.dim0)[None, :]
+        ncell = int(np.prod(icc))
+        g0, g1, g2 = np.meshgrid(*(np.arange(n) for n in icc), indexing="ij")
+        lat = phase_sum(np.stack([g0.ravel(), g1.ravel(), g2.ravel()], 1) + np.asarray(cr.dim0)[None, :])
+    for t in range(1, cr.nscat + 1):
+        sel = cr.iscat == t
+        sc = cr.scat[t]
+        f = sc[0] + sum(sc[2 * i - 1] * np.exp(-sc[2 * i] * s2) for i in range(1, 5))
+        cf = np.exp(-cr.dw[t] * s2) * cr.occ[t] * f
+        F += cf * phase_sum(cr.pos[sel])
+        if fave:
+            Fav += cf * phase_sum(fold[sel]) * lat / ncell
+        floor += sel.sum() * cf ** 2
+    return np.abs(F - Fav) ** 2, floor
+
+
 def adjoint_measure(ctx, engine, steps=3):
     """bwd/fwd on the gradient workload: rock salt a = 5.64 A, 25x25x20 cells
     x 8 = 100,000 atoms, 65^3 grid h,k,l in [-3.2,3.2]; target from a seeded
@@ -258,6 +415,32 @@ def adjoint_measure(ctx, engine, steps=3):
     return {"workload": "rocksalt-100000-atoms-65^3", "fwd_kernel_ms": f, "adjoint_ms": b,
             "bwd_over_fwd": b / f, "chi2": c2,
             "note": "adjoint = per-point weights + per-atom sums (tensor cores for the TC engine); fwd = type sums of the same engine"}
+
+
+# k_direct: warp instructions per computed (atom, point) pair, from the ncu
+# capture of one launch on the 108 000-atom alloy (smsp__inst_executed.sum /
+# computed pairs x 32 threads)
+DIRECT_INST_PER_PAIR = None
+
+
+def direct_roofline(pairs_computed, kernel_ms, pk):
+    """The CUDA-core engine is bound by instruction issue (FP32 pipe and the
+    sin/cos polynomial): 152 SMs x 4 schedulers x 1 warp instruction per
+    clock at the maximum SM clock; achieved = the kernel's thread
+    instructions per second (computed pairs x instructions per pair)."""
+    sms, clk = 152, pk.get("sm_max_mhz", 2070.0) * 1e6
+    peak = sms * 4 * 32 * clk / 1e12                 # T thread-instructions/s
+    ipp = DIRECT_INST_PER_PAIR
+    rate = pairs_computed / (kernel_ms * 1e-3)
+    if ipp is None:
+        return {"bound": "issue", "achieved": None, "peak": peak, "unit": "T inst/s", "frac": None,
+                "traffic": None, "computed_pairs_per_s": rate,
+                "note": "instructions per pair not captured"}
+    ach = rate * ipp / 1e12
+    return {"bound": "issue", "achieved": ach, "peak": peak, "unit": "T inst/s", "frac": ach / peak,
+            "traffic": None, "computed_pairs_per_s": rate, "inst_per_pair": ipp,
+            "note": "thread instructions per computed pair from ncu x computed pairs/s, against "
+                    "152 SMs x 128 lanes x max SM clock"}
 
 
 def plain_measure(ctx, c, g, op_tc, csf, acsf, dsi, flush, cr, grid, fave, pairs, steps=2):
@@ -284,8 +467,10 @@ def plain_measure(ctx, c, g, op_tc, csf, acsf, dsi, flush, cr, grid, fave, pairs
         ts.append(run())
     ms = sum(ts) / len(ts)
     err, npt = fp64_check(cr, grid, dsi.cpu().numpy().reshape(grid.inc, order="F"), fave=fave)
+    computed = cr.n_scattering() * int(np.prod(list(info.fnum)))
     return {"value": pairs / (ms * 1e-3) / 1e9, "unit": "G pairs/s", "ms_per_step": ms, "steps": steps,
-            "rel_err_vs_fp64": err, "engine": "direct (CUDA cores, FP32 phasors)"}
+            "rel_err_vs_fp64": err, "engine": "direct (CUDA cores, FP32 phasors)",
+            "roofline": direct_roofline(computed, info.kernel_ms, peaks()[0])}
 
 
 def lots_measure(ctx, c, g, op_main, csf, acsf, dsi, flush, cr, grid, steps=2, nlots=100, ls=10):
@@ -424,6 +609,7 @@ def run_reference(args, world, rank):
     # each takes the first part of the atoms instead, so that the run stays
     # within REF_BUDGET_S (the rate per pair does not depend on the atom count)
     v, nth, rows_used, sec0 = cpu_baseline(cr, grid, nthreads=nthreads)
+    secs = [sec0]
     frac = 1.0
     if args.steps * sec0 > REF_BUDGET_S - sec0:
         frac = max(0.01, (REF_BUDGET_S - sec0) / (args.steps * sec0))
@@ -432,6 +618,7 @@ def run_reference(args, world, rank):
     while len(vals) < args.steps:
         v, nth, rows_used, sec = cpu_baseline(cr, grid, nthreads=nthreads, atom_frac=frac)
         vals.append(v)
+        secs.append(sec)
     value = statistics.median(vals)
     pairs_full = cr.n_scattering() * grid.npoints
     line = {
@@ -447,6 +634,10 @@ def run_reference(args, world, rank):
                                    + (f" (the first {frac:.0%} of the atoms per step)" if frac < 1.0 else "")
                                    + ", credited per full-grid pair"},
         "e2e": {"value": value, "unit": "G pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "sample": {"rows_per_step": rows_used, "atom_fraction": frac, "seconds_measured": sum(secs),
+                   "samples": len(secs),
+                   "note": "ms_per_step is the full-grid time implied by the measured rate; the arm itself "
+                           "ran seconds_measured"},
     }
     print(json.dumps(line))
 
@@ -543,6 +734,15 @@ def run_ours(args, world, rank, local):
     acc_err, acc_pts, acc_diffuse, acc_bragg, n_bragg = fp64_check(cr, grid, dsi_host, fave=fave, split=True)
     plain = None if (args.no_plain or engine_used != _abi.ENGINE_TC) else plain_measure(
         ctx, c, g, op, csf, acsf, dsi, flush, cr, grid, fave, info.pairs)
+    full_grid = None
+    if plain:
+        # every grid point of the tensor-core result against the CUDA-core
+        # engine's (itself pinned to FP64 at the sampled points above)
+        i_direct = dsi.cpu().numpy().reshape(grid.inc, order="F")
+        full_grid = full_grid_error(dsi_host, i_direct, incoherent_floor(cr, grid))
+        full_grid["reference"] = "CUDA-core engine, every grid point"
+        full_grid["reference_vs_fp64_sampled"] = plain["rel_err_vs_fp64"]
+    c3 = None if args.no_c3 else c3_measure(ctx, flush)
     adj = None if args.no_adjoint else adjoint_measure(ctx, engine)
     bat = None if args.no_batch else batch_measure(ctx)
     lots = None if args.no_lots else lots_measure(ctx, c, g, op, csf, acsf, dsi, flush, cr, grid)
@@ -563,12 +763,7 @@ def run_ours(args, world, rank, local):
                         "DRAM bytes of one ncu capture of the same kernel on the 108 000-atom alloy, scaled by "
                         "the atom count (the bytes are the V operand images, which grow with the atoms)"}
     else:
-        # direct engine: FP32 pipe; 4 flops/pair of accumulation + phasor
-        flops = 4.0 * pairs_computed
-        achieved = flops / (kms * 1e-3) / 1e12
-        roof = {"bound": "tensor", "achieved": achieved, "peak": pk.get("bf16_tflops", 1900.0), "unit": "TFLOP/s",
-                "frac": achieved / pk.get("bf16_tflops", 1900.0), "traffic": None,
-                "note": "direct FP32 engine (no tensor cores); 4 algorithmic flops per computed pair"}
+        roof = direct_roofline(pairs_computed, kms, pk)
     line = {
         "metric": METRIC, "value": value, "unit": "G pairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -592,10 +787,18 @@ def run_ours(args, world, rank, local):
         "gpu_launches": LAUNCHES_PER_RUN.get(engine_used, 10) * args.steps,
         "accuracy": {"rel_err_vs_fp64": acc_err, "points": acc_pts,
                      "non_bragg": acc_diffuse, "bragg": acc_bragg, "bragg_points": n_bragg,
-                     "norm": "max |I-I64|/(I64 + N<|f|^2>) at sampled grid points"},
+                     "norm": "max |I-I64|/(I64 + N<|f|^2>) at sampled grid points",
+                     "full_grid": full_grid},
+        "parity_vs_ref22": None,
+        "c3": c3,
         "e2e": {"value": e2e_val, "unit": "G pairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
     }
     if not args.no_cpu_baseline:
+        # the oracle's REF22 restatement of the reference's arithmetic: timed
+        # as the CPU baseline, and the checker of the tensor-core engine's
+        # agreement with that arithmetic
+        if not args.no_ref22:
+            line["parity_vs_ref22"] = parity_ref22(ctx)
         v, nth, rows, sec = cpu_baseline(cr, grid)
         line["cpu_baseline"] = {"value": v, "unit": "G pairs/s", "cores": nth, "kind": "port",
                                 "sample": f"REF22 four_strucf_omp restatement (oracle), {rows} abscissa rows "
@@ -618,6 +821,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-lots", action="store_true")
     ap.add_argument("--no-powder", action="store_true")
+    ap.add_argument("--no-ref22", action="store_true")
+    ap.add_argument("--no-c3", action="store_true")
     ap.add_argument("--tc-flush", type=int, default=0, help="atoms per main-accumulator drain (0: default)")
     args = ap.parse_args()
     world, rank, local = dist_init()

@@ -140,6 +140,7 @@ class Info(C.Structure):
         ("kernel_ms", C.c_double),
         ("total_ms", C.c_double),
         ("tc_config", C.c_int32 * 4),
+        ("refined", C.c_int64),
     ]
 
 

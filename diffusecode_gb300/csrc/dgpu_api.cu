@@ -87,7 +87,7 @@ extern "C" int dgpu_ctx_destroy(dgpu_ctx *c)
                       &c->flag, &c->tc_part, &c->tc_work, &c->tc_mult, &c->tc_vimg, &c->adj_qimg,
                       &c->adj_items, &c->gq, &c->gpart, &c->grad, &c->batch_desc, &c->batch_aux,
                       &c->ianis, &c->geff, &c->ghist, &c->lpos, &c->ltype, &c->locc, &c->lplan, &c->lfac,
-                      &c->wbuf, &c->acc_csf, &c->acc_dsi, &c->slab_ph0};
+                      &c->wbuf, &c->acc_csf, &c->acc_dsi, &c->slab_ph0, &c->rlist, &c->rsum};
     for (DevBuf *b : bufs) b->release();
     c->stage.release();
     for (cudaEvent_t e : c->run_ev) cudaEventDestroy(e);
@@ -416,9 +416,15 @@ int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g,
 
     int warn = 0;
     int32_t ncell = 0;
-    int64_t pairs_aver = 0, pairs = 0;
+    int64_t pairs_aver = 0, pairs = 0, refined = 0;
     float kernel_ms = 0.f;
     int64_t ts[2 * 64 + 4];
+    // <F> of a box lattice in closed form: kept for the refinement of the
+    // points where it cancels most of F
+    int64_t ts_fold[2 * 64 + 4];
+    bool aver_closed = false;
+    int32_t alat_n[3] = {0, 0, 0};
+    double alat_d[3] = {0, 0, 0}, anorm = 0.0;
 
     // ---- <F> (four_aver): cells drawn over csize, lattice of the crystal or of a lot ----
     if (op->fave < 0.0) {
@@ -455,6 +461,7 @@ int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g,
         rc = engine_sums(ctx, engine, ctx->aph0, ctx->adu, ctx->adv, ctx->adw, ctx->aw, ts, cr->nscat, op, box,
                          ctx->apart, &aref);
         if (rc) return rc;
+        memcpy(ts_fold, ts, sizeof(int64_t) * (2 * cr->nscat + 1));
         for (int t = 0; t < cr->nscat; t++) pairs_aver += ts[cr->nscat + 1 + t] * np;
         // four_getav (fourier_sup.f90:2440-2510) + four_strucf(0, ...) on the full num:
         // a box (all cells at dim0, or a box lot at 0) has a closed form in EXACT64
@@ -511,6 +518,12 @@ int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g,
                                ctx->cfact.as<double2>(), closed ? nullptr : ctx->lat.as<double2>(), lat_nslice,
                                closed, lat_n, lat_d, norm, d_acsf);
         if (rc) return rc;
+        aver_closed = closed && ncell > 0;
+        for (int k = 0; k < 3; k++) {
+            alat_n[k] = lat_n[k];
+            alat_d[k] = lat_d[k];
+        }
+        anorm = norm;
         float ms = 0.f;
         DGPU_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]));
         kernel_ms += ms;
@@ -537,6 +550,43 @@ int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g,
         float ms = 0.f;
         DGPU_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]));
         kernel_ms += ms;
+        if (engine == DGPU_ENGINE_TC && aver_closed) {
+            // points where <F> cancels most of F: exact sums on CUDA cores
+            RefineSpec r;
+            memset(&r, 0, sizeof(r));
+            r.box = box;
+            r.fsm = &fsm;
+            r.fst = &fs;
+            r.istl = ctx->istl.as<int32_t>();
+            r.cfact = ctx->cfact.as<double2>();
+            r.ph0 = ctx->ph0.as<uint64_t>();
+            r.du = ctx->du.as<uint64_t>();
+            r.dv = ctx->dv.as<uint64_t>();
+            r.dw = ctx->dw.as<uint64_t>();
+            r.w = ctx->w.as<float>();
+            r.ts_main = ts;
+            r.ngroup = ngroup;
+            r.aph0 = ctx->aph0.as<uint64_t>();
+            r.adu = ctx->adu.as<uint64_t>();
+            r.adv = ctx->adv.as<uint64_t>();
+            r.adw = ctx->adw.as<uint64_t>();
+            r.aw = ctx->aw.as<float>();
+            r.ts_fold = ts_fold;
+            r.nscat = cr->nscat;
+            for (int k = 0; k < 3; k++) {
+                r.lat_n[k] = alat_n[k];
+                r.lat_d[k] = alat_d[k];
+            }
+            r.norm = anorm;
+            r.diff_scale = op->diff_scale;
+            DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
+            rc = dgpu_refine_aver(ctx, r, d_csf, d_acsf, d_dsi, &refined);
+            if (rc) return rc;
+            DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
+            DGPU_CUDA(ctx, cudaEventSynchronize(ctx->ev[3]));
+            DGPU_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]));
+            kernel_ms += ms;
+        }
         for (int t = 0; t < ngroup; t++) pairs += ts[ngroup + 1 + t] * np;
     } else {
         // ---- lots (fourier_sup.f90:136-257): chunks of lots, one engine launch each ----
@@ -576,6 +626,7 @@ int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g,
         info->engine_used = engine;
         info->pairs = pairs;
         info->pairs_aver = pairs_aver;
+        info->refined = refined;
         for (int k = 0; k < 7; k++) info->res[k] = res[k];
         info->kernel_ms = kernel_ms;
         for (int k = 0; k < 4; k++) info->tc_config[k] = engine == DGPU_ENGINE_TC ? ctx->tc_last[k] : -1;

@@ -70,3 +70,36 @@ __device__ __forceinline__ double2 form_group(const FormSpec *fs, const double2 
     }
     return c;
 }
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b)
+{
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// one-axis geometric series sum_{m<n} exp(2 pi i x m)
+__device__ __forceinline__ double2 geom_series(double x, int32_t n)
+{
+    double xr = x - rint(x);
+    if (xr == 0.0) return make_double2((double)n, 0.0);
+    double num = sinpi((double)n * xr), den = sinpi(xr);
+    double r = num / den, sp, cp;
+    sincospi(xr * (double)(n - 1), &sp, &cp);
+    return make_double2(r * cp, r * sp);
+}
+
+// Lattice sum of a box of c0 x c1 x c2 cells starting at d (four_strucf(0,..)
+// over the lattice of four_getav, fourier_sup.f90:1315-1318) in closed form:
+// a product of three geometric series times exp(2 pi i h.d), the phase
+// h.d reduced exactly.
+__device__ __forceinline__ double2 lattice_closed(const double h[3], int32_t c0, int32_t c1, int32_t c2, double d0,
+                                                  double d1, double d2)
+{
+    double2 L = cmul(cmul(geom_series(h[0], c0), geom_series(h[1], c1)), geom_series(h[2], c2));
+    double p0 = h[0] * d0, e0 = fma(h[0], d0, -p0);
+    double p1 = h[1] * d1, e1 = fma(h[1], d1, -p1);
+    double p2 = h[2] * d2, e2 = fma(h[2], d2, -p2);
+    double ph = (p0 - rint(p0)) + (p1 - rint(p1)) + (p2 - rint(p2)) + (e0 + e1 + e2);
+    double sp, cp;
+    sincospi(2.0 * ph, &sp, &cp);
+    return cmul(L, make_double2(cp, sp));
+}

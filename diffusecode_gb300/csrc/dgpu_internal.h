@@ -118,6 +118,7 @@ struct dgpu_ctx {
     DevBuf lpos, ltype, locc, lplan, lfac;  // lot crystals, lot plan, group factors
     FormSpec *fs_main = nullptr;            // host copy of the last main combine's FormSpec
     DevBuf wbuf, acc_csf, acc_dsi;          // four_weight staging; four_accumulate sums
+    DevBuf rlist, rsum;                     // refinement of <F>-cancelling points: list, exact sums
     DevBuf slab_ph0;                        // powder: per-slab origin phases of the atoms
     int64_t acc_np = 0;                     // points of the accumulated sums (0: none)
     DevBuf gq, gpart, grad, batch_desc, batch_aux;
@@ -349,6 +350,27 @@ int dgpu_aver_combine(dgpu_ctx *ctx, const FormSpec &fs, const BoxSpec &box,
                       const double2 *cfact, const double2 *lat, int32_t lat_nslice,
                       int32_t lat_closed, const int32_t icc[3], const double dim0[3],
                       double norm, double2 *acsf);
+
+// Points whose |<F>|^2 exceeds REFINE_TAU * N <|f|^2> are recomputed exactly
+// after a tensor-core run with <F> subtracted (k_refine.cu).
+#define REFINE_TAU 64.0
+struct RefineSpec {
+    BoxSpec box;
+    const FormSpec *fsm, *fst;             // host: groups of the main sums, plain types of <F>
+    const int32_t *istl;
+    const double2 *cfact;
+    const uint64_t *ph0, *du, *dv, *dw;    // main atom set, by group
+    const float *w;
+    const int64_t *ts_main;                // host type ranges (2 ngroup + 1 values)
+    int32_t ngroup;
+    const uint64_t *aph0, *adu, *adv, *adw;   // atoms folded into one cell, by type
+    const float *aw;
+    const int64_t *ts_fold;
+    int32_t nscat;
+    int32_t lat_n[3];                      // closed-form lattice of <F>
+    double lat_d[3], norm, diff_scale;
+};
+int dgpu_refine_aver(dgpu_ctx *ctx, const RefineSpec &r, double2 *csf, double2 *acsf, double *dsi, int64_t *nref);
 int dgpu_friedel_mirror(dgpu_ctx *ctx, const BoxSpec &box, int32_t idim, double2 *csf,
                         double2 *acsf, double *dsi);
 int dgpu_qinfo(dgpu_ctx *ctx, const double eck[3], const double vi[9], const int32_t num[3],

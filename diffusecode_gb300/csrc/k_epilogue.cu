@@ -15,11 +15,6 @@
 #include "dgpu_form.cuh"
 #include "dgpu_lots.h"
 
-__device__ __forceinline__ double2 cmul(double2 a, double2 b)
-{
-    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-
 __device__ __forceinline__ double2 ld_part(const double2 *p) { return *p; }
 __device__ __forceinline__ double2 ld_part(const float2 *p)
 {
@@ -129,17 +124,6 @@ __global__ void k_combine(const FormSpec *fs, BoxSpec box, const P *__restrict__
     dsi[idx] = (F.x * F.x + F.y * F.y) * ds;
 }
 
-// one-axis geometric series sum_{m<n} exp(2 pi i x m)
-__device__ __forceinline__ double2 geom_series(double x, int32_t n)
-{
-    double xr = x - rint(x);
-    if (xr == 0.0) return make_double2((double)n, 0.0);
-    double num = sinpi((double)n * xr), den = sinpi(xr);
-    double r = num / den, sp, cp;
-    sincospi(xr * (double)(n - 1), &sp, &cp);
-    return make_double2(r * cp, r * sp);
-}
-
 template <class P>
 __global__ void k_aver_combine(const FormSpec *fs, BoxSpec box, const P *__restrict__ apart,
                                int32_t anslice, PartLayout lay, const int32_t *__restrict__ istl,
@@ -171,16 +155,7 @@ __global__ void k_aver_combine(const FormSpec *fs, BoxSpec box, const P *__restr
     }
     double2 L;
     if (lat_closed) {
-        double2 g0 = geom_series(h[0], c0), g1 = geom_series(h[1], c1), g2 = geom_series(h[2], c2);
-        L = cmul(cmul(g0, g1), g2);
-        // exp(2 pi i h.dim0) with the phase reduced exactly
-        double p0 = h[0] * d0, e0 = fma(h[0], d0, -p0);
-        double p1 = h[1] * d1, e1 = fma(h[1], d1, -p1);
-        double p2 = h[2] * d2, e2 = fma(h[2], d2, -p2);
-        double ph = (p0 - rint(p0)) + (p1 - rint(p1)) + (p2 - rint(p2)) + (e0 + e1 + e2);
-        double sp, cp;
-        sincospi(2.0 * ph, &sp, &cp);
-        L = cmul(L, make_double2(cp, sp));
+        L = lattice_closed(h, c0, c1, c2, d0, d1, d2);
     } else {
         L = make_double2(0.0, 0.0);
         for (int k = 0; k < lat_nslice; k++) {

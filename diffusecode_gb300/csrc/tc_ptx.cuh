@@ -224,8 +224,8 @@ __device__ __forceinline__ uint64_t tc_rot(uint64_t j) { return j * 0x9E3779B97F
 
 // exp(2 pi i phase) of a 64-bit fixed-point turn to about one FP32 ulp: the
 // signed phase as x = 2 turns in [-1, 1) splits into its top 24 bits (exact
-// in FP32, evaluated by sincospif) and a remainder below 2^-23 applied as a
-// first-order rotation.  Used where a value is evaluated once per launch (the
+// in FP32, evaluated by sincospif) and a remainder below 2^-23 (its next 24
+// bits, 32-bit conversions only) applied as a first-order rotation.  Used where a value is evaluated once per launch (the
 // V operand images); the kernels' seeds use the hardware approximation above,
 // whose error (a few 1e-7, a smooth function of the phase) tc_rot makes
 // random from atom to atom.
@@ -233,7 +233,7 @@ __device__ __forceinline__ float2 phasor_acc(uint64_t ph)
 {
     const int64_t v = (int64_t)ph;
     const float xf = (float)(int32_t)(v >> 40) * 0x1p-23f;
-    const float dth = (float)((uint64_t)v & 0xFFFFFFFFFFull) * (3.14159265358979f * 0x1p-63f);
+    const float dth = (float)((uint32_t)(ph >> 16) & 0xFFFFFFu) * (3.14159265358979f * 0x1p-47f);
     float s, c;
     sincospif(xf, &s, &c);
     return make_float2(fmaf(-s, dth, c), fmaf(c, dth, s));

@@ -164,6 +164,10 @@ typedef struct dgpu_info {
     double  total_ms;          /* device time of the whole call                      */
     int32_t tc_config[4];      /* tensor-core engine: column axis, N tile, main
                                   accumulator buffers, atoms per K slice (-1 if unused) */
+    int64_t refined;           /* points recomputed exactly on CUDA cores after a
+                                  tensor-core run with <F> subtracted: those where
+                                  |<F>|^2 > 64 N<|f|^2>, whose F - <F> cancels
+                                  more digits than the FP32 type sums carry      */
 } dgpu_info;
 
 /* ---- context ------------------------------------------------------------ */

@@ -262,3 +262,20 @@ def powder_complete(cr, pw, opts, rod_lo=-1, rod_hi=-1, nthreads=0):
     rc = lib().oc_powder_complete(C.byref(c), C.byref(p), C.byref(opts), int(rod_lo), int(rod_hi), _d(qsp),
                                   C.byref(nr), C.byref(npts), nthreads)
     return rc, qsp, nr.value, npts.value
+
+
+def lut_floor_tol(grid, lmn):
+    """Tolerance of a comparison with the reference's table arithmetic
+    (four_strucf_OMP_mod.f90:143-148,169): the 2^-16-turn table index is a
+    truncation (uniform phase error, rms 2^-16/sqrt(12) turn; its mean is a
+    phase common to all atoms and drops out of |F|^2) and each 2^-22-turn
+    increment is rounded (+-2^-23 turn, times the point's index from the
+    origin of the increments, lmn + n, largest at a corner of the grid).  A
+    random per-atom phase error of
+    rms sigma moves |F|^2 by at most ~ sigma times a Gaussian in units of
+    I + N<|f|^2>; the tolerance is six sigma."""
+    import numpy as _np
+    n = _np.array([max(abs(lmn[k]), abs(lmn[k] + grid.inc[k] - 1)) for k in range(3)], float)
+    s_tab = 2 ** -16 / _np.sqrt(12.0)
+    s_inc = 2 ** -23 * _np.sqrt(_np.sum(n ** 2) / 3.0)
+    return float(6.0 * 2 * _np.pi * _np.hypot(s_tab, s_inc))

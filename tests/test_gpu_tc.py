@@ -84,6 +84,24 @@ def test_tc_bf16_split_error_is_reported(oracle, ctx):
     assert err <= 1e-3
 
 
+@pytest.mark.parametrize("case", ["perovskite", "fcc-alloy"])
+def test_tc_against_reference_arithmetic(oracle, ctx, case):
+    """The tensor-core engine (exact 64-bit phases) against the oracle's
+    REF22 four_run, the reference's own arithmetic (2^-22-turn increments,
+    2^-16-turn cos/sin table): the 5000-site perovskite plane (201 x 201
+    hk0) and a 12^3-cell fcc alloy on the 101^3 grid.  Every point within the
+    table's floor (oracle.lut_floor_tol: six sigma of the table truncation and
+    increment rounding, in units of I + N<|f|^2>)."""
+    cr, g = S.perovskite_plane() if case == "perovskite" else S.fcc_alloy_volume(cells=12)
+    r = FR.four_run(cr, g, tc_opts(), ctx=ctx)
+    rc, csf, acsf, ref, info = oracle.four_run(cr, g, K.opts(phase=_abi.PHASE_REF22))
+    tol = oracle.lut_floor_tol(g, list(info.lmn))
+    err = K.rel_err(r.dsi, ref, K.incoherent_floor(cr, g, tc_opts()))
+    print(f"{case}: TC vs REF22 {err:.2e} (table floor {tol:.2e})")
+    assert r.info.engine_used == _abi.ENGINE_TC
+    assert err <= tol
+
+
 def test_tc_ref22_rejected(ctx):
     cr, g = S.perovskite_plane(cells=2)
     with pytest.raises(Exception) as e:

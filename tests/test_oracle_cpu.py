@@ -76,6 +76,20 @@ def test_laue_ref22_within_table_floor(oracle):
     assert np.max(np.abs(csf - F)) <= n * fmax * (2 * np.pi / 65536) * 1.5
 
 
+def test_table_floor_tolerance_covers_ref22(oracle):
+    """The oracle's REF22 (the reference's table arithmetic) against its
+    EXACT64 on the 5000-site perovskite plane: the difference is the table's
+    floor, and oracle.lut_floor_tol, the tolerance the GPU comparisons with
+    REF22 use, must cover it (with the same form-factor table in both)."""
+    cr, g = S.perovskite_plane()
+    rc, _, _, a, info = oracle.four_run(cr, g, K.opts(phase=_abi.PHASE_REF22))
+    rc2, _, _, b, _ = oracle.four_run(cr, g, K.opts(phase=_abi.PHASE_EXACT64))
+    assert rc == rc2 == 0
+    err = K.rel_err(a, b, K.incoherent_floor(cr, g, K.opts()))
+    tol = oracle.lut_floor_tol(g, list(info.lmn))
+    assert 1e-6 < err <= tol / 2
+
+
 def test_two_atoms_exact(oracle):
     cr, g, F = K.two_atoms()
     op = K.opts(phase=_abi.PHASE_EXACT64, form=_abi.FORM_ANALYTIC, friedel=0)
