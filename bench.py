@@ -417,10 +417,10 @@ def adjoint_measure(ctx, engine, steps=3):
             "note": "adjoint = per-point weights + per-atom sums (tensor cores for the TC engine); fwd = type sums of the same engine"}
 
 
-# k_direct: warp instructions per computed (atom, point) pair, from the ncu
-# capture of one launch on the 108 000-atom alloy (smsp__inst_executed.sum /
-# computed pairs x 32 threads)
-DIRECT_INST_PER_PAIR = None
+# k_direct: thread instructions per computed (atom, point) pair, from the ncu
+# capture of one launch on the 108 000-atom alloy, 61^3 grid
+# (smsp__sass_thread_inst_executed.sum 5.9635e11 / 108 000 x 115 351 pairs)
+DIRECT_INST_PER_PAIR = 47.87
 
 
 def direct_roofline(pairs_computed, kernel_ms, pk):

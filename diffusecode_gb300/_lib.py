@@ -19,7 +19,7 @@ EXPORTS = [
     "dgpu_four_stltab", "dgpu_four_formtab", "dgpu_four_increments", "dgpu_chi2_grad",
     "dgpu_batch_run", "dgpu_batch_last_ms", "dgpu_four_strucf_noalloc", "dgpu_tc_last_kernel_ms",
     "dgpu_four_weight", "dgpu_four_weight_device", "dgpu_four_accumulate", "dgpu_qval",
-    "dgpu_calc_hkl", "dgpu_powder_npkt", "dgpu_powder_complete",
+    "dgpu_calc_hkl", "dgpu_powder_npkt", "dgpu_powder_complete", "dgpu_chi2_grad_device",
 ]
 
 
@@ -55,6 +55,7 @@ def load():
     L.dgpu_four_formtab.argtypes = [vp, CR, OP, dp]
     L.dgpu_four_increments.argtypes = [vp, dp, C.c_int64, dp, dp, dp, dp, i64p]
     L.dgpu_chi2_grad.argtypes = [vp, CR, GR, OP, dp, dp, dp, dp, dp, IN]
+    L.dgpu_chi2_grad_device.argtypes = [vp, CR, GR, OP, vp, vp, dp, vp, vp, IN]
     PP = C.POINTER(dp)
     L.dgpu_batch_run.argtypes = [vp, C.c_int32, CR, GR, OP, PP, PP, PP, dp, PP, PP]
     L.dgpu_batch_last_ms.argtypes = [vp]

@@ -71,6 +71,10 @@ extern "C" int dgpu_ctx_create(int device, dgpu_ctx **out)
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { delete c; return DGPU_ERR_CUDA; }
     for (int i = 0; i < DGPU_NEV; i++)
         if (cudaEventCreate(&c->ev[i]) != cudaSuccess) { delete c; return DGPU_ERR_CUDA; }
+    if (dgpu_tc_init(c) != DGPU_OK) {
+        dgpu_ctx_destroy(c);
+        return DGPU_ERR_CUDA;
+    }
     *out = c;
     return DGPU_OK;
 }
@@ -87,7 +91,7 @@ extern "C" int dgpu_ctx_destroy(dgpu_ctx *c)
                       &c->flag, &c->tc_part, &c->tc_work, &c->tc_mult, &c->tc_vimg, &c->adj_qimg,
                       &c->adj_items, &c->gq, &c->gpart, &c->grad, &c->batch_desc, &c->batch_aux,
                       &c->ianis, &c->geff, &c->ghist, &c->lpos, &c->ltype, &c->locc, &c->lplan, &c->lfac,
-                      &c->wbuf, &c->acc_csf, &c->acc_dsi, &c->slab_ph0, &c->rlist, &c->rsum};
+                      &c->wbuf, &c->acc_csf, &c->acc_dsi, &c->slab_ph0, &c->rlist, &c->rsum, &c->tc_tab};
     for (DevBuf *b : bufs) b->release();
     c->stage.release();
     for (cudaEvent_t e : c->run_ev) cudaEventDestroy(e);
@@ -837,4 +841,15 @@ extern "C" int dgpu_chi2_grad(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_
     if (!i_target || !chi2) return dgpu_set_error(ctx, DGPU_ERR_ARG, "i_target/chi2 missing");
     DGPU_CUDA(ctx, cudaSetDevice(ctx->device));
     return dgpu_chi2_grad_impl(ctx, cr, grid, opts, i_target, weight, chi2, grad_pos, grad_occ, info);
+}
+
+extern "C" int dgpu_chi2_grad_device(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid,
+                                     const dgpu_opts *opts, const double *d_i_target, const double *d_weight,
+                                     double *chi2, double *d_grad_pos, double *d_grad_occ, dgpu_info *info)
+{
+    int rc = check_inputs(ctx, cr, grid, opts);
+    if (rc) return rc;
+    if (!d_i_target || !chi2) return dgpu_set_error(ctx, DGPU_ERR_ARG, "i_target/chi2 missing");
+    DGPU_CUDA(ctx, cudaSetDevice(ctx->device));
+    return dgpu_chi2_grad_impl(ctx, cr, grid, opts, d_i_target, d_weight, chi2, d_grad_pos, d_grad_occ, info, true);
 }

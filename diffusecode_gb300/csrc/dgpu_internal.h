@@ -111,6 +111,7 @@ struct dgpu_ctx {
     DevBuf istl, cfact, part, apart, lat, csf, acsf, dsi, stats, flag;
     DevBuf tc_part, tc_work, aidx;          // aidx: original atom index of each prepared slot
     DevBuf tc_mult;                         // per-atom step factors of the tensor-core engine
+    DevBuf tc_tab;                          // exp(2 pi i k / 4096), FP64, for the step factors
     DevBuf tc_vimg;                         // V operand images of the tensor-core engine
     DevBuf adj_qimg, adj_items;             // tensor-core adjoint: Q images, work items
     int64_t ts_main[2 * 64 + 4] = {};      // type ranges of the last main atom preparation
@@ -297,6 +298,8 @@ int dgpu_tc_check(dgpu_ctx *ctx);                               // waits, reads 
 struct PartRef;
 // Per-atom step factors exp(2 pi i 8 d) of du, dv, dw (n atoms) into
 // out[axis * stride + atom]; enqueue only.
+// The step factors' FP64 table, once per context (at creation).
+int dgpu_tc_init(dgpu_ctx *ctx);
 int dgpu_tc_mult_async(dgpu_ctx *ctx, const uint64_t *du, const uint64_t *dv, const uint64_t *dw, int64_t n,
                        int64_t stride, float2 *out);
 // Layout of a problem's partials for the combine kernels.
@@ -449,7 +452,7 @@ int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g,
 // adjoint.cu / batch.cu ---------------------------------------------------
 int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid,
                         const dgpu_opts *op, const double *i_target, const double *weight,
-                        double *chi2, double *grad_pos, double *grad_occ, dgpu_info *info);
+                        double *chi2, double *grad_pos, double *grad_occ, dgpu_info *info, bool device = false);
 int dgpu_fill_formspec(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *op,
                        const dgpu_grid *g, FormSpec &fs);
 

@@ -158,9 +158,11 @@ __global__ void __launch_bounds__(ADJ_NT) k_adj_atoms(const uint64_t *__restrict
     }
 }
 
+// device: the crystal's per-atom arrays, i_target, weight and the two
+// gradient arrays are device pointers (chi2 stays a host pointer)
 int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid, const dgpu_opts *op,
                         const double *i_target, const double *weight, double *chi2, double *grad_pos,
-                        double *grad_occ, dgpu_info *info)
+                        double *grad_occ, dgpu_info *info, bool device)
 {
     if (op->fave != 0.0)
         return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "gradient with <F> subtraction (set aver) is not available");
@@ -171,9 +173,9 @@ int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
         return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "gradient with lots");
     const int64_t n = cr->natoms;
     const int64_t np = (int64_t)grid->inc[0] * grid->inc[1] * grid->inc[2];
-    // forward pass with host inputs
-    dgpu_crystal dc;
-    int rc = dgpu_stage_crystal(ctx, cr, dc);
+    // forward pass (host inputs are staged first)
+    dgpu_crystal dc = *cr;
+    int rc = device ? (int)DGPU_OK : dgpu_stage_crystal(ctx, cr, dc);
     if (rc) return rc;
     DGPU_CUDA(ctx, ctx->csf.ensure(np * sizeof(double2)));
     DGPU_CUDA(ctx, ctx->acsf.ensure(np * sizeof(double2)));
@@ -191,9 +193,9 @@ int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
     double *d_wt = d_it + np;
     double *d_g = d_wt + np;
     double *d_chi = d_g + np;
-    DGPU_CUDA(ctx, cudaMemcpyAsync(d_it, i_target, np * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    if (weight)
-        DGPU_CUDA(ctx, cudaMemcpyAsync(d_wt, weight, np * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    const cudaMemcpyKind in_kind = device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    DGPU_CUDA(ctx, cudaMemcpyAsync(d_it, i_target, np * sizeof(double), in_kind, ctx->stream));
+    if (weight) DGPU_CUDA(ctx, cudaMemcpyAsync(d_wt, weight, np * sizeof(double), in_kind, ctx->stream));
     k_adj_g<<<nblk, 256, 0, ctx->stream>>>(ctx->dsi.as<double>(), d_it, weight ? d_wt : nullptr, np, d_g, d_chi);
     DGPU_CUDA(ctx, cudaGetLastError());
     k_adj_chi<<<1, 32, 0, ctx->stream>>>(d_chi, nblk, d_chi + nblk);
@@ -250,10 +252,10 @@ int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
     }
     DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
     DGPU_CUDA(ctx, cudaMemcpyAsync(chi2, d_chi + nblk, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    const cudaMemcpyKind out_kind = device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
     if (grad_pos)
-        DGPU_CUDA(ctx, cudaMemcpyAsync(grad_pos, d_gpos, n * 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    if (grad_occ)
-        DGPU_CUDA(ctx, cudaMemcpyAsync(grad_occ, d_gocc, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        DGPU_CUDA(ctx, cudaMemcpyAsync(grad_pos, d_gpos, n * 3 * sizeof(double), out_kind, ctx->stream));
+    if (grad_occ) DGPU_CUDA(ctx, cudaMemcpyAsync(grad_occ, d_gocc, n * sizeof(double), out_kind, ctx->stream));
     DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (info) {
         *info = fwd;

@@ -19,7 +19,13 @@
 //
 // Set-up: the device address of the array is looked up once per device
 // (cudaGetSymbolAddress, with that device current) on the first call made on
-// that device; make that first call before any stream capture begins.
+// that device; make that first call before any stream capture begins.  The
+// address is kept with the CUDA context it belongs to and looked up again
+// when a later call finds a different context current on that device (for
+// instance a new primary context after cudaDeviceReset).  The stream must
+// belong to the device that is current at the call.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "dgpu_internal.h"
@@ -37,20 +43,47 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 namespace {
 
 std::mutex g_mu;
-void *g_addr[256];
+struct Cached {
+    CUcontext ctx;
+    void *addr;
+};
+Cached g_addr[256];
 
-// device address of the scratch array for the current device
+// the driver's cuCtxGetCurrent, through the runtime (the library does not
+// link the driver library itself)
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+CtxGetCurrentFn ctx_get_current()
+{
+    static CtxGetCurrentFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<CtxGetCurrentFn>(p);
+    }
+    return fn;
+}
+
+// device address of the scratch array for the current device and context
 int scratch_address(void **out)
 {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return DGPU_ERR_CUDA;
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_addr[dev]) {
+    const CtxGetCurrentFn get = ctx_get_current();
+    if (!get) return DGPU_ERR_CUDA;
+    CUcontext cur = nullptr;              // null before the runtime's first use on this thread
+    if (get(&cur) != CUDA_SUCCESS) return DGPU_ERR_CUDA;
+    if (!cur || !g_addr[dev].addr || g_addr[dev].ctx != cur) {
         void *p = nullptr;
+        // the look-up also makes the device's primary context current
         if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return DGPU_ERR_CUDA;
-        g_addr[dev] = p;
+        if (get(&cur) != CUDA_SUCCESS || !cur) return DGPU_ERR_CUDA;
+        g_addr[dev].addr = p;
+        g_addr[dev].ctx = cur;
     }
-    *out = g_addr[dev];
+    *out = g_addr[dev].addr;
     return DGPU_OK;
 }
 
@@ -91,7 +124,10 @@ __global__ void k_na_phase(const double *__restrict__ xat, int64_t n, Geo g, uin
 }
 
 // sum over all atoms for Q consecutive points along the first axis of fnum;
-// phases keep their top 16 bits (the reference's 2^16-entry table index)
+// phases keep their top 16 bits (the reference's 2^16-entry table index).
+// FP32 sums over a shared-memory chunk with Fast2Sum compensation (a coherent
+// sum of nearly equal terms, as on a Bragg row, would otherwise round with a
+// bias that grows with the chunk length), FP64 across chunks.
 __global__ void __launch_bounds__(NOALLOC_NT) k_na_sum(const uint64_t *__restrict__ ph0,
                                                        const uint64_t *__restrict__ du,
                                                        const uint64_t *__restrict__ dv,
@@ -120,9 +156,9 @@ __global__ void __launch_bounds__(NOALLOC_NT) k_na_sum(const uint64_t *__restric
             s_w[threadIdx.x] = dw[a0 + threadIdx.x];
         }
         __syncthreads();
-        float accf[NOALLOC_Q][2];
+        float accf[NOALLOC_Q][2], cmpf[NOALLOC_Q][2];
 #pragma unroll
-        for (int k = 0; k < NOALLOC_Q; k++) accf[k][0] = accf[k][1] = 0.f;
+        for (int k = 0; k < NOALLOC_Q; k++) accf[k][0] = accf[k][1] = cmpf[k][0] = cmpf[k][1] = 0.f;
         for (int a = 0; a < cnt; a++) {
             const uint64_t d = s_u[a];
             uint64_t ph = s_b[a] + i0 * d + j * s_v[a] + l * s_w[a];
@@ -131,15 +167,18 @@ __global__ void __launch_bounds__(NOALLOC_NT) k_na_sum(const uint64_t *__restric
                 const float x = (float)(int32_t)((ph & 0xFFFF000000000000ull) >> 32) * 4.656612873077393e-10f;
                 float sn, cs;
                 sincospif(x, &sn, &cs);
-                accf[k][0] += cs;
-                accf[k][1] += sn;
+                const float t0 = accf[k][0] + cs, t1 = accf[k][1] + sn;
+                cmpf[k][0] += cs - (t0 - accf[k][0]);
+                cmpf[k][1] += sn - (t1 - accf[k][1]);
+                accf[k][0] = t0;
+                accf[k][1] = t1;
                 ph += d;
             }
         }
 #pragma unroll
         for (int k = 0; k < NOALLOC_Q; k++) {
-            accd[k][0] += (double)accf[k][0];
-            accd[k][1] += (double)accf[k][1];
+            accd[k][0] += (double)accf[k][0] + (double)cmpf[k][0];
+            accd[k][1] += (double)accf[k][1] + (double)cmpf[k][1];
         }
     }
     if (!valid) return;
@@ -194,6 +233,12 @@ extern "C" int dgpu_four_strucf_noalloc(void *stream, const double *d_xat, int64
     int rc = scratch_address(&base);
     if (rc) return rc;
     cudaStream_t st = (cudaStream_t)stream;
+    if (st) {
+        // the scratch address and the launches belong to the current device
+        int sdev = -1, dev = -2;
+        if (cudaStreamGetDevice(st, &sdev) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess) return DGPU_ERR_ARG;
+        if (sdev != dev) return DGPU_ERR_ARG;
+    }
     Geo g;
     for (int k = 0; k < 3; k++) {
         g.u[k] = uin[k];

@@ -17,9 +17,10 @@
 //  * k_refine_select: one thread per point of the Friedel-reduced box,
 //    appends the flagged points to a list;
 //  * k_refine_sums: work item = (8 listed points, type, atom slice);
-//    FP64 partial per (point, type, slice).  The list is sorted, so that a
-//    point is usually the previous one plus one step along box axis 0 and
-//    its phase the previous phase plus one 64-bit add;
+//    FP64 partial per (point, type, slice).  The list is sorted with the
+//    box axis along which the flagged points are most often neighbours
+//    innermost, so that a point is usually the previous one plus one step
+//    along that axis and its phase the previous phase plus one 64-bit add;
 //  * k_refine_combine: one thread per listed point.
 #include <algorithm>
 #include <vector>
@@ -29,7 +30,8 @@
 
 #define RF_PTS 8            // points per work item (each atom's data is read once for all of them)
 #define RF_NT 256
-#define RF_CHUNK 16         // atoms per FP32 partial before it is added in FP64
+#define RF_CHUNK 16         // atoms per FP32 partial before it is added in FP64 (at the most coherent
+                            // points FP32 chunks of 32 atoms round alike chunk after chunk: 1.8e-5)
 #define RF_SLICE 65536      // atoms per work item
 
 struct RefineTypes {
@@ -71,12 +73,52 @@ __device__ __forceinline__ double warp_sum(double v)
     return v;
 }
 
+// The atoms of one work item: FP32 sums of RF_CHUNK atoms per point, added
+// to FP64.  RUN: the points are consecutive along the step axis sa and
+// their phases one 64-bit add apart.
+template <bool RUN>
+__device__ __forceinline__ void refine_loop(int64_t lo, int64_t hi, const uint64_t *__restrict__ ph0,
+                                            const uint64_t *__restrict__ du, const uint64_t *__restrict__ dv,
+                                            const uint64_t *__restrict__ dw, const float *__restrict__ w,
+                                            const uint32_t (&n0)[RF_PTS], const uint32_t (&n1)[RF_PTS],
+                                            const uint32_t (&n2)[RF_PTS], const bool (&stp)[RF_PTS],
+                                            double (&acc)[RF_PTS][2], float (&chk)[RF_PTS][2], int sa)
+{
+    int c = 0;
+    for (int64_t a = lo + threadIdx.x; a < hi; a += RF_NT) {
+        const uint64_t b = ph0[a], d0 = du[a], d1 = dv[a], d2 = dw[a];
+        const uint64_t ds = sa == 0 ? d0 : sa == 1 ? d1 : d2;
+        const float wa = w[a];
+        uint64_t ph = b + (uint64_t)n0[0] * d0 + (uint64_t)n1[0] * d1 + (uint64_t)n2[0] * d2;
+#pragma unroll
+        for (int k = 0; k < RF_PTS; k++) {
+            if (k > 0) {
+                if (RUN || stp[k]) ph += ds;
+                else ph = b + (uint64_t)n0[k] * d0 + (uint64_t)n1[k] * d1 + (uint64_t)n2[k] * d2;
+            }
+            const float2 e = phasor_acc(ph);
+            chk[k][0] = fmaf(wa, e.x, chk[k][0]);
+            chk[k][1] = fmaf(wa, e.y, chk[k][1]);
+        }
+        if (++c == RF_CHUNK) {
+            c = 0;
+#pragma unroll
+            for (int k = 0; k < RF_PTS; k++) {
+                acc[k][0] += (double)chk[k][0];
+                acc[k][1] += (double)chk[k][1];
+                chk[k][0] = chk[k][1] = 0.f;
+            }
+        }
+    }
+}
+
 // out[((k * ntype + t) * nsl + s)]: the type-t sum over atom slice s at
 // listed point k (box coordinates from the list entry)
 __global__ void __launch_bounds__(RF_NT, 2)
 k_refine_sums(const int32_t *__restrict__ list, int32_t npts, BoxSpec box, const uint64_t *__restrict__ ph0,
               const uint64_t *__restrict__ du, const uint64_t *__restrict__ dv, const uint64_t *__restrict__ dw,
-              const float *__restrict__ w, const RefineTypes rt, int32_t nsl, double2 *__restrict__ out)
+              const float *__restrict__ w, const RefineTypes rt, int32_t nsl, int32_t sa,
+              double2 *__restrict__ out)
 {
     __shared__ double red[RF_NT / 32][RF_PTS][2];
     const int64_t item = blockIdx.x;
@@ -85,16 +127,22 @@ k_refine_sums(const int32_t *__restrict__ list, int32_t npts, BoxSpec box, const
     const int pg = (int)(item / ((int64_t)nsl * rt.ntype));
     const int64_t lo = rt.ts[t] + (int64_t)s * RF_SLICE;
     const int64_t hi = min(rt.ts[t + 1], lo + RF_SLICE);
-    // the points' box coordinates; stp[k]: point k is point k-1 plus one step along axis 0
+    // the points' box coordinates; stp[k]: point k is point k-1 plus one step along axis sa
     __shared__ uint32_t s_n[RF_PTS][3];
     __shared__ int32_t s_stp[RF_PTS];
     if (threadIdx.x < RF_PTS) {
         const int k = threadIdx.x, pk = pg * RF_PTS + k;
-        const int64_t p = pk < npts ? list[pk] : 0, q = pk > 0 && pk - 1 < npts ? list[pk - 1] : -2;
-        s_n[k][0] = (uint32_t)(p % box.f[0]);
-        s_n[k][1] = (uint32_t)((p / box.f[0]) % box.f[1]);
-        s_n[k][2] = (uint32_t)(p / ((int64_t)box.f[0] * box.f[1]));
-        s_stp[k] = k > 0 && p == q + 1 && p % box.f[0] != 0;
+        const int64_t p = pk < npts ? list[pk] : 0, q = pk > 0 && pk - 1 < npts ? list[pk - 1] : 0;
+        const uint32_t c[3] = {(uint32_t)(p % box.f[0]), (uint32_t)((p / box.f[0]) % box.f[1]),
+                               (uint32_t)(p / ((int64_t)box.f[0] * box.f[1]))};
+        const uint32_t e[3] = {(uint32_t)(q % box.f[0]), (uint32_t)((q / box.f[0]) % box.f[1]),
+                               (uint32_t)(q / ((int64_t)box.f[0] * box.f[1]))};
+        bool st = k > 0 && pk < npts;
+        for (int a = 0; a < 3; a++) {
+            s_n[k][a] = c[a];
+            st = st && c[a] == e[a] + (a == sa ? 1u : 0u);
+        }
+        s_stp[k] = st;
     }
     __syncthreads();
     uint32_t n0[RF_PTS], n1[RF_PTS], n2[RF_PTS];
@@ -110,28 +158,13 @@ k_refine_sums(const int32_t *__restrict__ list, int32_t npts, BoxSpec box, const
     float chk[RF_PTS][2];
 #pragma unroll
     for (int k = 0; k < RF_PTS; k++) acc[k][0] = acc[k][1] = chk[k][0] = chk[k][1] = 0.f;
-    int c = 0;
-    for (int64_t a = lo + threadIdx.x; a < hi; a += RF_NT) {
-        const uint64_t b = ph0[a], d0 = du[a], d1 = dv[a], d2 = dw[a];
-        const float wa = w[a];
-        uint64_t ph = 0;
+    bool run = true;                 // every point the previous one plus one step along axis sa
 #pragma unroll
-        for (int k = 0; k < RF_PTS; k++) {
-            ph = stp[k] ? ph + d0 : b + (uint64_t)n0[k] * d0 + (uint64_t)n1[k] * d1 + (uint64_t)n2[k] * d2;
-            const float2 e = phasor_acc(ph);
-            chk[k][0] = fmaf(wa, e.x, chk[k][0]);
-            chk[k][1] = fmaf(wa, e.y, chk[k][1]);
-        }
-        if (++c == RF_CHUNK) {
-            c = 0;
-#pragma unroll
-            for (int k = 0; k < RF_PTS; k++) {
-                acc[k][0] += (double)chk[k][0];
-                acc[k][1] += (double)chk[k][1];
-                chk[k][0] = chk[k][1] = 0.f;
-            }
-        }
-    }
+    for (int k = 1; k < RF_PTS; k++) run = run && stp[k];
+    if (run)
+        refine_loop<true>(lo, hi, ph0, du, dv, dw, w, n0, n1, n2, stp, acc, chk, sa);
+    else
+        refine_loop<false>(lo, hi, ph0, du, dv, dw, w, n0, n1, n2, stp, acc, chk, sa);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < RF_PTS; k++) {
@@ -248,13 +281,36 @@ int dgpu_refine_aver(dgpu_ctx *ctx, const RefineSpec &r, double2 *csf, double2 *
     DGPU_CUDA(ctx, cudaMemcpyAsync(&npts, d_count, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
     DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));      // the FormSpec blocks and npts
     if (npts == 0) return DGPU_OK;
+    int32_t sa = 0;
     {
-        // box order (the appends above come in no fixed order)
+        // The appends above come in no fixed order.  Step axis: the box axis
+        // along which flagged points most often have a flagged neighbour;
+        // the list is sorted with that axis innermost.
         std::vector<int32_t> h((size_t)npts);
         DGPU_CUDA(ctx, cudaMemcpyAsync(h.data(), d_list, (size_t)npts * sizeof(int32_t), cudaMemcpyDeviceToHost,
                                        ctx->stream));
         DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         std::sort(h.begin(), h.end());
+        const int64_t st[3] = {1, box.f[0], (int64_t)box.f[0] * box.f[1]};
+        int64_t best = -1;
+        for (int a = 0; a < 3; a++) {
+            if (box.f[a] < 2) continue;
+            int64_t adj = 0;
+            for (int32_t p : h) {
+                const int64_t c = (p / st[a]) % box.f[a];
+                if (c + 1 < box.f[a] && std::binary_search(h.begin(), h.end(), (int32_t)(p + st[a]))) adj++;
+            }
+            if (adj > best) {
+                best = adj;
+                sa = a;
+            }
+        }
+        const int o1 = sa == 0 ? 1 : 0, o2 = 3 - sa - o1;     // the other axes, outer
+        auto key = [&](int32_t p) {
+            const int64_t c[3] = {p % box.f[0], (p / box.f[0]) % box.f[1], p / ((int64_t)box.f[0] * box.f[1])};
+            return (c[o2] * box.f[o1] + c[o1]) * box.f[sa] + c[sa];
+        };
+        std::sort(h.begin(), h.end(), [&](int32_t x, int32_t y) { return key(x) < key(y); });
         DGPU_CUDA(ctx, cudaMemcpyAsync(d_list, h.data(), (size_t)npts * sizeof(int32_t), cudaMemcpyHostToDevice,
                                        ctx->stream));
         DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));   // h is a host temporary
@@ -264,17 +320,17 @@ int dgpu_refine_aver(dgpu_ctx *ctx, const RefineSpec &r, double2 *csf, double2 *
     DGPU_CUDA(ctx, ctx->rsum.ensure((size_t)npts * ((size_t)r.ngroup * nslf + (size_t)r.nscat * nsla) *
                                     sizeof(double2)));
     double2 *sf = ctx->rsum.as<double2>();
-    double2 *sa = sf + (size_t)npts * r.ngroup * nslf;
+    double2 *sa_sum = sf + (size_t)npts * r.ngroup * nslf;
     const int64_t itf = ngrp * r.ngroup * nslf, ita = ngrp * r.nscat * nsla;
     if (itf > 0x7fffffffLL || ita > 0x7fffffffLL) return dgpu_set_error(ctx, DGPU_ERR_ARG, "refinement too large");
     k_refine_sums<<<(unsigned)itf, RF_NT, 0, ctx->stream>>>(d_list, npts, box, r.ph0, r.du, r.dv, r.dw, r.w, rm,
-                                                            nslf, sf);
+                                                            nslf, sa, sf);
     DGPU_CUDA(ctx, cudaGetLastError());
     k_refine_sums<<<(unsigned)ita, RF_NT, 0, ctx->stream>>>(d_list, npts, box, r.aph0, r.adu, r.adv, r.adw, r.aw, ra,
-                                                            nsla, sa);
+                                                            nsla, sa, sa_sum);
     DGPU_CUDA(ctx, cudaGetLastError());
     k_refine_combine<<<(unsigned)dgpu_cdiv(npts, 128), 128, 0, ctx->stream>>>(
-        d_list, npts, d_fsm, d_fst, box, r.istl, r.cfact, sf, nslf, sa, nsla, r.lat_n[0], r.lat_n[1], r.lat_n[2],
+        d_list, npts, d_fsm, d_fst, box, r.istl, r.cfact, sf, nslf, sa_sum, nsla, r.lat_n[0], r.lat_n[1], r.lat_n[2],
         r.lat_d[0], r.lat_d[1], r.lat_d[2], r.norm, r.diff_scale, sqrt(r.diff_scale), csf, acsf, dsi);
     DGPU_CUDA(ctx, cudaGetLastError());
     *nref = npts;

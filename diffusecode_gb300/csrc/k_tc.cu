@@ -852,13 +852,37 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
 
 // FP64 -> FP32 with stochastic rounding: y rounds up with probability equal
 // to its distance from the lower neighbour in units of the spacing (u is a
-// uniform 32-bit draw), so the rounding error has mean zero over draws.
+// uniform 32-bit draw), so the rounding error has mean zero over draws.  The
+// spacing is a power of two, so the division is exact in FP32.
 __device__ __forceinline__ float round_stochastic(double y, uint32_t u)
 {
     const float lo = __double2float_rd(y), hi = __double2float_ru(y);
     if (lo == hi) return lo;
-    const double p = (y - (double)lo) / ((double)hi - (double)lo);
-    return (double)u * 0x1p-32 < p ? hi : lo;
+    const float p = (float)(y - (double)lo) * (1.0f / (hi - lo));
+    return (float)(u >> 8) * 0x1p-24f < p ? hi : lo;
+}
+
+// exp(2 pi i t) for a 64-bit fixed-point turn t, in FP64 to about 1e-16:
+// the table entry of its top 12 bits (tab[k] = exp(2 pi i k / 4096)) times
+// exp(i e) of the remaining angle e < 2 pi 2^-12, by its Taylor series
+// (the first omitted terms are below 1e-16).
+__device__ __forceinline__ double2 phasor_f64(uint64_t t, const double2 *__restrict__ tab)
+{
+    const double2 a = tab[t >> 52];
+    const double e = (double)(t & 0xFFFFFFFFFFFFFull) * (6.283185307179586 * 0x1p-64);
+    const double e2 = e * e;
+    const double c = 1.0 - e2 * (0.5 - e2 * (1.0 / 24.0));
+    const double s = e * (1.0 - e2 * (1.0 / 6.0));
+    return make_double2(a.x * c - a.y * s, a.x * s + a.y * c);
+}
+
+__global__ void k_tc_tab(double2 *tab)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= 4096) return;
+    double s, c;
+    sincospi((double)k / 2048.0, &s, &c);
+    tab[k] = make_double2(c, s);
 }
 
 __device__ __forceinline__ uint64_t mix64(uint64_t z)
@@ -869,29 +893,29 @@ __device__ __forceinline__ uint64_t mix64(uint64_t z)
 }
 
 // Per-atom step factors exp(2 pi i 8 d) and exp(2 pi i 16 d) along the three
-// grid axes: FP64 sincospi of the exact turn, rounded stochastically to FP32
-// (a draw per atom and component).  The producers step a row by these
+// grid axes: FP64 values (table and Taylor series; the square of the first
+// for the second), rounded stochastically to FP32 (a draw per atom and
+// component).  The producers step a row by these
 // factors up to 16 times, so a factor's rounding error recurs in every value
 // of the chain; atoms at equivalent positions have identical increments, and
 // with round-to-nearest their chains would share one error and add it up
 // coherently.  Stochastic rounding gives each atom its own, zero-mean error.
 __global__ void k_tc_mult(const uint64_t *__restrict__ du, const uint64_t *__restrict__ dv,
-                          const uint64_t *__restrict__ dw, int64_t n, int64_t stride, float2 *__restrict__ out)
+                          const uint64_t *__restrict__ dw, int64_t n, int64_t stride,
+                          const double2 *__restrict__ tab, float2 *__restrict__ out)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint64_t *d[3] = {du, dv, dw};
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-#pragma unroll
-        for (int k = 0; k < 2; k++) {                   // 8 d, then 16 d
-            const int64_t v = (int64_t)(d[a][i] << (3 + k));
-            double s, c;
-            sincospi((double)v * 0x1p-63, &s, &c);     // angle pi x, x = 2 turns in [-1, 1)
-            const uint64_t r = mix64((uint64_t)i * 8u + (uint64_t)(2 * a + k) + 0x9E3779B97F4A7C15ull);
-            out[(3 * k + a) * stride + i] =
-                make_float2(round_stochastic(c, (uint32_t)r), round_stochastic(s, (uint32_t)(r >> 32)));
-        }
+        const double2 m = phasor_f64(d[a][i] << 3, tab);
+        const double2 m2 = make_double2(m.x * m.x - m.y * m.y, 2.0 * m.x * m.y);
+        const uint64_t r = mix64((uint64_t)i * 4u + (uint64_t)a + 0x9E3779B97F4A7C15ull);
+        const uint64_t q = mix64(r);
+        out[a * stride + i] = make_float2(round_stochastic(m.x, (uint32_t)r), round_stochastic(m.y, (uint32_t)(r >> 32)));
+        out[(3 + a) * stride + i] =
+            make_float2(round_stochastic(m2.x, (uint32_t)q), round_stochastic(m2.y, (uint32_t)(q >> 32)));
     }
 }
 
@@ -938,6 +962,15 @@ __global__ void __launch_bounds__(256) k_tc_vgen(const uint64_t *__restrict__ da
 }
 
 // ---------------------------------------------------------------------------
+int dgpu_tc_init(dgpu_ctx *ctx)
+{
+    DGPU_CUDA(ctx, ctx->tc_tab.ensure(4096 * sizeof(double2)));
+    k_tc_tab<<<16, 256, 0, ctx->stream>>>(ctx->tc_tab.as<double2>());
+    DGPU_CUDA(ctx, cudaGetLastError());
+    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return DGPU_OK;
+}
+
 bool dgpu_tc_available(dgpu_ctx *ctx)
 {
     if (ctx->tc_avail < 0) {
@@ -1209,7 +1242,8 @@ int dgpu_tc_mult_async(dgpu_ctx *ctx, const uint64_t *du, const uint64_t *dv, co
                        int64_t stride, float2 *out)
 {
     if (n < 1) return DGPU_OK;
-    k_tc_mult<<<(unsigned)dgpu_cdiv(n, 256), 256, 0, ctx->stream>>>(du, dv, dw, n, stride, out);
+    k_tc_mult<<<(unsigned)dgpu_cdiv(n, 256), 256, 0, ctx->stream>>>(du, dv, dw, n, stride,
+                                                                      ctx->tc_tab.as<double2>(), out);
     DGPU_CUDA(ctx, cudaGetLastError());
     return DGPU_OK;
 }

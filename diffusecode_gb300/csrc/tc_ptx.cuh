@@ -223,17 +223,20 @@ __device__ __forceinline__ float2 phasor_fast(uint64_t ph)
 __device__ __forceinline__ uint64_t tc_rot(uint64_t j) { return j * 0x9E3779B97F4A7C15ull; }
 
 // exp(2 pi i phase) of a 64-bit fixed-point turn to about one FP32 ulp: the
-// signed phase as x = 2 turns in [-1, 1) splits into its top 24 bits (exact
-// in FP32, evaluated by sincospif) and a remainder below 2^-23 (its next 24
-// bits, 32-bit conversions only) applied as a first-order rotation.  Used where a value is evaluated once per launch (the
-// V operand images); the kernels' seeds use the hardware approximation above,
-// whose error (a few 1e-7, a smooth function of the phase) tc_rot makes
+// signed phase as x = 2 turns in [-1, 1) splits into its top 23 bits (exact
+// in FP32, evaluated by sincospif) and a remainder below 2^-22 (its next 23
+// bits) applied as a first-order rotation; both integers become floats by the
+// exponent-bias construction (an integer add and one FP32 subtract), not by a
+// conversion instruction.  Used where a value is evaluated once per launch
+// (the V operand images); the kernels' seeds use the hardware approximation
+// above, whose error (a few 1e-7, a smooth function of the phase) tc_rot makes
 // random from atom to atom.
 __device__ __forceinline__ float2 phasor_acc(uint64_t ph)
 {
-    const int64_t v = (int64_t)ph;
-    const float xf = (float)(int32_t)(v >> 40) * 0x1p-23f;
-    const float dth = (float)((uint32_t)(ph >> 16) & 0xFFFFFFu) * (3.14159265358979f * 0x1p-47f);
+    const int32_t hi = (int32_t)((int64_t)ph >> 41);                  // in [-2^22, 2^22)
+    const uint32_t lo = (uint32_t)(ph >> 18) & 0x7FFFFFu;               // in [0, 2^23)
+    const float xf = (__int_as_float(0x4B400000 + hi) - 12582912.0f) * 0x1p-22f;
+    const float dth = (__uint_as_float(0x4B000000u | lo) - 8388608.0f) * (3.14159265358979f * 0x1p-45f);
     float s, c;
     sincospif(xf, &s, &c);
     return make_float2(fmaf(-s, dth, c), fmaf(c, dth, s));

@@ -215,14 +215,19 @@ int dgpu_four_strucf(dgpu_ctx *ctx, const double *xat, int64_t nxat,
  * enqueuing on a stream it does not own.  It has no counterpart in the
  * reference.  All pointers named d_* are device memory, arrays as in
  * dgpu_four_strucf (cfact = complex(0:CFPKT) or NULL, istl int32 num points,
- * tcsf complex num points); stream is a cudaStream_t (NULL = default stream).
- * The call only enqueues work: the result is ready when the stream reaches it.
+ * tcsf complex num points); stream is a cudaStream_t (NULL = default stream)
+ * of the device that is current at the call (another device's stream:
+ * DGPU_ERR_ARG).  The call only enqueues work: the result is ready when the
+ * stream reaches it.  An istl value outside 0..CFPKT gives a NaN at that
+ * point (no table read).
  * Working memory is one fixed __device__ array per GPU (8.5 MiB, held until
  * process exit): at most 131072 atoms and 262144 computed points
  * (fnum(1)*fnum(2)*fnum(3)) per call, else DGPU_ERR_SCRATCH_SIZE.  Calls that
  * overlap on the GPU share that array and race; calls on one stream are safe.
  * The first call on a device looks the array up (cudaGetSymbolAddress) and
- * should come before any stream capture.                                     */
+ * should come before any stream capture; it is looked up again when a later
+ * call finds another CUDA context current on that device (after
+ * cudaDeviceReset, say).                                                     */
 int dgpu_four_strucf_noalloc(void *stream, const double *d_xat, int64_t nxat,
                              const double uin[3], const double vin[3], const double win[3],
                              const double off_shift[9], const int32_t lmn[6],
@@ -392,6 +397,15 @@ int dgpu_powder_complete(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_powde
 int dgpu_chi2_grad(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid,
                    const dgpu_opts *opts, const double *i_target, const double *weight,
                    double *chi2, double *grad_pos, double *grad_occ, dgpu_info *info);
+
+/* Same as dgpu_chi2_grad with everything per atom and per point resident in
+ * HBM: cr->pos, cr->iscat, cr->atom_occ (and cr->ianis), d_i_target,
+ * d_weight, d_grad_pos and d_grad_occ are DEVICE pointers; chi2 is a host
+ * double.  For optimisation loops that keep the crystal on the GPU (the
+ * torch.autograd wrapper): no per-atom or per-point host copy per call.     */
+int dgpu_chi2_grad_device(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid,
+                          const dgpu_opts *opts, const double *d_i_target, const double *d_weight,
+                          double *chi2, double *d_grad_pos, double *d_grad_occ, dgpu_info *info);
 
 /* ---- batched population --------------------------------------------------- */
 /* Many independent crystals (a DIFFEV population, diffev/prog/with_mpi.f90:281-510

@@ -114,6 +114,30 @@ def test_autograd_wrapper(ctx):
     np.testing.assert_allclose(occ.grad.numpy(), go, rtol=1e-12)
 
 
+@pytest.mark.parametrize("engine", [_abi.ENGINE_DIRECT, _abi.ENGINE_TC])
+def test_autograd_wrapper_device_tensors(ctx, engine):
+    """CUDA tensors take the device-resident entry (dgpu_chi2_grad_device):
+    the same chi2 and gradients as the host entry on the same context (whose
+    tuned tensor-core tile both then use), and a second call reusing the
+    context's buffers agrees with the first."""
+    import torch
+    from diffusecode_gb300.autograd import chi2, chi2_grad
+    cr, g = S.small_random(seed=5, natoms=200, nscat=2, inc=(11, 9, 5))
+    it, wt = _target(cr, g, ctx)
+    op = K.opts(phase=_abi.PHASE_EXACT64, engine=engine)
+    dev = torch.device("cuda:0")
+    occ_h = np.linspace(0.9, 1.1, cr.natoms).astype(np.float32)
+    c2, gp, go, _ = chi2_grad(cr.with_positions(cr.pos, occ_h), g, op, it, wt)     # the default context
+    for _ in range(2):
+        pos = torch.tensor(cr.pos, device=dev, requires_grad=True)
+        occ = torch.tensor(occ_h, device=dev, requires_grad=True)
+        val = chi2(pos, occ, cr, g, op, torch.from_numpy(it).to(dev), torch.from_numpy(wt).to(dev))
+        val.backward()
+        assert abs(val.item() - c2) <= 1e-12 * c2
+        np.testing.assert_allclose(pos.grad.cpu().numpy(), gp, rtol=1e-12, atol=1e-12 * np.abs(gp).max())
+        np.testing.assert_allclose(occ.grad.cpu().numpy(), go, rtol=1e-6, atol=1e-9 * np.abs(go).max())
+
+
 def test_gradient_rejects_average(ctx):
     from diffusecode_gb300.autograd import chi2_grad
     cr, g = S.small_random(seed=4, natoms=30, inc=(5, 5, 3))
