@@ -123,6 +123,7 @@ class Opts(C.Structure):
         ("lperiod", C.c_int32),
         ("lot_origins", _ip),
         ("tc_vimg", C.c_int32),
+        ("tc_wait_us", C.c_int32),
     ]
 
 
@@ -227,6 +228,7 @@ def default_opts(**kw):
     o.lperiod = 1
     o.lot_origins = C.cast(None, _ip)
     o.tc_vimg = 0
+    o.tc_wait_us = 0
     for k, v in kw.items():
         if k in ("aver_cells", "lot_origins"):
             continue

@@ -53,6 +53,7 @@ extern "C" void dgpu_default_opts(dgpu_opts *o)
     o->lperiod = 1;
     o->lot_origins = nullptr;
     o->tc_vimg = 0;
+    o->tc_wait_us = 0;
 }
 
 extern "C" int dgpu_ctx_create(int device, dgpu_ctx **out)

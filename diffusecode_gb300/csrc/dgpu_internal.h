@@ -259,6 +259,7 @@ struct TcLaunch {
     int32_t vring;              // V operand streamed from images through a shared-memory ring
     uint32_t tmem_cols;
     int32_t *err;
+    uint64_t timeout_ns;        // limit of one wait for another warp's progress
 };
 
 #include <vector>

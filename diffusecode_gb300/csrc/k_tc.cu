@@ -519,7 +519,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
             load_pair(cur, src, a0 + kq);
             for (int st = 0; st < nst; st++, it++) {
                 if (st + 1 < nst) load_pair(nxt, src, a0 + (int64_t)(st + 1) * TC_KB + kq);
-                const bool got = round == 0 || mbar_wait(&empty[sb], (round - 1) & 1, err, 1);
+                const bool got = round == 0 || mbar_wait(&empty[sb], (round - 1) & 1, err, 1, L.timeout_ns);
                 if (!__all_sync(0xffffffffu, got)) {
                     ok = false;
                     break;
@@ -575,7 +575,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
             for (int st = 0; st < nst; st++, it++) {
                 cp_async_wait1();           // group st has landed (only the newest may be pending)
                 // one thread waits for the stage buffer, the barrier tells everybody
-                if (tid == 0 && ok && round > 0) ok = mbar_wait(&empty[sb], (round - 1) & 1, err, 1);
+                if (tid == 0 && ok && round > 0)
+                    ok = mbar_wait(&empty[sb], (round - 1) & 1, err, 1, L.timeout_ns);
                 if (producers_sync(!ok)) break;   // staged for every producer; slot of st-1 and stage sb free
                 if (st + 2 < nst)
                     stage_atoms(src, aslot + ((st + 2) % TC_NSLOT) * TC_ATOM_SLOT, a0 + (int64_t)(st + 2) * TC_KA,
@@ -624,14 +625,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
                 // B rows N.. : [Vi; -Vr]
                 const uint32_t b2off = (uint32_t)(N >> 3) * (L.vring ? TC_SBO128 : TC_SBO);
                 // the correction accumulator restarts with this item: previous one drained?
-                if (nitem > 0 && !mbar_wait(cempty, (nitem - 1) & 1, err, 2)) {
+                if (nitem > 0 && !mbar_wait(cempty, (nitem - 1) & 1, err, 2, L.timeout_ns)) {
                     ok = false;
                     break;
                 }
                 for (int st0 = 0; st0 < nst && ok; st0 += L.flush, nchunk++) {
                     const int b = (int)(nchunk % L.nbuf);
                     const uint32_t use = nchunk / L.nbuf;
-                    if (use > 0 && !mbar_wait(&mempty[b], (use - 1) & 1, err, 6)) {
+                    if (use > 0 && !mbar_wait(&mempty[b], (use - 1) & 1, err, 6, L.timeout_ns)) {
                         ok = false;
                         break;
                     }
@@ -639,8 +640,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
                     const uint32_t m_acc = tmem + 2u * NM * (1u + (uint32_t)b);
                     const int st1 = min(nst, st0 + L.flush);
                     for (int st = st0; st < st1; st++, it++) {
-                        if (!mbar_wait(&full[s], round & 1, err, 3) ||
-                            (L.vring && !mbar_wait(&vfull[it % TC_VSLOTS], (it / TC_VSLOTS) & 1, err, 8))) {
+                        if (!mbar_wait(&full[s], round & 1, err, 3, L.timeout_ns) ||
+                            (L.vring &&
+                             !mbar_wait(&vfull[it % TC_VSLOTS], (it / TC_VSLOTS) & 1, err, 8, L.timeout_ns))) {
                             ok = false;
                             break;
                         }
@@ -726,15 +728,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
             }
             for (int st0 = 0; st0 < nst; st0 += L.flush, nchunk++) {
                 const int b = (int)(nchunk % L.nbuf);
-                if (!__shfl_sync(0xffffffffu, lane == 0 ? mbar_wait(&mfull[b], (nchunk / L.nbuf) & 1, err, 5) : true,
-                                 0)) {
+                const bool got = lane == 0 ? mbar_wait(&mfull[b], (nchunk / L.nbuf) & 1, err, 5, L.timeout_ns) : true;
+                if (!__shfl_sync(0xffffffffu, got, 0)) {
                     ok = false;
                     break;
                 }
                 tc_fence_after();
                 const bool first = st0 == 0, last = st0 + L.flush >= nst;
                 if (last) {                                        // the item's corrections
-                    if (!__shfl_sync(0xffffffffu, lane == 0 ? mbar_wait(cfull, nitem & 1, err, 7) : true, 0)) {
+                    const bool gc = lane == 0 ? mbar_wait(cfull, nitem & 1, err, 7, L.timeout_ns) : true;
+                    if (!__shfl_sync(0xffffffffu, gc, 0)) {
                         ok = false;
                         break;
                     }
@@ -825,7 +828,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
                 for (int y = 0; y < nst; y++, x++) {
                     const int v = (int)(x % TC_VSLOTS);
                     if (x >= TC_VSLOTS) {
-                        if (!mbar_wait(&vempty[v], ((x / TC_VSLOTS) - 1) & 1, err, 9)) {
+                        if (!mbar_wait(&vempty[v], ((x / TC_VSLOTS) - 1) & 1, err, 9, L.timeout_ns)) {
                             ok = false;
                             break;
                         }
@@ -1198,6 +1201,7 @@ int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *o
     }
     DGPU_CUDA(ctx, ctx->flag.ensure(64));
     L.err = ctx->flag.as<int32_t>() + 8;
+    L.timeout_ns = op->tc_wait_us > 0 ? (uint64_t)op->tc_wait_us * 1000ull : TC_TIMEOUT_NS;
     return DGPU_OK;
 }
 

@@ -59,15 +59,17 @@ __device__ __forceinline__ bool mbar_try_suspend(uint64_t *bar, uint32_t parity)
     return ok != 0;
 }
 
-// bounded wait: false if the error flag is up or the wait timed out
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int32_t *err, int code)
+// bounded wait for another warp's progress: false if the error flag is up or
+// the wait ran longer than limit_ns (recorded as `code` in the flag)
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int32_t *err, int code,
+                                          uint64_t limit_ns = TC_TIMEOUT_NS)
 {
     if (mbar_try(bar, parity)) return true;
     const uint64_t t0 = gtimer();
     for (;;) {
         if (mbar_try_suspend(bar, parity)) return true;
         if (*err) return false;
-        if (gtimer() - t0 > TC_TIMEOUT_NS) {
+        if (gtimer() - t0 > limit_ns) {
             atomicCAS((int32_t *)err, 0, code);
             return false;
         }
@@ -94,8 +96,9 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
         : "memory");
 }
 
-// wait that ignores the error flag (time-bounded): used to let the CTA's own
-// bulk copies land before it exits after an error
+// wait that ignores the error flag (time-bounded, always the full
+// TC_TIMEOUT_NS): used to let the CTA's own MMAs and bulk copies complete
+// before it frees TMEM and exits after an error
 __device__ __forceinline__ void mbar_wait_quiet(uint64_t *bar, uint32_t parity)
 {
     const uint64_t t0 = gtimer();

@@ -146,6 +146,12 @@ typedef struct dgpu_opts {
                                   (fourier_sup.f90:2513-2530); unused with lot_all  */
     int32_t tc_vimg;        /* tensor-core V operand: 0 auto (images when each is
                                re-read by 4+ row tiles), 1 images, -1 in-kernel  */
+    int32_t tc_wait_us;     /* tensor-core type sums: limit of one wait of a warp
+                               for another's progress, microseconds (0: 2 s).  A
+                               wait that runs out stops the kernel, which waits
+                               for its own MMAs and copies, frees its tensor
+                               memory and returns DGPU_ERR_TIMEOUT; the context
+                               stays usable.  For tests of that path.            */
 } dgpu_opts;
 
 /* What four_run reports besides the arrays. */

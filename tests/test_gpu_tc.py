@@ -102,6 +102,25 @@ def test_tc_against_reference_arithmetic(oracle, ctx, case):
     assert err <= tol
 
 
+@pytest.mark.parametrize("vimg", [1, -1], ids=["v-images", "v-in-kernel"])
+def test_tc_wait_limit_runs_out_and_context_recovers(oracle, ctx, vimg):
+    """Failure detection on the device without a fault: with a 1 us limit on
+    every wait of one warp for another's progress, the drain warps' first
+    wait for the MMAs cannot be met; the kernel stops, waits for its own MMAs
+    and copies, frees its tensor memory, and the call returns
+    DGPU_ERR_TIMEOUT.  The next call on the same context, with the default
+    limit, gives the oracle's result."""
+    cr, g = S.perovskite_plane(cells=6)
+    with pytest.raises(Exception) as e:
+        FR.four_run(cr, g, tc_opts(tc_vimg=vimg, tc_wait_us=1), ctx=ctx)
+    assert getattr(e.value, "code", None) == _abi.DGPU_ERR_TIMEOUT
+    op = tc_opts(tc_vimg=vimg)
+    rc, csf, acsf, dsi, info = oracle.four_run(cr, g, op)
+    r = FR.four_run(cr, g, op, ctx=ctx)
+    assert r.info.engine_used == _abi.ENGINE_TC
+    assert K.rel_err(r.dsi, dsi, K.incoherent_floor(cr, g, op)) <= TOL
+
+
 def test_tc_ref22_rejected(ctx):
     cr, g = S.perovskite_plane(cells=2)
     with pytest.raises(Exception) as e:
