@@ -393,10 +393,79 @@ def fp64_points(cr, grid, idx, fave=0.0):
     return np.abs(F - Fav) ** 2, floor
 
 
-def adjoint_measure(ctx, engine, steps=3):
+def table_cfact(cr, h, ldbw=1):
+    """cfact of every type (rows 1..nscat) at the points h (P, 3), TABLE
+    form as four_stltab / four_formtab compute it: h rounded to REAL(4),
+    istl = NINT(s / 0.001), f(istl * 0.001) exp(-B s^2) occ (no anomalous
+    terms)."""
+    h32 = h.astype(np.float32).astype(np.float64)
+    q2 = np.einsum("pa,ab,pb->p", h32, cr.rten, h32) / 4.0
+    istl = np.floor(np.sqrt(q2) * 1000.0 + 0.5)
+    s2 = (istl * 0.001) ** 2
+    cf = np.zeros((cr.nscat + 1, h.shape[0]))
+    for t in range(1, cr.nscat + 1):
+        sc = cr.scat[t]
+        f = sc[0] + sum(sc[2 * i - 1] * np.exp(-sc[2 * i] * s2) for i in range(1, 5))
+        cf[t] = (np.exp(-cr.dw[t] * s2) if ldbw else 1.0) * cr.occ[t] * f
+    return cf
+
+
+def fp64_gradient_perfect_lattice(cr, grid, i_target, weight, atoms, ds=1.0, ldbw=1):
+    """chi2 = sum_h w (I - I_t)^2 and its gradient with respect to the
+    positions (lattice units) and occupancies of the listed atoms, in FP64,
+    for a crystal whose atoms sit exactly at cell + site (as the rock salt is
+    built): F(h) = L(h) sum_sites cfact exp(2 pi i h.u_s) with the lattice
+    sum L of the cell box, so that F costs O(points) and the gradient of one
+    atom one sum over the grid:
+        d chi2 / d w_j   = Re  sum_h g conj(F) c_t e_j,
+        d chi2 / d r_j,k = -2 pi w_j Im sum_h g conj(F) c_t h_k e_j,
+    g = 4 ds w (I - I_t), e_j = exp(2 pi i h.r_j)."""
+    ns, icc = cr.ncatoms, np.asarray(cr.icc)
+    j = np.arange(cr.natoms)
+    cell = j // ns
+    cvec = np.stack([cell % icc[0], (cell // icc[0]) % icc[1], cell // (icc[0] * icc[1])], 1).astype(np.float64)
+    u = cr.pos[:ns] - cvec[:ns]
+    if not np.array_equal(cr.pos, cvec + u[j % ns]) or not np.array_equal(cr.iscat, np.tile(cr.iscat[:ns], len(j) // ns)):
+        raise ValueError("not a perfect lattice of cell + site")
+    if cr.atom_occ is not None and not np.all(cr.atom_occ == 1.0):
+        raise ValueError("per-atom occupancies")
+    hk = grid.hkl()
+    h = np.stack([hk[a].reshape(-1, order="F") for a in range(3)], 1)
+    lat = np.ones(h.shape[0], complex)
+    for a in range(3):
+        lat *= np.exp(2j * np.pi * np.outer(h[:, a], np.arange(icc[a]))).sum(axis=1)
+    cf = table_cfact(cr, h, ldbw)
+    F = np.zeros(h.shape[0], complex)
+    for s in range(ns):
+        F += cf[cr.iscat[s]] * np.exp(2j * np.pi * (h @ u[s]))
+    F *= lat
+    I = ds * np.abs(F) ** 2
+    it = np.asarray(i_target, np.float64).reshape(-1, order="F")
+    wt = np.ones_like(it) if weight is None else np.asarray(weight, np.float64).reshape(-1, order="F")
+    chi2 = float(np.sum(wt * (I - it) ** 2))
+    g = 4.0 * ds * wt * (I - it)
+    gp = np.zeros((len(atoms), 3))
+    go = np.zeros(len(atoms))
+    for k0 in range(0, len(atoms), 16):
+        sel = np.asarray(atoms[k0:k0 + 16])
+        ph = h @ cr.pos[sel].T
+        ph -= np.round(ph)
+        e = np.exp(2j * np.pi * ph)                                # (P, m)
+        q = (g * np.conj(F))[:, None] * cf[cr.iscat[sel]].T * e
+        go[k0:k0 + len(sel)] = q.sum(axis=0).real
+        for a in range(3):
+            gp[k0:k0 + len(sel), a] = -2 * np.pi * (h[:, a:a + 1] * q).sum(axis=0).imag
+    return chi2, gp, go
+
+
+def adjoint_measure(ctx, engine, steps=3, check=True):
     """bwd/fwd on the gradient workload: rock salt a = 5.64 A, 25x25x20 cells
     x 8 = 100,000 atoms, 65^3 grid h,k,l in [-3.2,3.2]; target from a seeded
-    perturbed copy (0.05 A, occupancies +-0.1); w = 1/(I_target + 1)."""
+    perturbed copy (0.05 A, occupancies +-0.1); w = 1/(I_target + 1).
+    Accuracy at that scale, for 1000 seeded atoms: both engines' gradients
+    against the FP64 closed-form reference (fp64_gradient_perfect_lattice),
+    central differences of chi2 per coordinate (16 of the atoms) and along
+    random directions that move all 1000 atoms at once."""
     from diffusecode_gb300 import fourier as FR
     from diffusecode_gb300.autograd import chi2_grad
     cr, grid = S.rocksalt_volume()
@@ -412,9 +481,54 @@ def adjoint_measure(ctx, engine, steps=3):
             fwd.append(r.info.kernel_ms)
             bwd.append(info.total_ms)
     f, b = min(fwd), min(bwd)
-    return {"workload": "rocksalt-100000-atoms-65^3", "fwd_kernel_ms": f, "adjoint_ms": b,
-            "bwd_over_fwd": b / f, "chi2": c2,
-            "note": "adjoint = per-point weights + per-atom sums (tensor cores for the TC engine); fwd = type sums of the same engine"}
+    out = {"workload": "rocksalt-100000-atoms-65^3", "fwd_kernel_ms": f, "adjoint_ms": b,
+           "bwd_over_fwd": b / f, "chi2": c2,
+           "note": "adjoint = per-point weights + per-atom sums (tensor cores for the TC engine); "
+                   "fwd = type sums of the same engine"}
+    if not check:
+        return out
+    rng = np.random.Generator(np.random.PCG64(77))
+    atoms = np.sort(rng.choice(cr.natoms, 1000, replace=False))
+    c64, gp64, go64 = fp64_gradient_perfect_lattice(cr, grid, it, wt, atoms)
+    acc = {"atoms": 1000, "chi2_fp64": c64}
+    a_lat = 5.64
+    for name, eng in (("direct", _abi.ENGINE_DIRECT), ("tc", _abi.ENGINE_TC)):
+        o = _abi.default_opts(ldbw=1, phase=_abi.PHASE_EXACT64, engine=eng)
+        c, g_p, g_o, _ = chi2_grad(cr, grid, o, it, wt, ctx=ctx)
+        e = {"chi2_rel": abs(c - c64) / c64,
+             "grad_pos_max_rel": float(np.abs(g_p[atoms] - gp64).max() / np.abs(gp64).max()),
+             "grad_occ_max_rel": float(np.abs(g_o[atoms] - go64).max() / np.abs(go64).max())}
+        # central differences, step in A
+        for step in (1e-4, 1e-3):
+            hstep = step / a_lat
+            if name == "direct":
+                errs = []
+                for atom in atoms[:16]:
+                    for k in range(3):
+                        vals = []
+                        for sg in (1, -1):
+                            p = cr.pos.copy()
+                            p[atom, k] += sg * hstep
+                            vals.append(chi2_grad(cr.with_positions(p), grid, o, it, wt, ctx=ctx)[0])
+                        errs.append(abs((vals[0] - vals[1]) / (2 * hstep) - g_p[atom, k]))
+                e[f"fd_{step:g}A_per_coord_max_rel"] = float(max(errs) / np.abs(gp64).max())
+            derr = []
+            for d in range(3):
+                v = np.zeros_like(cr.pos)
+                v[atoms] = rng.normal(size=(len(atoms), 3))
+                v /= np.abs(v).max()
+                vals = []
+                for sg in (1, -1):
+                    vals.append(chi2_grad(cr.with_positions(cr.pos + sg * hstep * v), grid, o, it, wt, ctx=ctx)[0])
+                fd = (vals[0] - vals[1]) / (2 * hstep)
+                an = float(np.sum(v[atoms] * g_p[atoms]))
+                derr.append(abs(fd - an) / (np.abs(v[atoms]) * np.abs(g_p[atoms])).sum())
+            e[f"fd_{step:g}A_directional_max_rel"] = float(max(derr))
+        acc[name] = e
+    acc["norm"] = ("gradient errors relative to the largest FP64 component; directional differences relative "
+                   "to sum |v_j g_j| over the 1000 atoms")
+    out["accuracy"] = acc
+    return out
 
 
 # k_direct: thread instructions per computed (atom, point) pair, from the ncu

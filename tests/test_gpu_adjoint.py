@@ -138,6 +138,28 @@ def test_autograd_wrapper_device_tensors(ctx, engine):
         np.testing.assert_allclose(occ.grad.cpu().numpy(), go, rtol=1e-6, atol=1e-9 * np.abs(go).max())
 
 
+@pytest.mark.parametrize("engine", [_abi.ENGINE_DIRECT, _abi.ENGINE_TC])
+def test_gradient_vs_fp64_closed_form_rocksalt(ctx, engine):
+    """A 10 x 10 x 8-cell rock salt (6400 atoms) on a 33^3 grid: the gradient
+    of 300 seeded atoms against the FP64 closed-form reference of a perfect
+    lattice (bench.fp64_gradient_perfect_lattice, itself pinned to the
+    oracle), within 2e-4 of the largest component.  chi2 within 1e-6 on the
+    CUDA-core engine and 1e-4 on the tensor cores: on a perfect lattice the
+    Bragg peaks dominate chi2, where the tensor-core sums are coherent and
+    carry a relative error of ~1e-6, and chi2 amplifies it by I / (I - I_t)."""
+    import bench
+    from diffusecode_gb300.autograd import chi2_grad
+    cr, g = S.rocksalt_volume(cells=(10, 10, 8), inc=33, step=0.2)
+    it, wt = _target(cr, g, ctx, a_lat=5.64)
+    op = K.opts(phase=_abi.PHASE_EXACT64, engine=engine)
+    c2, gp, go, _ = chi2_grad(cr, g, op, it, wt, ctx=ctx)
+    atoms = np.sort(np.random.Generator(np.random.PCG64(6)).choice(cr.natoms, 300, replace=False))
+    c64, gp64, go64 = bench.fp64_gradient_perfect_lattice(cr, g, it, wt, atoms)
+    assert abs(c2 - c64) <= (1e-6 if engine == _abi.ENGINE_DIRECT else 1e-4) * c64
+    assert np.max(np.abs(gp[atoms] - gp64)) <= 2e-4 * np.abs(gp64).max()
+    assert np.max(np.abs(go[atoms] - go64)) <= 2e-4 * np.abs(go64).max()
+
+
 def test_gradient_rejects_average(ctx):
     from diffusecode_gb300.autograd import chi2_grad
     cr, g = S.small_random(seed=4, natoms=30, inc=(5, 5, 3))

@@ -91,3 +91,23 @@ def test_fill_bragg_neighbour_mean():
     np.testing.assert_allclose(out, ref, rtol=1e-14)
     np.testing.assert_allclose(zout, zref, rtol=1e-14)
     assert not np.array_equal(out, d)
+
+
+def test_closed_form_gradient_reference_matches_oracle(oracle):
+    """bench.fp64_gradient_perfect_lattice (F of a perfect lattice in closed
+    form, the FP64 reference of the adjoint at the 100 000-atom scale) against
+    the oracle's direct FP64 gradient on a 3 x 3 x 3-cell rock salt."""
+    import bench
+    from diffusecode_gb300 import _abi
+    from diffusecode_gb300 import structures as S
+    cr, g = S.rocksalt_volume(cells=(3, 3, 3), inc=9, step=0.3)
+    tgt = S.perturbed_copy(cr, 3, 0.05, 5.64, 0.1)
+    op = _abi.default_opts(ldbw=1, phase=_abi.PHASE_EXACT64)
+    rc, csf, acsf, it, info = oracle.four_run(tgt, g, op)
+    wt = 1.0 / (it + 1.0)
+    oc2, ogp, ogo = oracle.chi2_grad(cr, g, op, it, wt)
+    atoms = np.arange(0, cr.natoms, 7)
+    c2, gp, go = bench.fp64_gradient_perfect_lattice(cr, g, it, wt, atoms)
+    assert abs(c2 - oc2) <= 1e-10 * oc2
+    np.testing.assert_allclose(gp, ogp[atoms], rtol=0, atol=1e-9 * np.abs(ogp).max())
+    np.testing.assert_allclose(go, ogo[atoms], rtol=0, atol=1e-9 * np.abs(ogo).max())
