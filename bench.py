@@ -700,16 +700,26 @@ def batch_measure(ctx, steps=3):
         weights.append(1.0 / (it + 1.0))
     pairs = sum(c.n_scattering() * g.npoints for c, g in pop)
     fwd_ms, full_ms = [], []
+    dsi_f = None
     for s in range(steps + 1):
-        _, _, _, _, ms_f = FR.batch_run(crs, grids, op, ctx=ctx)
+        dsi_f, _, _, _, ms_f = FR.batch_run(crs, grids, op, ctx=ctx)
         _, chi2, gp, go, ms = FR.batch_run(crs, grids, op, targets, weights, ctx=ctx)
         if s:
             fwd_ms.append(ms_f)
             full_ms.append(ms)
     f, t = min(fwd_ms), min(full_ms)
+    # every member's |F|^2 against FP64 at 24 sampled points of its plane
+    errs = []
+    for k, ((cr, g), d) in enumerate(zip(pop, dsi_f)):
+        rng = np.random.Generator(np.random.PCG64(1000 + k))
+        idx = np.stack([rng.integers(0, n, 24) for n in g.inc], 1)
+        i64, fl = fp64_points(cr, g, idx)
+        errs.append(float(np.max(np.abs(d[idx[:, 0], idx[:, 1], idx[:, 2]] - i64) / (i64 + fl))))
     return {"workload": "population-64", "members": len(pop), "atoms": int(sum(c.n_scattering() for c in crs)),
             "pairs": int(pairs), "fwd_graph_ms": f, "fwd_grad_graph_ms": t,
-            "fwd_G_pairs_per_s": pairs / f / 1e6, "note": "one CUDA graph launch per step; device time"}
+            "fwd_G_pairs_per_s": pairs / f / 1e6, "note": "one CUDA graph launch per step; device time",
+            "per_crystal_rel_err_vs_fp64": {"max": max(errs), "median": float(np.median(errs)), "points": 24,
+                                            "norm": "max |I-I64|/(I64 + N<|f|^2>) per member"}}
 
 
 def run_reference(args, world, rank):

@@ -57,3 +57,20 @@ def test_batch_gradients_and_replay(ctx):
             assert abs(chi2[i] - c2) <= 1e-4 * c2
             assert np.max(np.abs(gp[i] - gps)) <= 1e-3 * np.abs(gps).max()
             assert np.max(np.abs(go[i] - gos)) <= 1e-3 * np.abs(gos).max()
+
+
+def test_population_members_vs_fp64_sampled(ctx):
+    """The 64-crystal population of the bench (2 000 - 200 000 atoms, planes of
+    129^2 - 257^2 points, one graph launch): every member's |F|^2 against an
+    FP64 numpy sum at 16 sampled points, within 1e-5 of I + N<|f|^2>."""
+    import bench
+    pop = S.population()
+    op = K.opts(phase=_abi.PHASE_EXACT64, engine=_abi.ENGINE_TC)
+    dsi, chi2, gp, go, ms = FR.batch_run([c for c, g in pop], [g for c, g in pop], op, ctx=ctx)
+    worst = 0.0
+    for k, ((cr, g), d) in enumerate(zip(pop, dsi)):
+        rng = np.random.Generator(np.random.PCG64(2000 + k))
+        idx = np.stack([rng.integers(0, n, 16) for n in g.inc], 1)
+        i64, fl = bench.fp64_points(cr, g, idx)
+        worst = max(worst, float(np.max(np.abs(d[idx[:, 0], idx[:, 1], idx[:, 2]] - i64) / (i64 + fl))))
+    assert worst <= TOL
