@@ -21,12 +21,16 @@ import torch
 
 from . import _abi
 from ._lib import default_context
+from .fourier import attach_selections
 from .structures import CrystalData, GridData
 
 
-def chi2_grad(cr: CrystalData, grid: GridData, opts, i_target, weight=None, ctx=None):
-    """(chi2, grad_pos (N,3), grad_occ (N,), info) through the host C-ABI."""
+def chi2_grad(cr: CrystalData, grid: GridData, opts, i_target, weight=None, ctx=None, aver_cells=None):
+    """(chi2, grad_pos (N,3), grad_occ (N,), info) through the host C-ABI.
+    opts.fave > 0 subtracts <F> (aver_cells: the cells drawn over csize when
+    fave < 1) and differentiates through it."""
     ctx = ctx or default_context()
+    keep = attach_selections(opts, aver_cells)
     it = np.asfortranarray(np.asarray(i_target, dtype=np.float64)).reshape(-1, order="F").copy()
     wt = None if weight is None else np.asfortranarray(np.asarray(weight, np.float64)).reshape(-1, order="F").copy()
     chi2 = np.zeros(1)
@@ -37,6 +41,7 @@ def chi2_grad(cr: CrystalData, grid: GridData, opts, i_target, weight=None, ctx=
     g = grid.to_c()
     ctx.check(ctx.lib.dgpu_chi2_grad(ctx.h, C.byref(c), C.byref(g), C.byref(opts), _abi.dptr(it), _abi.dptr(wt),
                                      _abi.dptr(chi2), _abi.dptr(gp), _abi.dptr(go), C.byref(info)))
+    del keep
     return float(chi2[0]), gp.reshape(-1, 3), go, info
 
 
@@ -49,12 +54,14 @@ def grid_flat(a, device):
 
 
 def chi2_grad_device(cr: CrystalData, grid: GridData, opts, pos, occ, i_target, weight=None, iscat=None,
-                     ctx=None):
+                     ctx=None, aver_cells=None):
     """(chi2, grad_pos (N,3), grad_occ (N,), info) with the per-atom and
     per-point arrays on the GPU: pos (N,3) float64 and occ (N,) CUDA tensors,
     i_target / weight shaped grid.inc (torch or numpy).  iscat: a cached
-    device copy of cr.iscat (made here when None)."""
+    device copy of cr.iscat (made here when None).  aver_cells as for
+    chi2_grad."""
     ctx = ctx or default_context()
+    keep = attach_selections(opts, aver_cells)
     dev = pos.device
     p = pos.detach().to(torch.float64).contiguous()
     o = occ.detach().to(torch.float32).contiguous()
@@ -77,6 +84,7 @@ def chi2_grad_device(cr: CrystalData, grid: GridData, opts, pos, occ, i_target, 
                                             C.c_void_p(wt.data_ptr()) if wt is not None else None,
                                             _abi.dptr(chi2), C.c_void_p(gp.data_ptr()), C.c_void_p(go.data_ptr()),
                                             C.byref(info)))
+    del keep
     return float(chi2[0]), gp, go, info
 
 

@@ -97,6 +97,7 @@ extern "C" int dgpu_ctx_destroy(dgpu_ctx *c)
     c->stage.release();
     for (cudaEvent_t e : c->run_ev) cudaEventDestroy(e);
     delete c->fs_main;
+    delete c->fs_type;
     for (int i = 0; i < DGPU_NEV; i++)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -421,6 +422,7 @@ int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g,
 
     int warn = 0;
     int32_t ncell = 0;
+    ctx->aver.on = 0;
     int64_t pairs_aver = 0, pairs = 0, refined = 0;
     float kernel_ms = 0.f;
     int64_t ts[2 * 64 + 4];
@@ -459,7 +461,7 @@ int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g,
             ncell = (int32_t)ncells;
         }
         rc = dgpu_prepare_atoms(ctx, cr->pos, cr->iscat, cr->atom_occ, cr->natoms, cr->nscat, geo, fold,
-                                ctx->aph0, ctx->adu, ctx->adv, ctx->adw, ctx->aw, ts);
+                                ctx->aph0, ctx->adu, ctx->adv, ctx->adw, ctx->aw, ts, &ctx->aaidx);
         if (rc) return rc;
         PartRef aref;
         DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
@@ -529,6 +531,14 @@ int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g,
             alat_d[k] = lat_d[k];
         }
         anorm = norm;
+        if (aver_closed) {
+            ctx->aver.on = 1;
+            ctx->aver.nscat = cr->nscat;
+            memcpy(ctx->aver.lat_n, lat_n, sizeof(lat_n));
+            memcpy(ctx->aver.lat_d, lat_d, sizeof(lat_d));
+            ctx->aver.norm = norm;
+            memcpy(ctx->aver.ts, ts, sizeof(int64_t) * (2 * cr->nscat + 1));
+        }
         float ms = 0.f;
         DGPU_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]));
         kernel_ms += ms;
@@ -612,6 +622,8 @@ int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g,
     }
     if (!ctx->fs_main) ctx->fs_main = new FormSpec();
     *ctx->fs_main = fsm;
+    if (!ctx->fs_type) ctx->fs_type = new FormSpec();
+    *ctx->fs_type = fs;
     if (cancelled(op)) return dgpu_set_error(ctx, DGPU_ERR_CANCELLED, "cancelled");
     rc = dgpu_friedel_mirror(ctx, box, idim, d_csf, d_acsf, d_dsi);
     if (rc) return rc;

@@ -108,6 +108,7 @@ struct dgpu_ctx {
     DevBuf counts;                      // per-block type counts, their scan, type starts
     DevBuf ph0, du, dv, dw, w;          // main atom set
     DevBuf aph0, adu, adv, adw, aw;     // folded atoms for <F>
+    DevBuf aaidx;                       // original atom index of each folded slot
     DevBuf istl, cfact, part, apart, lat, csf, acsf, dsi, stats, flag;
     DevBuf tc_part, tc_work, aidx;          // aidx: original atom index of each prepared slot
     DevBuf tc_mult;                         // per-atom step factors of the tensor-core engine
@@ -118,6 +119,17 @@ struct dgpu_ctx {
     DevBuf ianis, geff, ghist;              // ADP types, group of every atom, (type, ADP) histogram
     DevBuf lpos, ltype, locc, lplan, lfac;  // lot crystals, lot plan, group factors
     FormSpec *fs_main = nullptr;            // host copy of the last main combine's FormSpec
+    FormSpec *fs_type = nullptr;            // host copy of the last per-type FormSpec (<F> combine)
+    // <F> of the last four_run when it was a box lattice in closed form:
+    // A(h) = norm L(h) sum_t c_t(h) S_t(h) over the folded atoms (aph0.., ts)
+    struct AverKeep {
+        int32_t on = 0;
+        int32_t nscat = 0;
+        int32_t lat_n[3] = {0, 0, 0};
+        double lat_d[3] = {0, 0, 0};
+        double norm = 0.0;
+        int64_t ts[2 * 64 + 4] = {};
+    } aver;
     DevBuf wbuf, acc_csf, acc_dsi;          // four_weight staging; four_accumulate sums
     DevBuf rlist, rsum;                     // refinement of <F>-cancelling points: list, exact sums
     DevBuf slab_ph0;                        // powder: per-slab origin phases of the atoms
@@ -182,7 +194,7 @@ struct FoldSpec {
 int dgpu_prepare_atoms(dgpu_ctx *ctx, const double *d_pos, const int32_t *d_iscat,
                        const float *d_aocc, int64_t natoms, int32_t nscat,
                        const PhaseGeom &g, const FoldSpec &fs, DevBuf &ph0, DevBuf &du,
-                       DevBuf &dv, DevBuf &dw, DevBuf &w, int64_t *h_type_start);
+                       DevBuf &dv, DevBuf &dw, DevBuf &w, int64_t *h_type_start, DevBuf *idx = nullptr);
 // The same in two phases, for callers that learn the type starts of several
 // atom sets with one host wait: the count phase (per-block type counts,
 // their scan and the type starts d_ts, device only) into a region of
@@ -199,7 +211,9 @@ int dgpu_prepare_count(dgpu_ctx *ctx, const int32_t *d_iscat, int64_t natoms, in
                        const PrepRegion &r);
 int dgpu_prepare_scatter(dgpu_ctx *ctx, const double *d_pos, const int32_t *d_iscat, const float *d_aocc,
                          int64_t natoms, int32_t nscat, const PhaseGeom &g, const FoldSpec &fs, const PrepRegion &r,
-                         int64_t total, DevBuf &ph0, DevBuf &du, DevBuf &dv, DevBuf &dw, DevBuf &w);
+                         int64_t total, DevBuf &ph0, DevBuf &du, DevBuf &dv, DevBuf &dw, DevBuf &w,
+                         DevBuf *idx = nullptr);
+// idx: where the original atom index of every slot goes (ctx->aidx when null)
 // Lattice points of all cells (four_getav LOT_OFF) as one atom set.
 int dgpu_prepare_lattice(dgpu_ctx *ctx, const int32_t icc[3], const double dim0[3],
                          const PhaseGeom &g, DevBuf &ph0, DevBuf &du, DevBuf &dv,

@@ -16,6 +16,8 @@
 // mirror's G as well (I(-h) = I(h) without anomalous scattering).  The phase
 // of every (atom, point) pair is the exact 64-bit fixed point of the forward
 // pass; phasors in FP32, sums in FP32 over 256-point tiles and FP64 across.
+// With <F> subtracted (four_aver) the folded atoms form a second atom set
+// with their own Q (k_adj_qa); both sets add into the same gradient.
 #include <math.h>
 
 #include "dgpu_form.cuh"
@@ -53,6 +55,24 @@ __global__ void k_adj_chi(const double *part, int n, double *out)
     }
 }
 
+// Box point pb: its grid coordinates c, grid index and G (with the mirror's
+// G where the mirror lies outside the box)
+__device__ __forceinline__ double adj_point(const BoxSpec &box, int32_t halved, const double *__restrict__ g,
+                                            int64_t pb, int32_t c[3], int64_t &idx)
+{
+    c[0] = (int32_t)(pb % box.f[0]);
+    c[1] = (int32_t)((pb / box.f[0]) % box.f[1]);
+    c[2] = (int32_t)(pb / ((int64_t)box.f[0] * box.f[1]));
+    const int32_t *n = box.num;
+    idx = c[0] + (int64_t)n[0] * (c[1] + (int64_t)n[1] * c[2]);
+    double G = g[idx];
+    if (halved >= 1 && c[halved - 1] < box.f[halved - 1] - 1) {
+        const int64_t m = (n[0] - 1 - c[0]) + (int64_t)n[0] * ((n[1] - 1 - c[1]) + (int64_t)n[1] * (n[2] - 1 - c[2]));
+        G += g[m];
+    }
+    return G;
+}
+
 // Q_t(p) on the box, FP32 complex, layout [t][box point]
 __global__ void k_adj_q(const FormSpec *fs, BoxSpec box, int32_t halved, const double *__restrict__ g,
                         const double2 *__restrict__ csf, const int32_t *__restrict__ istl,
@@ -61,15 +81,9 @@ __global__ void k_adj_q(const FormSpec *fs, BoxSpec box, int32_t halved, const d
     const int64_t pb = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
     if (pb >= nb) return;
-    const int32_t c[3] = {(int32_t)(pb % box.f[0]), (int32_t)((pb / box.f[0]) % box.f[1]),
-                          (int32_t)(pb / ((int64_t)box.f[0] * box.f[1]))};
-    const int32_t *n = box.num;
-    const int64_t idx = c[0] + (int64_t)n[0] * (c[1] + (int64_t)n[1] * c[2]);
-    double G = g[idx];
-    if (halved >= 1 && c[halved - 1] < box.f[halved - 1] - 1) {
-        const int64_t m = (n[0] - 1 - c[0]) + (int64_t)n[0] * ((n[1] - 1 - c[1]) + (int64_t)n[1] * (n[2] - 1 - c[2]));
-        G += g[m];
-    }
+    int32_t c[3];
+    int64_t idx;
+    const double G = adj_point(box, halved, g, pb, c, idx);
     // conj(F) with F = csf / sqrt(ds):  2 ds G conj(F) c_t = 2 sqrt(ds) G conj(csf) c_t
     const double2 f = csf[idx];
     const double sc = 2.0 * sqds * G;
@@ -82,6 +96,37 @@ __global__ void k_adj_q(const FormSpec *fs, BoxSpec box, int32_t halved, const d
         const double qr = sc * (f.x * cr + f.y * ci);
         const double qi = sc * (f.x * ci - f.y * cr);
         Q[(int64_t)(t - 1) * nb + pb] = make_float2((float)qr, (float)qi);
+    }
+}
+
+// Q of the folded atoms.  With <F> subtracted, F = sum_t c_t S_t - A and
+// A(h) = norm L(h) sum_t c_t(h) S^fold_t(h) (four_aver: the atoms of the
+// selected cells moved into one cell, L the closed-form lattice sum of the
+// crystal, norm = 1/ncell), so the folded atoms take
+//   Q^A_t(h) = -norm L(h) 2 ds G(h) conj(F(h)) c_t(h)
+// with the per-type factor c_t of the <F> combine.  Layout [t][box point].
+__global__ void k_adj_qa(const FormSpec *fs, BoxSpec box, int32_t halved, const double *__restrict__ g,
+                         const double2 *__restrict__ csf, const int32_t *__restrict__ istl,
+                         const double2 *__restrict__ cfact, double sqds, int32_t l0, int32_t l1, int32_t l2,
+                         double d0, double d1, double d2, double norm, float2 *__restrict__ Q)
+{
+    const int64_t pb = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    if (pb >= nb) return;
+    int32_t c[3];
+    int64_t idx;
+    const double G = adj_point(box, halved, g, pb, c, idx);
+    double h[3];
+    form_hvec(fs, c[0], c[1], c[2], h);
+    const double2 L = lattice_closed(h, l0, l1, l2, d0, d1, d2);
+    const double2 f = csf[idx];
+    // -norm L 2 sqrt(ds) G conj(csf)
+    const double sc = -2.0 * sqds * G * norm;
+    const double2 b = make_double2(sc * (L.x * f.x + L.y * f.y), sc * (L.y * f.x - L.x * f.y));
+    const int32_t q = istl ? istl[idx] : 0;
+    for (int t = 1; t <= fs->nscat; t++) {
+        const double2 m = cmul(b, form_cfact(fs, cfact, q, t, h));
+        Q[(int64_t)(t - 1) * nb + pb] = make_float2((float)m.x, (float)m.y);
     }
 }
 
@@ -148,12 +193,14 @@ __global__ void __launch_bounds__(ADJ_NT) k_adj_atoms(const uint64_t *__restrict
     if (!valid) return;
     const int32_t o = aidx[a];
     if (o < 0) return;
+    // added to: an atom also appears once among the folded atoms of <F>
+    // (launched after its main sums, on the same stream)
     const double wj = (double)w[a];
-    if (grad_occ) grad_occ[o] = T0r;
+    if (grad_occ) grad_occ[o] += T0r;
     if (grad_pos) {
         const double zpi = 6.283185307179586476925286766559;
         for (int k = 0; k < 3; k++)
-            grad_pos[3 * (int64_t)o + k] =
+            grad_pos[3 * (int64_t)o + k] +=
                 -zpi * wj * (g.eck[k] * T0i + g.vi[k] * T1 + g.vi[3 + k] * T2 + g.vi[6 + k] * T3);
     }
 }
@@ -164,8 +211,6 @@ int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
                         const double *i_target, const double *weight, double *chi2, double *grad_pos,
                         double *grad_occ, dgpu_info *info, bool device)
 {
-    if (op->fave != 0.0)
-        return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "gradient with <F> subtraction (set aver) is not available");
     if (op->ano) return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "gradient with anomalous scattering");
     if (op->phase != DGPU_PHASE_EXACT64)
         return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "gradient needs EXACT64 phases");
@@ -184,6 +229,11 @@ int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
     rc = dgpu_four_run_dev(ctx, &dc, grid, op, ctx->csf.as<double2>(), ctx->acsf.as<double2>(),
                            ctx->dsi.as<double>(), &fwd);
     if (rc < 0) return rc;
+    // <F> subtracted: its folded atoms carry gradient too (closed-form lattice
+    // sum: EXACT64 without lots; no selected cell leaves <F> = 0)
+    const bool fold = op->fave > 0.0 && fwd.ncell > 0;
+    if (fold && !ctx->aver.on)
+        return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "gradient with <F> of a non-box lattice");
     DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
 
     // adjoint weights g(h) and chi^2
@@ -211,14 +261,28 @@ int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
     // the forward pass's groups: types, or (type, ADP type) pairs
     const FormSpec fs = *ctx->fs_main;
     const int32_t ngroup = fs.ngroup;
-    DGPU_CUDA(ctx, ctx->stats.ensure(sizeof(FormSpec)));
+    // device copies: the main FormSpec, then the per-type one of <F>
+    const size_t fso = (sizeof(FormSpec) + 63) & ~(size_t)63;
+    DGPU_CUDA(ctx, ctx->stats.ensure(fso + sizeof(FormSpec)));
     FormSpec *d_fs = ctx->stats.as<FormSpec>();
+    FormSpec *d_fst = (FormSpec *)((char *)ctx->stats.p + fso);
     DGPU_CUDA(ctx, cudaMemcpyAsync(d_fs, &fs, sizeof(FormSpec), cudaMemcpyHostToDevice, ctx->stream));
-    DGPU_CUDA(ctx, ctx->gpart.ensure((size_t)ngroup * nb * sizeof(float2)));
+    const int32_t nfold = fold ? ctx->aver.nscat : 0;
+    DGPU_CUDA(ctx, ctx->gpart.ensure((size_t)(ngroup + nfold) * nb * sizeof(float2)));
     k_adj_q<<<(unsigned)dgpu_cdiv(nb, 256), 256, 0, ctx->stream>>>(
         d_fs, box, fwd.friedel_dim, d_g, ctx->csf.as<double2>(), ctx->istl.as<int32_t>(), ctx->cfact.as<double2>(),
         sqrt(op->diff_scale), ctx->gpart.as<float2>());
     DGPU_CUDA(ctx, cudaGetLastError());
+    float2 *d_qa = ctx->gpart.as<float2>() + (int64_t)ngroup * nb;
+    if (fold) {
+        DGPU_CUDA(ctx, cudaMemcpyAsync(d_fst, ctx->fs_type, sizeof(FormSpec), cudaMemcpyHostToDevice, ctx->stream));
+        const auto &av = ctx->aver;
+        k_adj_qa<<<(unsigned)dgpu_cdiv(nb, 256), 256, 0, ctx->stream>>>(
+            d_fst, box, fwd.friedel_dim, d_g, ctx->csf.as<double2>(), ctx->istl.as<int32_t>(),
+            ctx->cfact.as<double2>(), sqrt(op->diff_scale), av.lat_n[0], av.lat_n[1], av.lat_n[2], av.lat_d[0],
+            av.lat_d[1], av.lat_d[2], av.norm, d_qa);
+        DGPU_CUDA(ctx, cudaGetLastError());
+    }
 
     // per-atom sums (atoms prepared by the forward pass, grouped by type)
     DGPU_CUDA(ctx, ctx->grad.ensure(n * 4 * sizeof(double)));
@@ -232,22 +296,33 @@ int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
     }
     ag.pbox = nb;
     memcpy(ag.vi, grid->vi, sizeof(ag.vi));
-    const int64_t *ts = ctx->ts_main;
-    if (fwd.engine_used == DGPU_ENGINE_TC) {
-        // same sums on the tensor cores, with the forward pass's engine
-        rc = dgpu_adjtc_sums(ctx, box, grid, ngroup, ts, ctx->ph0.as<uint64_t>(), ctx->du.as<uint64_t>(),
-                             ctx->dv.as<uint64_t>(), ctx->dw.as<uint64_t>(), ctx->w.as<float>(),
-                             ctx->aidx.as<int32_t>(), ctx->gpart.as<float2>(), d_gpos, d_gocc);
-        if (rc) return rc;
-    } else {
-        for (int t = 0; t < ngroup; t++) {
-            const int64_t lo = ts[t], hi = ts[t + 1];
-            if (hi <= lo) continue;
-            k_adj_atoms<<<(unsigned)dgpu_cdiv(hi - lo, ADJ_NT), ADJ_NT, 0, ctx->stream>>>(
-                ctx->ph0.as<uint64_t>(), ctx->du.as<uint64_t>(), ctx->dv.as<uint64_t>(), ctx->dw.as<uint64_t>(),
-                ctx->w.as<float>(), ctx->aidx.as<int32_t>(), lo, hi, ctx->gpart.as<float2>() + (int64_t)t * nb, ag,
-                d_gpos, d_gocc);
-            DGPU_CUDA(ctx, cudaGetLastError());
+    // the main atoms (by group), then the folded atoms of <F> (by type)
+    struct AtomSet {
+        DevBuf *ph0, *du, *dv, *dw, *w, *idx;
+        const int64_t *ts;
+        int32_t n;
+        const float2 *Q;
+    };
+    const AtomSet sets[2] = {
+        {&ctx->ph0, &ctx->du, &ctx->dv, &ctx->dw, &ctx->w, &ctx->aidx, ctx->ts_main, ngroup, ctx->gpart.as<float2>()},
+        {&ctx->aph0, &ctx->adu, &ctx->adv, &ctx->adw, &ctx->aw, &ctx->aaidx, ctx->aver.ts, nfold, d_qa}};
+    for (const AtomSet &A : sets) {
+        if (A.n == 0) continue;
+        if (fwd.engine_used == DGPU_ENGINE_TC) {
+            // same sums on the tensor cores, with the forward pass's engine
+            rc = dgpu_adjtc_sums(ctx, box, grid, A.n, A.ts, A.ph0->as<uint64_t>(), A.du->as<uint64_t>(),
+                                 A.dv->as<uint64_t>(), A.dw->as<uint64_t>(), A.w->as<float>(), A.idx->as<int32_t>(),
+                                 A.Q, d_gpos, d_gocc);
+            if (rc) return rc;
+        } else {
+            for (int t = 0; t < A.n; t++) {
+                const int64_t lo = A.ts[t], hi = A.ts[t + 1];
+                if (hi <= lo) continue;
+                k_adj_atoms<<<(unsigned)dgpu_cdiv(hi - lo, ADJ_NT), ADJ_NT, 0, ctx->stream>>>(
+                    A.ph0->as<uint64_t>(), A.du->as<uint64_t>(), A.dv->as<uint64_t>(), A.dw->as<uint64_t>(),
+                    A.w->as<float>(), A.idx->as<int32_t>(), lo, hi, A.Q + (int64_t)t * nb, ag, d_gpos, d_gocc);
+                DGPU_CUDA(ctx, cudaGetLastError());
+            }
         }
     }
     DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));

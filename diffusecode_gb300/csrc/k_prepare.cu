@@ -283,8 +283,10 @@ int dgpu_prepare_count(dgpu_ctx *ctx, const int32_t *d_iscat, int64_t natoms, in
 
 int dgpu_prepare_scatter(dgpu_ctx *ctx, const double *d_pos, const int32_t *d_iscat, const float *d_aocc,
                          int64_t natoms, int32_t nscat, const PhaseGeom &g, const FoldSpec &fs, const PrepRegion &r,
-                         int64_t total, DevBuf &ph0, DevBuf &du, DevBuf &dv, DevBuf &dw, DevBuf &w)
+                         int64_t total, DevBuf &ph0, DevBuf &du, DevBuf &dv, DevBuf &dw, DevBuf &w,
+                         DevBuf *idx)
 {
+    DevBuf &ib = idx ? *idx : ctx->aidx;
     size_t cap = (size_t)(total > 0 ? total : 1);
     DGPU_CUDA(ctx, ph0.ensure(cap * 8));
     DGPU_CUDA(ctx, du.ensure(cap * 8));
@@ -297,11 +299,11 @@ int dgpu_prepare_scatter(dgpu_ctx *ctx, const double *d_pos, const int32_t *d_is
     DGPU_CUDA(ctx, cudaMemsetAsync(dv.p, 0, cap * 8, ctx->stream));
     DGPU_CUDA(ctx, cudaMemsetAsync(dw.p, 0, cap * 8, ctx->stream));
     DGPU_CUDA(ctx, cudaMemsetAsync(w.p, 0, cap * 4, ctx->stream));
-    DGPU_CUDA(ctx, ctx->aidx.ensure(cap * 4));
-    DGPU_CUDA(ctx, cudaMemsetAsync(ctx->aidx.p, 0xFF, cap * 4, ctx->stream));   // padding: -1
+    DGPU_CUDA(ctx, ib.ensure(cap * 4));
+    DGPU_CUDA(ctx, cudaMemsetAsync(ib.p, 0xFF, cap * 4, ctx->stream));   // padding: -1
     k_scatter_atoms<<<(unsigned)r.nblk, PREP_BLK, 0, ctx->stream>>>(
         d_pos, d_iscat, d_aocc, natoms, nscat, fs, g, r.offs, r.nblk, r.d_ts, ph0.as<uint64_t>(),
-        du.as<uint64_t>(), dv.as<uint64_t>(), dw.as<uint64_t>(), w.as<float>(), ctx->aidx.as<int32_t>());
+        du.as<uint64_t>(), dv.as<uint64_t>(), dw.as<uint64_t>(), w.as<float>(), ib.as<int32_t>());
     DGPU_CUDA(ctx, cudaGetLastError());
     return DGPU_OK;
 }
@@ -309,7 +311,7 @@ int dgpu_prepare_scatter(dgpu_ctx *ctx, const double *d_pos, const int32_t *d_is
 int dgpu_prepare_atoms(dgpu_ctx *ctx, const double *d_pos, const int32_t *d_iscat,
                        const float *d_aocc, int64_t natoms, int32_t nscat, const PhaseGeom &g,
                        const FoldSpec &fs, DevBuf &ph0, DevBuf &du, DevBuf &dv, DevBuf &dw,
-                       DevBuf &w, int64_t *h_type_start)
+                       DevBuf &w, int64_t *h_type_start, DevBuf *idx)
 {
     if (nscat < 1 || nscat >= MAXT)
         return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "nscat=%d outside 1..%d", nscat, MAXT - 1);
@@ -321,7 +323,7 @@ int dgpu_prepare_atoms(dgpu_ctx *ctx, const double *d_pos, const int32_t *d_isca
                                    cudaMemcpyDeviceToHost, ctx->stream));
     DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return dgpu_prepare_scatter(ctx, d_pos, d_iscat, d_aocc, natoms, nscat, g, fs, r, h_type_start[nscat], ph0, du,
-                                dv, dw, w);
+                                dv, dw, w, idx);
 }
 
 __global__ void k_lattice(int64_t ncell, int32_t i0, int32_t i1, double d0, double d1, double d2,

@@ -887,9 +887,15 @@ done:
 }
 /* ---------------------------------------------------------------------- */
 /* chi^2 = sum_h wt(h) (I(h) - It(h))^2 and its gradient, exact FP64, full
- * grid, fave = 0, no Friedel reduction.  I = diff_scale |F|^2 with
- * F = sum_j cf_t(j)(h) D_a(j)(h) w_j exp(2 pi i h.r_j), D the anisotropic
- * Debye-Waller term of atom j's ADP type (1 for an isotropic crystal).      */
+ * grid, no Friedel reduction.  I = diff_scale |F|^2 with
+ * F = sum_j cf_t(j)(h) D_a(j)(h) w_j exp(2 pi i h.r_j) - A(h), D the
+ * anisotropic Debye-Waller term of atom j's ADP type (1 for an isotropic
+ * crystal).  A = 0 unless fave > 0; then (four_aver, fourier_sup.f90:
+ * 1194-1357, with the lattice of four_getav :2440-2510) the atoms of the
+ * cells selected over csize are moved into one cell,
+ *   A(h) = L(h)/ncell sum_{j selected} cf_t(j)(h) w_j exp(2 pi i h.(r_j - cell_j - dim0)),
+ *   L(h) = sum over all icc cells of exp(2 pi i h.(cell + dim0)),
+ * and every selected atom gets a second term with Q^A = -L/ncell Q.        */
 int oc_chi2_grad(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,
                  const double *it, const double *wt, double *chi2, double *grad_pos,
                  double *grad_occ, int nthreads)
@@ -907,6 +913,33 @@ int oc_chi2_grad(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op
     const int anis = cr->is_anis && op->ldbw;
     double *D = (double *)malloc(sizeof(double) * np * (anis ? cr->nanis : 1));
     (void)nthreads;
+    /* <F>: selected atoms, their folded positions, the lattice sum */
+    const int64_t na = cr->natoms;
+    unsigned char *insel = (unsigned char *)calloc(na > 0 ? na : 1, 1);
+    double *xf = (double *)malloc(sizeof(double) * 3 * (na > 0 ? na : 1));
+    double *Lh = (double *)calloc(2 * np, sizeof(double));
+    int32_t ncell = 0;
+    if (op->fave > 0.0) {
+        int32_t cs[3];
+        oc_csize(cr, op, cs);
+        for (int32_t kk = 0; kk < cs[2]; kk++)
+            for (int32_t jj = 0; jj < cs[1]; jj++)
+                for (int32_t ii = 0; ii < cs[0]; ii++) {
+                    int64_t s = ii + (int64_t)cs[0] * (jj + (int64_t)cs[1] * kk);
+                    if (!(op->fave >= 1.0 || (op->aver_cells && op->aver_cells[s] != 0))) continue;
+                    ncell++;
+                    int32_t icell[3] = {ii, jj, kk};
+                    int64_t c = ii + (int64_t)cr->icc[0] * (jj + (int64_t)cr->icc[1] * kk);
+                    for (int32_t is = 0; is < cr->ncatoms; is++) {
+                        int64_t ia = c * cr->ncatoms + is;
+                        if (ia >= na) continue;
+                        insel[ia] = 1;
+                        for (int k = 0; k < 3; k++)
+                            xf[3 * ia + k] = cr->pos[3 * ia + k] - (double)icell[k] - cr->dim0[k];
+                    }
+                }
+    }
+    const double anorm = ncell > 0 ? 1.0 / ncell : 0.0;
     oc_stltab(g->eck, g->vi, num, cr->rten, istl);
     oc_formtab(cr, op, cfact);
     for (int32_t l = 0; l < num[2]; l++)
@@ -947,6 +980,30 @@ int oc_chi2_grad(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op
             fr += br * c - bi * s;
             fi += br * s + bi * c;
         }
+        if (ncell > 0) {
+            double lr = 0, li = 0, ar = 0, ai = 0;
+            for (int32_t kk = 0; kk < cr->icc[2]; kk++)
+                for (int32_t jj = 0; jj < cr->icc[1]; jj++)
+                    for (int32_t ii = 0; ii < cr->icc[0]; ii++) {
+                        double ph = oc_frac_dot(H + 3 * p, ii + cr->dim0[0], jj + cr->dim0[1], kk + cr->dim0[2]);
+                        lr += cos(zpi * ph);
+                        li += sin(zpi * ph);
+                    }
+            for (int64_t a = 0; a < na; a++) {
+                int t = cr->iscat[a];
+                if (!insel[a] || t < 1 || t > ns) continue;
+                double ph = oc_frac_dot(H + 3 * p, xf[3 * a], xf[3 * a + 1], xf[3 * a + 2]);
+                double wa = cr->atom_occ ? (double)cr->atom_occ[a] : 1.0;
+                double c = cos(zpi * ph) * wa, s = sin(zpi * ph) * wa;
+                double br = cf[2 * ((int64_t)(t - 1) * np + p)], bi = cf[2 * ((int64_t)(t - 1) * np + p) + 1];
+                ar += br * c - bi * s;
+                ai += br * s + bi * c;
+            }
+            Lh[2 * p] = lr;
+            Lh[2 * p + 1] = li;
+            fr -= anorm * (lr * ar - li * ai);
+            fi -= anorm * (lr * ai + li * ar);
+        }
         F[2 * p] = fr; F[2 * p + 1] = fi;
     }
     double x2 = 0;
@@ -984,11 +1041,25 @@ int oc_chi2_grad(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op
                 for (int k = 0; k < 3; k++) gx[k] += H[3 * p + k] * zi;
             }
         }
+        if (t >= 1 && t <= ns && insel[a]) {
+            /* the atom's folded copy in <F>: Q^A = -L/ncell Q, no ADP term */
+            for (int64_t p = 0; p < np; p++) {
+                double ph = oc_frac_dot(H + 3 * p, xf[3 * a], xf[3 * a + 1], xf[3 * a + 2]);
+                double c = cos(zpi * ph), s = sin(zpi * ph);
+                double qr = Q[2 * ((int64_t)(t - 1) * np + p)], qi = Q[2 * ((int64_t)(t - 1) * np + p) + 1];
+                double lr = -anorm * Lh[2 * p], li = -anorm * Lh[2 * p + 1];
+                double ur = lr * qr - li * qi, ui = lr * qi + li * qr;
+                double zr = ur * c - ui * s, zi = ur * s + ui * c;
+                go += zr;
+                for (int k = 0; k < 3; k++) gx[k] += H[3 * p + k] * zi;
+            }
+        }
         double wa = cr->atom_occ ? (double)cr->atom_occ[a] : 1.0;
         if (grad_occ) grad_occ[a] = go;
         if (grad_pos) for (int k = 0; k < 3; k++) grad_pos[3 * a + k] = -zpi * wa * gx[k];
     }
     free(cf); free(F); free(Q); free(H); free(istl); free(cfact); free(D);
+    free(insel); free(xf); free(Lh);
     return DGPU_OK;
 }
 

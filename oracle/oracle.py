@@ -158,9 +158,16 @@ def four_run(cr, grid, opts, nthreads=0, aver_cells=None, lot_origins=None):
             dsi.reshape(shp, order="F"), info)
 
 
-def chi2_grad(cr, grid, opts, i_target, weight=None, nthreads=0):
+def chi2_grad(cr, grid, opts, i_target, weight=None, nthreads=0, aver_cells=None):
+    """(chi2, grad_pos (N,3), grad_occ (N,)) in FP64; with opts.fave > 0 the
+    <F> of the selected cells (aver_cells over csize when fave < 1) is
+    subtracted from F as four_run does."""
     if nthreads <= 0:
         nthreads = os.cpu_count() or 1
+    keep = None
+    if aver_cells is not None:
+        keep = np.ascontiguousarray(np.asarray(aver_cells, dtype=np.uint8).reshape(-1, order="F"))
+        opts.aver_cells = keep.ctypes.data_as(C.POINTER(C.c_uint8))
     c = cr.to_c()
     g = grid.to_c()
     it = np.asfortranarray(i_target, dtype=np.float64).reshape(-1, order="F").copy()
@@ -170,6 +177,7 @@ def chi2_grad(cr, grid, opts, i_target, weight=None, nthreads=0):
     go = np.zeros(cr.natoms)
     rc = lib().oc_chi2_grad(C.byref(c), C.byref(g), C.byref(opts), _d(it),
                             _d(wt) if wt is not None else None, _d(chi2), _d(gp), _d(go), nthreads)
+    del keep
     assert rc == 0
     return float(chi2[0]), gp.reshape(-1, 3), go
 

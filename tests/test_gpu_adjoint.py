@@ -160,9 +160,53 @@ def test_gradient_vs_fp64_closed_form_rocksalt(ctx, engine):
     assert np.max(np.abs(go[atoms] - go64)) <= 2e-4 * np.abs(go64).max()
 
 
-def test_gradient_rejects_average(ctx):
+@pytest.mark.parametrize("engine", [_abi.ENGINE_DIRECT, _abi.ENGINE_TC])
+@pytest.mark.parametrize("fave", [1.0, 0.5])
+def test_gradient_with_average_vs_oracle(oracle, ctx, engine, fave):
+    """<F> subtracted (four_aver): every atom of a selected cell enters A(h)
+    a second time, moved into one cell, and the gradient adds that term.
+    A perturbed 3 x 3 x 3-cell rock salt on a centred 9^3 grid (Friedel-
+    reduced), all cells (fave = 1) or a seeded half (fave = 0.5), against
+    the oracle's FP64 gradient with the same subtraction; an occupancy-weight
+    target makes the chi^2 diffuse, so the main and the folded sums cancel
+    at the Bragg points as in an RMC fit."""
+    from diffusecode_gb300.autograd import chi2_grad
+    cr0, g = S.rocksalt_volume(cells=(3, 3, 3), inc=9, step=0.37)
+    cr = S.perturbed_copy(cr0, 5, 0.04, 5.64, 0.1)
+    tgt = S.perturbed_copy(cr0, 3, 0.05, 5.64, 0.1)
+    cells = None
+    if fave < 1.0:
+        cells = (np.random.default_rng(1).random(27) < 0.5).astype(np.uint8).reshape((3, 3, 3), order="F")
+    rc, _, _, it, _ = oracle.four_run(tgt, g, K.opts(phase=_abi.PHASE_EXACT64, fave=fave), aver_cells=cells)
+    wt = 1.0 / (it + 1.0)
+    op = K.opts(phase=_abi.PHASE_EXACT64, engine=engine, fave=fave)
+    c2, gp, go, info = chi2_grad(cr, g, op, it, wt, ctx=ctx, aver_cells=cells)
+    assert info.friedel_dim >= 1 and info.ncell == (27 if cells is None else int(cells.sum()))
+    oc2, ogp, ogo = oracle.chi2_grad(cr, g, K.opts(phase=_abi.PHASE_EXACT64, fave=fave), it, wt, aver_cells=cells)
+    _, gp0, _ = oracle.chi2_grad(cr, g, K.opts(phase=_abi.PHASE_EXACT64), it, wt)
+    assert np.abs(ogp - gp0).max() > 0.1 * np.abs(ogp).max()       # the <F> term matters here
+    assert abs(c2 - oc2) <= 1e-4 * oc2
+    assert np.max(np.abs(gp - ogp)) <= 2e-4 * np.abs(ogp).max()
+    assert np.max(np.abs(go - ogo)) <= 2e-4 * np.abs(ogo).max()
+
+
+def test_gradient_with_average_no_cell(oracle, ctx):
+    """fave < 0 selects no cell: <F> = 0, the plain gradient."""
+    from diffusecode_gb300.autograd import chi2_grad
+    cr, g = S.small_random(seed=4, natoms=30, inc=(5, 5, 3))
+    it, wt = _target(cr, g, ctx)
+    c2, gp, go, info = chi2_grad(cr, g, K.opts(phase=_abi.PHASE_EXACT64, fave=-1.0), it, wt, ctx=ctx)
+    oc2, ogp, ogo = oracle.chi2_grad(cr, g, K.opts(phase=_abi.PHASE_EXACT64), it, wt)
+    assert info.ncell == 0
+    assert abs(c2 - oc2) <= 1e-4 * oc2
+    assert np.max(np.abs(gp - ogp)) <= 2e-4 * np.abs(ogp).max()
+
+
+def test_gradient_rejects_average_of_ref22(ctx):
+    """<F> of the REF22 phases is a table sum, not a closed-form lattice: the
+    gradient needs EXACT64 phases and says so."""
     from diffusecode_gb300.autograd import chi2_grad
     cr, g = S.small_random(seed=4, natoms=30, inc=(5, 5, 3))
     with pytest.raises(Exception) as e:
-        chi2_grad(cr, g, K.opts(fave=1.0), np.zeros(g.inc), ctx=ctx)
+        chi2_grad(cr, g, K.opts(fave=1.0, phase=_abi.PHASE_REF22), np.zeros(g.inc), ctx=ctx)
     assert getattr(e.value, "code", None) == _abi.DGPU_ERR_UNSUPPORTED
