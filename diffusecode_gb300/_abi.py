@@ -87,6 +87,16 @@ class Crystal(C.Structure):
         ("anis_full", _dp),
         ("ar", C.c_double * 3),
         ("dim_lo", C.c_double * 3),
+        ("isym", _ip),
+    ]
+
+
+class Discamb(C.Structure):
+    _fields_ = [
+        ("maxhkl", C.c_int32 * 3),
+        ("nsymm", _ip),
+        ("isymm", _ip),
+        ("form_tsc", _dp),
     ]
 
 
@@ -124,6 +134,7 @@ class Opts(C.Structure):
         ("lot_origins", _ip),
         ("tc_vimg", C.c_int32),
         ("tc_wait_us", C.c_int32),
+        ("discamb", C.POINTER(Discamb)),
     ]
 
 
@@ -229,6 +240,7 @@ def default_opts(**kw):
     o.lot_origins = C.cast(None, _ip)
     o.tc_vimg = 0
     o.tc_wait_us = 0
+    o.discamb = C.cast(None, C.POINTER(Discamb))
     for k, v in kw.items():
         if k in ("aver_cells", "lot_origins"):
             continue

@@ -92,7 +92,8 @@ extern "C" int dgpu_ctx_destroy(dgpu_ctx *c)
                       &c->flag, &c->tc_part, &c->tc_work, &c->tc_mult, &c->tc_vimg, &c->adj_qimg,
                       &c->adj_items, &c->gq, &c->gpart, &c->grad, &c->batch_desc, &c->batch_aux,
                       &c->ianis, &c->geff, &c->ghist, &c->lpos, &c->ltype, &c->locc, &c->lplan, &c->lfac,
-                      &c->wbuf, &c->acc_csf, &c->acc_dsi, &c->slab_ph0, &c->rlist, &c->rsum, &c->tc_tab};
+                      &c->wbuf, &c->acc_csf, &c->acc_dsi, &c->slab_ph0, &c->rlist, &c->rsum, &c->tc_tab,
+                      &c->aidx, &c->aaidx, &c->isymb, &c->dtab};
     for (DevBuf *b : bufs) b->release();
     c->stage.release();
     for (cudaEvent_t e : c->run_ev) cudaEventDestroy(e);
@@ -133,6 +134,19 @@ static int check_inputs(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
     if (op->diff_scale < 0.0) return dgpu_set_error(ctx, DGPU_ERR_ARG, "diff_scale<0");
     if (cr->is_anis && (cr->nanis < 1 || !cr->ianis || !cr->anis_full))
         return dgpu_set_error(ctx, DGPU_ERR_ARG, "anisotropic crystal without nanis/ianis/anis_full");
+    if (const dgpu_discamb *dc = op->discamb) {
+        if (!dc->nsymm || !dc->isymm || !dc->form_tsc || !cr->isym)
+            return dgpu_set_error(ctx, DGPU_ERR_ARG, "DISCAMB needs nsymm, isymm, form_tsc and the atoms' isym");
+        for (int k = 0; k < 3; k++)
+            if (dc->maxhkl[k] < 0 || dc->maxhkl[k] > 4096)
+                return dgpu_set_error(ctx, DGPU_ERR_ARG, "DISCAMB maxhkl(%d)=%d", k + 1, dc->maxhkl[k]);
+        for (int t = 0; t < cr->nscat; t++)
+            if (dc->nsymm[t] < 0) return dgpu_set_error(ctx, DGPU_ERR_ARG, "DISCAMB nsymm(%d)<0", t + 1);
+        if (op->fave != 0.0)
+            return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "DISCAMB form factors with <F> subtraction");
+        if (op->ldbw && (cr->nanis < 1 || !cr->ianis || !cr->anis_full))
+            return dgpu_set_error(ctx, DGPU_ERR_ARG, "DISCAMB with temp use needs nanis/ianis/anis_full");
+    }
     // lots: the checks of the lots command (fourier.f90:490-497) and the origins' range
     const bool lots = dgpu_lots_on(op);
     if (op->ilots != 0 && op->ilots != DGPU_LOT_OFF && !lots)
@@ -359,6 +373,37 @@ static int lots_sums(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *op,
     return DGPU_OK;
 }
 
+// DISCAMB: the caller's tables into device memory, and a check that every
+// point of the box maps into them (nint is monotonic and h linear over the
+// box, so its corners bound the indices)
+static int discamb_tables(dgpu_ctx *ctx, const dgpu_discamb *dc, int32_t nscat, const FormSpec &fs,
+                          const BoxSpec &box, FormSpec &fsm)
+{
+    int64_t ntab = 0, tsize = 1;
+    for (int t = 0; t < nscat; t++) ntab += dc->nsymm[t];
+    for (int k = 0; k < 3; k++) tsize *= 2 * (int64_t)dc->maxhkl[k] + 1;
+    if (ntab < 1 || ntab > 63 * (DGPU_DISC_MAXSYM + 1))
+        return dgpu_set_error(ctx, DGPU_ERR_ARG, "DISCAMB: %lld tables", (long long)ntab);
+    for (int c = 0; c < 8; c++) {
+        const int64_t ijl[3] = {(c & 1) ? box.f[0] - 1 : 0, (c & 2) ? box.f[1] - 1 : 0, (c & 4) ? box.f[2] - 1 : 0};
+        for (int k = 0; k < 3; k++) {
+            const double h = fs.eck[k] + fs.vi[k] * (double)ijl[0] + fs.vi[3 + k] * (double)ijl[1] +
+                             fs.vi[6 + k] * (double)ijl[2];
+            if (fabs(round(h)) > dc->maxhkl[k])
+                return dgpu_set_error(ctx, DGPU_ERR_ARG, "DISCAMB: h(%d)=%g outside the table's +-%d", k + 1, h,
+                                      dc->maxhkl[k]);
+        }
+    }
+    const size_t bytes = (size_t)(ntab * tsize) * sizeof(double2);
+    DGPU_CUDA(ctx, ctx->dtab.ensure(bytes));
+    DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->dtab.p, dc->form_tsc, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    fsm.disc = 1;
+    fsm.dntab = (int32_t)ntab;
+    for (int k = 0; k < 3; k++) fsm.dmax[k] = dc->maxhkl[k];
+    fsm.dtab = ctx->dtab.as<double2>();
+    return DGPU_OK;
+}
+
 // The whole path with device-resident crystal arrays and outputs.
 int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,
                         double2 *d_csf, double2 *d_acsf, double *d_dsi, dgpu_info *info)
@@ -406,7 +451,11 @@ int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g,
     FormSpec fsm = fs;
     const int32_t *eiscat = cr->iscat;
     int32_t ngroup = cr->nscat;
-    if (cr->is_anis) {
+    if (op->discamb) {
+        rc = discamb_tables(ctx, op->discamb, cr->nscat, fs, box, fsm);
+        if (rc) return rc;
+    }
+    if (cr->is_anis || op->discamb) {
         rc = dgpu_anis_groups(ctx, cr, op, fsm, &ngroup);
         if (rc) return rc;
         eiscat = ctx->geff.as<int32_t>();
@@ -686,10 +735,15 @@ int dgpu_stage_crystal(dgpu_ctx *ctx, const dgpu_crystal *cr, dgpu_crystal &dc)
         DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->aocc.p, cr->atom_occ, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
         dc.atom_occ = ctx->aocc.as<float>();
     }
-    if (cr->is_anis && cr->ianis) {
+    if (cr->ianis && cr->nanis >= 1) {
         DGPU_CUDA(ctx, ctx->ianis.ensure(n * sizeof(int32_t)));
         DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->ianis.p, cr->ianis, n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
         dc.ianis = ctx->ianis.as<int32_t>();
+    }
+    if (cr->isym) {
+        DGPU_CUDA(ctx, ctx->isymb.ensure(n * sizeof(int32_t)));
+        DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->isymb.p, cr->isym, n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+        dc.isym = ctx->isymb.as<int32_t>();
     }
     return DGPU_OK;
 }

@@ -52,17 +52,34 @@ __device__ __forceinline__ double form_anis_dbw(const FormSpec *fs, int g, const
     return exp(-arg);
 }
 
-// whether the factors need h (analytic form factor or anisotropic term)
+// whether the factors need h (analytic form factor, anisotropic term, DISCAMB)
 __device__ __forceinline__ bool form_needs_h(const FormSpec *fs)
 {
-    return fs->mode != DGPU_FORM_TABLE || fs->adbw;
+    return fs->mode != DGPU_FORM_TABLE || fs->adbw || fs->disc;
+}
+
+// DISCAMB table of group g at nint(h) (tcsf_form_discamb, fourier_form.f90:
+// 90-97; nint rounds half away from zero); NaN outside the table
+__device__ __forceinline__ double2 form_discamb(const FormSpec *fs, int g, const double h[3])
+{
+    const int32_t m0 = fs->gtab[g];
+    if (m0 < 0 || m0 >= fs->dntab) return make_double2(nan(""), nan(""));
+    int64_t idx = 0, stride = 1;
+    for (int k = 0; k < 3; k++) {
+        const double r = round(h[k]);
+        const int32_t m = fs->dmax[k];
+        if (!(r >= -(double)m && r <= (double)m)) return make_double2(nan(""), nan(""));
+        idx += ((int64_t)r + m) * stride;
+        stride *= 2 * (int64_t)m + 1;
+    }
+    return fs->dtab[(int64_t)m0 * stride + idx];
 }
 
 // factor of partial-sum group g (1-based)
 __device__ __forceinline__ double2 form_group(const FormSpec *fs, const double2 *cfact, int32_t istl, int g,
                                               const double h[3])
 {
-    double2 c = form_cfact(fs, cfact, istl, fs->gtype[g], h);
+    double2 c = fs->disc ? form_discamb(fs, g, h) : form_cfact(fs, cfact, istl, fs->gtype[g], h);
     if (fs->adbw) {
         const double d = form_anis_dbw(fs, g, h);
         c.x = __dmul_rn(c.x, d);

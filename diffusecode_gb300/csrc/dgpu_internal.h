@@ -13,6 +13,7 @@
 #include "../../include/discus_gpu.h"
 
 #define DGPU_NTAB (DGPU_CFPKT + 1)
+#define DGPU_DISC_MAXSYM 192   // DISCAMB symmetry operation numbers 0..192 (discus_discamb.f90:82)
 
 // ---------------------------------------------------------------------------
 // device buffer that only grows
@@ -117,6 +118,7 @@ struct dgpu_ctx {
     DevBuf adj_qimg, adj_items;             // tensor-core adjoint: Q images, work items
     int64_t ts_main[2 * 64 + 4] = {};      // type ranges of the last main atom preparation
     DevBuf ianis, geff, ghist;              // ADP types, group of every atom, (type, ADP) histogram
+    DevBuf isymb, dtab;                     // DISCAMB: symmetry of every atom, the form-factor tables
     DevBuf lpos, ltype, locc, lplan, lfac;  // lot crystals, lot plan, group factors
     FormSpec *fs_main = nullptr;            // host copy of the last main combine's FormSpec
     FormSpec *fs_type = nullptr;            // host copy of the last per-type FormSpec (<F> combine)
@@ -348,6 +350,11 @@ struct FormSpec {
     double eck[3], vi[9];
     double gU[64 * 6];     // U11, U22, U33, U23, U13, U12 of each group (A^2)
     double ar[3];          // reciprocal cell lengths (1/A)
+    // DISCAMB: group g takes table gtab[g] (< dntab) of dtab (device) at nint(h)
+    int32_t disc, dntab;
+    int32_t dmax[3];
+    int32_t gtab[64];
+    const double2 *dtab;
 };
 // Partial sums part[t][s][p] of either engine: double2 (direct) or float2 (TC).
 // Element (point i,j,l of the box, type t, slice k) at

@@ -55,10 +55,19 @@ __global__ void k_adj_chi(const double *part, int n, double *out)
     }
 }
 
-// Box point pb: its grid coordinates c, grid index and G (with the mirror's
-// G where the mirror lies outside the box)
+// Box point pb: its grid coordinates c, grid index and the weight G it
+// carries.  The forward pass computes the box and copies the rest
+// (four_apply_friedel, k_mirror): a point past the halved axis' middle is
+// its mirror's conjugate, and on the middle slab the second half (by the
+// linear index L over the later axes) copies the first, while the centre
+// is conjugated in place.  So a computed point carries its own G plus that
+// of every copy of it; a copied point carries nothing (skip), and at the
+// centre csf holds conj(F) (cj).  Without anomalous scattering and with
+// Friedel-symmetric form factors the copies equal what a direct
+// computation would give, so the rule only matters for complex (DISCAMB)
+// factors, but it is what the forward pass does in every case.
 __device__ __forceinline__ double adj_point(const BoxSpec &box, int32_t halved, const double *__restrict__ g,
-                                            int64_t pb, int32_t c[3], int64_t &idx)
+                                            int64_t pb, int32_t c[3], int64_t &idx, bool &skip, bool &cj)
 {
     c[0] = (int32_t)(pb % box.f[0]);
     c[1] = (int32_t)((pb / box.f[0]) % box.f[1]);
@@ -66,9 +75,23 @@ __device__ __forceinline__ double adj_point(const BoxSpec &box, int32_t halved, 
     const int32_t *n = box.num;
     idx = c[0] + (int64_t)n[0] * (c[1] + (int64_t)n[1] * c[2]);
     double G = g[idx];
-    if (halved >= 1 && c[halved - 1] < box.f[halved - 1] - 1) {
+    skip = false;
+    cj = false;
+    if (halved >= 1) {
+        const int a = halved - 1;
         const int64_t m = (n[0] - 1 - c[0]) + (int64_t)n[0] * ((n[1] - 1 - c[1]) + (int64_t)n[1] * (n[2] - 1 - c[2]));
-        G += g[m];
+        if (c[a] < box.f[a] - 1) {
+            G += g[m];
+        } else {
+            int64_t L = 0, N = 1;
+            for (int k = a + 1; k < 3; k++) {
+                L = L * n[k] + c[k];
+                N *= n[k];
+            }
+            if (2 * L < N - 1) G += g[m];
+            else if (2 * L > N - 1) skip = true;
+            else cj = true;
+        }
     }
     return G;
 }
@@ -83,10 +106,12 @@ __global__ void k_adj_q(const FormSpec *fs, BoxSpec box, int32_t halved, const d
     if (pb >= nb) return;
     int32_t c[3];
     int64_t idx;
-    const double G = adj_point(box, halved, g, pb, c, idx);
+    bool skip, cj;
+    const double G = adj_point(box, halved, g, pb, c, idx, skip, cj);
     // conj(F) with F = csf / sqrt(ds):  2 ds G conj(F) c_t = 2 sqrt(ds) G conj(csf) c_t
-    const double2 f = csf[idx];
-    const double sc = 2.0 * sqds * G;
+    double2 f = csf[idx];
+    if (cj) f.y = -f.y;
+    const double sc = skip ? 0.0 : 2.0 * sqds * G;
     double h[3];
     if (form_needs_h(fs)) form_hvec(fs, c[0], c[1], c[2], h);
     for (int t = 1; t <= fs->ngroup; t++) {
@@ -115,13 +140,15 @@ __global__ void k_adj_qa(const FormSpec *fs, BoxSpec box, int32_t halved, const 
     if (pb >= nb) return;
     int32_t c[3];
     int64_t idx;
-    const double G = adj_point(box, halved, g, pb, c, idx);
+    bool skip, cj;
+    const double G = adj_point(box, halved, g, pb, c, idx, skip, cj);
     double h[3];
     form_hvec(fs, c[0], c[1], c[2], h);
     const double2 L = lattice_closed(h, l0, l1, l2, d0, d1, d2);
-    const double2 f = csf[idx];
-    // -norm L 2 sqrt(ds) G conj(csf)
-    const double sc = -2.0 * sqds * G * norm;
+    double2 f = csf[idx];
+    if (cj) f.y = -f.y;
+    // -norm L 2 sqrt(ds) G conj(F)
+    const double sc = skip ? 0.0 : -2.0 * sqds * G * norm;
     const double2 b = make_double2(sc * (L.x * f.x + L.y * f.y), sc * (L.y * f.x - L.x * f.y));
     const int32_t q = istl ? istl[idx] : 0;
     for (int t = 1; t <= fs->nscat; t++) {

@@ -387,6 +387,8 @@ extern "C" int dgpu_batch_run(dgpu_ctx *ctx, int32_t nc, const dgpu_crystal *crs
         return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "batch: EXACT64 phases, no <F>, no anomalous scattering");
     if (op->ilots == DGPU_LOT_BOX || op->ilots == DGPU_LOT_ELI)
         return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "batch: lots are run by dgpu_four_run");
+    if (op->discamb)
+        return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "batch: DISCAMB form factors are run by dgpu_four_run");
     if (!dgpu_tc_available(ctx)) return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "batch needs the tensor-core engine");
     const bool targets = i_target != nullptr;
     if (targets && !chi2) return dgpu_set_error(ctx, DGPU_ERR_ARG, "chi2 output missing");

@@ -3,7 +3,10 @@
 //  * groups: an anisotropic crystal is summed per (scattering type, ADP type)
 //    pair present (four_nanis, discus/prog/fourier_sup.f90:4294-4326; the
 //    loop over them, :195-219), each group then multiplied by its type's
-//    cfact and its four_dbw (tcsf_form_aniso, fourier_form.f90:106-143).
+//    cfact and its four_dbw (tcsf_form_aniso, fourier_form.f90:106-143);
+//    with DISCAMB form factors per (type, symmetry operation, ADP type)
+//    (:166-193), multiplied by its table and four_dbw (tcsf_form_discamb,
+//    fourier_form.f90:63-102).
 //    The pairs are counted on the device, numbered on the host (by type, then
 //    ADP type) and every atom gets its group number, which the rest of the
 //    pipeline treats as its type.
@@ -19,14 +22,26 @@
 #include "dgpu_lots.h"
 
 #define GH_SHARED 4096
+#define DISC_MAXSYM DGPU_DISC_MAXSYM
 
-// (type, ADP type) histogram: hist[t*(nanis+1)+a]; bad counts atoms of a real
-// type whose ADP type lies outside 1..nanis
-__global__ void k_group_hist(const int32_t *__restrict__ iscat, const int32_t *__restrict__ ianis, int64_t n,
-                             int32_t nscat, int32_t nanis, int32_t *hist, int32_t *bad)
+// Slot of an atom: its type, or with DISCAMB (slut != null) the table slot of
+// its (type, symmetry operation); 0 when the symmetry has no table.
+__device__ __forceinline__ int32_t group_slot(int32_t t, const int32_t *isym, const int32_t *slut, int64_t i)
+{
+    if (!slut) return t;
+    const int32_t y = isym[i];
+    return (y >= 0 && y <= DISC_MAXSYM) ? slut[t * (DISC_MAXSYM + 1) + y] : 0;
+}
+
+// (slot, ADP type) histogram: hist[s*(nanis+1)+a]; bad counts atoms of a real
+// type whose ADP type lies outside 1..nanis or whose symmetry has no table.
+// ianis null: every atom has ADP type 1.
+__global__ void k_group_hist(const int32_t *__restrict__ iscat, const int32_t *__restrict__ ianis,
+                             const int32_t *__restrict__ isym, const int32_t *__restrict__ slut, int64_t n,
+                             int32_t nscat, int32_t nslot, int32_t nanis, int32_t *hist, int32_t *bad)
 {
     __shared__ int32_t sh[GH_SHARED];
-    const int32_t nb = (nscat + 1) * (nanis + 1);
+    const int32_t nb = (nslot + 1) * (nanis + 1);
     const bool use_sh = nb <= GH_SHARED;
     if (use_sh)
         for (int k = threadIdx.x; k < nb; k += blockDim.x) sh[k] = 0;
@@ -35,12 +50,13 @@ __global__ void k_group_hist(const int32_t *__restrict__ iscat, const int32_t *_
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const int32_t t = iscat[i];
         if (t < 1 || t > nscat) continue;
-        const int32_t a = ianis[i];
-        if (a < 1 || a > nanis) {
+        const int32_t a = ianis ? ianis[i] : 1;
+        const int32_t sl = group_slot(t, isym, slut, i);
+        if (a < 1 || a > nanis || sl < 1) {
             nbad++;
             continue;
         }
-        const int32_t b = t * (nanis + 1) + a;
+        const int32_t b = sl * (nanis + 1) + a;
         if (use_sh) atomicAdd(&sh[b], 1);
         else atomicAdd(&hist[b], 1);
     }
@@ -52,7 +68,8 @@ __global__ void k_group_hist(const int32_t *__restrict__ iscat, const int32_t *_
 }
 
 // group of every atom (0 for VOID or out-of-range types)
-__global__ void k_group_map(const int32_t *__restrict__ iscat, const int32_t *__restrict__ ianis, int64_t n,
+__global__ void k_group_map(const int32_t *__restrict__ iscat, const int32_t *__restrict__ ianis,
+                            const int32_t *__restrict__ isym, const int32_t *__restrict__ slut, int64_t n,
                             int32_t nscat, int32_t nanis, const int32_t *__restrict__ gmap, int32_t *__restrict__ geff)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -60,54 +77,101 @@ __global__ void k_group_map(const int32_t *__restrict__ iscat, const int32_t *__
     const int32_t t = iscat[i];
     int32_t g = 0;
     if (t >= 1 && t <= nscat) {
-        const int32_t a = ianis[i];
-        if (a >= 1 && a <= nanis) g = gmap[t * (nanis + 1) + a];
+        const int32_t a = ianis ? ianis[i] : 1;
+        const int32_t sl = group_slot(t, isym, slut, i);
+        if (a >= 1 && a <= nanis && sl >= 1) g = gmap[sl * (nanis + 1) + a];
     }
     geff[i] = g;
 }
 
+// Groups of the partial sums: (type, ADP type) pairs of an anisotropic
+// crystal, or with DISCAMB form factors (type, symmetry operation, ADP type)
+// triples (fourier_sup.f90:166-193).  Numbered by type, then symmetry in the
+// order of the type's table list, then ADP type (the reference's ADP order
+// is first appearance, four_nanis: only the FP64 order of the final sum over
+// groups differs).  With DISCAMB, fs gets each group's table and the device
+// tables must already be in fs.dtab.
 int dgpu_anis_groups(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *op, FormSpec &fs, int32_t *ngroup)
 {
     const int64_t n = cr->natoms;
-    const int64_t nbins = (int64_t)(cr->nscat + 1) * (cr->nanis + 1);
+    const dgpu_discamb *dc = op->discamb;
+    // ADP types: always for an anisotropic crystal; with DISCAMB when given
+    const int32_t *ianis = cr->nanis >= 1 ? cr->ianis : nullptr;
+    const int32_t nanis = ianis ? cr->nanis : 1;
+    // DISCAMB: slot of every (type, symmetry operation) with a table
+    int32_t nslot = cr->nscat;
+    std::vector<int32_t> slut, slot_type;
+    if (dc) {
+        slut.assign((size_t)(cr->nscat + 1) * (DISC_MAXSYM + 1), 0);
+        slot_type.assign(1, 0);
+        nslot = 0;
+        for (int t = 1; t <= cr->nscat; t++)
+            for (int k = 0; k < dc->nsymm[t - 1]; k++) {
+                const int32_t y = dc->isymm[nslot];
+                if (y < 0 || y > DISC_MAXSYM)
+                    return dgpu_set_error(ctx, DGPU_ERR_ARG, "DISCAMB symmetry number %d outside 0..%d", y,
+                                          DISC_MAXSYM);
+                int32_t &e = slut[(size_t)t * (DISC_MAXSYM + 1) + y];
+                if (e) return dgpu_set_error(ctx, DGPU_ERR_ARG, "DISCAMB symmetry %d listed twice for type %d", y, t);
+                e = ++nslot;
+                slot_type.push_back(t);
+            }
+        if (nslot != fs.dntab)           // the caller's nsymm changed since the tables were copied
+            return dgpu_set_error(ctx, DGPU_ERR_ARG, "DISCAMB: %d tables listed, %d copied", nslot, fs.dntab);
+    }
+    const int64_t nbins = (int64_t)(nslot + 1) * (nanis + 1);
     if (nbins > ((int64_t)1 << 30))
         return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "nanis=%d too large", cr->nanis);
-    DGPU_CUDA(ctx, ctx->ghist.ensure((size_t)(nbins + 16) * sizeof(int32_t)));
+    const size_t lut_n = slut.size();
+    DGPU_CUDA(ctx, ctx->ghist.ensure((size_t)(nbins + 16 + lut_n) * sizeof(int32_t)));
     int32_t *d_hist = ctx->ghist.as<int32_t>();
     int32_t *d_bad = d_hist + nbins;
+    int32_t *d_slut = dc ? d_bad + 16 : nullptr;
     DGPU_CUDA(ctx, cudaMemsetAsync(d_hist, 0, (size_t)(nbins + 16) * sizeof(int32_t), ctx->stream));
+    if (dc)
+        DGPU_CUDA(ctx, cudaMemcpyAsync(d_slut, slut.data(), lut_n * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                       ctx->stream));
+    const int32_t *isym = dc ? cr->isym : nullptr;
     const int64_t want = dgpu_cdiv(n, 1024);
     const unsigned nblk = (unsigned)(want < 8 * ctx->nsm ? (want > 0 ? want : 1) : 8 * ctx->nsm);
-    k_group_hist<<<nblk, 1024, 0, ctx->stream>>>(cr->iscat, cr->ianis, n, cr->nscat, cr->nanis, d_hist, d_bad);
+    k_group_hist<<<nblk, 1024, 0, ctx->stream>>>(cr->iscat, ianis, isym, d_slut, n, cr->nscat, nslot, nanis, d_hist,
+                                                 d_bad);
     DGPU_CUDA(ctx, cudaGetLastError());
     std::vector<int32_t> hist((size_t)nbins + 1);
     DGPU_CUDA(ctx, cudaMemcpyAsync(hist.data(), d_hist, (size_t)(nbins + 1) * sizeof(int32_t),
                                    cudaMemcpyDeviceToHost, ctx->stream));
-    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));        // also: the host tables were read
     if (hist[nbins] > 0)
-        return dgpu_set_error(ctx, DGPU_ERR_ARG, "%d atoms with an ADP type outside 1..%d", hist[nbins], cr->nanis);
+        return dgpu_set_error(ctx, DGPU_ERR_ARG,
+                              dc ? "%d atoms with an ADP type outside 1..%d or a symmetry without a DISCAMB table"
+                                 : "%d atoms with an ADP type outside 1..%d",
+                              hist[nbins], nanis);
     std::vector<int32_t> gmap((size_t)nbins, 0);
     int32_t g = 0;
-    for (int t = 1; t <= cr->nscat; t++)
-        for (int a = 1; a <= cr->nanis; a++) {
-            const int64_t b = (int64_t)t * (cr->nanis + 1) + a;
+    for (int sl = 1; sl <= nslot; sl++)
+        for (int a = 1; a <= nanis; a++) {
+            const int64_t b = (int64_t)sl * (nanis + 1) + a;
             if (hist[b] == 0) continue;
             if (++g > 63)
-                return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "more than 63 (type, ADP type) groups");
+                return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, dc ? "more than 63 (type, symmetry, ADP type) groups"
+                                                                    : "more than 63 (type, ADP type) groups");
             gmap[b] = g;
-            fs.gtype[g] = t;
-            for (int k = 0; k < 6; k++) fs.gU[6 * g + k] = cr->anis_full[6 * (int64_t)(a - 1) + k];
+            fs.gtype[g] = dc ? slot_type[sl] : sl;
+            fs.gtab[g] = sl - 1;
+            for (int k = 0; k < 6; k++)
+                fs.gU[6 * g + k] = cr->anis_full ? cr->anis_full[6 * (int64_t)(a - 1) + k] : 0.0;
         }
     if (g == 0) {                 // no scattering atom at all: one empty group
         g = 1;
         fs.gtype[1] = 1;
+        fs.gtab[1] = 0;
         for (int k = 0; k < 6; k++) fs.gU[6 + k] = 0.0;
     }
     DGPU_CUDA(ctx, cudaMemcpyAsync(d_hist, gmap.data(), (size_t)nbins * sizeof(int32_t), cudaMemcpyHostToDevice,
                                    ctx->stream));
     DGPU_CUDA(ctx, ctx->geff.ensure((size_t)(n > 0 ? n : 1) * sizeof(int32_t)));
-    k_group_map<<<(unsigned)dgpu_cdiv(n, 256), 256, 0, ctx->stream>>>(cr->iscat, cr->ianis, n, cr->nscat, cr->nanis,
-                                                                      d_hist, ctx->geff.as<int32_t>());
+    k_group_map<<<(unsigned)dgpu_cdiv(n, 256), 256, 0, ctx->stream>>>(cr->iscat, ianis, isym, d_slut, n, cr->nscat,
+                                                                      nanis, d_hist, ctx->geff.as<int32_t>());
     DGPU_CUDA(ctx, cudaGetLastError());
     // the map lives in ghist until the kernel has read it
     DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

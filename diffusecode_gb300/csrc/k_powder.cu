@@ -324,6 +324,7 @@ extern "C" int dgpu_powder_complete(dgpu_ctx *ctx, const dgpu_crystal *cr, const
     op.lperiod = 1;
     op.diff_scale = 1.0;
     op.ldbw = (opts->ldbw && !cr->is_anis) ? 1 : 0;
+    op.discamb = nullptr;           // the powder run has ldiscamb = .false. (fourier_sup.f90:507)
 
     int64_t maxnp = 1;
     for (const PowderSlab &s : plan.slabs) maxnp = std::max(maxnp, (int64_t)s.nh * s.nk * s.nl);

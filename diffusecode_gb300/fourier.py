@@ -41,6 +41,49 @@ def _cplx(buf, shape):
     return (buf[0::2] + 1j * buf[1::2]).reshape(shape, order="F")
 
 
+class DiscambTables:
+    """DISCAMB aspherical form factors (discus_discamb.f90:15-26): for every
+    scattering type t (1..nscat) the symmetry operation numbers isymm[t-1]
+    (cr_iscat(2,:) values) and one complex table per operation over integer
+    h in [-maxhkl, maxhkl]^3, tables[t-1][k][h+m0, k+m1, l+m2]
+    (disc_list(t)%four_form_tsc(h,k,l,k), discamb_set_form_tsc :447-546).
+    attach(opts) points opts at the flattened copy."""
+
+    def __init__(self, maxhkl, isymm, tables):
+        self.maxhkl = tuple(int(m) for m in maxhkl)
+        self.isymm = [list(int(y) for y in ys) for ys in isymm]
+        shape = tuple(2 * m + 1 for m in self.maxhkl)
+        flat = []
+        for ts, ys in zip(tables, self.isymm):
+            assert len(ts) == len(ys)
+            for tab in ts:
+                tab = np.asarray(tab, dtype=np.complex128)
+                assert tab.shape == shape, (tab.shape, shape)
+                flat.append(np.stack([tab.real, tab.imag], -1).transpose(2, 1, 0, 3).ravel())
+        self.tables = [[np.asarray(t, dtype=np.complex128) for t in ts] for ts in tables]
+        self._nsymm = np.asarray([len(ys) for ys in self.isymm], np.int32)
+        self._isymm = np.asarray([y for ys in self.isymm for y in ys] or [0], np.int32)
+        self._tsc = np.ascontiguousarray(np.concatenate(flat) if flat else np.zeros(2))
+        self._c = _abi.Discamb()
+        for k in range(3):
+            self._c.maxhkl[k] = self.maxhkl[k]
+        self._c.nsymm = _abi.iptr(self._nsymm)
+        self._c.isymm = _abi.iptr(self._isymm)
+        self._c.form_tsc = _abi.dptr(self._tsc)
+
+    def attach(self, opts: _abi.Opts):
+        """Points opts at the tables; opts keeps this object (and so the
+        host arrays the library copies from) alive."""
+        opts.discamb = C.pointer(self._c)
+        opts._discamb_owner = self
+        return self
+
+    def value(self, t, k, hkl):
+        """Table k (0-based) of type t (1-based) at integer hkl (nint of each component)."""
+        ijk = tuple(int(np.sign(x) * np.floor(abs(x) + 0.5)) + m for x, m in zip(hkl, self.maxhkl))
+        return self.tables[t - 1][k][ijk]
+
+
 def attach_selections(opts: _abi.Opts, aver_cells=None, lot_origins=None):
     """Points opts at the caller's random draws: the <F> cell selection
     cells(csize1,csize2,csize3) (fourier_sup.f90:1235-1241) and the lot origins

@@ -123,6 +123,7 @@ class CrystalData:
     anis_full: np.ndarray | None = None  # (nanis, 6) U11 U22 U33 U23 U13 U12, A^2
     ar: tuple = (0.0, 0.0, 0.0)          # reciprocal cell lengths, 1/A
     dim_lo: tuple | None = None          # cr_dim(:,1); None = min over the positions
+    isym: np.ndarray | None = None       # (natoms,) int32, cr_iscat(2,:): generating symmetry (DISCAMB)
     _keep: list = field(default_factory=list, repr=False)
 
     def __post_init__(self):
@@ -143,6 +144,8 @@ class CrystalData:
             self.anis_full = np.ascontiguousarray(np.asarray(self.anis_full, dtype=np.float64).reshape(-1, 6))
         if self.dim_lo is None:
             self.dim_lo = tuple(float(x) for x in self.pos.min(axis=0)) if len(self.pos) else (0.0, 0.0, 0.0)
+        if self.isym is not None:
+            self.isym = np.ascontiguousarray(self.isym, dtype=np.int32)
 
     @property
     def is_anis(self):
@@ -186,6 +189,8 @@ class CrystalData:
             cr.nanis = int(self.anis_full.shape[0])
             cr.ianis = ianis_ptr if ianis_ptr is not None else _abi.iptr(self.ianis)
             cr.anis_full = _abi.dptr(self.anis_full)
+        if self.isym is not None:
+            cr.isym = _abi.iptr(self.isym)
         return cr
 
     def with_positions(self, pos, atom_occ=None):
@@ -194,7 +199,7 @@ class CrystalData:
                            dw=self.dw, dim0=self.dim0, delfr=self.delfr, delfi=self.delfi,
                            atom_occ=self.atom_occ if atom_occ is None else atom_occ,
                            name=self.name, ianis=self.ianis, anis_full=self.anis_full, ar=self.ar,
-                           dim_lo=self.dim_lo)
+                           dim_lo=self.dim_lo, isym=self.isym)
 
 
 @dataclass

@@ -106,7 +106,28 @@ typedef struct dgpu_crystal {
     double         dim_lo[3];  /* cr_dim(:,1), lower corner of the atom positions; lots
                                   use it to place atoms stored after the
                                   ncatoms*icc(1)*icc(2)*icc(3) block (fourier_sup.f90:1886-1899) */
+    const int32_t *isym;       /* cr_iscat(2,:), the symmetry operation that generated
+                                  each atom; read only with DISCAMB form factors     */
 } dgpu_crystal;
+
+/* DISCAMB aspherical form factors (discus_discamb.f90:15-26): the tables
+ * discamb_read (:136-400) reads and discamb_set_form_tsc (:447-546) expands
+ * per symmetry operation, supplied by the caller as `cr_scat` is.  Type t
+ * (1..nscat) has nsymm[t-1] tables, one per symmetry operation number listed
+ * in isymm (disc_list(t)%isymm(1:), types one after another); table m holds
+ * complex values over integer h in [-maxhkl, maxhkl] per axis, element
+ * (h,k,l) at form_tsc[2*(m*T + (h+mh0) + (2mh0+1)((k+mh1) + (2mh1+1)(l+mh2)))]
+ * (real, imaginary), T = (2mh0+1)(2mh1+1)(2mh2+1).  four_run then sums the
+ * atoms per (type, symmetry, ADP type) group (fourier_sup.f90:166-193,
+ * four_getatm_discamb :2259-2436) and multiplies each group's sum at grid
+ * point h by table(nint(h)) and, with ldbw, by the group's four_dbw term
+ * (tcsf_form_discamb, fourier_form.f90:63-102).                             */
+typedef struct dgpu_discamb {
+    int32_t        maxhkl[3];
+    const int32_t *nsymm;      /* nscat values                                        */
+    const int32_t *isymm;      /* sum(nsymm) symmetry operation numbers, 0..192       */
+    const double  *form_tsc;   /* sum(nsymm) tables, host memory                      */
+} dgpu_discamb;
 
 /* The reciprocal-space grid: diffuse_mod eck/vi/inc (diffuse_mod.f90:100,113-119). */
 typedef struct dgpu_grid {
@@ -152,6 +173,11 @@ typedef struct dgpu_opts {
                                for its own MMAs and copies, frees its tensor
                                memory and returns DGPU_ERR_TIMEOUT; the context
                                stays usable.  For tests of that path.            */
+    const dgpu_discamb *discamb; /* DISCAMB form factors instead of the independent
+                               atom model (diff_table RAD_DISC, fourier_sup.f90:
+                               107-118); NULL = off.  Not with <F> subtraction:
+                               the reference multiplies its lattice sum by the
+                               table of type 0, which does not exist.            */
 } dgpu_opts;
 
 /* What four_run reports besides the arrays. */

@@ -529,9 +529,13 @@ static int oc_in_lot(const dgpu_opts *op, int32_t ii, int32_t jj, int32_t kk)
 }
 
 /* Atom i is of type t and, when a > 0, of ADP type a. */
-static int oc_match(const dgpu_crystal *cr, int64_t i, int t, int a)
+/* Atom i is of type t, ADP type a (any when a <= 0) and, with DISCAMB,
+ * generated by symmetry operation y (any when y < 0): four_getatm_anis /
+ * four_getatm_discamb (fourier_sup.f90:2012, 2246-2247). */
+static int oc_match(const dgpu_crystal *cr, int64_t i, int t, int a, int y)
 {
     if (cr->iscat[i] != t) return 0;
+    if (y >= 0 && cr->isym[i] != y) return 0;
     return a <= 0 || cr->ianis[i] == a;
 }
 
@@ -543,7 +547,7 @@ static int oc_match(const dgpu_crystal *cr, int64_t i, int t, int a)
  * stored after the periodic block whose INT(pos) is that cell, all shifted
  * by the lot origin.  xat == NULL counts only; xat is SoA with stride n.
  * *ncell receives the cells of the lot. */
-static int64_t oc_getatm_lot(const dgpu_crystal *cr, const dgpu_opts *op, int t, int a,
+static int64_t oc_getatm_lot(const dgpu_crystal *cr, const dgpu_opts *op, int t, int a, int y,
                              const int32_t lbeg[3], double *xat, float *w, int64_t n,
                              int32_t *ncell)
 {
@@ -551,7 +555,7 @@ static int64_t oc_getatm_lot(const dgpu_crystal *cr, const dgpu_opts *op, int t,
     if (!oc_lots_on(op)) {
         *ncell = cr->icc[0] * cr->icc[1] * cr->icc[2];
         for (int64_t i = 0; i < cr->natoms; i++)
-            if (oc_match(cr, i, t, a)) {
+            if (oc_match(cr, i, t, a, y)) {
                 if (xat) {
                     for (int k = 0; k < 3; k++) xat[k * n + m] = cr->pos[3 * i + k];
                     if (w) w[m] = cr->atom_occ ? cr->atom_occ[i] : 1.0f;
@@ -581,7 +585,7 @@ static int64_t oc_getatm_lot(const dgpu_crystal *cr, const dgpu_opts *op, int t,
                           + (icell[1] - 1) * (int64_t)cr->icc[0] + (icell[0] - 1);
                 for (int32_t is = 0; is < cr->ncatoms; is++) {
                     int64_t ia = c * cr->ncatoms + is;
-                    if (ia >= cr->natoms || !oc_match(cr, ia, t, a)) continue;
+                    if (ia >= cr->natoms || !oc_match(cr, ia, t, a, y)) continue;
                     if (xat) {
                         for (int k = 0; k < 3; k++) xat[k * n + m] = cr->pos[3 * ia + k] - off[k];
                         if (w) w[m] = cr->atom_occ ? cr->atom_occ[ia] : 1.0f;
@@ -592,7 +596,7 @@ static int64_t oc_getatm_lot(const dgpu_crystal *cr, const dgpu_opts *op, int t,
                 for (int k = 0; k < 3; k++) jc[k] = icell[k] + lround(cr->dim_lo[k]) - 1;
                 for (int64_t ir = cr_end; ir < cr->natoms; ir++) {
                     if ((int64_t)cr->pos[3 * ir] != jc[0] || (int64_t)cr->pos[3 * ir + 1] != jc[1] ||
-                        (int64_t)cr->pos[3 * ir + 2] != jc[2] || !oc_match(cr, ir, t, a))
+                        (int64_t)cr->pos[3 * ir + 2] != jc[2] || !oc_match(cr, ir, t, a, y))
                         continue;
                     if (xat) {
                         for (int k = 0; k < 3; k++) xat[k * n + m] = cr->pos[3 * ir + k] - off[k];
@@ -671,6 +675,44 @@ static void oc_apply_form(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu
             }
 }
 
+/* tcsf_form_discamb (fourier_form.f90:63-102): the sum of the atoms of type
+ * t, symmetry slot k (0-based) and ADP type a times the caller's table at
+ * nint(h), then times four_dbw(a) (1 without ldbw).  Returns 1 when a point
+ * maps outside the table. */
+static int oc_apply_discamb(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op, int t,
+                            int k, int a, const int32_t fnum[3], double *tcsf)
+{
+    const dgpu_discamb *dc = op->discamb;
+    const int32_t *num = g->inc, *mh = dc->maxhkl;
+    const int64_t n0 = 2 * mh[0] + 1, n1 = 2 * mh[1] + 1, tsz = n0 * n1 * (2 * mh[2] + 1);
+    int64_t m = k;
+    for (int u = 1; u < t; u++) m += dc->nsymm[u - 1];
+    const double *tab = dc->form_tsc + 2 * m * tsz;
+    for (int32_t l = 0; l < fnum[2]; l++)
+        for (int32_t j = 0; j < fnum[1]; j++)
+            for (int32_t i = 0; i < fnum[0]; i++) {
+                int64_t p = i + (int64_t)num[0] * (j + (int64_t)num[1] * l);
+                double h[3];
+                int64_t ii[3];
+                oc_hvec(g->eck, g->vi, i, j, l, h);
+                for (int c = 0; c < 3; c++) {
+                    ii[c] = lround(h[c]);
+                    if (ii[c] < -mh[c] || ii[c] > mh[c]) return 1;
+                }
+                const double *f = tab + 2 * ((ii[0] + mh[0]) + n0 * ((ii[1] + mh[1]) + n1 * (ii[2] + mh[2])));
+                double ar = tcsf[2 * p], ai = tcsf[2 * p + 1];
+                double xr = ar * f[0] - ai * f[1], xi = ar * f[1] + ai * f[0];
+                if (op->ldbw) {
+                    double d = oc_dbw(cr, a, h);
+                    xr *= d;
+                    xi *= d;
+                }
+                tcsf[2 * p] = xr;
+                tcsf[2 * p + 1] = xi;
+            }
+    return 0;
+}
+
 /* One type's (or the lattice's) sum into tcsf (zeroed over num first). */
 static void oc_strucf_mode(const dgpu_grid *g, const dgpu_opts *op, const double *xat,
                            const float *w, int64_t nxat, const int32_t lmn[6],
@@ -718,6 +760,11 @@ int oc_four_run(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,
     int rc, warn = 0;
     if (cr->natoms < 1) return DGPU_ERR_NO_ATOMS;
     if (cr->is_anis && (cr->nanis < 1 || !cr->ianis || !cr->anis_full)) return DGPU_ERR_ARG;
+    if (op->discamb) {
+        if (!cr->isym || !op->discamb->nsymm || !op->discamb->isymm || !op->discamb->form_tsc) return DGPU_ERR_ARG;
+        if (op->fave != 0.0) return DGPU_ERR_UNSUPPORTED;   /* four_aver would read disc_list(0) */
+        if (op->ldbw && (cr->nanis < 1 || !cr->ianis || !cr->anis_full)) return DGPU_ERR_ARG;
+    }
     oc_csize(cr, op, cs);
     rc = oc_check_lots(cr, op, cs);
     if (rc) return rc;
@@ -733,7 +780,7 @@ int oc_four_run(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,
     double *cex = (double *)malloc(sizeof(double) * 2 * DGPU_I2PI);
     double *xat = (double *)malloc(sizeof(double) * 3 * cr->natoms);
     float *w = (float *)malloc(sizeof(float) * cr->natoms);
-    int32_t *alist = (int32_t *)malloc(sizeof(int32_t) * (cr->is_anis ? cr->natoms : 1));
+    int32_t *alist = (int32_t *)malloc(sizeof(int32_t) * (cr->ianis ? cr->natoms : 1));
     int64_t pairs = 0;
 
     rc = oc_fourier_lmn(g->eck, g->vi, g->inc, lmn, off);
@@ -837,17 +884,27 @@ int oc_four_run(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,
             for (int k = 0; k < 3; k++) lbeg[k] = op->lot_origins[3 * lot + k];
         }
         memset(csf, 0, sizeof(double) * 2 * np);
-        for (int t = 1; t <= cr->nscat; t++) {
+        /* DISCAMB: (type, symmetry, ADP) groups (fourier_sup.f90:166-193) */
+        const dgpu_discamb *dc = op->discamb;
+        const int by_adp = cr->is_anis || (dc && cr->ianis && cr->nanis >= 1);
+        for (int t = 1, ks = 0; t <= cr->nscat; ks += dc ? dc->nsymm[t - 1] : 0, t++) {
             int na = 1;
-            if (cr->is_anis) na = oc_anis_list(cr, t, alist);
+            if (by_adp) na = oc_anis_list(cr, t, alist);
+            const int nk = dc ? dc->nsymm[t - 1] : 1;
+            for (int k = 0; k < nk; k++)
             for (int j = 0; j < na; j++) {
-                int a = cr->is_anis ? alist[j] : 0;
-                int64_t nx = oc_getatm_lot(cr, op, t, a, lbeg, NULL, NULL, 0, &lcell);
+                int a = by_adp ? alist[j] : 0;
+                int y = dc ? dc->isymm[ks + k] : -1;
+                int64_t nx = oc_getatm_lot(cr, op, t, a, y, lbeg, NULL, NULL, 0, &lcell);
                 if (nx <= 0) continue;
-                oc_getatm_lot(cr, op, t, a, lbeg, xat, w, nx, &lcell);
+                oc_getatm_lot(cr, op, t, a, y, lbeg, xat, w, nx, &lcell);
                 pairs += nx * np;
                 oc_strucf_mode(g, op, xat, cr->atom_occ ? w : NULL, nx, lmn, off, fnum, cex, nthreads, tcsf);
-                oc_apply_form(cr, g, op, t, a, cfact, istl, fnum, tcsf);
+                if (dc) {
+                    if (oc_apply_discamb(cr, g, op, t, k, a > 0 ? a : 1, fnum, tcsf)) { rc = DGPU_ERR_ARG; goto done; }
+                } else {
+                    oc_apply_form(cr, g, op, t, a, cfact, istl, fnum, tcsf);
+                }
                 for (int64_t p = 0; p < 2 * np; p++) csf[p] += tcsf[p];
                 if (op->cancel && *op->cancel) { rc = DGPU_ERR_CANCELLED; goto done; }
             }
@@ -1088,9 +1145,9 @@ double oc_time_ref_rows(const dgpu_crystal *cr, const dgpu_grid *g, int32_t row_
         memset(&whole, 0, sizeof(whole));
         whole.ilots = DGPU_LOT_OFF;
         int32_t nc;
-        int64_t nx = oc_getatm_lot(cr, &whole, t, 0, NULL, NULL, NULL, 0, &nc);
+        int64_t nx = oc_getatm_lot(cr, &whole, t, 0, -1, NULL, NULL, NULL, 0, &nc);
         if (nx <= 0) continue;
-        oc_getatm_lot(cr, &whole, t, 0, NULL, xat, NULL, nx, &nc);
+        oc_getatm_lot(cr, &whole, t, 0, -1, NULL, xat, NULL, nx, &nc);
         oc_strucf_ref(xat, NULL, nx, g->vi, g->vi + 3, g->vi + 6, off, lmn, num, fnum, cex,
                       row_lo, row_hi, nthreads, tcsf);
         pairs += nx * (int64_t)(row_hi - row_lo) * num[1] * num[2];

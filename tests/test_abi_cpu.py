@@ -39,14 +39,17 @@ def test_struct_layouts_match_c(tmp_path):
     prog = tmp_path / "sz.c"
     prog.write_text(
         '#include <stdio.h>\n#include <stddef.h>\n#include "discus_gpu.h"\n'
-        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu %zu\\n\", sizeof(dgpu_crystal), sizeof(dgpu_grid),"
-        " sizeof(dgpu_opts), sizeof(dgpu_info), offsetof(dgpu_opts, cancel), offsetof(dgpu_info, res),"
-        " offsetof(dgpu_crystal, delfi)); return 0;}\n")
+        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n\", sizeof(dgpu_crystal),"
+        " sizeof(dgpu_grid), sizeof(dgpu_opts), sizeof(dgpu_info), offsetof(dgpu_opts, cancel),"
+        " offsetof(dgpu_info, res), offsetof(dgpu_crystal, delfi), offsetof(dgpu_crystal, isym),"
+        " offsetof(dgpu_opts, discamb), sizeof(dgpu_discamb), offsetof(dgpu_discamb, form_tsc)); return 0;}\n")
     exe = tmp_path / "sz"
     subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(prog), "-o", str(exe)])
     vals = [int(x) for x in subprocess.check_output([str(exe)]).split()]
     assert vals == [C.sizeof(_abi.Crystal), C.sizeof(_abi.Grid), C.sizeof(_abi.Opts), C.sizeof(_abi.Info),
-                    _abi.Opts.cancel.offset, _abi.Info.res.offset, _abi.Crystal.delfi.offset]
+                    _abi.Opts.cancel.offset, _abi.Info.res.offset, _abi.Crystal.delfi.offset,
+                    _abi.Crystal.isym.offset, _abi.Opts.discamb.offset, C.sizeof(_abi.Discamb),
+                    _abi.Discamb.form_tsc.offset]
 
 
 def test_lmn_host_entry_needs_no_device(built_lib):
