@@ -140,7 +140,7 @@ struct dgpu_ctx {
     double batch_ms = 0.0;
     double tc_kernel_ms = 0.0;              // duration of the last single-problem tensor-core launch
     std::map<TcKey, TcChoice> tc_tuned;   // autotuner results per problem shape
-    BatchState *batch = nullptr;          // captured population graph and its buffers
+    BatchState *batch[2] = {nullptr, nullptr};   // captured population graphs (most recent first)
     int32_t tc_last[4] = {-1, -1, -1, -1};
     // Deferred tensor-core launches (a run of launches with one host wait at
     // its end): plans are uploaded from the pinned arena, the error flag is
@@ -415,6 +415,73 @@ void dgpu_formcoef_fill(const dgpu_crystal *cr, void *host);
 int dgpu_formtab_async(dgpu_ctx *ctx, const void *d_coef, int32_t nscat, const dgpu_opts *op, double2 *d_cfact);
 int dgpu_combine_async(dgpu_ctx *ctx, const FormSpec *d_fs, const BoxSpec &box, const PartRef &part,
                        const int32_t *istl, const double2 *cfact, double2 *csf, double *dsi, double diff_scale);
+
+// ---- member-indexed launches of a batch (one launch for all members) -----
+// Member blockIdx.y of a launch runs the blocks its own size needs; the rest
+// of the launch's blocks return at once.  The arrays of member descriptors
+// live in device memory (filled once per batch shape).
+struct PrepMember {
+    const double *pos;
+    const int32_t *iscat;
+    const float *aocc;
+    int64_t n, nblk;       // atoms, prepare blocks
+    int32_t nscat, num[3];
+    PhaseGeom g;
+    int32_t *counts;
+    int64_t *offs, *ts;
+    uint64_t *ph0, *du, *dv, *dw;
+    float *w;
+    int32_t *idx;
+    double rten[9];
+    int32_t *istl;
+    const void *coef;      // FormCoef of the member's types
+    double2 *cfact;
+};
+// type counts, scan and scatter of every member's atoms
+int dgpu_prepare_members(dgpu_ctx *ctx, const PrepMember *d_m, int32_t nc, int64_t max_nblk);
+// istl and cfact of every member (constants of a batch shape); flag: set
+// when an istl exceeds the form-factor table
+int dgpu_tables_members(dgpu_ctx *ctx, const PrepMember *d_m, int32_t nc, int64_t max_np, int32_t max_nscat,
+                        const dgpu_opts *op, int32_t *flag);
+
+struct PartLayout {
+    int64_t s0, s1, s2, slab;
+    int64_t m1, m2, nthr;      // strides of axes a1, a2; slots walked
+    int32_t a0, a1, a2;        // box axes from innermost to outermost
+};
+PartLayout dgpu_part_layout(const PartRef &r, const BoxSpec &box);
+struct EpiMember {
+    const FormSpec *fs;    // device
+    BoxSpec box;
+    const float2 *part;
+    int32_t nslice, idim;
+    PartLayout lay;
+    const int32_t *istl;
+    const double2 *cfact;
+    double2 *csf;
+    double *dsi;
+    double ds, sqds;
+    int64_t np;
+};
+// combine and Friedel mirror of every member (tensor-core FP32 partials)
+int dgpu_epilogue_members(dgpu_ctx *ctx, const EpiMember *d_m, int32_t nc, int64_t max_thr, int64_t max_np);
+struct AdjMember {
+    const FormSpec *fs;    // device
+    BoxSpec box;
+    int32_t idim, nscat;
+    const double2 *csf;
+    const double *dsi;
+    const int32_t *istl;
+    const double2 *cfact;
+    const double *it, *wt;
+    double *g, *chi;       // chi: 512 block parts, then chi^2 at chi[512]
+    double *chi_out;       // chi^2 again, contiguous over the members
+    double sqds;
+    int64_t np, nb;
+    float2 *Q;
+};
+// g, chi^2 and Q of every member (the per-atom sums follow on the tensor cores)
+int dgpu_adjoint_members(dgpu_ctx *ctx, const AdjMember *d_m, int32_t nc, int64_t max_nb);
 int dgpu_adjoint_async(dgpu_ctx *ctx, const FormSpec *d_fs, const BoxSpec &box, int32_t friedel_dim,
                        const dgpu_grid *grid, double diff_scale, int32_t nscat, const int64_t *ts,
                        const uint64_t *ph0, const uint64_t *du, const uint64_t *dv, const uint64_t *dw,
@@ -429,6 +496,8 @@ struct AdjItem {
     int32_t t;           // type (0-based)
     int32_t kc;          // column chunk
     int32_t rt0, rt1;    // row tiles
+    int32_t prob = 0;    // problem of the launch (batch member)
+    int32_t pad_ = 0;
 };
 
 // Geometry of one tensor-core adjoint launch.
@@ -451,6 +520,27 @@ struct AdjTcPlan {
 };
 void dgpu_adjtc_plan(dgpu_ctx *ctx, const BoxSpec &box, const dgpu_grid *grid, int32_t nscat, const int64_t *ts,
                      AdjTcPlan &plan);
+// One problem of a tensor-core adjoint launch: geometry, prepared atoms (row
+// axes and column axis), Q and its images and scale, gradient outputs.
+struct AdjTcProb {
+    AdjTcGeom g;
+    const uint64_t *ph0, *dra, *drb, *dac;
+    const float *w;
+    const int32_t *aidx;
+    const float2 *Q;
+    uint8_t *qimg;
+    uint32_t *qmax;
+    double *gpos, *gocc;
+    int64_t nimg;
+    int32_t nscat;
+};
+void dgpu_adjtc_prob(const AdjTcPlan &plan, const uint64_t *ph0, const uint64_t *du, const uint64_t *dv,
+                     const uint64_t *dw, const float *w, const int32_t *aidx, const float2 *Q, uint8_t *img,
+                     uint32_t *qmax, double *gpos, double *gocc, AdjTcProb &P);
+// Q scales (zeroed by the caller), Q images and the per-atom sums of every
+// member in three launches; d_items carry each item's member in prob.
+int dgpu_adjtc_members(dgpu_ctx *ctx, const AdjTcProb *d_probs, int32_t nc, int64_t max_nimg, const AdjItem *d_items,
+                       int64_t nitems, int32_t *err);
 size_t dgpu_adjtc_img_bytes(const AdjTcPlan &plan);
 // Enqueue only: Q scale, Q images, main kernel (d_items: the plan's items on
 // the device; err: zeroed by the caller, read after the stream).

@@ -25,13 +25,14 @@
 #define ADJ_NT 128
 #define ADJ_TP 256
 
-__global__ void k_adj_g(const double *__restrict__ dsi, const double *__restrict__ it,
-                        const double *__restrict__ wt, int64_t np, double *__restrict__ g,
-                        double *__restrict__ chi_part)
+// block bx of nbx (256 threads): g over a grid-stride range, this block's chi^2 part
+__device__ __forceinline__ void adj_g_block(const double *__restrict__ dsi, const double *__restrict__ it,
+                                            const double *__restrict__ wt, int64_t np, double *__restrict__ g,
+                                            double *__restrict__ chi_part, int64_t bx, int64_t nbx)
 {
     __shared__ double sh[256];
     double acc = 0.0;
-    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t p = bx * blockDim.x + threadIdx.x; p < np; p += nbx * blockDim.x) {
         const double d = dsi[p] - it[p];
         const double w = wt ? wt[p] : 1.0;
         g[p] = 2.0 * w * d;
@@ -43,7 +44,14 @@ __global__ void k_adj_g(const double *__restrict__ dsi, const double *__restrict
         if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
         __syncthreads();
     }
-    if (threadIdx.x == 0) chi_part[blockIdx.x] = sh[0];
+    if (threadIdx.x == 0) chi_part[bx] = sh[0];
+}
+
+__global__ void k_adj_g(const double *__restrict__ dsi, const double *__restrict__ it,
+                        const double *__restrict__ wt, int64_t np, double *__restrict__ g,
+                        double *__restrict__ chi_part)
+{
+    adj_g_block(dsi, it, wt, np, g, chi_part, blockIdx.x, gridDim.x);
 }
 
 __global__ void k_adj_chi(const double *part, int n, double *out)
@@ -97,11 +105,11 @@ __device__ __forceinline__ double adj_point(const BoxSpec &box, int32_t halved, 
 }
 
 // Q_t(p) on the box, FP32 complex, layout [t][box point]
-__global__ void k_adj_q(const FormSpec *fs, BoxSpec box, int32_t halved, const double *__restrict__ g,
-                        const double2 *__restrict__ csf, const int32_t *__restrict__ istl,
-                        const double2 *__restrict__ cfact, double sqds, float2 *__restrict__ Q)
+__device__ __forceinline__ void adj_q_point(const FormSpec *fs, const BoxSpec &box, int32_t halved,
+                                            const double *__restrict__ g, const double2 *__restrict__ csf,
+                                            const int32_t *__restrict__ istl, const double2 *__restrict__ cfact,
+                                            double sqds, float2 *__restrict__ Q, int64_t pb)
 {
-    const int64_t pb = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
     if (pb >= nb) return;
     int32_t c[3];
@@ -122,6 +130,50 @@ __global__ void k_adj_q(const FormSpec *fs, BoxSpec box, int32_t halved, const d
         const double qi = sc * (f.x * ci - f.y * cr);
         Q[(int64_t)(t - 1) * nb + pb] = make_float2((float)qr, (float)qi);
     }
+}
+
+__global__ void k_adj_q(const FormSpec *fs, BoxSpec box, int32_t halved, const double *__restrict__ g,
+                        const double2 *__restrict__ csf, const int32_t *__restrict__ istl,
+                        const double2 *__restrict__ cfact, double sqds, float2 *__restrict__ Q)
+{
+    adj_q_point(fs, box, halved, g, csf, istl, cfact, sqds, Q, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// member-indexed g, chi^2 and Q of a batch (member blockIdx.y, or blockIdx.x
+// for the one-block chi^2 sum)
+#define ADJ_G_BLOCKS 512
+__global__ void k_adj_g_m(const AdjMember *__restrict__ M)
+{
+    const AdjMember &m = M[blockIdx.y];
+    adj_g_block(m.dsi, m.it, m.wt, m.np, m.g, m.chi, blockIdx.x, ADJ_G_BLOCKS);
+}
+
+__global__ void k_adj_chi_m(const AdjMember *__restrict__ M)
+{
+    const AdjMember &m = M[blockIdx.x];
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int k = 0; k < ADJ_G_BLOCKS; k++) s += m.chi[k];
+        m.chi[ADJ_G_BLOCKS] = s;
+        *m.chi_out = s;
+    }
+}
+
+__global__ void k_adj_q_m(const AdjMember *__restrict__ M)
+{
+    const AdjMember &m = M[blockIdx.y];
+    adj_q_point(m.fs, m.box, m.idim, m.g, m.csf, m.istl, m.cfact, m.sqds, m.Q,
+                (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+int dgpu_adjoint_members(dgpu_ctx *ctx, const AdjMember *d_m, int32_t nc, int64_t max_nb)
+{
+    if (nc < 1) return DGPU_OK;
+    k_adj_g_m<<<dim3(ADJ_G_BLOCKS, (unsigned)nc), 256, 0, ctx->stream>>>(d_m);
+    k_adj_chi_m<<<(unsigned)nc, 32, 0, ctx->stream>>>(d_m);
+    k_adj_q_m<<<dim3((unsigned)dgpu_cdiv(max_nb, 256), (unsigned)nc), 256, 0, ctx->stream>>>(d_m);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    return DGPU_OK;
 }
 
 // Q of the folded atoms.  With <F> subtracted, F = sum_t c_t S_t - A and

@@ -78,10 +78,10 @@ __device__ __forceinline__ int adj_qexp(const uint32_t *qmax)
 
 // Q images: one block per (type, row tile, 32-column stage); thread unit =
 // (row r, column quad cq).  Rows and columns outside the box are zero.
-__global__ void __launch_bounds__(256) k_adjtc_qimg(const float2 *__restrict__ Q, AdjTcGeom g,
-                                                    const uint32_t *__restrict__ qmax, uint8_t *__restrict__ img)
+__device__ __forceinline__ void adjtc_qimg_block(const float2 *__restrict__ Q, const AdjTcGeom &g,
+                                                 const uint32_t *__restrict__ qmax, uint8_t *__restrict__ img,
+                                                 int64_t b)
 {
-    const int64_t b = blockIdx.x;
     const int sc = (int)(b % g.nstage);
     const int rt = (int)((b / g.nstage) % g.rtiles);
     const int t = (int)(b / ((int64_t)g.nstage * g.rtiles));
@@ -117,6 +117,12 @@ __global__ void __launch_bounds__(256) k_adjtc_qimg(const float2 *__restrict__ Q
     }
 }
 
+__global__ void __launch_bounds__(256) k_adjtc_qimg(const float2 *__restrict__ Q, AdjTcGeom g,
+                                                    const uint32_t *__restrict__ qmax, uint8_t *__restrict__ img)
+{
+    adjtc_qimg_block(Q, g, qmax, img, blockIdx.x);
+}
+
 // exp(2 pi i turn) for a 64-bit fixed-point turn to about one ulp: a float
 // part for sincospif and the remainder to first order
 __device__ __forceinline__ float2 phasor_accurate(uint64_t turn)
@@ -129,16 +135,14 @@ __device__ __forceinline__ float2 phasor_accurate(uint64_t turn)
     return make_float2(fmaf(-s, dth, c), fmaf(c, dth, s));
 }
 
+// One launch: its work items, and the problem (geometry, atoms, Q images,
+// gradient) of each -- p0 for a single problem, or probs[item.prob] in
+// device memory for the members of a batch.
 struct AdjTcLaunch {
     const AdjItem *items;
     int64_t nitems;
-    AdjTcGeom g;
-    const uint64_t *ph0, *dra, *drb, *dac;     // prepared atoms: row axes and column axis
-    const float *w;
-    const int32_t *aidx;
-    const uint8_t *qimg;
-    const uint32_t *qmax;
-    double *gpos, *gocc;
+    const AdjTcProb *probs;
+    AdjTcProb p0;
     int32_t *err;
 };
 
@@ -221,8 +225,8 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_adjtc(const AdjTcLaunch L)
     uint64_t *drain = xempty + 2;
     uint32_t *tbase = reinterpret_cast<uint32_t *>(drain + 1);
     volatile int32_t *err = L.err;
-    const AdjTcGeom &G = L.g;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    auto prob = [&](const AdjItem &I) -> const AdjTcProb & { return L.probs ? L.probs[I.prob] : L.p0; };
 
     if (threadIdx.x == 0) {
         mbar_init(afull, AT_PROD_WARPS);
@@ -256,12 +260,14 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_adjtc(const AdjTcLaunch L)
         bool ok = true;
         for (int64_t item = blockIdx.x; item < L.nitems; item += gridDim.x) {
             const AdjItem I = L.items[item];
+            const AdjTcProb &P = prob(I);
+            const AdjTcGeom &G = P.g;
             // the MMAs of the previous item are done with the A operands
             if (tid == 0 && ok && nit > 0) ok = mbar_wait(aempty, (nit - 1) & 1, err, 21);
             if (adj_prod_sync(!ok)) break;
             const int64_t a = I.a0 + tid;
             const bool valid = a < I.a_end;
-            adj_gen_a(Asm, tid, valid, valid ? L.dac[a] : 0ull, I.kc * AT_KC, G.ncols, G.ec);
+            adj_gen_a(Asm, tid, valid, valid ? P.dac[a] : 0ull, I.kc * AT_KC, G.ncols, G.ec);
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncwarp();
             if (lane == 0) mbar_arrive(afull);
@@ -279,7 +285,7 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_adjtc(const AdjTcLaunch L)
                         const int64_t im =
                             ((int64_t)I.t * G.rtiles + rt) * G.nstage + (int64_t)I.kc * (AT_KC / AT_KS) + s;
                         mbar_arrive_tx(&qfull[slot], AT_Q_BYTES);
-                        bulk_g2s(Qsm + (size_t)slot * AT_Q_BYTES, L.qimg + im * AT_Q_BYTES, AT_Q_BYTES, &qfull[slot]);
+                        bulk_g2s(Qsm + (size_t)slot * AT_Q_BYTES, P.qimg + im * AT_Q_BYTES, AT_Q_BYTES, &qfull[slot]);
                         qnext++;
                     }
             }
@@ -301,6 +307,8 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_adjtc(const AdjTcLaunch L)
             bool ok = true;
             for (int64_t item = blockIdx.x; item < L.nitems && ok; item += gridDim.x) {
                 const AdjItem I = L.items[item];
+                const AdjTcProb &P = prob(I);
+                const AdjTcGeom &G = P.g;
                 const int nks = adj_nks(G, I.kc);
                 if (!mbar_wait(afull, nit & 1, err, 23)) {
                     ok = false;
@@ -369,15 +377,17 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_adjtc(const AdjTcLaunch L)
         const int q = warp & 3;
         const int m = q * 32 + lane;
         const uint32_t lane_off = (uint32_t)(q * 32) << 16;
-        const int eq = adj_qexp(L.qmax);
-        const float sx = ldexpf(1.f, -(12 + eq)), sc = ldexpf(1.f, -(G.ec + eq));
         uint32_t nrt = 0;
         bool ok = true;
         for (int64_t item = blockIdx.x; item < L.nitems && ok; item += gridDim.x) {
             const AdjItem I = L.items[item];
+            const AdjTcProb &P = prob(I);
+            const AdjTcGeom &G = P.g;
             const int64_t a = I.a0 + m;
             const bool valid = a < I.a_end;
-            const uint64_t p0 = valid ? L.ph0[a] : 0ull, d0 = valid ? L.dra[a] : 0ull, d1 = valid ? L.drb[a] : 0ull;
+            const int eq = adj_qexp(P.qmax);
+            const float sx = ldexpf(1.f, -(12 + eq)), sc = ldexpf(1.f, -(G.ec + eq));
+            const uint64_t p0 = valid ? P.ph0[a] : 0ull, d0 = valid ? P.dra[a] : 0ull, d1 = valid ? P.drb[a] : 0ull;
             const float2 step = valid ? phasor_accurate(d0) : make_float2(1.f, 0.f);
             float t0r = 0.f, t0i = 0.f, tra = 0.f, trb = 0.f, tac = 0.f;
             // (na, nb) of the first row of each row tile, advanced by AT_R rows per tile
@@ -432,18 +442,18 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_adjtc(const AdjTcLaunch L)
                 if (lane == 0) mbar_arrive(&xempty[b]);
             }
             if (!ok) break;
-            const int32_t o = valid ? L.aidx[a] : -1;
+            const int32_t o = valid ? P.aidx[a] : -1;
             if (o >= 0) {
                 const double T0r = (double)t0r * sx, T0i = (double)t0i * sx;
                 const double Tra = (double)tra * sx, Trb = (double)trb * sx, Tac = (double)tac * sc;
-                const double wj = (double)L.w[a], zpi = 6.283185307179586476925286766559;
-                if (L.gocc) atomicAdd(&L.gocc[o], T0r);
-                if (L.gpos)
+                const double wj = (double)P.w[a], zpi = 6.283185307179586476925286766559;
+                if (P.gocc) atomicAdd(&P.gocc[o], T0r);
+                if (P.gpos)
 #pragma unroll
                     for (int k = 0; k < 3; k++) {
                         const double s = G.eck[k] * T0i + G.vi[3 * G.ra + k] * Tra + G.vi[3 * G.rb + k] * Trb +
                                          G.vi[3 * G.ac + k] * Tac;
-                        atomicAdd(&L.gpos[3 * (int64_t)o + k], -zpi * wj * s);
+                        atomicAdd(&P.gpos[3 * (int64_t)o + k], -zpi * wj * s);
                     }
             }
         }
@@ -550,23 +560,78 @@ int dgpu_adjtc_enqueue(dgpu_ctx *ctx, const AdjTcPlan &plan, const AdjItem *d_it
     DGPU_CUDA(ctx, cudaGetLastError());
     k_adjtc_qimg<<<(unsigned)plan.nimg, 256, 0, ctx->stream>>>(Q, g, d_qmax, d_img);
     DGPU_CUDA(ctx, cudaGetLastError());
-    const uint64_t *dd[3] = {du, dv, dw};
     AdjTcLaunch L;
     L.items = d_items;
     L.nitems = (int64_t)plan.items.size();
-    L.g = g;
-    L.ph0 = ph0;
-    L.dra = dd[g.ra];
-    L.drb = dd[g.rb];
-    L.dac = dd[g.ac];
-    L.w = w;
-    L.aidx = aidx;
-    L.qimg = d_img;
-    L.qmax = d_qmax;
-    L.gpos = gpos;
-    L.gocc = gocc;
+    L.probs = nullptr;
+    dgpu_adjtc_prob(plan, ph0, du, dv, dw, w, aidx, Q, d_img, d_qmax, gpos, gocc, L.p0);
     L.err = err;
     const int grid_n = (int)(L.nitems < ctx->nsm ? L.nitems : ctx->nsm);
+    k_adjtc<<<grid_n, AT_THREADS, AT_SMEM, ctx->stream>>>(L);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    return DGPU_OK;
+}
+
+void dgpu_adjtc_prob(const AdjTcPlan &plan, const uint64_t *ph0, const uint64_t *du, const uint64_t *dv,
+                     const uint64_t *dw, const float *w, const int32_t *aidx, const float2 *Q, uint8_t *img,
+                     uint32_t *qmax, double *gpos, double *gocc, AdjTcProb &P)
+{
+    const uint64_t *dd[3] = {du, dv, dw};
+    P.g = plan.g;
+    P.ph0 = ph0;
+    P.dra = dd[plan.g.ra];
+    P.drb = dd[plan.g.rb];
+    P.dac = dd[plan.g.ac];
+    P.w = w;
+    P.aidx = aidx;
+    P.Q = Q;
+    P.qimg = img;
+    P.qmax = qmax;
+    P.gpos = gpos;
+    P.gocc = gocc;
+    P.nimg = plan.nimg;
+    P.nscat = plan.nscat;
+}
+
+// member-indexed Q scale and Q images of a batch (member blockIdx.y)
+#define ADJ_QMAX_BLOCKS 64
+__global__ void k_adjtc_qmax_m(const AdjTcProb *__restrict__ M)
+{
+    const AdjTcProb &m = M[blockIdx.y];
+    const int64_t n = (int64_t)m.nscat * m.g.pbox;
+    float v = 0.f;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)ADJ_QMAX_BLOCKS * blockDim.x) {
+        const float2 q = m.Q[i];
+        v = fmaxf(v, fmaxf(fabsf(q.x), fabsf(q.y)));
+    }
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0 && v > 0.f) atomicMax(m.qmax, __float_as_uint(v));
+}
+
+__global__ void __launch_bounds__(256) k_adjtc_qimg_m(const AdjTcProb *__restrict__ M)
+{
+    const AdjTcProb &m = M[blockIdx.y];
+    if ((int64_t)blockIdx.x >= m.nimg) return;
+    adjtc_qimg_block(m.Q, m.g, m.qmax, m.qimg, blockIdx.x);
+}
+
+int dgpu_adjtc_members(dgpu_ctx *ctx, const AdjTcProb *d_probs, int32_t nc, int64_t max_nimg, const AdjItem *d_items,
+                       int64_t nitems, int32_t *err)
+{
+    if (nc < 1 || nitems < 1) return DGPU_OK;
+    k_adjtc_qmax_m<<<dim3(ADJ_QMAX_BLOCKS, (unsigned)nc), 256, 0, ctx->stream>>>(d_probs);
+    k_adjtc_qimg_m<<<dim3((unsigned)max_nimg, (unsigned)nc), 256, 0, ctx->stream>>>(d_probs);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    AdjTcLaunch L;
+    memset(&L, 0, sizeof(L));
+    L.items = d_items;
+    L.nitems = nitems;
+    L.probs = d_probs;
+    L.err = err;
+    if (!ctx->adj_attr &&
+        cudaFuncSetAttribute(k_adjtc, cudaFuncAttributeMaxDynamicSharedMemorySize, AT_SMEM) == cudaSuccess)
+        ctx->adj_attr = true;
+    const int grid_n = (int)(nitems < ctx->nsm ? nitems : ctx->nsm);
     k_adjtc<<<grid_n, AT_THREADS, AT_SMEM, ctx->stream>>>(L);
     DGPU_CUDA(ctx, cudaGetLastError());
     return DGPU_OK;

@@ -27,13 +27,8 @@ __device__ __forceinline__ double2 ld_part(const float2 *p)
 // combine kernels walk them: thread r takes slot r of the partials' own layout
 // (axis a0 innermost), so that the reads of the partials -- the bulk of the
 // traffic -- are coalesced; padding slots of the tensor-core layout idle.
-struct PartLayout {
-    int64_t s0, s1, s2, slab;
-    int64_t m1, m2, nthr;      // strides of axes a1, a2; slots walked
-    int32_t a0, a1, a2;        // box axes from innermost to outermost
-};
-
-static PartLayout layout_of(const PartRef &r, const BoxSpec &box)
+// (PartLayout: dgpu_internal.h)
+PartLayout dgpu_part_layout(const PartRef &r, const BoxSpec &box)
 {
     PartLayout L;
     int64_t s[3];
@@ -81,12 +76,12 @@ __device__ __forceinline__ bool part_point(const PartLayout &L, const BoxSpec &b
 }
 
 template <class P>
-__global__ void k_combine(const FormSpec *fs, BoxSpec box, const P *__restrict__ part,
-                          int32_t nslice, PartLayout lay, const int32_t *__restrict__ istl,
-                          const double2 *__restrict__ cfact, const double2 *__restrict__ acsf,
-                          double2 *__restrict__ csf, double *__restrict__ dsi, double ds, double sqds)
+__device__ __forceinline__ void combine_slot(const FormSpec *fs, const BoxSpec &box, const P *__restrict__ part,
+                                             int32_t nslice, const PartLayout &lay, const int32_t *__restrict__ istl,
+                                             const double2 *__restrict__ cfact, const double2 *__restrict__ acsf,
+                                             double2 *__restrict__ csf, double *__restrict__ dsi, double ds,
+                                             double sqds, int64_t r)
 {
-    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int64_t i, j, l;
     if (r >= lay.nthr || !part_point(lay, box, r, i, j, l)) return;
     int64_t idx = i + (int64_t)box.num[0] * (j + (int64_t)box.num[1] * l);
@@ -122,6 +117,16 @@ __global__ void k_combine(const FormSpec *fs, BoxSpec box, const P *__restrict__
     }
     csf[idx] = make_double2(F.x * sqds, F.y * sqds);
     dsi[idx] = (F.x * F.x + F.y * F.y) * ds;
+}
+
+template <class P>
+__global__ void k_combine(const FormSpec *fs, BoxSpec box, const P *__restrict__ part,
+                          int32_t nslice, PartLayout lay, const int32_t *__restrict__ istl,
+                          const double2 *__restrict__ cfact, const double2 *__restrict__ acsf,
+                          double2 *__restrict__ csf, double *__restrict__ dsi, double ds, double sqds)
+{
+    combine_slot(fs, box, part, nslice, lay, istl, cfact, acsf, csf, dsi, ds, sqds,
+                 (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 template <class P>
@@ -171,9 +176,9 @@ __global__ void k_aver_combine(const FormSpec *fs, BoxSpec box, const P *__restr
 // four_apply_friedel: points past the halved axis' middle take the conjugate
 // of their mirror; on the middle slab the sequential loop leaves the first
 // half, conjugates the centre and mirrors the second half.
-__global__ void k_mirror(BoxSpec box, int32_t a, double2 *csf, double2 *acsf, double *dsi)
+__device__ __forceinline__ void mirror_point(const BoxSpec &box, int32_t a, double2 *csf, double2 *acsf,
+                                             double *dsi, int64_t p)
 {
-    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int32_t *n = box.num;
     int64_t np = (int64_t)n[0] * n[1] * n[2];
     if (p >= np) return;
@@ -202,6 +207,35 @@ __global__ void k_mirror(BoxSpec box, int32_t a, double2 *csf, double2 *acsf, do
         acsf[p] = make_double2(u.x, -u.y);
     }
     dsi[p] = dsi[m];
+}
+
+__global__ void k_mirror(BoxSpec box, int32_t a, double2 *csf, double2 *acsf, double *dsi)
+{
+    mirror_point(box, a, csf, acsf, dsi, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// member-indexed combine and mirror of a batch (member blockIdx.y)
+__global__ void k_combine_m(const EpiMember *__restrict__ M)
+{
+    const EpiMember &m = M[blockIdx.y];
+    combine_slot<float2>(m.fs, m.box, m.part, m.nslice, m.lay, m.istl, m.cfact, nullptr, m.csf, m.dsi, m.ds,
+                         m.sqds, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__global__ void k_mirror_m(const EpiMember *__restrict__ M)
+{
+    const EpiMember &m = M[blockIdx.y];
+    if (m.idim < 1 || m.idim > 3) return;
+    mirror_point(m.box, m.idim - 1, m.csf, nullptr, m.dsi, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+int dgpu_epilogue_members(dgpu_ctx *ctx, const EpiMember *d_m, int32_t nc, int64_t max_thr, int64_t max_np)
+{
+    if (nc < 1) return DGPU_OK;
+    k_combine_m<<<dim3((unsigned)dgpu_cdiv(max_thr, 256), (unsigned)nc), 256, 0, ctx->stream>>>(d_m);
+    k_mirror_m<<<dim3((unsigned)dgpu_cdiv(max_np, 256), (unsigned)nc), 256, 0, ctx->stream>>>(d_m);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    return DGPU_OK;
 }
 
 struct QStat {
@@ -301,7 +335,7 @@ int dgpu_combine(dgpu_ctx *ctx, const FormSpec &fs, const BoxSpec &box, const Pa
     FormSpec *d;
     int rc = upload_formspec(ctx, fs, &d);
     if (rc) return rc;
-    const PartLayout lay = layout_of(part, box);
+    const PartLayout lay = dgpu_part_layout(part, box);
     const unsigned nblk = (unsigned)dgpu_cdiv(lay.nthr, 256);
     if (part.f32)
         k_combine<float2><<<nblk, 256, 0, ctx->stream>>>(d, box, (const float2 *)part.p, part.nslice, lay, istl,
@@ -322,7 +356,7 @@ int dgpu_aver_combine(dgpu_ctx *ctx, const FormSpec &fs, const BoxSpec &box, con
     FormSpec *d;
     int rc = upload_formspec(ctx, fs, &d);
     if (rc) return rc;
-    const PartLayout lay = layout_of(apart, box);
+    const PartLayout lay = dgpu_part_layout(apart, box);
     const unsigned nblk = (unsigned)dgpu_cdiv(lay.nthr, 256);
     if (apart.f32)
         k_aver_combine<float2><<<nblk, 256, 0, ctx->stream>>>(
@@ -375,7 +409,7 @@ int dgpu_qinfo(dgpu_ctx *ctx, const double eck[3], const double vi[9], const int
 int dgpu_combine_async(dgpu_ctx *ctx, const FormSpec *d_fs, const BoxSpec &box, const PartRef &part,
                        const int32_t *istl, const double2 *cfact, double2 *csf, double *dsi, double diff_scale)
 {
-    const PartLayout lay = layout_of(part, box);
+    const PartLayout lay = dgpu_part_layout(part, box);
     const unsigned nblk = (unsigned)dgpu_cdiv(lay.nthr, 256);
     if (part.f32)
         k_combine<float2><<<nblk, 256, 0, ctx->stream>>>(d_fs, box, (const float2 *)part.p, part.nslice, lay, istl,
@@ -570,7 +604,7 @@ int dgpu_lot_combine(dgpu_ctx *ctx, int32_t ngroup, int32_t nlot, const BoxSpec 
     PartRef none;
     memset(&none, 0, sizeof(none));
     const PartRef &r = part ? *part : none;
-    const PartLayout lay = layout_of(r, box);
+    const PartLayout lay = dgpu_part_layout(r, box);
     const unsigned nblk = (unsigned)dgpu_cdiv(lay.nthr, 256);
     const int32_t nslice = r.nslice > 0 ? r.nslice : 1;
     const int32_t nq = ngroup * nslice;

@@ -103,18 +103,25 @@ __device__ __forceinline__ int eff_type(const int32_t *iscat, int64_t i, int64_t
     return t;
 }
 
-__global__ void k_type_count(const int32_t *iscat, int64_t n, int32_t nscat, FoldSpec fs,
-                             int32_t *counts, int64_t nblk)
+// block bx of the per-(type, block) counts
+__device__ __forceinline__ void type_count_body(const int32_t *iscat, int64_t n, int32_t nscat, const FoldSpec &fs,
+                                                int32_t *counts, int64_t nblk, int64_t bx)
 {
     __shared__ int32_t hist[MAXT];
     for (int t = threadIdx.x; t < MAXT; t += blockDim.x) hist[t] = 0;
     __syncthreads();
-    int64_t i = (int64_t)blockIdx.x * PREP_BLK + threadIdx.x;
+    int64_t i = bx * PREP_BLK + threadIdx.x;
     int t = eff_type(iscat, i, n, nscat, fs);
     if (t) atomicAdd(&hist[t], 1);
     __syncthreads();
     for (int tt = threadIdx.x; tt < nscat; tt += blockDim.x)
-        counts[(int64_t)tt * nblk + blockIdx.x] = hist[tt + 1];
+        counts[(int64_t)tt * nblk + bx] = hist[tt + 1];
+}
+
+__global__ void k_type_count(const int32_t *iscat, int64_t n, int32_t nscat, FoldSpec fs,
+                             int32_t *counts, int64_t nblk)
+{
+    type_count_body(iscat, n, nscat, fs, counts, nblk, blockIdx.x);
 }
 
 // Exclusive scan of the per-(type, block) counts into int64 offsets, one CTA.
@@ -122,8 +129,8 @@ __global__ void k_type_count(const int32_t *iscat, int64_t n, int32_t nscat, Fol
 // type is padding (zero phase, zero weight) so that every 64-atom group of a
 // type (one tensor-core stage) is aligned and complete.
 #define TYPE_ALIGN 64
-__global__ void k_scan_counts(const int32_t *counts, int64_t len, int64_t *offs,
-                              int64_t nblk, int32_t nscat, int64_t *type_start)
+__device__ __forceinline__ void scan_counts_body(const int32_t *counts, int64_t *offs, int64_t nblk,
+                                                 int32_t nscat, int64_t *type_start)
 {
     __shared__ int64_t warp_sums[32];
     __shared__ int64_t carry;
@@ -166,6 +173,12 @@ __global__ void k_scan_counts(const int32_t *counts, int64_t len, int64_t *offs,
         __syncthreads();
     }
     if (threadIdx.x == 0) type_start[nscat] = (carry + TYPE_ALIGN - 1) / TYPE_ALIGN * TYPE_ALIGN;
+}
+
+__global__ void k_scan_counts(const int32_t *counts, int64_t len, int64_t *offs,
+                              int64_t nblk, int32_t nscat, int64_t *type_start)
+{
+    scan_counts_body(counts, offs, nblk, nscat, type_start);
     (void)len;
 }
 
@@ -200,16 +213,17 @@ __device__ __forceinline__ uint32_t slot_perm(uint32_t x, uint32_t n)
     return x;
 }
 
-__global__ void k_scatter_atoms(const double *pos, const int32_t *iscat, const float *aocc,
-                                int64_t n, int32_t nscat, FoldSpec fs, PhaseGeom g,
-                                const int64_t *offs, int64_t nblk, const int64_t *ts, uint64_t *ph0,
-                                uint64_t *du, uint64_t *dv, uint64_t *dw, float *w, int32_t *idx)
+__device__ __forceinline__ void scatter_atoms_body(const double *pos, const int32_t *iscat, const float *aocc,
+                                                   int64_t n, int32_t nscat, const FoldSpec &fs, const PhaseGeom &g,
+                                                   const int64_t *offs, int64_t nblk, const int64_t *ts,
+                                                   uint64_t *ph0, uint64_t *du, uint64_t *dv, uint64_t *dw,
+                                                   float *w, int32_t *idx, int64_t bx)
 {
     __shared__ int32_t wcnt[32][MAXT];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int k = threadIdx.x; k < 32 * MAXT; k += blockDim.x) (&wcnt[0][0])[k] = 0;
     __syncthreads();
-    int64_t i = (int64_t)blockIdx.x * PREP_BLK + threadIdx.x;
+    int64_t i = bx * PREP_BLK + threadIdx.x;
     int t = eff_type(iscat, i, n, nscat, fs);
     unsigned same = __match_any_sync(0xffffffffu, t);
     int rank = __popc(same & ((1u << lane) - 1u));
@@ -227,7 +241,7 @@ __global__ void k_scatter_atoms(const double *pos, const int32_t *iscat, const f
     __syncthreads();
     if (!t) return;
     // stable rank within the type, then the type's summation order
-    const int64_t rk = offs[(int64_t)(t - 1) * nblk + blockIdx.x] + wcnt[wid][t] + rank - ts[t - 1];
+    const int64_t rk = offs[(int64_t)(t - 1) * nblk + bx] + wcnt[wid][t] + rank - ts[t - 1];
     const int64_t dst = ts[t - 1] + slot_perm((uint32_t)rk, (uint32_t)ts[nscat + t]);
     double x0 = pos[3 * i], x1 = pos[3 * i + 1], x2 = pos[3 * i + 2];
     if (fs.fold) {
@@ -247,6 +261,14 @@ __global__ void k_scatter_atoms(const double *pos, const int32_t *iscat, const f
     dw[dst] = o.dw;
     w[dst] = aocc ? aocc[i] : 1.0f;
     idx[dst] = (int32_t)i;
+}
+
+__global__ void k_scatter_atoms(const double *pos, const int32_t *iscat, const float *aocc,
+                                int64_t n, int32_t nscat, FoldSpec fs, PhaseGeom g,
+                                const int64_t *offs, int64_t nblk, const int64_t *ts, uint64_t *ph0,
+                                uint64_t *du, uint64_t *dv, uint64_t *dw, float *w, int32_t *idx)
+{
+    scatter_atoms_body(pos, iscat, aocc, n, nscat, fs, g, offs, nblk, ts, ph0, du, dv, dw, w, idx, blockIdx.x);
 }
 
 size_t dgpu_prepare_region_bytes(int64_t natoms, int32_t nscat)
@@ -364,17 +386,16 @@ int dgpu_prepare_lattice(dgpu_ctx *ctx, const int32_t icc[3], const double dim0[
 // tables
 
 // istl(i,j,l) = NINT(sqrt(h.G*.h/4)/CFINC) with h rounded to REAL(4)
-__global__ void k_stltab(double e0, double e1, double e2, PhaseGeom vg, int32_t n0, int32_t n1,
-                         int32_t n2, double r00, double r10, double r20, double r01, double r11,
-                         double r21, double r02, double r12, double r22, int32_t *istl,
-                         int32_t *flag)
+// istl of grid point p; e = eck(:,1), r = rten column-major
+__device__ __forceinline__ void stltab_point(const double *e, const double *vi, int32_t n0, int32_t n1, int32_t n2,
+                                             const double *r, int32_t *istl, int32_t *flag, int64_t p)
 {
-    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int64_t np = (int64_t)n0 * n1 * n2;
     if (p >= np) return;
     int64_t i = p % n0, j = (p / n0) % n1, l = p / ((int64_t)n0 * n1);
-    const double *vi = vg.vi;
-    double e[3] = {e0, e1, e2}, h[3];
+    const double r00 = r[0], r10 = r[1], r20 = r[2], r01 = r[3], r11 = r[4], r21 = r[5], r02 = r[6], r12 = r[7],
+                 r22 = r[8];
+    double h[3];
     for (int k = 0; k < 3; k++) {
         double s = __dadd_rn(__dadd_rn(__dadd_rn(e[k], __dmul_rn(vi[k], (double)i)),
                                        __dmul_rn(vi[3 + k], (double)j)),
@@ -389,6 +410,15 @@ __global__ void k_stltab(double e0, double e1, double e2, PhaseGeom vg, int32_t 
     long long v = llround(__dmul_rn(__dsqrt_rn(q2), 1000.0));
     istl[p] = (int32_t)v;
     if (v > DGPU_CFPKT) atomicExch(flag, 1);
+}
+
+__global__ void k_stltab(double e0, double e1, double e2, PhaseGeom vg, int32_t n0, int32_t n1,
+                         int32_t n2, double r00, double r10, double r20, double r01, double r11,
+                         double r21, double r02, double r12, double r22, int32_t *istl,
+                         int32_t *flag)
+{
+    const double e[3] = {e0, e1, e2}, r[9] = {r00, r10, r20, r01, r11, r21, r02, r12, r22};
+    stltab_point(e, vg.vi, n0, n1, n2, r, istl, flag, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 int dgpu_stltab_dev(dgpu_ctx *ctx, const double eck[3], const double vi[9], const int32_t num[3],
@@ -420,10 +450,9 @@ struct FormCoef {
 };
 
 // cfact(iq,t) = sb*(f+f') + i sb*f'' ; f = c + sum_i a_i exp(-b_i s^2)
-__global__ void k_formtab(const FormCoef *fc, int32_t nscat, int32_t lxray, int32_t power,
-                          int32_t ano, int32_t ldbw, double2 *cfact)
+__device__ __forceinline__ void formtab_entry(const FormCoef *fc, int32_t nscat, int32_t lxray, int32_t power,
+                                              int32_t ano, int32_t ldbw, double2 *cfact, int64_t k)
 {
-    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= (int64_t)nscat * DGPU_NTAB) return;
     int t = (int)(k / DGPU_NTAB) + 1, iq = (int)(k % DGPU_NTAB);
     double s = __dmul_rn((double)iq, DGPU_CFINC);
@@ -435,6 +464,12 @@ __global__ void k_formtab(const FormCoef *fc, int32_t nscat, int32_t lxray, int3
     double fp = ano ? fc->delfr[t] : 0.0, fpp = ano ? fc->delfi[t] : 0.0;
     double sb = ldbw ? __dmul_rn(exp(-__dmul_rn(fc->dw[t], q2)), fc->occ[t]) : fc->occ[t];
     cfact[k] = make_double2(__dmul_rn(sb, __dadd_rn(f, fp)), __dmul_rn(sb, fpp));
+}
+
+__global__ void k_formtab(const FormCoef *fc, int32_t nscat, int32_t lxray, int32_t power,
+                          int32_t ano, int32_t ldbw, double2 *cfact)
+{
+    formtab_entry(fc, nscat, lxray, power, ano, ldbw, cfact, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 int dgpu_formtab_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *op, double2 *d_cfact)
@@ -527,6 +562,71 @@ int dgpu_prepare_async(dgpu_ctx *ctx, const double *d_pos, const int32_t *d_isca
     k_scan_counts<<<1, 1024, 0, ctx->stream>>>(counts, nblk * nscat, offs, nblk, nscat, ts_dev);
     k_scatter_atoms<<<(unsigned)nblk, PREP_BLK, 0, ctx->stream>>>(d_pos, d_iscat, d_aocc, natoms, nscat, nofold, g,
                                                                   offs, nblk, ts_dev, ph0, du, dv, dw, w, idx);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    return DGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// member-indexed launches (the batch): member blockIdx.y
+
+__global__ void __launch_bounds__(PREP_BLK) k_type_count_m(const PrepMember *__restrict__ M)
+{
+    const PrepMember &m = M[blockIdx.y];
+    if ((int64_t)blockIdx.x >= m.nblk) return;
+    const FoldSpec nofold = {0, 1, {1, 1, 1}, {0, 0, 0}, nullptr};
+    type_count_body(m.iscat, m.n, m.nscat, nofold, m.counts, m.nblk, blockIdx.x);
+}
+
+__global__ void k_scan_counts_m(const PrepMember *__restrict__ M)
+{
+    const PrepMember &m = M[blockIdx.x];
+    scan_counts_body(m.counts, m.offs, m.nblk, m.nscat, m.ts);
+}
+
+__global__ void __launch_bounds__(PREP_BLK) k_scatter_atoms_m(const PrepMember *__restrict__ M)
+{
+    const PrepMember &m = M[blockIdx.y];
+    if ((int64_t)blockIdx.x >= m.nblk) return;
+    const FoldSpec nofold = {0, 1, {1, 1, 1}, {0, 0, 0}, nullptr};
+    scatter_atoms_body(m.pos, m.iscat, m.aocc, m.n, m.nscat, nofold, m.g, m.offs, m.nblk, m.ts, m.ph0, m.du, m.dv,
+                       m.dw, m.w, m.idx, blockIdx.x);
+}
+
+__global__ void k_stltab_m(const PrepMember *__restrict__ M, int32_t *flag)
+{
+    const PrepMember &m = M[blockIdx.y];
+    stltab_point(m.g.eck, m.g.vi, m.num[0], m.num[1], m.num[2], m.rten, m.istl, flag,
+                 (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__global__ void k_formtab_m(const PrepMember *__restrict__ M, int32_t lxray, int32_t power, int32_t ano,
+                            int32_t ldbw)
+{
+    const PrepMember &m = M[blockIdx.y];
+    formtab_entry((const FormCoef *)m.coef, m.nscat, lxray, power, ano, ldbw, m.cfact,
+                  (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+int dgpu_prepare_members(dgpu_ctx *ctx, const PrepMember *d_m, int32_t nc, int64_t max_nblk)
+{
+    if (nc < 1) return DGPU_OK;
+    if (nc > 65535) return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "more than 65535 batch members");
+    const dim3 gp((unsigned)max_nblk, (unsigned)nc);
+    k_type_count_m<<<gp, PREP_BLK, 0, ctx->stream>>>(d_m);
+    k_scan_counts_m<<<(unsigned)nc, 1024, 0, ctx->stream>>>(d_m);
+    k_scatter_atoms_m<<<gp, PREP_BLK, 0, ctx->stream>>>(d_m);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    return DGPU_OK;
+}
+
+int dgpu_tables_members(dgpu_ctx *ctx, const PrepMember *d_m, int32_t nc, int64_t max_np, int32_t max_nscat,
+                        const dgpu_opts *op, int32_t *flag)
+{
+    if (nc < 1) return DGPU_OK;
+    if (nc > 65535) return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "more than 65535 batch members");
+    k_stltab_m<<<dim3((unsigned)dgpu_cdiv(max_np, 256), (unsigned)nc), 256, 0, ctx->stream>>>(d_m, flag);
+    k_formtab_m<<<dim3((unsigned)dgpu_cdiv((int64_t)max_nscat * DGPU_NTAB, 256), (unsigned)nc), 256, 0,
+                  ctx->stream>>>(d_m, op->lxray, op->power, op->ano, op->ldbw);
     DGPU_CUDA(ctx, cudaGetLastError());
     return DGPU_OK;
 }

@@ -853,16 +853,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc(const TcLaunch L)
     }
 }
 
-// FP64 -> FP32 with stochastic rounding: y rounds up with probability equal
-// to its distance from the lower neighbour in units of the spacing (u is a
-// uniform 32-bit draw), so the rounding error has mean zero over draws.  The
-// spacing is a power of two, so the division is exact in FP32.
+// FP64 -> FP32 with stochastic rounding, in integer arithmetic on the bits:
+// the 29 significand bits that FP32 drops get a uniform 29-bit draw added
+// (u >> 3) and are cut off, so the magnitude rounds up (a carry, which may
+// run into the exponent) with probability equal to its distance from the
+// lower neighbour in units of the spacing, and the rounding error has mean
+// zero over draws.  The FP32 word is then assembled from sign, rebased
+// exponent and the top 23 significand bits (no FP64 instruction: this part's
+// FP64 rate is low).  For |y| in the normal FP32 range; zero stays zero.
 __device__ __forceinline__ float round_stochastic(double y, uint32_t u)
 {
-    const float lo = __double2float_rd(y), hi = __double2float_ru(y);
-    if (lo == hi) return lo;
-    const float p = (float)(y - (double)lo) * (1.0f / (hi - lo));
-    return (float)(u >> 8) * 0x1p-24f < p ? hi : lo;
+    uint64_t b = (uint64_t)__double_as_longlong(y);
+    const int e0 = (int)((b >> 52) & 0x7FF);
+    if (e0 < 1023 - 125) return __uint_as_float((uint32_t)(b >> 32) & 0x80000000u);   // |y| < 2^-125: zero
+    b += (uint64_t)(u >> 3);
+    const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+    const uint32_t e = (uint32_t)((b >> 52) & 0x7FF) - 1023u + 127u;
+    const uint32_t man = (uint32_t)(b >> 29) & 0x7FFFFFu;
+    return __uint_as_float(sign | (e << 23) | man);
 }
 
 // exp(2 pi i t) for a 64-bit fixed-point turn t, in FP64 to about 1e-16:
@@ -1011,8 +1019,11 @@ static double tc_area(const BoxSpec &box, int ac, int N)
 }
 
 // Geometry of one problem for a column axis, tile width and slicing.
+// slice_atoms > 0: K slices of about that many atoms (a multi-problem launch,
+// where the items of all problems share the SMs), else about slice_mult
+// work items per SM for this problem alone
 static void tc_problem(dgpu_ctx *ctx, const TcInput &in, const dgpu_opts *op, int axis, int N, int slice_mult,
-                       TcProblem &g)
+                       int64_t slice_atoms, TcProblem &g)
 {
     memset(&g, 0, sizeof(g));
     const BoxSpec &box = in.box;
@@ -1042,6 +1053,8 @@ static void tc_problem(dgpu_ctx *ctx, const TcInput &in, const dgpu_opts *op, in
     int64_t nsl;
     if (op->tc_kslice > 0) {
         nsl = dgpu_cdiv(maxn, op->tc_kslice);
+    } else if (slice_atoms > 0) {
+        nsl = dgpu_cdiv(maxn, slice_atoms);
     } else {
         nsl = dgpu_cdiv((int64_t)slice_mult * ctx->nsm, tiles);
         if (nsl > 1 && dgpu_cdiv(maxn, nsl) < 2048) nsl = dgpu_cdiv(maxn, 2048);
@@ -1082,6 +1095,7 @@ int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *o
     plan.part_off.assign(nprob, 0);
     plan.nslice.assign(nprob, 0);
     int64_t items = 0, elems = 0;
+    std::vector<int> axes(nprob);
     for (int p = 0; p < nprob; p++) {
         int axis = in[p].axis;
         if (axis < 0) {
@@ -1092,8 +1106,25 @@ int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *o
             }
         }
         if (axis < 0) return dgpu_set_error(ctx, DGPU_ERR_ARG, "no tensor-core tile fits the box");
+        axes[p] = axis;
+    }
+    // several problems share the SMs: one slice length for all, from their
+    // total work (tiles x atoms), so that the whole launch has about
+    // slice_mult items per SM of about equal size (at least 2048 atoms)
+    int64_t slice_atoms = 0;
+    if (nprob > 1 && op->tc_kslice <= 0) {
+        double work = 0.0;
+        for (int p = 0; p < nprob; p++) {
+            TcProblem g;
+            tc_problem(ctx, in[p], op, axes[p], N, slice_mult, 0, g);
+            work += (double)(g.nitems / g.nslice) * (double)(g.nslice * g.slice_len);
+        }
+        slice_atoms = (int64_t)ceil(work / ((double)slice_mult * ctx->nsm));
+        if (slice_atoms < 2048) slice_atoms = 2048;
+    }
+    for (int p = 0; p < nprob; p++) {
         TcProblem &g = plan.probs[p];
-        tc_problem(ctx, in[p], op, axis, N, slice_mult, g);
+        tc_problem(ctx, in[p], op, axes[p], N, slice_mult, slice_atoms, g);
         g.item0 = items;
         items += g.nitems;
         plan.part_off[p] = elems;
