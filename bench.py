@@ -701,9 +701,12 @@ def batch_measure(ctx, steps=3):
     pairs = sum(c.n_scattering() * g.npoints for c, g in pop)
     fwd_ms, full_ms = [], []
     dsi_f = None
+    nodes = {}
     for s in range(steps + 1):
         dsi_f, _, _, _, ms_f = FR.batch_run(crs, grids, op, ctx=ctx)
+        nodes["fwd"] = FR.batch_graph_nodes(ctx)
         _, chi2, gp, go, ms = FR.batch_run(crs, grids, op, targets, weights, ctx=ctx)
+        nodes["fwd_grad"] = FR.batch_graph_nodes(ctx)
         if s:
             fwd_ms.append(ms_f)
             full_ms.append(ms)
@@ -718,6 +721,7 @@ def batch_measure(ctx, steps=3):
     return {"workload": "population-64", "members": len(pop), "atoms": int(sum(c.n_scattering() for c in crs)),
             "pairs": int(pairs), "fwd_graph_ms": f, "fwd_grad_graph_ms": t,
             "fwd_G_pairs_per_s": pairs / f / 1e6, "note": "one CUDA graph launch per step; device time",
+            "graph_nodes": {k: {"nodes": v[0], "kernels": v[1]} for k, v in nodes.items()},
             "per_crystal_rel_err_vs_fp64": {"max": max(errs), "median": float(np.median(errs)), "points": 24,
                                             "norm": "max |I-I64|/(I64 + N<|f|^2>) per member"}}
 

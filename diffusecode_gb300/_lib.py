@@ -17,7 +17,7 @@ EXPORTS = [
     "dgpu_ctx_create", "dgpu_ctx_destroy", "dgpu_last_error", "dgpu_default_opts",
     "dgpu_four_run", "dgpu_four_run_device", "dgpu_four_strucf", "dgpu_fourier_lmn",
     "dgpu_four_stltab", "dgpu_four_formtab", "dgpu_four_increments", "dgpu_chi2_grad",
-    "dgpu_batch_run", "dgpu_batch_last_ms", "dgpu_four_strucf_noalloc", "dgpu_tc_last_kernel_ms",
+    "dgpu_batch_run", "dgpu_batch_last_ms", "dgpu_batch_graph_nodes", "dgpu_four_strucf_noalloc", "dgpu_tc_last_kernel_ms",
     "dgpu_four_weight", "dgpu_four_weight_device", "dgpu_four_accumulate", "dgpu_qval",
     "dgpu_calc_hkl", "dgpu_powder_npkt", "dgpu_powder_complete", "dgpu_chi2_grad_device",
 ]
@@ -60,6 +60,8 @@ def load():
     L.dgpu_batch_run.argtypes = [vp, C.c_int32, CR, GR, OP, PP, PP, PP, dp, PP, PP]
     L.dgpu_batch_last_ms.argtypes = [vp]
     L.dgpu_batch_last_ms.restype = C.c_double
+    L.dgpu_batch_graph_nodes.argtypes = [vp, C.POINTER(C.c_int64)]
+    L.dgpu_batch_graph_nodes.restype = C.c_int64
     L.dgpu_tc_last_kernel_ms.argtypes = [vp]
     L.dgpu_tc_last_kernel_ms.restype = C.c_double
     L.dgpu_four_strucf_noalloc.argtypes = [vp, vp, C.c_int64, dp, dp, dp, dp, ip, ip, ip, vp, vp, vp]

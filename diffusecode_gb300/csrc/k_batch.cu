@@ -531,3 +531,20 @@ extern "C" int dgpu_batch_run(dgpu_ctx *ctx, int32_t nc, const dgpu_crystal *crs
 }
 
 extern "C" double dgpu_batch_last_ms(const dgpu_ctx *ctx) { return ctx ? ctx->batch_ms : 0.0; }
+
+extern "C" int64_t dgpu_batch_graph_nodes(const dgpu_ctx *ctx, int64_t *kernels)
+{
+    if (kernels) *kernels = 0;
+    if (!ctx || !ctx->batch[0] || !ctx->batch[0]->graph) return 0;
+    size_t n = 0;
+    if (cudaGraphGetNodes(ctx->batch[0]->graph, nullptr, &n) != cudaSuccess) return 0;
+    if (kernels && n) {
+        std::vector<cudaGraphNode_t> nodes(n);
+        if (cudaGraphGetNodes(ctx->batch[0]->graph, nodes.data(), &n) == cudaSuccess)
+            for (size_t i = 0; i < n; i++) {
+                cudaGraphNodeType t;
+                if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) (*kernels)++;
+            }
+    }
+    return (int64_t)n;
+}

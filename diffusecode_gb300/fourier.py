@@ -307,6 +307,14 @@ def batch_run(crystals, grids, opts, targets=None, weights=None, ctx=None):
     return dsi, chi2, [x.reshape(-1, 3) for x in gps], gos, ms
 
 
+def batch_graph_nodes(ctx=None):
+    """(all nodes, kernel nodes) of the graph the last batch_run launched."""
+    ctx = ctx or default_context()
+    k = C.c_int64(0)
+    n = ctx.lib.dgpu_batch_graph_nodes(ctx.h, C.byref(k))
+    return int(n), int(k.value)
+
+
 class Fourier:
     """Menu state of `fourier` with its reset defaults (fourier_reset.f90:42-101)."""
 

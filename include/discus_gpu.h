@@ -451,8 +451,13 @@ int dgpu_batch_run(dgpu_ctx *ctx, int32_t ncrystal, const dgpu_crystal *crystals
                    const double *const *i_target, const double *const *weight,
                    double *chi2, double *const *grad_pos, double *const *grad_occ);
 
-/* Device time of the last dgpu_batch_run call's persistent launch, ms. */
+/* Device time of the last dgpu_batch_run call's graph launch, ms. */
 double dgpu_batch_last_ms(const dgpu_ctx *ctx);
+
+/* Nodes (kernels, copies, memsets) and kernel nodes of the graph the last
+ * dgpu_batch_run call launched (kernels may be NULL).  Measurement aid; no
+ * counterpart in the reference. */
+int64_t dgpu_batch_graph_nodes(const dgpu_ctx *ctx, int64_t *kernels);
 
 /* Device time of the tensor-core type-sum kernel alone in the last
  * dgpu_four_run / dgpu_four_run_device call that used the tensor-core

@@ -35,6 +35,25 @@ def test_batch_forward_vs_oracle(oracle, ctx):
         assert K.rel_err(d, ref, K.incoherent_floor(cr, g, op)) <= TOL
 
 
+def test_batch_graph_size_does_not_grow_with_members(ctx):
+    """Every stage is one member-indexed launch: the forward graph has the
+    same nodes for 2 and for 5 members (under 20), and the gradient graph
+    adds a fixed set."""
+    mem = _members()
+    op = K.opts(phase=_abi.PHASE_EXACT64, engine=_abi.ENGINE_TC)
+    counts = {}
+    for k in (2, 5):
+        crs, grids = [m[0] for m in mem[:k]], [m[1] for m in mem[:k]]
+        FR.batch_run(crs, grids, op, ctx=ctx)
+        fwd = FR.batch_graph_nodes(ctx)
+        FR.batch_run(crs, grids, op, [np.ones(g.inc) for g in grids], None, ctx=ctx)
+        counts[k] = (fwd, FR.batch_graph_nodes(ctx))
+    assert counts[2] == counts[5]
+    (nf, kf), (ng, kg) = counts[5]
+    assert nf < 20 and kf <= 8
+    assert ng > nf and kg <= kf + 6
+
+
 def test_batch_gradients_and_replay(ctx):
     from diffusecode_gb300.autograd import chi2_grad
     mem = _members()
