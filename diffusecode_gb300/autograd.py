@@ -25,12 +25,15 @@ from .fourier import attach_selections
 from .structures import CrystalData, GridData
 
 
-def chi2_grad(cr: CrystalData, grid: GridData, opts, i_target, weight=None, ctx=None, aver_cells=None):
+def chi2_grad(cr: CrystalData, grid: GridData, opts, i_target, weight=None, ctx=None, aver_cells=None,
+              lot_origins=None):
     """(chi2, grad_pos (N,3), grad_occ (N,), info) through the host C-ABI.
     opts.fave > 0 subtracts <F> (aver_cells: the cells drawn over csize when
-    fave < 1) and differentiates through it."""
+    fave < 1) and differentiates through it; with lots (opts.ilots) the
+    intensity is the lots' normalised sum and an atom's gradient adds its
+    terms over the lots that hold it (lot_origins: lbeg(3,nlots))."""
     ctx = ctx or default_context()
-    keep = attach_selections(opts, aver_cells)
+    keep = attach_selections(opts, aver_cells, lot_origins)
     it = np.asfortranarray(np.asarray(i_target, dtype=np.float64)).reshape(-1, order="F").copy()
     wt = None if weight is None else np.asfortranarray(np.asarray(weight, np.float64)).reshape(-1, order="F").copy()
     chi2 = np.zeros(1)

@@ -93,12 +93,13 @@ extern "C" int dgpu_ctx_destroy(dgpu_ctx *c)
                       &c->adj_items, &c->gq, &c->gpart, &c->grad, &c->batch_desc, &c->batch_aux,
                       &c->ianis, &c->geff, &c->ghist, &c->lpos, &c->ltype, &c->locc, &c->lplan, &c->lfac,
                       &c->wbuf, &c->acc_csf, &c->acc_dsi, &c->slab_ph0, &c->rlist, &c->rsum, &c->tc_tab,
-                      &c->aidx, &c->aaidx, &c->isymb, &c->dtab};
+                      &c->aidx, &c->aaidx, &c->isymb, &c->dtab, &c->lorig};
     for (DevBuf *b : bufs) b->release();
     c->stage.release();
     for (cudaEvent_t e : c->run_ev) cudaEventDestroy(e);
     delete c->fs_main;
     delete c->fs_type;
+    delete c->lot_keep;
     for (int i = 0; i < DGPU_NEV; i++)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -373,6 +374,70 @@ static int lots_sums(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *op,
     return DGPU_OK;
 }
 
+// Adjoint of the lots (fourier_sup.f90:136-277): dsi = ds dnorm sum_L |F_L|^2
+// with F_L the lot's sum (atoms shifted by the lot origin) less <F>, so each
+// lot contributes per-point weights Q_L,g = 2 ds dnorm G conj(F_L) fac_g to
+// the atoms it holds.  The lots are taken chunk by chunk as in the forward
+// pass (gather, type ranges, scatter, type sums of the forward's engine --
+// F_L is recomputed, not stored), then Q of the chunk's (lot, group) types
+// and the per-atom sums, which add into the gradient of each slot's source
+// atom (atomically: an atom sits in several lots).  fsum (box points) gets
+// sum_L F_L for the <F> term.  d_g: dchi2/dI on the full grid.
+int dgpu_lots_adjoint(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid, const dgpu_opts *op,
+                      const BoxSpec &box, int32_t idim, const double *d_g, double *gpos, double *gocc, double2 *fsum)
+{
+    const LotKeep &K = *ctx->lot_keep;
+    const LotPlan &lp = K.lp;
+    const int64_t per_lot = lp.geo.per_lot;
+    const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    const FoldSpec nofold = {0, 1, {1, 1, 1}, {0, 0, 0}, nullptr};
+    const double scale = 2.0 * op->diff_scale * K.dnorm;
+    const double2 *acsf = op->fave > 0.0 ? ctx->acsf.as<double2>() : nullptr;
+    int rc;
+    for (int64_t lot0 = 0; lot0 < lp.nlots; lot0 += lp.per_chunk) {
+        const int32_t nl = (int32_t)(lp.nlots - lot0 < lp.per_chunk ? lp.nlots - lot0 : lp.per_chunk);
+        const int32_t ntype = nl * K.ngroup;
+        const int64_t m = (int64_t)nl * per_lot;
+        if (m == 0) continue;
+        DGPU_CUDA(ctx, ctx->lpos.ensure((size_t)m * 3 * sizeof(double)));
+        DGPU_CUDA(ctx, ctx->ltype.ensure((size_t)m * sizeof(int32_t)));
+        DGPU_CUDA(ctx, ctx->locc.ensure((size_t)m * sizeof(float)));
+        DGPU_CUDA(ctx, ctx->lorig.ensure((size_t)m * sizeof(int32_t)));
+        int64_t got = 0;
+        rc = dgpu_lot_gather(ctx, lp, lot0, nl, cr->pos, K.eiscat, cr->atom_occ, 0, &got, ctx->lorig.as<int32_t>());
+        if (rc) return rc;
+        int64_t ts[2 * 64 + 4];
+        rc = dgpu_prepare_atoms(ctx, ctx->lpos.as<double>(), ctx->ltype.as<int32_t>(),
+                                cr->atom_occ ? ctx->locc.as<float>() : nullptr, m, ntype, K.geo, nofold, ctx->ph0,
+                                ctx->du, ctx->dv, ctx->dw, ctx->w, ts);
+        if (rc) return rc;
+        if (ts[ntype] == 0) continue;
+        PartRef pref;
+        rc = engine_sums(ctx, K.engine, ctx->ph0, ctx->du, ctx->dv, ctx->dw, ctx->w, ts, ntype, op, box, ctx->part,
+                         &pref);
+        if (rc) return rc;
+        DGPU_CUDA(ctx, ctx->gpart.ensure((size_t)ntype * nb * sizeof(float2)));
+        rc = dgpu_lot_adj_q(ctx, K.ngroup, nl, box, idim, pref, ctx->lfac.as<double2>(), acsf, d_g, scale,
+                            ctx->gpart.as<float2>(), fsum);
+        if (rc) return rc;
+        // slot -> source atom
+        rc = dgpu_compose_index(ctx, ctx->aidx.as<int32_t>(), ctx->lorig.as<int32_t>(), ts[ntype]);
+        if (rc) return rc;
+        if (K.engine == DGPU_ENGINE_TC) {
+            rc = dgpu_adjtc_sums(ctx, box, grid, ntype, ts, ctx->ph0.as<uint64_t>(), ctx->du.as<uint64_t>(),
+                                 ctx->dv.as<uint64_t>(), ctx->dw.as<uint64_t>(), ctx->w.as<float>(),
+                                 ctx->aidx.as<int32_t>(), ctx->gpart.as<float2>(), gpos, gocc);
+        } else {
+            rc = dgpu_adj_atom_sums(ctx, box, grid, ntype, ts, ctx->ph0.as<uint64_t>(), ctx->du.as<uint64_t>(),
+                                    ctx->dv.as<uint64_t>(), ctx->dw.as<uint64_t>(), ctx->w.as<float>(),
+                                    ctx->aidx.as<int32_t>(), ctx->gpart.as<float2>(), gpos, gocc, true);
+        }
+        if (rc) return rc;
+        if (cancelled(op)) return dgpu_set_error(ctx, DGPU_ERR_CANCELLED, "cancelled");
+    }
+    return DGPU_OK;
+}
+
 // DISCAMB: the caller's tables into device memory, and a check that every
 // point of the box maps into them (nint is monotonic and h linear over the
 // box, so its corners bound the indices)
@@ -472,6 +537,8 @@ int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g,
     int warn = 0;
     int32_t ncell = 0;
     ctx->aver.on = 0;
+    delete ctx->lot_keep;
+    ctx->lot_keep = nullptr;
     int64_t pairs_aver = 0, pairs = 0, refined = 0;
     float kernel_ms = 0.f;
     int64_t ts[2 * 64 + 4];
@@ -668,6 +735,14 @@ int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g,
             dnorm = (double)((int64_t)cr->icc[0] * cr->icc[1] * cr->icc[2]) / (double)((int64_t)lp.ncell * lp.nlots);
         rc = dgpu_lot_scale(ctx, box, d_csf, d_dsi, dnorm * op->diff_scale, sqrt(op->diff_scale));
         if (rc) return rc;
+        if (!ctx->lot_keep) ctx->lot_keep = new LotKeep();
+        LotKeep &K = *ctx->lot_keep;
+        K.lp = lp;
+        K.ngroup = ngroup;
+        K.engine = engine;
+        K.eiscat = eiscat;
+        K.geo = geo;
+        K.dnorm = dnorm;
     }
     if (!ctx->fs_main) ctx->fs_main = new FormSpec();
     *ctx->fs_main = fsm;

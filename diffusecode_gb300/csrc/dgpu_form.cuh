@@ -120,3 +120,15 @@ __device__ __forceinline__ double2 lattice_closed(const double h[3], int32_t c0,
     sincospi(2.0 * ph, &sp, &cp);
     return cmul(L, make_double2(cp, sp));
 }
+
+// box point of partial-sum layout slot r (PartLayout), false for a padding slot
+__device__ __forceinline__ bool part_point(const PartLayout &L, const BoxSpec &box, int64_t r, int64_t &i,
+                                           int64_t &j, int64_t &l)
+{
+    const int64_t c2 = r / L.m2, rem = r - c2 * L.m2, c1 = L.m1 > 0 ? rem / L.m1 : 0, c0 = rem - c1 * L.m1;
+    if (c0 >= box.f[L.a0] || c1 >= box.f[L.a1] || c2 >= box.f[L.a2]) return false;
+    i = L.a0 == 0 ? c0 : L.a1 == 0 ? c1 : c2;
+    j = L.a0 == 1 ? c0 : L.a1 == 1 ? c1 : c2;
+    l = L.a0 == 2 ? c0 : L.a1 == 2 ? c1 : c2;
+    return true;
+}

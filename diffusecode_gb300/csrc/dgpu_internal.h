@@ -95,6 +95,7 @@ struct TcChoice {
 typedef std::tuple<int32_t, int32_t, int32_t, int32_t, int32_t, int32_t, int32_t> TcKey;
 
 struct BatchState;   // k_batch.cu
+struct LotKeep;      // dgpu_lots.h
 struct FormSpec;
 
 #define DGPU_NEV 10
@@ -122,6 +123,8 @@ struct dgpu_ctx {
     DevBuf lpos, ltype, locc, lplan, lfac;  // lot crystals, lot plan, group factors
     FormSpec *fs_main = nullptr;            // host copy of the last main combine's FormSpec
     FormSpec *fs_type = nullptr;            // host copy of the last per-type FormSpec (<F> combine)
+    LotKeep *lot_keep = nullptr;            // the last four_run's lots, for the gradient (null: no lots)
+    DevBuf lorig;                           // lots: source atom of each gathered slot
     // <F> of the last four_run when it was a box lattice in closed form:
     // A(h) = norm L(h) sum_t c_t(h) S_t(h) over the folded atoms (aph0.., ts)
     struct AverKeep {
@@ -482,6 +485,19 @@ struct AdjMember {
 };
 // g, chi^2 and Q of every member (the per-atom sums follow on the tensor cores)
 int dgpu_adjoint_members(dgpu_ctx *ctx, const AdjMember *d_m, int32_t nc, int64_t max_nb);
+
+// ---- adjoint of the lots (k_adjoint.cu, dgpu_api.cu) --------------------
+int dgpu_lot_adj_q(dgpu_ctx *ctx, int32_t ngroup, int32_t nlot, const BoxSpec &box, int32_t halved,
+                   const PartRef &part, const double2 *fac, const double2 *acsf, const double *g, double scale,
+                   float2 *Q, double2 *fsum);
+// idx[i] = src[idx[i]] (slot -> source atom), -1 kept
+int dgpu_compose_index(dgpu_ctx *ctx, int32_t *idx, const int32_t *src, int64_t n);
+// CUDA-core per-atom sums of ntype types with weights Q ([t][box point])
+int dgpu_adj_atom_sums(dgpu_ctx *ctx, const BoxSpec &box, const dgpu_grid *grid, int32_t ntype, const int64_t *ts,
+                       const uint64_t *ph0, const uint64_t *du, const uint64_t *dv, const uint64_t *dw,
+                       const float *w, const int32_t *aidx, const float2 *Q, double *gpos, double *gocc, bool atomic);
+int dgpu_lots_adjoint(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid, const dgpu_opts *op,
+                      const BoxSpec &box, int32_t idim, const double *d_g, double *gpos, double *gocc, double2 *fsum);
 int dgpu_adjoint_async(dgpu_ctx *ctx, const FormSpec *d_fs, const BoxSpec &box, int32_t friedel_dim,
                        const dgpu_grid *grid, double diff_scale, int32_t nscat, const int64_t *ts,
                        const uint64_t *ph0, const uint64_t *du, const uint64_t *dv, const uint64_t *dw,

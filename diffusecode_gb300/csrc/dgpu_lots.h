@@ -37,7 +37,19 @@ int dgpu_lot_plan(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *op, in
 // slot0 on (the caller sizes the buffers), types L*ngroup + group (0 = empty
 // slot); *nslots = nlot * per_lot.
 int dgpu_lot_gather(dgpu_ctx *ctx, const LotPlan &lp, int64_t lot0, int32_t nlot, const double *pos,
-                    const int32_t *geff, const float *aocc, int64_t slot0, int64_t *nslots);
+                    const int32_t *geff, const float *aocc, int64_t slot0, int64_t *nslots,
+                    int32_t *lorig = nullptr);   // lorig: the source atom of each slot (-1: empty)
+
+// What the chi^2 gradient needs of the last four_run with lots: its plan,
+// groups, phase geometry, engine and the lot normalisation.
+struct LotKeep {
+    LotPlan lp;
+    int32_t ngroup = 0;
+    int32_t engine = 0;
+    const int32_t *eiscat = nullptr;   // device: types, or the (type, ADP) groups
+    PhaseGeom geo;
+    double dnorm = 1.0;
+};
 
 // epilogue of the lots
 int dgpu_group_factors(dgpu_ctx *ctx, const FormSpec &fs, const BoxSpec &box, const int32_t *istl,

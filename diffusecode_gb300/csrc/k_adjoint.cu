@@ -21,9 +21,17 @@
 #include <math.h>
 
 #include "dgpu_form.cuh"
+#include "dgpu_lots.h"
 
 #define ADJ_NT 128
 #define ADJ_TP 256
+
+__device__ __forceinline__ double2 ld_adj(const double2 *p) { return *p; }
+__device__ __forceinline__ double2 ld_adj(const float2 *p)
+{
+    const float2 v = *p;
+    return make_double2((double)v.x, (double)v.y);
+}
 
 // block bx of nbx (256 threads): g over a grid-stride range, this block's chi^2 part
 __device__ __forceinline__ void adj_g_block(const double *__restrict__ dsi, const double *__restrict__ it,
@@ -182,10 +190,13 @@ int dgpu_adjoint_members(dgpu_ctx *ctx, const AdjMember *d_m, int32_t nc, int64_
 // crystal, norm = 1/ncell), so the folded atoms take
 //   Q^A_t(h) = -norm L(h) 2 ds G(h) conj(F(h)) c_t(h)
 // with the per-type factor c_t of the <F> combine.  Layout [t][box point].
+// fbox (lots): F per box point, freshly summed (sum over the lots of F_L,
+// unscaled: sqds then carries ds dnorm), instead of csf.
 __global__ void k_adj_qa(const FormSpec *fs, BoxSpec box, int32_t halved, const double *__restrict__ g,
                          const double2 *__restrict__ csf, const int32_t *__restrict__ istl,
                          const double2 *__restrict__ cfact, double sqds, int32_t l0, int32_t l1, int32_t l2,
-                         double d0, double d1, double d2, double norm, float2 *__restrict__ Q)
+                         double d0, double d1, double d2, double norm, float2 *__restrict__ Q,
+                         const double2 *__restrict__ fbox)
 {
     const int64_t pb = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
@@ -197,8 +208,8 @@ __global__ void k_adj_qa(const FormSpec *fs, BoxSpec box, int32_t halved, const 
     double h[3];
     form_hvec(fs, c[0], c[1], c[2], h);
     const double2 L = lattice_closed(h, l0, l1, l2, d0, d1, d2);
-    double2 f = csf[idx];
-    if (cj) f.y = -f.y;
+    double2 f = fbox ? fbox[pb] : csf[idx];
+    if (cj && !fbox) f.y = -f.y;
     // -norm L 2 sqrt(ds) G conj(F)
     const double sc = skip ? 0.0 : -2.0 * sqds * G * norm;
     const double2 b = make_double2(sc * (L.x * f.x + L.y * f.y), sc * (L.y * f.x - L.x * f.y));
@@ -215,7 +226,9 @@ struct AdjGeom {
     double eck[3], vi[9];
 };
 
-// one thread per prepared atom of one type: sums over all box points
+// one thread per prepared atom of one type: sums over all box points; ATOMIC
+// when several slots of a launch may share a source atom (lots)
+template <bool ATOMIC>
 __global__ void __launch_bounds__(ADJ_NT) k_adj_atoms(const uint64_t *__restrict__ ph0, const uint64_t *__restrict__ du,
                                                       const uint64_t *__restrict__ dv, const uint64_t *__restrict__ dw,
                                                       const float *__restrict__ w, const int32_t *__restrict__ aidx,
@@ -275,13 +288,130 @@ __global__ void __launch_bounds__(ADJ_NT) k_adj_atoms(const uint64_t *__restrict
     // added to: an atom also appears once among the folded atoms of <F>
     // (launched after its main sums, on the same stream)
     const double wj = (double)w[a];
-    if (grad_occ) grad_occ[o] += T0r;
+    if (grad_occ) {
+        if (ATOMIC) atomicAdd(&grad_occ[o], T0r);
+        else grad_occ[o] += T0r;
+    }
     if (grad_pos) {
         const double zpi = 6.283185307179586476925286766559;
-        for (int k = 0; k < 3; k++)
-            grad_pos[3 * (int64_t)o + k] +=
-                -zpi * wj * (g.eck[k] * T0i + g.vi[k] * T1 + g.vi[3 + k] * T2 + g.vi[6 + k] * T3);
+        for (int k = 0; k < 3; k++) {
+            const double v = -zpi * wj * (g.eck[k] * T0i + g.vi[k] * T1 + g.vi[3 + k] * T2 + g.vi[6 + k] * T3);
+            if (ATOMIC) atomicAdd(&grad_pos[3 * (int64_t)o + k], v);
+            else grad_pos[3 * (int64_t)o + k] += v;
+        }
     }
+}
+
+// Lots: Q of the (lot, group) types of a chunk on the box.  F_L = sum_g
+// fac_g S_L,g - <F> (FP64 from the engine's partials, slices first), G by
+// the Friedel rule of adj_point; Q_L,g = scale G conj(F_L) fac_g, layout
+// [L*ngroup + g][box point]; fsum += F_L over the lots (box order).
+template <class P>
+__global__ void k_lot_adj_q(int32_t ngroup, int32_t nlot, BoxSpec box, int32_t halved, const P *__restrict__ part,
+                            int32_t nslice, PartLayout lay, const double2 *__restrict__ fac,
+                            const double2 *__restrict__ acsf, const double *__restrict__ g, double scale,
+                            float2 *__restrict__ Q, double2 *__restrict__ fsum)
+{
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t i, j, l;
+    if (r >= lay.nthr || !part_point(lay, box, r, i, j, l)) return;
+    const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    const int64_t pb = i + (int64_t)box.f[0] * (j + (int64_t)box.f[1] * l);
+    int32_t c[3];
+    int64_t idx;
+    bool skip, cj;
+    const double G = adj_point(box, halved, g, pb, c, idx, skip, cj);
+    double2 a = acsf ? acsf[idx] : make_double2(0.0, 0.0);
+    if (cj) a.y = -a.y;                          // the mirror conjugated the centre in place
+    const int64_t off = i * lay.s0 + j * lay.s1 + l * lay.s2;
+    double2 fs = make_double2(0.0, 0.0);
+    for (int L = 0; L < nlot; L++) {
+        double2 F = make_double2(-a.x, -a.y);
+        for (int q = 0; q < ngroup; q++) {
+            const P *pt = part + (int64_t)(L * ngroup + q) * nslice * lay.slab + off;
+            double2 sl = make_double2(0.0, 0.0);
+            for (int k = 0; k < nslice; k++) {
+                const double2 v = ld_adj(pt + (int64_t)k * lay.slab);
+                sl.x += v.x;
+                sl.y += v.y;
+            }
+            const double2 m = cmul(sl, fac[(int64_t)q * nb + pb]);
+            F.x += m.x;
+            F.y += m.y;
+        }
+        fs.x += F.x;
+        fs.y += F.y;
+        const double sc = skip ? 0.0 : scale * G;
+        for (int q = 0; q < ngroup; q++) {
+            const double2 f = fac[(int64_t)q * nb + pb];
+            // conj(F) f
+            const double qr = sc * (F.x * f.x + F.y * f.y), qi = sc * (F.x * f.y - F.y * f.x);
+            Q[(int64_t)(L * ngroup + q) * nb + pb] = make_float2((float)qr, (float)qi);
+        }
+    }
+    if (fsum) {
+        const double2 o = fsum[pb];
+        fsum[pb] = make_double2(o.x + fs.x, o.y + fs.y);
+    }
+}
+
+int dgpu_lot_adj_q(dgpu_ctx *ctx, int32_t ngroup, int32_t nlot, const BoxSpec &box, int32_t halved,
+                   const PartRef &part, const double2 *fac, const double2 *acsf, const double *g, double scale,
+                   float2 *Q, double2 *fsum)
+{
+    const PartLayout lay = dgpu_part_layout(part, box);
+    const unsigned nblk = (unsigned)dgpu_cdiv(lay.nthr, 256);
+    const int32_t nslice = part.nslice > 0 ? part.nslice : 1;
+    if (part.f32)
+        k_lot_adj_q<float2><<<nblk, 256, 0, ctx->stream>>>(ngroup, nlot, box, halved, (const float2 *)part.p, nslice,
+                                                            lay, fac, acsf, g, scale, Q, fsum);
+    else
+        k_lot_adj_q<double2><<<nblk, 256, 0, ctx->stream>>>(ngroup, nlot, box, halved, (const double2 *)part.p,
+                                                             nslice, lay, fac, acsf, g, scale, Q, fsum);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    return DGPU_OK;
+}
+
+__global__ void k_compose_index(int32_t *__restrict__ idx, const int32_t *__restrict__ src, int64_t n)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int32_t k = idx[i];
+    idx[i] = k >= 0 ? src[k] : -1;
+}
+
+int dgpu_compose_index(dgpu_ctx *ctx, int32_t *idx, const int32_t *src, int64_t n)
+{
+    if (n < 1) return DGPU_OK;
+    k_compose_index<<<(unsigned)dgpu_cdiv(n, 256), 256, 0, ctx->stream>>>(idx, src, n);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    return DGPU_OK;
+}
+
+int dgpu_adj_atom_sums(dgpu_ctx *ctx, const BoxSpec &box, const dgpu_grid *grid, int32_t ntype, const int64_t *ts,
+                       const uint64_t *ph0, const uint64_t *du, const uint64_t *dv, const uint64_t *dw,
+                       const float *w, const int32_t *aidx, const float2 *Q, double *gpos, double *gocc, bool atomic)
+{
+    AdjGeom ag;
+    for (int k = 0; k < 3; k++) {
+        ag.f[k] = box.f[k];
+        ag.eck[k] = grid->eck[k];
+    }
+    ag.pbox = (int64_t)box.f[0] * box.f[1] * box.f[2];
+    memcpy(ag.vi, grid->vi, sizeof(ag.vi));
+    for (int t = 0; t < ntype; t++) {
+        const int64_t lo = ts[t], hi = ts[t + 1];
+        if (hi <= lo) continue;
+        const unsigned nblk = (unsigned)dgpu_cdiv(hi - lo, ADJ_NT);
+        if (atomic)
+            k_adj_atoms<true><<<nblk, ADJ_NT, 0, ctx->stream>>>(ph0, du, dv, dw, w, aidx, lo, hi,
+                                                                 Q + (int64_t)t * ag.pbox, ag, gpos, gocc);
+        else
+            k_adj_atoms<false><<<nblk, ADJ_NT, 0, ctx->stream>>>(ph0, du, dv, dw, w, aidx, lo, hi,
+                                                                  Q + (int64_t)t * ag.pbox, ag, gpos, gocc);
+        DGPU_CUDA(ctx, cudaGetLastError());
+    }
+    return DGPU_OK;
 }
 
 // device: the crystal's per-atom arrays, i_target, weight and the two
@@ -293,8 +423,6 @@ int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
     if (op->ano) return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "gradient with anomalous scattering");
     if (op->phase != DGPU_PHASE_EXACT64)
         return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "gradient needs EXACT64 phases");
-    if (op->ilots == DGPU_LOT_BOX || op->ilots == DGPU_LOT_ELI)
-        return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "gradient with lots");
     const int64_t n = cr->natoms;
     const int64_t np = (int64_t)grid->inc[0] * grid->inc[1] * grid->inc[2];
     // forward pass (host inputs are staged first)
@@ -313,6 +441,8 @@ int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
     const bool fold = op->fave > 0.0 && fwd.ncell > 0;
     if (fold && !ctx->aver.on)
         return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "gradient with <F> of a non-box lattice");
+    // lots: the forward pass kept its plan; the per-lot sums are redone below
+    const bool lots = ctx->lot_keep != nullptr;
     DGPU_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
 
     // adjoint weights g(h) and chi^2
@@ -347,27 +477,42 @@ int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
     FormSpec *d_fst = (FormSpec *)((char *)ctx->stats.p + fso);
     DGPU_CUDA(ctx, cudaMemcpyAsync(d_fs, &fs, sizeof(FormSpec), cudaMemcpyHostToDevice, ctx->stream));
     const int32_t nfold = fold ? ctx->aver.nscat : 0;
-    DGPU_CUDA(ctx, ctx->gpart.ensure((size_t)(ngroup + nfold) * nb * sizeof(float2)));
-    k_adj_q<<<(unsigned)dgpu_cdiv(nb, 256), 256, 0, ctx->stream>>>(
-        d_fs, box, fwd.friedel_dim, d_g, ctx->csf.as<double2>(), ctx->istl.as<int32_t>(), ctx->cfact.as<double2>(),
-        sqrt(op->diff_scale), ctx->gpart.as<float2>());
-    DGPU_CUDA(ctx, cudaGetLastError());
-    float2 *d_qa = ctx->gpart.as<float2>() + (int64_t)ngroup * nb;
-    if (fold) {
-        DGPU_CUDA(ctx, cudaMemcpyAsync(d_fst, ctx->fs_type, sizeof(FormSpec), cudaMemcpyHostToDevice, ctx->stream));
-        const auto &av = ctx->aver;
-        k_adj_qa<<<(unsigned)dgpu_cdiv(nb, 256), 256, 0, ctx->stream>>>(
-            d_fst, box, fwd.friedel_dim, d_g, ctx->csf.as<double2>(), ctx->istl.as<int32_t>(),
-            ctx->cfact.as<double2>(), sqrt(op->diff_scale), av.lat_n[0], av.lat_n[1], av.lat_n[2], av.lat_d[0],
-            av.lat_d[1], av.lat_d[2], av.norm, d_qa);
-        DGPU_CUDA(ctx, cudaGetLastError());
-    }
-
-    // per-atom sums (atoms prepared by the forward pass, grouped by type)
     DGPU_CUDA(ctx, ctx->grad.ensure(n * 4 * sizeof(double)));
     double *d_gpos = ctx->grad.as<double>();
     double *d_gocc = d_gpos + 3 * n;
     DGPU_CUDA(ctx, cudaMemsetAsync(d_gpos, 0, n * 4 * sizeof(double), ctx->stream));
+    // lots: every lot's atoms get their own weights (sum_L F_L kept for <F>)
+    double2 *d_fsum = nullptr;
+    if (lots) {
+        if (fold) {
+            DGPU_CUDA(ctx, ctx->lat.ensure((size_t)nb * sizeof(double2)));
+            d_fsum = ctx->lat.as<double2>();
+            DGPU_CUDA(ctx, cudaMemsetAsync(d_fsum, 0, (size_t)nb * sizeof(double2), ctx->stream));
+        }
+        rc = dgpu_lots_adjoint(ctx, &dc, grid, op, box, fwd.friedel_dim, d_g, d_gpos, d_gocc, d_fsum);
+        if (rc) return rc;
+    }
+    DGPU_CUDA(ctx, ctx->gpart.ensure((size_t)(ngroup + nfold) * nb * sizeof(float2)));
+    if (!lots) {
+        k_adj_q<<<(unsigned)dgpu_cdiv(nb, 256), 256, 0, ctx->stream>>>(
+            d_fs, box, fwd.friedel_dim, d_g, ctx->csf.as<double2>(), ctx->istl.as<int32_t>(),
+            ctx->cfact.as<double2>(), sqrt(op->diff_scale), ctx->gpart.as<float2>());
+        DGPU_CUDA(ctx, cudaGetLastError());
+    }
+    float2 *d_qa = ctx->gpart.as<float2>() + (int64_t)ngroup * nb;
+    if (fold) {
+        DGPU_CUDA(ctx, cudaMemcpyAsync(d_fst, ctx->fs_type, sizeof(FormSpec), cudaMemcpyHostToDevice, ctx->stream));
+        const auto &av = ctx->aver;
+        // with lots: F = sum_L F_L unscaled, so the weight is 2 ds dnorm
+        const double sq = lots ? op->diff_scale * ctx->lot_keep->dnorm : sqrt(op->diff_scale);
+        k_adj_qa<<<(unsigned)dgpu_cdiv(nb, 256), 256, 0, ctx->stream>>>(
+            d_fst, box, fwd.friedel_dim, d_g, ctx->csf.as<double2>(), ctx->istl.as<int32_t>(),
+            ctx->cfact.as<double2>(), sq, av.lat_n[0], av.lat_n[1], av.lat_n[2], av.lat_d[0], av.lat_d[1],
+            av.lat_d[2], av.norm, d_qa, d_fsum);
+        DGPU_CUDA(ctx, cudaGetLastError());
+    }
+
+    // per-atom sums (atoms prepared by the forward pass, grouped by type)
     AdjGeom ag;
     for (int k = 0; k < 3; k++) {
         ag.f[k] = box.f[k];
@@ -386,7 +531,7 @@ int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
         {&ctx->ph0, &ctx->du, &ctx->dv, &ctx->dw, &ctx->w, &ctx->aidx, ctx->ts_main, ngroup, ctx->gpart.as<float2>()},
         {&ctx->aph0, &ctx->adu, &ctx->adv, &ctx->adw, &ctx->aw, &ctx->aaidx, ctx->aver.ts, nfold, d_qa}};
     for (const AtomSet &A : sets) {
-        if (A.n == 0) continue;
+        if (A.n == 0 || (lots && &A == &sets[0])) continue;     // lots: summed per lot above
         if (fwd.engine_used == DGPU_ENGINE_TC) {
             // same sums on the tensor cores, with the forward pass's engine
             rc = dgpu_adjtc_sums(ctx, box, grid, A.n, A.ts, A.ph0->as<uint64_t>(), A.du->as<uint64_t>(),
@@ -397,7 +542,7 @@ int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
             for (int t = 0; t < A.n; t++) {
                 const int64_t lo = A.ts[t], hi = A.ts[t + 1];
                 if (hi <= lo) continue;
-                k_adj_atoms<<<(unsigned)dgpu_cdiv(hi - lo, ADJ_NT), ADJ_NT, 0, ctx->stream>>>(
+                k_adj_atoms<false><<<(unsigned)dgpu_cdiv(hi - lo, ADJ_NT), ADJ_NT, 0, ctx->stream>>>(
                     A.ph0->as<uint64_t>(), A.du->as<uint64_t>(), A.dv->as<uint64_t>(), A.dw->as<uint64_t>(),
                     A.w->as<float>(), A.idx->as<int32_t>(), lo, hi, A.Q + (int64_t)t * nb, ag, d_gpos, d_gocc);
                 DGPU_CUDA(ctx, cudaGetLastError());
@@ -450,7 +595,7 @@ int dgpu_adjoint_async(dgpu_ctx *ctx, const FormSpec *d_fs, const BoxSpec &box, 
     for (int t = 0; t < nscat; t++) {
         const int64_t lo = ts[t], hi = ts[t + 1];
         if (hi <= lo) continue;
-        k_adj_atoms<<<(unsigned)dgpu_cdiv(hi - lo, ADJ_NT), ADJ_NT, 0, ctx->stream>>>(
+        k_adj_atoms<false><<<(unsigned)dgpu_cdiv(hi - lo, ADJ_NT), ADJ_NT, 0, ctx->stream>>>(
             ph0, du, dv, dw, w, aidx, lo, hi, Q + (int64_t)t * nb, ag, gpos, gocc);
     }
     DGPU_CUDA(ctx, cudaGetLastError());

@@ -63,17 +63,6 @@ PartLayout dgpu_part_layout(const PartRef &r, const BoxSpec &box)
     return L;
 }
 
-// box point of layout slot r, false for a padding slot
-__device__ __forceinline__ bool part_point(const PartLayout &L, const BoxSpec &box, int64_t r, int64_t &i,
-                                           int64_t &j, int64_t &l)
-{
-    const int64_t c2 = r / L.m2, rem = r - c2 * L.m2, c1 = L.m1 > 0 ? rem / L.m1 : 0, c0 = rem - c1 * L.m1;
-    if (c0 >= box.f[L.a0] || c1 >= box.f[L.a1] || c2 >= box.f[L.a2]) return false;
-    i = L.a0 == 0 ? c0 : L.a1 == 0 ? c1 : c2;
-    j = L.a0 == 1 ? c0 : L.a1 == 1 ? c1 : c2;
-    l = L.a0 == 2 ? c0 : L.a1 == 2 ? c1 : c2;
-    return true;
-}
 
 template <class P>
 __device__ __forceinline__ void combine_slot(const FormSpec *fs, const BoxSpec &box, const P *__restrict__ part,
@@ -522,8 +511,9 @@ __global__ void k_lot_combine(int32_t ngroup, int32_t nlot, BoxSpec box, const P
 // known at compile time: partial q = g * nslice + k of lot L sits at
 // (L * NQ + q) * slab, and LB lots' partials are loaded before any is used,
 // so that each thread keeps about eight loads in flight (the kernel reads
-// nlot * nq partials per point and is bound by those reads).  For nslice = 1
-// the arithmetic is the generic kernel's, operation for operation.
+// nlot * nq partials per point and is bound by those reads).  The arithmetic
+// is the generic kernel's, operation for operation: a group's slices are
+// added first, then multiplied by its factor.
 template <int NQ>
 __global__ void k_lot_combine_f32(int32_t nslice, int32_t nlot, BoxSpec box, const float2 *__restrict__ part,
                                   PartLayout lay, const double2 *__restrict__ fac, const double2 *__restrict__ acsf,
@@ -556,11 +546,19 @@ __global__ void k_lot_combine_f32(int32_t nslice, int32_t nlot, BoxSpec box, con
 #pragma unroll
         for (int b = 0; b < LB; b++) {
             if (L0 + b < nlot) {
-                float fr = 0.f, fi = 0.f;
+                // the slices of a group added first (in slice order), then the
+                // group product: the generic kernel's arithmetic
+                float fr = 0.f, fi = 0.f, sr = 0.f, si = 0.f;
 #pragma unroll
                 for (int q = 0; q < NQ; q++) {
-                    fr = fmaf(v[b][q].x, fq[q].x, fmaf(-v[b][q].y, fq[q].y, fr));
-                    fi = fmaf(v[b][q].x, fq[q].y, fmaf(v[b][q].y, fq[q].x, fi));
+                    sr += v[b][q].x;
+                    si += v[b][q].y;
+                    if ((q + 1) % nslice == 0) {
+                        fr = fmaf(sr, fq[q].x, fmaf(-si, fq[q].y, fr));
+                        fi = fmaf(sr, fq[q].y, fmaf(si, fq[q].x, fi));
+                        sr = 0.f;
+                        si = 0.f;
+                    }
                 }
                 const double2 F = make_double2((double)fr - a.x, (double)fi - a.y);
                 acc += F.x * F.x + F.y * F.y;

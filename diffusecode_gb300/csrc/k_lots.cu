@@ -283,7 +283,7 @@ __global__ void k_lot_gather(LotGeom g, int64_t lot0, int32_t nlot, const int32_
                              const int32_t *__restrict__ shape, const int32_t *__restrict__ member,
                              const double *__restrict__ pos, const int32_t *__restrict__ geff,
                              const float *__restrict__ aocc, double *__restrict__ lpos, int32_t *__restrict__ ltype,
-                             float *__restrict__ locc)
+                             float *__restrict__ locc, int32_t *__restrict__ lorig)
 {
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= (int64_t)nlot * g.per_lot) return;
@@ -329,15 +329,17 @@ __global__ void k_lot_gather(LotGeom g, int64_t lot0, int32_t nlot, const int32_
         }
         ltype[s] = L * g.ngroup + t;
         locc[s] = aocc ? aocc[src] : 1.0f;
+        if (lorig) lorig[s] = (int32_t)src;
     } else {
         for (int k = 0; k < 3; k++) lpos[3 * s + k] = 0.0;
         ltype[s] = 0;
         locc[s] = 0.0f;
+        if (lorig) lorig[s] = -1;
     }
 }
 
 int dgpu_lot_gather(dgpu_ctx *ctx, const LotPlan &lp, int64_t lot0, int32_t nlot, const double *pos,
-                    const int32_t *geff, const float *aocc, int64_t slot0, int64_t *nslots)
+                    const int32_t *geff, const float *aocc, int64_t slot0, int64_t *nslots, int32_t *lorig)
 {
     const int64_t m = (int64_t)nlot * lp.geo.per_lot;
     *nslots = m;
@@ -347,7 +349,7 @@ int dgpu_lot_gather(dgpu_ctx *ctx, const LotPlan &lp, int64_t lot0, int32_t nlot
         return dgpu_set_error(ctx, DGPU_ERR_ARG, "lot buffers hold fewer than %lld slots", (long long)(slot0 + m));
     k_lot_gather<<<(unsigned)dgpu_cdiv(m, 256), 256, 0, ctx->stream>>>(
         lp.geo, lot0, nlot, lp.d_orig, lp.d_shape, lp.d_member, pos, geff, aocc, ctx->lpos.as<double>() + 3 * slot0,
-        ctx->ltype.as<int32_t>() + slot0, ctx->locc.as<float>() + slot0);
+        ctx->ltype.as<int32_t>() + slot0, ctx->locc.as<float>() + slot0, lorig ? lorig + slot0 : nullptr);
     DGPU_CUDA(ctx, cudaGetLastError());
     return DGPU_OK;
 }

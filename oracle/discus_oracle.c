@@ -549,7 +549,7 @@ static int oc_match(const dgpu_crystal *cr, int64_t i, int t, int a, int y)
  * *ncell receives the cells of the lot. */
 static int64_t oc_getatm_lot(const dgpu_crystal *cr, const dgpu_opts *op, int t, int a, int y,
                              const int32_t lbeg[3], double *xat, float *w, int64_t n,
-                             int32_t *ncell)
+                             int32_t *ncell, int64_t *src)
 {
     int64_t m = 0;
     if (!oc_lots_on(op)) {
@@ -559,6 +559,7 @@ static int64_t oc_getatm_lot(const dgpu_crystal *cr, const dgpu_opts *op, int t,
                 if (xat) {
                     for (int k = 0; k < 3; k++) xat[k * n + m] = cr->pos[3 * i + k];
                     if (w) w[m] = cr->atom_occ ? cr->atom_occ[i] : 1.0f;
+                    if (src) src[m] = i;
                 }
                 m++;
             }
@@ -589,6 +590,7 @@ static int64_t oc_getatm_lot(const dgpu_crystal *cr, const dgpu_opts *op, int t,
                     if (xat) {
                         for (int k = 0; k < 3; k++) xat[k * n + m] = cr->pos[3 * ia + k] - off[k];
                         if (w) w[m] = cr->atom_occ ? cr->atom_occ[ia] : 1.0f;
+                        if (src) src[m] = ia;
                     }
                     m++;
                 }
@@ -601,6 +603,7 @@ static int64_t oc_getatm_lot(const dgpu_crystal *cr, const dgpu_opts *op, int t,
                     if (xat) {
                         for (int k = 0; k < 3; k++) xat[k * n + m] = cr->pos[3 * ir + k] - off[k];
                         if (w) w[m] = cr->atom_occ ? cr->atom_occ[ir] : 1.0f;
+                        if (src) src[m] = ir;
                     }
                     m++;
                 }
@@ -895,9 +898,9 @@ int oc_four_run(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,
             for (int j = 0; j < na; j++) {
                 int a = by_adp ? alist[j] : 0;
                 int y = dc ? dc->isymm[ks + k] : -1;
-                int64_t nx = oc_getatm_lot(cr, op, t, a, y, lbeg, NULL, NULL, 0, &lcell);
+                int64_t nx = oc_getatm_lot(cr, op, t, a, y, lbeg, NULL, NULL, 0, &lcell, NULL);
                 if (nx <= 0) continue;
-                oc_getatm_lot(cr, op, t, a, y, lbeg, xat, w, nx, &lcell);
+                oc_getatm_lot(cr, op, t, a, y, lbeg, xat, w, nx, &lcell, NULL);
                 pairs += nx * np;
                 oc_strucf_mode(g, op, xat, cr->atom_occ ? w : NULL, nx, lmn, off, fnum, cex, nthreads, tcsf);
                 if (dc) {
@@ -953,10 +956,259 @@ done:
  *   A(h) = L(h)/ncell sum_{j selected} cf_t(j)(h) w_j exp(2 pi i h.(r_j - cell_j - dim0)),
  *   L(h) = sum over all icc cells of exp(2 pi i h.(cell + dim0)),
  * and every selected atom gets a second term with Q^A = -L/ncell Q.        */
+/* The same with lots (fourier_sup.f90:136-277): I = ds dnorm sum_L |F_L|^2,
+ * F_L the sum over lot L's atoms at their positions shifted by the lot
+ * origin (oc_getatm_lot) less <F>, dnorm = icc1 icc2 icc3 / (ncell nlots)
+ * when nlots != 1.  <F> (fave > 0) takes the lot's lattice: the cells of the
+ * lot shape at the origin (four_getav).  An atom's gradient adds its terms
+ * over every lot that holds it; a folded atom of <F> gets
+ * Q^A = -L/ncell 2 ds dnorm G conj(sum_L F_L) cf.                          */
+static int oc_chi2_grad_lots(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,
+                             const double *it, const double *wt, double *chi2, double *grad_pos,
+                             double *grad_occ, int nthreads)
+{
+    const double zpi = 6.283185307179586476925286766559;
+    const int32_t *num = g->inc;
+    const int64_t np = (int64_t)num[0] * num[1] * num[2];
+    const int ns = cr->nscat, na = (int)cr->natoms;
+    const int anis = cr->is_anis && op->ldbw;
+    int32_t cs[3];
+    oc_csize(cr, op, cs);
+    int rc = oc_check_lots(cr, op, cs);
+    if (rc) return rc;
+    const int64_t nlots = op->lot_all ? (int64_t)cs[0] * cs[1] * cs[2] : op->nlots;
+    double *cf = (double *)malloc(sizeof(double) * 2 * np * ns);
+    double *H = (double *)malloc(sizeof(double) * 3 * np);
+    double *D = (double *)malloc(sizeof(double) * np * (anis ? cr->nanis : 1));
+    int32_t *istl = (int32_t *)malloc(sizeof(int32_t) * np);
+    double *cfact = (double *)malloc(sizeof(double) * 2 * NTAB * ns);
+    oc_stltab(g->eck, g->vi, num, cr->rten, istl);
+    oc_formtab(cr, op, cfact);
+    for (int64_t p = 0; p < np; p++) {
+        int32_t i = (int32_t)(p % num[0]), j = (int32_t)((p / num[0]) % num[1]), l = (int32_t)(p / ((int64_t)num[0] * num[1]));
+        double h[3], tt[3];
+        oc_hvec(g->eck, g->vi, i, j, l, h);
+        for (int k = 0; k < 3; k++) H[3 * p + k] = h[k];
+        if (anis)
+            for (int a = 1; a <= cr->nanis; a++) D[(int64_t)(a - 1) * np + p] = oc_dbw(cr, a, h);
+        for (int a = 0; a < 3; a++)
+            tt[a] = M3(cr->rten,a,0) * h[0] + M3(cr->rten,a,1) * h[1] + M3(cr->rten,a,2) * h[2];
+        double q2 = (h[0] * tt[0] + h[1] * tt[1] + h[2] * tt[2]) / 4.0;
+        for (int t = 1; t <= ns; t++) {
+            double br, bi;
+            if (op->form == DGPU_FORM_TABLE) {
+                const double *c = cfact + 2 * ((int64_t)(t - 1) * NTAB + istl[p]);
+                br = c[0]; bi = c[1];
+            } else {
+                oc_cfact_at(cr, op, t, q2, &br, &bi);
+            }
+            cf[2 * ((int64_t)(t - 1) * np + p)] = br;
+            cf[2 * ((int64_t)(t - 1) * np + p) + 1] = bi;
+        }
+    }
+    /* the lots' atoms: positions, types, ADP types, weights, sources */
+    int64_t *lstart = (int64_t *)calloc(nlots + 1, sizeof(int64_t));
+    int64_t cap = 0;
+    int32_t lcell = 0;
+    for (int pass = 0; pass < 2; pass++) {
+        int64_t tot = 0;
+        for (int64_t L = 0; L < nlots; L++) {
+            int32_t lbeg[3];
+            if (op->lot_all) {
+                int64_t ii = L;
+                lbeg[2] = (int32_t)(ii / ((int64_t)cs[0] * cs[1])) + 1;
+                ii -= (int64_t)(lbeg[2] - 1) * cs[0] * cs[1];
+                lbeg[1] = (int32_t)(ii / cs[0]) + 1;
+                lbeg[0] = (int32_t)(ii % cs[0]) + 1;
+            } else {
+                for (int k = 0; k < 3; k++) lbeg[k] = op->lot_origins[3 * L + k];
+            }
+            if (pass == 0) lstart[L] = tot;
+            for (int t = 1; t <= ns; t++) {
+                int64_t nx = oc_getatm_lot(cr, op, t, 0, -1, lbeg, NULL, NULL, 0, &lcell, NULL);
+                tot += nx;
+            }
+        }
+        if (pass == 0) { lstart[nlots] = tot; cap = tot; }
+    }
+    double *lx = (double *)malloc(sizeof(double) * 3 * (cap > 0 ? cap : 1));
+    float *lw = (float *)malloc(sizeof(float) * (cap > 0 ? cap : 1));
+    int64_t *lsrc = (int64_t *)malloc(sizeof(int64_t) * (cap > 0 ? cap : 1));
+    int32_t *lt = (int32_t *)malloc(sizeof(int32_t) * (cap > 0 ? cap : 1));
+    {
+        double *xt = (double *)malloc(sizeof(double) * 3 * (na > 0 ? na : 1));
+        float *wt1 = (float *)malloc(sizeof(float) * (na > 0 ? na : 1));
+        int64_t *st1 = (int64_t *)malloc(sizeof(int64_t) * (na > 0 ? na : 1));
+        for (int64_t L = 0; L < nlots; L++) {
+            int32_t lbeg[3];
+            if (op->lot_all) {
+                int64_t ii = L;
+                lbeg[2] = (int32_t)(ii / ((int64_t)cs[0] * cs[1])) + 1;
+                ii -= (int64_t)(lbeg[2] - 1) * cs[0] * cs[1];
+                lbeg[1] = (int32_t)(ii / cs[0]) + 1;
+                lbeg[0] = (int32_t)(ii % cs[0]) + 1;
+            } else {
+                for (int k = 0; k < 3; k++) lbeg[k] = op->lot_origins[3 * L + k];
+            }
+            int64_t m = lstart[L];
+            for (int t = 1; t <= ns; t++) {
+                int64_t nx = oc_getatm_lot(cr, op, t, 0, -1, lbeg, NULL, NULL, 0, &lcell, NULL);
+                oc_getatm_lot(cr, op, t, 0, -1, lbeg, xt, wt1, nx, &lcell, st1);
+                for (int64_t q = 0; q < nx; q++, m++) {
+                    for (int k = 0; k < 3; k++) lx[3 * m + k] = xt[k * nx + q];
+                    lw[m] = cr->atom_occ ? wt1[q] : 1.0f;
+                    lsrc[m] = st1[q];
+                    lt[m] = t;
+                }
+            }
+        }
+        free(xt); free(wt1); free(st1);
+    }
+    /* <F>: the folded atoms of the cells selected over csize, the lot lattice */
+    unsigned char *insel = (unsigned char *)calloc(na > 0 ? na : 1, 1);
+    double *xf = (double *)malloc(sizeof(double) * 3 * (na > 0 ? na : 1));
+    int32_t ncell = 0;
+    if (op->fave > 0.0)
+        for (int32_t kk = 0; kk < cs[2]; kk++)
+            for (int32_t jj = 0; jj < cs[1]; jj++)
+                for (int32_t ii = 0; ii < cs[0]; ii++) {
+                    int64_t sidx = ii + (int64_t)cs[0] * (jj + (int64_t)cs[1] * kk);
+                    if (!(op->fave >= 1.0 || (op->aver_cells && op->aver_cells[sidx] != 0))) continue;
+                    ncell++;
+                    int32_t icell[3] = {ii, jj, kk};
+                    int64_t c = ii + (int64_t)cr->icc[0] * (jj + (int64_t)cr->icc[1] * kk);
+                    for (int32_t is = 0; is < cr->ncatoms; is++) {
+                        int64_t ia = c * cr->ncatoms + is;
+                        if (ia >= na) continue;
+                        insel[ia] = 1;
+                        for (int k = 0; k < 3; k++) xf[3 * ia + k] = cr->pos[3 * ia + k] - (double)icell[k] - cr->dim0[k];
+                    }
+                }
+    const double anorm = ncell > 0 ? 1.0 / ncell : 0.0;
+    double *A = (double *)calloc(2 * np, sizeof(double));
+    double *Lh = (double *)calloc(2 * np, sizeof(double));
+    if (ncell > 0) {
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads > 0 ? nthreads : 1)
+        for (int64_t p = 0; p < np; p++) {
+            double lr = 0, li = 0, ar = 0, ai = 0;
+            for (int32_t kk = 0; kk < op->ls_xyz[2]; kk++)
+                for (int32_t jj = 0; jj < op->ls_xyz[1]; jj++)
+                    for (int32_t ii = 0; ii < op->ls_xyz[0]; ii++) {
+                        if (!oc_in_lot(op, ii, jj, kk)) continue;
+                        double ph = oc_frac_dot(H + 3 * p, ii, jj, kk);
+                        lr += cos(zpi * ph);
+                        li += sin(zpi * ph);
+                    }
+            for (int64_t a = 0; a < na; a++) {
+                int t = cr->iscat[a];
+                if (!insel[a] || t < 1 || t > ns) continue;
+                double ph = oc_frac_dot(H + 3 * p, xf[3 * a], xf[3 * a + 1], xf[3 * a + 2]);
+                double wa = cr->atom_occ ? (double)cr->atom_occ[a] : 1.0;
+                double c = cos(zpi * ph) * wa, sn = sin(zpi * ph) * wa;
+                double br = cf[2 * ((int64_t)(t - 1) * np + p)], bi = cf[2 * ((int64_t)(t - 1) * np + p) + 1];
+                ar += br * c - bi * sn;
+                ai += br * sn + bi * c;
+            }
+            Lh[2 * p] = lr;
+            Lh[2 * p + 1] = li;
+            A[2 * p] = anorm * (lr * ar - li * ai);
+            A[2 * p + 1] = anorm * (lr * ai + li * ar);
+        }
+    }
+    /* F_L at every point */
+    double *F = (double *)malloc(sizeof(double) * 2 * np * (nlots > 0 ? nlots : 1));
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads > 0 ? nthreads : 1)
+    for (int64_t p = 0; p < np; p++)
+        for (int64_t L = 0; L < nlots; L++) {
+            double fr = -A[2 * p], fi = -A[2 * p + 1];
+            for (int64_t m = lstart[L]; m < lstart[L + 1]; m++) {
+                int t = lt[m];
+                double ph = oc_frac_dot(H + 3 * p, lx[3 * m], lx[3 * m + 1], lx[3 * m + 2]);
+                double wa = (double)lw[m];
+                if (anis) wa *= D[(int64_t)(cr->ianis[lsrc[m]] - 1) * np + p];
+                double c = cos(zpi * ph) * wa, sn = sin(zpi * ph) * wa;
+                double br = cf[2 * ((int64_t)(t - 1) * np + p)], bi = cf[2 * ((int64_t)(t - 1) * np + p) + 1];
+                fr += br * c - bi * sn;
+                fi += br * sn + bi * c;
+            }
+            F[2 * (L * np + p)] = fr;
+            F[2 * (L * np + p) + 1] = fi;
+        }
+    const double dnorm = nlots != 1 ? (double)((int64_t)cr->icc[0] * cr->icc[1] * cr->icc[2]) / (double)(lcell * nlots)
+                                     : 1.0;
+    double *G = (double *)malloc(sizeof(double) * np);
+    double x2 = 0;
+    for (int64_t p = 0; p < np; p++) {
+        double s = 0;
+        for (int64_t L = 0; L < nlots; L++) s += F[2 * (L * np + p)] * F[2 * (L * np + p)] + F[2 * (L * np + p) + 1] * F[2 * (L * np + p) + 1];
+        double I = op->diff_scale * dnorm * s;
+        double d = I - it[p];
+        double wp = wt ? wt[p] : 1.0;
+        x2 += wp * d * d;
+        G[p] = 2.0 * wp * d * 2.0 * op->diff_scale * dnorm;    /* 2 ds dnorm dchi2/dI */
+    }
+    if (chi2) *chi2 = x2;
+    if (grad_pos) memset(grad_pos, 0, sizeof(double) * 3 * na);
+    if (grad_occ) memset(grad_occ, 0, sizeof(double) * na);
+    /* per lot atom: T = sum_p G conj(F_L) cf D e^{2 pi i h.x} */
+    for (int64_t L = 0; L < nlots; L++)
+        for (int64_t m = lstart[L]; m < lstart[L + 1]; m++) {
+            int t = lt[m];
+            int64_t a = lsrc[m];
+            double go = 0, gx[3] = {0, 0, 0};
+            for (int64_t p = 0; p < np; p++) {
+                double br = cf[2 * ((int64_t)(t - 1) * np + p)], bi = cf[2 * ((int64_t)(t - 1) * np + p) + 1];
+                if (anis) {
+                    double d = D[(int64_t)(cr->ianis[a] - 1) * np + p];
+                    br *= d;
+                    bi *= d;
+                }
+                double fr = F[2 * (L * np + p)], fi = -F[2 * (L * np + p) + 1];
+                double qr = G[p] * (fr * br - fi * bi), qi = G[p] * (fr * bi + fi * br);
+                double ph = oc_frac_dot(H + 3 * p, lx[3 * m], lx[3 * m + 1], lx[3 * m + 2]);
+                double c = cos(zpi * ph), sn = sin(zpi * ph);
+                double zr = qr * c - qi * sn, zi = qr * sn + qi * c;
+                go += zr;
+                for (int k = 0; k < 3; k++) gx[k] += H[3 * p + k] * zi;
+            }
+            double wa = (double)lw[m];
+            if (grad_occ) grad_occ[a] += go;
+            if (grad_pos) for (int k = 0; k < 3; k++) grad_pos[3 * a + k] += -zpi * wa * gx[k];
+        }
+    /* folded atoms of <F> */
+    if (ncell > 0)
+        for (int64_t a = 0; a < na; a++) {
+            int t = cr->iscat[a];
+            if (!insel[a] || t < 1 || t > ns) continue;
+            double go = 0, gx[3] = {0, 0, 0};
+            for (int64_t p = 0; p < np; p++) {
+                double sr = 0, si = 0;
+                for (int64_t L = 0; L < nlots; L++) { sr += F[2 * (L * np + p)]; si += F[2 * (L * np + p) + 1]; }
+                double br = cf[2 * ((int64_t)(t - 1) * np + p)], bi = cf[2 * ((int64_t)(t - 1) * np + p) + 1];
+                /* Q^A = -anorm L G conj(sum F) cf */
+                double ur = sr * br + si * bi, ui = sr * bi - si * br;          /* conj(sum F) cf */
+                double lr = -anorm * Lh[2 * p], li = -anorm * Lh[2 * p + 1];
+                double qr = G[p] * (lr * ur - li * ui), qi = G[p] * (lr * ui + li * ur);
+                double ph = oc_frac_dot(H + 3 * p, xf[3 * a], xf[3 * a + 1], xf[3 * a + 2]);
+                double c = cos(zpi * ph), sn = sin(zpi * ph);
+                double zr = qr * c - qi * sn, zi = qr * sn + qi * c;
+                go += zr;
+                for (int k = 0; k < 3; k++) gx[k] += H[3 * p + k] * zi;
+            }
+            double wa = cr->atom_occ ? (double)cr->atom_occ[a] : 1.0;
+            if (grad_occ) grad_occ[a] += go;
+            if (grad_pos) for (int k = 0; k < 3; k++) grad_pos[3 * a + k] += -zpi * wa * gx[k];
+        }
+    free(cf); free(H); free(D); free(istl); free(cfact); free(lstart); free(lx); free(lw); free(lsrc); free(lt);
+    free(insel); free(xf); free(A); free(Lh); free(F); free(G);
+    return DGPU_OK;
+}
+
 int oc_chi2_grad(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,
                  const double *it, const double *wt, double *chi2, double *grad_pos,
                  double *grad_occ, int nthreads)
 {
+    if (oc_lots_on(op)) return oc_chi2_grad_lots(cr, g, op, it, wt, chi2, grad_pos, grad_occ, nthreads);
     const double zpi = 6.283185307179586476925286766559;
     const int32_t *num = g->inc;
     int64_t np = (int64_t)num[0] * num[1] * num[2];
@@ -1145,9 +1397,9 @@ double oc_time_ref_rows(const dgpu_crystal *cr, const dgpu_grid *g, int32_t row_
         memset(&whole, 0, sizeof(whole));
         whole.ilots = DGPU_LOT_OFF;
         int32_t nc;
-        int64_t nx = oc_getatm_lot(cr, &whole, t, 0, -1, NULL, NULL, NULL, 0, &nc);
+        int64_t nx = oc_getatm_lot(cr, &whole, t, 0, -1, NULL, NULL, NULL, 0, &nc, NULL);
         if (nx <= 0) continue;
-        oc_getatm_lot(cr, &whole, t, 0, -1, NULL, xat, NULL, nx, &nc);
+        oc_getatm_lot(cr, &whole, t, 0, -1, NULL, xat, NULL, nx, &nc, NULL);
         oc_strucf_ref(xat, NULL, nx, g->vi, g->vi + 3, g->vi + 6, off, lmn, num, fnum, cex,
                       row_lo, row_hi, nthreads, tcsf);
         pairs += nx * (int64_t)(row_hi - row_lo) * num[1] * num[2];

@@ -158,16 +158,22 @@ def four_run(cr, grid, opts, nthreads=0, aver_cells=None, lot_origins=None):
             dsi.reshape(shp, order="F"), info)
 
 
-def chi2_grad(cr, grid, opts, i_target, weight=None, nthreads=0, aver_cells=None):
+def chi2_grad(cr, grid, opts, i_target, weight=None, nthreads=0, aver_cells=None, lot_origins=None):
     """(chi2, grad_pos (N,3), grad_occ (N,)) in FP64; with opts.fave > 0 the
     <F> of the selected cells (aver_cells over csize when fave < 1) is
     subtracted from F as four_run does."""
     if nthreads <= 0:
         nthreads = os.cpu_count() or 1
-    keep = None
+    keep = []
     if aver_cells is not None:
-        keep = np.ascontiguousarray(np.asarray(aver_cells, dtype=np.uint8).reshape(-1, order="F"))
-        opts.aver_cells = keep.ctypes.data_as(C.POINTER(C.c_uint8))
+        a = np.ascontiguousarray(np.asarray(aver_cells, dtype=np.uint8).reshape(-1, order="F"))
+        opts.aver_cells = a.ctypes.data_as(C.POINTER(C.c_uint8))
+        keep.append(a)
+    if lot_origins is not None:
+        o = np.ascontiguousarray(np.asarray(lot_origins, dtype=np.int32).reshape(-1, 3))
+        opts.lot_origins = _i(o)
+        opts.nlots = o.shape[0]
+        keep.append(o)
     c = cr.to_c()
     g = grid.to_c()
     it = np.asfortranarray(i_target, dtype=np.float64).reshape(-1, order="F").copy()

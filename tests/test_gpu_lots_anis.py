@@ -142,3 +142,23 @@ def test_batch_rejects_lots_and_adps(ctx):
     with pytest.raises(Exception) as e:
         FR.batch_run([cr], [g], K.opts(phase=_abi.PHASE_EXACT64), ctx=ctx)
     assert getattr(e.value, "code", None) == _abi.DGPU_ERR_UNSUPPORTED
+
+
+def test_lots_tc_several_slices(oracle, ctx):
+    """Lots on the tensor-core engine with several K slices per (lot, group)
+    pair (tc_kslice = 64 atoms; 2 groups x 3 slices = 6 partials per lot,
+    the lot combine specialised for up to 8): its slices of a group are added
+    before the group product, as the generic combine does; against the
+    oracle and the CUDA-core engine."""
+    cr, g = S.small_lots_anis(anis=False, icc=(10, 8, 6), inc=(9, 9, 5))
+    origins = [(1, 1, 1), (4, 3, 2), (9, 7, 5)]
+    op = K.opts(phase=_abi.PHASE_EXACT64, engine=_abi.ENGINE_TC, ilots=_abi.LOT_BOX, ls_xyz=(8, 6, 4), nlots=3,
+                tc_kslice=64)
+    rc, csf, acsf, dsi, info = oracle.four_run(cr, g, op, lot_origins=origins)
+    r = FR.four_run(cr, g, op, ctx=ctx, lot_origins=origins)
+    assert rc == 0 and r.status == 0 and r.info.engine_used == _abi.ENGINE_TC
+    floor = K.incoherent_floor(cr, g, K.opts(ldbw=0))
+    assert K.rel_err(r.dsi, dsi, floor) <= TOL
+    d = FR.four_run(cr, g, K.opts(phase=_abi.PHASE_EXACT64, engine=_abi.ENGINE_DIRECT, ilots=_abi.LOT_BOX,
+                                  ls_xyz=(8, 6, 4), nlots=3), ctx=ctx, lot_origins=origins)
+    assert K.rel_err(r.dsi, d.dsi, floor) <= TOL

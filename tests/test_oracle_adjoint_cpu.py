@@ -74,3 +74,53 @@ def test_average_term_changes_the_gradient():
     _, gp1, _ = _chi2(cr, g, 1.0, it, wt, None)
     _, gp0, _ = _chi2(cr, g, 0.0, it, wt, None)
     assert np.abs(gp1 - gp0).max() > 0.1 * np.abs(gp1).max()
+
+
+LOT_CASES = {
+    "box": dict(anis=False, opts=dict(ilots=_abi.LOT_BOX, ls_xyz=(3, 2, 2), nlots=3), origins=[(1, 1, 1), (4, 3, 2), (5, 4, 3)]),
+    "box-aver-anis": dict(anis=True, opts=dict(ilots=_abi.LOT_BOX, ls_xyz=(3, 2, 2), nlots=3, fave=1.0),
+                          origins=[(1, 1, 1), (4, 3, 2), (5, 4, 3)]),
+    "eli-all": dict(anis=False, opts=dict(ilots=_abi.LOT_ELI, ls_xyz=(3, 3, 2), lot_all=1, lperiod=0)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(LOT_CASES))
+def test_lots_gradient_matches_forward_and_differences(name):
+    """With lots: the oracle's chi^2 equals that of its own four_run with the
+    same lots, and its gradient equals central differences (atoms in several
+    lots, wrapped lots, interstitial atoms, <F> of the lot lattice)."""
+    case = LOT_CASES[name]
+    cr, g = S.small_lots_anis(anis=case["anis"], icc=(5, 4, 3), inc=(7, 7, 3))
+    origins = case.get("origins")
+
+    def opts():
+        return _abi.default_opts(ldbw=1, phase=_abi.PHASE_EXACT64, **case["opts"])
+
+    def with_origins(op):
+        keep = None
+        if origins is not None:
+            keep = np.ascontiguousarray(np.asarray(origins, np.int32).reshape(-1, 3))
+            op.lot_origins = _abi.iptr(keep)
+        return op, keep
+
+    tgt = cr.with_positions(cr.pos + np.random.default_rng(2).normal(0, 0.01, cr.pos.shape))
+    rc, _, _, it, info = O.four_run(tgt, g, opts(), lot_origins=origins)
+    assert rc == 0
+    wt = 1.0 / (it + 1.0)
+    op, keep = with_origins(opts())
+    c2, gp, go = O.chi2_grad(cr, g, op, it, wt)
+    rc, _, _, dsi, _ = O.four_run(cr, g, opts(), lot_origins=origins)
+    assert abs(c2 - np.sum(wt * (dsi - it) ** 2)) <= 1e-11 * c2
+    eps = 1e-6
+    for a in [0, 7, cr.natoms - 2]:
+        if cr.iscat[a] == 0:
+            continue
+        for k in range(3):
+            vals = []
+            for sgn in (1, -1):
+                c = copy.deepcopy(cr)
+                c.pos[a, k] += sgn * eps
+                op, keep = with_origins(opts())
+                vals.append(O.chi2_grad(c, g, op, it, wt)[0])
+            fd = (vals[0] - vals[1]) / (2 * eps)
+            assert abs(fd - gp[a, k]) <= 1e-7 * np.abs(gp).max()
