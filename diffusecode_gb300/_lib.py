@@ -18,7 +18,7 @@ EXPORTS = [
     "dgpu_four_run", "dgpu_four_run_device", "dgpu_four_strucf", "dgpu_fourier_lmn",
     "dgpu_four_stltab", "dgpu_four_formtab", "dgpu_four_increments", "dgpu_chi2_grad",
     "dgpu_batch_run", "dgpu_batch_last_ms", "dgpu_batch_graph_nodes", "dgpu_four_strucf_noalloc", "dgpu_tc_last_kernel_ms",
-    "dgpu_four_weight", "dgpu_four_weight_device", "dgpu_four_accumulate", "dgpu_qval",
+    "dgpu_four_weight", "dgpu_four_weight_device", "dgpu_four_accumulate", "dgpu_set_symmetry", "dgpu_qval",
     "dgpu_calc_hkl", "dgpu_powder_npkt", "dgpu_powder_complete", "dgpu_chi2_grad_device",
 ]
 
@@ -68,6 +68,7 @@ def load():
     L.dgpu_four_weight.argtypes = [vp, CR, GR, OP, dp, dp]
     L.dgpu_four_weight_device.argtypes = [vp, CR, GR, OP, vp, vp]
     L.dgpu_four_accumulate.argtypes = [vp, C.c_int32, C.c_int32, GR, C.c_double, dp, dp]
+    L.dgpu_set_symmetry.argtypes = [vp, C.c_int32, dp]
     L.dgpu_qval.argtypes = [vp, CR, GR, OP, C.c_int32, C.c_int32, dp, dp, dp, dp, dp]
     L.dgpu_calc_hkl.argtypes = [vp, CR, OP, ip, C.c_int64, C.c_double, C.c_double, C.c_double, dp, dp, dp]
     PW = C.POINTER(_abi.Powder)

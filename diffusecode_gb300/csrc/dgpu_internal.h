@@ -139,6 +139,7 @@ struct dgpu_ctx {
     DevBuf rlist, rsum;                     // refinement of <F>-cancelling points: list, exact sums
     DevBuf slab_ph0;                        // powder: per-slab origin phases of the atoms
     int64_t acc_np = 0;                     // points of the accumulated sums (0: none)
+    std::vector<int32_t> symm_inv;          // inverses of the point-group operations (four_symm), 9 each
     DevBuf gq, gpart, grad, batch_desc, batch_aux;
     double batch_ms = 0.0;
     double tc_kernel_ms = 0.0;              // duration of the last single-problem tensor-core launch
@@ -428,7 +429,8 @@ struct PrepMember {
     const int32_t *iscat;
     const float *aocc;
     int64_t n, nblk;       // atoms, prepare blocks
-    int32_t nscat, num[3];
+    int32_t nscat, num[3]; // nscat: partial-sum groups
+    int32_t ncf, ldbw_cf;  // scattering types and isotropic Debye-Waller term of cfact
     PhaseGeom g;
     int32_t *counts;
     int64_t *offs, *ts;

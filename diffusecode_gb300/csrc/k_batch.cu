@@ -25,7 +25,10 @@ namespace {
 
 struct Member {
     int64_t natoms, abase, pbase;
-    int32_t nscat, idim;
+    int32_t nscat, idim;   // nscat: partial-sum groups (types, or (type, ADP type) pairs)
+    int32_t ntype;         // scattering types (cfact)
+    int32_t nanis = 0;     // > 0: anisotropic member, gmap numbers its (type, ADP type) pairs
+    std::vector<int32_t> gmap;
     int64_t ts[2 * 64 + 4];
     int64_t np, nb, nblk;
     BoxSpec box;
@@ -151,6 +154,41 @@ static int batch_enqueue(dgpu_ctx *ctx, BatchState &B, const dgpu_opts *op)
     return DGPU_OK;
 }
 
+// (type, ADP type) groups of an anisotropic member (four_nanis,
+// fourier_sup.f90:4294-4326): the pairs present, numbered by type, then ADP
+// type, as the single-crystal path numbers them; gmap[t*(nanis+1)+a] = group.
+// Returns the group count, or -1 for an ADP type outside 1..nanis.
+static int32_t member_groups(const dgpu_crystal &cr, std::vector<int32_t> &gmap)
+{
+    const int32_t na = cr.nanis;
+    gmap.assign((size_t)(cr.nscat + 1) * (na + 1), 0);
+    for (int64_t i = 0; i < cr.natoms; i++) {
+        const int32_t t = cr.iscat[i];
+        if (t < 1 || t > cr.nscat) continue;
+        const int32_t a = cr.ianis[i];
+        if (a < 1 || a > na) return -1;
+        gmap[(size_t)t * (na + 1) + a] = 1;
+    }
+    int32_t g = 0;
+    for (int32_t t = 1; t <= cr.nscat; t++)
+        for (int32_t a = 1; a <= na; a++) {
+            int32_t &e = gmap[(size_t)t * (na + 1) + a];
+            if (e) e = ++g;
+        }
+    return g;
+}
+
+// the group of every atom of an anisotropic member (0: VOID)
+static void member_group_ids(const dgpu_crystal &cr, const std::vector<int32_t> &gmap, int32_t *out)
+{
+    const int32_t na = cr.nanis;
+    for (int64_t i = 0; i < cr.natoms; i++) {
+        const int32_t t = cr.iscat[i];
+        const int32_t a = (t >= 1 && t <= cr.nscat) ? cr.ianis[i] : 0;
+        out[i] = (t >= 1 && t <= cr.nscat && a >= 1 && a <= na) ? gmap[(size_t)t * (na + 1) + a] : 0;
+    }
+}
+
 // Member descriptors of the folded launches (fixed per batch shape: the
 // buffers they point into belong to the batch state).
 static int batch_members(dgpu_ctx *ctx, BatchState &B, int32_t nc, const dgpu_opts *op)
@@ -172,6 +210,8 @@ static int batch_members(dgpu_ctx *ctx, BatchState &B, int32_t nc, const dgpu_op
         p.n = m.natoms;
         p.nblk = m.nblk;
         p.nscat = m.nscat;
+        p.ncf = m.ntype;
+        p.ldbw_cf = (op->ldbw && m.nanis == 0) ? 1 : 0;
         for (int k = 0; k < 3; k++) p.num[k] = m.grid.inc[k];
         p.g = m.geo;
         p.counts = B.d_cnt.as<int32_t>() + m.cnt_off;
@@ -190,7 +230,7 @@ static int batch_members(dgpu_ctx *ctx, BatchState &B, int32_t nc, const dgpu_op
         B.max_nblk = std::max(B.max_nblk, m.nblk);
         B.max_np = std::max(B.max_np, m.np);
         B.max_nb = std::max(B.max_nb, m.nb);
-        B.max_nscat = std::max(B.max_nscat, m.nscat);
+        B.max_nscat = std::max(B.max_nscat, m.ntype);
 
         EpiMember &e = em[c];
         memset(&e, 0, sizeof(e));
@@ -261,13 +301,27 @@ static int batch_build(dgpu_ctx *ctx, BatchState &B, int32_t nc, const dgpu_crys
         Member &m = B.mem[c];
         const dgpu_crystal &cr = crs[c];
         m.natoms = cr.natoms;
+        m.ntype = cr.nscat;
         m.nscat = cr.nscat;
+        if (cr.is_anis) {
+            m.nanis = cr.nanis;
+            m.nscat = member_groups(cr, m.gmap);
+            if (m.nscat < 0)
+                return dgpu_set_error(ctx, DGPU_ERR_ARG, "member %d: ADP type outside 1..%d", c, cr.nanis);
+            if (m.nscat > 63)
+                return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "member %d: more than 63 (type, ADP type) groups", c);
+            if (m.nscat == 0) m.nscat = 1;
+            std::vector<int32_t> gid((size_t)cr.natoms);
+            member_group_ids(cr, m.gmap, gid.data());
+            dgpu_type_ranges(gid.data(), cr.natoms, m.nscat, m.ts);
+        } else {
+            dgpu_type_ranges(cr.iscat, cr.natoms, cr.nscat, m.ts);
+        }
         m.abase = abase;
         m.pbase = pbase;
         m.grid = grids[c];
         m.ds = op->diff_scale;
         memcpy(m.rten, cr.rten, sizeof(m.rten));
-        dgpu_type_ranges(cr.iscat, cr.natoms, cr.nscat, m.ts);
         int32_t fnum[3];
         m.idim = dgpu_friedel_test(&grids[c], op, fnum);
         for (int k = 0; k < 3; k++) {
@@ -292,14 +346,14 @@ static int batch_build(dgpu_ctx *ctx, BatchState &B, int32_t nc, const dgpu_crys
         m.tsd_off = tsd;
         m.chi_off = (int64_t)c * 520;
         abase += cr.natoms;
-        pbase += m.ts[cr.nscat] > 0 ? m.ts[cr.nscat] : 0;
+        pbase += m.ts[m.nscat] > 0 ? m.ts[m.nscat] : 0;
         pbase = (pbase + 31) / 32 * 32;
         np_tot += m.np;
         istl += m.np;
-        cf += (int64_t)cr.nscat * DGPU_NTAB;
-        q += (int64_t)cr.nscat * m.nb;
-        cnt += m.nblk * cr.nscat;
-        tsd += 2 * cr.nscat + 1;
+        cf += (int64_t)m.ntype * DGPU_NTAB;
+        q += (int64_t)m.nscat * m.nb;
+        cnt += m.nblk * m.nscat;
+        tsd += 2 * m.nscat + 1;
     }
     B.tot_atoms = abase;
     B.tot_pad = pbase > 0 ? pbase : 32;
@@ -349,6 +403,22 @@ static int batch_build(dgpu_ctx *ctx, BatchState &B, int32_t nc, const dgpu_crys
     for (int c = 0; c < nc; c++) {
         dgpu_formcoef_fill(&crs[c], coef.data() + c * cb);
         dgpu_fill_formspec(ctx, &crs[c], op, &grids[c], fs[c]);
+        const Member &m = B.mem[c];
+        if (m.nanis > 0) {             // (type, ADP type) groups: four_dbw on top of a DW-free cfact
+            FormSpec &f = fs[c];
+            f.ngroup = m.nscat;
+            for (int32_t t = 1; t <= crs[c].nscat; t++)
+                for (int32_t a = 1; a <= m.nanis; a++) {
+                    const int32_t g = m.gmap[(size_t)t * (m.nanis + 1) + a];
+                    if (!g) continue;
+                    f.gtype[g] = t;
+                    for (int k = 0; k < 6; k++) f.gU[6 * g + k] = crs[c].anis_full[6 * (int64_t)(a - 1) + k];
+                }
+            if (f.ngroup == 1 && !m.gmap.empty() && f.gtype[1] == 0) f.gtype[1] = 1;
+            f.adbw = op->ldbw ? 1 : 0;
+            f.ldbw = 0;
+            for (int k = 0; k < 3; k++) f.ar[k] = crs[c].ar[k];
+        }
     }
     DGPU_CUDA(ctx, cudaMemcpyAsync(B.d_coef.p, coef.data(), coef.size(), cudaMemcpyHostToDevice, ctx->stream));
     DGPU_CUDA(ctx, cudaMemcpyAsync(B.d_fs.p, fs.data(), fs.size() * sizeof(FormSpec), cudaMemcpyHostToDevice,
@@ -427,8 +497,8 @@ extern "C" int dgpu_batch_run(dgpu_ctx *ctx, int32_t nc, const dgpu_crystal *crs
     for (int c = 0; c < nc; c++) {
         if (crs[c].natoms < 1 || !crs[c].pos || !crs[c].iscat || crs[c].nscat < 1 || crs[c].nscat > 63)
             return dgpu_set_error(ctx, DGPU_ERR_ARG, "batch member %d: bad crystal", c);
-        if (crs[c].is_anis)
-            return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "batch member %d: anisotropic ADPs are run by dgpu_four_run", c);
+        if (crs[c].is_anis && (crs[c].nanis < 1 || !crs[c].ianis || !crs[c].anis_full))
+            return dgpu_set_error(ctx, DGPU_ERR_ARG, "member %d: anisotropic without nanis/ianis/anis_full", c);
         if (!dsi[c] || (targets && !i_target[c])) return dgpu_set_error(ctx, DGPU_ERR_ARG, "member %d: buffers", c);
         for (int k = 0; k < 3; k++)
             if (grids[c].inc[k] < 1) return dgpu_set_error(ctx, DGPU_ERR_ARG, "member %d: inc", c);
@@ -447,8 +517,22 @@ extern "C" int dgpu_batch_run(dgpu_ctx *ctx, int32_t nc, const dgpu_crystal *crs
         sig.push_back(crs[c].nscat);
         sig.push_back(crs[c].atom_occ != nullptr);
         int64_t ts[2 * 64 + 4];
-        dgpu_type_ranges(crs[c].iscat, crs[c].natoms, crs[c].nscat, ts);
-        for (int t = 0; t <= crs[c].nscat; t++) sig.push_back(ts[t]);
+        sig.push_back(crs[c].is_anis ? crs[c].nanis : 0);
+        if (crs[c].is_anis) {
+            // the groups present and their sizes, and the ADP tensors
+            std::vector<int32_t> gmap, gid((size_t)crs[c].natoms);
+            const int32_t ng = member_groups(crs[c], gmap);
+            if (ng < 0) return dgpu_set_error(ctx, DGPU_ERR_ARG, "member %d: ADP type outside 1..%d", c, crs[c].nanis);
+            for (int32_t v : gmap) sig.push_back(v);
+            member_group_ids(crs[c], gmap, gid.data());
+            dgpu_type_ranges(gid.data(), crs[c].natoms, ng > 0 ? ng : 1, ts);
+            for (int t = 0; t <= (ng > 0 ? ng : 1); t++) sig.push_back(ts[t]);
+            for (int k = 0; k < 6 * crs[c].nanis; k++) sig.push_back((int64_t)(crs[c].anis_full[k] * 1e15));
+            for (int k = 0; k < 3; k++) sig.push_back((int64_t)(crs[c].ar[k] * 1e15));
+        } else {
+            dgpu_type_ranges(crs[c].iscat, crs[c].natoms, crs[c].nscat, ts);
+            for (int t = 0; t <= crs[c].nscat; t++) sig.push_back(ts[t]);
+        }
         for (int k = 0; k < 12; k++) sig.push_back((int64_t)(grids[c].eck[k] * 1e9));
         for (int k = 0; k < 9; k++) sig.push_back((int64_t)(grids[c].vi[k] * 1e12));
         for (int k = 0; k < 3; k++) sig.push_back(grids[c].inc[k]);
@@ -479,7 +563,8 @@ extern "C" int dgpu_batch_run(dgpu_ctx *ctx, int32_t nc, const dgpu_crystal *crs
     for (int c = 0; c < nc; c++) {
         const Member &m = B.mem[c];
         memcpy((double *)B.h_pos.p + 3 * m.abase, crs[c].pos, m.natoms * 3 * sizeof(double));
-        memcpy((int32_t *)B.h_isc.p + m.abase, crs[c].iscat, m.natoms * sizeof(int32_t));
+        if (m.nanis > 0) member_group_ids(crs[c], m.gmap, (int32_t *)B.h_isc.p + m.abase);
+        else memcpy((int32_t *)B.h_isc.p + m.abase, crs[c].iscat, m.natoms * sizeof(int32_t));
         if (B.has_occ) {
             float *o = (float *)B.h_aocc.p + m.abase;
             if (crs[c].atom_occ) memcpy(o, crs[c].atom_occ, m.natoms * sizeof(float));

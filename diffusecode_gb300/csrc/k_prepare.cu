@@ -599,11 +599,10 @@ __global__ void k_stltab_m(const PrepMember *__restrict__ M, int32_t *flag)
                  (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-__global__ void k_formtab_m(const PrepMember *__restrict__ M, int32_t lxray, int32_t power, int32_t ano,
-                            int32_t ldbw)
+__global__ void k_formtab_m(const PrepMember *__restrict__ M, int32_t lxray, int32_t power, int32_t ano)
 {
     const PrepMember &m = M[blockIdx.y];
-    formtab_entry((const FormCoef *)m.coef, m.nscat, lxray, power, ano, ldbw, m.cfact,
+    formtab_entry((const FormCoef *)m.coef, m.ncf, lxray, power, ano, m.ldbw_cf, m.cfact,
                   (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -626,7 +625,7 @@ int dgpu_tables_members(dgpu_ctx *ctx, const PrepMember *d_m, int32_t nc, int64_
     if (nc > 65535) return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "more than 65535 batch members");
     k_stltab_m<<<dim3((unsigned)dgpu_cdiv(max_np, 256), (unsigned)nc), 256, 0, ctx->stream>>>(d_m, flag);
     k_formtab_m<<<dim3((unsigned)dgpu_cdiv((int64_t)max_nscat * DGPU_NTAB, 256), (unsigned)nc), 256, 0,
-                  ctx->stream>>>(d_m, op->lxray, op->power, op->ano, op->ldbw);
+                  ctx->stream>>>(d_m, op->lxray, op->power, op->ano);
     DGPU_CUDA(ctx, cudaGetLastError());
     return DGPU_OK;
 }

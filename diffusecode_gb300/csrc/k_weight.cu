@@ -229,6 +229,139 @@ static void fill_bragg(const dgpu_grid *g, T *a)
             }
 }
 
+// ---------------------------------------------------------------------------
+// four_symm_csf / four_symm_dsi (fourier_sup.f90:4048-4290): the average over
+// the point-group operations 2..nops of the pixels a pixel is mapped to.  The
+// reference scatters: for operation i, pixel h goes to izero + NINT((h -
+// izero) S_i) (a row vector times the operation), adding its value and a
+// weight there; then every pixel is divided by its weight and by nops.  The
+// operations are integer matrices of determinant +-1, so each maps pixels one
+// to one and a pixel receives at most one value per operation: here each
+// pixel gathers them through the inverse matrix, in operation order -- the
+// order in which the reference's sums reach that pixel.
+
+struct SymmGrid {
+    int32_t num[3], izero[3];
+    int32_t nops;
+};
+
+__device__ __forceinline__ void sy_add(double &a, double b) { a += b; }
+__device__ __forceinline__ void sy_add(double2 &a, double2 b)
+{
+    a.x += b.x;
+    a.y += b.y;
+}
+// (a / w) / n, the reference's order
+__device__ __forceinline__ double sy_div(double a, double w, double n) { return a / w / n; }
+__device__ __forceinline__ double2 sy_div(double2 a, double w, double n) { return make_double2(a.x / w / n, a.y / w / n); }
+
+template <class T>
+__global__ void k_symm_avg(SymmGrid g, const int32_t *__restrict__ inv, const T *__restrict__ in, T *__restrict__ out)
+{
+    const int64_t np = (int64_t)g.num[0] * g.num[1] * g.num[2];
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    const int32_t t[3] = {(int32_t)(p % g.num[0]), (int32_t)((p / g.num[0]) % g.num[1]),
+                          (int32_t)(p / ((int64_t)g.num[0] * g.num[1]))};
+    const int32_t o[3] = {t[0] + 1 - g.izero[0], t[1] + 1 - g.izero[1], t[2] + 1 - g.izero[2]};
+    T sum = in[p];
+    int32_t w = 1;
+    for (int i = 1; i < g.nops; i++) {
+        const int32_t *m = inv + 9 * i;            // column-major: (r, c) at r + 3c
+        int32_t src[3];
+        bool ok = true;
+        for (int c = 0; c < 3; c++) {
+            src[c] = g.izero[c] - 1 + o[0] * m[0 + 3 * c] + o[1] * m[1 + 3 * c] + o[2] * m[2 + 3 * c];
+            ok = ok && src[c] >= 0 && src[c] < g.num[c];
+        }
+        if (!ok) continue;
+        sy_add(sum, in[src[0] + (int64_t)g.num[0] * (src[1] + (int64_t)g.num[1] * src[2])]);
+        w++;
+    }
+    out[p] = sy_div(sum, (double)w, (double)g.nops);
+}
+
+// pixel of hkl = 0 (fourier_sup.f90:4077-4100): the columns of vi (unit
+// vectors along single-point axes), inverted, applied to -eck(:,1)
+static void symm_izero(const dgpu_grid *grid, int32_t izero[3])
+{
+    double a[9];
+    for (int c = 0; c < 3; c++)
+        for (int r = 0; r < 3; r++) a[r + 3 * c] = grid->inc[c] > 1 ? grid->vi[r + 3 * c] : (r == c ? 1.0 : 0.0);
+    const double det = a[0] * (a[4] * a[8] - a[7] * a[5]) - a[3] * (a[1] * a[8] - a[7] * a[2]) +
+                       a[6] * (a[1] * a[5] - a[4] * a[2]);
+    double inv[9];
+    inv[0] = (a[4] * a[8] - a[7] * a[5]) / det;
+    inv[3] = (a[6] * a[5] - a[3] * a[8]) / det;
+    inv[6] = (a[3] * a[7] - a[6] * a[4]) / det;
+    inv[1] = (a[7] * a[2] - a[1] * a[8]) / det;
+    inv[4] = (a[0] * a[8] - a[6] * a[2]) / det;
+    inv[7] = (a[6] * a[1] - a[0] * a[7]) / det;
+    inv[2] = (a[1] * a[5] - a[4] * a[2]) / det;
+    inv[5] = (a[3] * a[2] - a[0] * a[5]) / det;
+    inv[8] = (a[0] * a[4] - a[3] * a[1]) / det;
+    for (int r = 0; r < 3; r++) {
+        const double u = -(inv[r] * grid->eck[0] + inv[r + 3] * grid->eck[1] + inv[r + 6] * grid->eck[2]);
+        izero[r] = grid->inc[r] > 1 ? (int32_t)llround(1.0 + u) : 1;
+    }
+}
+
+extern "C" int dgpu_set_symmetry(dgpu_ctx *ctx, int32_t nops, const double *mats)
+{
+    if (!ctx) return DGPU_ERR_ARG;
+    if (nops < 0 || nops > 192 || (nops > 0 && !mats)) return dgpu_set_error(ctx, DGPU_ERR_ARG, "nops=%d", nops);
+    std::vector<int32_t> inv((size_t)9 * (nops > 0 ? nops : 1), 0);
+    for (int i = 0; i < nops; i++) {
+        // the integer matrix and its inverse (adjugate / determinant, determinant +-1)
+        int32_t m[9];
+        for (int k = 0; k < 9; k++) {
+            const double v = mats[9 * i + k];
+            m[k] = (int32_t)llround(v);
+            if (fabs(v - m[k]) > 1e-6)
+                return dgpu_set_error(ctx, DGPU_ERR_ARG, "symmetry operation %d is not an integer matrix", i + 1);
+        }
+        const int32_t det = m[0] * (m[4] * m[8] - m[7] * m[5]) - m[3] * (m[1] * m[8] - m[7] * m[2]) +
+                            m[6] * (m[1] * m[5] - m[4] * m[2]);
+        if (det != 1 && det != -1)
+            return dgpu_set_error(ctx, DGPU_ERR_ARG, "symmetry operation %d has determinant %d", i + 1, det);
+        int32_t *q = inv.data() + 9 * i;
+        q[0] = (m[4] * m[8] - m[7] * m[5]) * det;
+        q[3] = (m[6] * m[5] - m[3] * m[8]) * det;
+        q[6] = (m[3] * m[7] - m[6] * m[4]) * det;
+        q[1] = (m[7] * m[2] - m[1] * m[8]) * det;
+        q[4] = (m[0] * m[8] - m[6] * m[2]) * det;
+        q[7] = (m[6] * m[1] - m[0] * m[7]) * det;
+        q[2] = (m[1] * m[5] - m[4] * m[2]) * det;
+        q[5] = (m[3] * m[2] - m[0] * m[5]) * det;
+        q[8] = (m[0] * m[4] - m[3] * m[1]) * det;
+    }
+    ctx->symm_inv.assign(inv.begin(), inv.begin() + 9 * nops);
+    return DGPU_OK;
+}
+
+// csf (complex, 2 np doubles) and dsi on the device, averaged into out (3 np)
+static int symm_average(dgpu_ctx *ctx, const dgpu_grid *grid, const double *d_csf, const double *d_dsi,
+                        double *d_out)
+{
+    const int32_t nops = (int32_t)(ctx->symm_inv.size() / 9);
+    if (nops < 1) return dgpu_set_error(ctx, DGPU_ERR_ARG, "symmetry averaging without operations (dgpu_set_symmetry)");
+    SymmGrid sg;
+    for (int k = 0; k < 3; k++) sg.num[k] = grid->inc[k];
+    symm_izero(grid, sg.izero);
+    sg.nops = nops;
+    const int64_t np = (int64_t)grid->inc[0] * grid->inc[1] * grid->inc[2];
+    DGPU_CUDA(ctx, ctx->flag.ensure(64 + ctx->symm_inv.size() * sizeof(int32_t)));
+    int32_t *d_inv = reinterpret_cast<int32_t *>(ctx->flag.as<char>() + 64);
+    DGPU_CUDA(ctx, cudaMemcpyAsync(d_inv, ctx->symm_inv.data(), ctx->symm_inv.size() * sizeof(int32_t),
+                                   cudaMemcpyHostToDevice, ctx->stream));
+    const unsigned nblk = (unsigned)dgpu_cdiv(np, 256);
+    k_symm_avg<double2><<<nblk, 256, 0, ctx->stream>>>(sg, d_inv, (const double2 *)d_csf, (double2 *)d_out);
+    k_symm_avg<double><<<nblk, 256, 0, ctx->stream>>>(sg, d_inv, d_dsi, d_out + 2 * np);
+    DGPU_CUDA(ctx, cudaGetLastError());
+    DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));      // host symm_inv copy and the caller's arrays
+    return DGPU_OK;
+}
+
 extern "C" int dgpu_four_accumulate(dgpu_ctx *ctx, int32_t mode, int32_t symm, const dgpu_grid *grid, double fave,
                                     double *csf, double *dsi)
 {
@@ -236,9 +369,28 @@ extern "C" int dgpu_four_accumulate(dgpu_ctx *ctx, int32_t mode, int32_t symm, c
     DGPU_CUDA(ctx, cudaSetDevice(ctx->device));
     const int64_t np = (int64_t)grid->inc[0] * grid->inc[1] * grid->inc[2];
     switch (mode) {
-    case DGPU_ACCUM_SINGLE:
-        if (symm) return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "reciprocal-space symmetry averaging");
+    case DGPU_ACCUM_SINGLE: {
+        // one pattern: averaged over the point group, then the Bragg fill
+        if (!symm) return DGPU_OK;
+        if (!csf || !dsi) return DGPU_ERR_ARG;
+        // csf (complex) at the start of each half, so the halves start on
+        // 16-byte boundaries: the output at an even number of doubles
+        const int64_t half = (3 * np + 1) & ~(int64_t)1;
+        DGPU_CUDA(ctx, ctx->wbuf.ensure((size_t)(half + 3 * np) * sizeof(double)));
+        double *d_in = ctx->wbuf.as<double>(), *d_out = d_in + half;
+        DGPU_CUDA(ctx, cudaMemcpyAsync(d_in, csf, np * 2 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        DGPU_CUDA(ctx, cudaMemcpyAsync(d_in + 2 * np, dsi, np * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        int rc = symm_average(ctx, grid, d_in, d_in + 2 * np, d_out);
+        if (rc) return rc;
+        DGPU_CUDA(ctx, cudaMemcpyAsync(csf, d_out, np * 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        DGPU_CUDA(ctx, cudaMemcpyAsync(dsi, d_out + 2 * np, np * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (fave < 0.0) {
+            fill_bragg(grid, reinterpret_cast<std::complex<double> *>(csf));
+            fill_bragg(grid, dsi);
+        }
         return DGPU_OK;
+    }
     case DGPU_ACCUM_INIT:
         ctx->acc_csf.release();
         ctx->acc_dsi.release();
@@ -270,13 +422,19 @@ extern "C" int dgpu_four_accumulate(dgpu_ctx *ctx, int32_t mode, int32_t symm, c
         if (!csf || !dsi) return DGPU_ERR_ARG;
         if (ctx->acc_np == 0)
             return dgpu_set_error(ctx, DGPU_ERR_NO_ACCUM, "accumulation finished without accumulated sums");
-        if (symm) return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "reciprocal-space symmetry averaging");
         if (ctx->acc_np != np)
             return dgpu_set_error(ctx, DGPU_ERR_ARG, "accumulated grid has %lld points, this one %lld",
                                   (long long)ctx->acc_np, (long long)np);
-        DGPU_CUDA(ctx, cudaMemcpyAsync(csf, ctx->acc_csf.p, np * 2 * sizeof(double), cudaMemcpyDeviceToHost,
-                                       ctx->stream));
-        DGPU_CUDA(ctx, cudaMemcpyAsync(dsi, ctx->acc_dsi.p, np * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        const double *src_c = ctx->acc_csf.as<double>(), *src_d = ctx->acc_dsi.as<double>();
+        if (symm) {                     // point-group average of the sums before the Bragg fill
+            DGPU_CUDA(ctx, ctx->wbuf.ensure((size_t)np * 3 * sizeof(double)));
+            int rc = symm_average(ctx, grid, src_c, src_d, ctx->wbuf.as<double>());
+            if (rc) return rc;
+            src_c = ctx->wbuf.as<double>();
+            src_d = src_c + 2 * np;
+        }
+        DGPU_CUDA(ctx, cudaMemcpyAsync(csf, src_c, np * 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        DGPU_CUDA(ctx, cudaMemcpyAsync(dsi, src_d, np * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
         DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         if (fave < 0.0) {
             fill_bragg(grid, reinterpret_cast<std::complex<double> *>(csf));

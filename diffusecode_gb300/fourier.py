@@ -151,6 +151,15 @@ def four_accumulate(mode, grid: GridData, csf=None, dsi=None, fave=0.0, symm=0, 
     return _cplx(cbuf, grid.inc), dbuf.reshape(grid.inc, order="F")
 
 
+def set_symmetry(mats, ctx=None):
+    """The point-group operations of four_symm (spc_mat(1:3,1:3,1:nops), the
+    first the identity): an array (nops, 3, 3) of integer matrices."""
+    ctx = ctx or default_context()
+    m = np.asarray(mats, dtype=np.float64).reshape(-1, 3, 3)
+    flat = np.ascontiguousarray(np.transpose(m, (0, 2, 1)).reshape(-1))     # column-major per matrix
+    ctx.check(ctx.lib.dgpu_set_symmetry(ctx.h, int(m.shape[0]), _abi.dptr(flat)))
+
+
 def _interleave(z):
     z = np.asfortranarray(z).reshape(-1, order="F")
     b = np.empty(2 * z.size)

@@ -300,12 +300,23 @@ int dgpu_four_weight_device(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_gr
  * 154-157): INIT clears the sums, ACCUM adds csf/dsi (host arrays of the
  * grid), FINISHED writes the sums into csf/dsi and clears them (with
  * fave < 0 the Bragg points first take the mean of their grid neighbours,
- * four_fill_csf/four_fill_dsi :3844-4044), SINGLE does nothing.  symm != 0
- * (reciprocal-space symmetry averaging) is DGPU_ERR_UNSUPPORTED.            */
+ * four_fill_csf/four_fill_dsi :3844-4044), SINGLE does nothing unless
+ * symm != 0.  symm != 0 (four_symm): SINGLE and FINISHED first average
+ * csf/dsi over the point-group operations set by dgpu_set_symmetry
+ * (four_symm_csf/four_symm_dsi, :4048-4290), then fill the Bragg points.    */
 #define DGPU_ACCUM_INIT      (-1)
 #define DGPU_ACCUM_SINGLE      0
 #define DGPU_ACCUM_ACCUM       1
 #define DGPU_ACCUM_FINISHED    2
+/* The point-group operations of four_symm: spc_mat(1:3,1:3,i), i = 1..nops
+ * with nops = spc_n / n_center (n_center from the first letter of
+ * cr_spcgr: P 1, A/B/C/I 2, F 4, R with cr_syst 6 3; fourier_sup.f90:
+ * 4102-4118), column-major 3x3 each, operation 1 the identity.  Integer
+ * matrices of determinant +-1 (DGPU_ERR_ARG otherwise).  Kept in the
+ * context; nops = 0 clears them.  Replaces the reference's read of the
+ * global spc_mat / spc_n (wyckoff_mod).                                      */
+int dgpu_set_symmetry(dgpu_ctx *ctx, int32_t nops, const double *mats);
+
 int dgpu_four_accumulate(dgpu_ctx *ctx, int32_t mode, int32_t symm, const dgpu_grid *grid, double fave,
                          double *csf, double *dsi);
 

@@ -1527,6 +1527,58 @@ int oc_four_weight(const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *
 
 /* four_fill_csf / four_fill_dsi with fave < 0 (fourier_sup.f90:3844-4044):
  * in place, h slowest; comp = 2 for interleaved complex, 1 for real. */
+/* four_symm_csf / four_symm_dsi (fourier_sup.f90:4048-4290): the pixel of
+ * hkl = 0 from the inverted step matrix, then for every operation 2..nops
+ * (spc_mat, column-major 3x3) each pixel h adds its value and a weight at
+ * izero + NINT((h - izero) S) (row vector times matrix), in the reference's
+ * loop order; finally value / weight / nops.  a: comp = 2 (complex, re/im
+ * interleaved) or 1 values per pixel.                                      */
+void oc_four_symm(const dgpu_grid *g, int32_t nops, const double *mats, double *a, int comp)
+{
+    const int32_t *num = g->inc;
+    const int64_t np = (int64_t)num[0] * num[1] * num[2];
+    double m[9], inv[9];
+    for (int c = 0; c < 3; c++)
+        for (int r = 0; r < 3; r++) m[r + 3 * c] = num[c] > 1 ? g->vi[r + 3 * c] : (r == c ? 1.0 : 0.0);
+    double det = m[0] * (m[4] * m[8] - m[7] * m[5]) - m[3] * (m[1] * m[8] - m[7] * m[2]) + m[6] * (m[1] * m[5] - m[4] * m[2]);
+    inv[0] = (m[4] * m[8] - m[7] * m[5]) / det; inv[3] = (m[6] * m[5] - m[3] * m[8]) / det;
+    inv[6] = (m[3] * m[7] - m[6] * m[4]) / det; inv[1] = (m[7] * m[2] - m[1] * m[8]) / det;
+    inv[4] = (m[0] * m[8] - m[6] * m[2]) / det; inv[7] = (m[6] * m[1] - m[0] * m[7]) / det;
+    inv[2] = (m[1] * m[5] - m[4] * m[2]) / det; inv[5] = (m[3] * m[2] - m[0] * m[5]) / det;
+    inv[8] = (m[0] * m[4] - m[3] * m[1]) / det;
+    int32_t iz[3];
+    for (int r = 0; r < 3; r++) {
+        double u = -(inv[r] * g->eck[0] + inv[r + 3] * g->eck[1] + inv[r + 6] * g->eck[2]);
+        iz[r] = num[r] > 1 ? (int32_t)lround(1.0 + u) : 1;
+    }
+    double *sym = (double *)malloc(sizeof(double) * comp * np);
+    int32_t *w = (int32_t *)malloc(sizeof(int32_t) * np);
+    memcpy(sym, a, sizeof(double) * comp * np);
+    for (int64_t p = 0; p < np; p++) w[p] = 1;
+    for (int i = 1; i < nops; i++) {
+        const double *S = mats + 9 * i;
+        for (int32_t l = 1; l <= num[2]; l++)
+            for (int32_t k = 1; k <= num[1]; k++)
+                for (int32_t h = 1; h <= num[0]; h++) {
+                    double hkl[3] = {(double)(h - iz[0]), (double)(k - iz[1]), (double)(l - iz[2])};
+                    int32_t t[3];
+                    for (int c = 0; c < 3; c++) {
+                        double u = hkl[0] * S[0 + 3 * c] + hkl[1] * S[1 + 3 * c] + hkl[2] * S[2 + 3 * c];
+                        t[c] = iz[c] + (int32_t)lround(u);
+                    }
+                    if (t[0] < 1 || t[0] > num[0] || t[1] < 1 || t[1] > num[1] || t[2] < 1 || t[2] > num[2]) continue;
+                    int64_t src = (h - 1) + (int64_t)num[0] * ((k - 1) + (int64_t)num[1] * (l - 1));
+                    int64_t dst = (t[0] - 1) + (int64_t)num[0] * ((t[1] - 1) + (int64_t)num[1] * (t[2] - 1));
+                    for (int q = 0; q < comp; q++) sym[comp * dst + q] += a[comp * src + q];
+                    w[dst]++;
+                }
+    }
+    for (int64_t p = 0; p < np; p++)
+        for (int q = 0; q < comp; q++) a[comp * p + q] = sym[comp * p + q] / (double)w[p] / (double)nops;
+    free(sym);
+    free(w);
+}
+
 void oc_fill_bragg(const dgpu_grid *g, double *a, int comp)
 {
     const int32_t *num = g->inc;

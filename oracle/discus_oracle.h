@@ -55,6 +55,7 @@ int  oc_chi2_grad(const dgpu_crystal *cr, const dgpu_grid *grid, const dgpu_opts
 int  oc_four_weight(const dgpu_crystal *cr, const dgpu_grid *grid, const dgpu_opts *op,
                     const double *dsi, double *dsi3d, double *scalef);
 void oc_fill_bragg(const dgpu_grid *grid, double *a, int comp);
+void oc_four_symm(const dgpu_grid *grid, int32_t nops, const double *mats, double *a, int comp);
 int  oc_qval(const dgpu_crystal *cr, const dgpu_grid *grid, const dgpu_opts *op, int value, int laver,
              const double *csf, const double *acsf, const double *dsi, const double *rnd, double *out);
 int  oc_calc_hkl(const dgpu_crystal *cr, const dgpu_opts *op, const int32_t *hkl, int64_t nrefl, double scale,

@@ -45,6 +45,8 @@ def lib():
                                      dp, dp, dp]
         L.oc_fill_bragg.argtypes = [C.POINTER(_abi.Grid), dp, C.c_int]
         L.oc_fill_bragg.restype = None
+        L.oc_four_symm.argtypes = [C.POINTER(_abi.Grid), C.c_int32, dp, dp, C.c_int]
+        L.oc_four_symm.restype = None
         L.oc_calc_hkl.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Opts), C.POINTER(C.c_int32), C.c_int64,
                                   C.c_double, C.c_double, C.c_double, dp, dp, dp, C.c_int]
         L.oc_qval.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Grid), C.POINTER(_abi.Opts), C.c_int,
@@ -212,6 +214,23 @@ def four_weight(cr, grid, dsi, opts):
     sc = np.zeros(1)
     lib().oc_four_weight(C.byref(c), C.byref(g), C.byref(opts), _d(d), _d(out), _d(sc))
     return out.reshape(grid.inc, order="F"), float(sc[0])
+
+
+def four_symm(grid, arr, mats):
+    """four_symm_csf / four_symm_dsi on a grid array (real or complex, shaped
+    grid.inc); mats (nops, 3, 3), the first the identity."""
+    g = grid.to_c()
+    m = np.asarray(mats, dtype=np.float64).reshape(-1, 3, 3)
+    flat = np.ascontiguousarray(np.transpose(m, (0, 2, 1)).reshape(-1))
+    a = np.asfortranarray(arr).reshape(-1, order="F")
+    if np.iscomplexobj(a):
+        buf = np.empty(2 * a.size)
+        buf[0::2], buf[1::2] = a.real, a.imag
+        lib().oc_four_symm(C.byref(g), m.shape[0], _d(flat), _d(buf), 2)
+        return (buf[0::2] + 1j * buf[1::2]).reshape(grid.inc, order="F")
+    buf = np.ascontiguousarray(a, dtype=np.float64).copy()
+    lib().oc_four_symm(C.byref(g), m.shape[0], _d(flat), _d(buf), 1)
+    return buf.reshape(grid.inc, order="F")
 
 
 def fill_bragg(grid, arr):

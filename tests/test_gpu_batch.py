@@ -93,3 +93,32 @@ def test_population_members_vs_fp64_sampled(ctx):
         i64, fl = bench.fp64_points(cr, g, idx)
         worst = max(worst, float(np.max(np.abs(d[idx[:, 0], idx[:, 1], idx[:, 2]] - i64) / (i64 + fl))))
     assert worst <= TOL
+
+
+def test_batch_anisotropic_members(oracle, ctx):
+    """Members with anisotropic ADPs (three ADP types) beside isotropic ones:
+    each summed per (type, ADP type) group with its four_dbw term, against
+    the oracle; gradients against the single-crystal adjoint."""
+    from diffusecode_gb300.autograd import chi2_grad
+    mem = []
+    for k, icc in enumerate([(5, 4, 3), (4, 4, 2), (6, 3, 3)]):
+        cr, g = S.small_lots_anis(seed=7 + k, icc=icc, anis=(k != 1))
+        mem.append((cr, g))
+    op = K.opts(phase=_abi.PHASE_EXACT64, engine=_abi.ENGINE_TC, ldbw=1)
+    crs, grids = [m[0] for m in mem], [m[1] for m in mem]
+    dsi, _, _, _, _ = FR.batch_run(crs, grids, op, ctx=ctx)
+    for (cr, g), d in zip(mem, dsi):
+        rc, csf, acsf, ref, info = oracle.four_run(cr, g, op)
+        assert rc == 0
+        assert K.rel_err(d, ref, K.incoherent_floor(cr, g, K.opts(ldbw=0))) <= TOL
+    targets = [d * 1.1 for d in dsi]
+    weights = [1.0 / (t + 1.0) for t in targets]
+    _, chi2, gp, go, _ = FR.batch_run(crs, grids, op, targets, weights, ctx=ctx)
+    for k, (cr, g) in enumerate(mem):
+        c2, gp1, go1, _ = chi2_grad(cr, g, op, targets[k], weights[k], ctx=ctx)
+        # the two runs may pick different tensor-core tiles (rounding ~1e-7
+        # of I, amplified by I / (I - I_t) = 10 in chi^2): the bounds of the
+        # isotropic batch test
+        assert abs(chi2[k] - c2) <= 1e-4 * c2
+        assert np.max(np.abs(gp[k] - gp1)) <= 1e-3 * np.abs(gp1).max()
+        assert np.max(np.abs(go[k] - go1)) <= 1e-3 * np.abs(go1).max()

@@ -137,10 +137,13 @@ def test_gradient_anisotropic(oracle, ctx, engine):
     assert np.max(np.abs(go - ogo)) <= 2e-4 * np.abs(ogo).max()
 
 
-def test_batch_rejects_lots_and_adps(ctx):
+def test_batch_rejects_lots(ctx):
+    """Lots stay with dgpu_four_run (anisotropic members are batched:
+    test_batch_anisotropic_members)."""
     cr, g = S.small_lots_anis(anis=True)
     with pytest.raises(Exception) as e:
-        FR.batch_run([cr], [g], K.opts(phase=_abi.PHASE_EXACT64), ctx=ctx)
+        FR.batch_run([cr], [g], K.opts(phase=_abi.PHASE_EXACT64, ilots=_abi.LOT_BOX, ls_xyz=(3, 2, 2), lot_all=1),
+                     ctx=ctx)
     assert getattr(e.value, "code", None) == _abi.DGPU_ERR_UNSUPPORTED
 
 

@@ -58,9 +58,10 @@ def test_four_accumulate(oracle, ctx):
     c_out, d_out = FR.four_accumulate(_abi.ACCUM_FINISHED, g, runs[0][0], runs[0][1], fave=-1.0, ctx=ctx)
     np.testing.assert_allclose(c_out, oracle.fill_bragg(g, csum), rtol=1e-14)
     np.testing.assert_allclose(d_out, oracle.fill_bragg(g, dsum), rtol=1e-14)
-    # finished without sums, symmetry averaging
+    # finished without sums; symmetry averaging with no operations set
+    FR.set_symmetry(np.zeros((0, 3, 3)), ctx=ctx)
     for mode, kw, code in ((_abi.ACCUM_FINISHED, {}, _abi.DGPU_ERR_NO_ACCUM),
-                           (_abi.ACCUM_SINGLE, {"symm": 1}, _abi.DGPU_ERR_UNSUPPORTED)):
+                           (_abi.ACCUM_SINGLE, {"symm": 1}, _abi.DGPU_ERR_ARG)):
         with pytest.raises(Exception) as e:
             FR.four_accumulate(mode, g, runs[0][0], runs[0][1], ctx=ctx, **kw)
         assert getattr(e.value, "code", None) == code
@@ -77,3 +78,55 @@ def test_negative_fave_is_no_cell(oracle, ctx):
     assert not np.any(r.acsf) and not np.any(acsf)
     r0 = FR.four_run(cr, g, K.opts(phase=_abi.PHASE_EXACT64), ctx=ctx)
     np.testing.assert_allclose(r.dsi, r0.dsi, rtol=1e-12)
+
+
+def _mmm():
+    return np.array([np.diag([sx, sy, sz]).astype(float) for sx in (1, -1) for sy in (1, -1) for sz in (1, -1)])
+
+
+def _four_fold():
+    r = np.array([[0.0, -1.0, 0.0], [1.0, 0.0, 0.0], [0.0, 0.0, 1.0]])
+    return np.array([np.linalg.matrix_power(r, k) for k in range(4)])
+
+
+@pytest.mark.parametrize("ops", ["mmm", "4"])
+def test_four_symm_single_vs_oracle(oracle, ctx, ops):
+    """four_symm on one pattern (SINGLE with symm): the point-group average of
+    csf and dsi on a 3D grid off-centre along x (images falling outside keep
+    their own weight), the same arithmetic in the same order as the oracle's
+    sequential restatement of four_symm_csf / four_symm_dsi."""
+    mats = _mmm() if ops == "mmm" else _four_fold()
+    g = _grid(np.diag([0.25, 0.25, 0.5]), (13, 13, 5), lo=(-1.25, -1.5, -1.0))
+    rng = np.random.default_rng(3)
+    d = rng.random(g.inc)
+    z = d * np.exp(2j * np.pi * rng.random(g.inc))
+    FR.set_symmetry(mats, ctx=ctx)
+    c, di = FR.four_accumulate(_abi.ACCUM_SINGLE, g, z, d, fave=0.0, symm=1, ctx=ctx)
+    np.testing.assert_array_equal(di, oracle.four_symm(g, d, mats))
+    np.testing.assert_array_equal(c, oracle.four_symm(g, z, mats))
+
+
+def test_four_symm_finished_with_bragg_fill(oracle, ctx):
+    """Two accumulated patterns finished with symm and fave < 0: the point-
+    group average of the sums, then the Bragg fill (four_fill_csf /
+    four_fill_dsi, fourier_sup.f90:3844-4044)."""
+    mats = _mmm()
+    g = _grid(np.diag([0.25, 0.25, 0.5]), (13, 13, 5), lo=(-1.5, -1.5, -1.0))
+    rng = np.random.default_rng(5)
+    FR.set_symmetry(mats, ctx=ctx)
+    FR.four_accumulate(_abi.ACCUM_INIT, g, ctx=ctx)
+    tot_d, tot_z = 0.0, 0.0
+    for _ in range(2):
+        d = rng.random(g.inc)
+        z = d * np.exp(2j * np.pi * rng.random(g.inc))
+        FR.four_accumulate(_abi.ACCUM_ACCUM, g, z, d, ctx=ctx)
+        tot_d, tot_z = tot_d + d, tot_z + z
+    c, di = FR.four_accumulate(_abi.ACCUM_FINISHED, g, fave=-1.0, symm=1, ctx=ctx)
+    np.testing.assert_allclose(di, oracle.fill_bragg(g, oracle.four_symm(g, tot_d, mats)), rtol=1e-14)
+    np.testing.assert_allclose(c, oracle.fill_bragg(g, oracle.four_symm(g, tot_z, mats)), rtol=1e-14, atol=1e-14)
+
+
+def test_four_symm_rejects_non_integer_operations(ctx):
+    with pytest.raises(Exception) as e:
+        FR.set_symmetry([np.eye(3), np.diag([0.5, 2.0, 1.0])], ctx=ctx)
+    assert getattr(e.value, "code", None) == _abi.DGPU_ERR_ARG

@@ -111,3 +111,41 @@ def test_closed_form_gradient_reference_matches_oracle(oracle):
     assert abs(c2 - oc2) <= 1e-10 * oc2
     np.testing.assert_allclose(gp, ogp[atoms], rtol=0, atol=1e-9 * np.abs(ogp).max())
     np.testing.assert_allclose(go, ogo[atoms], rtol=0, atol=1e-9 * np.abs(ogo).max())
+
+
+def _point_group_mmm():
+    ops = []
+    for sx in (1, -1):
+        for sy in (1, -1):
+            for sz in (1, -1):
+                ops.append(np.diag([sx, sy, sz]).astype(float))
+    return np.array(ops)
+
+
+def test_four_symm_known_answers():
+    """four_symm on a centred 5 x 5 x 1 grid: a 2-fold axis along z averages
+    each pixel with its mirror through the centre and divides by the two
+    operations as well (csf_sym / weight / nops, fourier_sup.f90:4161); the
+    identity alone returns the array; an off-centre grid leaves the pixels
+    whose image falls outside with weight 1."""
+    g = _grid(np.diag([0.5, 0.5, 0.0]), (5, 5, 1), lo=(-1.0, -1.0, 0.0))
+    rng = np.random.default_rng(4)
+    d = rng.random(g.inc)
+    two = np.array([np.eye(3), np.diag([-1.0, -1.0, 1.0])])
+    out = O.four_symm(g, d, two)
+    want = (d + d[::-1, ::-1, :]) / 2 / 2
+    np.testing.assert_allclose(out, want, rtol=1e-15)
+    np.testing.assert_array_equal(O.four_symm(g, d, np.eye(3)[None]), d)
+    z = d + 1j * rng.random(g.inc)
+    np.testing.assert_allclose(O.four_symm(g, z, two), (z + z[::-1, ::-1, :]) / 4, rtol=1e-15)
+    # off centre by one pixel along x: pixel column 0 has no image inside
+    g2 = _grid(np.diag([0.5, 0.5, 0.0]), (5, 5, 1), lo=(-0.5, -1.0, 0.0))
+    out2 = O.four_symm(g2, d, two)
+    # hkl = 0 at pixel (1, 2): h -> 2 - h along x, k -> 4 - k along y
+    for h in range(5):
+        for k in range(5):
+            hh = 2 - h
+            if 0 <= hh < 5:
+                assert abs(out2[h, k, 0] - (d[h, k, 0] + d[hh, 4 - k, 0]) / 2 / 2) < 1e-15
+            else:
+                assert abs(out2[h, k, 0] - d[h, k, 0] / 1 / 2) < 1e-15
