@@ -901,9 +901,12 @@ extern "C" int dgpu_four_strucf(dgpu_ctx *ctx, const double *xat, int64_t nxat, 
         rc = dgpu_direct_sums(ctx, ctx->ph0.as<uint64_t>(), ctx->du.as<uint64_t>(), ctx->dv.as<uint64_t>(),
                               ctx->dw.as<uint64_t>(), ctx->w.as<float>(), ts, 1, 1, box, ctx->part, &nslice);
         if (rc) return rc;
-        // form factor: table lookup through istl, or unity
+        // form factor: table lookup through istl, or unity (the caller's
+        // tables replace the cached ones)
         DGPU_CUDA(ctx, ctx->cfact.ensure(DGPU_NTAB * sizeof(double2)));
         DGPU_CUDA(ctx, ctx->istl.ensure(np * sizeof(int32_t)));
+        ctx->stl_key.p = nullptr;
+        ctx->cf_key.p = nullptr;
         if (cfact) {
             DGPU_CUDA(ctx, cudaMemcpyAsync(ctx->cfact.p, cfact, DGPU_NTAB * sizeof(double2), cudaMemcpyHostToDevice,
                                            ctx->stream));

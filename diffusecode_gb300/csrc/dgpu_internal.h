@@ -140,6 +140,14 @@ struct dgpu_ctx {
     DevBuf slab_ph0;                        // powder: per-slab origin phases of the atoms
     int64_t acc_np = 0;                     // points of the accumulated sums (0: none)
     std::vector<int32_t> symm_inv;          // inverses of the point-group operations (four_symm), 9 each
+    // what ctx->istl and ctx->cfact hold (the reference recomputes its tables
+    // only when the grid or the form factors change, four_layer,
+    // fourier_sup.f90:2578-2582): buffer, capacity and the inputs
+    struct TabKey {
+        const void *p = nullptr;
+        size_t cap = 0;
+        std::vector<double> k;
+    } stl_key, cf_key;
     DevBuf gq, gpart, grad, batch_desc, batch_aux;
     double batch_ms = 0.0;
     double tc_kernel_ms = 0.0;              // duration of the last single-problem tensor-core launch

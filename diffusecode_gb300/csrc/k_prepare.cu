@@ -7,6 +7,8 @@
 //    into the unit cell for <F> (four_aver, fourier_sup.f90:1243-1281);
 //  * istl (four_stltab, fourier_sup.f90:2637-2687) and cfact
 //    (four_formtab, fourier_sup.f90:2691-2743) on the device.
+#include <vector>
+
 #include "dgpu_internal.h"
 
 #define PREP_BLK 1024
@@ -421,9 +423,22 @@ __global__ void k_stltab(double e0, double e1, double e2, PhaseGeom vg, int32_t 
     stltab_point(e, vg.vi, n0, n1, n2, r, istl, flag, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
+// the table in ctx's buffer p already holds what key describes
+static bool tab_cached(const dgpu_ctx::TabKey &t, const DevBuf &b, const void *p, const std::vector<double> &key)
+{
+    return t.p == p && b.p == p && t.cap == b.cap && t.k == key;
+}
+
 int dgpu_stltab_dev(dgpu_ctx *ctx, const double eck[3], const double vi[9], const int32_t num[3],
                     const double rten[9], int32_t *d_istl)
 {
+    // the context's own table for the same grid and metric: already there
+    std::vector<double> key(eck, eck + 3);
+    key.insert(key.end(), vi, vi + 9);
+    key.insert(key.end(), rten, rten + 9);
+    for (int k = 0; k < 3; k++) key.push_back((double)num[k]);
+    if (tab_cached(ctx->stl_key, ctx->istl, d_istl, key)) return DGPU_OK;
+    ctx->stl_key.p = nullptr;
     int64_t np = (int64_t)num[0] * num[1] * num[2];
     DGPU_CUDA(ctx, ctx->flag.ensure(64));
     int32_t *flag = ctx->flag.as<int32_t>();
@@ -441,6 +456,11 @@ int dgpu_stltab_dev(dgpu_ctx *ctx, const double eck[3], const double vi[9], cons
     if (hflag)
         return dgpu_set_error(ctx, DGPU_ERR_STL_RANGE,
                               "sin(theta)/lambda beyond the form-factor table (istl > %d)", DGPU_CFPKT);
+    if (d_istl == ctx->istl.as<int32_t>()) {
+        ctx->stl_key.p = d_istl;
+        ctx->stl_key.cap = ctx->istl.cap;
+        ctx->stl_key.k = key;
+    }
     return DGPU_OK;
 }
 
@@ -485,15 +505,30 @@ int dgpu_formtab_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *op,
         h.delfr[t] = cr->delfr ? cr->delfr[t] : 0.0;
         h.delfi[t] = cr->delfi ? cr->delfi[t] : 0.0;
     }
+    const int32_t ldbw = op->ldbw && !cr->is_anis;
+    std::vector<double> key(reinterpret_cast<const double *>(&h),
+                            reinterpret_cast<const double *>(&h) + (sizeof(h) / sizeof(double)));
+    key.push_back(cr->nscat);
+    key.push_back(op->lxray);
+    key.push_back(op->power);
+    key.push_back(op->ano);
+    key.push_back(ldbw);
+    if (tab_cached(ctx->cf_key, ctx->cfact, d_cfact, key)) return DGPU_OK;
+    ctx->cf_key.p = nullptr;
     DGPU_CUDA(ctx, ctx->stats.ensure(sizeof(FormCoef)));
     FormCoef *d = ctx->stats.as<FormCoef>();
     DGPU_CUDA(ctx, cudaMemcpyAsync(d, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->stream));
     int64_t n = (int64_t)cr->nscat * DGPU_NTAB;
     k_formtab<<<(unsigned)dgpu_cdiv(n, 256), 256, 0, ctx->stream>>>(d, cr->nscat, op->lxray, op->power,
-                                                                      op->ano, op->ldbw && !cr->is_anis, d_cfact);
+                                                                      op->ano, ldbw, d_cfact);
     DGPU_CUDA(ctx, cudaGetLastError());
     // the coefficient block lives in ctx->stats: finish before it is reused
     DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (d_cfact == ctx->cfact.as<double2>()) {
+        ctx->cf_key.p = d_cfact;
+        ctx->cf_key.cap = ctx->cfact.cap;
+        ctx->cf_key.k = key;
+    }
     return DGPU_OK;
 }
 

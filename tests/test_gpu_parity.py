@@ -253,3 +253,31 @@ def test_all_void_crystal_gives_zero(ctx):
     cr.iscat[:] = 0
     r = FR.four_run(cr, g, K.opts(engine=_abi.ENGINE_DIRECT), ctx=ctx)
     assert np.all(r.dsi == 0) and r.info.pairs == 0
+
+
+def test_cached_tables_follow_the_grid_and_form_factors(oracle, ctx):
+    """istl and cfact are kept between calls while the grid, metric and form
+    factors stay (as four_layer does): a second grid of the same size, other
+    form-factor coefficients, and a per-type call that loads the caller's
+    tables in between all give the oracle's result."""
+    cr, g = S.small_random(seed=5, natoms=200, nscat=2, inc=(9, 7, 5))
+    op = K.opts(phase=_abi.PHASE_EXACT64, engine=_abi.ENGINE_DIRECT)
+    floor = K.incoherent_floor(cr, g, op)
+    g2 = S.GridData(eck=g.eck + 0.37, vi=g.vi * 1.1, inc=g.inc)
+    for grid in (g, g, g2, g):
+        r = FR.four_run(cr, grid, op, ctx=ctx)
+        rc, _, _, ref, _ = oracle.four_run(cr, grid, op)
+        assert K.rel_err(r.dsi, ref, K.incoherent_floor(cr, grid, op)) <= 1e-5
+    cr2 = cr.with_positions(cr.pos)
+    cr2.scat = cr.scat * 1.3
+    r = FR.four_run(cr2, g, op, ctx=ctx)
+    rc, _, _, ref, _ = oracle.four_run(cr2, g, op)
+    assert K.rel_err(r.dsi, ref, K.incoherent_floor(cr2, g, op)) <= 1e-5
+    # a per-type call with the caller's tables, then the run again
+    rc, lmn, off = FR.fourier_lmn(g.eck, g.vi, g.inc, ctx=ctx)
+    xat = cr.pos[cr.iscat == 1]
+    fnum = g.inc
+    FR.four_strucf(xat, g.vi[:, 0], g.vi[:, 1], g.vi[:, 2], off, lmn, g.inc, fnum, None, None, ctx=ctx)
+    r = FR.four_run(cr, g, op, ctx=ctx)
+    rc, _, _, ref, _ = oracle.four_run(cr, g, op)
+    assert K.rel_err(r.dsi, ref, floor) <= 1e-5
