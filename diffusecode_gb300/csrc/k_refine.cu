@@ -9,8 +9,11 @@
 // 3.4e-7 times that ratio, measured against FP64.  Those points are found
 // after the combine (|acsf|^2 > REFINE_TAU * N <|f|^2>) and their type sums
 // -- of the crystal and of the atoms folded into one cell -- are evaluated
-// again on CUDA cores: FP32 phasors of the exact 64-bit phase, FP32 sums of
-// short chunks, FP64 across chunks and threads.  csf, acsf and dsi of those
+// again on CUDA cores: FP32 phasors of the exact 64-bit phase by table-driven
+// angle addition (1024-entry table of exp(2 pi i j / 1024) in shared memory
+// times a two-term series for the remainder, the method of Tang's
+// table-driven elementary functions), FP32 sums of short chunks, FP64 across
+// chunks and threads.  csf, acsf and dsi of those
 // points are then formed with the same form-factor and lattice code as the
 // combine kernels.
 //
@@ -33,6 +36,12 @@
 #define RF_CHUNK 16         // atoms per FP32 partial before it is added in FP64 (at the most coherent
                             // points FP32 chunks of 32 atoms round alike chunk after chunk: 1.8e-5)
 #define RF_SLICE 65536      // atoms per work item
+#define RF_TAB 1024         // table angles 2 pi j / RF_TAB
+#define RF_ROUND ((1ull << 53) + (1ull << 30))   // added to a phase: table index and remainder rounded to nearest
+
+// radians per unit of the 23-bit remainder (2 pi / 2^33) and -(that)^2 / 6
+#define RF_KAPPA (3.14159265358979f * 0x1p-32f)
+#define RF_S6 (-(RF_KAPPA * RF_KAPPA) / 6.0f)
 
 struct RefineTypes {
     int64_t ts[65];         // type ranges of a prepared atom set (0-based types)
@@ -73,6 +82,35 @@ __device__ __forceinline__ double warp_sum(double v)
     return v;
 }
 
+// exp(2 pi i j / RF_TAB), FP64 rounded to FP32
+__global__ void k_refine_table(float2 *__restrict__ tab)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= RF_TAB) return;
+    double s, c;
+    sincospi((double)j * (2.0 / RF_TAB), &s, &c);
+    tab[j] = make_float2((float)c, (float)s);
+}
+
+// (x, y) += w exp(2 pi i ph / 2^64), ph carrying the offset RF_ROUND: the
+// top 10 bits select the table angle T, the next 23 bits (less 2^22) give
+// the remainder d in units of RF_KAPPA, |d| <= pi / 1024 rad, and
+// exp(i d) = 1 - d^2/2 + i d (1 - d^2/6) to within 4e-12.  w T is formed
+// exactly inside the last FMA, so a weighted phasor is rounded once (plus
+// the table's own rounding) before it enters the FP32 chunk sum.
+// wk = w RF_KAPPA, wc = -w RF_KAPPA^2 / 2.
+__device__ __forceinline__ void phasor_tab_acc(uint64_t ph, const float2 *__restrict__ tab, float wa, float wk,
+                                               float wc, float &x, float &y)
+{
+    const float2 T = tab[(uint32_t)(ph >> 54)];
+    const float d = __uint_as_float(((uint32_t)(ph >> 31) & 0x7FFFFFu) | 0x4B000000u) - 12582912.0f;
+    const float d2 = d * d;
+    const float v = (wk * d) * fmaf(d2, RF_S6, 1.0f);          // w sin(d)
+    const float u = d2 * wc;                                    // w (cos(d) - 1)
+    x += fmaf(T.x, wa, fmaf(T.x, u, -T.y * v));
+    y += fmaf(T.y, wa, fmaf(T.y, u, T.x * v));
+}
+
 // The atoms of one work item: FP32 sums of RF_CHUNK atoms per point, added
 // to FP64.  RUN: the points are consecutive along the step axis sa and
 // their phases one 64-bit add apart.
@@ -80,15 +118,17 @@ template <bool RUN>
 __device__ __forceinline__ void refine_loop(int64_t lo, int64_t hi, const uint64_t *__restrict__ ph0,
                                             const uint64_t *__restrict__ du, const uint64_t *__restrict__ dv,
                                             const uint64_t *__restrict__ dw, const float *__restrict__ w,
-                                            const uint32_t (&n0)[RF_PTS], const uint32_t (&n1)[RF_PTS],
-                                            const uint32_t (&n2)[RF_PTS], const bool (&stp)[RF_PTS],
-                                            double (&acc)[RF_PTS][2], float (&chk)[RF_PTS][2], int sa)
+                                            const float2 *__restrict__ tab, const uint32_t (&n0)[RF_PTS],
+                                            const uint32_t (&n1)[RF_PTS], const uint32_t (&n2)[RF_PTS],
+                                            const bool (&stp)[RF_PTS], double (&acc)[RF_PTS][2],
+                                            float (&chk)[RF_PTS][2], int sa, bool f0, bool f1, bool f2)
 {
     int c = 0;
     for (int64_t a = lo + threadIdx.x; a < hi; a += RF_NT) {
-        const uint64_t b = ph0[a], d0 = du[a], d1 = dv[a], d2 = dw[a];
+        // an axis of extent 1 has n = 0 at every point: its step is not read
+        const uint64_t b = ph0[a] + RF_ROUND, d0 = f0 ? du[a] : 0, d1 = f1 ? dv[a] : 0, d2 = f2 ? dw[a] : 0;
         const uint64_t ds = sa == 0 ? d0 : sa == 1 ? d1 : d2;
-        const float wa = w[a];
+        const float wa = w[a], wk = wa * RF_KAPPA, wc = wa * (-0.5f * RF_KAPPA * RF_KAPPA);
         uint64_t ph = b + (uint64_t)n0[0] * d0 + (uint64_t)n1[0] * d1 + (uint64_t)n2[0] * d2;
 #pragma unroll
         for (int k = 0; k < RF_PTS; k++) {
@@ -96,9 +136,7 @@ __device__ __forceinline__ void refine_loop(int64_t lo, int64_t hi, const uint64
                 if (RUN || stp[k]) ph += ds;
                 else ph = b + (uint64_t)n0[k] * d0 + (uint64_t)n1[k] * d1 + (uint64_t)n2[k] * d2;
             }
-            const float2 e = phasor_acc(ph);
-            chk[k][0] = fmaf(wa, e.x, chk[k][0]);
-            chk[k][1] = fmaf(wa, e.y, chk[k][1]);
+            phasor_tab_acc(ph, tab, wa, wk, wc, chk[k][0], chk[k][1]);
         }
         if (++c == RF_CHUNK) {
             c = 0;
@@ -117,10 +155,12 @@ __device__ __forceinline__ void refine_loop(int64_t lo, int64_t hi, const uint64
 __global__ void __launch_bounds__(RF_NT, 2)
 k_refine_sums(const int32_t *__restrict__ list, int32_t npts, BoxSpec box, const uint64_t *__restrict__ ph0,
               const uint64_t *__restrict__ du, const uint64_t *__restrict__ dv, const uint64_t *__restrict__ dw,
-              const float *__restrict__ w, const RefineTypes rt, int32_t nsl, int32_t sa,
-              double2 *__restrict__ out)
+              const float *__restrict__ w, const float2 *__restrict__ gtab, const RefineTypes rt, int32_t nsl,
+              int32_t sa, double2 *__restrict__ out)
 {
     __shared__ double red[RF_NT / 32][RF_PTS][2];
+    __shared__ float2 tab[RF_TAB];
+    for (int j = threadIdx.x; j < RF_TAB; j += RF_NT) tab[j] = gtab[j];
     const int64_t item = blockIdx.x;
     const int s = (int)(item % nsl);
     const int t = (int)((item / nsl) % rt.ntype);
@@ -161,10 +201,11 @@ k_refine_sums(const int32_t *__restrict__ list, int32_t npts, BoxSpec box, const
     bool run = true;                 // every point the previous one plus one step along axis sa
 #pragma unroll
     for (int k = 1; k < RF_PTS; k++) run = run && stp[k];
+    const bool f0 = box.f[0] > 1, f1 = box.f[1] > 1, f2 = box.f[2] > 1;
     if (run)
-        refine_loop<true>(lo, hi, ph0, du, dv, dw, w, n0, n1, n2, stp, acc, chk, sa);
+        refine_loop<true>(lo, hi, ph0, du, dv, dw, w, tab, n0, n1, n2, stp, acc, chk, sa, f0, f1, f2);
     else
-        refine_loop<false>(lo, hi, ph0, du, dv, dw, w, n0, n1, n2, stp, acc, chk, sa);
+        refine_loop<false>(lo, hi, ph0, du, dv, dw, w, tab, n0, n1, n2, stp, acc, chk, sa, f0, f1, f2);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < RF_PTS; k++) {
@@ -264,13 +305,14 @@ int dgpu_refine_aver(dgpu_ctx *ctx, const RefineSpec &r, double2 *csf, double2 *
     RefineTypes rm, ra;
     fill_types(rm, r.ts_main, r.ngroup);
     fill_types(ra, r.ts_fold, r.nscat);
-    // two FormSpec blocks, the point list and its count
-    const size_t fsb = (sizeof(FormSpec) + 255) & ~(size_t)255;
-    DGPU_CUDA(ctx, ctx->rlist.ensure(2 * fsb + 256 + (size_t)nb * sizeof(int32_t)));
+    // two FormSpec blocks, the phasor table, the point list and its count
+    const size_t fsb = (sizeof(FormSpec) + 255) & ~(size_t)255, tb = RF_TAB * sizeof(float2);
+    DGPU_CUDA(ctx, ctx->rlist.ensure(2 * fsb + tb + 256 + (size_t)nb * sizeof(int32_t)));
     FormSpec *d_fsm = ctx->rlist.as<FormSpec>();
     FormSpec *d_fst = (FormSpec *)((char *)ctx->rlist.p + fsb);
-    int32_t *d_count = (int32_t *)((char *)ctx->rlist.p + 2 * fsb);
-    int32_t *d_list = (int32_t *)((char *)ctx->rlist.p + 2 * fsb + 256);
+    float2 *d_tab = (float2 *)((char *)ctx->rlist.p + 2 * fsb);
+    int32_t *d_count = (int32_t *)((char *)ctx->rlist.p + 2 * fsb + tb);
+    int32_t *d_list = (int32_t *)((char *)ctx->rlist.p + 2 * fsb + tb + 256);
     DGPU_CUDA(ctx, cudaMemcpyAsync(d_fsm, r.fsm, sizeof(FormSpec), cudaMemcpyHostToDevice, ctx->stream));
     DGPU_CUDA(ctx, cudaMemcpyAsync(d_fst, r.fst, sizeof(FormSpec), cudaMemcpyHostToDevice, ctx->stream));
     DGPU_CUDA(ctx, cudaMemsetAsync(d_count, 0, sizeof(int32_t), ctx->stream));
@@ -315,6 +357,8 @@ int dgpu_refine_aver(dgpu_ctx *ctx, const RefineSpec &r, double2 *csf, double2 *
                                        ctx->stream));
         DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));   // h is a host temporary
     }
+    k_refine_table<<<RF_TAB / 256, 256, 0, ctx->stream>>>(d_tab);
+    DGPU_CUDA(ctx, cudaGetLastError());
     const int32_t nslf = slices_of(rm), nsla = slices_of(ra);
     const int64_t ngrp = dgpu_cdiv(npts, RF_PTS);
     DGPU_CUDA(ctx, ctx->rsum.ensure((size_t)npts * ((size_t)r.ngroup * nslf + (size_t)r.nscat * nsla) *
@@ -323,11 +367,11 @@ int dgpu_refine_aver(dgpu_ctx *ctx, const RefineSpec &r, double2 *csf, double2 *
     double2 *sa_sum = sf + (size_t)npts * r.ngroup * nslf;
     const int64_t itf = ngrp * r.ngroup * nslf, ita = ngrp * r.nscat * nsla;
     if (itf > 0x7fffffffLL || ita > 0x7fffffffLL) return dgpu_set_error(ctx, DGPU_ERR_ARG, "refinement too large");
-    k_refine_sums<<<(unsigned)itf, RF_NT, 0, ctx->stream>>>(d_list, npts, box, r.ph0, r.du, r.dv, r.dw, r.w, rm,
-                                                            nslf, sa, sf);
+    k_refine_sums<<<(unsigned)itf, RF_NT, 0, ctx->stream>>>(d_list, npts, box, r.ph0, r.du, r.dv, r.dw, r.w, d_tab,
+                                                            rm, nslf, sa, sf);
     DGPU_CUDA(ctx, cudaGetLastError());
-    k_refine_sums<<<(unsigned)ita, RF_NT, 0, ctx->stream>>>(d_list, npts, box, r.aph0, r.adu, r.adv, r.adw, r.aw, ra,
-                                                            nsla, sa, sa_sum);
+    k_refine_sums<<<(unsigned)ita, RF_NT, 0, ctx->stream>>>(d_list, npts, box, r.aph0, r.adu, r.adv, r.adw, r.aw,
+                                                            d_tab, ra, nsla, sa, sa_sum);
     DGPU_CUDA(ctx, cudaGetLastError());
     k_refine_combine<<<(unsigned)dgpu_cdiv(npts, 128), 128, 0, ctx->stream>>>(
         d_list, npts, d_fsm, d_fst, box, r.istl, r.cfact, sf, nslf, sa_sum, nsla, r.lat_n[0], r.lat_n[1], r.lat_n[2],
