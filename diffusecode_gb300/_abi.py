@@ -21,6 +21,7 @@ DGPU_ERR_CANCELLED = -14
 DGPU_ERR_NO_ATOMS = -198
 DGPU_ERR_SCRATCH_SIZE = -20
 DGPU_ERR_NO_ACCUM = -175
+DGPU_ERR_IO = -21
 
 CFPKT = 9999
 CFINC = 0.001
@@ -59,6 +60,17 @@ LOT_ELI = 3
 PREF_NONE = 0
 PREF_RIETVELD = 1
 PREF_MARCH = 2
+HKL_CIF = 1
+HKL_HKLF4 = 4
+OUT_STANDARD = 0
+OUT_GNUPLOT = 3
+OUT_HKLF4 = 6
+OUT_LIST5 = 7
+OUT_LIST9 = 8
+OUT_NIPL3D = 9
+OUT_VTK = 11
+OUT_MRC = 12
+OUT_XPLOR = 14
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
@@ -250,3 +262,53 @@ def default_opts(**kw):
             continue
         setattr(o, k, v)
     return o
+
+
+class Nipl(C.Structure):
+    _fields_ = [
+        ("natoms", C.c_int64),
+        ("nscat", C.c_int32),
+        ("ncatoms", C.c_int32),
+        ("at_lis", C.c_char_p),
+        ("amount", C.POINTER(C.c_int64)),
+        ("dw", _dp),
+        ("four_last", C.c_int32),
+        ("radiation", C.c_int32),
+        ("rlambda", C.c_double),
+        ("lambda_", C.c_char_p),
+        ("ldbw", C.c_int32),
+        ("ano", C.c_int32),
+        ("inc", C.c_int32 * 3),
+        ("eck", C.c_double * 12),
+        ("vi", C.c_double * 9),
+    ]
+
+
+class Output(C.Structure):
+    _fields_ = [
+        ("format", C.c_int32),
+        ("value", C.c_int32),
+        ("inc", C.c_int32 * 3),
+        ("extr_abs", C.c_int32),
+        ("extr_ord", C.c_int32),
+        ("extr_top", C.c_int32),
+        ("eck", C.c_double * 12),
+        ("vi", C.c_double * 9),
+        ("rten", C.c_double * 9),
+        ("ar", C.c_double * 3),
+        ("wrez", C.c_double * 3),
+        ("icc", C.c_int32 * 3),
+        ("lrange", C.c_int32),
+        ("lcenter", C.c_int32),
+        ("lpixel", C.c_int32),
+        ("center", C.c_int32 * 3),
+        ("pixel", C.c_int32 * 3),
+        ("quad", C.c_char * 4),
+        ("valmax", C.c_double),
+        ("f000", C.c_double),
+        ("exti", C.c_double),
+        ("rlambda", C.c_double),
+        ("name", C.c_char_p),
+        ("nipl", C.POINTER(Nipl)),
+        ("out_fac", C.c_double),
+    ]

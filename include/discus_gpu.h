@@ -40,6 +40,7 @@ extern "C" {
 #define DGPU_ERR_NO_ATOMS   (-198)  /* cr_natoms < 1 (ier_num=-198, ER_APPL)                   */
 #define DGPU_ERR_SCRATCH_SIZE (-20) /* request exceeds a fixed scratch capacity                */
 #define DGPU_ERR_NO_ACCUM   (-175)  /* accumulation finished without sums (ier_num=-175, ER_APPL) */
+#define DGPU_ERR_IO          (-21)  /* a file could not be opened, read or written (ier_num=-2, ER_IO) */
 
 /* ---- tables (discus/prog/discus_config_mod.f90:27-28, diffuse_mod.f90:20-21) */
 #define DGPU_CFPKT   9999          /* last index of the sin(theta)/lambda table              */
@@ -360,6 +361,97 @@ int dgpu_qval(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *grid, cons
 int dgpu_calc_hkl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *opts, const int32_t *hkl,
                   int64_t nrefl, double scale, double exti, double rlambda, double *icalc, double *sigi,
                   double *phase);
+
+/* ---- output files --------------------------------------------------------- */
+/* calc_hkl with its files (fourier_sup.f90:3230-3549): reads the reflections
+ * of infile -- HKLF4 records (3I4,2F8.2), a line starting with '#', '!' or
+ * 'd' is DGPU_ERR_ARG; or a CIF whose _refln_ loop starts with index_h,
+ * index_k, index_l and carries at most three values before its last column
+ * -- runs dgpu_calc_hkl on them and writes calcfile (HKLF4: h k l icalc sigi,
+ * (3I4,2F8.2); CIF: h k l and the row's values with _refln_F_squared_calc
+ * replaced by icalc, (3I4,3F12.2)) and the list file, calcfile with its
+ * trailing "hkl" replaced by "fcf" or ".fcf" appended (3I4,2F10.2,F7.2:
+ * h k l, sqrt|Iobs| (HKLF4) or h (CIF), sqrt|icalc|, phase).  The reflection
+ * 0 0 0 is written as zeros to calcfile only.                                */
+#define DGPU_HKL_CIF    1
+#define DGPU_HKL_HKLF4  4
+int dgpu_calc_hkl_files(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *opts, const char *infile,
+                        const char *calcfile, int32_t style, double scale, double exti, double rlambda);
+
+/* The writers of the output menu, host-side (format = the reference's ityp):
+ *   STANDARD  do_output ityp 0 (graphic.f90:1704-1847): 1D "x y" records
+ *             (2(1X,E12.5)); 2D a NIPL file (header lines, npkt1 npkt2,
+ *             x/y ranges, rows of 5(1X,E12.5), output_save_file_2d,
+ *             discus_s_out_file.f90:124-260); 3D one such file per layer,
+ *             named path.PART_nnnn;
+ *   GNUPLOT   ityp 3: 2D rows "h_abs h_ord value h_third" (4(1X,E12.5)), a
+ *             blank record after each row; nothing for 1D data;
+ *   HKLF4, LIST5, LIST9  ityp 6-8: reflections with INT(h) /= 0 0 0, the
+ *             amplitude per unit cell, extinction and scale (valmax) as
+ *             graphic.f90:1598-1702,1893-1991 and the 1D rows :2012-2109;
+ *   NIPL3D    ityp 9: list-directed inc and ranges, then the rows of the
+ *             first layer (the reference closes the file after it);
+ *   VTK       vtk_write (vtk_mod.f90:4-35): STRUCTURED_POINTS header and the
+ *             values (the caller's dsi, nvalues of them) as E13.6E2;
+ *   MRC       mrc_write (lib_f90/mrc_data.f90:19-139): 1024-byte header,
+ *             3072-byte extended header, REAL(4) map, i fastest;
+ *   XPLOR     xplor_write (discus_xplor.f90:16-139), path gets ".xplor"
+ *             unless it ends in it; the output range (lrange ...) applies.
+ * values: qval's array for `value` over inc (Fortran order, nvalues =
+ * inc1 inc2 inc3; VTK: dsi).  ampl/phase: qval's arrays for values 2 and 3
+ * (SHELX formats; HKLF4 needs no phase on 2D/3D grids).  PGM and PPM are
+ * disabled in the reference, HDF5 and NeXus need libraries this build does
+ * not link, postscript is a plot: DGPU_ERR_UNSUPPORTED.                      */
+#define DGPU_OUT_STANDARD  0
+#define DGPU_OUT_GNUPLOT   3
+#define DGPU_OUT_HKLF4     6
+#define DGPU_OUT_LIST5     7
+#define DGPU_OUT_LIST9     8
+#define DGPU_OUT_NIPL3D    9
+#define DGPU_OUT_VTK      11
+#define DGPU_OUT_MRC      12
+#define DGPU_OUT_XPLOR    14
+
+typedef struct dgpu_nipl {            /* write_discus_nipl_header (discus_nipl_header.f90:5-172)  */
+    int64_t natoms;                   /* cr_natoms                                              */
+    int32_t nscat, ncatoms;           /* cr_nscat, cr_ncatoms                                   */
+    const char *at_lis;               /* cr_at_lis(0:nscat): 4 characters each, blank padded    */
+    const int64_t *amount;            /* cr_amount(0:nscat)                                     */
+    const double *dw;                 /* cr_dw(0:nscat)                                         */
+    int32_t four_last;                /* |four_last| < 3: FOURIER section; < 0: with lots       */
+    int32_t radiation;                /* diff_radiation: 1 xray, 2 neutron, 3 electron          */
+    double rlambda;
+    const char *lambda;               /* wave-length symbol, "" when given as a number          */
+    int32_t ldbw, ano;
+    int32_t inc[3];                   /* the Fourier's inc, eck(3,4), vi(3,3) (column-major)    */
+    double eck[12];
+    double vi[9];
+} dgpu_nipl;
+
+typedef struct dgpu_output {
+    int32_t format;                   /* DGPU_OUT_*                                             */
+    int32_t value;                    /* qval code of values (XPLOR title, 1D SHELX rows)       */
+    int32_t inc[3];                   /* out_inc                                                */
+    int32_t extr_abs, extr_ord, extr_top;   /* 1..3                                             */
+    double eck[12];                   /* out_eck(3,4), column-major                             */
+    double vi[9];                     /* out_vi(3,3), column-major                              */
+    double rten[9];                   /* cr_rten: |h| for the extinction and the header angles  */
+    double ar[3], wrez[3];            /* cr_ar, cr_wrez (MRC, XPLOR)                            */
+    int32_t icc[3];                   /* cr_icc: the amplitude per unit cell                    */
+    int32_t lrange, lcenter, lpixel;  /* XPLOR range: out_lrange, out_lcenter, out_lpixel       */
+    int32_t center[3], pixel[3];      /* out_center, out_pixel                                  */
+    char quad[4];                     /* out_quad ('l', 'r' or blank per axis)                  */
+    double valmax;                    /* SHELX scale: NINT -1 by F(000), -2 by the largest
+                                         reflection, > 0 this factor, else 1                    */
+    double f000;                      /* qval(1,1,1,2) of the run at 0 0 0 (valmax -1)          */
+    double exti, rlambda;             /* diff_exti, rlambda                                     */
+    const char *name;                 /* cr_name (XPLOR title)                                  */
+    const dgpu_nipl *nipl;            /* header of STANDARD 2D/3D files; NULL: no header lines  */
+    double out_fac;                   /* out: the SHELX scale applied                           */
+} dgpu_output;
+
+int dgpu_output_write(const char *path, dgpu_output *out, const double *values, const double *ampl,
+                      const double *phase, int64_t nvalues);
 
 /* ---- powder pattern, "complete" mode -------------------------------------- */
 /* powder_complete (discus/prog/powder.f90:1829-2593) with pow_four_mode =

@@ -52,6 +52,23 @@ def test_struct_layouts_match_c(tmp_path):
                     _abi.Discamb.form_tsc.offset]
 
 
+def test_output_struct_layouts_match_c(tmp_path):
+    fields = [("dgpu_output", _abi.Output, f) for f, _ in _abi.Output._fields_]
+    fields += [("dgpu_nipl", _abi.Nipl, f) for f, _ in _abi.Nipl._fields_]
+    cname = {"lambda_": "lambda"}
+    expr = ", ".join(f"offsetof({s}, {cname.get(f, f)})" for s, _, f in fields)
+    prog = tmp_path / "so.c"
+    prog.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "discus_gpu.h"\n'
+        "int main(void){size_t v[] = {sizeof(dgpu_output), sizeof(dgpu_nipl), " + expr + "};"
+        " for (size_t k = 0; k < sizeof v / sizeof v[0]; k++) printf(\"%zu \", v[k]); return 0;}\n")
+    exe = tmp_path / "so"
+    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(prog), "-o", str(exe)])
+    vals = [int(x) for x in subprocess.check_output([str(exe)]).split()]
+    want = [C.sizeof(_abi.Output), C.sizeof(_abi.Nipl)] + [getattr(t, f).offset for _, t, f in fields]
+    assert vals == want
+
+
 def test_lmn_host_entry_needs_no_device(built_lib):
     """dgpu_fourier_lmn is host code (quad precision) and runs without a GPU."""
     import kat_cases as K
