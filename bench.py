@@ -342,6 +342,14 @@ def c3_measure(ctx, flush, steps=3):
     sel = (idx[:, 0], idx[:, 1], idx[:, 2])
     e64_tc = np.abs(i_tc[sel] - i64) / (i64 + floor64)
     e64_d = np.abs(d.dsi[sel] - i64) / (i64 + floor64)
+    # FP64 at the 16 points where the two engines disagree most: which of
+    # them carries the difference
+    rel = np.abs(i_tc - d.dsi) / (d.dsi + fl)
+    worst = np.array(np.unravel_index(np.argsort(rel.reshape(-1, order="F"))[::-1][:16], grid.inc, order="F")).T
+    w64, wfl = fp64_points(cr, grid, worst, fave=1.0)
+    wsel = (worst[:, 0], worst[:, 1], worst[:, 2])
+    e["worst16_vs_fp64"] = {"tc_max": float((np.abs(i_tc[wsel] - w64) / (w64 + wfl)).max()),
+                            "direct_max": float((np.abs(d.dsi[wsel] - w64) / (w64 + wfl)).max())}
     return {"workload": "hex-layers-1001^2 (fave 1)", "atoms": cr.n_scattering(), "ms_per_step": ms,
             "pairs": int(info.pairs), "aver_pairs": int(info.pairs_aver),
             "G_pairs_per_s": info.pairs / (ms * 1e-3) / 1e9, "refined_points": refined,

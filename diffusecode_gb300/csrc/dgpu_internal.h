@@ -150,6 +150,7 @@ struct dgpu_ctx {
     } stl_key, cf_key;
     DevBuf gq, gpart, grad, batch_desc, batch_aux;
     double batch_ms = 0.0;
+    bool batch_by_member = false;           // the last dgpu_batch_run ran member by member (no graph)
     double tc_kernel_ms = 0.0;              // duration of the last single-problem tensor-core launch
     std::map<TcKey, TcChoice> tc_tuned;   // autotuner results per problem shape
     BatchState *batch[2] = {nullptr, nullptr};   // captured population graphs (most recent first)

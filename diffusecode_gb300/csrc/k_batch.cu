@@ -16,6 +16,7 @@
 #include <stdlib.h>
 
 #include <algorithm>
+#include <chrono>
 
 #include <vector>
 
@@ -479,20 +480,53 @@ static int batch_build(dgpu_ctx *ctx, BatchState &B, int32_t nc, const dgpu_crys
     return DGPU_OK;
 }
 
+// Options outside the population graph (<F>, lots, DISCAMB, REF22 phases,
+// anomalous scattering, the CUDA-core engine): every member through the
+// single-crystal entries, with the same outputs.  batch_ms is then the wall
+// time of the loop.
+static int batch_by_member(dgpu_ctx *ctx, int32_t nc, const dgpu_crystal *crs, const dgpu_grid *grids,
+                           const dgpu_opts *op, double *const *dsi, const double *const *i_target,
+                           const double *const *weight, double *chi2, double *const *grad_pos,
+                           double *const *grad_occ)
+{
+    // the caller's cell selection of four_aver applies to every member: one cell count
+    if (op->aver_cells && op->fave > 0.0 && op->fave < 1.0)
+        for (int c = 1; c < nc; c++)
+            for (int k = 0; k < 3; k++)
+                if (crs[c].icc[k] != crs[0].icc[k])
+                    return dgpu_set_error(ctx, DGPU_ERR_ARG, "batch: aver_cells needs members of one cell count");
+    const auto t0 = std::chrono::steady_clock::now();
+    std::vector<double> csf;
+    for (int c = 0; c < nc; c++) {
+        const int64_t np = (int64_t)grids[c].inc[0] * grids[c].inc[1] * grids[c].inc[2];
+        csf.resize((size_t)(2 * np));
+        int rc = dgpu_four_run(ctx, &crs[c], &grids[c], op, csf.data(), nullptr, dsi[c], nullptr);
+        if (rc < 0) return rc;                                 // warnings (> 0) pass, as in four_run
+        if (i_target) {
+            rc = dgpu_chi2_grad(ctx, &crs[c], &grids[c], op, i_target[c], weight ? weight[c] : nullptr, &chi2[c],
+                                grad_pos ? grad_pos[c] : nullptr, grad_occ ? grad_occ[c] : nullptr, nullptr);
+            if (rc < 0) return rc;
+        }
+    }
+    ctx->batch_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    ctx->batch_by_member = true;
+    return DGPU_OK;
+}
+
 extern "C" int dgpu_batch_run(dgpu_ctx *ctx, int32_t nc, const dgpu_crystal *crs, const dgpu_grid *grids,
                               const dgpu_opts *op, double *const *dsi, const double *const *i_target,
                               const double *const *weight, double *chi2, double *const *grad_pos,
                               double *const *grad_occ)
 {
     if (!ctx || nc < 1 || !crs || !grids || !op || !dsi) return DGPU_ERR_ARG;
-    if (op->phase != DGPU_PHASE_EXACT64 || op->fave != 0.0 || op->ano)
-        return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "batch: EXACT64 phases, no <F>, no anomalous scattering");
-    if (op->ilots == DGPU_LOT_BOX || op->ilots == DGPU_LOT_ELI)
-        return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "batch: lots are run by dgpu_four_run");
-    if (op->discamb)
-        return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "batch: DISCAMB form factors are run by dgpu_four_run");
-    if (!dgpu_tc_available(ctx)) return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "batch needs the tensor-core engine");
     const bool targets = i_target != nullptr;
+    if (targets && !chi2) return dgpu_set_error(ctx, DGPU_ERR_ARG, "chi2 output missing");
+    for (int c = 0; c < nc; c++)
+        if (!dsi[c] || (targets && !i_target[c])) return dgpu_set_error(ctx, DGPU_ERR_ARG, "member %d: buffers", c);
+    if (op->phase != DGPU_PHASE_EXACT64 || op->fave != 0.0 || op->ano || op->ilots == DGPU_LOT_BOX ||
+        op->ilots == DGPU_LOT_ELI || op->discamb || op->engine == DGPU_ENGINE_DIRECT || !dgpu_tc_available(ctx))
+        return batch_by_member(ctx, nc, crs, grids, op, dsi, i_target, weight, chi2, grad_pos, grad_occ);
+    ctx->batch_by_member = false;
     if (targets && !chi2) return dgpu_set_error(ctx, DGPU_ERR_ARG, "chi2 output missing");
     for (int c = 0; c < nc; c++) {
         if (crs[c].natoms < 1 || !crs[c].pos || !crs[c].iscat || crs[c].nscat < 1 || crs[c].nscat > 63)
@@ -620,7 +654,7 @@ extern "C" double dgpu_batch_last_ms(const dgpu_ctx *ctx) { return ctx ? ctx->ba
 extern "C" int64_t dgpu_batch_graph_nodes(const dgpu_ctx *ctx, int64_t *kernels)
 {
     if (kernels) *kernels = 0;
-    if (!ctx || !ctx->batch[0] || !ctx->batch[0]->graph) return 0;
+    if (!ctx || ctx->batch_by_member || !ctx->batch[0] || !ctx->batch[0]->graph) return 0;
     size_t n = 0;
     if (cudaGraphGetNodes(ctx->batch[0]->graph, nullptr, &n) != cudaSuccess) return 0;
     if (kernels && n) {

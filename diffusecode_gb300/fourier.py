@@ -283,8 +283,9 @@ def four_strucf(xat, uin, vin, win, off, lmn, num, fnum, cfact=None, istl=None, 
 
 def batch_run(crystals, grids, opts, targets=None, weights=None, ctx=None):
     """A population of crystals in one captured launch sequence
-    (dgpu_batch_run).  Returns (dsi list, chi2 array or None, grad_pos list,
-    grad_occ list, device ms of the graph launch)."""
+    (dgpu_batch_run; options outside the graph run member by member).
+    Returns (dsi list, chi2 array or None, grad_pos list, grad_occ list, ms
+    of the graph launch or of the member loop)."""
     ctx = ctx or default_context()
     n = len(crystals)
     crs = (_abi.Crystal * n)(*[c.to_c() for c in crystals])

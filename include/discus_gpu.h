@@ -547,7 +547,12 @@ int dgpu_chi2_grad_device(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid
  * farms one four_run per member) in one persistent launch.  dsi[c] receives
  * crystal c's intensity (host buffer, num(1)*num(2)*num(3) of grids[c]);
  * when i_target != NULL, chi2[c] and the gradients of member c are returned
- * as well (grad_pos[c], grad_occ[c] may be NULL).                           */
+ * as well (grad_pos[c], grad_occ[c] may be NULL).  The population graph
+ * covers EXACT64 phases on the tensor-core engine without <F>, lots,
+ * DISCAMB or anomalous scattering; with any of those (or the CUDA-core
+ * engine) the members run one after another through dgpu_four_run and
+ * dgpu_chi2_grad, with the same outputs, and dgpu_batch_last_ms is the wall
+ * time of that loop.                                                        */
 int dgpu_batch_run(dgpu_ctx *ctx, int32_t ncrystal, const dgpu_crystal *crystals,
                    const dgpu_grid *grids, const dgpu_opts *opts,
                    double *const *dsi,
@@ -558,8 +563,8 @@ int dgpu_batch_run(dgpu_ctx *ctx, int32_t ncrystal, const dgpu_crystal *crystals
 double dgpu_batch_last_ms(const dgpu_ctx *ctx);
 
 /* Nodes (kernels, copies, memsets) and kernel nodes of the graph the last
- * dgpu_batch_run call launched (kernels may be NULL).  Measurement aid; no
- * counterpart in the reference. */
+ * dgpu_batch_run call launched (kernels may be NULL); 0 when it ran member
+ * by member.  Measurement aid; no counterpart in the reference. */
 int64_t dgpu_batch_graph_nodes(const dgpu_ctx *ctx, int64_t *kernels);
 
 /* Device time of the tensor-core type-sum kernel alone in the last

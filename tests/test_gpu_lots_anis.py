@@ -137,14 +137,29 @@ def test_gradient_anisotropic(oracle, ctx, engine):
     assert np.max(np.abs(go - ogo)) <= 2e-4 * np.abs(ogo).max()
 
 
-def test_batch_rejects_lots(ctx):
-    """Lots stay with dgpu_four_run (anisotropic members are batched:
-    test_batch_anisotropic_members)."""
-    cr, g = S.small_lots_anis(anis=True)
-    with pytest.raises(Exception) as e:
-        FR.batch_run([cr], [g], K.opts(phase=_abi.PHASE_EXACT64, ilots=_abi.LOT_BOX, ls_xyz=(3, 2, 2), lot_all=1),
-                     ctx=ctx)
-    assert getattr(e.value, "code", None) == _abi.DGPU_ERR_UNSUPPORTED
+def test_batch_member_path_for_lots_and_average(ctx):
+    """Options outside the population graph (lots, <F>) run member by member
+    through dgpu_four_run / dgpu_chi2_grad: the same intensities and chi^2
+    as those single-crystal calls, the same gradients to FP64 rounding, and
+    no graph."""
+    from diffusecode_gb300.autograd import chi2_grad
+    pop = [S.small_lots_anis(anis=a, icc=icc, inc=(9, 9, 3)) for a, icc in ((True, (6, 5, 4)), (False, (5, 5, 5)))]
+    crs, grids = [p[0] for p in pop], [p[1] for p in pop]
+    for op in (K.opts(phase=_abi.PHASE_EXACT64, ilots=_abi.LOT_BOX, ls_xyz=(3, 2, 2), lot_all=1, ldbw=1),
+               K.opts(phase=_abi.PHASE_EXACT64, fave=1.0, ldbw=1)):
+        targets = [FR.four_run(c, g, K.opts(phase=_abi.PHASE_EXACT64, engine=_abi.ENGINE_DIRECT), ctx=ctx).dsi
+                   for c, g in zip(crs, grids)]
+        weights = [1.0 / (t + 1.0) for t in targets]
+        dsi, c2, gp, go, ms = FR.batch_run(crs, grids, op, targets=targets, weights=weights, ctx=ctx)
+        assert ms > 0 and FR.batch_graph_nodes(ctx=ctx) == (0, 0)
+        for k, (c, g) in enumerate(zip(crs, grids)):
+            one = FR.four_run(c, g, op, ctx=ctx).dsi
+            np.testing.assert_array_equal(dsi[k], one)
+            oc2, ogp, ogo, _ = chi2_grad(c, g, op, targets[k], weights[k], ctx=ctx)
+            assert c2[k] == oc2
+            # the lot gradient adds per-atom sums atomically: same values to FP64 rounding
+            np.testing.assert_allclose(gp[k], ogp, rtol=1e-12, atol=1e-12 * np.abs(ogp).max())
+            np.testing.assert_allclose(go[k], ogo, rtol=1e-12, atol=1e-12 * np.abs(ogo).max())
 
 
 def test_lots_tc_several_slices(oracle, ctx):
