@@ -118,23 +118,23 @@ template <bool RUN>
 __device__ __forceinline__ void refine_loop(int64_t lo, int64_t hi, const uint64_t *__restrict__ ph0,
                                             const uint64_t *__restrict__ du, const uint64_t *__restrict__ dv,
                                             const uint64_t *__restrict__ dw, const float *__restrict__ w,
-                                            const float2 *__restrict__ tab, const uint32_t (&n0)[RF_PTS],
-                                            const uint32_t (&n1)[RF_PTS], const uint32_t (&n2)[RF_PTS],
-                                            const bool (&stp)[RF_PTS], double (&acc)[RF_PTS][2],
-                                            float (&chk)[RF_PTS][2], int sa, bool f0, bool f1, bool f2)
+                                            const float2 *__restrict__ tab, const uint32_t (*sn)[3],
+                                            const int32_t *sstp, double (*acc)[RF_NT], float (&chk)[RF_PTS][2],
+                                            int sa, bool f0, bool f1, bool f2)
 {
+    const uint32_t m0 = sn[0][0], m1 = sn[0][1], m2 = sn[0][2];
     int c = 0;
     for (int64_t a = lo + threadIdx.x; a < hi; a += RF_NT) {
         // an axis of extent 1 has n = 0 at every point: its step is not read
         const uint64_t b = ph0[a] + RF_ROUND, d0 = f0 ? du[a] : 0, d1 = f1 ? dv[a] : 0, d2 = f2 ? dw[a] : 0;
         const uint64_t ds = sa == 0 ? d0 : sa == 1 ? d1 : d2;
         const float wa = w[a], wk = wa * RF_KAPPA, wc = wa * (-0.5f * RF_KAPPA * RF_KAPPA);
-        uint64_t ph = b + (uint64_t)n0[0] * d0 + (uint64_t)n1[0] * d1 + (uint64_t)n2[0] * d2;
+        uint64_t ph = b + (uint64_t)m0 * d0 + (uint64_t)m1 * d1 + (uint64_t)m2 * d2;
 #pragma unroll
         for (int k = 0; k < RF_PTS; k++) {
             if (k > 0) {
-                if (RUN || stp[k]) ph += ds;
-                else ph = b + (uint64_t)n0[k] * d0 + (uint64_t)n1[k] * d1 + (uint64_t)n2[k] * d2;
+                if (RUN || sstp[k]) ph += ds;
+                else ph = b + (uint64_t)sn[k][0] * d0 + (uint64_t)sn[k][1] * d1 + (uint64_t)sn[k][2] * d2;
             }
             phasor_tab_acc(ph, tab, wa, wk, wc, chk[k][0], chk[k][1]);
         }
@@ -142,8 +142,8 @@ __device__ __forceinline__ void refine_loop(int64_t lo, int64_t hi, const uint64
             c = 0;
 #pragma unroll
             for (int k = 0; k < RF_PTS; k++) {
-                acc[k][0] += (double)chk[k][0];
-                acc[k][1] += (double)chk[k][1];
+                acc[2 * k][threadIdx.x] += (double)chk[k][0];
+                acc[2 * k + 1][threadIdx.x] += (double)chk[k][1];
                 chk[k][0] = chk[k][1] = 0.f;
             }
         }
@@ -151,8 +151,10 @@ __device__ __forceinline__ void refine_loop(int64_t lo, int64_t hi, const uint64
 }
 
 // out[((k * ntype + t) * nsl + s)]: the type-t sum over atom slice s at
-// listed point k (box coordinates from the list entry)
-__global__ void __launch_bounds__(RF_NT, 2)
+// listed point k (box coordinates from the list entry).  The FP64 sums of
+// the chunks live in shared memory (one column per thread): 3 blocks of 256
+// threads per SM.
+__global__ void __launch_bounds__(RF_NT, 3)
 k_refine_sums(const int32_t *__restrict__ list, int32_t npts, BoxSpec box, const uint64_t *__restrict__ ph0,
               const uint64_t *__restrict__ du, const uint64_t *__restrict__ dv, const uint64_t *__restrict__ dw,
               const float *__restrict__ w, const float2 *__restrict__ gtab, const RefineTypes rt, int32_t nsl,
@@ -160,14 +162,17 @@ k_refine_sums(const int32_t *__restrict__ list, int32_t npts, BoxSpec box, const
 {
     __shared__ double red[RF_NT / 32][RF_PTS][2];
     __shared__ float2 tab[RF_TAB];
+    __shared__ double acc[2 * RF_PTS][RF_NT];
     for (int j = threadIdx.x; j < RF_TAB; j += RF_NT) tab[j] = gtab[j];
+#pragma unroll
+    for (int k = 0; k < 2 * RF_PTS; k++) acc[k][threadIdx.x] = 0.0;
     const int64_t item = blockIdx.x;
     const int s = (int)(item % nsl);
     const int t = (int)((item / nsl) % rt.ntype);
     const int pg = (int)(item / ((int64_t)nsl * rt.ntype));
     const int64_t lo = rt.ts[t] + (int64_t)s * RF_SLICE;
     const int64_t hi = min(rt.ts[t + 1], lo + RF_SLICE);
-    // the points' box coordinates; stp[k]: point k is point k-1 plus one step along axis sa
+    // the points' box coordinates; s_stp[k]: point k is point k-1 plus one step along axis sa
     __shared__ uint32_t s_n[RF_PTS][3];
     __shared__ int32_t s_stp[RF_PTS];
     if (threadIdx.x < RF_PTS) {
@@ -185,32 +190,22 @@ k_refine_sums(const int32_t *__restrict__ list, int32_t npts, BoxSpec box, const
         s_stp[k] = st;
     }
     __syncthreads();
-    uint32_t n0[RF_PTS], n1[RF_PTS], n2[RF_PTS];
-    bool stp[RF_PTS];
-#pragma unroll
-    for (int k = 0; k < RF_PTS; k++) {
-        n0[k] = s_n[k][0];
-        n1[k] = s_n[k][1];
-        n2[k] = s_n[k][2];
-        stp[k] = s_stp[k] != 0;
-    }
-    double acc[RF_PTS][2];
     float chk[RF_PTS][2];
 #pragma unroll
-    for (int k = 0; k < RF_PTS; k++) acc[k][0] = acc[k][1] = chk[k][0] = chk[k][1] = 0.f;
+    for (int k = 0; k < RF_PTS; k++) chk[k][0] = chk[k][1] = 0.f;
     bool run = true;                 // every point the previous one plus one step along axis sa
 #pragma unroll
-    for (int k = 1; k < RF_PTS; k++) run = run && stp[k];
+    for (int k = 1; k < RF_PTS; k++) run = run && s_stp[k] != 0;
     const bool f0 = box.f[0] > 1, f1 = box.f[1] > 1, f2 = box.f[2] > 1;
     if (run)
-        refine_loop<true>(lo, hi, ph0, du, dv, dw, w, tab, n0, n1, n2, stp, acc, chk, sa, f0, f1, f2);
+        refine_loop<true>(lo, hi, ph0, du, dv, dw, w, tab, s_n, s_stp, acc, chk, sa, f0, f1, f2);
     else
-        refine_loop<false>(lo, hi, ph0, du, dv, dw, w, tab, n0, n1, n2, stp, acc, chk, sa, f0, f1, f2);
+        refine_loop<false>(lo, hi, ph0, du, dv, dw, w, tab, s_n, s_stp, acc, chk, sa, f0, f1, f2);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < RF_PTS; k++) {
-        const double x = warp_sum(acc[k][0] + (double)chk[k][0]);
-        const double y = warp_sum(acc[k][1] + (double)chk[k][1]);
+        const double x = warp_sum(acc[2 * k][threadIdx.x] + (double)chk[k][0]);
+        const double y = warp_sum(acc[2 * k + 1][threadIdx.x] + (double)chk[k][1]);
         if (lane == 0) {
             red[wid][k][0] = x;
             red[wid][k][1] = y;
