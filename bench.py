@@ -541,13 +541,13 @@ def adjoint_measure(ctx, engine, steps=3, check=True):
 
 # k_direct: thread instructions per computed (atom, point) pair, from the ncu
 # capture of one launch on the 108 000-atom alloy, 61^3 grid
-# (smsp__sass_thread_inst_executed.sum 5.9635e11 / 108 000 x 115 351 pairs)
-DIRECT_INST_PER_PAIR = 47.87
+# (smsp__sass_thread_inst_executed.sum 4.41707e11 / 108 000 x 115 351 pairs)
+DIRECT_INST_PER_PAIR = 35.46
 
 
 def direct_roofline(pairs_computed, kernel_ms, pk):
     """The CUDA-core engine is bound by instruction issue (FP32 pipe and the
-    sin/cos polynomial): 152 SMs x 4 schedulers x 1 warp instruction per
+    table-driven phasor): 152 SMs x 4 schedulers x 1 warp instruction per
     clock at the maximum SM clock; achieved = the kernel's thread
     instructions per second (computed pairs x instructions per pair)."""
     sms, clk = 152, pk.get("sm_max_mhz", 2070.0) * 1e6

@@ -92,7 +92,7 @@ extern "C" int dgpu_ctx_destroy(dgpu_ctx *c)
                       &c->flag, &c->tc_part, &c->tc_work, &c->tc_mult, &c->tc_vimg, &c->adj_qimg,
                       &c->adj_items, &c->gq, &c->gpart, &c->grad, &c->batch_desc, &c->batch_aux,
                       &c->ianis, &c->geff, &c->ghist, &c->lpos, &c->ltype, &c->locc, &c->lplan, &c->lfac,
-                      &c->wbuf, &c->acc_csf, &c->acc_dsi, &c->slab_ph0, &c->rlist, &c->rsum, &c->tc_tab,
+                      &c->wbuf, &c->acc_csf, &c->acc_dsi, &c->slab_ph0, &c->rlist, &c->rsum, &c->tc_tab, &c->ph_tab,
                       &c->aidx, &c->aaidx, &c->isymb, &c->dtab, &c->lorig};
     for (DevBuf *b : bufs) b->release();
     c->stage.release();

@@ -115,6 +115,7 @@ struct dgpu_ctx {
     DevBuf tc_part, tc_work, aidx;          // aidx: original atom index of each prepared slot
     DevBuf tc_mult;                         // per-atom step factors of the tensor-core engine
     DevBuf tc_tab;                          // exp(2 pi i k / 4096), FP64, for the step factors
+    DevBuf ph_tab;                          // exp(2 pi i j / 1024), FP32, the CUDA-core phasor table
     DevBuf tc_vimg;                         // V operand images of the tensor-core engine
     DevBuf adj_qimg, adj_items;             // tensor-core adjoint: Q images, work items
     int64_t ts_main[2 * 64 + 4] = {};      // type ranges of the last main atom preparation

@@ -3,7 +3,8 @@
 // Replaces the hot loop of four_strucf_omp (discus/prog/four_strucf_OMP_mod.f90:155-182):
 // for every grid point of the computed box and every atom of a type,
 // phase = ph0 + n0*d0 + n1*d1 + n2*d2 (64-bit fixed point, exact mod 1),
-// then sin/cos(2 pi phase) in FP32 (sincospif) accumulated in FP32 over one
+// then w exp(2 pi i phase) in FP32 by table-driven angle addition
+// (dgpu_phasor.cuh, the table in shared memory) accumulated in FP32 over one
 // shared-memory chunk of atoms and in FP64 across chunks.  Each thread owns
 // Q consecutive points along one grid axis, so consecutive points differ by
 // one 64-bit add.  In REF22 mode the phase keeps only its top 16 bits, the
@@ -13,6 +14,7 @@
 // atom type.  Each (type, slice) writes its own partial sum part[t][s][p];
 // the combine kernel adds the slices in a fixed order (deterministic).
 #include "dgpu_internal.h"
+#include "dgpu_phasor.cuh"
 
 #define DIR_NT 128
 #define DIR_Q 8
@@ -32,10 +34,13 @@ template <bool REF>
 __global__ void __launch_bounds__(DIR_NT)
 k_direct(const uint64_t *__restrict__ ph0, const uint64_t *__restrict__ du,
          const uint64_t *__restrict__ dv, const uint64_t *__restrict__ dw,
-         const float *__restrict__ w, const DirectGeom g, double2 *__restrict__ part)
+         const float *__restrict__ w, const float2 *__restrict__ gtab, const DirectGeom g,
+         double2 *__restrict__ part)
 {
     __shared__ uint64_t s_b[DIR_NT], s_d0[DIR_NT], s_d1[DIR_NT], s_d2[DIR_NT];
     __shared__ float s_w[DIR_NT];
+    __shared__ float2 tab[PH_TAB];
+    for (int j = threadIdx.x; j < PH_TAB; j += DIR_NT) tab[j] = gtab[j];
 
     const int t = blockIdx.z, s = blockIdx.y;
     const int64_t a_lo = g.ts[t] + (int64_t)s * g.slice_len;
@@ -64,7 +69,7 @@ k_direct(const uint64_t *__restrict__ ph0, const uint64_t *__restrict__ du,
         if (threadIdx.x < cnt) {
             int64_t a = base + threadIdx.x;
             uint64_t d[3] = {du[a], dv[a], dw[a]};
-            s_b[threadIdx.x] = ph0[a];
+            s_b[threadIdx.x] = REF ? ph0[a] : ph0[a] + PH_ROUND;
             s_d0[threadIdx.x] = d[g.a0];
             s_d1[threadIdx.x] = d[g.a1];
             s_d2[threadIdx.x] = d[g.a2];
@@ -80,14 +85,13 @@ k_direct(const uint64_t *__restrict__ ph0, const uint64_t *__restrict__ du,
         for (int j = 0; j < cnt; j++) {
             const uint64_t d0 = s_d0[j];
             uint64_t ph = s_b[j] + m0 * d0 + m1 * s_d1[j] + m2 * s_d2[j];
-            const float wj = s_w[j];
+            const PhWeight wj = ph_weight(s_w[j]);
 #pragma unroll
             for (int k = 0; k < DIR_Q; k++) {
-                uint64_t q = REF ? (ph & 0xFFFF000000000000ull) : ph;
-                float x = (float)(int32_t)(q >> 32) * 4.656612873077393e-10f;   // turns * 2
-                float sn, cs;
-                sincospif(x, &sn, &cs);
-                const float y0 = wj * cs, y1 = wj * sn;
+                // REF22: the top 16 bits, the reference's table index, then rounded as any phase
+                const uint64_t q = REF ? (ph & 0xFFFF000000000000ull) + PH_ROUND : ph;
+                const float2 e = ph_phasor(q, tab, wj);
+                const float y0 = e.x, y1 = e.y;
                 const float t0 = accf[k][0] + y0, t1 = accf[k][1] + y1;
                 cmpf[k][0] += y0 - (t0 - accf[k][0]);
                 cmpf[k][1] += y1 - (t1 - accf[k][1]);
@@ -149,9 +153,11 @@ int dgpu_direct_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, con
     if (tiles > 0x7fffffff) return dgpu_set_error(ctx, DGPU_ERR_ARG, "grid too large");
     dim3 grid((unsigned)tiles, (unsigned)nslice, (unsigned)ntype);
     if (ref_mask)
-        k_direct<true><<<grid, DIR_NT, 0, ctx->stream>>>(ph0, du, dv, dw, w, g, part.as<double2>());
+        k_direct<true><<<grid, DIR_NT, 0, ctx->stream>>>(ph0, du, dv, dw, w, ctx->ph_tab.as<float2>(), g,
+                                                         part.as<double2>());
     else
-        k_direct<false><<<grid, DIR_NT, 0, ctx->stream>>>(ph0, du, dv, dw, w, g, part.as<double2>());
+        k_direct<false><<<grid, DIR_NT, 0, ctx->stream>>>(ph0, du, dv, dw, w, ctx->ph_tab.as<float2>(), g,
+                                                          part.as<double2>());
     DGPU_CUDA(ctx, cudaGetLastError());
     *nslice_out = nslice;
     return DGPU_OK;

@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "dgpu_form.cuh"
+#include "dgpu_phasor.cuh"
 #include "tc_ptx.cuh"
 
 #define RF_PTS 8            // points per work item (each atom's data is read once for all of them)
@@ -36,13 +37,6 @@
 #define RF_CHUNK 16         // atoms per FP32 partial before it is added in FP64 (at the most coherent
                             // points FP32 chunks of 32 atoms round alike chunk after chunk: 1.8e-5)
 #define RF_SLICE 65536      // atoms per work item
-#define RF_TAB 1024         // table angles 2 pi j / RF_TAB
-#define RF_ROUND ((1ull << 53) + (1ull << 30))   // added to a phase: table index and remainder rounded to nearest
-
-// radians per unit of the 23-bit remainder (2 pi / 2^33) and -(that)^2 / 6
-#define RF_KAPPA (3.14159265358979f * 0x1p-32f)
-#define RF_S6 (-(RF_KAPPA * RF_KAPPA) / 6.0f)
-
 struct RefineTypes {
     int64_t ts[65];         // type ranges of a prepared atom set (0-based types)
     double n[64];           // atoms per type
@@ -82,35 +76,6 @@ __device__ __forceinline__ double warp_sum(double v)
     return v;
 }
 
-// exp(2 pi i j / RF_TAB), FP64 rounded to FP32
-__global__ void k_refine_table(float2 *__restrict__ tab)
-{
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= RF_TAB) return;
-    double s, c;
-    sincospi((double)j * (2.0 / RF_TAB), &s, &c);
-    tab[j] = make_float2((float)c, (float)s);
-}
-
-// (x, y) += w exp(2 pi i ph / 2^64), ph carrying the offset RF_ROUND: the
-// top 10 bits select the table angle T, the next 23 bits (less 2^22) give
-// the remainder d in units of RF_KAPPA, |d| <= pi / 1024 rad, and
-// exp(i d) = 1 - d^2/2 + i d (1 - d^2/6) to within 4e-12.  w T is formed
-// exactly inside the last FMA, so a weighted phasor is rounded once (plus
-// the table's own rounding) before it enters the FP32 chunk sum.
-// wk = w RF_KAPPA, wc = -w RF_KAPPA^2 / 2.
-__device__ __forceinline__ void phasor_tab_acc(uint64_t ph, const float2 *__restrict__ tab, float wa, float wk,
-                                               float wc, float &x, float &y)
-{
-    const float2 T = tab[(uint32_t)(ph >> 54)];
-    const float d = __uint_as_float(((uint32_t)(ph >> 31) & 0x7FFFFFu) | 0x4B000000u) - 12582912.0f;
-    const float d2 = d * d;
-    const float v = (wk * d) * fmaf(d2, RF_S6, 1.0f);          // w sin(d)
-    const float u = d2 * wc;                                    // w (cos(d) - 1)
-    x += fmaf(T.x, wa, fmaf(T.x, u, -T.y * v));
-    y += fmaf(T.y, wa, fmaf(T.y, u, T.x * v));
-}
-
 // The atoms of one work item: FP32 sums of RF_CHUNK atoms per point, added
 // to FP64.  RUN: the points are consecutive along the step axis sa and
 // their phases one 64-bit add apart.
@@ -126,9 +91,9 @@ __device__ __forceinline__ void refine_loop(int64_t lo, int64_t hi, const uint64
     int c = 0;
     for (int64_t a = lo + threadIdx.x; a < hi; a += RF_NT) {
         // an axis of extent 1 has n = 0 at every point: its step is not read
-        const uint64_t b = ph0[a] + RF_ROUND, d0 = f0 ? du[a] : 0, d1 = f1 ? dv[a] : 0, d2 = f2 ? dw[a] : 0;
+        const uint64_t b = ph0[a] + PH_ROUND, d0 = f0 ? du[a] : 0, d1 = f1 ? dv[a] : 0, d2 = f2 ? dw[a] : 0;
         const uint64_t ds = sa == 0 ? d0 : sa == 1 ? d1 : d2;
-        const float wa = w[a], wk = wa * RF_KAPPA, wc = wa * (-0.5f * RF_KAPPA * RF_KAPPA);
+        const PhWeight wa = ph_weight(w[a]);
         uint64_t ph = b + (uint64_t)m0 * d0 + (uint64_t)m1 * d1 + (uint64_t)m2 * d2;
 #pragma unroll
         for (int k = 0; k < RF_PTS; k++) {
@@ -136,7 +101,9 @@ __device__ __forceinline__ void refine_loop(int64_t lo, int64_t hi, const uint64
                 if (RUN || sstp[k]) ph += ds;
                 else ph = b + (uint64_t)sn[k][0] * d0 + (uint64_t)sn[k][1] * d1 + (uint64_t)sn[k][2] * d2;
             }
-            phasor_tab_acc(ph, tab, wa, wk, wc, chk[k][0], chk[k][1]);
+            const float2 e = ph_phasor(ph, tab, wa);
+            chk[k][0] += e.x;
+            chk[k][1] += e.y;
         }
         if (++c == RF_CHUNK) {
             c = 0;
@@ -161,9 +128,9 @@ k_refine_sums(const int32_t *__restrict__ list, int32_t npts, BoxSpec box, const
               int32_t sa, double2 *__restrict__ out)
 {
     __shared__ double red[RF_NT / 32][RF_PTS][2];
-    __shared__ float2 tab[RF_TAB];
+    __shared__ float2 tab[PH_TAB];
     __shared__ double acc[2 * RF_PTS][RF_NT];
-    for (int j = threadIdx.x; j < RF_TAB; j += RF_NT) tab[j] = gtab[j];
+    for (int j = threadIdx.x; j < PH_TAB; j += RF_NT) tab[j] = gtab[j];
 #pragma unroll
     for (int k = 0; k < 2 * RF_PTS; k++) acc[k][threadIdx.x] = 0.0;
     const int64_t item = blockIdx.x;
@@ -300,14 +267,14 @@ int dgpu_refine_aver(dgpu_ctx *ctx, const RefineSpec &r, double2 *csf, double2 *
     RefineTypes rm, ra;
     fill_types(rm, r.ts_main, r.ngroup);
     fill_types(ra, r.ts_fold, r.nscat);
-    // two FormSpec blocks, the phasor table, the point list and its count
-    const size_t fsb = (sizeof(FormSpec) + 255) & ~(size_t)255, tb = RF_TAB * sizeof(float2);
-    DGPU_CUDA(ctx, ctx->rlist.ensure(2 * fsb + tb + 256 + (size_t)nb * sizeof(int32_t)));
+    // two FormSpec blocks, the point list and its count
+    const size_t fsb = (sizeof(FormSpec) + 255) & ~(size_t)255;
+    DGPU_CUDA(ctx, ctx->rlist.ensure(2 * fsb + 256 + (size_t)nb * sizeof(int32_t)));
     FormSpec *d_fsm = ctx->rlist.as<FormSpec>();
     FormSpec *d_fst = (FormSpec *)((char *)ctx->rlist.p + fsb);
-    float2 *d_tab = (float2 *)((char *)ctx->rlist.p + 2 * fsb);
-    int32_t *d_count = (int32_t *)((char *)ctx->rlist.p + 2 * fsb + tb);
-    int32_t *d_list = (int32_t *)((char *)ctx->rlist.p + 2 * fsb + tb + 256);
+    int32_t *d_count = (int32_t *)((char *)ctx->rlist.p + 2 * fsb);
+    int32_t *d_list = (int32_t *)((char *)ctx->rlist.p + 2 * fsb + 256);
+    const float2 *d_tab = ctx->ph_tab.as<float2>();
     DGPU_CUDA(ctx, cudaMemcpyAsync(d_fsm, r.fsm, sizeof(FormSpec), cudaMemcpyHostToDevice, ctx->stream));
     DGPU_CUDA(ctx, cudaMemcpyAsync(d_fst, r.fst, sizeof(FormSpec), cudaMemcpyHostToDevice, ctx->stream));
     DGPU_CUDA(ctx, cudaMemsetAsync(d_count, 0, sizeof(int32_t), ctx->stream));
@@ -352,8 +319,6 @@ int dgpu_refine_aver(dgpu_ctx *ctx, const RefineSpec &r, double2 *csf, double2 *
                                        ctx->stream));
         DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));   // h is a host temporary
     }
-    k_refine_table<<<RF_TAB / 256, 256, 0, ctx->stream>>>(d_tab);
-    DGPU_CUDA(ctx, cudaGetLastError());
     const int32_t nslf = slices_of(rm), nsla = slices_of(ra);
     const int64_t ngrp = dgpu_cdiv(npts, RF_PTS);
     DGPU_CUDA(ctx, ctx->rsum.ensure((size_t)npts * ((size_t)r.ngroup * nslf + (size_t)r.nscat * nsla) *

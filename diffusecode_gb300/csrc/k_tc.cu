@@ -89,6 +89,7 @@
 #define TC_V_SCALE 4096.0f
 #define TC_UNSCALE (1.0f / 4096.0f)
 
+#include "dgpu_phasor.cuh"
 #include "tc_ptx.cuh"
 
 // barrier among the producer warps only; returns the OR of `stop` over them,
@@ -896,6 +897,14 @@ __global__ void k_tc_tab(double2 *tab)
     tab[k] = make_double2(c, s);
 }
 
+// the CUDA-core engines' phasor table (dgpu_phasor.cuh): exp(2 pi i j / 1024)
+// rounded to FP32, entry 4j of the table above
+__global__ void k_ph_tab(const double2 *__restrict__ tc_tab, float2 *__restrict__ tab)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < PH_TAB) tab[j] = make_float2((float)tc_tab[4 * j].x, (float)tc_tab[4 * j].y);
+}
+
 __device__ __forceinline__ uint64_t mix64(uint64_t z)
 {
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -977,6 +986,9 @@ int dgpu_tc_init(dgpu_ctx *ctx)
 {
     DGPU_CUDA(ctx, ctx->tc_tab.ensure(4096 * sizeof(double2)));
     k_tc_tab<<<16, 256, 0, ctx->stream>>>(ctx->tc_tab.as<double2>());
+    DGPU_CUDA(ctx, cudaGetLastError());
+    DGPU_CUDA(ctx, ctx->ph_tab.ensure(PH_TAB * sizeof(float2)));
+    k_ph_tab<<<PH_TAB / 256, 256, 0, ctx->stream>>>(ctx->tc_tab.as<double2>(), ctx->ph_tab.as<float2>());
     DGPU_CUDA(ctx, cudaGetLastError());
     DGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return DGPU_OK;
