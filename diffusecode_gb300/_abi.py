@@ -60,6 +60,8 @@ LOT_ELI = 3
 PREF_NONE = 0
 PREF_RIETVELD = 1
 PREF_MARCH = 2
+FILTER_OFF = 0
+FILTER_LANCZOS = 1
 HKL_CIF = 1
 HKL_HKLF4 = 4
 OUT_STANDARD = 0
@@ -147,6 +149,10 @@ class Opts(C.Structure):
         ("tc_vimg", C.c_int32),
         ("tc_wait_us", C.c_int32),
         ("discamb", C.POINTER(Discamb)),
+        ("filter", C.c_int32),
+        ("filter_width", C.c_int32),
+        ("filter_damp", C.c_double),
+        ("filter_scale", C.c_double),
     ]
 
 
@@ -253,6 +259,10 @@ def default_opts(**kw):
     o.tc_vimg = 0
     o.tc_wait_us = 0
     o.discamb = C.cast(None, C.POINTER(Discamb))
+    o.filter = FILTER_OFF
+    o.filter_width = 4
+    o.filter_damp = 0.5
+    o.filter_scale = 1.0
     for k, v in kw.items():
         if k in ("aver_cells", "lot_origins"):
             continue

@@ -20,7 +20,7 @@ EXPORTS = [
     "dgpu_batch_run", "dgpu_batch_last_ms", "dgpu_batch_graph_nodes", "dgpu_four_strucf_noalloc", "dgpu_tc_last_kernel_ms",
     "dgpu_four_weight", "dgpu_four_weight_device", "dgpu_four_accumulate", "dgpu_set_symmetry", "dgpu_qval",
     "dgpu_calc_hkl", "dgpu_powder_npkt", "dgpu_powder_complete", "dgpu_chi2_grad_device",
-    "dgpu_calc_hkl_files", "dgpu_output_write",
+    "dgpu_calc_hkl_files", "dgpu_output_write", "dgpu_four_filter",
 ]
 
 
@@ -75,6 +75,7 @@ def load():
     L.dgpu_calc_hkl_files.argtypes = [vp, CR, OP, C.c_char_p, C.c_char_p, C.c_int32, C.c_double, C.c_double,
                                       C.c_double]
     L.dgpu_output_write.argtypes = [C.c_char_p, C.POINTER(_abi.Output), dp, dp, dp, C.c_int64]
+    L.dgpu_four_filter.argtypes = [vp, ip, OP, dp]
     PW = C.POINTER(_abi.Powder)
     L.dgpu_powder_npkt.argtypes = [PW]
     L.dgpu_powder_npkt.restype = C.c_int32

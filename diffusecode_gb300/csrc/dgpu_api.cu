@@ -54,6 +54,10 @@ extern "C" void dgpu_default_opts(dgpu_opts *o)
     o->lot_origins = nullptr;
     o->tc_vimg = 0;
     o->tc_wait_us = 0;
+    o->filter = DGPU_FILTER_OFF;
+    o->filter_width = 4;
+    o->filter_damp = 0.5;
+    o->filter_scale = 1.0;
 }
 
 extern "C" int dgpu_ctx_create(int device, dgpu_ctx **out)
@@ -92,7 +96,7 @@ extern "C" int dgpu_ctx_destroy(dgpu_ctx *c)
                       &c->flag, &c->tc_part, &c->tc_work, &c->tc_mult, &c->tc_vimg, &c->adj_qimg,
                       &c->adj_items, &c->gq, &c->gpart, &c->grad, &c->batch_desc, &c->batch_aux,
                       &c->ianis, &c->geff, &c->ghist, &c->lpos, &c->ltype, &c->locc, &c->lplan, &c->lfac,
-                      &c->wbuf, &c->acc_csf, &c->acc_dsi, &c->slab_ph0, &c->rlist, &c->rsum, &c->tc_tab, &c->ph_tab,
+                      &c->wbuf, &c->acc_csf, &c->acc_dsi, &c->slab_ph0, &c->rlist, &c->rsum, &c->tc_tab, &c->ph_tab, &c->filt, &c->filt_slice,
                       &c->aidx, &c->aaidx, &c->isymb, &c->dtab, &c->lorig};
     for (DevBuf *b : bufs) b->release();
     c->stage.release();
@@ -750,6 +754,9 @@ int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g,
     *ctx->fs_type = fs;
     if (cancelled(op)) return dgpu_set_error(ctx, DGPU_ERR_CANCELLED, "cancelled");
     rc = dgpu_friedel_mirror(ctx, box, idim, d_csf, d_acsf, d_dsi);
+    if (rc) return rc;
+    // the Lanczos filter of dsi (fourier_sup.f90:284-285), before the statistics
+    rc = dgpu_four_filter_dev(ctx, num, op, d_dsi);
     if (rc) return rc;
     double res[7];
     rc = dgpu_qinfo(ctx, g->eck, g->vi, num, d_dsi, res);

@@ -116,6 +116,7 @@ struct dgpu_ctx {
     DevBuf tc_mult;                         // per-atom step factors of the tensor-core engine
     DevBuf tc_tab;                          // exp(2 pi i k / 4096), FP64, for the step factors
     DevBuf ph_tab;                          // exp(2 pi i j / 1024), FP32, the CUDA-core phasor table
+    DevBuf filt, filt_slice;                // Lanczos filter: work fields, sums, pass tables; one slice
     DevBuf tc_vimg;                         // V operand images of the tensor-core engine
     DevBuf adj_qimg, adj_items;             // tensor-core adjoint: Q images, work items
     int64_t ts_main[2 * 64 + 4] = {};      // type ranges of the last main atom preparation
@@ -586,6 +587,8 @@ void dgpu_batch_free(dgpu_ctx *ctx);
 
 // the whole four_run with device-resident crystal arrays and outputs
 int dgpu_stage_crystal(dgpu_ctx *ctx, const dgpu_crystal *cr, dgpu_crystal &dc);
+// do_four_filter on the device array dsi(num) when opts->filter is set (k_filter.cu)
+int dgpu_four_filter_dev(dgpu_ctx *ctx, const int32_t num[3], const dgpu_opts *op, double *d_dsi);
 int dgpu_four_run_dev(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *g, const dgpu_opts *op,
                       double2 *d_csf, double2 *d_acsf, double *d_dsi, dgpu_info *info);
 

@@ -421,6 +421,7 @@ int dgpu_chi2_grad_impl(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_grid *
                         double *grad_occ, dgpu_info *info, bool device)
 {
     if (op->ano) return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "gradient with anomalous scattering");
+    if (op->filter) return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "gradient of a filtered intensity");
     if (op->phase != DGPU_PHASE_EXACT64)
         return dgpu_set_error(ctx, DGPU_ERR_UNSUPPORTED, "gradient needs EXACT64 phases");
     const int64_t n = cr->natoms;

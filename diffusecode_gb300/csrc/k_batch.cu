@@ -481,7 +481,7 @@ static int batch_build(dgpu_ctx *ctx, BatchState &B, int32_t nc, const dgpu_crys
 }
 
 // Options outside the population graph (<F>, lots, DISCAMB, REF22 phases,
-// anomalous scattering, the CUDA-core engine): every member through the
+// anomalous scattering, the CUDA-core engine, the Lanczos filter): every member through the
 // single-crystal entries, with the same outputs.  batch_ms is then the wall
 // time of the loop.
 static int batch_by_member(dgpu_ctx *ctx, int32_t nc, const dgpu_crystal *crs, const dgpu_grid *grids,
@@ -524,7 +524,8 @@ extern "C" int dgpu_batch_run(dgpu_ctx *ctx, int32_t nc, const dgpu_crystal *crs
     for (int c = 0; c < nc; c++)
         if (!dsi[c] || (targets && !i_target[c])) return dgpu_set_error(ctx, DGPU_ERR_ARG, "member %d: buffers", c);
     if (op->phase != DGPU_PHASE_EXACT64 || op->fave != 0.0 || op->ano || op->ilots == DGPU_LOT_BOX ||
-        op->ilots == DGPU_LOT_ELI || op->discamb || op->engine == DGPU_ENGINE_DIRECT || !dgpu_tc_available(ctx))
+        op->ilots == DGPU_LOT_ELI || op->discamb || op->engine == DGPU_ENGINE_DIRECT || op->filter ||
+        !dgpu_tc_available(ctx))
         return batch_by_member(ctx, nc, crs, grids, op, dsi, i_target, weight, chi2, grad_pos, grad_occ);
     ctx->batch_by_member = false;
     if (targets && !chi2) return dgpu_set_error(ctx, DGPU_ERR_ARG, "chi2 output missing");

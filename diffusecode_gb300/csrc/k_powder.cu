@@ -317,6 +317,7 @@ extern "C" int dgpu_powder_complete(dgpu_ctx *ctx, const dgpu_crystal *cr, const
     // anisotropic crystal
     dc.is_anis = 0;
     dgpu_opts op = *opts;
+    op.filter = DGPU_FILTER_OFF;                 // four_run_powder filters no slab
     op.fave = 0.0;
     op.aver_cells = nullptr;
     op.ilots = DGPU_LOT_OFF;

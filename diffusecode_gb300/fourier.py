@@ -167,6 +167,19 @@ def _interleave(z):
     return b
 
 
+def four_filter(dsi, opts: _abi.Opts, ctx=None):
+    """do_four_filter (fourier_sup.f90:1646-1803) on a copy of dsi(num), on
+    the device (dgpu_four_filter): the Lanczos filter set by opts.filter,
+    filter_width, filter_damp, filter_scale."""
+    ctx = ctx or default_context()
+    d = np.asfortranarray(np.asarray(dsi, dtype=np.float64))
+    shape = d.shape + (1,) * (3 - d.ndim)
+    flat = d.reshape(-1, order="F").copy()
+    num = np.asarray(shape, dtype=np.int32)
+    ctx.check(ctx.lib.dgpu_four_filter(ctx.h, _abi.iptr(num), C.byref(opts), _abi.dptr(flat)))
+    return flat.reshape(d.shape, order="F")
+
+
 def qval(cr: CrystalData, grid: GridData, opts: _abi.Opts, value, result: FourierResult, laver=False,
          rand=None, ctx=None):
     """qval (discus/prog/qval.f90:65-290) on the device: the output value of

@@ -179,7 +179,17 @@ typedef struct dgpu_opts {
                                107-118); NULL = off.  Not with <F> subtraction:
                                the reference multiplies its lattice sum by the
                                table of type 0, which does not exist.            */
+    /* Lanczos filter of dsi at the end of four_run (do_four_filter,
+       fourier_sup.f90:284-290,1646-1803; 'set filter,lanczos', fourier.f90:
+       1156-1186; defaults fourier_reset.f90:101-105).                          */
+    int32_t filter;         /* DGPU_FILTER_OFF / DGPU_FILTER_LANCZOS               */
+    int32_t filter_width;   /* four_width m: window |q-g| < m (default 4)           */
+    double  filter_damp;    /* four_damp: sinc(pi (q-g) damp) (default 0.5)          */
+    double  filter_scale;   /* four_rscale (default 1; other values UNSUPPORTED)     */
 } dgpu_opts;
+
+#define DGPU_FILTER_OFF      0
+#define DGPU_FILTER_LANCZOS  1
 
 /* What four_run reports besides the arrays. */
 typedef struct dgpu_info {
@@ -320,6 +330,19 @@ int dgpu_set_symmetry(dgpu_ctx *ctx, int32_t nops, const double *mats);
 
 int dgpu_four_accumulate(dgpu_ctx *ctx, int32_t mode, int32_t symm, const dgpu_grid *grid, double fave,
                          double *csf, double *dsi);
+
+/* do_four_filter (fourier_sup.f90:1646-1803) on a host array dsi(num)
+ * (Fortran order), in place: with filter = LANCZOS the field is convolved
+ * with the windowed sinc kernel the reference builds (do_lanczos_{1,2,3}d_fft,
+ * lib_f90/lib_lanczos.f90), circularly, with the index shifts of its FFT
+ * maps (lib_f90/map_1dtofield.f90), and scaled to the input's sum.  3D grids
+ * with an extent <= 2 width + 1 are filtered in 2D slices as the reference
+ * does; planes must span axes 1-2 and lines axis 1 (where the reference
+ * reads outside its kernel table otherwise: DGPU_ERR_UNSUPPORTED, as for a
+ * filtered extent below 2 width + 3, or 2 width + 4 when even).
+ * dgpu_four_run applies it to dsi before the statistics; this entry is for
+ * the caller's dsi3d copy (fourier_sup.f90:287-290, fave == 0).            */
+int dgpu_four_filter(dgpu_ctx *ctx, const int32_t num[3], const dgpu_opts *opts, double *dsi);
 
 /* ---- output values ------------------------------------------------------- */
 /* qval (discus/prog/qval.f90:65-290): the value the output menu writes at a
