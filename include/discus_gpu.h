@@ -422,9 +422,9 @@ int dgpu_calc_hkl_files(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *
  *             unless it ends in it; the output range (lrange ...) applies.
  * values: qval's array for `value` over inc (Fortran order, nvalues =
  * inc1 inc2 inc3; VTK: dsi).  ampl/phase: qval's arrays for values 2 and 3
- * (SHELX formats; HKLF4 needs no phase on 2D/3D grids).  PGM and PPM are
- * disabled in the reference, HDF5 and NeXus need libraries this build does
- * not link, postscript is a plot: DGPU_ERR_UNSUPPORTED.                      */
+ * (SHELX formats; HKLF4 needs no phase on 2D/3D grids).  PGM, PPM and
+ * postscript are disabled in the reference (error -6), HDF5 and NeXus need
+ * libraries this build does not link: DGPU_ERR_UNSUPPORTED.                 */
 #define DGPU_OUT_STANDARD  0
 #define DGPU_OUT_GNUPLOT   3
 #define DGPU_OUT_HKLF4     6
