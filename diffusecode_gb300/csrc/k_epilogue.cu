@@ -507,14 +507,25 @@ __global__ void k_lot_combine(int32_t ngroup, int32_t nlot, BoxSpec box, const P
     dsi[idx] += acc;
 }
 
+// (hi, lo) += x in float-float: Knuth's TwoSum, the error carried in lo
+__device__ __forceinline__ void ff_add(float &hi, float &lo, float x)
+{
+    const float s = hi + x, bp = s - hi;
+    lo += (hi - (s - bp)) + (x - bp);
+    hi = s;
+}
+
 // k_lot_combine for FP32 partials with nq = ngroup * nslice partials per lot
 // known at compile time: partial q = g * nslice + k of lot L sits at
 // (L * NQ + q) * slab, and LB lots' partials are loaded before any is used,
 // so that each thread keeps about eight loads in flight (the kernel reads
 // nlot * nq partials per point and is bound by those reads).  The arithmetic
 // is the generic kernel's, operation for operation: a group's slices are
-// added first, then multiplied by its factor.
-template <int NQ>
+// added first, then multiplied by its factor.  Without <F> (AV false) F of a
+// lot is an FP32 pair and |F|^2 is summed over the lots in float-float (exact
+// FMA products, TwoSum, 48-bit significands) rather than FP64, whose rate on
+// this part made that sum the kernel's bound; F - <F> keeps FP64.
+template <int NQ, bool AV>
 __global__ void k_lot_combine_f32(int32_t nslice, int32_t nlot, BoxSpec box, const float2 *__restrict__ part,
                                   PartLayout lay, const double2 *__restrict__ fac, const double2 *__restrict__ acsf,
                                   double2 *__restrict__ csf, double *__restrict__ dsi, int32_t last)
@@ -526,7 +537,7 @@ __global__ void k_lot_combine_f32(int32_t nslice, int32_t nlot, BoxSpec box, con
     const int64_t nb = (int64_t)box.f[0] * box.f[1] * box.f[2];
     const int64_t pb = i + (int64_t)box.f[0] * (j + (int64_t)box.f[1] * l);
     const int64_t idx = i + (int64_t)box.num[0] * (j + (int64_t)box.num[1] * l);
-    const double2 a = acsf ? acsf[idx] : make_double2(0.0, 0.0);
+    const double2 a = AV ? acsf[idx] : make_double2(0.0, 0.0);
     const float2 *p0 = part + i * lay.s0 + j * lay.s1 + l * lay.s2;
     const int64_t slab = lay.slab;
     float2 fq[NQ];                         // the group factor of each partial of a lot
@@ -536,6 +547,7 @@ __global__ void k_lot_combine_f32(int32_t nslice, int32_t nlot, BoxSpec box, con
         fq[q] = make_float2((float)f.x, (float)f.y);
     }
     double acc = 0.0;
+    float ah = 0.f, al = 0.f;              // float-float sum of |F|^2 (AV false)
     for (int L0 = 0; L0 < nlot; L0 += LB) {
         float2 v[LB][NQ];
 #pragma unroll
@@ -560,13 +572,22 @@ __global__ void k_lot_combine_f32(int32_t nslice, int32_t nlot, BoxSpec box, con
                         si = 0.f;
                     }
                 }
-                const double2 F = make_double2((double)fr - a.x, (double)fi - a.y);
-                acc += F.x * F.x + F.y * F.y;
-                if (L0 + b == last) csf[idx] = F;
+                if (AV) {
+                    const double2 F = make_double2((double)fr - a.x, (double)fi - a.y);
+                    acc += F.x * F.x + F.y * F.y;
+                    if (L0 + b == last) csf[idx] = F;
+                } else {
+                    const float pr = fr * fr, pi = fi * fi;
+                    const float er = fmaf(fr, fr, -pr), ei = fmaf(fi, fi, -pi);   // exact product errors
+                    ff_add(ah, al, pr);
+                    ff_add(ah, al, pi);
+                    al += er + ei;
+                    if (L0 + b == last) csf[idx] = make_double2((double)fr, (double)fi);
+                }
             }
         }
     }
-    dsi[idx] += acc;
+    dsi[idx] += AV ? acc : (double)ah + (double)al;
 }
 
 // dsi *= dscale, csf *= cscale on the box (lot normalisation and diff_scale)
@@ -611,7 +632,12 @@ int dgpu_lot_combine(dgpu_ctx *ctx, int32_t ngroup, int32_t nlot, const BoxSpec 
         switch (nq) {
 #define LOT_F32(Q)                                                                                              \
     case Q:                                                                                                     \
-        k_lot_combine_f32<Q><<<nblk, 256, 0, ctx->stream>>>(nslice, nlot, box, p, lay, fac, acsf, csf, dsi, last); \
+        if (acsf)                                                                                               \
+            k_lot_combine_f32<Q, true><<<nblk, 256, 0, ctx->stream>>>(nslice, nlot, box, p, lay, fac, acsf, csf,  \
+                                                                      dsi, last);                               \
+        else                                                                                                    \
+            k_lot_combine_f32<Q, false><<<nblk, 256, 0, ctx->stream>>>(nslice, nlot, box, p, lay, fac, acsf, csf, \
+                                                                       dsi, last);                              \
         break;
             LOT_F32(1) LOT_F32(2) LOT_F32(3) LOT_F32(4) LOT_F32(5) LOT_F32(6) LOT_F32(7) LOT_F32(8)
 #undef LOT_F32
