@@ -9,7 +9,7 @@ the index maps maptofftfd / mapfftfdtoline (lib_f90/map_1dtofield.f90:39-62,
 with the reference's 1-based loops, the forward maps, numpy's unnormalised
 forward FFT for FFTW_FORWARD (applied a second time for the "back" FFT, as
 the reference does), the back maps, the weight and the sum normalisation.
-Parity unpinned: no Fortran compiler here or on the GPU machine.
+Parity unpinned: no Fortran compiler is available to run the reference's filter.
 """
 import math
 

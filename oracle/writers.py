@@ -17,7 +17,7 @@ Each writer follows the reference routine it names:
   mrc_write                 lib_f90/mrc_data.f90:19-139
   xplor_write               discus/prog/discus_xplor.f90:16-139
   calc_hkl (files)          discus/prog/fourier_sup.f90:3230-3549
-Parity unpinned: no Fortran compiler here or on the GPU machine to run them.
+Parity unpinned: no Fortran compiler is available to run the reference's writers.
 """
 import math
 import struct
