@@ -337,3 +337,20 @@ def test_oracle_header_angles_closed_form():
     assert math.isclose(ang[0], (math.pi / 2) / float(np.float32(math.pi / 180)), rel_tol=1e-15)
     assert W.F(12, 5, ang[0]) == "    90.00000" and ang[1:] == (90.0, 90.0)
     assert math.isclose(avr[0], 1.0)
+
+
+def test_shelx_overflow_and_scaling_bring_values_into_the_field(lib, tmp_path):
+    """HKLF4's F8.2 overflows to asterisks for large intensities, as the
+    reference's records do; scaling by the largest reflection (valmax -2)
+    brings them back into the field."""
+    g = shelx_grid((5, 4, 3))
+    cr = Cr(icc=(1, 1, 1))
+    amp = np.full(g.inc, 2000.0)                 # |F|^2 = 4e6 per cell: beyond F8.2
+    ph = np.zeros(g.inc)
+    p, fac = ours(tmp_path, "big", "hklf4", g, amp, amp, ph, cr=cr, value=2)
+    got = open(p, "rb").read()
+    assert b"********" in got
+    assert got == W.other(oracle_spec(6, g, value=2, rten=RTEN.reshape(-1, order="F"), icc=cr.icc),
+                          flat(amp), flat(amp), flat(ph))[0]
+    p2, fac2 = ours(tmp_path, "scaled", "hklf4", g, amp, amp, ph, cr=cr, value=2, valmax=-2.0)
+    assert fac2 == 10.0 ** -3 and b"*" not in open(p2, "rb").read()
