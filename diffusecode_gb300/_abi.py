@@ -72,6 +72,7 @@ OUT_LIST9 = 8
 OUT_NIPL3D = 9
 OUT_VTK = 11
 OUT_MRC = 12
+OUT_HDF5 = 13
 OUT_XPLOR = 14
 
 _dp = C.POINTER(C.c_double)
@@ -321,4 +322,7 @@ class Output(C.Structure):
         ("name", C.c_char_p),
         ("nipl", C.POINTER(Nipl)),
         ("out_fac", C.c_double),
+        ("a0", C.c_double * 3),
+        ("win", C.c_double * 3),
+        ("scale", C.c_double),
     ]

@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "../../include/discus_gpu.h"
+#include "hdf5_yell.h"
 
 namespace {
 
@@ -821,6 +822,7 @@ int dgpu_output_write(const char *path, dgpu_output *out, const double *values, 
     case DGPU_OUT_LIST9:
     case DGPU_OUT_NIPL3D: return write_other(path, out, values, ampl, phase);
     case DGPU_OUT_MRC: return write_mrc(path, out, values);
+    case DGPU_OUT_HDF5: return dgpu_hdf5::write_yell(path, out, values);
     case DGPU_OUT_XPLOR: return write_xplor(path, out, values);
     default: return DGPU_ERR_UNSUPPORTED;
     }

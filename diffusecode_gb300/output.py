@@ -3,7 +3,7 @@
 library, the values come from qval on the device).
 
 Mirrors discus/prog/graphic.f90's `output` menu: `format` is the menu's
-format (standard, gnuplot, hklf4, list5, list9, 3d, vtk, mrc, xplor), the
+format (standard, gnuplot, hklf4, list5, list9, 3d, vtk, mrc, hdf5, xplor), the
 grid the last Fourier's (out_inc, out_eck, out_vi), `value` the qval code.
 """
 import ctypes as C
@@ -15,7 +15,7 @@ from ._lib import default_context, load
 
 FORMATS = {"standard": _abi.OUT_STANDARD, "gnuplot": _abi.OUT_GNUPLOT, "hklf4": _abi.OUT_HKLF4,
            "shelx": _abi.OUT_HKLF4, "list5": _abi.OUT_LIST5, "list9": _abi.OUT_LIST9, "3d": _abi.OUT_NIPL3D,
-           "vtk": _abi.OUT_VTK, "mrc": _abi.OUT_MRC, "xplor": _abi.OUT_XPLOR}
+           "vtk": _abi.OUT_VTK, "mrc": _abi.OUT_MRC, "hdf5": _abi.OUT_HDF5, "xplor": _abi.OUT_XPLOR}
 
 
 def _flat(a):
@@ -69,9 +69,11 @@ def _nipl_c(n, keep):
 
 def output_spec(fmt, grid, value=1, extr=(1, 2, 3), cr=None, ar=(1.0, 1.0, 1.0), wrez=(90.0, 90.0, 90.0),
                 valmax=0.0, f000=0.0, exti=0.0, rlambda=0.70932, name="crystal", lrange=0, lcenter=0, lpixel=0,
-                center=(1, 1, 1), pixel=(1, 1, 1), quad="   ", nipl=None):
+                center=(1, 1, 1), pixel=(1, 1, 1), quad="   ", nipl=None, scale=1.0, a0=None, win=None):
     """The output menu's settings as a dgpu_output struct (plus the objects
-    its pointers refer to)."""
+    its pointers refer to).  a0/win: cr_a0 and cr_win (HDF5 unit_cell); when
+    omitted, the cell of cr's direct metric (the inverse of cr.rten), else
+    1 and 90.  scale: out_scale (HDF5)."""
     o = _abi.Output()
     keep = []
     o.format = FORMATS[fmt] if isinstance(fmt, str) else int(fmt)
@@ -95,6 +97,17 @@ def output_spec(fmt, grid, value=1, extr=(1, 2, 3), cr=None, ar=(1.0, 1.0, 1.0),
     o.lrange, o.lcenter, o.lpixel = int(lrange), int(lcenter), int(lpixel)
     o.quad = quad.encode()[:3].ljust(3)
     o.valmax, o.f000, o.exti, o.rlambda = float(valmax), float(f000), float(exti), float(rlambda)
+    if (a0 is None or win is None) and cr is not None:
+        g = np.linalg.inv(np.asarray(cr.rten, dtype=np.float64))
+        la = np.sqrt(np.diag(g))
+        ang = [np.degrees(np.arccos(g[(k + 1) % 3, (k + 2) % 3] / (la[(k + 1) % 3] * la[(k + 2) % 3])))
+               for k in range(3)]
+        a0 = la if a0 is None else a0
+        win = ang if win is None else win
+    for k in range(3):
+        o.a0[k] = 1.0 if a0 is None else float(a0[k])
+        o.win[k] = 90.0 if win is None else float(win[k])
+    o.scale = float(scale)
     nm = name.encode()
     keep.append(nm)
     o.name = nm

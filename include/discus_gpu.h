@@ -423,8 +423,16 @@ int dgpu_calc_hkl_files(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *
  * values: qval's array for `value` over inc (Fortran order, nvalues =
  * inc1 inc2 inc3; VTK: dsi).  ampl/phase: qval's arrays for values 2 and 3
  * (SHELX formats; HKLF4 needs no phase on 2D/3D grids).  PGM, PPM and
- * postscript are disabled in the reference (error -6), HDF5 and NeXus need
- * libraries this build does not link: DGPU_ERR_UNSUPPORTED.                 */
+ * postscript are disabled in the reference (error -6), NeXus needs a
+ * library this build does not link: DGPU_ERR_UNSUPPORTED.
+ *   HDF5      gen_hdf5_write (lib_f90/hdf_write.f90:12-326), the "Yell 1.0"
+ *             file of the 'hdf5' format (graphic.f90:604-635): data =
+ *             values x scale with dimensions (inc1, inc2, inc3), the third
+ *             fastest, the largest scaled to valmax when valmax > 0;
+ *             format, is_direct (value 14 or 15), lower_limits, step_sizes,
+ *             step_sizes_abs/_ord/_top, unit_cell (a0, win), PROGRAM.
+ *             Written without an HDF5 library, from the file format
+ *             specification.                                               */
 #define DGPU_OUT_STANDARD  0
 #define DGPU_OUT_GNUPLOT   3
 #define DGPU_OUT_HKLF4     6
@@ -433,6 +441,7 @@ int dgpu_calc_hkl_files(dgpu_ctx *ctx, const dgpu_crystal *cr, const dgpu_opts *
 #define DGPU_OUT_NIPL3D    9
 #define DGPU_OUT_VTK      11
 #define DGPU_OUT_MRC      12
+#define DGPU_OUT_HDF5     13
 #define DGPU_OUT_XPLOR    14
 
 typedef struct dgpu_nipl {            /* write_discus_nipl_header (discus_nipl_header.f90:5-172)  */
@@ -465,12 +474,15 @@ typedef struct dgpu_output {
     int32_t center[3], pixel[3];      /* out_center, out_pixel                                  */
     char quad[4];                     /* out_quad ('l', 'r' or blank per axis)                  */
     double valmax;                    /* SHELX scale: NINT -1 by F(000), -2 by the largest
-                                         reflection, > 0 this factor, else 1                    */
+                                         reflection, > 0 this factor, else 1;
+                                         HDF5: > 0 the largest value written                    */
     double f000;                      /* qval(1,1,1,2) of the run at 0 0 0 (valmax -1)          */
     double exti, rlambda;             /* diff_exti, rlambda                                     */
     const char *name;                 /* cr_name (XPLOR title)                                  */
     const dgpu_nipl *nipl;            /* header of STANDARD 2D/3D files; NULL: no header lines  */
     double out_fac;                   /* out: the SHELX scale applied                           */
+    double a0[3], win[3];             /* cr_a0, cr_win (HDF5 unit_cell)                         */
+    double scale;                     /* out_scale (HDF5: values x scale; 0 reads as 1)         */
 } dgpu_output;
 
 int dgpu_output_write(const char *path, dgpu_output *out, const double *values, const double *ampl,

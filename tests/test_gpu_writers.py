@@ -1,7 +1,8 @@
 """The output path end to end on the device: four_run, qval of the values
 the writers need, the file through dgpu_output_write, against the oracle's
 writer fed with the same arrays (the writer's bytes; qval and four_run are
-checked against the oracle in their own tests) -- and calc_hkl with its
+checked against the oracle in their own tests; HDF5 read back with the
+oracle's reader) -- and calc_hkl with its
 files (HKLF4 and CIF in, calcfile and .fcf out), against the oracle's
 calc_hkl values and file restatement."""
 import math
@@ -14,6 +15,7 @@ from diffusecode_gb300 import _abi
 from diffusecode_gb300 import fourier as FR
 from diffusecode_gb300 import output as OUT
 from diffusecode_gb300 import structures as S
+from oracle import hdf5 as H5
 from oracle import writers as W
 
 pytestmark = pytest.mark.gpu
@@ -90,6 +92,21 @@ def test_standard_2d_plane_with_fourier_header(ctx, tmp_path):
     assert got == W.standard(theirs, flat(v))[""]
     assert b"# FOURIER : type        ;1C:: 2D Fourier complete crystal" in got
     assert b"# FOURIER : radiation   ;1C:: neutron" in got
+
+
+@pytest.mark.parametrize("valmax,scale", [(0.0, 1.0), (10000.0, 1.0), (-1.0, 0.25)])
+def test_hdf5_from_device_values(run, tmp_path, valmax, scale):
+    cr, g, op, r, vals = run
+    p = str(tmp_path / "yell.h5")
+    a0, win = (3.9, 3.9, 3.9), (90.0, 90.0, 90.0)
+    OUT.write(p, OUT.output_spec("hdf5", g, cr=cr, valmax=valmax, scale=scale, a0=a0, win=win), vals[1])
+    got = H5.read(open(p, "rb").read())
+    want = H5.yell(g.inc, g.eck, g.vi, (1, 2, 3), a0, win, 1, flat(vals[1]), valmax=valmax, scale=scale)
+    for name, w in want.items():
+        if isinstance(w, np.ndarray):
+            np.testing.assert_array_equal(got[name][0], w, err_msg=name)
+        else:
+            assert got[name][0] == w, name
 
 
 def test_vtk_from_device_dsi(run, tmp_path):
