@@ -35,6 +35,24 @@ def test_tc_random_vs_oracle(oracle, ctx, inc, natoms, vimg):
         assert K.rel_err(r.dsi, dsi, K.incoherent_floor(cr, g, op)) <= TOL
 
 
+@pytest.mark.parametrize("engine", [_abi.ENGINE_TC, _abi.ENGINE_DIRECT], ids=["tc", "direct"])
+@pytest.mark.parametrize("inc", [(1, 1, 1), (1, 1, 9), (1, 7, 1), (2, 2, 2), (4, 1, 3)])
+def test_degenerate_grids_and_absent_types(oracle, ctx, engine, inc):
+    """One point, rods along the second and third axes, 2 x 2 x 2 and a
+    plane across axes 1 and 3; of three types the second is absent and the
+    third holds a single atom (an empty type range beside a one-atom one)."""
+    cr, g = S.small_random(seed=41, natoms=150, nscat=3, inc=inc)
+    cr.iscat[cr.iscat == 2] = 1
+    cr.iscat[cr.iscat == 3] = 0
+    cr.iscat[17] = 3
+    op = K.opts(phase=_abi.PHASE_EXACT64, engine=engine)
+    rc, csf, acsf, dsi, info = oracle.four_run(cr, g, op)
+    r = FR.four_run(cr, g, op, ctx=ctx)
+    assert r.info.engine_used == engine
+    assert K.rel_err(r.dsi, dsi, K.incoherent_floor(cr, g, op)) <= TOL
+    np.testing.assert_allclose(r.csf, csf, rtol=0, atol=3e-3 * np.sqrt(np.abs(dsi).max() + 1.0))
+
+
 @pytest.mark.parametrize("vimg", [1, -1], ids=["v-images", "v-in-kernel"])
 @pytest.mark.parametrize("tile_n,kslice", [(16, 1024), (64, 2048), (112, 0), (128, 96), (80, 4096)])
 def test_tc_tiles_and_slices(oracle, ctx, tile_n, kslice, vimg):
