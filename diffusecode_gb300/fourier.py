@@ -120,6 +120,21 @@ def four_run(cr: CrystalData, grid: GridData, opts: _abi.Opts, ctx=None, aver_ce
     return FourierResult(_cplx(csf, shp), _cplx(acsf, shp), dsi.reshape(shp, order="F"), info, rc)
 
 
+def calc_000(cr: CrystalData, opts: _abi.Opts, rhkl, ctx=None):
+    """calc_000 (fourier_sup.f90:3149-3226): four_run at the single point
+    rhkl (inc 1 1 1, every corner rhkl, vi = 0); res_para(0:4) = 4, Re F,
+    Im F and both per unit cell (divided by cr_icc(1) cr_icc(2) cr_icc(3)).
+    For a single point fourier_lmn keeps only the nearest integers of the
+    corner (identity offsets), so in PHASE_REF22 the phases are those of the
+    rounded hkl while istl (the form factors) follows rhkl itself, as in the
+    reference; PHASE_EXACT64 takes the phases at rhkl."""
+    h = np.asarray(rhkl, dtype=np.float64).reshape(3)
+    grid = GridData(eck=np.repeat(h[:, None], 4, axis=1), vi=np.zeros((3, 3)), inc=(1, 1, 1))
+    f = complex(four_run(cr, grid, opts, ctx=ctx).csf.reshape(-1)[0])
+    ncell = float(cr.icc[0]) * float(cr.icc[1]) * float(cr.icc[2])
+    return [4.0, f.real, f.imag, f.real / ncell, f.imag / ncell]
+
+
 def four_weight(cr: CrystalData, grid: GridData, dsi, opts: _abi.Opts, ctx=None):
     """four_weight (fourier_sup.f90:1428-1643): the dsi3d copy of dsi with
     the Bragg points re-weighted."""

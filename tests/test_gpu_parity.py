@@ -248,6 +248,29 @@ def test_argument_errors(ctx):
     assert getattr(e.value, "code", None) == _abi.DGPU_ERR_NO_ATOMS
 
 
+@pytest.mark.parametrize("phase", [_abi.PHASE_REF22, _abi.PHASE_EXACT64], ids=["ref22", "exact64"])
+@pytest.mark.parametrize("rhkl", [(0.0, 0.0, 0.0), (1.0, -2.0, 3.0), (0.5, 0.25, -1.5)])
+def test_calc_000_single_point(oracle, ctx, phase, rhkl):
+    """calc_000: four_run on one point with zero increments (a single spot
+    for fourier_lmn: identity offsets); res_para against the oracle's
+    four_run on the same grid, and F(000) = sum_t N_t cfact_t(0)."""
+    cr, _ = S.small_random(seed=5, natoms=300, nscat=2)
+    op = K.opts(phase=phase)
+    res = FR.calc_000(cr, op, rhkl, ctx=ctx)
+    g = S.GridData(eck=np.repeat(np.asarray(rhkl)[:, None], 4, axis=1), vi=np.zeros((3, 3)), inc=(1, 1, 1))
+    rc, csf, acsf, dsi, info = oracle.four_run(cr, g, op)
+    assert rc == 0 and res[0] == 4.0
+    f = complex(csf.reshape(-1)[0])
+    scale = np.sqrt(abs(f) ** 2 + float(K.incoherent_floor(cr, g, op).reshape(-1)[0]))
+    assert abs(complex(res[1], res[2]) - f) <= 1e-5 * scale
+    ncell = float(np.prod(cr.icc))
+    assert res[3] == res[1] / ncell and res[4] == res[2] / ncell
+    if rhkl == (0.0, 0.0, 0.0):
+        cfact = oracle.formtab(cr, op)
+        f000 = sum(np.count_nonzero(cr.iscat == t) * cfact[t - 1, 0] for t in range(1, cr.nscat + 1))
+        assert abs(complex(res[1], res[2]) - f000) <= 1e-6 * abs(f000)
+
+
 def test_all_void_crystal_gives_zero(ctx):
     cr, g = S.perovskite_plane(cells=2)
     cr.iscat[:] = 0
