@@ -64,6 +64,52 @@ PartLayout dgpu_part_layout(const PartRef &r, const BoxSpec &box)
 }
 
 
+// (hi, lo) += x in float-float: Knuth's TwoSum, the error carried in lo
+__device__ __forceinline__ void ff_add(float &hi, float &lo, float x)
+{
+    const float s = hi + x, bp = s - hi;
+    lo += (hi - (s - bp)) + (x - bp);
+    hi = s;
+}
+
+// The sum of a group's K-slice partials at one point, in slice order, eight
+// slices loaded before any is added (loads in flight).  FP32 partials are
+// added in float-float (TwoSum, 48-bit significands) rather than FP64, whose
+// rate on this part bounded the combine; FP64 partials in FP64.
+__device__ __forceinline__ double2 slice_sum(const float2 *__restrict__ pt, int32_t nslice, int64_t slab)
+{
+    float hx = 0.f, lx = 0.f, hy = 0.f, ly = 0.f;
+    for (int k0 = 0; k0 < nslice; k0 += 8) {
+        float2 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) v[u] = k0 + u < nslice ? pt[(int64_t)(k0 + u) * slab] : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+            if (k0 + u < nslice) {
+                ff_add(hx, lx, v[u].x);
+                ff_add(hy, ly, v[u].y);
+            }
+    }
+    return make_double2((double)hx + (double)lx, (double)hy + (double)ly);
+}
+
+__device__ __forceinline__ double2 slice_sum(const double2 *__restrict__ pt, int32_t nslice, int64_t slab)
+{
+    double2 s = make_double2(0.0, 0.0);
+    for (int k0 = 0; k0 < nslice; k0 += 8) {
+        double2 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) v[u] = k0 + u < nslice ? pt[(int64_t)(k0 + u) * slab] : make_double2(0.0, 0.0);
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+            if (k0 + u < nslice) {
+                s.x += v[u].x;
+                s.y += v[u].y;
+            }
+    }
+    return s;
+}
+
 template <class P>
 __device__ __forceinline__ void combine_slot(const FormSpec *fs, const BoxSpec &box, const P *__restrict__ part,
                                              int32_t nslice, const PartLayout &lay, const int32_t *__restrict__ istl,
@@ -79,21 +125,8 @@ __device__ __forceinline__ void combine_slot(const FormSpec *fs, const BoxSpec &
     int32_t q = istl ? istl[idx] : 0;
     double2 F = make_double2(0.0, 0.0);
     for (int t = 1; t <= fs->ngroup; t++) {
-        double2 s = make_double2(0.0, 0.0);
         const P *pt = part + (int64_t)(t - 1) * nslice * lay.slab + i * lay.s0 + j * lay.s1 + l * lay.s2;
-        // eight slices loaded before any is added (loads in flight), added in slice order
-        for (int k0 = 0; k0 < nslice; k0 += 8) {
-            double2 v[8];
-#pragma unroll
-            for (int u = 0; u < 8; u++)
-                v[u] = k0 + u < nslice ? ld_part(pt + (int64_t)(k0 + u) * lay.slab) : make_double2(0.0, 0.0);
-#pragma unroll
-            for (int u = 0; u < 8; u++)
-                if (k0 + u < nslice) {
-                    s.x += v[u].x;
-                    s.y += v[u].y;
-                }
-        }
+        const double2 s = slice_sum(pt, nslice, lay.slab);
         double2 c = form_group(fs, cfact, q, t, h);
         double2 m = cmul(s, c);
         F.x += m.x;
@@ -243,6 +276,18 @@ __device__ __forceinline__ void qmerge(QStat &a, const QStat &b)
     a.nd += b.nd;
 }
 
+// Whether h = e + v0 i + v1 j + v2 l can be an integer: the FP32 estimate
+// errs by at most 7 roundings of 2^-24 times mag = |e| + |v0| i + |v1| j +
+// |v2| l (four inputs, three FMAs), well inside 1e-6 mag + 1e-5, so an
+// estimate farther than that from every integer rules the point out and the
+// FP64 test in the reference's order is needed only near integers.
+__device__ __forceinline__ bool maybe_integral(float e, float v0, float v1, float v2, float fi, float fj, float fl)
+{
+    const float h = fmaf(v2, fl, fmaf(v1, fj, fmaf(v0, fi, e)));
+    const float mag = fabsf(e) + fabsf(v0) * fi + fabsf(v1) * fj + fabsf(v2) * fl;
+    return fabsf(h - rintf(h)) <= fmaf(1e-6f, mag, 1e-5f);
+}
+
 #define QNT 256
 __global__ void k_qinfo_part(double e0, double e1, double e2, FormSpec const *fs, int32_t n0,
                              int32_t n1, int32_t n2, const double *dsi, QStat *out)
@@ -250,15 +295,35 @@ __global__ void k_qinfo_part(double e0, double e1, double e2, FormSpec const *fs
     QStat s = {-9999.0, (double)1e19f, -9999.0, (double)1e19f, 0.0, 0.0, 0};
     int64_t np = (int64_t)n0 * n1 * n2;
     double e[3] = {e0, e1, e2};
+    float ef[3], vf[9];
+#pragma unroll
+    for (int k = 0; k < 3; k++) ef[k] = (float)e[k];
+#pragma unroll
+    for (int k = 0; k < 9; k++) vf[k] = (float)fs->vi[k];
+    const bool narrow = np <= (int64_t)0xFFFFFFFFll;     // 32-bit index arithmetic
     for (int64_t p = (int64_t)blockIdx.x * QNT + threadIdx.x; p < np; p += (int64_t)gridDim.x * QNT) {
-        int64_t i = p % n0, j = (p / n0) % n1, l = p / ((int64_t)n0 * n1);
-        bool bragg = true;
-        for (int k = 0; k < 3; k++) {
-            double h = __dadd_rn(__dadd_rn(__dadd_rn(e[k], __dmul_rn(fs->vi[k], (double)(float)i)),
-                                           __dmul_rn(fs->vi[3 + k], (double)(float)j)),
-                                 __dmul_rn(fs->vi[6 + k], (double)(float)l));
-            bragg = bragg && (h == trunc(h));
+        int64_t i, j, l;
+        if (narrow) {
+            const uint32_t q = (uint32_t)p, a = q / (uint32_t)n0;
+            i = q - a * (uint32_t)n0;
+            j = a % (uint32_t)n1;
+            l = a / (uint32_t)n1;
+        } else {
+            i = p % n0;
+            j = (p / n0) % n1;
+            l = p / ((int64_t)n0 * n1);
         }
+        const float fi = (float)i, fj = (float)j, fl = (float)l;
+        bool bragg = true;
+#pragma unroll
+        for (int k = 0; k < 3; k++) bragg = bragg && maybe_integral(ef[k], vf[k], vf[3 + k], vf[6 + k], fi, fj, fl);
+        if (bragg)
+            for (int k = 0; k < 3; k++) {
+                double h = __dadd_rn(__dadd_rn(__dadd_rn(e[k], __dmul_rn(fs->vi[k], (double)fi)),
+                                               __dmul_rn(fs->vi[3 + k], (double)fj)),
+                                     __dmul_rn(fs->vi[6 + k], (double)fl));
+                bragg = bragg && (h == trunc(h));
+            }
         double v = dsi[p];
         if (bragg) {
             s.bmax = fmax(s.bmax, v);
@@ -505,14 +570,6 @@ __global__ void k_lot_combine(int32_t ngroup, int32_t nlot, BoxSpec box, const P
         }
     }
     dsi[idx] += acc;
-}
-
-// (hi, lo) += x in float-float: Knuth's TwoSum, the error carried in lo
-__device__ __forceinline__ void ff_add(float &hi, float &lo, float x)
-{
-    const float s = hi + x, bp = s - hi;
-    lo += (hi - (s - bp)) + (x - bp);
-    hi = s;
 }
 
 // k_lot_combine for FP32 partials with nq = ngroup * nslice partials per lot
