@@ -332,8 +332,9 @@ struct PartRef;
 // out[axis * stride + atom]; enqueue only.
 // The step factors' FP64 table, once per context (at creation).
 int dgpu_tc_init(dgpu_ctx *ctx);
+// mask: the axes (bit a for axis a) whose factors are written
 int dgpu_tc_mult_async(dgpu_ctx *ctx, const uint64_t *du, const uint64_t *dv, const uint64_t *dw, int64_t n,
-                       int64_t stride, float2 *out);
+                       int64_t stride, float2 *out, int mask = 7);
 // Layout of a problem's partials for the combine kernels.
 void dgpu_tc_partref(const TcProblem &g, const float2 *p, PartRef &ref);
 // Single problem with autotuned tile; partial sums are float2 (FP32, one per

@@ -920,15 +920,17 @@ __device__ __forceinline__ uint64_t mix64(uint64_t z)
 // of the chain; atoms at equivalent positions have identical increments, and
 // with round-to-nearest their chains would share one error and add it up
 // coherently.  Stochastic rounding gives each atom its own, zero-mean error.
+// mask: bit a set for each axis a whose factors are written.
 __global__ void k_tc_mult(const uint64_t *__restrict__ du, const uint64_t *__restrict__ dv,
                           const uint64_t *__restrict__ dw, int64_t n, int64_t stride,
-                          const double2 *__restrict__ tab, float2 *__restrict__ out)
+                          const double2 *__restrict__ tab, float2 *__restrict__ out, int mask)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint64_t *d[3] = {du, dv, dw};
 #pragma unroll
     for (int a = 0; a < 3; a++) {
+        if (!((mask >> a) & 1)) continue;
         const double2 m = phasor_f64(d[a][i] << 3, tab);
         const double2 m2 = make_double2(m.x * m.x - m.y * m.y, 2.0 * m.x * m.y);
         const uint64_t r = mix64((uint64_t)i * 4u + (uint64_t)a + 0x9E3779B97F4A7C15ull);
@@ -942,20 +944,23 @@ __global__ void k_tc_mult(const uint64_t *__restrict__ du, const uint64_t *__res
 // V operand images: for every (64-atom group gi, column tile nt) the B rows
 // [Vr; Vi; -Vr] (hi operand, then lo) of the tile's N columns, in the
 // 128-byte-swizzled K-major layout the MMAs read (768 N bytes).  Each value is
-// evaluated from its exact 64-bit phase; grid: one block per (gi, nt).  The
-// image is built in shared memory and written out in 16-byte coalesced stores.
+// evaluated from its exact 64-bit phase; grid: one block per (gi, nt).  A
+// half-warp takes the 16 atom quads of one column, i.e. one 128-byte row of
+// each of the six row blocks, so every 8-byte store instruction of a warp
+// fills two whole rows and goes straight to global memory (no staging in
+// shared memory, no block barrier: the warps' evaluation and stores overlap).
 template <bool BF>
 __global__ void __launch_bounds__(256) k_tc_vgen(const uint64_t *__restrict__ dac, int N, int n_tiles,
                                                   uint8_t *__restrict__ vimg)
 {
-    extern __shared__ __align__(1024) uint8_t vs[];
+    constexpr int NQ = TC_KB / 4;      // atom quads per row
     const int64_t gi = blockIdx.x / n_tiles;
     const int nt = (int)(blockIdx.x % n_tiles);
     const uint32_t vbytes = (uint32_t)N * 768u;
-    uint8_t *img = vs;                 // built in shared memory, then written out coalesced
+    uint8_t *img = vimg + (int64_t)blockIdx.x * vbytes;
     const uint32_t half = vbytes / 2, blk = (uint32_t)(N >> 3) * TC_SBO128;
-    for (int u = threadIdx.x; u < N * (TC_KB / 4); u += blockDim.x) {
-        const int c = u % N, jq = u / N;                       // column, atom quad
+    for (int u = threadIdx.x; u < N * NQ; u += blockDim.x) {
+        const int c = u / NQ, jq = u % NQ;                     // column, atom quad
         const uint32_t nc = (uint32_t)(nt * N + c);
         float2 x[4];
 #pragma unroll
@@ -975,10 +980,6 @@ __global__ void __launch_bounds__(256) k_tc_vgen(const uint64_t *__restrict__ da
         *reinterpret_cast<uint2 *>(d + 2 * blk) = make_uint2(rh.x ^ 0x80008000u, rh.y ^ 0x80008000u);
         *reinterpret_cast<uint2 *>(d + 2 * blk + half) = make_uint2(rl.x ^ 0x80008000u, rl.y ^ 0x80008000u);
     }
-    __syncthreads();
-    uint4 *out = reinterpret_cast<uint4 *>(vimg + (int64_t)blockIdx.x * vbytes);
-    const uint4 *src = reinterpret_cast<const uint4 *>(vs);
-    for (uint32_t i = threadIdx.x; i < vbytes / 16u; i += blockDim.x) out[i] = src[i];
 }
 
 // ---------------------------------------------------------------------------
@@ -1236,10 +1237,6 @@ int dgpu_tc_plan(dgpu_ctx *ctx, int nprob, const TcInput *in, const dgpu_opts *o
     if (!ctx->tc_attr) {              // once per context (and device), outside any stream capture
         DGPU_CUDA(ctx, cudaFuncSetAttribute(k_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
         DGPU_CUDA(ctx, cudaFuncSetAttribute(k_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-        DGPU_CUDA(ctx, cudaFuncSetAttribute(k_tc_vgen<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            227 * 1024));
-        DGPU_CUDA(ctx, cudaFuncSetAttribute(k_tc_vgen<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            227 * 1024));
         ctx->tc_attr = true;
     }
     DGPU_CUDA(ctx, ctx->flag.ensure(64));
@@ -1257,11 +1254,9 @@ int dgpu_tc_launch(dgpu_ctx *ctx, const TcPlan &plan, bool timed)
             const int64_t nimg = (g.ts[g.ntype] / TC_KB) * g.vstride;
             if (nimg < 1) continue;
             if (plan.L.bf16)
-                k_tc_vgen<true><<<(unsigned)nimg, 256, (size_t)g.N * 768, ctx->stream>>>(g.dac, g.N, g.vstride,
-                                                                                          g.vimg);
+                k_tc_vgen<true><<<(unsigned)nimg, 256, 0, ctx->stream>>>(g.dac, g.N, g.vstride, g.vimg);
             else
-                k_tc_vgen<false><<<(unsigned)nimg, 256, (size_t)g.N * 768, ctx->stream>>>(g.dac, g.N, g.vstride,
-                                                                                           g.vimg);
+                k_tc_vgen<false><<<(unsigned)nimg, 256, 0, ctx->stream>>>(g.dac, g.N, g.vstride, g.vimg);
             if (plan.vshared) break;                        // one set for all problems
         }
     const int grid = (int)(plan.L.nitems < ctx->nsm ? plan.L.nitems : ctx->nsm);
@@ -1286,11 +1281,11 @@ int dgpu_tc_check(dgpu_ctx *ctx)
 }
 
 int dgpu_tc_mult_async(dgpu_ctx *ctx, const uint64_t *du, const uint64_t *dv, const uint64_t *dw, int64_t n,
-                       int64_t stride, float2 *out)
+                       int64_t stride, float2 *out, int mask)
 {
-    if (n < 1) return DGPU_OK;
+    if (n < 1 || !(mask & 7)) return DGPU_OK;
     k_tc_mult<<<(unsigned)dgpu_cdiv(n, 256), 256, 0, ctx->stream>>>(du, dv, dw, n, stride,
-                                                                      ctx->tc_tab.as<double2>(), out);
+                                                                      ctx->tc_tab.as<double2>(), out, mask & 7);
     DGPU_CUDA(ctx, cudaGetLastError());
     return DGPU_OK;
 }
@@ -1340,8 +1335,7 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
     }
     const int64_t npad = h_type_start[ntype];
     DGPU_CUDA(ctx, ctx->tc_mult.ensure((size_t)TC_MULT_ARRAYS * (npad > 0 ? npad : 1) * sizeof(float2)));
-    int rc = dgpu_tc_mult_async(ctx, du, dv, dw, npad, npad, ctx->tc_mult.as<float2>());
-    if (rc) return rc;
+    int rc;
     int lg = 0;
     while ((1LL << lg) < maxn) lg++;
     const TcKey key(box.f[0], box.f[1], box.f[2], ntype, lg, op->split * 1000 + want_n,
@@ -1359,9 +1353,13 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
     in.box = box;
     TcChoice choice;
     auto hit = ctx->tc_tuned.find(key);
-    if (hit != ctx->tc_tuned.end()) {
+    const bool cached = hit != ctx->tc_tuned.end();
+    if (cached) {
         choice = hit->second;
     } else {
+        // the candidates use every axis as row or column axis: all step factors
+        rc = dgpu_tc_mult_async(ctx, du, dv, dw, npad, npad, ctx->tc_mult.as<float2>(), 7);
+        if (rc) return rc;
         TcChoice cand[64];
         int nc = 0;
         tc_candidates(box, want_n, op->tc_kslice, cand, nc);
@@ -1393,6 +1391,14 @@ int dgpu_tc_sums(dgpu_ctx *ctx, const uint64_t *ph0, const uint64_t *du, const u
     TcPlan plan;
     rc = dgpu_tc_plan(ctx, 1, &in, op, choice.N, choice.slice_mult, plan, part, ctx->tc_part, &ctx->tc_vimg);
     if (rc) return rc;
+    if (cached) {
+        // the factors this plan reads: the row axis ra (the producers' steps),
+        // on the in-kernel V path also the column axis
+        const TcProblem &g = plan.probs[0];
+        rc = dgpu_tc_mult_async(ctx, du, dv, dw, npad, npad, ctx->tc_mult.as<float2>(),
+                                (1 << g.ra) | (plan.vimg ? 0 : 1 << g.ac));
+        if (rc) return rc;
+    }
     rc = dgpu_tc_launch(ctx, plan, !ctx->tc_defer);
     if (rc) return rc;
     if (!ctx->tc_defer) {
