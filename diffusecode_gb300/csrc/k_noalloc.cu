@@ -49,8 +49,8 @@ struct Cached {
 };
 Cached g_addr[256];
 
-// the driver's cuCtxGetCurrent, through the runtime (the library does not
-// link the driver library itself)
+// cuCtxGetCurrent of the CUDA driver API, looked up through the runtime
+// (the library does not link libcuda itself)
 typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
 CtxGetCurrentFn ctx_get_current()
 {
