@@ -679,14 +679,14 @@ def powder_measure(ctx, cr, flush, steps=2, cpu=True):
         nth = os.cpu_count() or 1
         mid = int(info.rods) // 2
         t0 = time.perf_counter()
-        _, _, _, n0 = O.powder_complete(cr, pw, op_ref, mid, mid + nth, nthreads=nth)
+        _, _, _, n0 = O.powder_complete(cr, pw, op_ref, mid, mid + nth, nthreads=nth, timing=True)
         t_cal = time.perf_counter() - t0
         nrod = max(nth, min(int(info.rods) - mid, int(nth * 8.0 / max(t_cal, 1e-3))))
         t0 = time.perf_counter()
-        _, _, _, npts = O.powder_complete(cr, pw, op_ref, mid, mid + nrod, nthreads=nth)
+        _, _, _, npts = O.powder_complete(cr, pw, op_ref, mid, mid + nrod, nthreads=nth, timing=True)
         sec = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": natoms * npts / sec / 1e9, "unit": "G pairs/s", "cores": nth,
-                               "kind": "port", "sample": f"oracle rod loop (REF22), rods {mid}..{mid + nrod} "
+                               "kind": "port", "sample": f"oracle rod loop (REF22, built -O3 -ffast-math), rods {mid}..{mid + nrod} "
                                                          f"({npts} points), {sec:.1f} s"}
     return out
 
@@ -765,7 +765,8 @@ def run_reference(args, world, rank):
         "config": {"workload": args.workload, "atoms": cr.n_scattering(), "grid": list(grid.inc),
                    "pairs_per_step": pairs_full, "l2": "n/a (CPU)"},
         "cpu_baseline": {"value": value, "unit": "G pairs/s", "cores": nthreads, "kind": "port",
-                         "sample": f"REF22 four_strucf_omp restatement, {rows_used} abscissa rows of the "
+                         "sample": f"REF22 four_strucf_omp restatement (built -O3 -ffast-math, the reference's "
+                                   f"release flags), {rows_used} abscissa rows of the "
                                    f"Friedel half per step (one per thread), all atom types"
                                    + (f" (the first {frac:.0%} of the atoms per step)" if frac < 1.0 else "")
                                    + ", credited per full-grid pair"},
@@ -937,7 +938,8 @@ def run_ours(args, world, rank, local):
             line["parity_vs_ref22"] = parity_ref22(ctx)
         v, nth, rows, sec = cpu_baseline(cr, grid)
         line["cpu_baseline"] = {"value": v, "unit": "G pairs/s", "cores": nth, "kind": "port",
-                                "sample": f"REF22 four_strucf_omp restatement (oracle), {rows} abscissa rows "
+                                "sample": f"REF22 four_strucf_omp restatement (oracle built -O3 -ffast-math, the "
+                                          f"reference's release flags), {rows} abscissa rows "
                                           f"of the Friedel half (one per thread), {sec:.1f} s, credited per "
                                           f"full-grid pair"}
     print(json.dumps(line))

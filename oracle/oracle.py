@@ -14,7 +14,11 @@ from diffusecode_gb300 import _abi
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = os.path.join(_HERE, "_build", "liboracle.so")
+# the same source built with the reference's release flags (-O3 -ffast-math,
+# OpenMP): only for timing the reference's loops (bench CPU legs)
+_TLIB = os.path.join(_HERE, "_build", "liboracle_timing.so")
 _lib = None
+_tlib = None
 
 
 def build():
@@ -24,39 +28,52 @@ def build():
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(_LIB):
-            build()
-        L = C.CDLL(_LIB)
-        dp, ip, fp = C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_float)
-        L.oc_fourier_lmn.argtypes = [dp, dp, ip, ip, dp]
-        L.oc_cexpt.argtypes = [dp]
-        L.oc_stltab.argtypes = [dp, dp, ip, dp, ip]
-        L.oc_formtab.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Opts), dp]
-        L.oc_increments.argtypes = [dp, C.c_int64, dp, dp, dp, dp, C.POINTER(C.c_int64)]
-        L.oc_four_strucf.argtypes = [dp, C.c_int64, dp, dp, dp, dp, ip, ip, ip, dp, ip, dp]
-        L.oc_four_run.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Grid), C.POINTER(_abi.Opts),
-                                  dp, dp, dp, C.POINTER(_abi.Info), C.c_int]
-        L.oc_chi2_grad.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Grid), C.POINTER(_abi.Opts),
-                                   dp, dp, dp, dp, dp, C.c_int]
-        L.oc_time_ref_rows.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Grid), C.c_int32,
-                                       C.c_int32, C.c_int, C.POINTER(C.c_int64)]
-        L.oc_time_ref_rows.restype = C.c_double
-        L.oc_four_weight.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Grid), C.POINTER(_abi.Opts),
-                                     dp, dp, dp]
-        L.oc_fill_bragg.argtypes = [C.POINTER(_abi.Grid), dp, C.c_int]
-        L.oc_fill_bragg.restype = None
-        L.oc_four_symm.argtypes = [C.POINTER(_abi.Grid), C.c_int32, dp, dp, C.c_int]
-        L.oc_four_symm.restype = None
-        L.oc_calc_hkl.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Opts), C.POINTER(C.c_int32), C.c_int64,
-                                  C.c_double, C.c_double, C.c_double, dp, dp, dp, C.c_int]
-        L.oc_qval.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Grid), C.POINTER(_abi.Opts), C.c_int,
-                              C.c_int, dp, dp, dp, dp, dp]
-        L.oc_powder_npkt.argtypes = [C.POINTER(_abi.Powder)]
-        L.oc_powder_complete.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Powder), C.POINTER(_abi.Opts),
-                                         C.c_int64, C.c_int64, dp, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
-                                         C.c_int]
-        _lib = L
+        _lib = _load(_LIB)
     return _lib
+
+
+def timing_lib():
+    """The oracle built with the reference's release flags; its results are
+    not checked, only its time is used."""
+    global _tlib
+    if _tlib is None:
+        _tlib = _load(_TLIB)
+    return _tlib
+
+
+def _load(path):
+    if not os.path.exists(path):
+        build()
+    L = C.CDLL(path)
+    dp, ip, fp = C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_float)
+    L.oc_fourier_lmn.argtypes = [dp, dp, ip, ip, dp]
+    L.oc_cexpt.argtypes = [dp]
+    L.oc_stltab.argtypes = [dp, dp, ip, dp, ip]
+    L.oc_formtab.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Opts), dp]
+    L.oc_increments.argtypes = [dp, C.c_int64, dp, dp, dp, dp, C.POINTER(C.c_int64)]
+    L.oc_four_strucf.argtypes = [dp, C.c_int64, dp, dp, dp, dp, ip, ip, ip, dp, ip, dp]
+    L.oc_four_run.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Grid), C.POINTER(_abi.Opts),
+                              dp, dp, dp, C.POINTER(_abi.Info), C.c_int]
+    L.oc_chi2_grad.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Grid), C.POINTER(_abi.Opts),
+                               dp, dp, dp, dp, dp, C.c_int]
+    L.oc_time_ref_rows.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Grid), C.c_int32,
+                                   C.c_int32, C.c_int, C.POINTER(C.c_int64)]
+    L.oc_time_ref_rows.restype = C.c_double
+    L.oc_four_weight.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Grid), C.POINTER(_abi.Opts),
+                                 dp, dp, dp]
+    L.oc_fill_bragg.argtypes = [C.POINTER(_abi.Grid), dp, C.c_int]
+    L.oc_fill_bragg.restype = None
+    L.oc_four_symm.argtypes = [C.POINTER(_abi.Grid), C.c_int32, dp, dp, C.c_int]
+    L.oc_four_symm.restype = None
+    L.oc_calc_hkl.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Opts), C.POINTER(C.c_int32), C.c_int64,
+                              C.c_double, C.c_double, C.c_double, dp, dp, dp, C.c_int]
+    L.oc_qval.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Grid), C.POINTER(_abi.Opts), C.c_int,
+                          C.c_int, dp, dp, dp, dp, dp]
+    L.oc_powder_npkt.argtypes = [C.POINTER(_abi.Powder)]
+    L.oc_powder_complete.argtypes = [C.POINTER(_abi.Crystal), C.POINTER(_abi.Powder), C.POINTER(_abi.Opts),
+                                     C.c_int64, C.c_int64, dp, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                     C.c_int]
+    return L
 
 
 def _d(a):
@@ -192,7 +209,8 @@ def chi2_grad(cr, grid, opts, i_target, weight=None, nthreads=0, aver_cells=None
 
 def time_ref_rows(cr, grid, row_lo, row_hi, nthreads=0, natoms=None):
     """Seconds and pairs for the REF22 type sums over abscissa rows [lo,hi)
-    (over the first natoms atoms when given)."""
+    (over the first natoms atoms when given), in the build with the
+    reference's release flags."""
     if nthreads <= 0:
         nthreads = os.cpu_count() or 1
     c = cr.to_c()
@@ -200,7 +218,7 @@ def time_ref_rows(cr, grid, row_lo, row_hi, nthreads=0, natoms=None):
         c.natoms = min(int(natoms), int(c.natoms))
     g = grid.to_c()
     pairs = C.c_int64(0)
-    sec = lib().oc_time_ref_rows(C.byref(c), C.byref(g), int(row_lo), int(row_hi), int(nthreads),
+    sec = timing_lib().oc_time_ref_rows(C.byref(c), C.byref(g), int(row_lo), int(row_hi), int(nthreads),
                                  C.byref(pairs))
     return sec, int(pairs.value)
 
@@ -278,21 +296,23 @@ def calc_hkl(cr, opts, hkl, scale=1.0, exti=0.0, rlambda=0.70932, nthreads=0):
     return rc, ic, sg, ph
 
 
-def powder_complete(cr, pw, opts, rod_lo=-1, rod_hi=-1, nthreads=0):
+def powder_complete(cr, pw, opts, rod_lo=-1, rod_hi=-1, nthreads=0, timing=False):
     """powder_complete (powder.f90:1829-2593), literal rod loop: (rc, pow_qsp,
     rods, rod points evaluated).  rod_lo/rod_hi restrict the evaluation to
     the rods [rod_lo, rod_hi) of the reference's loop order (a bounded CPU
-    sample); the half-volume doubling is applied either way."""
+    sample); the half-volume doubling is applied either way.  timing: run
+    the build with the reference's release flags (for timing only)."""
     if nthreads <= 0:
         nthreads = os.cpu_count() or 1
+    L = timing_lib() if timing else lib()
     p = pw.to_c()
-    n = lib().oc_powder_npkt(C.byref(p))
+    n = L.oc_powder_npkt(C.byref(p))
     if n < 0:
         return -1, None, 0, 0
     qsp = np.zeros(n + 1)
     c = cr.to_c()
     nr, npts = C.c_int64(0), C.c_int64(0)
-    rc = lib().oc_powder_complete(C.byref(c), C.byref(p), C.byref(opts), int(rod_lo), int(rod_hi), _d(qsp),
+    rc = L.oc_powder_complete(C.byref(c), C.byref(p), C.byref(opts), int(rod_lo), int(rod_hi), _d(qsp),
                                   C.byref(nr), C.byref(npts), nthreads)
     return rc, qsp, nr.value, npts.value
 
