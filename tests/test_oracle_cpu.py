@@ -190,3 +190,27 @@ def test_oracle_gradient_matches_finite_differences(oracle):
             p[a, k] -= 2 * h
             cm, _, _ = oracle.chi2_grad(cr.with_positions(p), g, op, it, wt)
             assert abs((cp - cm) / (2 * h) - gp[a, k]) <= 1e-6 * np.abs(gp).max()
+
+
+def test_timing_build_computes_the_same_sums(oracle):
+    """The release-flag build (-O3 -ffast-math) timed as the CPU baseline runs
+    the same REF22 loop: its four_run agrees with the exact build to FP64
+    reassociation, and its timed row sample counts the same pairs."""
+    import ctypes as C
+    cr, g = S.small_random(seed=9, natoms=400, nscat=2, inc=(11, 9, 5))
+    op = K.opts(phase=_abi.PHASE_REF22)
+    out = []
+    for L in (oracle.lib(), oracle.timing_lib()):
+        np_ = g.npoints
+        csf, acsf, dsi = np.zeros(2 * np_), np.zeros(2 * np_), np.zeros(np_)
+        info = _abi.Info()
+        c, gg = cr.to_c(), g.to_c()
+        rc = L.oc_four_run(C.byref(c), C.byref(gg), C.byref(op), oracle._d(csf), oracle._d(acsf), oracle._d(dsi),
+                           C.byref(info), 2)
+        assert rc == 0
+        pairs = C.c_int64(0)
+        L.oc_time_ref_rows(C.byref(c), C.byref(gg), 0, 3, 2, C.byref(pairs))
+        out.append((dsi, pairs.value))
+    (d0, p0), (d1, p1) = out
+    assert p0 == p1 > 0
+    np.testing.assert_allclose(d1, d0, rtol=1e-9, atol=1e-9 * d0.max())
